@@ -1,0 +1,220 @@
+/*
+ * tdep_gb300.h -- C-ABI of the GB300 (sm_103a) three/four-phonon scattering path.
+ *
+ * The entry points replace the Fortran call sequence of TDEP's thermal_conductivity
+ * program around its scattering hot path:
+ *
+ *   src/thermal_conductivity/main.f90:191      call sr%generate(qp, dr, uc, fct, fcf, opts, ...)
+ *   src/thermal_conductivity/scattering.f90:58 subroutine generate            -> tdg_scattering
+ *   src/thermal_conductivity/main.f90:219,231  get_kappa / iterative_solution -> tdg_kappa
+ *   src/thermal_conductivity/kappa.f90:326     subroutine iterative_solution  -> tdg_kappa
+ *
+ * Conventions (all arrays are caller-owned host memory; the library copies what it needs
+ * and never frees or retains caller pointers):
+ *   - indices that TDEP stores 1-based (q-points, operations, modes in degeneracy tables,
+ *     atoms) are passed 1-based exactly as stored in the Fortran types;
+ *   - 3x3 matrices are column-major (Fortran order);
+ *   - complex numbers are interleaved (re, im) doubles;
+ *   - units are TDEP's internal atomic units (Hartree, Bohr, electron masses).
+ *
+ * Every entry returns an int status. The codes reuse src/libolle/konstanter.f90:160-172:
+ *   0 ok, 1 bad dimension, 2 linear algebra, 3 unphysical value, 4 symmetry,
+ *   5 bad parameter, 6 IO; plus TDG_ERR_DEVICE (8) for a CUDA error or a device-side
+ *   check that failed. The message of the last error is returned by tdg_last_error().
+ *
+ * One context per host thread; calls are synchronous; a context is not re-entrant.
+ */
+#ifndef TDEP_GB300_H
+#define TDEP_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TDG_OK 0
+#define TDG_ERR_BADDIM 1
+#define TDG_ERR_LINALG 2
+#define TDG_ERR_PHYSICAL 3
+#define TDG_ERR_SYMMETRY 4
+#define TDG_ERR_PARAM 5
+#define TDG_ERR_IO 6
+#define TDG_ERR_DEVICE 8
+
+#define TDG_PREC_FP64 0  /* FP64 everywhere                                          */
+#define TDG_PREC_MIXED 1 /* FP32 pretransform/contraction, FP64 weights and sums     */
+
+/*
+ * The flattened inputs of lo_scattering_rates%generate (scattering.f90:58): the crystal
+ * (uc), the FFT q-mesh (qp), the harmonic phonons on the full mesh (dr%aq, dr%iq) and the
+ * third/fourth-order force constants (fct, fcf). A Fortran caller fills it from its
+ * derived types; the C++ host stage (tdg_problem_load) fills it from infile.* files.
+ */
+typedef struct tdg_problem {
+    /* crystal: type_crystalstructure */
+    int32_t n_atom;            /* uc%na                                                  */
+    int32_t n_mode;            /* 3*uc%na                                                */
+    double latvec[9];          /* uc%latticevectors, column j = a_j, Bohr                 */
+    double reclat[9];          /* uc%reciprocal_latticevectors, a_i.b_j = delta_ij, 1/Bohr */
+    double inv_reclat[9];      /* uc%inv_reciprocal_latticevectors                         */
+    double volume;             /* uc%volume, Bohr^3                                        */
+    const double *mass_disorder; /* [n_atom] uc%isotope(:)%disorderparameter               */
+    /* symmetry: uc%sym%op(1:n_op) */
+    int32_t n_op;
+    const double *op_cart;     /* [n_op*9] op%m, Cartesian rotation, column-major          */
+    const int32_t *op_recfrac; /* [n_op*9] op%rfm, integer rotation of fractional
+                                  reciprocal coordinates, column-major                     */
+    /* FFT mesh: type_qpointmesh (lo_fft_mesh) */
+    int32_t grid[3];           /* qp%griddensity                                            */
+    int32_t n_full;            /* qp%n_full_point = grid[0]*grid[1]*grid[2]                 */
+    int32_t n_irr;             /* qp%n_irr_point                                            */
+    const double *q_full;      /* [n_full*3] qp%ap(:)%r, Cartesian, 1/Bohr without 2*pi     */
+    const int32_t *full_irr;   /* [n_full] qp%ap(:)%irreducible_index (1-based)             */
+    const int32_t *full_op;    /* [n_full] qp%ap(:)%operation_from_irreducible (signed)     */
+    const int32_t *irr_full;   /* [n_irr] qp%ip(:)%full_index (1-based)                     */
+    const double *irr_weight;  /* [n_irr] qp%ip(:)%integration_weight                       */
+    const int32_t *irr_nop;    /* [n_irr] qp%ip(:)%n_invariant_operation                    */
+    const int32_t *irr_ops;    /* [n_irr*n_op] qp%ip(:)%invariant_operation, 0-padded       */
+    /* harmonic phonons on the full mesh: dr%aq(:) (dr%iq(i) == dr%aq(irr_full(i)))        */
+    const double *omega;       /* [n_full*n_mode] omega, Hartree, mode fastest              */
+    const double *egv;         /* [n_full*n_mode*n_mode*2] egv(:,b), element r of mode b at
+                                  ((q*n_mode + b)*n_mode + r)*2 (+1 for imaginary part)     */
+    const double *vel;         /* [n_full*n_mode*3] vel(:,b) at (q*n_mode + b)*3 + xyz      */
+    const int32_t *degen;      /* [n_full*n_mode] degeneracy(b)                              */
+    const int32_t *degen_mode; /* [n_full*n_mode*n_mode] degenmode(j,b) at
+                                  (q*n_mode + b)*n_mode + j, 1-based                         */
+    /* third order: type_forceconstant_thirdorder, triplets of all atoms concatenated      */
+    int32_t n_fc3;
+    const int32_t *fc3_atoms;  /* [n_fc3*3] i1,i2,i3 (1-based)                               */
+    const int32_t *fc3_lv;     /* [n_fc3*6] lv2, lv3 in integer fractional coordinates       */
+    const double *fc3_lvcart;  /* [n_fc3*6] lv2, lv3 Cartesian, Bohr                         */
+    const double *fc3_mwm;     /* [n_fc3*27] mwm(i,j,k) at i + 3j + 9k (0-based, Fortran)    */
+    /* fourth order: type_forceconstant_fourthorder                                         */
+    int32_t n_fc4;
+    const int32_t *fc4_atoms;  /* [n_fc4*4] i1..i4 (1-based)                                 */
+    const int32_t *fc4_lv;     /* [n_fc4*9] lv2, lv3, lv4, integer fractional                */
+    const double *fc4_lvcart;  /* [n_fc4*9] lv2, lv3, lv4 Cartesian, Bohr                    */
+    const double *fc4_mwm;     /* [n_fc4*81] mwm(i,j,k,l) at i + 3j + 9k + 27l               */
+} tdg_problem;
+
+/* The hot-path subset of lo_opts (src/thermal_conductivity/options.f90). */
+typedef struct tdg_opts {
+    double temperature;        /* --temperature, K                                          */
+    int32_t integrationtype;   /* -it 1 (fixed Gaussian), 2 (adaptive), 6 (velocity diff)   */
+    double sigma;              /* --sigma, THz, used with -it 1                              */
+    int32_t thirdorder;        /* not --nothirdorder                                          */
+    int32_t fourthorder;       /* --fourthorder                                               */
+    int32_t isotope;           /* not --noisotope                                             */
+    int32_t classical;         /* --classical                                                 */
+    double mfp_max;            /* --max_mfp converted to Bohr; <= 0 disables boundary term    */
+    int32_t qg3ph[3];          /* -qg3ph after defaulting (options.f90:205-235)               */
+    int32_t qg4ph[3];          /* -qg4ph after defaulting                                     */
+    int32_t seed;              /* --seed (> 0)                                                */
+    int32_t precision;         /* TDG_PREC_FP64 or TDG_PREC_MIXED                             */
+} tdg_opts;
+
+/*
+ * Scattering-matrix rows: (q1, b1) over irreducible q1 ascending, modes ascending, skipping
+ * omega < lo_freqtol (scattering.f90:170-209 with one rank). Monte-Carlo q' samples are per
+ * row in CSR form: row r uses list[ptr[r] .. ptr[r+1]) with weight 1/(ptr[r+1]-ptr[r]).
+ * For four-phonon each row has two samples of equal length (list4a, list4b).
+ */
+typedef struct tdg_qlists {
+    int32_t n_row;
+    const int32_t *row_q1;     /* [n_row] irreducible index (1-based)                          */
+    const int32_t *row_b1;     /* [n_row] mode (1-based)                                       */
+    const int64_t *ptr3;       /* [n_row+1] or NULL when third order is off                    */
+    const int32_t *list3;      /* q' (1-based full index)                                      */
+    const int64_t *ptr4;       /* [n_row+1] or NULL when fourth order is off                   */
+    const int32_t *list4a;
+    const int32_t *list4b;
+} tdg_qlists;
+
+typedef struct tdg_ctx tdg_ctx;
+
+/* Last error message of this thread (static storage, never NULL). */
+const char *tdg_last_error(void);
+
+/* Library version string. */
+const char *tdg_version(void);
+
+/* Number of CUDA devices visible (0 without a GPU); never fails. */
+int tdg_device_count(void);
+
+/* Create a context on CUDA device `device` and upload the problem (replaces the
+ * allocations of scattering.f90:85-212). Fails with TDG_ERR_DEVICE without a GPU. */
+int tdg_create(tdg_ctx **out, const tdg_problem *prob, int device);
+
+void tdg_destroy(tdg_ctx *ctx);
+
+/*
+ * Rows and Monte-Carlo q' samples, generated on the host exactly as the reference does:
+ * MT19937-64 seeded by init_genrand64(iseed=0, rseed=1/seed) (lo_randomnumbers.f90:203-236),
+ * one stratified sample per row and order (lo_fftgrid_helper.f90:56-99), consumed row by
+ * row in the order isotope, three-phonon, four-phonon (scattering.f90:227-243).
+ * Writes n_row and the rows into the caller's arrays (capacity n_irr*n_mode) and the
+ * samples into list3 (capacity n_row*prod(qg3ph)) / list4a, list4b (n_row*prod(qg4ph)).
+ * Any list pointer may be NULL when that order is off. CPU only.
+ */
+int tdg_mc_qlists(const tdg_problem *prob, const tdg_opts *opts, int32_t *n_row,
+                  int32_t *row_q1, int32_t *row_b1, int64_t *ptr3, int32_t *list3,
+                  int64_t *ptr4, int32_t *list4a, int32_t *list4b);
+
+/*
+ * The scattering rates (scattering.f90:58-358): isotope, three-phonon, four-phonon and
+ * boundary linewidths for every row, degeneracy averaging, and the symmetrised
+ * scattering matrix Xi, which stays in device memory for tdg_kappa.
+ * Outputs (n_irr*n_mode, mode fastest, zero for skipped modes):
+ *   linewidth  dr%iq(:)%linewidth (Hartree)
+ *   qs         dr%iq(:)%qs = 2*linewidth
+ * stats (may be NULL): [0] accepted irreducible q-triplets, [1] q-quartets,
+ *   [2] scattering time on the device in ms, [3] candidate q-pairs.
+ */
+int tdg_scattering(tdg_ctx *ctx, const tdg_opts *opts, const tdg_qlists *lists,
+                   double *linewidth, double *qs, double *stats);
+
+/* Copy the device-resident scattering matrix (n_row x n_full*n_mode, row-major, FP64). */
+int tdg_get_xi(tdg_ctx *ctx, double *xi);
+
+/*
+ * Irreducible q-triplets of one sample, enumerated on the device (kernel K1). Replaces the
+ * per-candidate q3 index and triplet_is_irreducible of scattering_threephonon.f90:72-77,
+ * 319-448. q1 is the irreducible index (1-based) and sample holds full-mesh indices
+ * (1-based). For every accepted q2, in sample order, writes q2, q3, k and the k
+ * equivalent pairs (q2', q3') in operation order (all 1-based) into out. *written
+ * receives the number of ints; TDG_ERR_PARAM when cap is too small.
+ */
+int tdg_triplets(tdg_ctx *ctx, int32_t q1, const int32_t *sample, int64_t n, int32_t *out, int64_t cap,
+                 int64_t *written);
+
+/*
+ * Thermal conductivity from the current scattering state (main.f90:216-244):
+ * kappa_sma (get_kappa, kappa.f90:28-75), the iterative BTE (kappa.f90:326-495) with
+ * maxiter steps and tolerance tol, kappa_iter, both symmetrised (kappa.f90:308-324).
+ * All tensors 3x3 column-major in atomic units (multiply by lo_kappa_au_to_SI for W/m/K).
+ * fn_out (may be NULL): final Fn, [n_irr*n_mode*3]. n_iter receives the iteration count.
+ */
+int tdg_kappa(tdg_ctx *ctx, const tdg_opts *opts, int32_t maxiter, double tol,
+              double *kappa_sma, double *kappa_iter, double *fn_out, int32_t *n_iter);
+
+/*
+ * Host stage of thermal_conductivity (main.f90:42-181) for the C++ driver and tests:
+ * reads infile.ucposcar, infile.forceconstant, infile.forceconstant_thirdorder and, when
+ * fourthorder != 0, infile.forceconstant_fourthorder from `dir` (masses from infile.isotopes
+ * when readiso != 0), finds the symmetry operations, builds the FFT mesh `grid` and the
+ * harmonic phonons. The returned problem owns its arrays; free with tdg_problem_free.
+ */
+int tdg_problem_load(const char *dir, const int32_t grid[3], int fourthorder, int readiso,
+                     int timereversal, tdg_problem **out);
+void tdg_problem_free(tdg_problem *prob);
+
+/* Writes outfile.thermal_conductivity (main.f90:246-294) into `dir`. Tensors in a.u. */
+int tdg_write_outfile(const char *dir, double temperature, const double *kappa_sma,
+                      const double *kappa_iter, const double *kappa_offdiag);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TDEP_GB300_H */

@@ -1,0 +1,402 @@
+// Crystal structure input, masses and space-group operations.
+#include "crystal.hpp"
+
+#include <algorithm>
+#include <fstream>
+#include <map>
+#include <sstream>
+
+namespace tdg {
+
+namespace {
+
+// Standard atomic weights (amu) of the elements the synthetic workloads and the
+// reference's test fixtures use. Other elements need infile.isotopes.
+const std::map<std::string, double> &atomic_weights() {
+    static const std::map<std::string, double> w = {
+        {"H", 1.008},     {"Li", 6.94},     {"Be", 9.0122},  {"B", 10.81},    {"C", 12.011},
+        {"N", 14.007},    {"O", 15.999},    {"F", 18.998},   {"Na", 22.990},  {"Mg", 24.305},
+        {"Al", 26.982},   {"Si", 28.085},   {"P", 30.974},   {"S", 32.06},    {"Cl", 35.45},
+        {"K", 39.098},    {"Ca", 40.078},   {"Sc", 44.956},  {"Ti", 47.867},  {"V", 50.942},
+        {"Cr", 51.996},   {"Mn", 54.938},   {"Fe", 55.845},  {"Co", 58.933},  {"Ni", 58.693},
+        {"Cu", 63.546},   {"Zn", 65.38},    {"Ga", 69.723},  {"Ge", 72.630},  {"As", 74.922},
+        {"Se", 78.971},   {"Br", 79.904},   {"Rb", 85.468},  {"Sr", 87.62},   {"Y", 88.906},
+        {"Zr", 91.224},   {"Nb", 92.906},   {"Mo", 95.95},   {"Ag", 107.87},  {"Cd", 112.41},
+        {"In", 114.82},   {"Sn", 118.71},   {"Sb", 121.76},  {"Te", 127.60},  {"I", 126.90},
+        {"Cs", 132.91},   {"Ba", 137.33},   {"La", 138.91},  {"Hf", 178.49},  {"Ta", 180.95},
+        {"W", 183.84},    {"Pt", 195.08},   {"Au", 196.97},  {"Pb", 207.2},   {"Bi", 208.98},
+    };
+    return w;
+}
+
+std::vector<std::string> split_ws(const std::string &s) {
+    std::istringstream is(s);
+    std::vector<std::string> out;
+    std::string t;
+    while (is >> t) out.push_back(t);
+    return out;
+}
+
+bool getline_nonempty(std::istream &is, std::string &line) {
+    while (std::getline(is, line)) {
+        if (line.find_first_not_of(" \t\r") != std::string::npos) return true;
+    }
+    return false;
+}
+
+}  // namespace
+
+int read_poscar(const std::string &path, Crystal &c) {
+    std::ifstream f(path);
+    if (!f) return set_error(kErrIo, "cannot open " + path);
+    std::string line;
+    std::getline(f, line);  // header
+    if (!getline_nonempty(f, line)) return set_error(kErrIo, "truncated " + path);
+    const double latpar = std::stod(split_ws(line).at(0));
+    M3 m;
+    for (int j = 0; j < 3; ++j) {
+        if (!getline_nonempty(f, line)) return set_error(kErrIo, "truncated " + path);
+        auto t = split_ws(line);
+        if (t.size() < 3) return set_error(kErrIo, "bad lattice line in " + path);
+        for (int i = 0; i < 3; ++i) m(i, j) = std::stod(t[i]);
+    }
+    if (!getline_nonempty(f, line)) return set_error(kErrIo, "truncated " + path);
+    c.symbols = split_ws(line);
+    if (!getline_nonempty(f, line)) return set_error(kErrIo, "truncated " + path);
+    auto counts = split_ws(line);
+    if (counts.size() != c.symbols.size()) return set_error(kErrIo, "species/count mismatch in " + path);
+    if (!getline_nonempty(f, line)) return set_error(kErrIo, "truncated " + path);
+    char mode = line[line.find_first_not_of(" \t")];
+    if (mode == 's' || mode == 'S') {
+        if (!getline_nonempty(f, line)) return set_error(kErrIo, "truncated " + path);
+        mode = line[line.find_first_not_of(" \t")];
+    }
+    bool cartesian;
+    if (mode == 'C' || mode == 'c')
+        cartesian = true;
+    else if (mode == 'D' || mode == 'd')
+        cartesian = false;
+    else
+        return set_error(kErrIo, "Specify either Cartesian or direct coordinates in " + path);
+    // Lattice parameter scales the lattice (negative = volume, as in VASP).
+    double scale = latpar;
+    if (latpar < 0) scale = std::cbrt(-latpar / std::fabs(det(m)));
+    for (double &x : m.a) x *= scale * kAToBohr;
+    c.lat = m;
+    c.inv_lat = inverse(m);
+    c.reclat = transpose(c.inv_lat);  // b_j: columns of A^{-T}
+    c.inv_reclat = inverse(c.reclat);
+    c.volume = std::fabs(det(m));
+    c.frac.clear();
+    c.species.clear();
+    for (size_t s = 0; s < counts.size(); ++s) {
+        const int cnt = std::stoi(counts[s]);
+        for (int k = 0; k < cnt; ++k) {
+            if (!getline_nonempty(f, line)) return set_error(kErrIo, "truncated positions in " + path);
+            auto t = split_ws(line);
+            if (t.size() < 3) return set_error(kErrIo, "bad position line in " + path);
+            V3 v;
+            for (int i = 0; i < 3; ++i) v[i] = std::stod(t[i]);
+            if (cartesian) {
+                for (int i = 0; i < 3; ++i) v[i] *= scale * kAToBohr;
+                v = mul(c.inv_lat, v);
+            }
+            c.frac.push_back(v);
+            c.species.push_back((int)s);
+        }
+    }
+    c.na = (int)c.frac.size();
+    c.rcart.resize(c.na);
+    c.mass.assign(c.na, 0.0);
+    c.invsqrtmass.assign(c.na, 0.0);
+    c.disorder.assign(c.na, 0.0);
+    for (int a = 0; a < c.na; ++a) {
+        c.rcart[a] = c.frac_to_cart(c.frac[a]);
+        const auto &w = atomic_weights();
+        auto it = w.find(c.symbols[c.species[a]]);
+        if (it != w.end()) {
+            c.mass[a] = it->second * kAmuToEmu;
+            c.invsqrtmass[a] = 1.0 / std::sqrt(c.mass[a]);
+        }
+    }
+    return kOk;
+}
+
+int read_isotopes(const std::string &path, Crystal &c) {
+    std::ifstream f(path);
+    if (!f) return set_error(kErrIo, "cannot open " + path);
+    for (int a = 0; a < c.na; ++a) {
+        int n = 0;
+        if (!(f >> n) || n < 1) return set_error(kErrIo, "bad isotope count in " + path);
+        std::vector<double> conc(n), mass(n);
+        double csum = 0;
+        for (int j = 0; j < n; ++j) {
+            if (!(f >> conc[j] >> mass[j])) return set_error(kErrIo, "truncated " + path);
+            mass[j] *= kAmuToEmu;
+            csum += conc[j];
+        }
+        double mean = 0;
+        for (int j = 0; j < n; ++j) {
+            conc[j] /= csum;
+            mean += conc[j] * mass[j];
+        }
+        double g = 0;
+        for (int j = 0; j < n; ++j) g += conc[j] * (mass[j] - mean) * (mass[j] - mean);
+        c.mass[a] = mean;
+        c.invsqrtmass[a] = 1.0 / std::sqrt(mean);
+        c.disorder[a] = g / (mean * mean);
+    }
+    return kOk;
+}
+
+namespace {
+// Distance of a fractional vector to the nearest lattice point, in Bohr.
+double frac_dist(const Crystal &c, const V3 &d) {
+    V3 w;
+    for (int i = 0; i < 3; ++i) w[i] = d[i] - anint(d[i]);
+    return std::sqrt(sqnorm(c.frac_to_cart(w)));
+}
+}  // namespace
+
+int find_symmetry(Crystal &c) {
+    // Metric tensor G = A^T A; a lattice rotation W (integer, fractional) keeps it.
+    const M3 G = mul(transpose(c.lat), c.lat);
+    double gscale = 0;
+    for (double x : G.a) gscale = std::max(gscale, std::fabs(x));
+    std::vector<SymOp> ops;
+    int w[9];
+    for (int code = 0; code < 19683; ++code) {
+        int r = code;
+        for (int k = 0; k < 9; ++k) {
+            w[k] = r % 3 - 1;
+            r /= 3;
+        }
+        M3 W;
+        for (int k = 0; k < 9; ++k) W.a[k] = w[k];
+        const double d = det(W);
+        if (std::fabs(std::fabs(d) - 1.0) > 1e-8) continue;
+        const M3 GW = mul(mul(transpose(W), G), W);
+        bool ok = true;
+        for (int k = 0; k < 9 && ok; ++k) ok = std::fabs(GW.a[k] - G.a[k]) < 1e-6 * gscale;
+        if (!ok) continue;
+        // Candidate translations map atom 0 onto any atom of the same species.
+        for (int j = 0; j < c.na; ++j) {
+            if (c.species[j] != c.species[0]) continue;
+            const V3 w0 = mul(W, c.frac[0]);
+            V3 t;
+            for (int i = 0; i < 3; ++i) t[i] = c.frac[j][i] - w0[i];
+            for (int i = 0; i < 3; ++i) t[i] -= std::floor(t[i] + 1e-9);
+            bool maps = true;
+            for (int a = 0; a < c.na && maps; ++a) {
+                const V3 wa = mul(W, c.frac[a]);
+                bool found = false;
+                for (int b = 0; b < c.na && !found; ++b) {
+                    if (c.species[b] != c.species[a]) continue;
+                    V3 dd;
+                    for (int i = 0; i < 3; ++i) dd[i] = wa[i] + t[i] - c.frac[b][i];
+                    found = frac_dist(c, dd) < 1e-4;
+                }
+                maps = found;
+            }
+            if (!maps) continue;
+            SymOp op;
+            for (int k = 0; k < 9; ++k) op.fm[k] = w[k];
+            op.m = mul(mul(c.lat, W), c.inv_lat);
+            // reciprocal fractional rotation: B^-1 m B = W^{-T}
+            const M3 rf = transpose(inverse(W));
+            for (int k = 0; k < 9; ++k) op.rfm[k] = (int32_t)anint(rf.a[k]);
+            op.tr = t;
+            ops.push_back(op);
+        }
+    }
+    // Identity (with zero translation) first, the rest in enumeration order.
+    auto is_identity = [](const SymOp &o) {
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j)
+                if (o.fm[i + 3 * j] != (i == j ? 1 : 0)) return false;
+        return true;
+    };
+    std::stable_partition(ops.begin(), ops.end(), is_identity);
+    if (ops.empty() || !is_identity(ops[0])) return set_error(kErrSymmetry, "identity operation not found");
+    c.ops = ops;
+    return kOk;
+}
+
+int read_fc2(const std::string &path, const Crystal &c, FC2 &fc) {
+    std::ifstream f(path);
+    if (!f) return set_error(kErrIo, "cannot open " + path);
+    std::string line;
+    auto first_tokens = [&](int k, std::vector<double> &out) -> bool {
+        if (!getline_nonempty(f, line)) return false;
+        auto t = split_ws(line);
+        if ((int)t.size() < k) return false;
+        out.resize(k);
+        for (int i = 0; i < k; ++i) out[i] = std::stod(t[i]);
+        return true;
+    };
+    std::vector<double> v;
+    if (!first_tokens(1, v)) return set_error(kErrIo, "truncated " + path);
+    fc.na = (int)v[0];
+    if (fc.na != c.na)
+        return set_error(kErrIo, "different number of atoms in \"" + path + "\" and the structure");
+    if (!first_tokens(1, v)) return set_error(kErrIo, "truncated " + path);  // cutoff
+    fc.pairs.clear();
+    for (int a1 = 0; a1 < fc.na; ++a1) {
+        if (!first_tokens(1, v)) return set_error(kErrIo, "truncated " + path);
+        const int n = (int)v[0];
+        for (int i = 0; i < n; ++i) {
+            FC2Pair p;
+            p.a1 = a1;
+            if (!first_tokens(1, v)) return set_error(kErrIo, "truncated " + path);
+            p.a2 = (int)v[0] - 1;
+            if (p.a2 < 0 || p.a2 >= c.na) return set_error(kErrIo, "bad atom index in " + path);
+            if (!first_tokens(3, v)) return set_error(kErrIo, "truncated " + path);
+            V3 lvf;
+            for (int k = 0; k < 3; ++k) lvf[k] = v[k];
+            p.lv = c.frac_to_cart(lvf);
+            for (int k = 0; k < 3; ++k)
+                if (std::fabs(p.lv[k]) < kSqTol) p.lv[k] = 0.0;
+            for (int j = 0; j < 3; ++j) {
+                if (!first_tokens(3, v)) return set_error(kErrIo, "truncated " + path);
+                for (int k = 0; k < 3; ++k) p.m[j + 3 * k] = v[k] * kFc2EvAToHaBohr;
+            }
+            fc.pairs.push_back(p);
+        }
+    }
+    // Polar correction flag; the long-range block itself is not used by this build.
+    if (first_tokens(1, v)) fc.polar = (int)v[0];
+    return kOk;
+}
+
+namespace {
+int read_int_line(std::istream &f, int &x) {
+    std::string line;
+    if (!getline_nonempty(f, line)) return 0;
+    auto t = split_ws(line);
+    x = std::stoi(t.at(0));
+    return 1;
+}
+int read_vec_line(std::istream &f, double *x) {
+    std::string line;
+    if (!getline_nonempty(f, line)) return 0;
+    auto t = split_ws(line);
+    if (t.size() < 3) return 0;
+    for (int i = 0; i < 3; ++i) x[i] = std::stod(t[i]);
+    return 1;
+}
+// A force-constant lattice vector must be integer in fractional coordinates.
+int to_lattice(const double *x, int32_t *out) {
+    for (int i = 0; i < 3; ++i) {
+        const double r = anint(x[i]);
+        if (std::fabs(x[i] - r) > 1e-6) return 0;
+        out[i] = (int32_t)r;
+    }
+    return 1;
+}
+}  // namespace
+
+int read_fc3(const std::string &path, const Crystal &c, FC3 &fc) {
+    std::ifstream f(path);
+    if (!f) return set_error(kErrIo, "cannot open " + path);
+    int na = 0;
+    double cut[3];
+    if (!read_int_line(f, na)) return set_error(kErrIo, "truncated " + path);
+    std::string line;
+    if (!getline_nonempty(f, line)) return set_error(kErrIo, "truncated " + path);
+    (void)cut;
+    if (na != c.na) return set_error(kErrIo, "different number of atoms in \"" + path + "\" and the structure");
+    fc.atoms.clear();
+    fc.lv.clear();
+    fc.lvcart.clear();
+    fc.mwm.clear();
+    for (int a1 = 0; a1 < na; ++a1) {
+        int n = 0;
+        if (!read_int_line(f, n)) return set_error(kErrIo, "truncated " + path);
+        for (int t = 0; t < n; ++t) {
+            int ii[3];
+            for (int k = 0; k < 3; ++k)
+                if (!read_int_line(f, ii[k])) return set_error(kErrIo, "truncated " + path);
+            for (int k = 0; k < 3; ++k)
+                if (ii[k] < 1 || ii[k] > na) return set_error(kErrIo, "bad atom index in " + path);
+            double lvs[9];
+            for (int k = 0; k < 3; ++k)
+                if (!read_vec_line(f, lvs + 3 * k)) return set_error(kErrIo, "truncated " + path);
+            int32_t lvi[9];
+            for (int k = 0; k < 3; ++k)
+                if (!to_lattice(lvs + 3 * k, lvi + 3 * k))
+                    return set_error(kErrIo, "non-integer lattice vector in " + path);
+            double m[27];
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) {
+                    double v[3];
+                    if (!read_vec_line(f, v)) return set_error(kErrIo, "truncated " + path);
+                    for (int k = 0; k < 3; ++k) m[i + 3 * j + 9 * k] = v[k] * kFc3EvAToHaBohr;
+                }
+            const double w = c.invsqrtmass[ii[0] - 1] * c.invsqrtmass[ii[1] - 1] * c.invsqrtmass[ii[2] - 1];
+            for (int k = 0; k < 3; ++k) fc.atoms.push_back(ii[k]);
+            for (int k = 3; k < 9; ++k) fc.lv.push_back(lvi[k]);
+            for (int k = 1; k < 3; ++k) {
+                V3 lf;
+                for (int i = 0; i < 3; ++i) lf[i] = lvs[3 * k + i];
+                V3 lc = c.frac_to_cart(lf);
+                for (int i = 0; i < 3; ++i) fc.lvcart.push_back(std::fabs(lc[i]) < kSqTol ? 0.0 : lc[i]);
+            }
+            for (int k = 0; k < 27; ++k) fc.mwm.push_back(m[k] * w);
+        }
+    }
+    return kOk;
+}
+
+int read_fc4(const std::string &path, const Crystal &c, FC4 &fc) {
+    std::ifstream f(path);
+    if (!f) return set_error(kErrIo, "cannot open " + path);
+    int na = 0;
+    if (!read_int_line(f, na)) return set_error(kErrIo, "truncated " + path);
+    std::string line;
+    if (!getline_nonempty(f, line)) return set_error(kErrIo, "truncated " + path);
+    if (na != c.na) return set_error(kErrIo, "different number of atoms in \"" + path + "\" and the structure");
+    fc.atoms.clear();
+    fc.lv.clear();
+    fc.lvcart.clear();
+    fc.mwm.clear();
+    for (int a1 = 0; a1 < na; ++a1) {
+        int n = 0;
+        if (!read_int_line(f, n)) return set_error(kErrIo, "truncated " + path);
+        for (int t = 0; t < n; ++t) {
+            int ii[4];
+            for (int k = 0; k < 4; ++k)
+                if (!read_int_line(f, ii[k])) return set_error(kErrIo, "truncated " + path);
+            for (int k = 0; k < 4; ++k)
+                if (ii[k] < 1 || ii[k] > na) return set_error(kErrIo, "bad atom index in " + path);
+            double lvs[12];
+            for (int k = 0; k < 4; ++k)
+                if (!read_vec_line(f, lvs + 3 * k)) return set_error(kErrIo, "truncated " + path);
+            int32_t lvi[12];
+            for (int k = 0; k < 4; ++k)
+                if (!to_lattice(lvs + 3 * k, lvi + 3 * k))
+                    return set_error(kErrIo, "non-integer lattice vector in " + path);
+            double m[81];
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j)
+                    for (int k = 0; k < 3; ++k) {
+                        double v[3];
+                        if (!read_vec_line(f, v)) return set_error(kErrIo, "truncated " + path);
+                        for (int l = 0; l < 3; ++l) m[i + 3 * j + 9 * k + 27 * l] = v[l] * kFc4EvAToHaBohr;
+                    }
+            const double w = c.invsqrtmass[ii[0] - 1] * c.invsqrtmass[ii[1] - 1] *
+                             c.invsqrtmass[ii[2] - 1] * c.invsqrtmass[ii[3] - 1];
+            for (int k = 0; k < 4; ++k) fc.atoms.push_back(ii[k]);
+            for (int k = 3; k < 12; ++k) fc.lv.push_back(lvi[k]);
+            for (int k = 1; k < 4; ++k) {
+                V3 lf;
+                for (int i = 0; i < 3; ++i) lf[i] = lvs[3 * k + i];
+                V3 lc = c.frac_to_cart(lf);
+                for (int i = 0; i < 3; ++i) fc.lvcart.push_back(std::fabs(lc[i]) < kSqTol ? 0.0 : lc[i]);
+            }
+            for (int k = 0; k < 81; ++k) fc.mwm.push_back(m[k] * w);
+        }
+    }
+    return kOk;
+}
+
+}  // namespace tdg

@@ -1,0 +1,108 @@
+// Host-side model of the inputs of thermal_conductivity: crystal structure with its
+// symmetry operations, force constants of order 2/3/4, the FFT q-mesh and the harmonic
+// phonons. These mirror the libolle types the scattering path consumes.
+#pragma once
+
+#include "common.hpp"
+
+namespace tdg {
+
+struct SymOp {
+    M3 m;              // Cartesian rotation (op%m)
+    int32_t fm[9];     // integer rotation of fractional real-space coordinates
+    int32_t rfm[9];    // integer rotation of fractional reciprocal coordinates (op%rfm)
+    V3 tr;             // fractional translation
+};
+
+struct Crystal {
+    int na = 0;
+    M3 lat;            // latticevectors (columns), Bohr
+    M3 inv_lat;
+    M3 reclat;         // reciprocal_latticevectors (columns), a_i.b_j = delta_ij
+    M3 inv_reclat;
+    double volume = 0;
+    std::vector<V3> frac;             // fractional positions
+    std::vector<V3> rcart;            // Cartesian positions
+    std::vector<int> species;         // 0-based species index
+    std::vector<std::string> symbols; // per species
+    std::vector<double> mass;         // electron masses
+    std::vector<double> invsqrtmass;
+    std::vector<double> disorder;     // isotope mass-disorder parameter
+    std::vector<SymOp> ops;
+
+    V3 frac_to_cart(const V3 &v) const { return mul(lat, v); }
+};
+
+// type_crystalstructure_io.f90:9 (readfromfile). Masses from standard atomic weights.
+int read_poscar(const std::string &path, Crystal &c);
+// type_crystalstructure_io.f90:921-957 (readisotopefromfile).
+int read_isotopes(const std::string &path, Crystal &c);
+// Space-group operations of the cell: lattice rotations that map the crystal onto
+// itself with some fractional translation. Identity first.
+int find_symmetry(Crystal &c);
+
+struct FC2Pair {
+    int a1, a2;        // 0-based
+    V3 lv;             // Cartesian lattice vector, Bohr
+    double m[9];       // Hartree/Bohr^2, m(i,j) at i + 3j
+};
+struct FC2 {
+    int na = 0;
+    std::vector<FC2Pair> pairs;
+    int polar = 0;
+};
+// type_forceconstant_secondorder_io.f90:136-200. The polar block is read and ignored.
+int read_fc2(const std::string &path, const Crystal &c, FC2 &fc);
+
+struct FC3 {
+    std::vector<int32_t> atoms;    // n*3, 1-based
+    std::vector<int32_t> lv;       // n*6 fractional integer (lv2, lv3)
+    std::vector<double> lvcart;    // n*6 Cartesian (lv2, lv3)
+    std::vector<double> mwm;       // n*27
+    int n() const { return (int)(atoms.size() / 3); }
+};
+// type_forceconstant_thirdorder.f90:243-311.
+int read_fc3(const std::string &path, const Crystal &c, FC3 &fc);
+
+struct FC4 {
+    std::vector<int32_t> atoms;    // n*4
+    std::vector<int32_t> lv;       // n*9
+    std::vector<double> lvcart;    // n*9
+    std::vector<double> mwm;       // n*81
+    int n() const { return (int)(atoms.size() / 4); }
+};
+// type_forceconstant_fourthorder.f90:259-330.
+int read_fc4(const std::string &path, const Crystal &c, FC4 &fc);
+
+struct QMesh {
+    int grid[3] = {0, 0, 0};
+    int n_full = 0, n_irr = 0;
+    std::vector<V3> q_full;               // Cartesian, folded to the first zone
+    std::vector<V3> qfrac;                // fractional (folded)
+    std::vector<int32_t> full_irr;        // 1-based
+    std::vector<int32_t> full_op;         // signed 1-based
+    std::vector<int32_t> irr_full;        // 1-based
+    std::vector<double> irr_weight;
+    std::vector<int32_t> irr_nop;
+    std::vector<int32_t> irr_ops;         // n_irr * n_op, 0-padded, 1-based
+};
+// type_qpointmesh_gridgeneration.f90:8-545 for the Gamma-centred FFT mesh.
+int build_fft_mesh(const Crystal &c, const int grid[3], bool timereversal, QMesh &qp);
+
+struct Phonons {
+    int n_mode = 0;
+    std::vector<double> omega;    // n_full*n
+    std::vector<double> egv;      // n_full*n*n*2
+    std::vector<double> vel;      // n_full*n*3
+    std::vector<int32_t> degen;   // n_full*n
+    std::vector<int32_t> degen_mode; // n_full*n*n
+};
+// D(q) (type_forceconstant_secondorder_dynamicalmatrix.f90:484-788), Hermitian
+// diagonalisation, group velocities and degeneracy tables at every mesh point.
+int build_phonons(const Crystal &c, const FC2 &fc, const QMesh &qp, Phonons &ph);
+
+// Complex Hermitian Jacobi eigensolver: a is n x n column-major, overwritten.
+// Eigenvalues unsorted in w, eigenvectors as columns of v.
+int hermitian_jacobi(int n, std::vector<cplx> &a, std::vector<double> &w, std::vector<cplx> &v);
+
+}  // namespace tdg

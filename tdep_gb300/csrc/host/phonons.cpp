@@ -1,0 +1,236 @@
+// Harmonic phonons on every point of the mesh: dynamical matrix and its gradient
+// (type_forceconstant_secondorder_dynamicalmatrix.f90:484-788, non-polar branch),
+// Hermitian diagonalisation (:113-164), group velocities (:167-200) and the degeneracy
+// tables (type_phonon_dispersions.f90:1190-1212).
+//
+// Unlike the reference, which diagonalises the irreducible points and rotates the
+// eigenvectors onto the rest of the mesh, every point is diagonalised directly; the
+// eigenvector gauge inside degenerate subspaces therefore differs, while every
+// degeneracy-summed quantity (linewidths, kappa) is the same.
+#include <algorithm>
+#include <numeric>
+#include <thread>
+
+#include "crystal.hpp"
+
+namespace tdg {
+
+int hermitian_jacobi(int n, std::vector<cplx> &a, std::vector<double> &w, std::vector<cplx> &v) {
+    // Cyclic Jacobi with complex rotations: for each (p,q) the phase of a_pq is absorbed
+    // into column q, then a real Jacobi rotation zeroes the (now real) off-diagonal.
+    v.assign((size_t)n * n, cplx(0, 0));
+    for (int i = 0; i < n; ++i) v[i + (size_t)n * i] = 1.0;
+    auto A = [&](int i, int j) -> cplx & { return a[i + (size_t)n * j]; };
+    double scale = 0;
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) scale += std::norm(A(i, j));
+    if (scale == 0) {
+        w.assign(n, 0.0);
+        return kOk;
+    }
+    for (int sweep = 0; sweep < 100; ++sweep) {
+        double off = 0;
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i < n; ++i)
+                if (i != j) off += std::norm(A(i, j));
+        if (off <= 1e-30 * scale) break;
+        for (int p = 0; p < n - 1; ++p)
+            for (int q = p + 1; q < n; ++q) {
+                const cplx g = A(p, q);
+                const double ag = std::abs(g);
+                if (ag <= 1e-300) continue;
+                const cplx u = g / ag;
+                const double app = A(p, p).real(), aqq = A(q, q).real();
+                const double tau = (aqq - app) / (2.0 * ag);
+                const double t = (tau >= 0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1.0 + tau * tau));
+                const double cs = 1.0 / std::sqrt(1.0 + t * t);
+                const double sn = t * cs;
+                // J = [[c, s], [-conj(u) s, conj(u) c]] acting on columns p, q.
+                const cplx jqp = -std::conj(u) * sn, jqq = std::conj(u) * cs;
+                for (int k = 0; k < n; ++k) {  // A <- A J
+                    const cplx akp = A(k, p), akq = A(k, q);
+                    A(k, p) = akp * cs + akq * jqp;
+                    A(k, q) = akp * sn + akq * jqq;
+                }
+                for (int k = 0; k < n; ++k) {  // A <- J^H A
+                    const cplx apk = A(p, k), aqk = A(q, k);
+                    A(p, k) = cs * apk + std::conj(jqp) * aqk;
+                    A(q, k) = sn * apk + std::conj(jqq) * aqk;
+                }
+                A(p, q) = 0.0;
+                A(q, p) = 0.0;
+                A(p, p) = A(p, p).real();
+                A(q, q) = A(q, q).real();
+                for (int k = 0; k < n; ++k) {  // V <- V J
+                    const cplx vkp = v[k + (size_t)n * p], vkq = v[k + (size_t)n * q];
+                    v[k + (size_t)n * p] = vkp * cs + vkq * jqp;
+                    v[k + (size_t)n * q] = vkp * sn + vkq * jqq;
+                }
+            }
+        if (sweep == 99) return set_error(kErrLinalg, "Jacobi eigensolver did not converge");
+    }
+    w.resize(n);
+    for (int i = 0; i < n; ++i) w[i] = A(i, i).real();
+    return kOk;
+}
+
+namespace {
+
+double negsqrt(double x) { return x >= 0 ? std::sqrt(x) : -std::sqrt(-x); }
+
+int solve_point(const Crystal &c, const FC2 &fc, const V3 &qr, int nb, double *omega, double *egv,
+                double *vel) {
+    // D((a2,j),(a1,i)) = sum_pairs exp(i q.R) m(i,j) / sqrt(m1 m2), q with 2*pi.
+    V3 qv;
+    for (int d = 0; d < 3; ++d) {
+        qv[d] = qr[d] * kTwoPi;
+        if (std::fabs(qv[d]) < 1e-13) qv[d] = 0.0;
+    }
+    std::vector<cplx> D((size_t)nb * nb, 0.0), G((size_t)3 * nb * nb, 0.0);
+    for (const auto &p : fc.pairs) {
+        const double qdotr = p.lv[0] * qv[0] + p.lv[1] * qv[1] + p.lv[2] * qv[2];
+        const cplx e(std::cos(qdotr), std::sin(qdotr));
+        const double ms = c.invsqrtmass[p.a1] * c.invsqrtmass[p.a2];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                const int ii = p.a2 * 3 + j, jj = p.a1 * 3 + i;
+                const cplx val = e * p.m[i + 3 * j] * ms;
+                D[ii + (size_t)nb * jj] += val;
+                for (int d = 0; d < 3; ++d) G[(size_t)d * nb * nb + ii + (size_t)nb * jj] += cplx(0, p.lv[d]) * val;
+            }
+    }
+    // Hermitise against rounding before diagonalising.
+    for (int i = 0; i < nb; ++i)
+        for (int j = i; j < nb; ++j) {
+            const cplx s = 0.5 * (D[i + (size_t)nb * j] + std::conj(D[j + (size_t)nb * i]));
+            D[i + (size_t)nb * j] = s;
+            D[j + (size_t)nb * i] = std::conj(s);
+        }
+    std::vector<cplx> A = D, V;
+    std::vector<double> w;
+    int st = hermitian_jacobi(nb, A, w, V);
+    if (st) return st;
+    // Acoustic modes at Gamma: zero the three smallest |eigenvalues|.
+    if (sqnorm(qr) < kSqTol) {
+        std::vector<int> idx(nb);
+        std::iota(idx.begin(), idx.end(), 0);
+        std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return std::fabs(w[a]) < std::fabs(w[b]); });
+        for (int i = 0; i < std::min(3, nb); ++i) w[idx[i]] = 0.0;
+    }
+    std::vector<int> ord(nb);
+    std::iota(ord.begin(), ord.end(), 0);
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return negsqrt(w[a]) < negsqrt(w[b]); });
+    std::vector<cplx> E((size_t)nb * nb);
+    std::vector<double> om(nb);
+    for (int b = 0; b < nb; ++b) {
+        om[b] = negsqrt(w[ord[b]]);
+        for (int r = 0; r < nb; ++r) E[r + (size_t)nb * b] = V[r + (size_t)nb * ord[b]];
+    }
+    // Degenerate subspaces: rotate the eigenvectors so that the velocity operator along
+    // a fixed generic direction is diagonal inside each subspace, then use
+    // Hellmann-Feynman velocities v = <e|dD/dk|e> / (2 omega).
+    const double dir[3] = {1.0, 1.33, 1.45624623};
+    for (int b0 = 0; b0 < nb;) {
+        int b1 = b0 + 1;
+        while (b1 < nb && std::fabs(om[b1] - om[b0]) < kFreqTol) ++b1;
+        const int k = b1 - b0;
+        if (k > 1) {
+            std::vector<cplx> P((size_t)k * k, 0.0);
+            for (int x = 0; x < k; ++x)
+                for (int y = 0; y < k; ++y) {
+                    cplx s = 0;
+                    for (int d = 0; d < 3; ++d)
+                        for (int r = 0; r < nb; ++r) {
+                            cplx gy = 0;
+                            for (int cc = 0; cc < nb; ++cc)
+                                gy += G[(size_t)d * nb * nb + r + (size_t)nb * cc] * E[cc + (size_t)nb * (b0 + y)];
+                            s += dir[d] * std::conj(E[r + (size_t)nb * (b0 + x)]) * gy;
+                        }
+                    P[x + (size_t)k * y] = s;
+                }
+            for (int x = 0; x < k; ++x)
+                for (int y = x; y < k; ++y) {
+                    const cplx s = 0.5 * (P[x + (size_t)k * y] + std::conj(P[y + (size_t)k * x]));
+                    P[x + (size_t)k * y] = s;
+                    P[y + (size_t)k * x] = std::conj(s);
+                }
+            std::vector<double> pw;
+            std::vector<cplx> U;
+            st = hermitian_jacobi(k, P, pw, U);
+            if (st) return st;
+            std::vector<int> po(k);
+            std::iota(po.begin(), po.end(), 0);
+            std::stable_sort(po.begin(), po.end(), [&](int a, int b) { return pw[a] < pw[b]; });
+            std::vector<cplx> sub((size_t)nb * k, 0.0);
+            for (int y = 0; y < k; ++y)
+                for (int r = 0; r < nb; ++r) {
+                    cplx s = 0;
+                    for (int x = 0; x < k; ++x) s += E[r + (size_t)nb * (b0 + x)] * U[x + (size_t)k * po[y]];
+                    sub[r + (size_t)nb * y] = s;
+                }
+            for (int y = 0; y < k; ++y)
+                for (int r = 0; r < nb; ++r) E[r + (size_t)nb * (b0 + y)] = sub[r + (size_t)nb * y];
+        }
+        b0 = b1;
+    }
+    for (int b = 0; b < nb; ++b) {
+        omega[b] = om[b];
+        for (int r = 0; r < nb; ++r) {
+            egv[((size_t)b * nb + r) * 2] = E[r + (size_t)nb * b].real();
+            egv[((size_t)b * nb + r) * 2 + 1] = E[r + (size_t)nb * b].imag();
+        }
+        for (int d = 0; d < 3; ++d) {
+            cplx s = 0;
+            for (int r = 0; r < nb; ++r) {
+                cplx gy = 0;
+                for (int cc = 0; cc < nb; ++cc) gy += G[(size_t)d * nb * nb + r + (size_t)nb * cc] * E[cc + (size_t)nb * b];
+                s += std::conj(E[r + (size_t)nb * b]) * gy;
+            }
+            vel[b * 3 + d] = om[b] > kFreqTol ? s.real() / (2.0 * om[b]) : 0.0;
+        }
+    }
+    return kOk;
+}
+
+}  // namespace
+
+int build_phonons(const Crystal &c, const FC2 &fc, const QMesh &qp, Phonons &ph) {
+    const int nb = 3 * c.na;
+    const int np = qp.n_full;
+    ph.n_mode = nb;
+    ph.omega.assign((size_t)np * nb, 0.0);
+    ph.egv.assign((size_t)np * nb * nb * 2, 0.0);
+    ph.vel.assign((size_t)np * nb * 3, 0.0);
+    ph.degen.assign((size_t)np * nb, 0);
+    ph.degen_mode.assign((size_t)np * nb * nb, 0);
+    unsigned nth = std::max(1u, std::thread::hardware_concurrency());
+    nth = std::min<unsigned>(nth, 64);
+    std::vector<int> status(nth, kOk);
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nth; ++t)
+        th.emplace_back([&, t]() {
+            for (int q = (int)t; q < np; q += (int)nth) {
+                int st = solve_point(c, fc, qp.q_full[q], nb, &ph.omega[(size_t)q * nb],
+                                     &ph.egv[(size_t)q * nb * nb * 2], &ph.vel[(size_t)q * nb * 3]);
+                if (st) {
+                    status[t] = st;
+                    return;
+                }
+            }
+        });
+    for (auto &x : th) x.join();
+    for (int st : status)
+        if (st) return st;
+    for (int q = 0; q < np; ++q) {
+        const double *om = &ph.omega[(size_t)q * nb];
+        for (int b1 = 0; b1 < nb; ++b1) {
+            int l = 0;
+            for (int b2 = 0; b2 < nb; ++b2)
+                if (std::fabs(om[b1] - om[b2]) < kFreqTol) ph.degen_mode[((size_t)q * nb + b1) * nb + l++] = b2 + 1;
+            ph.degen[(size_t)q * nb + b1] = l;
+        }
+    }
+    return kOk;
+}
+
+}  // namespace tdg

@@ -1,0 +1,248 @@
+// Isotope scattering, the two scattering-matrix symmetrisations and the BTE product.
+#include <cuda_runtime.h>
+
+#include "tdg_internal.cuh"
+
+namespace tdg {
+
+namespace {
+
+constexpr double kIsotopePrefactor = 3.141592653589793 / 4.0;
+constexpr double kSqrt2PiInv = 0.398942280401433;
+constexpr double kFreqTolD = 1E-9;
+
+__device__ __forceinline__ double lo_gauss(double x, double mu, double sigma) {
+    if (fabs(x - mu) > 8.0 * sigma) return 0.0;
+    const double invsig = 1.0 / sigma;
+    return exp(-(x - mu) * (x - mu) * 0.5 * invsig * invsig) * kSqrt2PiInv * invsig;
+}
+
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < (int)((blockDim.x + 31) / 32); ++i) s += sh[i];
+    __syncthreads();
+    return s;
+}
+
+// compute_isotope_scattering (scattering_isotope.f90:1-91): one thread per (q2, b2) of a row.
+__global__ void k_isotope(MeshDev m, PhononDev ph, RowsDev rows, const int32_t *row_q1, const int32_t *row_b1,
+                          const double *disorder, int32_t n_atom, double *gamma, double *xi) {
+    __shared__ double sh[32];
+    const int n = m.n_mode;
+    const int r = blockIdx.y;
+    const int q1 = row_q1[r], b1 = row_b1[r];
+    const int f1 = m.irr_full[q1];
+    const int64_t ld = (int64_t)m.n_full * n;
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double f0 = 0.0;
+    if (j < ld) {
+        const int q2 = (int)(j / n), b2 = (int)(j % n);
+        const double om1 = ph.omega[(size_t)f1 * n + b1];
+        const double om2 = ph.omega[(size_t)q2 * n + b2];
+        if (!(om2 < kFreqTolD)) {
+            double sigma;
+            if (ph.integrationtype == 1) {
+                sigma = ph.sigma_fixed;
+            } else if (ph.integrationtype == 2) {
+                sigma = sqrt(ph.sigsq[(size_t)q1 * n + b1] + ph.sigsq[(size_t)m.full_irr[q2] * n + b2]);
+            } else {
+                const double *v = ph.vel + ((size_t)q2 * n + b2) * 3;
+                double mx = 0.0;
+                for (int jj = 0; jj < 3; ++jj) {
+                    double s = 0.0;
+                    for (int i = 0; i < 3; ++i) s += v[i] * ph.reclat_g[i + 3 * jj];
+                    mx = fmax(mx, s * s);
+                }
+                sigma = sqrt(mx * 0.5) + ph.thresh_sigma;
+            }
+            const double2 *e1 = ph.egv + ((size_t)f1 * n + b1) * n;
+            const double2 *e2 = ph.egv + ((size_t)q2 * n + b2) * n;
+            double f1s = 0.0;
+            for (int a = 0; a < n_atom; ++a) {
+                double fa = 0.0;
+                for (int x = 0; x < 3; ++x) {
+                    const double2 u = e1[a * 3 + x], v = e2[a * 3 + x];
+                    // |conjg(u) * v|
+                    const double re = u.x * v.x + u.y * v.y, im = u.x * v.y - u.y * v.x;
+                    fa += sqrt(re * re + im * im);
+                }
+                fa = fa * fa;
+                f1s += fa * disorder[a];
+            }
+            const double prefactor = kIsotopePrefactor * (1.0 / (double)m.n_full);
+            const double psisq = f1s * prefactor;
+            f0 = psisq * om1 * om2 * lo_gauss(om1, om2, sigma);
+            if (f0 != 0.0) xi[(int64_t)r * ld + j] += f0 * om2 / om1;
+        }
+    }
+    const double s = block_sum(f0, sh);
+    if (threadIdx.x == 0 && s != 0.0) atomicAdd(gamma + r, s);
+}
+
+// symmetrize_and_distribute (scattering_threephonon.f90:143-205, scattering_fourphonon.f90:195-250).
+// One CTA per row. Every orbit is handled by its smallest member (an image smaller than
+// q2 skips q2, as in the reference), so threads never touch the same entries. A bitmap
+// ignores repeated entries of a sample, which the reference would process to the same
+// result.
+__global__ void k_sym_distribute(MeshDev m, const int32_t *row_q1, const int64_t *ptr, const int32_t *list,
+                                 double *od, double *xi) {
+    extern __shared__ uint32_t seen[];
+    const int n = m.n_mode;
+    const int r = blockIdx.x;
+    const int q1 = row_q1[r];
+    const int nop = m.irr_nop[q1];
+    const int32_t *ops = m.irr_ops + (size_t)q1 * m.n_op;
+    const int64_t ld = (int64_t)m.n_full * n;
+    double *odr = od + (int64_t)r * ld;
+    const int nw = (m.n_full + 31) / 32;
+    for (int i = threadIdx.x; i < nw; i += blockDim.x) seen[i] = 0u;
+    __syncthreads();
+    for (int64_t qi = ptr[r] + threadIdx.x; qi < ptr[r + 1]; qi += blockDim.x) {
+        const int q2 = list[qi] - 1;
+        const uint32_t bit = 1u << (q2 & 31);
+        if (atomicOr(&seen[q2 >> 5], bit) & bit) continue;
+        bool skip = false;
+        for (int j = 0; j < nop && !skip; ++j) {
+            const int q2p = m.rot[(size_t)ops[j] * m.n_full + q2];
+            if (q2p >= 0 && q2p < q2) skip = true;
+        }
+        if (skip) continue;
+        for (int b2 = 0; b2 < n; ++b2) {
+            double buf = 0.0;
+            int nn = 0;
+            for (int j = 0; j < nop; ++j) {
+                const int q2p = m.rot[(size_t)ops[j] * m.n_full + q2];
+                if (q2p < 0) continue;
+                const double v = odr[(int64_t)q2p * n + b2];
+                if (v > 0.0) {
+                    ++nn;
+                    buf += v;
+                }
+            }
+            if (nn == 0) continue;
+            const double avg = buf / (double)nn;
+            for (int j = 0; j < nop; ++j) {
+                const int q2p = m.rot[(size_t)ops[j] * m.n_full + q2];
+                if (q2p < 0) continue;
+                odr[(int64_t)q2p * n + b2] = avg;
+            }
+        }
+    }
+    __syncthreads();
+    double *xr = xi + (int64_t)r * ld;
+    for (int64_t j = threadIdx.x; j < ld; j += blockDim.x) xr[j] += odr[j];
+}
+
+// symmetrize_scatmat (scattering.f90:296-357). One CTA per row, one thread per q2 orbit.
+__global__ void k_sym_scatmat(MeshDev m, const int32_t *row_q1, double *xi) {
+    const int n = m.n_mode;
+    const int r = blockIdx.y;
+    const int q2 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q2 >= m.n_full) return;
+    const int q1 = row_q1[r];
+    const int nop = m.irr_nop[q1];
+    const int32_t *ops = m.irr_ops + (size_t)q1 * m.n_op;
+    double *xr = xi + (int64_t)r * m.n_full * n;
+    int cnt = 0;
+    for (int j = 0; j < nop; ++j) {
+        const int q2p = m.rot[(size_t)ops[j] * m.n_full + q2];
+        if (q2p < 0) continue;
+        if (q2p < q2) return;
+        ++cnt;
+    }
+    if (cnt == 0) return;
+    for (int b2 = 0; b2 < n; ++b2) {
+        double buf = 0.0;
+        for (int j = 0; j < nop; ++j) {
+            const int q2p = m.rot[(size_t)ops[j] * m.n_full + q2];
+            if (q2p < 0) continue;
+            buf += xr[(int64_t)q2p * n + b2];
+        }
+        buf /= (double)cnt;
+        for (int j = 0; j < nop; ++j) {
+            const int q2p = m.rot[(size_t)ops[j] * m.n_full + q2];
+            if (q2p < 0) continue;
+            xr[(int64_t)q2p * n + b2] = buf;
+        }
+    }
+}
+
+// K8: three dot products per row of Xi (kappa.f90:411-413, the lo_gemv calls).
+// Xi streams from HBM once; F (3 x n_col) stays in L2.
+__global__ void k_xi_gemv(const double *__restrict__ xi, int64_t n_col, const double *__restrict__ fbb,
+                          double *buf) {
+    __shared__ double sh[3][32];
+    const int r = blockIdx.x;
+    const double *row = xi + (int64_t)r * n_col;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    for (int64_t j = threadIdx.x; j < n_col; j += blockDim.x) {
+        const double x = __ldcs(row + j);
+        const double *f = fbb + j * 3;
+        s0 = fma(x, __ldg(f), s0);
+        s1 = fma(x, __ldg(f + 1), s1);
+        s2 = fma(x, __ldg(f + 2), s2);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_down_sync(0xffffffffu, s0, o);
+        s1 += __shfl_down_sync(0xffffffffu, s1, o);
+        s2 += __shfl_down_sync(0xffffffffu, s2, o);
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        sh[0][w] = s0;
+        sh[1][w] = s1;
+        sh[2][w] = s2;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double s = 0.0;
+        for (int i = 0; i < (int)(blockDim.x / 32); ++i) s += sh[threadIdx.x][i];
+        buf[(int64_t)r * 3 + threadIdx.x] = s;
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_isotope(const MeshDev &m, const PhononDev &ph, const RowsDev &rows, const int32_t *row_q1,
+                           const int32_t *row_b1, const double *disorder, int32_t n_atom, double *gamma,
+                           double *xi, cudaStream_t s) {
+    if (rows.n_row <= 0) return cudaSuccess;
+    const int64_t ld = (int64_t)m.n_full * m.n_mode;
+    dim3 grid((unsigned)((ld + 255) / 256), (unsigned)rows.n_row);
+    k_isotope<<<grid, 256, 0, s>>>(m, ph, rows, row_q1, row_b1, disorder, n_atom, gamma, xi);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sym_distribute(const MeshDev &m, int32_t n_row, const int32_t *row_q1, const int64_t *ptr,
+                                  const int32_t *list, double *od, double *xi, cudaStream_t s) {
+    if (n_row <= 0) return cudaSuccess;
+    const size_t sm = sizeof(uint32_t) * (size_t)((m.n_full + 31) / 32);
+    if (sm > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_sym_distribute, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+    }
+    k_sym_distribute<<<n_row, 256, sm, s>>>(m, row_q1, ptr, list, od, xi);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sym_scatmat(const MeshDev &m, int32_t n_row, const int32_t *row_q1, double *xi, cudaStream_t s) {
+    if (n_row <= 0) return cudaSuccess;
+    dim3 grid((unsigned)((m.n_full + 127) / 128), (unsigned)n_row);
+    k_sym_scatmat<<<grid, 128, 0, s>>>(m, row_q1, xi);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_xi_gemv(const double *xi, int32_t n_row, int64_t n_col, const double *fbb, double *buf,
+                           int n_sm, cudaStream_t s) {
+    (void)n_sm;
+    if (n_row <= 0) return cudaSuccess;
+    k_xi_gemv<<<n_row, 256, 0, s>>>(xi, n_col, fbb, buf);
+    return cudaGetLastError();
+}
+
+}  // namespace tdg

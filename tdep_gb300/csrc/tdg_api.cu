@@ -1,0 +1,934 @@
+// C-ABI entry points: context, upload, scattering orchestration and the BTE solve.
+//
+// tdg_scattering follows lo_scattering_rates%generate (scattering.f90:58-358):
+//   init (:85-212)                     be, sigsq, rows            -> host, uploaded
+//   per row: isotope (:229-233)        K_iso                       -> device
+//            three-phonon (:234-238)   K1 enumerate, K2-4 fused, K5a symmetrise -> device
+//            four-phonon (:239-243)    K1 quartets, fused kernel, K5a            -> device
+//            boundary (:245-250)       host
+//   allreduce + degeneracy (:261-292) host (N_irr x n values)
+//   symmetrize_scatmat (:296-357)     K5b -> device
+// tdg_kappa follows get_kappa / iterative_solution / symmetrize_kappa (kappa.f90:28-75,
+// 308-495) with the Xi product on the device.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/tdep_gb300.h"
+#include "host/common.hpp"
+#include "tdg_internal.cuh"
+
+using namespace tdg;
+
+namespace {
+
+#define CUDA_TRY(expr)                                                                                 \
+    do {                                                                                               \
+        cudaError_t e_ = (expr);                                                                       \
+        if (e_ != cudaSuccess)                                                                         \
+            return set_error(kErrDevice, std::string(#expr) + ": " + cudaGetErrorString(e_));          \
+    } while (0)
+
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t alloc(size_t count) {
+        if (count <= n && p) return cudaSuccess;
+        release();
+        if (count == 0) count = 1;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e == cudaSuccess) n = count;
+        return e;
+    }
+    cudaError_t upload(const T *h, size_t count, cudaStream_t s) {
+        cudaError_t e = alloc(count);
+        if (e != cudaSuccess) return e;
+        if (count == 0) return cudaSuccess;
+        return cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s);
+    }
+};
+
+int gcd_i(int a, int b) { return b == 0 ? a : gcd_i(b, a % b); }
+
+// lo_chop (gottochblandat.f90:1286-1376): snap to 0, +-n/m (m <= 10), +-1/sqrt2, +-sqrt3/2, +-1.
+double lo_chop(double x, double tol) {
+    if (std::fabs(x) < tol) return 0.0;
+    static std::vector<double> wd;
+    if (wd.empty()) {
+        for (int mm = 2; mm <= 10; ++mm)
+            for (int nn = 1; nn < mm; ++nn) wd.push_back((double)nn / mm);
+        wd.push_back(0.7071067811865475);
+        wd.push_back(0.8660254037844386);
+        wd.push_back(1.0);
+    }
+    for (double w : wd) {
+        if (std::fabs(x - w) < tol) return w;
+        if (std::fabs(x + w) < tol) return -w;
+    }
+    return x;
+}
+
+}  // namespace
+
+struct tdg_ctx {
+    int device = 0;
+    int n_sm = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // host copy of the problem
+    int na = 0, n = 0, nop = 0, N = 0, nirr = 0;
+    int grid[3] = {0, 0, 0};
+    double latvec[9], reclat[9], inv_reclat[9], volume = 0;
+    std::vector<double> disorder, op_cart, omega, vel, irr_weight;
+    std::vector<int32_t> op_recfrac, full_irr, full_op, irr_full, irr_nop, irr_ops, degen, degen_mode;
+    int n_fc3 = 0, n_fc4 = 0;
+    // device copies
+    DevBuf<int32_t> rot, d_irr_full, d_full_irr, d_irr_nop, d_irr_ops;
+    DevBuf<double> d_omega, d_vel, d_be, d_sigsq, d_disorder;
+    DevBuf<double2> d_egv;
+    DevBuf<float2> d_egv32;
+    DevBuf<int32_t> fc3_blk, fc3_lv, fc4_blk, fc4_lv;
+    DevBuf<double> fc3_mwm, fc4_mwm;
+    DevBuf<float> fc3_mwm32, fc4_mwm32;
+    DevBuf<double2> tw;
+    DevBuf<float2> tw32;
+    int L = 1, lmul[3] = {1, 1, 1};
+    // scattering state
+    int n_row = 0;
+    std::vector<int32_t> row_q1, row_b1;
+    DevBuf<int32_t> d_row_q1, d_row_b1, d_rowidx;
+    DevBuf<double> d_w3, d_w4, d_gamma, d_xi, d_od;
+    DevBuf<int32_t> d_status;
+    bool have_scattering = false;
+    std::vector<double> linewidth, qs, F0, Fn;  // irr-point arrays
+    // BTE buffers
+    DevBuf<double> d_fbb, d_buf;
+
+    MeshDev mesh() const {
+        MeshDev m;
+        m.n_full = N;
+        m.n_irr = nirr;
+        m.n_op = nop;
+        m.n_mode = n;
+        for (int i = 0; i < 3; ++i) m.grid[i] = grid[i];
+        m.L = L;
+        for (int i = 0; i < 3; ++i) m.lmul[i] = lmul[i];
+        m.rot = rot.p;
+        m.irr_full = d_irr_full.p;
+        m.full_irr = d_full_irr.p;
+        m.irr_nop = d_irr_nop.p;
+        m.irr_ops = d_irr_ops.p;
+        return m;
+    }
+};
+
+extern "C" int tdg_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+namespace {
+
+int check_problem(const tdg_problem *p) {
+    if (!p) return set_error(kErrParam, "null problem");
+    if (p->n_atom < 1 || p->n_mode != 3 * p->n_atom) return set_error(kErrBadDim, "n_mode must be 3*n_atom");
+    if (p->n_op < 1) return set_error(kErrSymmetry, "no symmetry operations");
+    for (int i = 0; i < 3; ++i)
+        if (p->grid[i] < 1) return set_error(kErrBadDim, "grid dimensions must be positive");
+    if ((int64_t)p->grid[0] * p->grid[1] * p->grid[2] != p->n_full)
+        return set_error(kErrBadDim, "n_full != product of the grid dimensions");
+    if (p->n_irr < 1 || p->n_irr > p->n_full) return set_error(kErrBadDim, "bad n_irr");
+    if (!p->op_cart || !p->op_recfrac || !p->full_irr || !p->full_op || !p->irr_full || !p->irr_weight ||
+        !p->irr_nop || !p->irr_ops || !p->omega || !p->egv || !p->vel || !p->degen || !p->degen_mode ||
+        !p->mass_disorder)
+        return set_error(kErrParam, "null array in problem");
+    for (int i = 0; i < p->n_irr; ++i)
+        if (p->irr_full[i] < 1 || p->irr_full[i] > p->n_full) return set_error(kErrParam, "irr_full out of range");
+    for (int i = 0; i < p->n_full; ++i) {
+        if (p->full_irr[i] < 1 || p->full_irr[i] > p->n_irr) return set_error(kErrParam, "full_irr out of range");
+        if (p->full_op[i] == 0 || std::abs(p->full_op[i]) > p->n_op)
+            return set_error(kErrParam, "full_op out of range");
+    }
+    for (int i = 0; i < p->n_irr; ++i) {
+        if (p->irr_nop[i] < 1 || p->irr_nop[i] > p->n_op) return set_error(kErrParam, "irr_nop out of range");
+        if (p->irr_nop[i] > 192) return set_error(kErrParam, "little group larger than 192 operations");
+        for (int j = 0; j < p->irr_nop[i]; ++j) {
+            const int o = p->irr_ops[(size_t)i * p->n_op + j];
+            if (o < 1 || o > p->n_op) return set_error(kErrParam, "irr_ops out of range");
+        }
+    }
+    const size_t nm = (size_t)p->n_full * p->n_mode;
+    for (size_t i = 0; i < nm; ++i) {
+        if (!std::isfinite(p->omega[i])) return set_error(kErrPhysical, "non-finite frequency");
+        if (p->degen[i] < 1 || p->degen[i] > p->n_mode) return set_error(kErrParam, "degeneracy out of range");
+        for (int j = 0; j < p->degen[i]; ++j) {
+            const int b = p->degen_mode[i * p->n_mode + j];
+            if (b < 1 || b > p->n_mode) return set_error(kErrParam, "degenmode out of range");
+        }
+    }
+    if (p->n_fc3 < 0 || p->n_fc4 < 0) return set_error(kErrParam, "negative force-constant count");
+    if (p->n_fc3 > 0 && (!p->fc3_atoms || !p->fc3_lv || !p->fc3_mwm)) return set_error(kErrParam, "null fc3 array");
+    if (p->n_fc4 > 0 && (!p->fc4_atoms || !p->fc4_lv || !p->fc4_mwm)) return set_error(kErrParam, "null fc4 array");
+    for (int t = 0; t < p->n_fc3; ++t)
+        for (int k = 0; k < 3; ++k)
+            if (p->fc3_atoms[3 * t + k] < 1 || p->fc3_atoms[3 * t + k] > p->n_atom)
+                return set_error(kErrParam, "fc3 atom index out of range");
+    for (int t = 0; t < p->n_fc4; ++t)
+        for (int k = 0; k < 4; ++k)
+            if (p->fc4_atoms[4 * t + k] < 1 || p->fc4_atoms[4 * t + k] > p->n_atom)
+                return set_error(kErrParam, "fc4 atom index out of range");
+    return kOk;
+}
+
+// Image of every mesh point under every operation, in exact integer arithmetic on the
+// grid coordinates; -1 when the rotated point is not on the mesh.
+void build_rot_table(const tdg_problem *p, int L, std::vector<int32_t> &rot) {
+    const int N = p->n_full;
+    const int *g = p->grid;
+    rot.assign((size_t)p->n_op * N, -1);
+    for (int o = 0; o < p->n_op; ++o) {
+        const int32_t *R = p->op_recfrac + 9 * o;
+        for (int q = 0; q < N; ++q) {
+            const int gi[3] = {q / (g[1] * g[2]), (q / g[2]) % g[1], q % g[2]};
+            int out[3];
+            bool ok = true;
+            for (int i = 0; i < 3 && ok; ++i) {
+                // (R q)_i = sum_j R_ij g_j / N_j = num / L
+                int64_t num = 0;
+                for (int j = 0; j < 3; ++j) num += (int64_t)R[i + 3 * j] * gi[j] * (L / g[j]);
+                const int64_t t = num * g[i];
+                if (t % L != 0) {
+                    ok = false;
+                    break;
+                }
+                int64_t v = (t / L) % g[i];
+                if (v < 0) v += g[i];
+                out[i] = (int)v;
+            }
+            if (ok) rot[(size_t)o * N + q] = (out[0] * g[1] + out[1]) * g[2] + out[2];
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
+    if (!out) return set_error(kErrParam, "tdg_create: null output");
+    *out = nullptr;
+    int st = check_problem(p);
+    if (st) return st;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return set_error(kErrDevice, "no CUDA device available: the GB300 path has no CPU fallback");
+    }
+    if (device < 0 || device >= ndev) return set_error(kErrParam, "device index out of range");
+    CUDA_TRY(cudaSetDevice(device));
+    auto *c = new tdg_ctx();
+    c->device = device;
+    auto fail = [&](int code) {
+        delete c;
+        return code;
+    };
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return fail(set_error(kErrDevice, "device query failed"));
+    if (prop.major < 10) return fail(set_error(kErrDevice, "device is not Blackwell (sm_100 family required)"));
+    c->n_sm = prop.multiProcessorCount;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess)
+        return fail(set_error(kErrDevice, "stream/event creation failed"));
+    c->na = p->n_atom;
+    c->n = p->n_mode;
+    c->nop = p->n_op;
+    c->N = p->n_full;
+    c->nirr = p->n_irr;
+    for (int i = 0; i < 3; ++i) c->grid[i] = p->grid[i];
+    std::memcpy(c->latvec, p->latvec, sizeof(c->latvec));
+    std::memcpy(c->reclat, p->reclat, sizeof(c->reclat));
+    std::memcpy(c->inv_reclat, p->inv_reclat, sizeof(c->inv_reclat));
+    c->volume = p->volume;
+    const size_t nm = (size_t)c->N * c->n;
+    c->disorder.assign(p->mass_disorder, p->mass_disorder + c->na);
+    c->op_cart.assign(p->op_cart, p->op_cart + 9 * c->nop);
+    c->op_recfrac.assign(p->op_recfrac, p->op_recfrac + 9 * c->nop);
+    c->omega.assign(p->omega, p->omega + nm);
+    c->vel.assign(p->vel, p->vel + nm * 3);
+    c->irr_weight.assign(p->irr_weight, p->irr_weight + c->nirr);
+    c->full_irr.assign(p->full_irr, p->full_irr + c->N);
+    c->full_op.assign(p->full_op, p->full_op + c->N);
+    c->irr_full.assign(p->irr_full, p->irr_full + c->nirr);
+    c->irr_nop.assign(p->irr_nop, p->irr_nop + c->nirr);
+    c->irr_ops.assign(p->irr_ops, p->irr_ops + (size_t)c->nirr * c->nop);
+    c->degen.assign(p->degen, p->degen + nm);
+    c->degen_mode.assign(p->degen_mode, p->degen_mode + nm * c->n);
+    c->n_fc3 = p->n_fc3;
+    c->n_fc4 = p->n_fc4;
+    c->L = 1;
+    for (int i = 0; i < 3; ++i) c->L = c->L / gcd_i(c->L, c->grid[i]) * c->grid[i];
+    for (int i = 0; i < 3; ++i) c->lmul[i] = c->L / c->grid[i];
+
+    cudaStream_t s = c->stream;
+    std::vector<int32_t> rot;
+    build_rot_table(p, c->L, rot);
+    std::vector<int32_t> irr_full0(c->nirr), full_irr0(c->N), irr_ops0((size_t)c->nirr * c->nop, 0);
+    for (int i = 0; i < c->nirr; ++i) irr_full0[i] = c->irr_full[i] - 1;
+    for (int i = 0; i < c->N; ++i) full_irr0[i] = c->full_irr[i] - 1;
+    for (size_t i = 0; i < irr_ops0.size(); ++i) irr_ops0[i] = c->irr_ops[i] > 0 ? c->irr_ops[i] - 1 : -1;
+    std::vector<double2> egv(nm * c->n);
+    std::vector<float2> egv32(nm * c->n);
+    for (size_t i = 0; i < egv.size(); ++i) {
+        egv[i] = make_double2(p->egv[2 * i], p->egv[2 * i + 1]);
+        egv32[i] = make_float2((float)p->egv[2 * i], (float)p->egv[2 * i + 1]);
+    }
+    // Force constants sorted by atom block (a1,a2,a3).
+    const int na = c->na;
+    std::vector<int32_t> blk_ptr3(na * na * na + 1, 0), lv3;
+    std::vector<double> mwm3;
+    std::vector<float> mwm3f;
+    {
+        std::vector<int> idx(c->n_fc3);
+        std::iota(idx.begin(), idx.end(), 0);
+        auto blk = [&](int t) {
+            const int32_t *a = p->fc3_atoms + 3 * t;
+            return ((a[0] - 1) * na + (a[1] - 1)) * na + (a[2] - 1);
+        };
+        std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return blk(x) < blk(y); });
+        for (int t : idx) {
+            blk_ptr3[blk(t) + 1]++;
+            lv3.insert(lv3.end(), p->fc3_lv + 6 * t, p->fc3_lv + 6 * t + 6);
+            for (int k = 0; k < 27; ++k) {
+                mwm3.push_back(p->fc3_mwm[27 * t + k]);
+                mwm3f.push_back((float)p->fc3_mwm[27 * t + k]);
+            }
+        }
+        for (size_t b = 1; b < blk_ptr3.size(); ++b) blk_ptr3[b] += blk_ptr3[b - 1];
+    }
+    std::vector<int32_t> blk_ptr4(na * na * na * na + 1, 0), lv4;
+    std::vector<double> mwm4;
+    std::vector<float> mwm4f;
+    {
+        std::vector<int> idx(c->n_fc4);
+        std::iota(idx.begin(), idx.end(), 0);
+        auto blk = [&](int t) {
+            const int32_t *a = p->fc4_atoms + 4 * t;
+            return (((a[0] - 1) * na + (a[1] - 1)) * na + (a[2] - 1)) * na + (a[3] - 1);
+        };
+        std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return blk(x) < blk(y); });
+        for (int t : idx) {
+            blk_ptr4[blk(t) + 1]++;
+            lv4.insert(lv4.end(), p->fc4_lv + 9 * t, p->fc4_lv + 9 * t + 9);
+            for (int k = 0; k < 81; ++k) {
+                mwm4.push_back(p->fc4_mwm[81 * t + k]);
+                mwm4f.push_back((float)p->fc4_mwm[81 * t + k]);
+            }
+        }
+        for (size_t b = 1; b < blk_ptr4.size(); ++b) blk_ptr4[b] += blk_ptr4[b - 1];
+    }
+    std::vector<double2> tw(c->L);
+    std::vector<float2> tw32(c->L);
+    for (int k = 0; k < c->L; ++k) {
+        const double ang = kTwoPi * (double)k / (double)c->L;
+        tw[k] = make_double2(std::cos(ang), -std::sin(ang));
+        tw32[k] = make_float2((float)tw[k].x, (float)tw[k].y);
+    }
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t x) {
+        if (e == cudaSuccess) e = x;
+    };
+    chk(c->rot.upload(rot.data(), rot.size(), s));
+    chk(c->d_irr_full.upload(irr_full0.data(), irr_full0.size(), s));
+    chk(c->d_full_irr.upload(full_irr0.data(), full_irr0.size(), s));
+    chk(c->d_irr_nop.upload(c->irr_nop.data(), c->irr_nop.size(), s));
+    chk(c->d_irr_ops.upload(irr_ops0.data(), irr_ops0.size(), s));
+    chk(c->d_omega.upload(c->omega.data(), c->omega.size(), s));
+    chk(c->d_vel.upload(c->vel.data(), c->vel.size(), s));
+    chk(c->d_egv.upload(egv.data(), egv.size(), s));
+    chk(c->d_egv32.upload(egv32.data(), egv32.size(), s));
+    chk(c->d_disorder.upload(c->disorder.data(), c->disorder.size(), s));
+    chk(c->fc3_blk.upload(blk_ptr3.data(), blk_ptr3.size(), s));
+    chk(c->fc3_lv.upload(lv3.data(), lv3.size(), s));
+    chk(c->fc3_mwm.upload(mwm3.data(), mwm3.size(), s));
+    chk(c->fc3_mwm32.upload(mwm3f.data(), mwm3f.size(), s));
+    chk(c->fc4_blk.upload(blk_ptr4.data(), blk_ptr4.size(), s));
+    chk(c->fc4_lv.upload(lv4.data(), lv4.size(), s));
+    chk(c->fc4_mwm.upload(mwm4.data(), mwm4.size(), s));
+    chk(c->fc4_mwm32.upload(mwm4f.data(), mwm4f.size(), s));
+    chk(c->tw.upload(tw.data(), tw.size(), s));
+    chk(c->tw32.upload(tw32.data(), tw32.size(), s));
+    chk(c->d_status.alloc(1));
+    chk(cudaStreamSynchronize(s));
+    if (e != cudaSuccess) return fail(set_error(kErrDevice, std::string("upload failed: ") + cudaGetErrorString(e)));
+    *out = c;
+    return kOk;
+}
+
+extern "C" void tdg_destroy(tdg_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+namespace {
+
+int validate_opts(const tdg_opts *o) {
+    if (!o) return set_error(kErrParam, "null options");
+    if (o->integrationtype != 1 && o->integrationtype != 2 && o->integrationtype != 6)
+        return set_error(kErrParam, "integrationtype must be 1, 2 or 6");
+    if (!(o->temperature >= 0) || !std::isfinite(o->temperature)) return set_error(kErrPhysical, "bad temperature");
+    if (o->integrationtype == 1 && !(o->sigma > 0)) return set_error(kErrParam, "sigma must be positive");
+    if (o->precision != TDG_PREC_FP64 && o->precision != TDG_PREC_MIXED)
+        return set_error(kErrParam, "precision must be TDG_PREC_FP64 or TDG_PREC_MIXED");
+    return kOk;
+}
+
+int check_list(const char *what, int n_row, const int64_t *ptr, const int32_t *l, int N) {
+    if (!ptr) return set_error(kErrParam, std::string(what) + ": missing row pointer");
+    if (ptr[0] != 0) return set_error(kErrParam, std::string(what) + ": ptr[0] must be 0");
+    for (int r = 0; r < n_row; ++r) {
+        if (ptr[r + 1] < ptr[r]) return set_error(kErrParam, std::string(what) + ": decreasing row pointer");
+        if (ptr[r + 1] == ptr[r]) return set_error(kErrParam, std::string(what) + ": empty q' sample for a row");
+    }
+    if (ptr[n_row] > 0 && !l) return set_error(kErrParam, std::string(what) + ": missing list");
+    for (int64_t i = 0; i < ptr[n_row]; ++i)
+        if (l[i] < 1 || l[i] > N) return set_error(kErrParam, std::string(what) + ": q' index out of range");
+    return kOk;
+}
+
+int read_status(tdg_ctx *c) {
+    int32_t st = 0;
+    CUDA_TRY(cudaMemcpyAsync(&st, c->d_status.p, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (st != kDevOk) return set_error(kErrDevice, "device-side index check failed (status " + std::to_string(st) + ")");
+    return kOk;
+}
+
+}  // namespace
+
+extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *ql, double *linewidth, double *qs_out,
+                              double *stats) {
+    if (!c || !ql || !linewidth) return set_error(kErrParam, "tdg_scattering: null argument");
+    int st = validate_opts(o);
+    if (st) return st;
+    CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    const int n = c->n, N = c->N, nirr = c->nirr;
+    // ---- rows: must be exactly the reference's row set, in order ----
+    std::vector<int32_t> exp_q1, exp_b1;
+    for (int q1 = 0; q1 < nirr; ++q1) {
+        const int f = c->irr_full[q1] - 1;
+        for (int b1 = 0; b1 < n; ++b1)
+            if (!(c->omega[(size_t)f * n + b1] < kFreqTol)) {
+                exp_q1.push_back(q1 + 1);
+                exp_b1.push_back(b1 + 1);
+            }
+    }
+    if (ql->n_row != (int)exp_q1.size() || !ql->row_q1 || !ql->row_b1)
+        return set_error(kErrParam, "rows do not match the (q1,b1) set with omega >= lo_freqtol");
+    for (int r = 0; r < ql->n_row; ++r)
+        if (ql->row_q1[r] != exp_q1[r] || ql->row_b1[r] != exp_b1[r])
+            return set_error(kErrParam, "rows do not match the (q1,b1) set with omega >= lo_freqtol");
+    const int nr = ql->n_row;
+    if (o->thirdorder) {
+        st = check_list("three-phonon sample", nr, ql->ptr3, ql->list3, N);
+        if (st) return st;
+        if (c->n_fc3 < 1) return set_error(kErrParam, "three-phonon scattering requested without force constants");
+        if (n > 18) return set_error(kErrParam, "this build's fused three-phonon kernel supports up to 6 atoms");
+    }
+    if (o->fourthorder) {
+        st = check_list("four-phonon sample", nr, ql->ptr4, ql->list4a, N);
+        if (st) return st;
+        st = check_list("four-phonon sample", nr, ql->ptr4, ql->list4b, N);
+        if (st) return st;
+        if (c->n_fc4 < 1) return set_error(kErrParam, "four-phonon scattering requested without force constants");
+        if (n > 18) return set_error(kErrParam, "this build's four-phonon kernel supports up to 6 atoms");
+    }
+    c->n_row = nr;
+    c->row_q1.assign(ql->row_q1, ql->row_q1 + nr);
+    c->row_b1.assign(ql->row_b1, ql->row_b1 + nr);
+
+    // ---- init block (scattering.f90:126-168) ----
+    std::vector<double> be((size_t)nirr * n, 0.0), sigsq((size_t)nirr * n, 0.0), sigavg(n, 0.0);
+    double reclat_g[9];
+    for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i) reclat_g[i + 3 * j] = c->reclat[i + 3 * j] / c->grid[j];
+    for (int q1 = 0; q1 < nirr; ++q1) {
+        const int f = c->irr_full[q1] - 1;
+        for (int b1 = 0; b1 < n; ++b1) {
+            const double om = c->omega[(size_t)f * n + b1];
+            if (om < kFreqTol) continue;
+            be[(size_t)q1 * n + b1] = o->classical ? kKbHartree * o->temperature / om : planck(o->temperature, om);
+            const double *v = &c->vel[((size_t)f * n + b1) * 3];
+            double sg = 0.0;
+            for (int j = 0; j < 3; ++j) {
+                double x = 0.0;
+                for (int i = 0; i < 3; ++i) x += std::fabs(v[i]) * reclat_g[i + 3 * j];
+                sg = std::max(sg, x * x * 0.5);
+            }
+            sigsq[(size_t)q1 * n + b1] = sg;
+            sigavg[b1] += sg * c->irr_weight[q1];
+        }
+    }
+    const double maxavg = *std::max_element(sigavg.begin(), sigavg.end());
+    for (double &x : sigsq) x += maxavg * 1e-4;
+    PhononDev ph;
+    ph.omega = c->d_omega.p;
+    ph.egv = c->d_egv.p;
+    ph.egv32 = c->d_egv32.p;
+    ph.vel = c->d_vel.p;
+    std::memcpy(ph.reclat_g, reclat_g, sizeof(reclat_g));
+    ph.sigma_fixed = o->sigma * kFreqTHzToHartree;
+    ph.thresh_sigma = maxavg * 1e-4;
+    ph.integrationtype = o->integrationtype;
+
+    std::vector<int32_t> rowidx((size_t)nirr * n, -1), rq1(nr), rb1(nr);
+    std::vector<double> w3(nr, 0.0), w4(nr, 0.0);
+    for (int r = 0; r < nr; ++r) {
+        rq1[r] = c->row_q1[r] - 1;
+        rb1[r] = c->row_b1[r] - 1;
+        rowidx[(size_t)rq1[r] * n + rb1[r]] = r;
+        if (o->thirdorder) w3[r] = 1.0 / (double)(ql->ptr3[r + 1] - ql->ptr3[r]);
+        if (o->fourthorder) {
+            const double np4 = (double)(ql->ptr4[r + 1] - ql->ptr4[r]);
+            w4[r] = 1.0 / np4;
+        }
+    }
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t x) {
+        if (e == cudaSuccess) e = x;
+    };
+    chk(c->d_be.upload(be.data(), be.size(), s));
+    chk(c->d_sigsq.upload(sigsq.data(), sigsq.size(), s));
+    chk(c->d_rowidx.upload(rowidx.data(), rowidx.size(), s));
+    chk(c->d_row_q1.upload(rq1.data(), rq1.size(), s));
+    chk(c->d_row_b1.upload(rb1.data(), rb1.size(), s));
+    chk(c->d_w3.upload(w3.data(), w3.size(), s));
+    chk(c->d_w4.upload(w4.data(), w4.size(), s));
+    const int64_t ld = (int64_t)N * n;
+    chk(c->d_xi.alloc((size_t)nr * ld));
+    chk(c->d_gamma.alloc(nr));
+    if (e != cudaSuccess) return set_error(kErrDevice, std::string("allocation failed: ") + cudaGetErrorString(e));
+    ph.be = c->d_be.p;
+    ph.sigsq = c->d_sigsq.p;
+    RowsDev rows;
+    rows.n_row = nr;
+    rows.rowidx = c->d_rowidx.p;
+    rows.weight3 = c->d_w3.p;
+    rows.weight4 = c->d_w4.p;
+    const MeshDev mesh = c->mesh();
+
+    CUDA_TRY(cudaEventRecord(c->ev0, s));
+    CUDA_TRY(cudaMemsetAsync(c->d_xi.p, 0, sizeof(double) * (size_t)nr * ld, s));
+    CUDA_TRY(cudaMemsetAsync(c->d_gamma.p, 0, sizeof(double) * nr, s));
+    CUDA_TRY(cudaMemsetAsync(c->d_status.p, 0, sizeof(int32_t), s));
+    double n_trip_total = 0, n_quart_total = 0, n_cand_total = 0;
+
+    if (o->isotope) {
+        CUDA_TRY(launch_isotope(mesh, ph, rows, c->d_row_q1.p, c->d_row_b1.p, c->d_disorder.p, c->na, c->d_gamma.p,
+                                c->d_xi.p, s));
+    }
+    if (o->thirdorder || o->fourthorder) {
+        CUDA_TRY(c->d_od.alloc((size_t)nr * ld));
+    }
+    if (o->thirdorder) {
+        // Candidates: per q1 the union of its rows' samples, with the set of rows as a mask.
+        std::vector<int2> cand;
+        std::vector<uint32_t> masks;
+        std::vector<uint32_t> mark((size_t)N * 4, 0u);
+        std::vector<int32_t> touched;
+        int r0 = 0;
+        for (int q1 = 0; q1 < nirr; ++q1) {
+            int r1 = r0;
+            while (r1 < nr && rq1[r1] == q1) ++r1;
+            touched.clear();
+            for (int r = r0; r < r1; ++r) {
+                const int b1 = rb1[r];
+                for (int64_t i = ql->ptr3[r]; i < ql->ptr3[r + 1]; ++i) {
+                    const int q2 = ql->list3[i] - 1;
+                    uint32_t *mk = &mark[(size_t)q2 * 4];
+                    if (!(mk[0] | mk[1] | mk[2] | mk[3])) touched.push_back(q2);
+                    mk[b1 >> 5] |= 1u << (b1 & 31);
+                }
+            }
+            std::sort(touched.begin(), touched.end());
+            for (int q2 : touched) {
+                cand.push_back(make_int2(q1, q2));
+                uint32_t *mk = &mark[(size_t)q2 * 4];
+                masks.insert(masks.end(), mk, mk + 4);
+                mk[0] = mk[1] = mk[2] = mk[3] = 0u;
+            }
+            r0 = r1;
+        }
+        const int32_t nc = (int32_t)cand.size();
+        n_cand_total += nc;
+        DevBuf<int2> d_cand;
+        DevBuf<uint32_t> d_mask;
+        DevBuf<int32_t> d_nt, d_nrd, d_toff, d_roff, d_tmp;
+        chk(d_cand.upload(cand.data(), cand.size(), s));
+        chk(d_mask.upload(masks.data(), masks.size(), s));
+        chk(d_nt.alloc(nc + 1));
+        chk(d_nrd.alloc(nc + 1));
+        chk(d_toff.alloc(nc + 1));
+        chk(d_roff.alloc(nc + 1));
+        chk(d_tmp.alloc(exclusive_scan_tmp_elems(nc)));
+        if (e != cudaSuccess) return set_error(kErrDevice, std::string("allocation failed: ") + cudaGetErrorString(e));
+        CUDA_TRY(launch_triplet_count(mesh, d_cand.p, nc, d_nt.p, d_nrd.p, c->d_status.p, s));
+        CUDA_TRY(exclusive_scan_i32(d_nt.p, d_toff.p, nc, d_tmp.p, s));
+        CUDA_TRY(exclusive_scan_i32(d_nrd.p, d_roff.p, nc, d_tmp.p, s));
+        int32_t tot[2] = {0, 0};
+        CUDA_TRY(cudaMemcpyAsync(&tot[0], d_toff.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(cudaMemcpyAsync(&tot[1], d_roff.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        st = read_status(c);
+        if (st) return st;
+        const int32_t ntrip = tot[0], nred = tot[1];
+        n_trip_total += ntrip;
+        DevBuf<TripletRec> d_trip;
+        DevBuf<int2> d_red;
+        chk(d_trip.alloc(ntrip));
+        chk(d_red.alloc(nred));
+        if (e != cudaSuccess) return set_error(kErrDevice, std::string("allocation failed: ") + cudaGetErrorString(e));
+        CUDA_TRY(launch_triplet_fill(mesh, d_cand.p, nc, d_toff.p, d_roff.p, d_trip.p, d_red.p, s));
+        CUDA_TRY(cudaMemsetAsync(c->d_od.p, 0, sizeof(double) * (size_t)nr * ld, s));
+        ThreePhArgs a;
+        a.mesh = mesh;
+        a.ph = ph;
+        a.rows = rows;
+        a.fc.n = c->n_fc3;
+        a.fc.n_atom = c->na;
+        a.fc.blk_ptr = c->fc3_blk.p;
+        a.fc.lv = c->fc3_lv.p;
+        a.fc.mwm = c->fc3_mwm.p;
+        a.fc.mwm32 = c->fc3_mwm32.p;
+        a.fc.twiddle = c->tw.p;
+        a.fc.twiddle32 = c->tw32.p;
+        a.trip = d_trip.p;
+        a.n_trip = ntrip;
+        a.red = d_red.p;
+        a.cand_mask = d_mask.p;
+        a.gamma = c->d_gamma.p;
+        a.od = c->d_od.p;
+        a.status = c->d_status.p;
+        CUDA_TRY(launch_threephonon(a, o->precision, c->n_sm, s));
+        DevBuf<int64_t> d_ptr;
+        DevBuf<int32_t> d_list;
+        chk(d_ptr.upload(ql->ptr3, nr + 1, s));
+        chk(d_list.upload(ql->list3, ql->ptr3[nr], s));
+        if (e != cudaSuccess) return set_error(kErrDevice, std::string("upload failed: ") + cudaGetErrorString(e));
+        CUDA_TRY(launch_sym_distribute(mesh, nr, c->d_row_q1.p, d_ptr.p, d_list.p, c->d_od.p, c->d_xi.p, s));
+        CUDA_TRY(cudaStreamSynchronize(s));  // scoped buffers are released below
+    }
+    if (o->fourthorder) {
+        return set_error(kErrParam, "four-phonon scattering is not available in this build");
+    }
+    // ---- gamma to host: boundary, degeneracy averaging (scattering.f90:244-292) ----
+    std::vector<double> gamma(nr);
+    CUDA_TRY(cudaMemcpyAsync(gamma.data(), c->d_gamma.p, sizeof(double) * nr, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(launch_sym_scatmat(mesh, nr, c->d_row_q1.p, c->d_xi.p, s));
+    CUDA_TRY(cudaEventRecord(c->ev1, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    st = read_status(c);
+    if (st) return st;
+    float ms = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+
+    std::vector<double> buf_lw((size_t)nirr * n, 0.0);
+    for (int r = 0; r < nr; ++r) {
+        double b = gamma[r];
+        if (o->mfp_max > 0.0) {
+            const int f = c->irr_full[rq1[r]] - 1;
+            const double *v = &c->vel[((size_t)f * n + rb1[r]) * 3];
+            const double vn = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+            if (vn > kGroupVelTol) b += vn / o->mfp_max;
+        }
+        buf_lw[(size_t)rq1[r] * n + rb1[r]] = b;
+    }
+    c->linewidth.assign((size_t)nirr * n, 0.0);
+    c->qs.assign((size_t)nirr * n, 0.0);
+    c->F0.assign((size_t)nirr * n * 3, 0.0);
+    c->Fn.assign((size_t)nirr * n * 3, 0.0);
+    for (int q1 = 0; q1 < nirr; ++q1) {
+        const int f = c->irr_full[q1] - 1;
+        for (int b1 = 0; b1 < n; ++b1) {
+            if (c->omega[(size_t)f * n + b1] < kFreqTol) continue;
+            const int dg = c->degen[(size_t)f * n + b1];
+            const int32_t *dm = &c->degen_mode[((size_t)f * n + b1) * n];
+            double f0 = 0.0;
+            for (int j = 0; j < dg; ++j) f0 += buf_lw[(size_t)q1 * n + dm[j] - 1];
+            f0 /= (double)dg;
+            for (int j = 0; j < dg; ++j) buf_lw[(size_t)q1 * n + dm[j] - 1] = f0;
+            const double lw = buf_lw[(size_t)q1 * n + b1];
+            c->linewidth[(size_t)q1 * n + b1] = lw;
+            c->qs[(size_t)q1 * n + b1] = 2.0 * lw;
+            if (lw > kFreqTol) {
+                const double *v = &c->vel[((size_t)f * n + b1) * 3];
+                for (int d = 0; d < 3; ++d) {
+                    const double mfp = v[d] / c->qs[(size_t)q1 * n + b1];
+                    c->F0[((size_t)q1 * n + b1) * 3 + d] = mfp;
+                    c->Fn[((size_t)q1 * n + b1) * 3 + d] = mfp;
+                }
+            }
+        }
+    }
+    std::memcpy(linewidth, c->linewidth.data(), sizeof(double) * c->linewidth.size());
+    if (qs_out) std::memcpy(qs_out, c->qs.data(), sizeof(double) * c->qs.size());
+    if (stats) {
+        stats[0] = n_trip_total;
+        stats[1] = n_quart_total;
+        stats[2] = ms;
+        stats[3] = n_cand_total;
+    }
+    c->d_od.release();
+    c->have_scattering = true;
+    return kOk;
+}
+
+extern "C" int tdg_get_xi(tdg_ctx *c, double *xi) {
+    if (!c || !xi) return set_error(kErrParam, "tdg_get_xi: null argument");
+    if (!c->have_scattering) return set_error(kErrParam, "tdg_get_xi: call tdg_scattering first");
+    CUDA_TRY(cudaSetDevice(c->device));
+    const size_t cnt = (size_t)c->n_row * c->N * c->n;
+    CUDA_TRY(cudaMemcpyAsync(xi, c->d_xi.p, sizeof(double) * cnt, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return kOk;
+}
+
+extern "C" int tdg_triplets(tdg_ctx *c, int32_t q1, const int32_t *sample, int64_t n, int32_t *out, int64_t cap,
+                            int64_t *written) {
+    if (!c || !sample || !out || !written) return set_error(kErrParam, "tdg_triplets: null argument");
+    if (q1 < 1 || q1 > c->nirr) return set_error(kErrParam, "tdg_triplets: q1 out of range");
+    if (n < 0 || n > (int64_t)1 << 30) return set_error(kErrParam, "tdg_triplets: bad sample length");
+    for (int64_t i = 0; i < n; ++i)
+        if (sample[i] < 1 || sample[i] > c->N) return set_error(kErrParam, "tdg_triplets: q' index out of range");
+    CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    const int32_t nc = (int32_t)n;
+    std::vector<int2> cand(nc);
+    for (int32_t i = 0; i < nc; ++i) cand[i] = make_int2(q1 - 1, sample[i] - 1);
+    DevBuf<int2> d_cand;
+    DevBuf<int32_t> d_nt, d_nrd, d_toff, d_roff, d_tmp;
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t x) {
+        if (e == cudaSuccess) e = x;
+    };
+    chk(d_cand.upload(cand.data(), cand.size(), s));
+    chk(d_nt.alloc(nc + 1));
+    chk(d_nrd.alloc(nc + 1));
+    chk(d_toff.alloc(nc + 1));
+    chk(d_roff.alloc(nc + 1));
+    chk(d_tmp.alloc(exclusive_scan_tmp_elems(nc)));
+    if (e != cudaSuccess) return set_error(kErrDevice, std::string("allocation failed: ") + cudaGetErrorString(e));
+    const MeshDev mesh = c->mesh();
+    CUDA_TRY(cudaMemsetAsync(c->d_status.p, 0, sizeof(int32_t), s));
+    CUDA_TRY(launch_triplet_count(mesh, d_cand.p, nc, d_nt.p, d_nrd.p, c->d_status.p, s));
+    CUDA_TRY(exclusive_scan_i32(d_nt.p, d_toff.p, nc, d_tmp.p, s));
+    CUDA_TRY(exclusive_scan_i32(d_nrd.p, d_roff.p, nc, d_tmp.p, s));
+    int32_t tot[2] = {0, 0};
+    CUDA_TRY(cudaMemcpyAsync(&tot[0], d_toff.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaMemcpyAsync(&tot[1], d_roff.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    int st = read_status(c);
+    if (st) return st;
+    DevBuf<TripletRec> d_trip;
+    DevBuf<int2> d_red;
+    chk(d_trip.alloc(tot[0]));
+    chk(d_red.alloc(tot[1]));
+    if (e != cudaSuccess) return set_error(kErrDevice, std::string("allocation failed: ") + cudaGetErrorString(e));
+    CUDA_TRY(launch_triplet_fill(mesh, d_cand.p, nc, d_toff.p, d_roff.p, d_trip.p, d_red.p, s));
+    std::vector<TripletRec> trip(tot[0]);
+    std::vector<int2> red(tot[1]);
+    if (tot[0] > 0)
+        CUDA_TRY(cudaMemcpyAsync(trip.data(), d_trip.p, sizeof(TripletRec) * tot[0], cudaMemcpyDeviceToHost, s));
+    if (tot[1] > 0) CUDA_TRY(cudaMemcpyAsync(red.data(), d_red.p, sizeof(int2) * tot[1], cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    int64_t w = 0;
+    for (const auto &t : trip) {
+        if (w + 3 + 2 * (int64_t)t.red_cnt > cap) return set_error(kErrParam, "tdg_triplets: output capacity too small");
+        out[w++] = t.q2 + 1;
+        out[w++] = t.q3 + 1;
+        out[w++] = t.red_cnt;
+        for (int k = 0; k < t.red_cnt; ++k) {
+            out[w++] = red[t.red_off + k].x + 1;
+            out[w++] = red[t.red_off + k].y + 1;
+        }
+    }
+    *written = w;
+    return kOk;
+}
+
+namespace {
+
+// op%m applied to a vector, with an optional sign (time reversal).
+inline void rotate(const double *m, const double *v, double *out, double sg = 1.0) {
+    for (int i = 0; i < 3; ++i) out[i] = sg * (m[i] * v[0] + m[i + 3] * v[1] + m[i + 6] * v[2]);
+}
+
+// get_kappa (kappa.f90:28-75).
+void get_kappa(const tdg_ctx *c, const std::vector<double> &Fn, double T, bool classical, double *kappa) {
+    const int n = c->n;
+    for (int i = 0; i < 9; ++i) kappa[i] = 0.0;
+    for (int q1 = 0; q1 < c->nirr; ++q1) {
+        const int f = c->irr_full[q1] - 1;
+        for (int b1 = 0; b1 < n; ++b1) {
+            const double om1 = c->omega[(size_t)f * n + b1];
+            if (om1 < kFreqTol) continue;
+            const double cv = classical ? kKbHartree : harmonic_oscillator_cv(T, om1);
+            double v2[9] = {0};
+            for (int j = 0; j < c->nop; ++j) {
+                double v0[3], v1[3];
+                rotate(&c->op_cart[9 * j], &Fn[((size_t)q1 * n + b1) * 3], v0);
+                rotate(&c->op_cart[9 * j], &c->vel[((size_t)f * n + b1) * 3], v1);
+                for (int x = 0; x < 3; ++x)
+                    for (int y = 0; y < 3; ++y) v2[x + 3 * y] += v0[x] * v1[y] / c->nop;
+            }
+            for (int k = 0; k < 9; ++k) kappa[k] += cv * v2[k] / c->volume * c->irr_weight[q1];
+        }
+    }
+    double tol = 0.0;
+    for (int k = 0; k < 9; ++k) tol += std::fabs(kappa[k]);
+    tol *= 1e-6;
+    for (int k = 0; k < 9; ++k) kappa[k] = lo_chop(kappa[k], tol);
+}
+
+// symmetrize_kappa (kappa.f90:308-324): average of R kappa R^T over the operations.
+void symmetrize_kappa(const tdg_ctx *c, double *kappa) {
+    double tmp[9] = {0};
+    for (int o = 0; o < c->nop; ++o) {
+        const double *m = &c->op_cart[9 * o];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                double s = 0.0;
+                for (int k = 0; k < 3; ++k)
+                    for (int l = 0; l < 3; ++l) s += m[i + 3 * k] * kappa[k + 3 * l] * m[j + 3 * l];
+                tmp[i + 3 * j] += s;
+            }
+    }
+    double tol = 0.0;
+    for (int k = 0; k < 9; ++k) {
+        kappa[k] = tmp[k] / c->nop;
+        tol += std::fabs(kappa[k]);
+    }
+    tol *= 1e-6;
+    for (int k = 0; k < 9; ++k) kappa[k] = lo_chop(kappa[k], tol);
+}
+
+}  // namespace
+
+extern "C" int tdg_kappa(tdg_ctx *c, const tdg_opts *o, int32_t maxiter, double tol, double *kappa_sma,
+                         double *kappa_iter, double *fn_out, int32_t *n_iter) {
+    if (!c || !kappa_sma || !kappa_iter) return set_error(kErrParam, "tdg_kappa: null argument");
+    int st = validate_opts(o);
+    if (st) return st;
+    if (!c->have_scattering) return set_error(kErrParam, "tdg_kappa: call tdg_scattering first");
+    if (maxiter < 0) return set_error(kErrParam, "tdg_kappa: negative iteration count");
+    CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    const int n = c->n, N = c->N, nirr = c->nirr, nr = c->n_row;
+    const bool classical = o->classical != 0;
+    const double T = o->temperature;
+    if (T < kTemperatureTol) {
+        for (int i = 0; i < 9; ++i) kappa_sma[i] = kappa_iter[i] = 0.0;
+        if (n_iter) *n_iter = 0;
+        return kOk;
+    }
+    // Every call starts from Fn = F0, the state sr%generate leaves (scattering.f90:288-289).
+    std::vector<double> Fn = c->F0;
+    get_kappa(c, Fn, T, classical, kappa_sma);
+    int iters = 0;
+    if (maxiter > 0) {
+        const int64_t ncol = (int64_t)N * n;
+        CUDA_TRY(c->d_fbb.alloc((size_t)ncol * 3));
+        CUDA_TRY(c->d_buf.alloc((size_t)nr * 3));
+        std::vector<double> Fbb((size_t)ncol * 3), buf((size_t)nr * 3), Fnb((size_t)nirr * n * 3);
+        std::vector<double> scf(maxiter, 0.0);
+        double mixing = 0.95;
+        double kap[9];
+        for (int iter = 1; iter <= maxiter; ++iter) {
+            iters = iter;
+            // foldout (kappa.f90:382-404)
+            for (int iq = 0; iq < N; ++iq) {
+                const int iop = c->full_op[iq], jq = c->full_irr[iq] - 1;
+                const double *m = &c->op_cart[9 * (std::abs(iop) - 1)];
+                for (int b1 = 0; b1 < n; ++b1)
+                    rotate(m, &Fn[((size_t)jq * n + b1) * 3], &Fbb[((size_t)iq * n + b1) * 3], iop > 0 ? 1.0 : -1.0);
+            }
+            CUDA_TRY(cudaMemcpyAsync(c->d_fbb.p, Fbb.data(), sizeof(double) * Fbb.size(), cudaMemcpyHostToDevice, s));
+            CUDA_TRY(launch_xi_gemv(c->d_xi.p, nr, ncol, c->d_fbb.p, c->d_buf.p, c->n_sm, s));
+            CUDA_TRY(cudaMemcpyAsync(buf.data(), c->d_buf.p, sizeof(double) * buf.size(), cudaMemcpyDeviceToHost, s));
+            CUDA_TRY(cudaStreamSynchronize(s));
+            // applyXi (kappa.f90:407-426)
+            std::fill(Fnb.begin(), Fnb.end(), 0.0);
+            for (int r = 0; r < nr; ++r) {
+                const int q1 = c->row_q1[r] - 1, b1 = c->row_b1[r] - 1;
+                const double q = c->qs[(size_t)q1 * n + b1];
+                for (int d = 0; d < 3; ++d)
+                    Fnb[((size_t)q1 * n + b1) * 3 + d] = q < kFreqTol ? 0.0 : -buf[(size_t)r * 3 + d] / q;
+            }
+            // distributeF (kappa.f90:429-448), in place as in the reference
+            for (int q1 = 0; q1 < nirr; ++q1) {
+                const int f = c->irr_full[q1] - 1;
+                for (int b1 = 0; b1 < n; ++b1) {
+                    const int dg = c->degen[(size_t)f * n + b1];
+                    const int32_t *dm = &c->degen_mode[((size_t)f * n + b1) * n];
+                    double v0[3] = {0, 0, 0};
+                    for (int j = 0; j < dg; ++j)
+                        for (int d = 0; d < 3; ++d) v0[d] += Fnb[((size_t)q1 * n + dm[j] - 1) * 3 + d];
+                    for (int d = 0; d < 3; ++d) v0[d] /= (double)dg;
+                    for (int j = 0; j < dg; ++j)
+                        for (int d = 0; d < 3; ++d) Fnb[((size_t)q1 * n + dm[j] - 1) * 3 + d] = v0[d];
+                    for (int d = 0; d < 3; ++d)
+                        Fnb[((size_t)q1 * n + b1) * 3 + d] =
+                            c->F0[((size_t)q1 * n + b1) * 3 + d] + Fnb[((size_t)q1 * n + b1) * 3 + d];
+                }
+            }
+            // addandcheck (kappa.f90:451-490)
+            double g0 = 0.0;
+            for (int q = 0; q < nirr; ++q)
+                for (int j = 0; j < n; ++j) {
+                    double *fn = &Fn[((size_t)q * n + j) * 3];
+                    const double *fb = &Fnb[((size_t)q * n + j) * 3];
+                    double g1 = 0.0, g2 = 0.0;
+                    for (int d = 0; d < 3; ++d) {
+                        g1 += (fn[d] - fb[d]) * (fn[d] - fb[d]);
+                        g2 += fn[d] * fn[d];
+                    }
+                    if (g2 > kSqTol) g0 += g1 / g2;
+                    for (int d = 0; d < 3; ++d) fn[d] = fn[d] * (1.0 - mixing) + mixing * fb[d];
+                }
+            scf[iter - 1] = g0 / nirr / n;
+            get_kappa(c, Fn, T, classical, kap);
+            if (iter >= 3) {
+                const double g = scf[iter - 3] + scf[iter - 2] + scf[iter - 1];
+                if (g < tol) break;
+            }
+            if (iter > 15 && mixing > 0.50) mixing *= 0.98;
+        }
+    }
+    get_kappa(c, Fn, T, classical, kappa_iter);
+    symmetrize_kappa(c, kappa_iter);
+    symmetrize_kappa(c, kappa_sma);
+    c->Fn = Fn;
+    if (fn_out) std::memcpy(fn_out, Fn.data(), sizeof(double) * Fn.size());
+    if (n_iter) *n_iter = iters;
+    return kOk;
+}

@@ -1,0 +1,147 @@
+// Internal device-side declarations shared by the kernels and the C-ABI layer.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace tdg {
+
+// Work item of the three-phonon kernel: one accepted irreducible q-triplet.
+struct TripletRec {
+    int32_t q1;       // irreducible index of q1 (0-based)
+    int32_t q2, q3;   // full-mesh indices (0-based)
+    int32_t cand;     // candidate index (for the row mask)
+    int32_t red_off;  // first equivalent triplet in the red list
+    int32_t red_cnt;  // number of equivalent triplets (size(red_triplet,2))
+};
+
+// Work item of the four-phonon kernel: one accepted irreducible q-quartet.
+struct QuartetRec {
+    int32_t q1, q2, q3, q4;
+    int32_t cand;
+    int32_t red_off, red_cnt;
+    int32_t pad;
+};
+
+// Mesh description shared by the kernels.
+struct MeshDev {
+    int32_t n_full, n_irr, n_op, n_mode;
+    int32_t grid[3];
+    int32_t L;          // lcm of the grid dimensions
+    int32_t lmul[3];    // L / grid[d]
+    const int32_t *rot;      // [n_op * n_full] image of each point, -1 when off grid
+    const int32_t *irr_full; // [n_irr] 0-based
+    const int32_t *full_irr; // [n_full] 0-based
+    const int32_t *irr_nop;  // [n_irr]
+    const int32_t *irr_ops;  // [n_irr * n_op] 0-based operation indices
+};
+
+// Phonon/occupation data on the device.
+struct PhononDev {
+    const double *omega;     // [n_full*n]
+    const double2 *egv;      // [n_full*n*n], (q, b, r)
+    const float2 *egv32;     // same in FP32 (mixed precision)
+    const double *vel;       // [n_full*n*3]
+    const double *be;        // [n_irr*n]
+    const double *sigsq;     // [n_irr*n]
+    double reclat_g[9];      // sr%reclat: reciprocal lattice / grid, column-major
+    double sigma_fixed;      // integrationtype 1, Hartree
+    double thresh_sigma;     // integrationtype 6
+    int32_t integrationtype;
+};
+
+// Rows of the scattering matrix.
+struct RowsDev {
+    int32_t n_row;
+    const int32_t *rowidx;    // [n_irr*n] row of (q1,b1), -1 when absent
+    const double *weight3;    // [n_row] 1/len of the row's three-phonon sample
+    const double *weight4;    // [n_row] 1/len of the row's four-phonon sample
+};
+
+struct Fc3Dev {
+    int32_t n;                // number of force-constant triplets
+    int32_t n_atom;
+    const int32_t *blk_ptr;   // [n_atom^3 + 1] triplets sorted by atom block (a1,a2,a3)
+    const int32_t *lv;        // [n*6] integer lattice vectors lv2, lv3
+    const double *mwm;        // [n*27]
+    const float *mwm32;       // [n*27]
+    const double2 *twiddle;   // [L] exp(-2 pi i K / L)
+    const float2 *twiddle32;
+};
+
+struct Fc4Dev {
+    int32_t n;
+    int32_t n_atom;
+    const int32_t *blk_ptr;   // [n_atom^4 + 1]
+    const int32_t *lv;        // [n*9]
+    const double *mwm;        // [n*81]
+    const float *mwm32;
+};
+
+// Device status word: kernels record the first failed check here.
+enum DevStatus : int32_t { kDevOk = 0, kDevBadIndex = 1, kDevOverflow = 2 };
+
+// ---- launch wrappers (each returns cudaError_t of the launch) ----
+// K1: count/fill passes of the irreducible-triplet enumeration.
+cudaError_t launch_triplet_count(const MeshDev &m, const int2 *cand, int32_t n_cand, int32_t *n_trip,
+                                 int32_t *n_red, int32_t *status, cudaStream_t s);
+cudaError_t launch_triplet_fill(const MeshDev &m, const int2 *cand, int32_t n_cand, const int32_t *trip_off,
+                                const int32_t *red_off, TripletRec *trip, int2 *red, cudaStream_t s);
+cudaError_t launch_quartet_count(const MeshDev &m, const int4 *cand, int32_t n_cand, int32_t *n_quart,
+                                 int32_t *n_red, int32_t *status, cudaStream_t s);
+cudaError_t launch_quartet_fill(const MeshDev &m, const int4 *cand, int32_t n_cand, const int32_t *q_off,
+                                const int32_t *red_off, QuartetRec *quart, int4 *red, cudaStream_t s);
+// Exclusive scan of int32 (n <= 2^31), result in out; total in out[n].
+cudaError_t exclusive_scan_i32(const int32_t *in, int32_t *out, int32_t n, int32_t *tmp, cudaStream_t s);
+size_t exclusive_scan_tmp_elems(int32_t n);
+
+// K2+K3+K4: fused pretransform, contraction and delta/Bose accumulation.
+struct ThreePhArgs {
+    MeshDev mesh;
+    PhononDev ph;
+    RowsDev rows;
+    Fc3Dev fc;
+    const TripletRec *trip;
+    int32_t n_trip;
+    const int2 *red;
+    const uint32_t *cand_mask;  // [n_cand*4] bit b1 set when row (q1,b1) samples q2
+    double *gamma;              // [n_row]
+    double *od;                 // [n_row * n_full*n]
+    int32_t *status;
+};
+cudaError_t launch_threephonon(const ThreePhArgs &a, int precision, int n_sm, cudaStream_t s);
+size_t threephonon_smem_bytes(int n, int precision, int n_fc);
+
+struct FourPhArgs {
+    MeshDev mesh;
+    PhononDev ph;
+    RowsDev rows;
+    Fc4Dev fc;
+    const double2 *twiddle;
+    const float2 *twiddle32;
+    const QuartetRec *quart;
+    int32_t n_quart;
+    const int4 *red;
+    const uint32_t *cand_mask;
+    double *gamma;
+    double *od;
+    int32_t *status;
+};
+cudaError_t launch_fourphonon(const FourPhArgs &a, int precision, int n_sm, cudaStream_t s);
+
+// Isotope scattering (scattering_isotope.f90): adds into gamma and xi.
+cudaError_t launch_isotope(const MeshDev &m, const PhononDev &ph, const RowsDev &rows, const int32_t *row_q1,
+                           const int32_t *row_b1, const double *disorder, int32_t n_atom, double *gamma,
+                           double *xi, cudaStream_t s);
+
+// K5a: symmetrize_and_distribute of one order, od -> xi (scattering_threephonon.f90:143-205).
+cudaError_t launch_sym_distribute(const MeshDev &m, int32_t n_row, const int32_t *row_q1, const int64_t *ptr,
+                                  const int32_t *list, double *od, double *xi, cudaStream_t s);
+// K5b: symmetrize_scatmat (scattering.f90:296-357).
+cudaError_t launch_sym_scatmat(const MeshDev &m, int32_t n_row, const int32_t *row_q1, double *xi,
+                               cudaStream_t s);
+// K8: buf[r*3+a] = sum_j xi[r, j] * fbb[j*3 + a].
+cudaError_t launch_xi_gemv(const double *xi, int32_t n_row, int64_t n_col, const double *fbb, double *buf,
+                           int n_sm, cudaStream_t s);
+
+}  // namespace tdg

@@ -1,0 +1,350 @@
+"""Host-side mirror of TDEP's scattering interface over the GB300 C-ABI.
+
+Names follow the reference:
+  Problem            the flattened (uc, qp, dr, fct, fcf) that sr%generate consumes
+  Options            the hot-path subset of lo_opts (src/thermal_conductivity/options.f90)
+  QLists             rows (q1, b1) and their Monte-Carlo q' samples
+  ScatteringRates    lo_scattering_rates (scattering.f90:34-55): generate(), Xi, and the
+                     kappa solves of kappa.f90 (get_kappa / iterative_solution)
+Errors raise TdgError with the reference's exit-code meaning (konstanter.f90:160-172).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+
+from . import _native as N
+
+# Unit conversions used at the interface (src/libolle/konstanter.f90).
+HARTREE_TO_EV = 27.21138602
+BOHR_TO_M = 0.52917721067e-10
+EV_TO_JOULE = 1.6021766208e-19
+HBAR_EV = 6.582119514e-16
+KAPPA_AU_TO_SI = (HARTREE_TO_EV * EV_TO_JOULE) / (HBAR_EV * EV_TO_JOULE / (HARTREE_TO_EV * EV_TO_JOULE)) / BOHR_TO_M
+FREQ_HARTREE_TO_THZ = 1e-12 / 6.283185307179586 / (HBAR_EV / HARTREE_TO_EV)
+LO_FREQTOL = 1e-9
+
+_FIELDS_F64 = {
+    "mass_disorder": ("n_atom",),
+    "op_cart": ("n_op", 9),
+    "q_full": ("n_full", 3),
+    "irr_weight": ("n_irr",),
+    "omega": ("n_full", "n_mode"),
+    "egv": ("n_full", "n_mode", "n_mode", 2),
+    "vel": ("n_full", "n_mode", 3),
+    "fc3_lvcart": ("n_fc3", 6),
+    "fc3_mwm": ("n_fc3", 27),
+    "fc4_lvcart": ("n_fc4", 9),
+    "fc4_mwm": ("n_fc4", 81),
+}
+_FIELDS_I32 = {
+    "op_recfrac": ("n_op", 9),
+    "full_irr": ("n_full",),
+    "full_op": ("n_full",),
+    "irr_full": ("n_irr",),
+    "irr_nop": ("n_irr",),
+    "irr_ops": ("n_irr", "n_op"),
+    "degen": ("n_full", "n_mode"),
+    "degen_mode": ("n_full", "n_mode", "n_mode"),
+    "fc3_atoms": ("n_fc3", 3),
+    "fc3_lv": ("n_fc3", 6),
+    "fc4_atoms": ("n_fc4", 4),
+    "fc4_lv": ("n_fc4", 9),
+}
+_SCALARS = ("n_atom", "n_mode", "n_op", "n_full", "n_irr", "n_fc3", "n_fc4")
+
+
+class Problem:
+    """Numpy-owned tdg_problem. Arrays use the C-ABI layouts (see include/tdep_gb300.h)."""
+
+    def __init__(self, **kw):
+        for k in _SCALARS:
+            setattr(self, k, int(kw[k]))
+        for k in ("latvec", "reclat", "inv_reclat"):
+            setattr(self, k, np.ascontiguousarray(kw[k], dtype=np.float64).reshape(9))
+        self.volume = float(kw["volume"])
+        self.grid = np.ascontiguousarray(kw["grid"], dtype=np.int32).reshape(3)
+        for k, shp in _FIELDS_F64.items():
+            setattr(self, k, np.ascontiguousarray(kw[k], dtype=np.float64).reshape(self._shape(shp)))
+        for k, shp in _FIELDS_I32.items():
+            setattr(self, k, np.ascontiguousarray(kw[k], dtype=np.int32).reshape(self._shape(shp)))
+        self._struct = None
+
+    def _shape(self, shp):
+        return tuple(getattr(self, s) if isinstance(s, str) else s for s in shp)
+
+    @classmethod
+    def load(cls, directory, qgrid, fourthorder=False, readiso=False, timereversal=True) -> "Problem":
+        """Read infile.* from `directory` and build mesh and phonons (main.f90:42-181)."""
+        L = N.lib()
+        out = C.POINTER(N.TdgProblem)()
+        g = np.ascontiguousarray(qgrid, dtype=np.int32)
+        N.check(L.tdg_problem_load(str(directory).encode(), N.ptr(g, C.c_int32), int(bool(fourthorder)),
+                                   int(bool(readiso)), int(bool(timereversal)), C.byref(out)), "tdg_problem_load")
+        try:
+            return cls.from_struct(out.contents)
+        finally:
+            L.tdg_problem_free(out)
+
+    @classmethod
+    def from_struct(cls, s: N.TdgProblem) -> "Problem":
+        kw = {k: getattr(s, k) for k in _SCALARS}
+        for k in ("latvec", "reclat", "inv_reclat"):
+            kw[k] = np.array(getattr(s, k)[:], dtype=np.float64)
+        kw["volume"] = s.volume
+        kw["grid"] = np.array(s.grid[:], dtype=np.int32)
+        dims = dict(kw)
+        for table, ct in ((_FIELDS_F64, np.float64), (_FIELDS_I32, np.int32)):
+            for k, shp in table.items():
+                n = int(np.prod([dims[x] if isinstance(x, str) else x for x in shp]))
+                p = getattr(s, k)
+                kw[k] = np.ctypeslib.as_array(p, shape=(n,)).copy() if (n > 0 and p) else np.zeros(n, dtype=ct)
+        return cls(**kw)
+
+    def struct(self) -> N.TdgProblem:
+        s = N.TdgProblem()
+        for k in _SCALARS:
+            setattr(s, k, getattr(self, k))
+        for k in ("latvec", "reclat", "inv_reclat"):
+            getattr(s, k)[:] = list(getattr(self, k))
+        s.volume = self.volume
+        s.grid[:] = [int(x) for x in self.grid]
+        for k in _FIELDS_F64:
+            setattr(s, k, N.ptr(getattr(self, k), C.c_double))
+        for k in _FIELDS_I32:
+            setattr(s, k, N.ptr(getattr(self, k), C.c_int32))
+        self._struct = s  # keep alive with the arrays it points into
+        return s
+
+    def rows(self):
+        """(q1, b1) 1-based rows with omega >= lo_freqtol (scattering.f90:170-209)."""
+        om = self.omega[self.irr_full - 1]
+        q1, b1 = np.nonzero(om >= LO_FREQTOL)
+        return (q1 + 1).astype(np.int32), (b1 + 1).astype(np.int32)
+
+
+@dataclass
+class Options:
+    """Hot-path subset of lo_opts, same flag meaning as options.f90."""
+
+    temperature: float = 300.0
+    integrationtype: int = 2
+    sigma: float = 1.0
+    thirdorder: bool = True
+    fourthorder: bool = False
+    isotopescattering: bool = True
+    classical: bool = False
+    mfp_max: float = -1.0  # metres, as --max_mfp
+    qg3ph: tuple = (-1, -1, -1)
+    qg4ph: tuple = (-1, -1, -1)
+    seed: int = 1
+    precision: str = "fp64"  # "fp64" or "mixed"
+    itertol: float = 1e-5
+    itermaxsteps: int = 200
+
+    def resolved(self, qgrid):
+        """options.f90:205-235: grids default to (and are capped by) the full q-grid.
+        A zero dimension, which the reference would divide by, also takes the full grid."""
+        q3 = tuple(int(m) if 0 < int(m) <= int(g) else int(g) for m, g in zip(self.qg3ph, qgrid))
+        q4 = tuple(int(m) if 0 < int(m) <= int(g) else int(g) for m, g in zip(self.qg4ph, qgrid))
+        return q3, q4
+
+    def struct(self, qgrid) -> N.TdgOpts:
+        o = N.TdgOpts()
+        o.temperature = float(self.temperature)
+        o.integrationtype = int(self.integrationtype)
+        o.sigma = float(self.sigma)
+        o.thirdorder = int(bool(self.thirdorder))
+        o.fourthorder = int(bool(self.fourthorder))
+        o.isotope = int(bool(self.isotopescattering))
+        o.classical = int(bool(self.classical))
+        o.mfp_max = float(self.mfp_max) / BOHR_TO_M if self.mfp_max > 0 else -1.0
+        q3, q4 = self.resolved(qgrid)
+        o.qg3ph[:] = list(q3)
+        o.qg4ph[:] = list(q4)
+        o.seed = int(self.seed)
+        if self.precision not in ("fp64", "mixed"):
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        o.precision = N.TDG_PREC_FP64 if self.precision == "fp64" else N.TDG_PREC_MIXED
+        return o
+
+
+@dataclass
+class QLists:
+    """Rows and their q' samples (CSR). All indices 1-based as in the reference."""
+
+    row_q1: np.ndarray
+    row_b1: np.ndarray
+    ptr3: np.ndarray | None = None
+    list3: np.ndarray | None = None
+    ptr4: np.ndarray | None = None
+    list4a: np.ndarray | None = None
+    list4b: np.ndarray | None = None
+    _keep: list = field(default_factory=list, repr=False)
+
+    @property
+    def n_row(self) -> int:
+        return int(self.row_q1.size)
+
+    @classmethod
+    def monte_carlo(cls, prob: Problem, opts: Options) -> "QLists":
+        """Samples drawn exactly as the reference draws them (tdg_mc_qlists)."""
+        L = N.lib()
+        q3, q4 = opts.resolved(prob.grid)
+        cap = prob.n_irr * prob.n_mode
+        np3, np4 = int(np.prod(q3)), int(np.prod(q4))
+        rq1 = np.zeros(cap, np.int32)
+        rb1 = np.zeros(cap, np.int32)
+        p3 = np.zeros(cap + 1, np.int64)
+        p4 = np.zeros(cap + 1, np.int64)
+        l3 = np.zeros(cap * np3 if opts.thirdorder else 1, np.int32)
+        l4a = np.zeros(cap * np4 if opts.fourthorder else 1, np.int32)
+        l4b = np.zeros(cap * np4 if opts.fourthorder else 1, np.int32)
+        nr = C.c_int32(0)
+        ps = prob.struct()
+        os_ = opts.struct(prob.grid)
+        N.check(L.tdg_mc_qlists(C.byref(ps), C.byref(os_), C.byref(nr), N.ptr(rq1, C.c_int32), N.ptr(rb1, C.c_int32),
+                                N.ptr(p3, C.c_int64), N.ptr(l3, C.c_int32), N.ptr(p4, C.c_int64),
+                                N.ptr(l4a, C.c_int32), N.ptr(l4b, C.c_int32)), "tdg_mc_qlists")
+        n = nr.value
+        return cls(rq1[:n].copy(), rb1[:n].copy(),
+                   p3[: n + 1].copy() if opts.thirdorder else None,
+                   l3[: n * np3].copy() if opts.thirdorder else None,
+                   p4[: n + 1].copy() if opts.fourthorder else None,
+                   l4a[: n * np4].copy() if opts.fourthorder else None,
+                   l4b[: n * np4].copy() if opts.fourthorder else None)
+
+    @classmethod
+    def per_irreducible(cls, prob: Problem, samples3: dict | None = None, samples4: dict | None = None) -> "QLists":
+        """Explicit samples per irreducible q1 (1-based key), shared by all rows of q1."""
+        rq1, rb1 = prob.rows()
+        p3 = l3 = p4 = l4a = l4b = None
+        if samples3 is not None:
+            lists = [np.asarray(samples3[int(q)], np.int32) for q in rq1]
+            p3 = np.concatenate([[0], np.cumsum([x.size for x in lists])]).astype(np.int64)
+            l3 = np.concatenate(lists).astype(np.int32)
+        if samples4 is not None:
+            la = [np.asarray(samples4[int(q)][0], np.int32) for q in rq1]
+            lb = [np.asarray(samples4[int(q)][1], np.int32) for q in rq1]
+            p4 = np.concatenate([[0], np.cumsum([x.size for x in la])]).astype(np.int64)
+            l4a = np.concatenate(la).astype(np.int32)
+            l4b = np.concatenate(lb).astype(np.int32)
+        return cls(rq1, rb1, p3, l3, p4, l4a, l4b)
+
+    def struct(self) -> N.TdgQlists:
+        s = N.TdgQlists()
+        arrs = [np.ascontiguousarray(x) if x is not None else None
+                for x in (self.row_q1, self.row_b1, self.ptr3, self.list3, self.ptr4, self.list4a, self.list4b)]
+        self._keep = arrs
+        s.n_row = self.n_row
+        s.row_q1 = N.ptr(arrs[0], C.c_int32)
+        s.row_b1 = N.ptr(arrs[1], C.c_int32)
+        s.ptr3 = N.ptr(arrs[2], C.c_int64)
+        s.list3 = N.ptr(arrs[3], C.c_int32)
+        s.ptr4 = N.ptr(arrs[4], C.c_int64)
+        s.list4a = N.ptr(arrs[5], C.c_int32)
+        s.list4b = N.ptr(arrs[6], C.c_int32)
+        return s
+
+
+class ScatteringRates:
+    """lo_scattering_rates on one GB300 (scattering.f90:34-55)."""
+
+    def __init__(self, prob: Problem, device: int = 0):
+        self.prob = prob
+        self._lib = N.lib()
+        self._ctx = C.c_void_p()
+        ps = prob.struct()
+        N.check(self._lib.tdg_create(C.byref(self._ctx), C.byref(ps), int(device)), "tdg_create")
+        self.linewidth = None
+        self.qs = None
+        self.stats = None
+        self.lists = None
+
+    def close(self):
+        if self._ctx:
+            self._lib.tdg_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def generate(self, opts: Options, lists: QLists | None = None) -> np.ndarray:
+        """sr%generate: linewidths (n_irr, n_mode) in Hartree; Xi stays on the device."""
+        p = self.prob
+        if lists is None:
+            lists = QLists.monte_carlo(p, opts)
+        self.lists = lists
+        lw = np.zeros(p.n_irr * p.n_mode)
+        qs = np.zeros(p.n_irr * p.n_mode)
+        st = np.zeros(4)
+        o = opts.struct(p.grid)
+        q = lists.struct()
+        N.check(self._lib.tdg_scattering(self._ctx, C.byref(o), C.byref(q), N.ptr(lw, C.c_double),
+                                         N.ptr(qs, C.c_double), N.ptr(st, C.c_double)), "tdg_scattering")
+        self.linewidth = lw.reshape(p.n_irr, p.n_mode)
+        self.qs = qs.reshape(p.n_irr, p.n_mode)
+        self.stats = {"triplets": int(st[0]), "quartets": int(st[1]), "device_ms": float(st[2]),
+                      "candidates": int(st[3])}
+        return self.linewidth
+
+    def triplets(self, q1: int, sample) -> list:
+        """Device enumeration of the irreducible triplets of one sample (1-based indices):
+        [(q2, q3, [(q2', q3'), ...]), ...] in sample order."""
+        sample = np.ascontiguousarray(sample, dtype=np.int32)
+        cap = max(64, 8 * sample.size * (2 + 2 * self.prob.n_op))
+        out = np.zeros(cap, np.int32)
+        w = C.c_int64(0)
+        N.check(self._lib.tdg_triplets(self._ctx, int(q1), N.ptr(sample, C.c_int32), sample.size,
+                                       N.ptr(out, C.c_int32), cap, C.byref(w)), "tdg_triplets")
+        res, i = [], 0
+        while i < w.value:
+            q2, q3, k = int(out[i]), int(out[i + 1]), int(out[i + 2])
+            pairs = [(int(out[i + 3 + 2 * j]), int(out[i + 4 + 2 * j])) for j in range(k)]
+            res.append((q2, q3, pairs))
+            i += 3 + 2 * k
+        return res
+
+    @property
+    def Xi(self) -> np.ndarray:
+        p = self.prob
+        xi = np.zeros((self.lists.n_row, p.n_full * p.n_mode))
+        N.check(self._lib.tdg_get_xi(self._ctx, N.ptr(xi, C.c_double)), "tdg_get_xi")
+        return xi
+
+    def kappa(self, opts: Options, maxiter: int | None = None, tol: float | None = None):
+        """get_kappa (SMA), iterative_solution, symmetrize_kappa. Returns a.u. 3x3 tensors."""
+        p = self.prob
+        o = opts.struct(p.grid)
+        ks = np.zeros(9)
+        ki = np.zeros(9)
+        fn = np.zeros(p.n_irr * p.n_mode * 3)
+        nit = C.c_int32(0)
+        mi = opts.itermaxsteps if maxiter is None else maxiter
+        tl = opts.itertol if tol is None else tol
+        N.check(self._lib.tdg_kappa(self._ctx, C.byref(o), int(mi), float(tl), N.ptr(ks, C.c_double),
+                                    N.ptr(ki, C.c_double), N.ptr(fn, C.c_double), C.byref(nit)), "tdg_kappa")
+        self.n_iter = nit.value
+        self.Fn = fn.reshape(p.n_irr, p.n_mode, 3)
+        return ks.reshape(3, 3, order="F"), ki.reshape(3, 3, order="F")
+
+
+def write_outfile(directory, temperature, kappa_sma, kappa_iter, kappa_offdiag=None) -> Path:
+    """outfile.thermal_conductivity (main.f90:246-294); tensors in atomic units."""
+    L = N.lib()
+    ks = np.ascontiguousarray(np.asarray(kappa_sma).reshape(3, 3).ravel(order="F"))
+    ki = np.ascontiguousarray(np.asarray(kappa_iter).reshape(3, 3).ravel(order="F"))
+    ko = np.zeros(9) if kappa_offdiag is None else np.ascontiguousarray(np.asarray(kappa_offdiag).reshape(3, 3).ravel(order="F"))
+    N.check(L.tdg_write_outfile(str(directory).encode(), float(temperature), N.ptr(ks, C.c_double),
+                                N.ptr(ki, C.c_double), N.ptr(ko, C.c_double)), "tdg_write_outfile")
+    return Path(directory) / "outfile.thermal_conductivity"
+
+
+def device_count() -> int:
+    return int(N.lib().tdg_device_count())

@@ -1,0 +1,33 @@
+"""Shared fixtures: synthetic crystals written by tdep_gb300.synth into a session tmpdir."""
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GB300 device (runs the native sm_103a path)")
+
+
+@pytest.fixture(scope="session")
+def built():
+    from tdep_gb300 import build
+
+    build.build_all()
+    return True
+
+
+@pytest.fixture(scope="session")
+def configs(tmp_path_factory, built):
+    from tdep_gb300 import synth
+
+    base = tmp_path_factory.mktemp("configs")
+    return {
+        "fcc": synth.write_config("fcc_morse", base / "fcc", seed=1),
+        "rocksalt": synth.write_config("rocksalt", base / "rocksalt", seed=1),
+        "perovskite": synth.write_config("perovskite", base / "perovskite", seed=1),
+    }

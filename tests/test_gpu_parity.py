@@ -1,0 +1,145 @@
+"""Parity of the GB300 path (through the C-ABI) with the oracle's CPU restatement.
+
+Bars: integer triplet enumeration bit-exact; FP64 linewidths rtol 1e-10, Xi within
+1e-9 of its largest entry, kappa rtol 1e-9; mixed precision kappa rtol 1e-4 against the
+FP64 GPU path, as the benchmark spec states.
+"""
+import numpy as np
+import pytest
+
+from oracle import binding as orc
+from tdep_gb300 import Options, Problem, QLists, ScatteringRates, device_count
+
+pytestmark = pytest.mark.gpu
+
+LW_RTOL = 1e-10
+KAPPA_RTOL = 1e-9
+XI_REL = 1e-9
+MIXED_KAPPA_RTOL = 1e-4
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _require_gpu(built):
+    assert device_count() > 0, "GPU tests need a CUDA device; the GB300 path has no CPU fallback"
+
+
+def distinct_triplets(prob, lists):
+    """Accepted irreducible q-triplets counted once per q1 over the union of its rows' samples
+    (the oracle, like the reference, revisits each of them once per row)."""
+    total = 0
+    for q1 in np.unique(lists.row_q1):
+        rows = np.nonzero(lists.row_q1 == q1)[0]
+        union = np.unique(np.concatenate([lists.list3[lists.ptr3[r]:lists.ptr3[r + 1]] for r in rows]))
+        total += len(orc.triplets(prob, int(q1), union.astype(np.int32)))
+    return total
+
+
+def _compare(prob, opts, lists, lw_rtol=LW_RTOL, kappa_rtol=KAPPA_RTOL, check_xi=True):
+    sr = ScatteringRates(prob)
+    lw = sr.generate(opts, lists)
+    xi = sr.Xi if check_xi else None
+    ks, ki = sr.kappa(opts)
+    ref = orc.full_run(prob, opts, lists)
+    assert sr.stats["triplets"] == distinct_triplets(prob, lists)
+    np.testing.assert_allclose(lw, ref["linewidth"], rtol=lw_rtol, atol=1e-14 * np.abs(ref["linewidth"]).max())
+    if check_xi:
+        scale = np.abs(ref["xi"]).max()
+        np.testing.assert_allclose(xi, ref["xi"], rtol=0, atol=XI_REL * scale)
+    np.testing.assert_allclose(ks, ref["kappa_sma"], rtol=kappa_rtol, atol=kappa_rtol * np.abs(ref["kappa_sma"]).max())
+    np.testing.assert_allclose(ki, ref["kappa_iter"], rtol=kappa_rtol, atol=kappa_rtol * np.abs(ref["kappa_iter"]).max())
+    assert sr.n_iter == ref["n_iter"]
+    sr.close()
+    return lw, ki, ref
+
+
+@pytest.mark.parametrize("name,grid", [("fcc", (8, 8, 8)), ("rocksalt", (6, 6, 6)), ("perovskite", (4, 4, 4))])
+def test_triplet_enumeration_bit_exact(configs, name, grid):
+    prob = Problem.load(configs[name], grid, readiso=True)
+    sr = ScatteringRates(prob)
+    rng = np.random.default_rng(3)
+    full = np.arange(1, prob.n_full + 1, dtype=np.int32)
+    for q1 in range(1, prob.n_irr + 1):
+        for sample in (full, rng.permutation(full)[: max(1, prob.n_full // 3)]):
+            assert sr.triplets(q1, sample) == orc.triplets(prob, q1, sample)
+    sr.close()
+
+
+def test_fp64_fcc_gaussian(configs):
+    prob = Problem.load(configs["fcc"], (8, 8, 8), readiso=True)
+    opts = Options(temperature=300.0, integrationtype=1, sigma=1.0, isotopescattering=False, seed=42, itertol=1e-6)
+    _compare(prob, opts, QLists.monte_carlo(prob, opts))
+
+
+@pytest.mark.parametrize("temperature", [100.0, 300.0, 700.0])
+def test_fp64_rocksalt_adaptive(configs, temperature):
+    prob = Problem.load(configs["rocksalt"], (6, 6, 6), readiso=True)
+    opts = Options(temperature=temperature, integrationtype=2, isotopescattering=False, seed=7)
+    _compare(prob, opts, QLists.monte_carlo(prob, opts))
+
+
+def test_fp64_perovskite_15_modes(configs):
+    prob = Problem.load(configs["perovskite"], (4, 4, 4), readiso=True)
+    opts = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=11)
+    _compare(prob, opts, QLists.monte_carlo(prob, opts))
+
+
+def test_fp64_isotope_boundary_velocity_smearing(configs, tmp_path):
+    import shutil
+
+    d = tmp_path / "rs_iso"
+    shutil.copytree(configs["rocksalt"], d)
+    # two isotopes per site: a non-zero mass-disorder parameter
+    (d / "infile.isotopes").write_text("2\n0.75 22.0\n0.25 24.0\n2\n0.7577 34.969\n0.2423 36.966\n")
+    prob = Problem.load(d, (6, 6, 6), readiso=True)
+    assert prob.mass_disorder.min() > 0
+    opts = Options(temperature=300.0, integrationtype=6, isotopescattering=True, mfp_max=1e-7, seed=5)
+    _compare(prob, opts, QLists.monte_carlo(prob, opts))
+
+
+def test_fp64_monte_carlo_rows_differ(configs):
+    prob = Problem.load(configs["fcc"], (8, 8, 8), readiso=True)
+    opts = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=42, qg3ph=(4, 4, 4))
+    lists = QLists.monte_carlo(prob, opts)
+    # every row draws its own stratified sample
+    assert not np.array_equal(lists.list3[lists.ptr3[0]:lists.ptr3[1]], lists.list3[lists.ptr3[1]:lists.ptr3[2]])
+    _compare(prob, opts, lists)
+
+
+def test_fp64_classical_uneven_per_q1_samples(configs):
+    prob = Problem.load(configs["perovskite"], (4, 4, 4), readiso=True)
+    rng = np.random.default_rng(17)
+    samples = {q: np.sort(rng.choice(np.arange(1, prob.n_full + 1), size=int(rng.integers(8, prob.n_full)),
+                                     replace=False)).astype(np.int32) for q in range(1, prob.n_irr + 1)}
+    lists = QLists.per_irreducible(prob, samples3=samples)
+    opts = Options(temperature=500.0, integrationtype=2, classical=True, isotopescattering=False)
+    _compare(prob, opts, lists)
+
+
+def test_mixed_precision_kappa(configs):
+    prob = Problem.load(configs["rocksalt"], (8, 8, 8), readiso=True)
+    o64 = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=3)
+    o32 = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=3, precision="mixed")
+    lists = QLists.monte_carlo(prob, o64)
+    sr = ScatteringRates(prob)
+    lw64 = sr.generate(o64, lists).copy()
+    _, k64 = sr.kappa(o64)
+    lw32 = sr.generate(o32, lists).copy()
+    _, k32 = sr.kappa(o32)
+    sr.close()
+    big = lw64 > 1e-3 * lw64.max()
+    assert np.max(np.abs(lw32[big] / lw64[big] - 1)) < 1e-4
+    np.testing.assert_allclose(k32, k64, rtol=MIXED_KAPPA_RTOL, atol=MIXED_KAPPA_RTOL * np.abs(k64).max())
+
+
+def test_repeat_calls_are_stable(configs):
+    prob = Problem.load(configs["rocksalt"], (6, 6, 6), readiso=True)
+    opts = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=9)
+    lists = QLists.monte_carlo(prob, opts)
+    sr = ScatteringRates(prob)
+    a = sr.generate(opts, lists).copy()
+    _, ka = sr.kappa(opts)
+    b = sr.generate(opts, lists).copy()
+    _, kb = sr.kappa(opts)
+    sr.close()
+    np.testing.assert_allclose(a, b, rtol=1e-12, atol=0)
+    np.testing.assert_allclose(ka, kb, rtol=1e-12, atol=0)
