@@ -1,0 +1,339 @@
+"""Benchmark of the GB300 three-phonon scattering path.
+
+Default workload (the configuration the headline metric is quoted on): 2-atom rocksalt,
+24x24x24 Gamma-centred mesh, adaptive Gaussian smearing, T = 300 K, full q' grid (the
+reference's default -qg3ph), seeded Born-Mayer + spring force constants, mixed precision
+(FP32 pretransform and contraction, FP64 delta weights and accumulation).
+
+One step = one pass of the scattering path (sr%generate: triplet enumeration, fused
+pretransform/contraction/accumulation, symmetrisation) over the whole mesh.
+  value : accepted irreducible q-triplets per second, device time of the pipeline with all
+          inputs resident in HBM (CUDA events on the library's stream)
+  e2e   : the same metric through the public API with host buffers: context creation
+          (H2D of phonons and force constants), generate (H2D of the samples, D2H of the
+          linewidths) and the kappa solve, per step
+  cpu_baseline / --impl reference : the oracle's restatement of the reference on the host
+          cores (OpenMP), timed on complete q1 groups of the same workload.
+
+  python bench.py [--gpus 1] [--steps K] [--warmup W] [--impl gb300|reference] [--config NAME]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "3-phonon triplets/s & κ wall time at 1 GB300, mixed vs FP64 at ≤1e-4 κ rel err"
+
+CONFIGS = {
+    "rocksalt24": dict(synth="rocksalt", grid=(24, 24, 24), it=2, temperature=300.0,
+                       workload="rocksalt Na/Cl 2-atom (6 modes), 24x24x24 mesh, adaptive smearing, T=300 K, "
+                                "full q' grid, no isotope"),
+    "perovskite16": dict(synth="perovskite", grid=(16, 16, 16), it=2, temperature=300.0, uneven=(200, 4000),
+                         workload="cubic perovskite 5-atom (15 modes), 16x16x16 mesh, adaptive smearing, T=300 K, "
+                                  "seeded per-q1 q' samples of 200-4000 points, no isotope"),
+    "fcc12": dict(synth="fcc_morse", grid=(12, 12, 12), it=1, temperature=300.0,
+                  workload="fcc Morse 1-atom (3 modes), 12x12x12 mesh, Gaussian smearing 1 THz, T=300 K"),
+    # small cases of the same kernels for ncu captures (a few hundred MB on the device)
+    "rocksalt12": dict(synth="rocksalt", grid=(12, 12, 12), it=2, temperature=300.0,
+                       workload="rocksalt Na/Cl 2-atom (6 modes), 12x12x12 mesh, adaptive smearing, T=300 K"),
+    "perovskite8": dict(synth="perovskite", grid=(8, 8, 8), it=2, temperature=300.0,
+                        workload="cubic perovskite 5-atom (15 modes), 8x8x8 mesh, adaptive smearing, T=300 K"),
+}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def setup(cfg_name, precision="mixed"):
+    from tdep_gb300 import Options, Problem, QLists, synth
+
+    cfg = CONFIGS[cfg_name]
+    tmp = tempfile.mkdtemp(prefix="tdg_bench_")
+    d = synth.write_config(cfg["synth"], Path(tmp) / cfg["synth"], seed=1)
+    t0 = time.perf_counter()
+    prob = Problem.load(d, cfg["grid"], readiso=True)
+    log(f"[bench] problem: n_mode={prob.n_mode} n_full={prob.n_full} n_irr={prob.n_irr} n_fc3={prob.n_fc3} "
+        f"({time.perf_counter() - t0:.1f}s)")
+    opts = Options(temperature=cfg["temperature"], integrationtype=cfg["it"], sigma=1.0, isotopescattering=False,
+                   seed=1, precision=precision, itertol=1e-6, itermaxsteps=200)
+    if "uneven" in cfg:
+        lo, hi = cfg["uneven"]
+        rng = np.random.default_rng(1)
+        samples = {q: np.sort(rng.choice(np.arange(1, prob.n_full + 1), size=int(rng.integers(lo, hi + 1)),
+                                         replace=False)).astype(np.int32) for q in range(1, prob.n_irr + 1)}
+        lists = QLists.per_irreducible(prob, samples3=samples)
+    else:
+        lists = QLists.monte_carlo(prob, opts)
+    return cfg, prob, opts, lists
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names[1:], parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d["hbm_gbs"], d["bf16_tflops"], "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def cpu_sample(prob, opts, lists, budget_s=12.0, nthreads=None):
+    """Time the oracle on complete q1 groups until the budget is used; returns
+    (distinct q-triplets covered, seconds, description, threads)."""
+    from oracle import binding as orc
+
+    nthreads = nthreads or os.cpu_count() or 1
+    q1s = np.unique(lists.row_q1)
+    # blocks of consecutive q1 groups from the middle of the wedge, so that one call keeps
+    # every thread busy; each block is whole rows of whole q1 groups
+    per_block = max(1, -(-nthreads // max(1, prob.n_mode)))
+    start = len(q1s) // 2
+    done_trip, done_s, used = 0, 0.0, []
+    for b0 in range(start, start + len(q1s), per_block):
+        block = [q1s[i % len(q1s)] for i in range(b0, b0 + per_block)]
+        if len(set(block)) < len(block) or any(q in used for q in block):
+            break
+        rows = np.nonzero(np.isin(lists.row_q1, block))[0]
+        r0, r1 = int(rows[0]), int(rows[-1]) + 1
+        if r1 - r0 != rows.size:
+            break
+        t0 = time.perf_counter()
+        orc.scattering(prob, opts, lists, nthreads=nthreads, rows=(r0, r1))
+        done_s += time.perf_counter() - t0
+        for q1 in block:
+            rr = np.nonzero(lists.row_q1 == q1)[0]
+            union = np.unique(np.concatenate([lists.list3[lists.ptr3[r]:lists.ptr3[r + 1]] for r in rr]))
+            done_trip += len(orc.triplets(prob, int(q1), union.astype(np.int32)))
+            used.append(int(q1))
+        if done_s >= budget_s:
+            break
+    desc = (f"oracle restatement (per-row zgeru/dot_product contraction as in scattering_threephonon.f90), "
+            f"{len(used)} complete irreducible q1 groups ({done_trip} q-triplets) of the same workload")
+    return done_trip, done_s, desc, nthreads
+
+
+def run_reference(args):
+    cfg, prob, opts, lists = setup(args.config, precision="fp64")
+    per_step = max(2.0, 20.0 / max(1, args.steps))
+    for _ in range(args.warmup):
+        cpu_sample(prob, opts, lists, budget_s=0.5)
+    trip, secs = 0, 0.0
+    desc, cores = "", os.cpu_count()
+    for _ in range(args.steps):
+        t, s, desc, cores = cpu_sample(prob, opts, lists, budget_s=per_step)
+        trip += t
+        secs += s
+    value = trip / secs
+    line = {"metric": METRIC, "value": value, "unit": "q-triplets/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": cfg["workload"]},
+            "cpu_baseline": {"value": value, "unit": "q-triplets/s", "cores": cores, "kind": "port", "sample": desc},
+            "e2e": {"value": value, "unit": "q-triplets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_profile(args):
+    """--profile: warm-up passes then `steps` scattering passes, nothing else (for ncu)."""
+    from tdep_gb300 import ScatteringRates
+
+    cfg, prob, opts, lists = setup(args.config, precision=args.precision)
+    sr = ScatteringRates(prob)
+    for _ in range(args.warmup + args.steps):
+        sr.generate(opts, lists)
+    log(f"[bench] profile: {sr.stats}")
+    sr.close()
+
+
+def run_gb300(args):
+    import torch
+
+    from tdep_gb300 import ScatteringRates
+
+    cfg, prob, opts, lists = setup(args.config, precision="mixed")
+    n = prob.n_mode
+    torch.cuda.init()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > 129 MB L2
+
+    sr = ScatteringRates(prob)
+    for _ in range(args.warmup):
+        sr.generate(opts, lists)
+    # ---- resident timing: device time of each pipeline pass, L2 flushed between passes ----
+    clocks = ClockSampler()
+    clocks.start()
+    dev_ms, fused_ms, launches, trip = [], [], 0, 0
+    torch.cuda.synchronize()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        sr.generate(opts, lists)
+        st = sr.stats
+        dev_ms.append(st["device_ms"])
+        fused_ms.append(st["threephonon_ms"])
+        launches += st["launches"]
+        trip = st["triplets"]
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    lw_mixed = sr.linewidth.copy()
+    t0 = time.perf_counter()
+    ks32, ki32 = sr.kappa(opts)
+    kappa_ms = 1e3 * (time.perf_counter() - t0)
+    kappa_iters = sr.n_iter
+    stats = dict(sr.stats)
+
+    # ---- FP64 path on the same workload: kappa error bar and speedup ----
+    o64 = type(opts)(**{**opts.__dict__, "precision": "fp64"})
+    sr.generate(o64, lists)
+    fp64_ms = sr.stats["device_ms"]
+    _, ki64 = sr.kappa(o64)
+    sr.close()
+    kappa_err = float(np.max(np.abs(ki32 - ki64)) / np.max(np.abs(ki64)))
+
+    # ---- end to end through the public API with host buffers ----
+    e2e_s = []
+    h2d = d2h = 0
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s2 = ScatteringRates(prob)
+        s2.generate(opts, lists)
+        s2.kappa(opts)
+        s2.close()
+        torch.cuda.synchronize()
+        e2e_s.append(time.perf_counter() - t0)
+    nrow, ncol = lists.n_row, prob.n_full * n
+    h2d = (prob.omega.nbytes + prob.vel.nbytes + prob.egv.nbytes * 3 // 2 + prob.n_op * prob.n_full * 4 +
+           prob.fc3_mwm.nbytes * 3 // 2 + prob.fc3_lv.nbytes + lists.list3.nbytes + lists.ptr3.nbytes +
+           stats["candidates"] * 16 + 2 * prob.n_irr * n * 8 + kappa_iters * ncol * 3 * 8)
+    d2h = nrow * 8 + prob.n_irr * n * 8 * 2 + 18 * 8 + kappa_iters * nrow * 3 * 8
+
+    # ---- roofline of the dominant kernel (fused pretransform + contraction + epilogue) ----
+    hbm, bf16, src = peaks()
+    flop_per_trip = 24 * n**4 + 4 * 27 * prob.n_fc3
+    fused_s = float(np.mean(fused_ms)) / 1e3
+    achieved = flop_per_trip * trip / fused_s / 1e12
+    roof = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16,
+            "traffic": None, "kernel": "k_threephonon (FP32 SIMT)",
+            "per_unit": f"{flop_per_trip} flop per q-triplet (24 n^4 contraction + 108 N_t pretransform)",
+            "peak_source": f"{src} dense bf16"}
+
+    cpu_trip, cpu_s, desc, cores = cpu_sample(prob, opts, lists, budget_s=args.cpu_budget)
+    value = trip * args.steps / (sum(dev_ms) / 1e3)
+    line = {
+        "metric": METRIC, "value": value, "unit": "q-triplets/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": float(np.mean(dev_ms)), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": cfg["workload"], "mesh": list(cfg["grid"]), "n_mode": n, "q_triplets_per_step": trip,
+                   "precision": "mixed: FP32 pretransform+contraction, FP64 delta weights/occupations/accumulation",
+                   "l2": "256 MB buffer written between steps (L2 flush); Xi+od working set 2x%.2f GB" %
+                         (nrow * ncol * 8 / 1e9)},
+        "e2e": {"value": trip / float(np.mean(e2e_s)), "unit": "q-triplets/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "includes": "context creation, generate, kappa solve"},
+        "roofline": roof,
+        "cpu_baseline": {"value": cpu_trip / cpu_s, "unit": "q-triplets/s", "cores": cores, "kind": "port",
+                         "sample": desc},
+        "clocks": clk,
+        "gpu_launches": int(launches),
+        "stage_ms": {k: stats[k] for k in ("enumerate_ms", "threephonon_ms", "symmetrize_ms", "device_ms")},
+        "mode_triplets_per_s": value * n**3,
+        "kappa_wall_ms": kappa_ms, "kappa_iterations": kappa_iters,
+        "fp64": {"value": trip / (fp64_ms / 1e3), "ms_per_step": fp64_ms,
+                 "mixed_speedup": fp64_ms / float(np.mean(dev_ms)), "kappa_rel_err_mixed_vs_fp64": kappa_err},
+        "linewidth_max_hartree": float(lw_mixed.max()),
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="rocksalt24", choices=sorted(CONFIGS))
+    ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--profile", action="store_true", help="only run scattering passes (for ncu captures)")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"], help="with --profile")
+    args = ap.parse_args()
+    if args.profile:
+        run_profile(args)
+        return
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
+    if world > 1:
+        # The path does not shard across GPUs in this build: replicas only. Rank 0 reports.
+        local = int(os.environ.get("LOCAL_RANK", "0"))
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+        if rank != 0:
+            return
+    run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -85,18 +85,66 @@ __global__ void k_isotope(MeshDev m, PhononDev ph, RowsDev rows, const int32_t *
 }
 
 // symmetrize_and_distribute (scattering_threephonon.f90:143-205, scattering_fourphonon.f90:195-250).
-// One CTA per row. Every orbit is handled by its smallest member (an image smaller than
-// q2 skips q2, as in the reference), so threads never touch the same entries. A bitmap
-// ignores repeated entries of a sample, which the reference would process to the same
-// result.
-__global__ void k_sym_distribute(MeshDev m, const int32_t *row_q1, const int64_t *ptr, const int32_t *list,
-                                 double *od, double *xi) {
+// Orbit tables of the little group of every irreducible q1, built once per mesh: q2 is a
+// representative when no on-grid image is smaller (the reference's "cycle allq2" rule);
+// its images are kept in operation order, -1 for operations that leave the grid.
+__global__ void k_orbit_flag(MeshDev m, int32_t *flag) {
+    const int q2 = blockIdx.x * blockDim.x + threadIdx.x;
+    const int q1 = blockIdx.y;
+    if (q2 >= m.n_full) return;
+    const int nop = m.irr_nop[q1];
+    const int32_t *ops = m.irr_ops + (size_t)q1 * m.n_op;
+    int rep = 1;
+    for (int j = 0; j < nop; ++j) {
+        const int q2p = m.rot[(size_t)ops[j] * m.n_full + q2];
+        if (q2p >= 0 && q2p < q2) {
+            rep = 0;
+            break;
+        }
+    }
+    flag[(size_t)q1 * m.n_full + q2] = rep;
+}
+
+__global__ void k_orbit_fill(MeshDev m, const int32_t *flag, const int32_t *scan, int32_t *orb_of, int32_t *rep,
+                             int32_t *img, int32_t *cnt) {
+    const int q2 = blockIdx.x * blockDim.x + threadIdx.x;
+    const int q1 = blockIdx.y;
+    if (q2 >= m.n_full) return;
+    const size_t i = (size_t)q1 * m.n_full + q2;
+    if (!flag[i]) {
+        orb_of[i] = -1;
+        return;
+    }
+    const int k = scan[i];
+    orb_of[i] = k;
+    rep[k] = q2;
+    const int nop = m.irr_nop[q1];
+    const int32_t *ops = m.irr_ops + (size_t)q1 * m.n_op;
+    int c = 0;
+    for (int j = 0; j < m.n_op; ++j) {
+        int q2p = -1;
+        if (j < nop) {
+            q2p = m.rot[(size_t)ops[j] * m.n_full + q2];
+            if (q2p >= 0) ++c;
+        }
+        img[(size_t)k * m.n_op + j] = q2p;
+    }
+    cnt[k] = c;
+}
+
+// symmetrize_and_distribute (scattering_threephonon.f90:143-205, scattering_fourphonon.f90:195-250)
+// in place on one row per CTA: for every sampled q2 that represents its orbit, each mode's
+// entries with od > 0 are averaged and the average is written to every image. Orbits are
+// disjoint, so threads never touch the same entries; a bitmap ignores repeated entries of
+// a sample (the reference would process them again to the same result).
+// When xi != nullptr the symmetrised row is then added to xi.
+__global__ void k_sym_distribute(MeshDev m, OrbitDev o, const int32_t *row_q1, const int64_t *ptr,
+                                 const int32_t *list, double *od, double *xi) {
     extern __shared__ uint32_t seen[];
     const int n = m.n_mode;
     const int r = blockIdx.x;
     const int q1 = row_q1[r];
     const int nop = m.irr_nop[q1];
-    const int32_t *ops = m.irr_ops + (size_t)q1 * m.n_op;
     const int64_t ld = (int64_t)m.n_full * n;
     double *odr = od + (int64_t)r * ld;
     const int nw = (m.n_full + 31) / 32;
@@ -104,19 +152,16 @@ __global__ void k_sym_distribute(MeshDev m, const int32_t *row_q1, const int64_t
     __syncthreads();
     for (int64_t qi = ptr[r] + threadIdx.x; qi < ptr[r + 1]; qi += blockDim.x) {
         const int q2 = list[qi] - 1;
+        const int k = o.orb_of[(size_t)q1 * m.n_full + q2];
+        if (k < 0) continue;
         const uint32_t bit = 1u << (q2 & 31);
         if (atomicOr(&seen[q2 >> 5], bit) & bit) continue;
-        bool skip = false;
-        for (int j = 0; j < nop && !skip; ++j) {
-            const int q2p = m.rot[(size_t)ops[j] * m.n_full + q2];
-            if (q2p >= 0 && q2p < q2) skip = true;
-        }
-        if (skip) continue;
+        const int32_t *im = o.img + (size_t)k * m.n_op;
         for (int b2 = 0; b2 < n; ++b2) {
             double buf = 0.0;
             int nn = 0;
             for (int j = 0; j < nop; ++j) {
-                const int q2p = m.rot[(size_t)ops[j] * m.n_full + q2];
+                const int q2p = im[j];
                 if (q2p < 0) continue;
                 const double v = odr[(int64_t)q2p * n + b2];
                 if (v > 0.0) {
@@ -127,48 +172,43 @@ __global__ void k_sym_distribute(MeshDev m, const int32_t *row_q1, const int64_t
             if (nn == 0) continue;
             const double avg = buf / (double)nn;
             for (int j = 0; j < nop; ++j) {
-                const int q2p = m.rot[(size_t)ops[j] * m.n_full + q2];
+                const int q2p = im[j];
                 if (q2p < 0) continue;
                 odr[(int64_t)q2p * n + b2] = avg;
             }
         }
     }
+    if (xi == nullptr) return;
     __syncthreads();
     double *xr = xi + (int64_t)r * ld;
     for (int64_t j = threadIdx.x; j < ld; j += blockDim.x) xr[j] += odr[j];
 }
 
-// symmetrize_scatmat (scattering.f90:296-357). One CTA per row, one thread per q2 orbit.
-__global__ void k_sym_scatmat(MeshDev m, const int32_t *row_q1, double *xi) {
+// symmetrize_scatmat (scattering.f90:296-357): one thread per (row, orbit, mode).
+__global__ void k_sym_scatmat(MeshDev m, OrbitDev o, const int32_t *row_q1, double *xi) {
     const int n = m.n_mode;
     const int r = blockIdx.y;
-    const int q2 = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q2 >= m.n_full) return;
     const int q1 = row_q1[r];
-    const int nop = m.irr_nop[q1];
-    const int32_t *ops = m.irr_ops + (size_t)q1 * m.n_op;
-    double *xr = xi + (int64_t)r * m.n_full * n;
-    int cnt = 0;
-    for (int j = 0; j < nop; ++j) {
-        const int q2p = m.rot[(size_t)ops[j] * m.n_full + q2];
-        if (q2p < 0) continue;
-        if (q2p < q2) return;
-        ++cnt;
-    }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nrep = o.rep_ptr[q1 + 1] - o.rep_ptr[q1];
+    if (i >= nrep * n) return;
+    const int k = o.rep_ptr[q1] + i / n, b2 = i % n;
+    const int cnt = o.cnt[k];
     if (cnt == 0) return;
-    for (int b2 = 0; b2 < n; ++b2) {
-        double buf = 0.0;
-        for (int j = 0; j < nop; ++j) {
-            const int q2p = m.rot[(size_t)ops[j] * m.n_full + q2];
-            if (q2p < 0) continue;
-            buf += xr[(int64_t)q2p * n + b2];
-        }
-        buf /= (double)cnt;
-        for (int j = 0; j < nop; ++j) {
-            const int q2p = m.rot[(size_t)ops[j] * m.n_full + q2];
-            if (q2p < 0) continue;
-            xr[(int64_t)q2p * n + b2] = buf;
-        }
+    const int nop = m.irr_nop[q1];
+    const int32_t *im = o.img + (size_t)k * m.n_op;
+    double *xr = xi + (int64_t)r * m.n_full * n;
+    double buf = 0.0;
+    for (int j = 0; j < nop; ++j) {
+        const int q2p = im[j];
+        if (q2p < 0) continue;
+        buf += xr[(int64_t)q2p * n + b2];
+    }
+    buf /= (double)cnt;
+    for (int j = 0; j < nop; ++j) {
+        const int q2p = im[j];
+        if (q2p < 0) continue;
+        xr[(int64_t)q2p * n + b2] = buf;
     }
 }
 
@@ -218,22 +258,45 @@ cudaError_t launch_isotope(const MeshDev &m, const PhononDev &ph, const RowsDev 
     return cudaGetLastError();
 }
 
-cudaError_t launch_sym_distribute(const MeshDev &m, int32_t n_row, const int32_t *row_q1, const int64_t *ptr,
-                                  const int32_t *list, double *od, double *xi, cudaStream_t s) {
+namespace {
+__global__ void k_rep_ptr(const int32_t *scan, int32_t n_irr, int32_t n_full, int32_t *rep_ptr) {
+    const int q1 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q1 <= n_irr) rep_ptr[q1] = scan[(size_t)q1 * n_full];
+}
+}  // namespace
+
+cudaError_t launch_orbit_flag(const MeshDev &m, int32_t *flag, cudaStream_t s) {
+    dim3 grid((unsigned)((m.n_full + 127) / 128), (unsigned)m.n_irr);
+    k_orbit_flag<<<grid, 128, 0, s>>>(m, flag);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_orbit_fill(const MeshDev &m, const int32_t *flag, const int32_t *scan, OrbitDev &o,
+                              cudaStream_t s) {
+    dim3 grid((unsigned)((m.n_full + 127) / 128), (unsigned)m.n_irr);
+    k_orbit_fill<<<grid, 128, 0, s>>>(m, flag, scan, const_cast<int32_t *>(o.orb_of), const_cast<int32_t *>(o.rep),
+                                      const_cast<int32_t *>(o.img), const_cast<int32_t *>(o.cnt));
+    k_rep_ptr<<<(m.n_irr + 1 + 127) / 128, 128, 0, s>>>(scan, m.n_irr, m.n_full, const_cast<int32_t *>(o.rep_ptr));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sym_distribute(const MeshDev &m, const OrbitDev &o, int32_t n_row, const int32_t *row_q1,
+                                  const int64_t *ptr, const int32_t *list, double *od, double *xi, cudaStream_t s) {
     if (n_row <= 0) return cudaSuccess;
     const size_t sm = sizeof(uint32_t) * (size_t)((m.n_full + 31) / 32);
     if (sm > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k_sym_distribute, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
     }
-    k_sym_distribute<<<n_row, 256, sm, s>>>(m, row_q1, ptr, list, od, xi);
+    k_sym_distribute<<<n_row, 256, sm, s>>>(m, o, row_q1, ptr, list, od, xi);
     return cudaGetLastError();
 }
 
-cudaError_t launch_sym_scatmat(const MeshDev &m, int32_t n_row, const int32_t *row_q1, double *xi, cudaStream_t s) {
-    if (n_row <= 0) return cudaSuccess;
-    dim3 grid((unsigned)((m.n_full + 127) / 128), (unsigned)n_row);
-    k_sym_scatmat<<<grid, 128, 0, s>>>(m, row_q1, xi);
+cudaError_t launch_sym_scatmat(const MeshDev &m, const OrbitDev &o, int32_t n_row, const int32_t *row_q1, double *xi,
+                               cudaStream_t s) {
+    if (n_row <= 0 || o.max_rep <= 0) return cudaSuccess;
+    dim3 grid((unsigned)(((int64_t)o.max_rep * m.n_mode + 127) / 128), (unsigned)n_row);
+    k_sym_scatmat<<<grid, 128, 0, s>>>(m, o, row_q1, xi);
     return cudaGetLastError();
 }
 

@@ -15,6 +15,11 @@
 // lattice vectors, so q.lv = sum_d g_d lv_d / N_d and exp(-2 pi i q.lv) is one entry of a
 // table of exp(-2 pi i K / L), L = lcm of the mesh dimensions.
 //
+// The delta weights stay FP64 as in the reference, but GB300's FP64 pipe is narrow, so
+// every mode triplet is first screened in FP32 against the 8-sigma window of lo_gauss
+// with a safety margin; only triplets that may fall inside it take the exact FP64 path,
+// which reproduces the reference's arithmetic (same window test, same formulas).
+//
 // Everything for one triplet lives in shared memory: P and T (two n^3 complex buffers),
 // the three scaled eigenvector matrices, the phase chunk and per-mode scalars. Precision R
 // is double (FP64 path) or float (mixed path: FP32 pretransform and contraction, FP64
@@ -45,14 +50,14 @@ struct CT<float> {
 };
 
 template <typename C>
-__device__ __forceinline__ C cmake(double x, double y);
+__device__ __forceinline__ C czero();
 template <>
-__device__ __forceinline__ double2 cmake<double2>(double x, double y) {
-    return make_double2(x, y);
+__device__ __forceinline__ double2 czero<double2>() {
+    return make_double2(0.0, 0.0);
 }
 template <>
-__device__ __forceinline__ float2 cmake<float2>(double x, double y) {
-    return make_float2((float)x, (float)y);
+__device__ __forceinline__ float2 czero<float2>() {
+    return make_float2(0.f, 0.f);
 }
 
 template <typename C>
@@ -63,22 +68,24 @@ __device__ __forceinline__ void cfma(C &acc, const C &a, const C &b) {
     acc.y = fma(a.y, b.x, acc.y);
 }
 
-// lo_gauss with the 8-sigma cutoff (gottochblandat_calculus.f90:268-288).
-__device__ __forceinline__ double lo_gauss(double x, double mu, double sigma) {
+__device__ __forceinline__ bool nonzero(double x) { return (__double_as_longlong(x) << 1) != 0; }
+
+// lo_gauss (gottochblandat_calculus.f90:268-288) with 1/sigma supplied.
+__device__ __forceinline__ double gauss(double x, double mu, double sigma, double invsig) {
     if (fabs(x - mu) > 8.0 * sigma) return 0.0;
-    const double invsig = 1.0 / sigma;
     return exp(-(x - mu) * (x - mu) * 0.5 * invsig * invsig) * kSqrt2PiInv * invsig;
 }
 
-__device__ __forceinline__ double adaptive_pair(const double *va, const double *vb, const double *rl) {
+template <typename T>
+__device__ __forceinline__ T adaptive_pair(const T *va, const T *vb, const double *rl) {
     // sqrt(maxval(matmul(va - vb, reclat)**2) * 0.5)
-    double m = 0.0;
+    T m = 0;
     for (int j = 0; j < 3; ++j) {
-        double s = 0.0;
-        for (int i = 0; i < 3; ++i) s += (va[i] - vb[i]) * rl[i + 3 * j];
-        m = fmax(m, s * s);
+        T s = 0;
+        for (int i = 0; i < 3; ++i) s += (va[i] - vb[i]) * (T)rl[i + 3 * j];
+        m = max(m, s * s);
     }
-    return sqrt(m * 0.5);
+    return sqrt(m * (T)0.5);
 }
 
 template <typename R>
@@ -104,28 +111,31 @@ __device__ __forceinline__ float2 twiddle_at<float2>(const Fc3Dev &fc, int k) {
 }
 
 template <typename C>
-__device__ __forceinline__ C egv_at(const PhononDev &ph, size_t i);
+__device__ __forceinline__ const C *egvs_ptr(const PhononDev &ph);
 template <>
-__device__ __forceinline__ double2 egv_at<double2>(const PhononDev &ph, size_t i) {
-    return ph.egv[i];
+__device__ __forceinline__ const double2 *egvs_ptr<double2>(const PhononDev &ph) {
+    return ph.egvs;
 }
 template <>
-__device__ __forceinline__ float2 egv_at<float2>(const PhononDev &ph, size_t i) {
-    return ph.egv32[i];
+__device__ __forceinline__ const float2 *egvs_ptr<float2>(const PhononDev &ph) {
+    return ph.egvs32;
 }
 
 // Shared-memory layout (bytes) for mode count n and complex size cs.
 struct Layout {
-    size_t om1, om2, om3, be2, be3, s1, s2, s3, v1, v2, v3, wrow, E1, E2, E3, A, B, ph, rowid, red, total;
+    size_t om1, om2, om3, inv1, be2, be3, s1, s2, s3, v1, v2, v3, wrow, r2, f32, E1, E2, E3, A, B, ph, rowid, red,
+        total;
 };
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 __host__ __device__ inline Layout make_layout(int n, int cs) {
     Layout L;
     size_t o = 0;
     const size_t dn = align16(sizeof(double) * n);
+    const size_t n2 = (size_t)n * n, n3 = n2 * n;
     L.om1 = o; o += dn;
     L.om2 = o; o += dn;
     L.om3 = o; o += dn;
+    L.inv1 = o; o += dn;
     L.be2 = o; o += dn;
     L.be3 = o; o += dn;
     L.s1 = o; o += dn;
@@ -135,7 +145,8 @@ __host__ __device__ inline Layout make_layout(int n, int cs) {
     L.v2 = o; o += 3 * dn;
     L.v3 = o; o += 3 * dn;
     L.wrow = o; o += dn;
-    const size_t n2 = (size_t)n * n, n3 = n2 * n;
+    L.r2 = o; o += align16(sizeof(double) * n2);
+    L.f32 = o; o += align16(sizeof(float) * n * 6);  // float copies: om1..3, s1..3
     L.E1 = o; o += align16(cs * n2);
     L.E2 = o; o += align16(cs * n2);
     L.E3 = o; o += align16(cs * n2);
@@ -162,6 +173,7 @@ __global__ void __launch_bounds__(((N * N + 31) / 32) * 32)
     double *om1 = (double *)(smem + L.om1);
     double *om2 = (double *)(smem + L.om2);
     double *om3 = (double *)(smem + L.om3);
+    double *inv1 = (double *)(smem + L.inv1);
     double *be2 = (double *)(smem + L.be2);
     double *be3 = (double *)(smem + L.be3);
     double *s1 = (double *)(smem + L.s1);
@@ -171,6 +183,9 @@ __global__ void __launch_bounds__(((N * N + 31) / 32) * 32)
     double *v2 = (double *)(smem + L.v2);
     double *v3 = (double *)(smem + L.v3);
     double *wrow = (double *)(smem + L.wrow);
+    double *R2 = (double *)(smem + L.r2);
+    float *fo1 = (float *)(smem + L.f32);
+    float *fo2 = fo1 + N, *fo3 = fo2 + N, *fs1 = fo3 + N, *fs2 = fs1 + N, *fs3 = fs2 + N;
     C *E1 = (C *)(smem + L.E1);
     C *E2 = (C *)(smem + L.E2);
     C *E3 = (C *)(smem + L.E3);
@@ -184,7 +199,10 @@ __global__ void __launch_bounds__(((N * N + 31) / 32) * 32)
     const PhononDev &P = a.ph;
     const Fc3Dev &fc = a.fc;
     const R *mwm = mwm_ptr<R>(fc);
+    const C *egvs = egvs_ptr<C>(P);
     const int64_t ld = (int64_t)m.n_full * N;
+    const int it = P.integrationtype;
+    const float sigfix32 = (float)P.sigma_fixed;
 
     for (int t = blockIdx.x; t < a.n_trip; t += gridDim.x) {
         const TripletRec rec = a.trip[t];
@@ -198,11 +216,18 @@ __global__ void __launch_bounds__(((N * N + 31) / 32) * 32)
             om1[b] = P.omega[(size_t)f1 * N + b];
             om2[b] = P.omega[(size_t)q2 * N + b];
             om3[b] = P.omega[(size_t)q3 * N + b];
+            inv1[b] = om1[b] > 0.0 ? 1.0 / om1[b] : 0.0;
             be2[b] = P.be[(size_t)i2 * N + b];
             be3[b] = P.be[(size_t)i3 * N + b];
             s1[b] = P.sigsq[(size_t)rec.q1 * N + b];
             s2[b] = P.sigsq[(size_t)i2 * N + b];
             s3[b] = P.sigsq[(size_t)i3 * N + b];
+            fo1[b] = (float)om1[b];
+            fo2[b] = (float)om2[b];
+            fo3[b] = (float)om3[b];
+            fs1[b] = (float)s1[b];
+            fs2[b] = (float)s2[b];
+            fs3[b] = (float)s3[b];
             for (int d = 0; d < 3; ++d) {
                 v1[b * 3 + d] = P.vel[((size_t)f1 * N + b) * 3 + d];
                 v2[b * 3 + d] = P.vel[((size_t)q2 * N + b) * 3 + d];
@@ -214,27 +239,15 @@ __global__ void __launch_bounds__(((N * N + 31) / 32) * 32)
             wrow[b] = r >= 0 ? a.rows.weight3[r] : 0.0;
         }
         for (int i = tid; i < nred && i < kMaxRed; i += bd) red[i] = a.red[rec.red_off + i];
-        __syncthreads();
         for (int i = tid; i < 3 * N2; i += bd) {
             const int which = i / N2, e = i % N2;
             const int r = e / N, b = e % N;  // element (r) of mode b
             const int q = which == 0 ? f1 : (which == 1 ? q2 : q3);
-            const double *om = which == 0 ? om1 : (which == 1 ? om2 : om3);
             C *E = which == 0 ? E1 : (which == 1 ? E2 : E3);
-            C v = egv_at<C>(P, ((size_t)q * N + b) * N + r);
-            const double w = om[b];
-            if (w < kFreqTolD) {
-                v.x = 0;
-                v.y = 0;
-            } else {
-                const R s = (R)(1.0 / sqrt(w));
-                v.x *= s;
-                v.y *= s;
-            }
-            E[r * N + b] = v;
+            E[r * N + b] = egvs[((size_t)q * N + b) * N + r];
         }
         // ---- K2: pretransform into A ----
-        for (int i = tid; i < N3; i += bd) A[i] = cmake<C>(0.0, 0.0);
+        for (int i = tid; i < N3; i += bd) A[i] = czero<C>();
         int gi2[3], gi3[3];
         {
             const int n12 = m.grid[1] * m.grid[2];
@@ -278,7 +291,7 @@ __global__ void __launch_bounds__(((N * N + 31) / 32) * 32)
             const int bc = tid;
             C acc[N];
 #pragma unroll
-            for (int b1 = 0; b1 < N; ++b1) acc[b1] = cmake<C>(0.0, 0.0);
+            for (int b1 = 0; b1 < N; ++b1) acc[b1] = czero<C>();
 #pragma unroll 3
             for (int aa = 0; aa < N; ++aa) {
                 const C p = A[aa * N2 + bc];
@@ -293,7 +306,7 @@ __global__ void __launch_bounds__(((N * N + 31) / 32) * 32)
             const int b1 = tid / N, c = tid % N;
             C acc[N];
 #pragma unroll
-            for (int b2 = 0; b2 < N; ++b2) acc[b2] = cmake<C>(0.0, 0.0);
+            for (int b2 = 0; b2 < N; ++b2) acc[b2] = czero<C>();
 #pragma unroll 3
             for (int b = 0; b < N; ++b) {
                 const C tv = B[(b1 * N + b) * N + c];
@@ -304,13 +317,13 @@ __global__ void __launch_bounds__(((N * N + 31) / 32) * 32)
             for (int b2 = 0; b2 < N; ++b2) A[(b1 * N + b2) * N + c] = acc[b2];
         }
         __syncthreads();
-        // ---- Psi and K4 epilogue: F[b1][b2][b3] into B (as doubles) ----
+        // ---- Psi and K4 epilogue: F[b1][b2][b3] into B (as doubles), R2 = sum over b3 ----
         double *F = (double *)B;
         if (tid < N2) {
             const int b1 = tid / N, b2 = tid % N;
             C acc[N];
 #pragma unroll
-            for (int b3 = 0; b3 < N; ++b3) acc[b3] = cmake<C>(0.0, 0.0);
+            for (int b3 = 0; b3 < N; ++b3) acc[b3] = czero<C>();
 #pragma unroll 3
             for (int c = 0; c < N; ++c) {
                 const C tv = A[(b1 * N + b2) * N + c];
@@ -319,54 +332,82 @@ __global__ void __launch_bounds__(((N * N + 31) / 32) * 32)
             }
             const int row = rowid[b1];
             const double o1 = om1[b1], o2 = om2[b2];
+            const float f_o1 = fo1[b1], f_o2 = fo2[b2];
             const double perm = (q2 == q3) ? 1.0 : 2.0;
             const bool skip12 = row < 0 || o2 < kFreqTolD || fabs(o1 - o2) < kFreqTolD;
+            double r2 = 0.0;
 #pragma unroll
             for (int b3 = 0; b3 < N; ++b3) {
                 double f = 0.0;
                 const double o3 = om3[b3];
                 if (!skip12 && !(o3 < kFreqTolD) && !(fabs(o1 - o3) < kFreqTolD || fabs(o2 - o3) < kFreqTolD)) {
-                    double sigma;
-                    if (P.integrationtype == 1) {
-                        sigma = P.sigma_fixed;
-                    } else if (P.integrationtype == 2) {
-                        sigma = sqrt(s1[b1] + s2[b2] + s3[b3]);
-                    } else {
-                        sigma = adaptive_pair(v1 + 3 * b1, v2 + 3 * b2, P.reclat_g) / 3.0;
-                        sigma += adaptive_pair(v1 + 3 * b1, v3 + 3 * b3, P.reclat_g) / 3.0;
-                        sigma += adaptive_pair(v2 + 3 * b2, v3 + 3 * b3, P.reclat_g) / 3.0;
-                        sigma += P.thresh_sigma;
+                    // FP32 screen: the nearest of the four Gaussian centres against 8 sigma,
+                    // with a relative margin and an absolute margin of the FP32 rounding.
+                    const float f_o3 = fo3[b3];
+                    float sg = 0.f;
+                    if (it == 1) {
+                        sg = sigfix32;
+                    } else if (it == 2) {
+                        sg = sqrtf(fs1[b1] + fs2[b2] + fs3[b3]);
                     }
-                    const double d0 = lo_gauss(o1, -o2 + o3, sigma) - lo_gauss(o1, o2 - o3, sigma);
-                    const double d1 = lo_gauss(o1, o2 + o3, sigma) - lo_gauss(o1, -o2 - o3, sigma);
-                    if (d0 != 0.0 || d1 != 0.0) {
-                        const double cr = (double)acc[b3].x, ci = (double)acc[b3].y;
-                        const double psisq = kThreePhononPrefactor * (cr * cr + ci * ci) * wrow[b1];
-                        const double n2 = be2[b2], n3 = be3[b3];
-                        const double plf0 = n2 - n3;
-                        const double plf1 = n2 + n3 + 1.0;
-                        const double f0 = perm * psisq * plf0 * d0;
-                        const double f1 = perm * psisq * plf1 * d1;
-                        f = f0 + f1;
+                    // One bit per Gaussian of get_dirac that may lie inside its window; the
+                    // velocity-difference width of -it 6 can cancel in FP32, so it is not screened.
+                    const float win = 8.0f * sg * 1.001f + 1e-6f * (f_o1 + f_o2 + f_o3);
+                    unsigned live = 15u;
+                    if (it != 6) {
+                        live = (fabsf(f_o1 + f_o2 - f_o3) <= win ? 1u : 0u) | (fabsf(f_o1 - f_o2 + f_o3) <= win ? 2u : 0u) |
+                               (fabsf(f_o1 - f_o2 - f_o3) <= win ? 4u : 0u) | (f_o1 + f_o2 + f_o3 <= win ? 8u : 0u);
+                    }
+                    if (live) {
+                        double sigma, invsig;
+                        if (it == 1) {
+                            sigma = P.sigma_fixed;
+                            invsig = 1.0 / sigma;
+                        } else if (it == 2) {
+                            const double s = s1[b1] + s2[b2] + s3[b3];
+                            invsig = rsqrt(s);
+                            sigma = s * invsig;
+                        } else {
+                            sigma = adaptive_pair<double>(v1 + 3 * b1, v2 + 3 * b2, P.reclat_g) / 3.0;
+                            sigma += adaptive_pair<double>(v1 + 3 * b1, v3 + 3 * b3, P.reclat_g) / 3.0;
+                            sigma += adaptive_pair<double>(v2 + 3 * b2, v3 + 3 * b3, P.reclat_g) / 3.0;
+                            sigma += P.thresh_sigma;
+                            invsig = 1.0 / sigma;
+                        }
+                        const double ga = (live & 1u) ? gauss(o1, -o2 + o3, sigma, invsig) : 0.0;
+                        const double gb = (live & 2u) ? gauss(o1, o2 - o3, sigma, invsig) : 0.0;
+                        const double gc = (live & 4u) ? gauss(o1, o2 + o3, sigma, invsig) : 0.0;
+                        const double gd = (live & 8u) ? gauss(o1, -o2 - o3, sigma, invsig) : 0.0;
+                        const double d0 = ga - gb;
+                        const double d1 = gc - gd;
+                        if (nonzero(d0) || nonzero(d1)) {
+                            const double cr = (double)acc[b3].x, ci = (double)acc[b3].y;
+                            const double psisq = kThreePhononPrefactor * (cr * cr + ci * ci) * wrow[b1];
+                            const double n2 = be2[b2], n3 = be3[b3];
+                            const double plf0 = n2 - n3;
+                            const double plf1 = n2 + n3 + 1.0;
+                            const double f0 = perm * psisq * plf0 * d0;
+                            const double f1 = perm * psisq * plf1 * d1;
+                            f = f0 + f1;
+                            r2 += f;
+                        }
                     }
                 }
                 F[(b1 * N + b2) * N + b3] = f;
             }
+            R2[tid] = r2;
         }
         __syncthreads();
-        // ---- reductions over b3 (R2) and b2 (R3) into A (as doubles) ----
-        double *R2 = (double *)A;
-        double *R3 = R2 + N2;
-        for (int i = tid; i < 2 * N2; i += bd) {
+        // ---- R3 = sum over b2, into A (as doubles); Gamma per b1 ----
+        double *R3 = (double *)A;
+        for (int e = tid; e < N2; e += bd) {
+            const int b1 = e / N, b3 = e % N;
             double s = 0.0;
-            if (i < N2) {
-                for (int b3 = 0; b3 < N; ++b3) s += F[i * N + b3];
-                R2[i] = s;
-            } else {
-                const int e = i - N2, b1 = e / N, b3 = e % N;
-                for (int b2 = 0; b2 < N; ++b2) s += F[(b1 * N + b2) * N + b3];
-                R3[e] = s;
+            for (int b2 = 0; b2 < N; ++b2) {
+                const double f = F[(b1 * N + b2) * N + b3];
+                if (nonzero(f)) s += f;
             }
+            R3[e] = s;
         }
         __syncthreads();
         if (tid < N) {
@@ -374,7 +415,7 @@ __global__ void __launch_bounds__(((N * N + 31) / 32) * 32)
             if (row >= 0) {
                 double g = 0.0;
                 for (int b2 = 0; b2 < N; ++b2) g += R2[tid * N + b2];
-                if (g != 0.0) atomicAdd(a.gamma + row, (double)nred * g);
+                if (nonzero(g)) atomicAdd(a.gamma + row, (double)nred * g);
             }
         }
         for (int i = tid; i < 2 * N2 * nred; i += bd) {
@@ -384,14 +425,14 @@ __global__ void __launch_bounds__(((N * N + 31) / 32) * 32)
                 const int b1 = e / N, b2 = e % N;
                 const int row = rowid[b1];
                 const double v = R2[e];
-                if (row >= 0 && v != 0.0)
-                    atomicAdd(a.od + row * ld + (int64_t)pr.x * N + b2, 2.0 * v * om2[b2] / om1[b1]);
+                if (row >= 0 && nonzero(v))
+                    atomicAdd(a.od + row * ld + (int64_t)pr.x * N + b2, 2.0 * v * om2[b2] * inv1[b1]);
             } else {
                 const int e3 = e - N2, b1 = e3 / N, b3 = e3 % N;
                 const int row = rowid[b1];
                 const double v = R3[e3];
-                if (row >= 0 && v != 0.0)
-                    atomicAdd(a.od + row * ld + (int64_t)pr.y * N + b3, 2.0 * v * om3[b3] / om1[b1]);
+                if (row >= 0 && nonzero(v))
+                    atomicAdd(a.od + row * ld + (int64_t)pr.y * N + b3, 2.0 * v * om3[b3] * inv1[b1]);
             }
         }
         __syncthreads();

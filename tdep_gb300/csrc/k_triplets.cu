@@ -155,7 +155,7 @@ __device__ int quartet_images(const MeshDev &m, int q1, int q2, int q3, int q4, 
     return cnt;
 }
 
-__global__ void k_triplet_count(MeshDev m, const int2 *cand, int32_t n_cand, int32_t *n_trip, int32_t *n_red,
+__global__ void k_triplet_count(MeshDev m, const int4 *cand, int32_t n_cand, int32_t *n_trip, int32_t *n_red,
                                 int32_t *status) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n_cand) return;
@@ -177,7 +177,7 @@ __global__ void k_triplet_count(MeshDev m, const int2 *cand, int32_t n_cand, int
     n_red[c] = nr;
 }
 
-__global__ void k_triplet_fill(MeshDev m, const int2 *cand, int32_t n_cand, const int32_t *trip_off,
+__global__ void k_triplet_fill(MeshDev m, const int4 *cand, int32_t n_cand, const int32_t *trip_off,
                                const int32_t *red_off, TripletRec *trip, int2 *red) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n_cand) return;
@@ -189,7 +189,7 @@ __global__ void k_triplet_fill(MeshDev m, const int2 *cand, int32_t n_cand, cons
     r.q1 = q1;
     r.q2 = q2;
     r.q3 = q3;
-    r.cand = c;
+    r.cand = cand[c].z;
     r.red_off = red_off[c];
     r.red_cnt = k;
     trip[trip_off[c]] = r;
@@ -309,14 +309,14 @@ cudaError_t exclusive_scan_i32(const int32_t *in, int32_t *out, int32_t n, int32
     return cudaGetLastError();
 }
 
-cudaError_t launch_triplet_count(const MeshDev &m, const int2 *cand, int32_t n_cand, int32_t *n_trip,
+cudaError_t launch_triplet_count(const MeshDev &m, const int4 *cand, int32_t n_cand, int32_t *n_trip,
                                  int32_t *n_red, int32_t *status, cudaStream_t s) {
     if (n_cand <= 0) return cudaSuccess;
     k_triplet_count<<<(n_cand + 127) / 128, 128, 0, s>>>(m, cand, n_cand, n_trip, n_red, status);
     return cudaGetLastError();
 }
 
-cudaError_t launch_triplet_fill(const MeshDev &m, const int2 *cand, int32_t n_cand, const int32_t *trip_off,
+cudaError_t launch_triplet_fill(const MeshDev &m, const int4 *cand, int32_t n_cand, const int32_t *trip_off,
                                 const int32_t *red_off, TripletRec *trip, int2 *red, cudaStream_t s) {
     if (n_cand <= 0) return cudaSuccess;
     k_triplet_fill<<<(n_cand + 127) / 128, 128, 0, s>>>(m, cand, n_cand, trip_off, red_off, trip, red);

@@ -161,7 +161,7 @@ int main(int argc, char **argv) {
     ql.list4a = l4a.data();
     ql.list4b = l4b.data();
     std::vector<double> lw(cap), qs(cap);
-    double stats[4];
+    double stats[10];
     const auto t1 = std::chrono::steady_clock::now();
     st = tdg_scattering(ctx, &o, &ql, lw.data(), qs.data(), stats);
     if (st) return die(st);

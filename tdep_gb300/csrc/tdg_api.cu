@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -89,7 +90,8 @@ struct tdg_ctx {
     int device = 0;
     int n_sm = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    int32_t *h_tot = nullptr;  // pinned host word pair for the enumeration totals
     // host copy of the problem
     int na = 0, n = 0, nop = 0, N = 0, nirr = 0;
     int grid[3] = {0, 0, 0};
@@ -100,8 +102,8 @@ struct tdg_ctx {
     // device copies
     DevBuf<int32_t> rot, d_irr_full, d_full_irr, d_irr_nop, d_irr_ops;
     DevBuf<double> d_omega, d_vel, d_be, d_sigsq, d_disorder;
-    DevBuf<double2> d_egv;
-    DevBuf<float2> d_egv32;
+    DevBuf<double2> d_egv, d_egvs;
+    DevBuf<float2> d_egvs32;
     DevBuf<int32_t> fc3_blk, fc3_lv, fc4_blk, fc4_lv;
     DevBuf<double> fc3_mwm, fc4_mwm;
     DevBuf<float> fc3_mwm32, fc4_mwm32;
@@ -113,9 +115,19 @@ struct tdg_ctx {
     std::vector<int32_t> row_q1, row_b1;
     DevBuf<int32_t> d_row_q1, d_row_b1, d_rowidx;
     DevBuf<double> d_w3, d_w4, d_gamma, d_xi, d_od;
+    // orbits of the little groups (built once per context)
+    DevBuf<int32_t> d_orb_rep_ptr, d_orb_rep, d_orb_img, d_orb_cnt, d_orb_of;
+    OrbitDev orbits{};
     DevBuf<int32_t> d_status;
     bool have_scattering = false;
     std::vector<double> linewidth, qs, F0, Fn;  // irr-point arrays
+    // enumeration and sample buffers, kept across calls (they only grow)
+    DevBuf<int4> d_cand;
+    DevBuf<uint32_t> d_mask;
+    DevBuf<int32_t> d_nt, d_nrd, d_toff, d_roff, d_tmp, d_list3;
+    DevBuf<int64_t> d_ptr3;
+    DevBuf<TripletRec> d_trip;
+    DevBuf<int2> d_red;
     // BTE buffers
     DevBuf<double> d_fbb, d_buf;
 
@@ -253,9 +265,12 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
     if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return fail(set_error(kErrDevice, "device query failed"));
     if (prop.major < 10) return fail(set_error(kErrDevice, "device is not Blackwell (sm_100 family required)"));
     c->n_sm = prop.multiProcessorCount;
-    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess)
-        return fail(set_error(kErrDevice, "stream/event creation failed"));
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(set_error(kErrDevice, "stream creation failed"));
+    for (auto &x : c->ev)
+        if (cudaEventCreate(&x) != cudaSuccess) return fail(set_error(kErrDevice, "event creation failed"));
+    if (cudaMallocHost(&c->h_tot, 2 * sizeof(int32_t)) != cudaSuccess)
+        return fail(set_error(kErrDevice, "pinned allocation failed"));
     c->na = p->n_atom;
     c->n = p->n_mode;
     c->nop = p->n_op;
@@ -293,11 +308,19 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
     for (int i = 0; i < c->nirr; ++i) irr_full0[i] = c->irr_full[i] - 1;
     for (int i = 0; i < c->N; ++i) full_irr0[i] = c->full_irr[i] - 1;
     for (size_t i = 0; i < irr_ops0.size(); ++i) irr_ops0[i] = c->irr_ops[i] > 0 ? c->irr_ops[i] - 1 : -1;
-    std::vector<double2> egv(nm * c->n);
-    std::vector<float2> egv32(nm * c->n);
-    for (size_t i = 0; i < egv.size(); ++i) {
-        egv[i] = make_double2(p->egv[2 * i], p->egv[2 * i + 1]);
-        egv32[i] = make_float2((float)p->egv[2 * i], (float)p->egv[2 * i + 1]);
+    // Eigenvectors as stored, and scaled by 1/sqrt(omega) as the scattering routines use
+    // them (egv(:,b)/sqrt(om), scattering_threephonon.f90:67,93,102), once per mode.
+    std::vector<double2> egv(nm * c->n), egvs(nm * c->n);
+    std::vector<float2> egvs32(nm * c->n);
+    for (size_t qb = 0; qb < nm; ++qb) {
+        const double om = c->omega[qb];
+        const double sq = om < kFreqTol ? 0.0 : std::sqrt(om);
+        for (int r = 0; r < c->n; ++r) {
+            const size_t i = qb * c->n + r;
+            egv[i] = make_double2(p->egv[2 * i], p->egv[2 * i + 1]);
+            egvs[i] = om < kFreqTol ? make_double2(0.0, 0.0) : make_double2(egv[i].x / sq, egv[i].y / sq);
+            egvs32[i] = make_float2((float)egvs[i].x, (float)egvs[i].y);
+        }
     }
     // Force constants sorted by atom block (a1,a2,a3).
     const int na = c->na;
@@ -362,7 +385,8 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
     chk(c->d_omega.upload(c->omega.data(), c->omega.size(), s));
     chk(c->d_vel.upload(c->vel.data(), c->vel.size(), s));
     chk(c->d_egv.upload(egv.data(), egv.size(), s));
-    chk(c->d_egv32.upload(egv32.data(), egv32.size(), s));
+    chk(c->d_egvs.upload(egvs.data(), egvs.size(), s));
+    chk(c->d_egvs32.upload(egvs32.data(), egvs32.size(), s));
     chk(c->d_disorder.upload(c->disorder.data(), c->disorder.size(), s));
     chk(c->fc3_blk.upload(blk_ptr3.data(), blk_ptr3.size(), s));
     chk(c->fc3_lv.upload(lv3.data(), lv3.size(), s));
@@ -377,6 +401,41 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
     chk(c->d_status.alloc(1));
     chk(cudaStreamSynchronize(s));
     if (e != cudaSuccess) return fail(set_error(kErrDevice, std::string("upload failed: ") + cudaGetErrorString(e)));
+    {
+        // Orbit tables: flags, global scan over (q1, q2), fill; representatives per q1.
+        const int32_t nflag = c->nirr * c->N;
+        if ((int64_t)c->nirr * c->N >= (int64_t)1 << 31) return fail(set_error(kErrBadDim, "mesh too large"));
+        DevBuf<int32_t> flag, scan, tmp;
+        chk(flag.alloc(nflag));
+        chk(scan.alloc(nflag + 1));
+        chk(tmp.alloc(exclusive_scan_tmp_elems(nflag)));
+        chk(c->d_orb_rep_ptr.alloc(c->nirr + 1));
+        chk(c->d_orb_of.alloc(nflag));
+        if (e != cudaSuccess) return fail(set_error(kErrDevice, std::string("allocation failed: ") + cudaGetErrorString(e)));
+        const MeshDev mesh = c->mesh();
+        chk(launch_orbit_flag(mesh, flag.p, s));
+        chk(exclusive_scan_i32(flag.p, scan.p, nflag, tmp.p, s));
+        int32_t nrep = 0;
+        chk(cudaMemcpyAsync(&nrep, scan.p + nflag, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        chk(cudaStreamSynchronize(s));
+        chk(c->d_orb_rep.alloc(nrep));
+        chk(c->d_orb_img.alloc((size_t)nrep * c->nop));
+        chk(c->d_orb_cnt.alloc(nrep));
+        if (e != cudaSuccess) return fail(set_error(kErrDevice, std::string("orbit tables: ") + cudaGetErrorString(e)));
+        c->orbits.rep_ptr = c->d_orb_rep_ptr.p;
+        c->orbits.rep = c->d_orb_rep.p;
+        c->orbits.img = c->d_orb_img.p;
+        c->orbits.cnt = c->d_orb_cnt.p;
+        c->orbits.orb_of = c->d_orb_of.p;
+        chk(launch_orbit_fill(mesh, flag.p, scan.p, c->orbits, s));
+        std::vector<int32_t> rp(c->nirr + 1);
+        chk(cudaMemcpyAsync(rp.data(), c->d_orb_rep_ptr.p, sizeof(int32_t) * rp.size(), cudaMemcpyDeviceToHost, s));
+        chk(cudaStreamSynchronize(s));
+        if (e != cudaSuccess) return fail(set_error(kErrDevice, std::string("orbit tables: ") + cudaGetErrorString(e)));
+        int mx = 0;
+        for (int q = 0; q < c->nirr; ++q) mx = std::max(mx, rp[q + 1] - rp[q]);
+        c->orbits.max_rep = mx;
+    }
     *out = c;
     return kOk;
 }
@@ -385,8 +444,9 @@ extern "C" void tdg_destroy(tdg_ctx *c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    if (c->ev0) cudaEventDestroy(c->ev0);
-    if (c->ev1) cudaEventDestroy(c->ev1);
+    for (auto &x : c->ev)
+        if (x) cudaEventDestroy(x);
+    if (c->h_tot) cudaFreeHost(c->h_tot);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -463,7 +523,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         st = check_list("four-phonon sample", nr, ql->ptr4, ql->list4b, N);
         if (st) return st;
         if (c->n_fc4 < 1) return set_error(kErrParam, "four-phonon scattering requested without force constants");
-        if (n > 18) return set_error(kErrParam, "this build's four-phonon kernel supports up to 6 atoms");
+        return set_error(kErrParam, "four-phonon scattering is not available in this build");
     }
     c->n_row = nr;
     c->row_q1.assign(ql->row_q1, ql->row_q1 + nr);
@@ -496,7 +556,8 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     PhononDev ph;
     ph.omega = c->d_omega.p;
     ph.egv = c->d_egv.p;
-    ph.egv32 = c->d_egv32.p;
+    ph.egvs = c->d_egvs.p;
+    ph.egvs32 = c->d_egvs32.p;
     ph.vel = c->d_vel.p;
     std::memcpy(ph.reclat_g, reclat_g, sizeof(reclat_g));
     ph.sigma_fixed = o->sigma * kFreqTHzToHartree;
@@ -510,54 +571,15 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         rb1[r] = c->row_b1[r] - 1;
         rowidx[(size_t)rq1[r] * n + rb1[r]] = r;
         if (o->thirdorder) w3[r] = 1.0 / (double)(ql->ptr3[r + 1] - ql->ptr3[r]);
-        if (o->fourthorder) {
-            const double np4 = (double)(ql->ptr4[r + 1] - ql->ptr4[r]);
-            w4[r] = 1.0 / np4;
-        }
     }
-    cudaError_t e = cudaSuccess;
-    auto chk = [&](cudaError_t x) {
-        if (e == cudaSuccess) e = x;
-    };
-    chk(c->d_be.upload(be.data(), be.size(), s));
-    chk(c->d_sigsq.upload(sigsq.data(), sigsq.size(), s));
-    chk(c->d_rowidx.upload(rowidx.data(), rowidx.size(), s));
-    chk(c->d_row_q1.upload(rq1.data(), rq1.size(), s));
-    chk(c->d_row_b1.upload(rb1.data(), rb1.size(), s));
-    chk(c->d_w3.upload(w3.data(), w3.size(), s));
-    chk(c->d_w4.upload(w4.data(), w4.size(), s));
-    const int64_t ld = (int64_t)N * n;
-    chk(c->d_xi.alloc((size_t)nr * ld));
-    chk(c->d_gamma.alloc(nr));
-    if (e != cudaSuccess) return set_error(kErrDevice, std::string("allocation failed: ") + cudaGetErrorString(e));
-    ph.be = c->d_be.p;
-    ph.sigsq = c->d_sigsq.p;
-    RowsDev rows;
-    rows.n_row = nr;
-    rows.rowidx = c->d_rowidx.p;
-    rows.weight3 = c->d_w3.p;
-    rows.weight4 = c->d_w4.p;
-    const MeshDev mesh = c->mesh();
-
-    CUDA_TRY(cudaEventRecord(c->ev0, s));
-    CUDA_TRY(cudaMemsetAsync(c->d_xi.p, 0, sizeof(double) * (size_t)nr * ld, s));
-    CUDA_TRY(cudaMemsetAsync(c->d_gamma.p, 0, sizeof(double) * nr, s));
-    CUDA_TRY(cudaMemsetAsync(c->d_status.p, 0, sizeof(int32_t), s));
-    double n_trip_total = 0, n_quart_total = 0, n_cand_total = 0;
-
-    if (o->isotope) {
-        CUDA_TRY(launch_isotope(mesh, ph, rows, c->d_row_q1.p, c->d_row_b1.p, c->d_disorder.p, c->na, c->d_gamma.p,
-                                c->d_xi.p, s));
-    }
-    if (o->thirdorder || o->fourthorder) {
-        CUDA_TRY(c->d_od.alloc((size_t)nr * ld));
-    }
+    // ---- three-phonon candidates: per q1 the union of its rows' samples; the set of
+    // rows sampling q2 is a bit mask, stored once in a table of distinct masks ----
+    std::vector<int4> cand;
+    std::vector<uint32_t> masks;
     if (o->thirdorder) {
-        // Candidates: per q1 the union of its rows' samples, with the set of rows as a mask.
-        std::vector<int2> cand;
-        std::vector<uint32_t> masks;
         std::vector<uint32_t> mark((size_t)N * 4, 0u);
         std::vector<int32_t> touched;
+        std::vector<std::array<uint32_t, 4>> table;
         int r0 = 0;
         for (int q1 = 0; q1 < nirr; ++q1) {
             int r1 = r0;
@@ -574,43 +596,92 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
             }
             std::sort(touched.begin(), touched.end());
             for (int q2 : touched) {
-                cand.push_back(make_int2(q1, q2));
                 uint32_t *mk = &mark[(size_t)q2 * 4];
-                masks.insert(masks.end(), mk, mk + 4);
+                const std::array<uint32_t, 4> key = {mk[0], mk[1], mk[2], mk[3]};
+                int id = -1;
+                for (int t = (int)table.size() - 1; t >= 0 && t >= (int)table.size() - 8; --t)
+                    if (table[t] == key) {
+                        id = t;
+                        break;
+                    }
+                if (id < 0) {
+                    id = (int)table.size();
+                    table.push_back(key);
+                }
+                cand.push_back(make_int4(q1, q2, id, 0));
                 mk[0] = mk[1] = mk[2] = mk[3] = 0u;
             }
             r0 = r1;
         }
-        const int32_t nc = (int32_t)cand.size();
-        n_cand_total += nc;
-        DevBuf<int2> d_cand;
-        DevBuf<uint32_t> d_mask;
-        DevBuf<int32_t> d_nt, d_nrd, d_toff, d_roff, d_tmp;
-        chk(d_cand.upload(cand.data(), cand.size(), s));
-        chk(d_mask.upload(masks.data(), masks.size(), s));
-        chk(d_nt.alloc(nc + 1));
-        chk(d_nrd.alloc(nc + 1));
-        chk(d_toff.alloc(nc + 1));
-        chk(d_roff.alloc(nc + 1));
-        chk(d_tmp.alloc(exclusive_scan_tmp_elems(nc)));
-        if (e != cudaSuccess) return set_error(kErrDevice, std::string("allocation failed: ") + cudaGetErrorString(e));
-        CUDA_TRY(launch_triplet_count(mesh, d_cand.p, nc, d_nt.p, d_nrd.p, c->d_status.p, s));
-        CUDA_TRY(exclusive_scan_i32(d_nt.p, d_toff.p, nc, d_tmp.p, s));
-        CUDA_TRY(exclusive_scan_i32(d_nrd.p, d_roff.p, nc, d_tmp.p, s));
-        int32_t tot[2] = {0, 0};
-        CUDA_TRY(cudaMemcpyAsync(&tot[0], d_toff.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-        CUDA_TRY(cudaMemcpyAsync(&tot[1], d_roff.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        for (const auto &t : table) masks.insert(masks.end(), t.begin(), t.end());
+    }
+    const int32_t nc = (int32_t)cand.size();
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t x) {
+        if (e == cudaSuccess) e = x;
+    };
+    chk(c->d_be.upload(be.data(), be.size(), s));
+    chk(c->d_sigsq.upload(sigsq.data(), sigsq.size(), s));
+    chk(c->d_rowidx.upload(rowidx.data(), rowidx.size(), s));
+    chk(c->d_row_q1.upload(rq1.data(), rq1.size(), s));
+    chk(c->d_row_b1.upload(rb1.data(), rb1.size(), s));
+    chk(c->d_w3.upload(w3.data(), w3.size(), s));
+    chk(c->d_w4.upload(w4.data(), w4.size(), s));
+    const int64_t ld = (int64_t)N * n;
+    chk(c->d_xi.alloc((size_t)nr * ld));
+    chk(c->d_gamma.alloc(nr));
+    if (o->thirdorder) {
+        chk(c->d_cand.upload(cand.data(), cand.size(), s));
+        chk(c->d_mask.upload(masks.data(), masks.size(), s));
+        chk(c->d_nt.alloc(nc + 1));
+        chk(c->d_nrd.alloc(nc + 1));
+        chk(c->d_toff.alloc(nc + 1));
+        chk(c->d_roff.alloc(nc + 1));
+        chk(c->d_tmp.alloc(exclusive_scan_tmp_elems(nc)));
+        chk(c->d_ptr3.upload(ql->ptr3, nr + 1, s));
+        chk(c->d_list3.upload(ql->list3, ql->ptr3[nr], s));
+    }
+    chk(cudaStreamSynchronize(s));
+    if (e != cudaSuccess) return set_error(kErrDevice, std::string("allocation/upload failed: ") + cudaGetErrorString(e));
+    ph.be = c->d_be.p;
+    ph.sigsq = c->d_sigsq.p;
+    RowsDev rows;
+    rows.n_row = nr;
+    rows.rowidx = c->d_rowidx.p;
+    rows.weight3 = c->d_w3.p;
+    rows.weight4 = c->d_w4.p;
+    const MeshDev mesh = c->mesh();
+
+    // ---- device pipeline; inputs are resident from here on ----
+    cudaEvent_t *ev = c->ev;
+    int launches = 0;
+    // Xi starts at zero and the three-phonon row terms accumulate into it directly: the
+    // per-order symmetrisation (od_terms > 0 filter) then runs on Xi in place, and the
+    // isotope terms, which the reference adds unsymmetrised, come after it.
+    CUDA_TRY(cudaEventRecord(ev[0], s));
+    CUDA_TRY(cudaMemsetAsync(c->d_xi.p, 0, sizeof(double) * (size_t)nr * ld, s));
+    CUDA_TRY(cudaMemsetAsync(c->d_gamma.p, 0, sizeof(double) * nr, s));
+    CUDA_TRY(cudaMemsetAsync(c->d_status.p, 0, sizeof(int32_t), s));
+    CUDA_TRY(cudaEventRecord(ev[1], s));
+    int32_t ntrip = 0, nred = 0;
+    if (o->thirdorder) {
+        CUDA_TRY(launch_triplet_count(mesh, c->d_cand.p, nc, c->d_nt.p, c->d_nrd.p, c->d_status.p, s));
+        CUDA_TRY(exclusive_scan_i32(c->d_nt.p, c->d_toff.p, nc, c->d_tmp.p, s));
+        CUDA_TRY(exclusive_scan_i32(c->d_nrd.p, c->d_roff.p, nc, c->d_tmp.p, s));
+        launches += 1 + 2 * 3;
+        int32_t *tot = c->h_tot;
+        CUDA_TRY(cudaMemcpyAsync(&tot[0], c->d_toff.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(cudaMemcpyAsync(&tot[1], c->d_roff.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         st = read_status(c);
         if (st) return st;
-        const int32_t ntrip = tot[0], nred = tot[1];
-        n_trip_total += ntrip;
-        DevBuf<TripletRec> d_trip;
-        DevBuf<int2> d_red;
-        chk(d_trip.alloc(ntrip));
-        chk(d_red.alloc(nred));
+        ntrip = tot[0];
+        nred = tot[1];
+        chk(c->d_trip.alloc(ntrip));
+        chk(c->d_red.alloc(nred));
         if (e != cudaSuccess) return set_error(kErrDevice, std::string("allocation failed: ") + cudaGetErrorString(e));
-        CUDA_TRY(launch_triplet_fill(mesh, d_cand.p, nc, d_toff.p, d_roff.p, d_trip.p, d_red.p, s));
-        CUDA_TRY(cudaMemsetAsync(c->d_od.p, 0, sizeof(double) * (size_t)nr * ld, s));
+        CUDA_TRY(launch_triplet_fill(mesh, c->d_cand.p, nc, c->d_toff.p, c->d_roff.p, c->d_trip.p, c->d_red.p, s));
+        ++launches;
+        CUDA_TRY(cudaEventRecord(ev[2], s));
         ThreePhArgs a;
         a.mesh = mesh;
         a.ph = ph;
@@ -623,36 +694,50 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         a.fc.mwm32 = c->fc3_mwm32.p;
         a.fc.twiddle = c->tw.p;
         a.fc.twiddle32 = c->tw32.p;
-        a.trip = d_trip.p;
+        a.trip = c->d_trip.p;
         a.n_trip = ntrip;
-        a.red = d_red.p;
-        a.cand_mask = d_mask.p;
+        a.red = c->d_red.p;
+        a.cand_mask = c->d_mask.p;
         a.gamma = c->d_gamma.p;
-        a.od = c->d_od.p;
+        a.od = c->d_xi.p;
         a.status = c->d_status.p;
         CUDA_TRY(launch_threephonon(a, o->precision, c->n_sm, s));
-        DevBuf<int64_t> d_ptr;
-        DevBuf<int32_t> d_list;
-        chk(d_ptr.upload(ql->ptr3, nr + 1, s));
-        chk(d_list.upload(ql->list3, ql->ptr3[nr], s));
-        if (e != cudaSuccess) return set_error(kErrDevice, std::string("upload failed: ") + cudaGetErrorString(e));
-        CUDA_TRY(launch_sym_distribute(mesh, nr, c->d_row_q1.p, d_ptr.p, d_list.p, c->d_od.p, c->d_xi.p, s));
-        CUDA_TRY(cudaStreamSynchronize(s));  // scoped buffers are released below
+        ++launches;
+        CUDA_TRY(cudaEventRecord(ev[3], s));
+        CUDA_TRY(launch_sym_distribute(mesh, c->orbits, nr, c->d_row_q1.p, c->d_ptr3.p, c->d_list3.p, c->d_xi.p,
+                                       nullptr, s));
+        ++launches;
+    } else {
+        CUDA_TRY(cudaEventRecord(ev[2], s));
+        CUDA_TRY(cudaEventRecord(ev[3], s));
     }
-    if (o->fourthorder) {
-        return set_error(kErrParam, "four-phonon scattering is not available in this build");
+    CUDA_TRY(cudaEventRecord(ev[4], s));
+    if (o->isotope) {
+        CUDA_TRY(launch_isotope(mesh, ph, rows, c->d_row_q1.p, c->d_row_b1.p, c->d_disorder.p, c->na, c->d_gamma.p,
+                                c->d_xi.p, s));
+        ++launches;
     }
-    // ---- gamma to host: boundary, degeneracy averaging (scattering.f90:244-292) ----
+    CUDA_TRY(cudaEventRecord(ev[5], s));
+    // ---- gamma to host; symmetrize_scatmat on the device meanwhile ----
     std::vector<double> gamma(nr);
     CUDA_TRY(cudaMemcpyAsync(gamma.data(), c->d_gamma.p, sizeof(double) * nr, cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(launch_sym_scatmat(mesh, nr, c->d_row_q1.p, c->d_xi.p, s));
-    CUDA_TRY(cudaEventRecord(c->ev1, s));
+    CUDA_TRY(launch_sym_scatmat(mesh, c->orbits, nr, c->d_row_q1.p, c->d_xi.p, s));
+    ++launches;
+    CUDA_TRY(cudaEventRecord(ev[6], s));
     CUDA_TRY(cudaStreamSynchronize(s));
     st = read_status(c);
     if (st) return st;
-    float ms = 0.f;
-    CUDA_TRY(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    float ms_total = 0.f, ms_iso = 0.f, ms_k1 = 0.f, ms_fused = 0.f, ms_sym = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&ms_total, ev[0], ev[6]));
+    CUDA_TRY(cudaEventElapsedTime(&ms_iso, ev[4], ev[5]));
+    CUDA_TRY(cudaEventElapsedTime(&ms_k1, ev[1], ev[2]));
+    CUDA_TRY(cudaEventElapsedTime(&ms_fused, ev[2], ev[3]));
+    float ms_s1 = 0.f, ms_s2 = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&ms_s1, ev[3], ev[4]));
+    CUDA_TRY(cudaEventElapsedTime(&ms_s2, ev[5], ev[6]));
+    ms_sym = ms_s1 + ms_s2;
 
+    // ---- boundary, degeneracy averaging (scattering.f90:244-292) ----
     std::vector<double> buf_lw((size_t)nirr * n, 0.0);
     for (int r = 0; r < nr; ++r) {
         double b = gamma[r];
@@ -694,12 +779,17 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     std::memcpy(linewidth, c->linewidth.data(), sizeof(double) * c->linewidth.size());
     if (qs_out) std::memcpy(qs_out, c->qs.data(), sizeof(double) * c->qs.size());
     if (stats) {
-        stats[0] = n_trip_total;
-        stats[1] = n_quart_total;
-        stats[2] = ms;
-        stats[3] = n_cand_total;
+        stats[0] = ntrip;
+        stats[1] = 0;
+        stats[2] = ms_total;
+        stats[3] = nc;
+        stats[4] = ms_k1;
+        stats[5] = ms_fused;
+        stats[6] = ms_sym;
+        stats[7] = ms_iso;
+        stats[8] = launches;
+        stats[9] = nred;
     }
-    c->d_od.release();
     c->have_scattering = true;
     return kOk;
 }
@@ -724,9 +814,9 @@ extern "C" int tdg_triplets(tdg_ctx *c, int32_t q1, const int32_t *sample, int64
     CUDA_TRY(cudaSetDevice(c->device));
     cudaStream_t s = c->stream;
     const int32_t nc = (int32_t)n;
-    std::vector<int2> cand(nc);
-    for (int32_t i = 0; i < nc; ++i) cand[i] = make_int2(q1 - 1, sample[i] - 1);
-    DevBuf<int2> d_cand;
+    std::vector<int4> cand(nc);
+    for (int32_t i = 0; i < nc; ++i) cand[i] = make_int4(q1 - 1, sample[i] - 1, 0, 0);
+    DevBuf<int4> d_cand;
     DevBuf<int32_t> d_nt, d_nrd, d_toff, d_roff, d_tmp;
     cudaError_t e = cudaSuccess;
     auto chk = [&](cudaError_t x) {

@@ -10,7 +10,7 @@ namespace tdg {
 struct TripletRec {
     int32_t q1;       // irreducible index of q1 (0-based)
     int32_t q2, q3;   // full-mesh indices (0-based)
-    int32_t cand;     // candidate index (for the row mask)
+    int32_t cand;     // index of its row mask (bit b1 set when row (q1,b1) samples q2)
     int32_t red_off;  // first equivalent triplet in the red list
     int32_t red_cnt;  // number of equivalent triplets (size(red_triplet,2))
 };
@@ -40,7 +40,8 @@ struct MeshDev {
 struct PhononDev {
     const double *omega;     // [n_full*n]
     const double2 *egv;      // [n_full*n*n], (q, b, r)
-    const float2 *egv32;     // same in FP32 (mixed precision)
+    const double2 *egvs;     // egv / sqrt(omega), 0 where omega < lo_freqtol
+    const float2 *egvs32;    // same in FP32 (mixed precision)
     const double *vel;       // [n_full*n*3]
     const double *be;        // [n_irr*n]
     const double *sigsq;     // [n_irr*n]
@@ -83,9 +84,9 @@ enum DevStatus : int32_t { kDevOk = 0, kDevBadIndex = 1, kDevOverflow = 2 };
 
 // ---- launch wrappers (each returns cudaError_t of the launch) ----
 // K1: count/fill passes of the irreducible-triplet enumeration.
-cudaError_t launch_triplet_count(const MeshDev &m, const int2 *cand, int32_t n_cand, int32_t *n_trip,
+cudaError_t launch_triplet_count(const MeshDev &m, const int4 *cand, int32_t n_cand, int32_t *n_trip,
                                  int32_t *n_red, int32_t *status, cudaStream_t s);
-cudaError_t launch_triplet_fill(const MeshDev &m, const int2 *cand, int32_t n_cand, const int32_t *trip_off,
+cudaError_t launch_triplet_fill(const MeshDev &m, const int4 *cand, int32_t n_cand, const int32_t *trip_off,
                                 const int32_t *red_off, TripletRec *trip, int2 *red, cudaStream_t s);
 cudaError_t launch_quartet_count(const MeshDev &m, const int4 *cand, int32_t n_cand, int32_t *n_quart,
                                  int32_t *n_red, int32_t *status, cudaStream_t s);
@@ -104,7 +105,7 @@ struct ThreePhArgs {
     const TripletRec *trip;
     int32_t n_trip;
     const int2 *red;
-    const uint32_t *cand_mask;  // [n_cand*4] bit b1 set when row (q1,b1) samples q2
+    const uint32_t *cand_mask;  // [n_mask*4] distinct row masks, indexed by TripletRec::cand
     double *gamma;              // [n_row]
     double *od;                 // [n_row * n_full*n]
     int32_t *status;
@@ -134,11 +135,24 @@ cudaError_t launch_isotope(const MeshDev &m, const PhononDev &ph, const RowsDev 
                            const int32_t *row_b1, const double *disorder, int32_t n_atom, double *gamma,
                            double *xi, cudaStream_t s);
 
-// K5a: symmetrize_and_distribute of one order, od -> xi (scattering_threephonon.f90:143-205).
-cudaError_t launch_sym_distribute(const MeshDev &m, int32_t n_row, const int32_t *row_q1, const int64_t *ptr,
-                                  const int32_t *list, double *od, double *xi, cudaStream_t s);
+// Orbits of the little group of every irreducible q1 on the mesh (built once per context).
+struct OrbitDev {
+    const int32_t *rep_ptr;  // [n_irr+1] first representative of q1
+    const int32_t *rep;      // [n_rep] representative q2 (smallest member of its orbit)
+    const int32_t *img;      // [n_rep * n_op] images in operation order, -1 off grid
+    const int32_t *cnt;      // [n_rep] number of on-grid images
+    const int32_t *orb_of;   // [n_irr * n_full] representative index of q2, -1 otherwise
+    int32_t max_rep;         // largest number of representatives of one q1
+};
+cudaError_t launch_orbit_flag(const MeshDev &m, int32_t *flag, cudaStream_t s);
+cudaError_t launch_orbit_fill(const MeshDev &m, const int32_t *flag, const int32_t *scan, OrbitDev &o,
+                              cudaStream_t s);
+// K5a: symmetrize_and_distribute of one order in place on od, then xi += od when xi is
+// not null (scattering_threephonon.f90:143-205).
+cudaError_t launch_sym_distribute(const MeshDev &m, const OrbitDev &o, int32_t n_row, const int32_t *row_q1,
+                                  const int64_t *ptr, const int32_t *list, double *od, double *xi, cudaStream_t s);
 // K5b: symmetrize_scatmat (scattering.f90:296-357).
-cudaError_t launch_sym_scatmat(const MeshDev &m, int32_t n_row, const int32_t *row_q1, double *xi,
+cudaError_t launch_sym_scatmat(const MeshDev &m, const OrbitDev &o, int32_t n_row, const int32_t *row_q1, double *xi,
                                cudaStream_t s);
 // K8: buf[r*3+a] = sum_j xi[r, j] * fbb[j*3 + a].
 cudaError_t launch_xi_gemv(const double *xi, int32_t n_row, int64_t n_col, const double *fbb, double *buf,

@@ -283,7 +283,7 @@ class ScatteringRates:
         self.lists = lists
         lw = np.zeros(p.n_irr * p.n_mode)
         qs = np.zeros(p.n_irr * p.n_mode)
-        st = np.zeros(4)
+        st = np.zeros(10)
         o = opts.struct(p.grid)
         q = lists.struct()
         N.check(self._lib.tdg_scattering(self._ctx, C.byref(o), C.byref(q), N.ptr(lw, C.c_double),
@@ -291,7 +291,9 @@ class ScatteringRates:
         self.linewidth = lw.reshape(p.n_irr, p.n_mode)
         self.qs = qs.reshape(p.n_irr, p.n_mode)
         self.stats = {"triplets": int(st[0]), "quartets": int(st[1]), "device_ms": float(st[2]),
-                      "candidates": int(st[3])}
+                      "candidates": int(st[3]), "enumerate_ms": float(st[4]), "threephonon_ms": float(st[5]),
+                      "symmetrize_ms": float(st[6]), "isotope_ms": float(st[7]), "launches": int(st[8]),
+                      "equivalent_triplets": int(st[9])}
         return self.linewidth
 
     def triplets(self, q1: int, sample) -> list:
