@@ -15,15 +15,18 @@
 // lattice vectors, so q.lv = sum_d g_d lv_d / N_d and exp(-2 pi i q.lv) is one entry of a
 // table of exp(-2 pi i K / L), L = lcm of the mesh dimensions.
 //
-// The delta weights stay FP64 as in the reference, but GB300's FP64 pipe is narrow, so
-// every mode triplet is first screened in FP32 against the 8-sigma window of lo_gauss
-// with a safety margin; only triplets that may fall inside it take the exact FP64 path,
-// which reproduces the reference's arithmetic (same window test, same formulas).
+// Delta weights stay FP64 as in the reference. GB300's FP64 pipe is narrow and the mode
+// triplets whose Gaussians fall inside the 8-sigma window of lo_gauss are sparse, so:
+//   1. the reference's skip rules become per-triplet bit masks (3 n^2 FP64 compares);
+//   2. every mode triplet and each of the four Gaussians of get_dirac is screened in FP32
+//      against the window, with a relative margin of 1e-3 and an absolute margin far
+//      above FP32 rounding (a Gaussian the screen drops is exactly 0 in the reference);
+//   3. the survivors are compacted into a shared-memory queue (block scan) and evaluated
+//      in FP64 by full warps, with the reference's own window test and formulas.
 //
-// Everything for one triplet lives in shared memory: P and T (two n^3 complex buffers),
-// the three scaled eigenvector matrices, the phase chunk and per-mode scalars. Precision R
-// is double (FP64 path) or float (mixed path: FP32 pretransform and contraction, FP64
-// delta weights, occupations and accumulation).
+// Everything for one triplet lives in shared memory. Precision R is double (FP64 path)
+// or float (mixed path: FP32 pretransform and contraction, FP64 delta weights,
+// occupations and accumulation).
 #include <cuda_runtime.h>
 
 #include "tdg_internal.cuh"
@@ -36,7 +39,7 @@ constexpr double kThreePhononPrefactor = 3.141592653589793 / 16.0;
 constexpr double kSqrt2PiInv = 0.398942280401433;
 constexpr double kFreqTolD = 1E-9;
 constexpr int kMaxRed = 192;
-constexpr int kPhaseChunk = 1024;
+constexpr int kPhaseChunk = 512;
 
 template <typename R>
 struct CT;
@@ -76,16 +79,15 @@ __device__ __forceinline__ double gauss(double x, double mu, double sigma, doubl
     return exp(-(x - mu) * (x - mu) * 0.5 * invsig * invsig) * kSqrt2PiInv * invsig;
 }
 
-template <typename T>
-__device__ __forceinline__ T adaptive_pair(const T *va, const T *vb, const double *rl) {
+__device__ __forceinline__ double adaptive_pair(const double *va, const double *vb, const double *rl) {
     // sqrt(maxval(matmul(va - vb, reclat)**2) * 0.5)
-    T m = 0;
+    double m = 0;
     for (int j = 0; j < 3; ++j) {
-        T s = 0;
-        for (int i = 0; i < 3; ++i) s += (va[i] - vb[i]) * (T)rl[i + 3 * j];
-        m = max(m, s * s);
+        double s = 0;
+        for (int i = 0; i < 3; ++i) s += (va[i] - vb[i]) * rl[i + 3 * j];
+        m = fmax(m, s * s);
     }
-    return sqrt(m * (T)0.5);
+    return sqrt(m * 0.5);
 }
 
 template <typename R>
@@ -121,10 +123,35 @@ __device__ __forceinline__ const float2 *egvs_ptr<float2>(const PhononDev &ph) {
     return ph.egvs32;
 }
 
+// Exclusive scan of one int per thread over the block (blockDim a multiple of 32).
+__device__ __forceinline__ int block_exclusive_scan(int v, int *wsum, int &total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int s = lane < nw ? wsum[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < nw) wsum[lane] = s;
+    }
+    __syncthreads();
+    total = wsum[nw - 1];
+    const int res = (w > 0 ? wsum[w - 1] : 0) + x - v;
+    __syncthreads();
+    return res;
+}
+
 // Shared-memory layout (bytes) for mode count n and complex size cs.
 struct Layout {
-    size_t om1, om2, om3, inv1, be2, be3, s1, s2, s3, v1, v2, v3, wrow, r2, f32, E1, E2, E3, A, B, ph, rowid, red,
-        total;
+    size_t om1, om2, om3, inv1, be2, be3, s1, s2, s3, v1, v2, v3, wrow, r2, f32, masks, E1, E2, E3, ph, Q, A, B,
+        rowid, red, wsum, total;
 };
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 __host__ __device__ inline Layout make_layout(int n, int cs) {
@@ -146,28 +173,43 @@ __host__ __device__ inline Layout make_layout(int n, int cs) {
     L.v3 = o; o += 3 * dn;
     L.wrow = o; o += dn;
     L.r2 = o; o += align16(sizeof(double) * n2);
-    L.f32 = o; o += align16(sizeof(float) * n * 6);  // float copies: om1..3, s1..3
-    L.E1 = o; o += align16(cs * n2);
-    L.E2 = o; o += align16(cs * n2);
-    L.E3 = o; o += align16(cs * n2);
-    // A and B must each hold n^3 complex values and at least n^3 doubles.
+    L.f32 = o; o += align16(sizeof(float) * n * 6);            // om1..3, s1..3 in FP32
+    L.masks = o; o += align16(sizeof(uint32_t) * (3 * n + 2));  // m12, m13, m23, z2, z3
+    // E1..E3 and the phase chunk are dead once Psi is formed: the survivor queue reuses them.
+    const size_t ez = align16(cs * n2);
+    L.E1 = o;
+    L.E2 = o + ez;
+    L.E3 = o + 2 * ez;
+    L.ph = o + 3 * ez;
+    const size_t eph = 3 * ez + align16((size_t)cs * kPhaseChunk);
+    const size_t qsz = align16(sizeof(uint32_t) * n3);
+    L.Q = o;
+    o += eph > qsz ? eph : qsz;
+    // A and B each hold n^3 complex values and at least n^3 doubles.
     const size_t csz = (size_t)cs > sizeof(double) ? (size_t)cs : sizeof(double);
     const size_t buf = align16(csz * n3);
     L.A = o; o += buf;
     L.B = o; o += buf;
-    L.ph = o; o += align16((size_t)cs * kPhaseChunk);
     L.rowid = o; o += align16(sizeof(int) * n);
     L.red = o; o += align16(sizeof(int2) * kMaxRed);
+    L.wsum = o; o += align16(sizeof(int) * 33);
     L.total = o;
     return L;
 }
 
+__host__ __device__ constexpr int threads_for(int n) { return ((n * n + 31) / 32) * 32; }
+// Resident CTAs per SM the register budget is sized for; FP64 buffers at n >= 12 already
+// limit residency through shared memory.
+__host__ __device__ constexpr int min_blocks_for(int n, bool dbl) {
+    return n <= 3 ? 16 : (n <= 6 ? 12 : (n <= 9 ? 6 : (dbl ? (n <= 12 ? 2 : 1) : (n <= 15 ? 3 : 2))));
+}
+
 template <int N, typename R>
-__global__ void __launch_bounds__(((N * N + 31) / 32) * 32)
-    k_threephonon(ThreePhArgs a) {
+__global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) == 8)) k_threephonon(ThreePhArgs a) {
     using C = typename CT<R>::C;
     constexpr int N2 = N * N, N3 = N2 * N;
     constexpr int NA = N / 3;
+    constexpr uint32_t kAll = (N >= 32) ? 0xffffffffu : ((1u << N) - 1u);
     extern __shared__ __align__(16) unsigned char smem[];
     const Layout L = make_layout(N, sizeof(C));
     double *om1 = (double *)(smem + L.om1);
@@ -186,14 +228,18 @@ __global__ void __launch_bounds__(((N * N + 31) / 32) * 32)
     double *R2 = (double *)(smem + L.r2);
     float *fo1 = (float *)(smem + L.f32);
     float *fo2 = fo1 + N, *fo3 = fo2 + N, *fs1 = fo3 + N, *fs2 = fs1 + N, *fs3 = fs2 + N;
+    uint32_t *m12 = (uint32_t *)(smem + L.masks);
+    uint32_t *m13 = m12 + N, *m23 = m13 + N, *zmask = m23 + N;  // zmask[0]: omega2 < tol, zmask[1]: omega3 < tol
     C *E1 = (C *)(smem + L.E1);
     C *E2 = (C *)(smem + L.E2);
     C *E3 = (C *)(smem + L.E3);
+    C *ph = (C *)(smem + L.ph);
+    uint32_t *Q = (uint32_t *)(smem + L.Q);
     C *A = (C *)(smem + L.A);
     C *B = (C *)(smem + L.B);
-    C *ph = (C *)(smem + L.ph);
     int *rowid = (int *)(smem + L.rowid);
     int2 *red = (int2 *)(smem + L.red);
+    int *wsum = (int *)(smem + L.wsum);
     const int tid = threadIdx.x, bd = blockDim.x;
     const MeshDev &m = a.mesh;
     const PhononDev &P = a.ph;
@@ -211,7 +257,8 @@ __global__ void __launch_bounds__(((N * N + 31) / 32) * 32)
         const int i2 = m.full_irr[q2], i3 = m.full_irr[q3];
         const uint32_t *mask = a.cand_mask + (size_t)rec.cand * 4;
         const int nred = rec.red_cnt;
-        // ---- per-mode scalars and scaled eigenvectors ----
+        const double perm = (q2 == q3) ? 1.0 : 2.0;
+        // ---- per-mode scalars ----
         for (int b = tid; b < N; b += bd) {
             om1[b] = P.omega[(size_t)f1 * N + b];
             om2[b] = P.omega[(size_t)q2 * N + b];
@@ -237,6 +284,13 @@ __global__ void __launch_bounds__(((N * N + 31) / 32) * 32)
             const bool on = (mask[b >> 5] >> (b & 31)) & 1u;
             rowid[b] = on ? r : -1;
             wrow[b] = r >= 0 ? a.rows.weight3[r] : 0.0;
+            m12[b] = 0u;
+            m13[b] = 0u;
+            m23[b] = 0u;
+        }
+        if (tid == 0) {
+            zmask[0] = 0u;
+            zmask[1] = 0u;
         }
         for (int i = tid; i < nred && i < kMaxRed; i += bd) red[i] = a.red[rec.red_off + i];
         for (int i = tid; i < 3 * N2; i += bd) {
@@ -246,8 +300,23 @@ __global__ void __launch_bounds__(((N * N + 31) / 32) * 32)
             C *E = which == 0 ? E1 : (which == 1 ? E2 : E3);
             E[r * N + b] = egvs[((size_t)q * N + b) * N + r];
         }
-        // ---- K2: pretransform into A ----
         for (int i = tid; i < N3; i += bd) A[i] = czero<C>();
+        __syncthreads();
+        // ---- skip rules of scattering_threephonon.f90:90-101 as bit masks ----
+        for (int i = tid; i < 3 * N2 + 2 * N; i += bd) {
+            if (i < 3 * N2) {
+                const int which = i / N2, x = (i % N2) / N, y = i % N;
+                const double *pa = which == 2 ? om2 : om1;
+                const double *pb = which == 0 ? om2 : om3;
+                uint32_t *mk = which == 0 ? m12 : (which == 1 ? m13 : m23);
+                if (fabs(pa[x] - pb[y]) < kFreqTolD) atomicOr(mk + x, 1u << y);
+            } else {
+                const int j = i - 3 * N2, which = j / N, b = j % N;
+                const double w = which == 0 ? om2[b] : om3[b];
+                if (w < kFreqTolD) atomicOr(zmask + which, 1u << b);
+            }
+        }
+        // ---- K2: pretransform into A ----
         int gi2[3], gi3[3];
         {
             const int n12 = m.grid[1] * m.grid[2];
@@ -317,8 +386,11 @@ __global__ void __launch_bounds__(((N * N + 31) / 32) * 32)
             for (int b2 = 0; b2 < N; ++b2) A[(b1 * N + b2) * N + c] = acc[b2];
         }
         __syncthreads();
-        // ---- Psi and K4 epilogue: F[b1][b2][b3] into B (as doubles), R2 = sum over b3 ----
-        double *F = (double *)B;
+        // ---- Psi into B; FP32 screen of the Gaussians, survivors counted per thread ----
+        uint32_t allowed = 0u;  // b3 that pass the reference's skip rules
+        uint32_t live_lo = 0u, live_hi = 0u;  // 4-bit live masks of b3 = 0..7 and 8..15
+        uint32_t live_x = 0u;                 // b3 = 16, 17
+        int nsurv = 0;
         if (tid < N2) {
             const int b1 = tid / N, b2 = tid % N;
             C acc[N];
@@ -330,84 +402,107 @@ __global__ void __launch_bounds__(((N * N + 31) / 32) * 32)
 #pragma unroll
                 for (int b3 = 0; b3 < N; ++b3) cfma(acc[b3], E3[c * N + b3], tv);
             }
-            const int row = rowid[b1];
-            const double o1 = om1[b1], o2 = om2[b2];
+#pragma unroll
+            for (int b3 = 0; b3 < N; ++b3) B[(b1 * N + b2) * N + b3] = acc[b3];
+            const bool skip12 = rowid[b1] < 0 || ((zmask[0] | m12[b1]) >> b2) & 1u;
+            allowed = skip12 ? 0u : (kAll & ~(zmask[1] | m13[b1] | m23[b2]));
             const float f_o1 = fo1[b1], f_o2 = fo2[b2];
-            const double perm = (q2 == q3) ? 1.0 : 2.0;
-            const bool skip12 = row < 0 || o2 < kFreqTolD || fabs(o1 - o2) < kFreqTolD;
-            double r2 = 0.0;
 #pragma unroll
             for (int b3 = 0; b3 < N; ++b3) {
-                double f = 0.0;
-                const double o3 = om3[b3];
-                if (!skip12 && !(o3 < kFreqTolD) && !(fabs(o1 - o3) < kFreqTolD || fabs(o2 - o3) < kFreqTolD)) {
-                    // FP32 screen: the nearest of the four Gaussian centres against 8 sigma,
-                    // with a relative margin and an absolute margin of the FP32 rounding.
-                    const float f_o3 = fo3[b3];
-                    float sg = 0.f;
-                    if (it == 1) {
-                        sg = sigfix32;
-                    } else if (it == 2) {
-                        sg = sqrtf(fs1[b1] + fs2[b2] + fs3[b3]);
-                    }
-                    // One bit per Gaussian of get_dirac that may lie inside its window; the
-                    // velocity-difference width of -it 6 can cancel in FP32, so it is not screened.
-                    const float win = 8.0f * sg * 1.001f + 1e-6f * (f_o1 + f_o2 + f_o3);
-                    unsigned live = 15u;
-                    if (it != 6) {
-                        live = (fabsf(f_o1 + f_o2 - f_o3) <= win ? 1u : 0u) | (fabsf(f_o1 - f_o2 + f_o3) <= win ? 2u : 0u) |
-                               (fabsf(f_o1 - f_o2 - f_o3) <= win ? 4u : 0u) | (f_o1 + f_o2 + f_o3 <= win ? 8u : 0u);
-                    }
-                    if (live) {
-                        double sigma, invsig;
-                        if (it == 1) {
-                            sigma = P.sigma_fixed;
-                            invsig = 1.0 / sigma;
-                        } else if (it == 2) {
-                            const double s = s1[b1] + s2[b2] + s3[b3];
-                            invsig = rsqrt(s);
-                            sigma = s * invsig;
-                        } else {
-                            sigma = adaptive_pair<double>(v1 + 3 * b1, v2 + 3 * b2, P.reclat_g) / 3.0;
-                            sigma += adaptive_pair<double>(v1 + 3 * b1, v3 + 3 * b3, P.reclat_g) / 3.0;
-                            sigma += adaptive_pair<double>(v2 + 3 * b2, v3 + 3 * b3, P.reclat_g) / 3.0;
-                            sigma += P.thresh_sigma;
-                            invsig = 1.0 / sigma;
-                        }
-                        const double ga = (live & 1u) ? gauss(o1, -o2 + o3, sigma, invsig) : 0.0;
-                        const double gb = (live & 2u) ? gauss(o1, o2 - o3, sigma, invsig) : 0.0;
-                        const double gc = (live & 4u) ? gauss(o1, o2 + o3, sigma, invsig) : 0.0;
-                        const double gd = (live & 8u) ? gauss(o1, -o2 - o3, sigma, invsig) : 0.0;
-                        const double d0 = ga - gb;
-                        const double d1 = gc - gd;
-                        if (nonzero(d0) || nonzero(d1)) {
-                            const double cr = (double)acc[b3].x, ci = (double)acc[b3].y;
-                            const double psisq = kThreePhononPrefactor * (cr * cr + ci * ci) * wrow[b1];
-                            const double n2 = be2[b2], n3 = be3[b3];
-                            const double plf0 = n2 - n3;
-                            const double plf1 = n2 + n3 + 1.0;
-                            const double f0 = perm * psisq * plf0 * d0;
-                            const double f1 = perm * psisq * plf1 * d1;
-                            f = f0 + f1;
-                            r2 += f;
-                        }
-                    }
+                if (!((allowed >> b3) & 1u)) continue;
+                const float f_o3 = fo3[b3];
+                float sg = 0.f;
+                if (it == 1) sg = sigfix32;
+                else if (it == 2) sg = sqrtf(fs1[b1] + fs2[b2] + fs3[b3]);
+                const float win = 8.0f * sg * 1.001f + 1e-6f * (f_o1 + f_o2 + f_o3);
+                uint32_t live = 15u;  // the -it 6 width can cancel in FP32: not screened
+                if (it != 6) {
+                    live = (fabsf(f_o1 + f_o2 - f_o3) <= win ? 1u : 0u) | (fabsf(f_o1 - f_o2 + f_o3) <= win ? 2u : 0u) |
+                           (fabsf(f_o1 - f_o2 - f_o3) <= win ? 4u : 0u) | (f_o1 + f_o2 + f_o3 <= win ? 8u : 0u);
                 }
-                F[(b1 * N + b2) * N + b3] = f;
+                if (live) {
+                    ++nsurv;
+                    if (b3 < 8) live_lo |= live << (4 * b3);
+                    else if (b3 < 16) live_hi |= live << (4 * (b3 - 8));
+                    else live_x |= live << (4 * (b3 - 16));
+                }
             }
-            R2[tid] = r2;
+        }
+        int nq = 0;
+        const int off = block_exclusive_scan(nsurv, wsum, nq);  // contains __syncthreads
+        // E1..E3 and the phases are dead: the queue overwrites them.
+        if (tid < N2 && nsurv) {
+            int k = off;
+#pragma unroll
+            for (int b3 = 0; b3 < N; ++b3) {
+                const uint32_t live = b3 < 8 ? (live_lo >> (4 * b3)) & 15u
+                                             : (b3 < 16 ? (live_hi >> (4 * (b3 - 8))) & 15u : (live_x >> (4 * (b3 - 16))) & 15u);
+                if (live) Q[k++] = (uint32_t)(tid * N + b3) | (live << 16);
+            }
+        }
+        // dense F (doubles) in A, zero where no survivor
+        double *F = (double *)A;
+        for (int i = tid; i < N3; i += bd) F[i] = 0.0;
+        __syncthreads();
+        // ---- FP64 delta weights and occupations for the survivors, full warps ----
+        for (int s = tid; s < nq; s += bd) {
+            const uint32_t qv = Q[s];
+            const int idx = (int)(qv & 0xffffu);
+            const uint32_t live = qv >> 16;
+            const int b1 = idx / N2, b2 = (idx / N) % N, b3 = idx % N;
+            const double o1 = om1[b1], o2 = om2[b2], o3 = om3[b3];
+            double sigma, invsig;
+            if (it == 1) {
+                sigma = P.sigma_fixed;
+                invsig = 1.0 / sigma;
+            } else if (it == 2) {
+                const double sq = s1[b1] + s2[b2] + s3[b3];
+                invsig = rsqrt(sq);
+                sigma = sq * invsig;
+            } else {
+                sigma = adaptive_pair(v1 + 3 * b1, v2 + 3 * b2, P.reclat_g) / 3.0;
+                sigma += adaptive_pair(v1 + 3 * b1, v3 + 3 * b3, P.reclat_g) / 3.0;
+                sigma += adaptive_pair(v2 + 3 * b2, v3 + 3 * b3, P.reclat_g) / 3.0;
+                sigma += P.thresh_sigma;
+                invsig = 1.0 / sigma;
+            }
+            const double ga = (live & 1u) ? gauss(o1, -o2 + o3, sigma, invsig) : 0.0;
+            const double gb = (live & 2u) ? gauss(o1, o2 - o3, sigma, invsig) : 0.0;
+            const double gc = (live & 4u) ? gauss(o1, o2 + o3, sigma, invsig) : 0.0;
+            const double gd = (live & 8u) ? gauss(o1, -o2 - o3, sigma, invsig) : 0.0;
+            const double d0 = ga - gb;
+            const double d1 = gc - gd;
+            if (nonzero(d0) || nonzero(d1)) {
+                const C psi = B[idx];
+                const double cr = (double)psi.x, ci = (double)psi.y;
+                const double psisq = kThreePhononPrefactor * (cr * cr + ci * ci) * wrow[b1];
+                const double n2 = be2[b2], n3 = be3[b3];
+                const double plf0 = n2 - n3;
+                const double plf1 = n2 + n3 + 1.0;
+                const double f0 = perm * psisq * plf0 * d0;
+                const double f1 = perm * psisq * plf1 * d1;
+                F[idx] = f0 + f1;
+            }
         }
         __syncthreads();
-        // ---- R3 = sum over b2, into A (as doubles); Gamma per b1 ----
-        double *R3 = (double *)A;
-        for (int e = tid; e < N2; e += bd) {
-            const int b1 = e / N, b3 = e % N;
-            double s = 0.0;
-            for (int b2 = 0; b2 < N; ++b2) {
-                const double f = F[(b1 * N + b2) * N + b3];
-                if (nonzero(f)) s += f;
+        // ---- R2 = sum over b3, R3 = sum over b2 (into B as doubles) ----
+        double *R3 = (double *)B;
+        for (int e = tid; e < 2 * N2; e += bd) {
+            double sum = 0.0;
+            if (e < N2) {
+                for (int b3 = 0; b3 < N; ++b3) {
+                    const double f = F[e * N + b3];
+                    if (nonzero(f)) sum += f;
+                }
+                R2[e] = sum;
+            } else {
+                const int e3 = e - N2, b1 = e3 / N, b3 = e3 % N;
+                for (int b2 = 0; b2 < N; ++b2) {
+                    const double f = F[(b1 * N + b2) * N + b3];
+                    if (nonzero(f)) sum += f;
+                }
+                R3[e3] = sum;
             }
-            R3[e] = s;
         }
         __syncthreads();
         if (tid < N) {
@@ -442,7 +537,7 @@ __global__ void __launch_bounds__(((N * N + 31) / 32) * 32)
 template <int N, typename R>
 cudaError_t launch_n(const ThreePhArgs &a, int n_sm, cudaStream_t s) {
     const Layout L = make_layout(N, sizeof(typename CT<R>::C));
-    const int threads = ((N * N + 31) / 32) * 32;
+    const int threads = threads_for(N);
     cudaError_t e = cudaFuncSetAttribute(k_threephonon<N, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)L.total);
     if (e != cudaSuccess) return e;
