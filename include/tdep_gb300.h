@@ -142,6 +142,11 @@ const char *tdg_version(void);
 /* Number of CUDA devices visible (0 without a GPU); never fails. */
 int tdg_device_count(void);
 
+/* Diagnostic, no counterpart in the reference: evaluates on the current device the FP64
+ * exponential the delta weights use, out[i] = exp(-t[i]) for 0 <= t[i] <= 40 (the range
+ * of lo_gauss inside its 8-sigma window), so tests can bound its error. */
+int tdg_check_exp(const double *t, int32_t n, double *out);
+
 /* Create a context on CUDA device `device` and upload the problem (replaces the
  * allocations of scattering.f90:85-212). Fails with TDG_ERR_DEVICE without a GPU. */
 int tdg_create(tdg_ctx **out, const tdg_problem *prob, int device);

@@ -106,6 +106,7 @@ SIGNATURES = {
     "tdg_last_error": (C.c_char_p, []),
     "tdg_version": (C.c_char_p, []),
     "tdg_device_count": (C.c_int, []),
+    "tdg_check_exp": (C.c_int, [_f64p, C.c_int32, _f64p]),
     "tdg_create": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(TdgProblem), C.c_int]),
     "tdg_destroy": (None, [C.c_void_p]),
     "tdg_mc_qlists": (C.c_int, [C.POINTER(TdgProblem), C.POINTER(TdgOpts), _i32p, _i32p, _i32p, _i64p, _i32p,

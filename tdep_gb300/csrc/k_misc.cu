@@ -105,77 +105,86 @@ __global__ void k_orbit_flag(MeshDev m, int32_t *flag) {
     flag[(size_t)q1 * m.n_full + q2] = rep;
 }
 
-__global__ void k_orbit_fill(MeshDev m, const int32_t *flag, const int32_t *scan, int32_t *orb_of, int32_t *rep,
-                             int32_t *img, int32_t *cnt) {
+// Images are stored once each, in order of first appearance over the operations, with
+// their multiplicity (operations that map q2 to the same point); cnt counts every
+// on-grid operation, as the reference's averages do.
+__global__ void k_orbit_fill(MeshDev m, const int32_t *flag, const int32_t *scan, OrbitDev o) {
     const int q2 = blockIdx.x * blockDim.x + threadIdx.x;
     const int q1 = blockIdx.y;
     if (q2 >= m.n_full) return;
     const size_t i = (size_t)q1 * m.n_full + q2;
+    int32_t *orb_of = const_cast<int32_t *>(o.orb_of);
     if (!flag[i]) {
         orb_of[i] = -1;
         return;
     }
     const int k = scan[i];
     orb_of[i] = k;
-    rep[k] = q2;
+    const_cast<int32_t *>(o.rep)[k] = q2;
     const int nop = m.irr_nop[q1];
     const int32_t *ops = m.irr_ops + (size_t)q1 * m.n_op;
-    int c = 0;
-    for (int j = 0; j < m.n_op; ++j) {
-        int q2p = -1;
-        if (j < nop) {
-            q2p = m.rot[(size_t)ops[j] * m.n_full + q2];
-            if (q2p >= 0) ++c;
+    int32_t *img = const_cast<int32_t *>(o.img) + (size_t)k * m.n_op;
+    int32_t *mult = const_cast<int32_t *>(o.mult) + (size_t)k * m.n_op;
+    int c = 0, nu = 0;
+    for (int j = 0; j < nop; ++j) {
+        const int q2p = m.rot[(size_t)ops[j] * m.n_full + q2];
+        if (q2p < 0) continue;
+        ++c;
+        int u = 0;
+        while (u < nu && img[u] != q2p) ++u;
+        if (u == nu) {
+            img[nu] = q2p;
+            mult[nu] = 0;
+            ++nu;
         }
-        img[(size_t)k * m.n_op + j] = q2p;
+        ++mult[u];
     }
-    cnt[k] = c;
+    const_cast<int32_t *>(o.cnt)[k] = c;
+    const_cast<int32_t *>(o.nuniq)[k] = nu;
 }
+
+__device__ __forceinline__ bool positive(double v) { return __double_as_longlong(v) > 0; }  // v > 0, v not NaN
 
 // symmetrize_and_distribute (scattering_threephonon.f90:143-205, scattering_fourphonon.f90:195-250)
 // in place on one row per CTA: for every sampled q2 that represents its orbit, each mode's
-// entries with od > 0 are averaged and the average is written to every image. Orbits are
-// disjoint, so threads never touch the same entries; a bitmap ignores repeated entries of
-// a sample (the reference would process them again to the same result).
+// entries with od > 0 are averaged over the on-grid operations (images counted with their
+// multiplicity) and the average is written to every image. Orbits are disjoint, so
+// threads never touch the same entries; a bitmap ignores repeated entries of a sample
+// (the reference would process them again to the same result).
 // When xi != nullptr the symmetrised row is then added to xi.
-__global__ void k_sym_distribute(MeshDev m, OrbitDev o, const int32_t *row_q1, const int64_t *ptr,
-                                 const int32_t *list, double *od, double *xi) {
+__global__ void k_sym_distribute(MeshDev m, OrbitDev o, const int32_t *row_q1, const int64_t *rbeg,
+                                 const int32_t *rlen, const int32_t *list, double *od, double *xi) {
     extern __shared__ uint32_t seen[];
     const int n = m.n_mode;
     const int r = blockIdx.x;
     const int q1 = row_q1[r];
-    const int nop = m.irr_nop[q1];
     const int64_t ld = (int64_t)m.n_full * n;
     double *odr = od + (int64_t)r * ld;
     const int nw = (m.n_full + 31) / 32;
     for (int i = threadIdx.x; i < nw; i += blockDim.x) seen[i] = 0u;
     __syncthreads();
-    for (int64_t qi = ptr[r] + threadIdx.x; qi < ptr[r + 1]; qi += blockDim.x) {
+    for (int64_t qi = rbeg[r] + threadIdx.x; qi < rbeg[r] + rlen[r]; qi += blockDim.x) {
         const int q2 = list[qi] - 1;
         const int k = o.orb_of[(size_t)q1 * m.n_full + q2];
         if (k < 0) continue;
         const uint32_t bit = 1u << (q2 & 31);
         if (atomicOr(&seen[q2 >> 5], bit) & bit) continue;
         const int32_t *im = o.img + (size_t)k * m.n_op;
+        const int32_t *mu = o.mult + (size_t)k * m.n_op;
+        const int nu = o.nuniq[k];
         for (int b2 = 0; b2 < n; ++b2) {
             double buf = 0.0;
             int nn = 0;
-            for (int j = 0; j < nop; ++j) {
-                const int q2p = im[j];
-                if (q2p < 0) continue;
-                const double v = odr[(int64_t)q2p * n + b2];
-                if (v > 0.0) {
-                    ++nn;
-                    buf += v;
+            for (int u = 0; u < nu; ++u) {
+                const double v = odr[(int64_t)im[u] * n + b2];
+                if (positive(v)) {
+                    nn += mu[u];
+                    for (int rep = 0; rep < mu[u]; ++rep) buf += v;
                 }
             }
             if (nn == 0) continue;
-            const double avg = buf / (double)nn;
-            for (int j = 0; j < nop; ++j) {
-                const int q2p = im[j];
-                if (q2p < 0) continue;
-                odr[(int64_t)q2p * n + b2] = avg;
-            }
+            const double avg = buf * o.rcp[nn];
+            for (int u = 0; u < nu; ++u) odr[(int64_t)im[u] * n + b2] = avg;
         }
     }
     if (xi == nullptr) return;
@@ -195,21 +204,26 @@ __global__ void k_sym_scatmat(MeshDev m, OrbitDev o, const int32_t *row_q1, doub
     const int k = o.rep_ptr[q1] + i / n, b2 = i % n;
     const int cnt = o.cnt[k];
     if (cnt == 0) return;
-    const int nop = m.irr_nop[q1];
+    const int nu = o.nuniq[k];
     const int32_t *im = o.img + (size_t)k * m.n_op;
+    const int32_t *mu = o.mult + (size_t)k * m.n_op;
     double *xr = xi + (int64_t)r * m.n_full * n;
     double buf = 0.0;
-    for (int j = 0; j < nop; ++j) {
-        const int q2p = im[j];
-        if (q2p < 0) continue;
-        buf += xr[(int64_t)q2p * n + b2];
+    int u = 0;
+    for (; u + 4 <= nu; u += 4) {
+        const double x0 = xr[(int64_t)im[u] * n + b2], x1 = xr[(int64_t)im[u + 1] * n + b2];
+        const double x2 = xr[(int64_t)im[u + 2] * n + b2], x3 = xr[(int64_t)im[u + 3] * n + b2];
+        for (int rep = 0; rep < mu[u]; ++rep) buf += x0;
+        for (int rep = 0; rep < mu[u + 1]; ++rep) buf += x1;
+        for (int rep = 0; rep < mu[u + 2]; ++rep) buf += x2;
+        for (int rep = 0; rep < mu[u + 3]; ++rep) buf += x3;
     }
-    buf /= (double)cnt;
-    for (int j = 0; j < nop; ++j) {
-        const int q2p = im[j];
-        if (q2p < 0) continue;
-        xr[(int64_t)q2p * n + b2] = buf;
+    for (; u < nu; ++u) {
+        const double x = xr[(int64_t)im[u] * n + b2];
+        for (int rep = 0; rep < mu[u]; ++rep) buf += x;
     }
+    buf *= o.rcp[cnt];
+    for (u = 0; u < nu; ++u) xr[(int64_t)im[u] * n + b2] = buf;
 }
 
 // K8: three dot products per row of Xi (kappa.f90:411-413, the lo_gemv calls).
@@ -274,21 +288,21 @@ cudaError_t launch_orbit_flag(const MeshDev &m, int32_t *flag, cudaStream_t s) {
 cudaError_t launch_orbit_fill(const MeshDev &m, const int32_t *flag, const int32_t *scan, OrbitDev &o,
                               cudaStream_t s) {
     dim3 grid((unsigned)((m.n_full + 127) / 128), (unsigned)m.n_irr);
-    k_orbit_fill<<<grid, 128, 0, s>>>(m, flag, scan, const_cast<int32_t *>(o.orb_of), const_cast<int32_t *>(o.rep),
-                                      const_cast<int32_t *>(o.img), const_cast<int32_t *>(o.cnt));
+    k_orbit_fill<<<grid, 128, 0, s>>>(m, flag, scan, o);
     k_rep_ptr<<<(m.n_irr + 1 + 127) / 128, 128, 0, s>>>(scan, m.n_irr, m.n_full, const_cast<int32_t *>(o.rep_ptr));
     return cudaGetLastError();
 }
 
 cudaError_t launch_sym_distribute(const MeshDev &m, const OrbitDev &o, int32_t n_row, const int32_t *row_q1,
-                                  const int64_t *ptr, const int32_t *list, double *od, double *xi, cudaStream_t s) {
+                                  const int64_t *rbeg, const int32_t *rlen, const int32_t *list, double *od, double *xi,
+                                  cudaStream_t s) {
     if (n_row <= 0) return cudaSuccess;
     const size_t sm = sizeof(uint32_t) * (size_t)((m.n_full + 31) / 32);
     if (sm > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k_sym_distribute, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
     }
-    k_sym_distribute<<<n_row, 256, sm, s>>>(m, o, row_q1, ptr, list, od, xi);
+    k_sym_distribute<<<n_row, 256, sm, s>>>(m, o, row_q1, rbeg, rlen, list, od, xi);
     return cudaGetLastError();
 }
 

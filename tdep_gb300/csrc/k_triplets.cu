@@ -296,6 +296,23 @@ __global__ void k_scan_add(int32_t *out, int32_t n, const int32_t *sums) {
 
 }  // namespace
 
+namespace {
+__global__ void k_build_candidates(const int4 *desc, const int32_t *list, int4 *cand) {
+    const int q1 = blockIdx.y;
+    const int4 d = desc[q1];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.y; i += gridDim.x * blockDim.x)
+        cand[d.z + i] = make_int4(q1, list[d.x + i] - 1, d.w, 0);
+}
+}  // namespace
+
+cudaError_t launch_build_candidates(const int4 *desc, int32_t n_irr, int32_t max_len, const int32_t *list, int4 *cand,
+                                    cudaStream_t s) {
+    if (n_irr <= 0 || max_len <= 0) return cudaSuccess;
+    dim3 grid((unsigned)((max_len + 255) / 256), (unsigned)n_irr);
+    k_build_candidates<<<grid, 256, 0, s>>>(desc, list, cand);
+    return cudaGetLastError();
+}
+
 size_t exclusive_scan_tmp_elems(int32_t n) { return (size_t)(n + kScanItems - 1) / kScanItems + 1; }
 
 cudaError_t exclusive_scan_i32(const int32_t *in, int32_t *out, int32_t n, int32_t *tmp, cudaStream_t s) {

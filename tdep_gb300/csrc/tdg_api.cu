@@ -66,6 +66,14 @@ struct DevBuf {
 
 int gcd_i(int a, int b) { return b == 0 ? a : gcd_i(b, a % b); }
 
+// 2^(-j/64), j = 0..63, for the device exponential; long double keeps the rounding to
+// double correct.
+std::vector<double> exp2_table() {
+    std::vector<double> t(64);
+    for (int j = 0; j < 64; ++j) t[j] = (double)std::exp2l(-(long double)j / 64.0L);
+    return t;
+}
+
 // lo_chop (gottochblandat.f90:1286-1376): snap to 0, +-n/m (m <= 10), +-1/sqrt2, +-sqrt3/2, +-1.
 double lo_chop(double x, double tol) {
     if (std::fabs(x) < tol) return 0.0;
@@ -109,6 +117,7 @@ struct tdg_ctx {
     DevBuf<float> fc3_mwm32, fc4_mwm32;
     DevBuf<double2> tw;
     DevBuf<float2> tw32;
+    DevBuf<double> d_exp2tab;
     int L = 1, lmul[3] = {1, 1, 1};
     // scattering state
     int n_row = 0;
@@ -116,7 +125,8 @@ struct tdg_ctx {
     DevBuf<int32_t> d_row_q1, d_row_b1, d_rowidx;
     DevBuf<double> d_w3, d_w4, d_gamma, d_xi, d_od;
     // orbits of the little groups (built once per context)
-    DevBuf<int32_t> d_orb_rep_ptr, d_orb_rep, d_orb_img, d_orb_cnt, d_orb_of;
+    DevBuf<int32_t> d_orb_rep_ptr, d_orb_rep, d_orb_img, d_orb_mult, d_orb_nuniq, d_orb_cnt, d_orb_of;
+    DevBuf<double> d_rcp;
     OrbitDev orbits{};
     DevBuf<int32_t> d_status;
     bool have_scattering = false;
@@ -124,8 +134,9 @@ struct tdg_ctx {
     // enumeration and sample buffers, kept across calls (they only grow)
     DevBuf<int4> d_cand;
     DevBuf<uint32_t> d_mask;
-    DevBuf<int32_t> d_nt, d_nrd, d_toff, d_roff, d_tmp, d_list3;
-    DevBuf<int64_t> d_ptr3;
+    DevBuf<int32_t> d_nt, d_nrd, d_toff, d_roff, d_tmp, d_list3, d_rlen;
+    DevBuf<int64_t> d_rbeg;
+    DevBuf<int4> d_qdesc;
     DevBuf<TripletRec> d_trip;
     DevBuf<int2> d_red;
     // BTE buffers
@@ -148,6 +159,25 @@ struct tdg_ctx {
         return m;
     }
 };
+
+extern "C" int tdg_check_exp(const double *t, int32_t n, double *out) {
+    if (!t || !out || n < 0) return set_error(kErrParam, "tdg_check_exp: bad argument");
+    for (int32_t i = 0; i < n; ++i)
+        if (!(t[i] >= 0.0 && t[i] <= 40.0)) return set_error(kErrParam, "tdg_check_exp: t outside [0, 40]");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return set_error(kErrDevice, "no CUDA device available");
+    }
+    DevBuf<double> dt, dout, dtab;
+    const std::vector<double> tab = exp2_table();
+    CUDA_TRY(dt.upload(t, n, nullptr));
+    CUDA_TRY(dtab.upload(tab.data(), tab.size(), nullptr));
+    CUDA_TRY(dout.alloc(n));
+    CUDA_TRY(launch_exp_neg_check(dt.p, n, dout.p, dtab.p, nullptr));
+    CUDA_TRY(cudaMemcpy(out, dout.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    return kOk;
+}
 
 extern "C" int tdg_device_count(void) {
     int n = 0;
@@ -398,6 +428,8 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
     chk(c->fc4_mwm32.upload(mwm4f.data(), mwm4f.size(), s));
     chk(c->tw.upload(tw.data(), tw.size(), s));
     chk(c->tw32.upload(tw32.data(), tw32.size(), s));
+    const std::vector<double> e2t = exp2_table();
+    chk(c->d_exp2tab.upload(e2t.data(), e2t.size(), s));
     chk(c->d_status.alloc(1));
     chk(cudaStreamSynchronize(s));
     if (e != cudaSuccess) return fail(set_error(kErrDevice, std::string("upload failed: ") + cudaGetErrorString(e)));
@@ -421,11 +453,19 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
         chk(c->d_orb_rep.alloc(nrep));
         chk(c->d_orb_img.alloc((size_t)nrep * c->nop));
         chk(c->d_orb_cnt.alloc(nrep));
+        chk(c->d_orb_mult.alloc((size_t)nrep * c->nop));
+        chk(c->d_orb_nuniq.alloc(nrep));
+        std::vector<double> rcp(c->nop + 1, 0.0);
+        for (int i = 1; i <= c->nop; ++i) rcp[i] = 1.0 / (double)i;
+        chk(c->d_rcp.upload(rcp.data(), rcp.size(), s));
         if (e != cudaSuccess) return fail(set_error(kErrDevice, std::string("orbit tables: ") + cudaGetErrorString(e)));
         c->orbits.rep_ptr = c->d_orb_rep_ptr.p;
         c->orbits.rep = c->d_orb_rep.p;
         c->orbits.img = c->d_orb_img.p;
         c->orbits.cnt = c->d_orb_cnt.p;
+        c->orbits.mult = c->d_orb_mult.p;
+        c->orbits.nuniq = c->d_orb_nuniq.p;
+        c->orbits.rcp = c->d_rcp.p;
         c->orbits.orb_of = c->d_orb_of.p;
         chk(launch_orbit_fill(mesh, flag.p, scan.p, c->orbits, s));
         std::vector<int32_t> rp(c->nirr + 1);
@@ -563,6 +603,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     ph.sigma_fixed = o->sigma * kFreqTHzToHartree;
     ph.thresh_sigma = maxavg * 1e-4;
     ph.integrationtype = o->integrationtype;
+    ph.exp2tab = c->d_exp2tab.p;
 
     std::vector<int32_t> rowidx((size_t)nirr * n, -1), rq1(nr), rb1(nr);
     std::vector<double> w3(nr, 0.0), w4(nr, 0.0);
@@ -572,50 +613,105 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         rowidx[(size_t)rq1[r] * n + rb1[r]] = r;
         if (o->thirdorder) w3[r] = 1.0 / (double)(ql->ptr3[r + 1] - ql->ptr3[r]);
     }
-    // ---- three-phonon candidates: per q1 the union of its rows' samples; the set of
-    // rows sampling q2 is a bit mask, stored once in a table of distinct masks ----
-    std::vector<int4> cand;
-    std::vector<uint32_t> masks;
+    // ---- three-phonon samples and candidates ----
+    // When all rows of a q1 share one sample (the full grid, or samples given per q1) it is
+    // uploaded once per q1 and the candidates (q1, q2, mask of every row of q1) are formed
+    // on the device, in sample order. Otherwise the candidates are, per q1, the union of
+    // its rows' samples, with the set of rows that sampled q2 as a bit mask. Masks are
+    // stored once in a table of distinct masks. A sample that repeats a q-point is
+    // rejected: the reference would count that point twice.
+    std::vector<int4> cand;                 // union path
+    std::vector<uint32_t> masks;            // distinct row masks (4 words each)
+    std::vector<int64_t> rbeg(nr, 0);       // per row: start of its sample in the uploaded list
+    std::vector<int32_t> rlen(nr, 0);
+    std::vector<int32_t> slist;             // shared path: one sample per q1
+    std::vector<int4> qdesc;                // shared path: per q1 (list start, length, first candidate, mask)
+    bool shared = true;
+    int64_t nc64 = 0;
     if (o->thirdorder) {
-        std::vector<uint32_t> mark((size_t)N * 4, 0u);
-        std::vector<int32_t> touched;
-        std::vector<std::array<uint32_t, 4>> table;
-        int r0 = 0;
-        for (int q1 = 0; q1 < nirr; ++q1) {
-            int r1 = r0;
+        std::vector<int> qr0(nirr + 1, nr);
+        for (int r = nr - 1; r >= 0; --r) qr0[rq1[r]] = r;
+        for (int q1 = nirr - 1; q1 >= 0; --q1)
+            if (qr0[q1] == nr) qr0[q1] = qr0[q1 + 1];
+        auto rows_of = [&](int q1, int &r0, int &r1) {
+            r0 = qr0[q1];
+            r1 = r0;
             while (r1 < nr && rq1[r1] == q1) ++r1;
-            touched.clear();
-            for (int r = r0; r < r1; ++r) {
-                const int b1 = rb1[r];
-                for (int64_t i = ql->ptr3[r]; i < ql->ptr3[r + 1]; ++i) {
-                    const int q2 = ql->list3[i] - 1;
-                    uint32_t *mk = &mark[(size_t)q2 * 4];
-                    if (!(mk[0] | mk[1] | mk[2] | mk[3])) touched.push_back(q2);
-                    mk[b1 >> 5] |= 1u << (b1 & 31);
-                }
+        };
+        for (int q1 = 0; q1 < nirr && shared; ++q1) {
+            int r0, r1;
+            rows_of(q1, r0, r1);
+            for (int r = r0 + 1; r < r1 && shared; ++r) {
+                const int64_t L = ql->ptr3[r0 + 1] - ql->ptr3[r0];
+                shared = (ql->ptr3[r + 1] - ql->ptr3[r] == L) &&
+                         std::memcmp(ql->list3 + ql->ptr3[r], ql->list3 + ql->ptr3[r0], sizeof(int32_t) * L) == 0;
             }
-            std::sort(touched.begin(), touched.end());
-            for (int q2 : touched) {
-                uint32_t *mk = &mark[(size_t)q2 * 4];
-                const std::array<uint32_t, 4> key = {mk[0], mk[1], mk[2], mk[3]};
-                int id = -1;
-                for (int t = (int)table.size() - 1; t >= 0 && t >= (int)table.size() - 8; --t)
-                    if (table[t] == key) {
-                        id = t;
-                        break;
+        }
+        std::vector<std::array<uint32_t, 4>> table;
+        auto mask_id = [&](const std::array<uint32_t, 4> &key) {
+            for (int t = (int)table.size() - 1; t >= 0 && t >= (int)table.size() - 8; --t)
+                if (table[t] == key) return t;
+            table.push_back(key);
+            return (int)table.size() - 1;
+        };
+        std::vector<int32_t> stamp(N, -1);
+        if (shared) {
+            qdesc.assign(nirr, make_int4(0, 0, 0, 0));
+            for (int q1 = 0; q1 < nirr; ++q1) {
+                int r0, r1;
+                rows_of(q1, r0, r1);
+                if (r0 == r1) continue;
+                std::array<uint32_t, 4> key = {0u, 0u, 0u, 0u};
+                for (int r = r0; r < r1; ++r) key[rb1[r] >> 5] |= 1u << (rb1[r] & 31);
+                const int64_t L = ql->ptr3[r0 + 1] - ql->ptr3[r0];
+                const int64_t start = (int64_t)slist.size();
+                for (int64_t i = 0; i < L; ++i) {
+                    const int32_t q2 = ql->list3[ql->ptr3[r0] + i];
+                    if (stamp[q2 - 1] == q1) return set_error(kErrParam, "three-phonon sample repeats a q-point");
+                    stamp[q2 - 1] = q1;
+                    slist.push_back(q2);
+                }
+                qdesc[q1] = make_int4((int32_t)start, (int32_t)L, (int32_t)nc64, mask_id(key));
+                for (int r = r0; r < r1; ++r) {
+                    rbeg[r] = start;
+                    rlen[r] = (int32_t)L;
+                }
+                nc64 += L;
+            }
+        } else {
+            std::vector<uint32_t> mark((size_t)N * 4, 0u);
+            std::vector<int32_t> touched;
+            for (int q1 = 0; q1 < nirr; ++q1) {
+                int r0, r1;
+                rows_of(q1, r0, r1);
+                touched.clear();
+                for (int r = r0; r < r1; ++r) {
+                    const int b1 = rb1[r];
+                    rbeg[r] = ql->ptr3[r];
+                    rlen[r] = (int32_t)(ql->ptr3[r + 1] - ql->ptr3[r]);
+                    for (int64_t i = ql->ptr3[r]; i < ql->ptr3[r + 1]; ++i) {
+                        const int q2 = ql->list3[i] - 1;
+                        if (stamp[q2] == r) return set_error(kErrParam, "three-phonon sample repeats a q-point");
+                        stamp[q2] = r;
+                        uint32_t *mk = &mark[(size_t)q2 * 4];
+                        if (!(mk[0] | mk[1] | mk[2] | mk[3])) touched.push_back(q2);
+                        mk[b1 >> 5] |= 1u << (b1 & 31);
                     }
-                if (id < 0) {
-                    id = (int)table.size();
-                    table.push_back(key);
                 }
-                cand.push_back(make_int4(q1, q2, id, 0));
-                mk[0] = mk[1] = mk[2] = mk[3] = 0u;
+                std::sort(touched.begin(), touched.end());
+                for (int q2 : touched) {
+                    uint32_t *mk = &mark[(size_t)q2 * 4];
+                    cand.push_back(make_int4(q1, q2, mask_id({mk[0], mk[1], mk[2], mk[3]}), 0));
+                    mk[0] = mk[1] = mk[2] = mk[3] = 0u;
+                }
             }
-            r0 = r1;
+            nc64 = (int64_t)cand.size();
         }
         for (const auto &t : table) masks.insert(masks.end(), t.begin(), t.end());
+        if (nc64 >= ((int64_t)1 << 31) - 1 || (int64_t)slist.size() >= ((int64_t)1 << 31))
+            return set_error(kErrBadDim, "too many three-phonon candidates for one call");
     }
-    const int32_t nc = (int32_t)cand.size();
+    const int32_t nc = (int32_t)nc64;
     cudaError_t e = cudaSuccess;
     auto chk = [&](cudaError_t x) {
         if (e == cudaSuccess) e = x;
@@ -631,15 +727,25 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     chk(c->d_xi.alloc((size_t)nr * ld));
     chk(c->d_gamma.alloc(nr));
     if (o->thirdorder) {
-        chk(c->d_cand.upload(cand.data(), cand.size(), s));
         chk(c->d_mask.upload(masks.data(), masks.size(), s));
         chk(c->d_nt.alloc(nc + 1));
         chk(c->d_nrd.alloc(nc + 1));
         chk(c->d_toff.alloc(nc + 1));
         chk(c->d_roff.alloc(nc + 1));
         chk(c->d_tmp.alloc(exclusive_scan_tmp_elems(nc)));
-        chk(c->d_ptr3.upload(ql->ptr3, nr + 1, s));
-        chk(c->d_list3.upload(ql->list3, ql->ptr3[nr], s));
+        chk(c->d_rbeg.upload(rbeg.data(), rbeg.size(), s));
+        chk(c->d_rlen.upload(rlen.data(), rlen.size(), s));
+        if (shared) {
+            chk(c->d_list3.upload(slist.data(), slist.size(), s));
+            chk(c->d_qdesc.upload(qdesc.data(), qdesc.size(), s));
+            chk(c->d_cand.alloc(nc));
+            int maxL = 0;
+            for (const auto &d : qdesc) maxL = std::max(maxL, d.y);
+            chk(launch_build_candidates(c->d_qdesc.p, nirr, maxL, c->d_list3.p, c->d_cand.p, s));
+        } else {
+            chk(c->d_cand.upload(cand.data(), cand.size(), s));
+            chk(c->d_list3.upload(ql->list3, ql->ptr3[nr], s));
+        }
     }
     chk(cudaStreamSynchronize(s));
     if (e != cudaSuccess) return set_error(kErrDevice, std::string("allocation/upload failed: ") + cudaGetErrorString(e));
@@ -704,8 +810,8 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         CUDA_TRY(launch_threephonon(a, o->precision, c->n_sm, s));
         ++launches;
         CUDA_TRY(cudaEventRecord(ev[3], s));
-        CUDA_TRY(launch_sym_distribute(mesh, c->orbits, nr, c->d_row_q1.p, c->d_ptr3.p, c->d_list3.p, c->d_xi.p,
-                                       nullptr, s));
+        CUDA_TRY(launch_sym_distribute(mesh, c->orbits, nr, c->d_row_q1.p, c->d_rbeg.p, c->d_rlen.p, c->d_list3.p,
+                                       c->d_xi.p, nullptr, s));
         ++launches;
     } else {
         CUDA_TRY(cudaEventRecord(ev[2], s));
@@ -873,26 +979,35 @@ inline void rotate(const double *m, const double *v, double *out, double sg = 1.
     for (int i = 0; i < 3; ++i) out[i] = sg * (m[i] * v[0] + m[i + 3] * v[1] + m[i + 6] * v[2]);
 }
 
-// get_kappa (kappa.f90:28-75).
+// get_kappa (kappa.f90:28-75). The reference symmetrises every mode's F (x) v over the
+// operations, (1/nop) sum_R (R F) (x) (R v) = (1/nop) sum_R R (F (x) v) R^T; that map is
+// linear, so the per-mode tensors are summed first and the operations applied once.
 void get_kappa(const tdg_ctx *c, const std::vector<double> &Fn, double T, bool classical, double *kappa) {
     const int n = c->n;
-    for (int i = 0; i < 9; ++i) kappa[i] = 0.0;
+    double M[9] = {0};
     for (int q1 = 0; q1 < c->nirr; ++q1) {
         const int f = c->irr_full[q1] - 1;
         for (int b1 = 0; b1 < n; ++b1) {
             const double om1 = c->omega[(size_t)f * n + b1];
             if (om1 < kFreqTol) continue;
             const double cv = classical ? kKbHartree : harmonic_oscillator_cv(T, om1);
-            double v2[9] = {0};
-            for (int j = 0; j < c->nop; ++j) {
-                double v0[3], v1[3];
-                rotate(&c->op_cart[9 * j], &Fn[((size_t)q1 * n + b1) * 3], v0);
-                rotate(&c->op_cart[9 * j], &c->vel[((size_t)f * n + b1) * 3], v1);
-                for (int x = 0; x < 3; ++x)
-                    for (int y = 0; y < 3; ++y) v2[x + 3 * y] += v0[x] * v1[y] / c->nop;
-            }
-            for (int k = 0; k < 9; ++k) kappa[k] += cv * v2[k] / c->volume * c->irr_weight[q1];
+            const double w = cv / c->volume * c->irr_weight[q1];
+            const double *F = &Fn[((size_t)q1 * n + b1) * 3];
+            const double *v = &c->vel[((size_t)f * n + b1) * 3];
+            for (int x = 0; x < 3; ++x)
+                for (int y = 0; y < 3; ++y) M[x + 3 * y] += w * F[x] * v[y];
         }
+    }
+    for (int i = 0; i < 9; ++i) kappa[i] = 0.0;
+    for (int j = 0; j < c->nop; ++j) {
+        const double *m = &c->op_cart[9 * j];
+        for (int x = 0; x < 3; ++x)
+            for (int y = 0; y < 3; ++y) {
+                double s = 0.0;
+                for (int k = 0; k < 3; ++k)
+                    for (int l = 0; l < 3; ++l) s += m[x + 3 * k] * M[k + 3 * l] * m[y + 3 * l];
+                kappa[x + 3 * y] += s / c->nop;
+            }
     }
     double tol = 0.0;
     for (int k = 0; k < 9; ++k) tol += std::fabs(kappa[k]);

@@ -49,7 +49,11 @@ struct PhononDev {
     double sigma_fixed;      // integrationtype 1, Hartree
     double thresh_sigma;     // integrationtype 6
     int32_t integrationtype;
+    const double *exp2tab;   // [64] 2^(-j/64), the table of exp_neg
 };
+
+// exp(-t), 0 <= t <= 40, on the device (diagnostic for tests): out[i] = exp_neg(t[i]).
+cudaError_t launch_exp_neg_check(const double *t, int32_t n, double *out, const double *tab, cudaStream_t s);
 
 // Rows of the scattering matrix.
 struct RowsDev {
@@ -139,9 +143,12 @@ cudaError_t launch_isotope(const MeshDev &m, const PhononDev &ph, const RowsDev 
 struct OrbitDev {
     const int32_t *rep_ptr;  // [n_irr+1] first representative of q1
     const int32_t *rep;      // [n_rep] representative q2 (smallest member of its orbit)
-    const int32_t *img;      // [n_rep * n_op] images in operation order, -1 off grid
-    const int32_t *cnt;      // [n_rep] number of on-grid images
+    const int32_t *img;      // [n_rep * n_op] distinct on-grid images, first appearance order
+    const int32_t *mult;     // [n_rep * n_op] number of operations giving each image
+    const int32_t *nuniq;    // [n_rep] number of distinct images
+    const int32_t *cnt;      // [n_rep] number of on-grid operations (sum of mult)
     const int32_t *orb_of;   // [n_irr * n_full] representative index of q2, -1 otherwise
+    const double *rcp;       // [n_op+1] 1/i, replaces the FP64 divisions by counts
     int32_t max_rep;         // largest number of representatives of one q1
 };
 cudaError_t launch_orbit_flag(const MeshDev &m, int32_t *flag, cudaStream_t s);
@@ -149,8 +156,14 @@ cudaError_t launch_orbit_fill(const MeshDev &m, const int32_t *flag, const int32
                               cudaStream_t s);
 // K5a: symmetrize_and_distribute of one order in place on od, then xi += od when xi is
 // not null (scattering_threephonon.f90:143-205).
+// Row r's sample is list[rbeg[r] .. rbeg[r] + rlen[r]).
 cudaError_t launch_sym_distribute(const MeshDev &m, const OrbitDev &o, int32_t n_row, const int32_t *row_q1,
-                                  const int64_t *ptr, const int32_t *list, double *od, double *xi, cudaStream_t s);
+                                  const int64_t *rbeg, const int32_t *rlen, const int32_t *list, double *od, double *xi,
+                                  cudaStream_t s);
+// Candidates of q1 when all its rows share one sample: desc[q1] = (start in list, length,
+// first candidate, mask id); cand[desc.z + i] = (q1, list[desc.x + i] - 1, desc.w, 0).
+cudaError_t launch_build_candidates(const int4 *desc, int32_t n_irr, int32_t max_len, const int32_t *list, int4 *cand,
+                                    cudaStream_t s);
 // K5b: symmetrize_scatmat (scattering.f90:296-357).
 cudaError_t launch_sym_scatmat(const MeshDev &m, const OrbitDev &o, int32_t n_row, const int32_t *row_q1, double *xi,
                                cudaStream_t s);

@@ -199,3 +199,20 @@ def test_driver_matches_api(configs, tmp_path):
     sr.close()
     np.testing.assert_allclose(vals[0][:3], np.diag(ks) * KAPPA_AU_TO_SI, rtol=1e-9)
     np.testing.assert_allclose(vals[3][:3], np.diag(ki) * KAPPA_AU_TO_SI, rtol=1e-9)
+
+
+def test_device_exponential_accuracy(built):
+    """The FP64 exp(-t) of the delta weights (Cody-Waite reduction, 2^(-j/64) table,
+    Taylor series) stays within 2 ulp of the host libm over the lo_gauss window."""
+    import ctypes as C
+    import math
+
+    from tdep_gb300 import _native as N
+
+    rng = np.random.default_rng(0)
+    t = np.concatenate([np.linspace(0.0, 40.0, 20001), rng.uniform(0.0, 40.0, 50000), [0.0, 1e-300, 1e-12, 32.0]])
+    out = np.zeros_like(t)
+    N.check(N.lib().tdg_check_exp(N.ptr(t, C.c_double), t.size, N.ptr(out, C.c_double)), "tdg_check_exp")
+    ref = np.array([math.exp(-x) for x in t])
+    ulp = np.spacing(ref)
+    assert np.max(np.abs(out - ref) / ulp) <= 2.0
