@@ -196,6 +196,24 @@ int tdg_triplets(tdg_ctx *ctx, int32_t q1, const int32_t *sample, int64_t n, int
                  int64_t *written);
 
 /*
+ * tdg_triplets without device allocation: same arguments and same output, bit for bit.
+ * This entry point has no counterpart in the reference; it exists for callers that
+ * cannot call cudaMalloc at the time of the call. Its device scratch is one fixed
+ * file-scope array (about 4.3 MiB per device) instead of per-call allocations, so it
+ * calls no cudaMalloc, cudaFree or other allocating routine.
+ * Limits: n <= 32768 q-points, and at most 131072 equivalent triplets in the result
+ * (always met on meshes of up to 131072 points); beyond either, TDG_ERR_PARAM with a
+ * message naming the limit, before any device work on the result.
+ * The first call on each device looks the array up (cudaGetSymbolAddress, which loads the
+ * module); make that first call before any stream capture. Only the status word of the
+ * scratch must start at zero, and each call clears it itself. All calls on one device
+ * share the array: calls that overlap in time (several threads or contexts on the same
+ * device) race, so the caller serialises them.
+ */
+int tdg_triplets_static(tdg_ctx *ctx, int32_t q1, const int32_t *sample, int64_t n, int32_t *out, int64_t cap,
+                        int64_t *written);
+
+/*
  * Thermal conductivity from the current scattering state (main.f90:216-244):
  * kappa_sma (get_kappa, kappa.f90:28-75), the iterative BTE (kappa.f90:326-495) with
  * maxiter steps and tolerance tol, kappa_iter, both symmetrised (kappa.f90:308-324).

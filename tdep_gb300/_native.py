@@ -114,6 +114,7 @@ SIGNATURES = {
     "tdg_scattering": (C.c_int, [C.c_void_p, C.POINTER(TdgOpts), C.POINTER(TdgQlists), _f64p, _f64p, _f64p]),
     "tdg_get_xi": (C.c_int, [C.c_void_p, _f64p]),
     "tdg_triplets": (C.c_int, [C.c_void_p, C.c_int32, _i32p, C.c_int64, _i32p, C.c_int64, _i64p]),
+    "tdg_triplets_static": (C.c_int, [C.c_void_p, C.c_int32, _i32p, C.c_int64, _i32p, C.c_int64, _i64p]),
     "tdg_kappa": (C.c_int, [C.c_void_p, C.POINTER(TdgOpts), C.c_int32, C.c_double, _f64p, _f64p, _f64p, _i32p]),
     "tdg_problem_load": (C.c_int, [C.c_char_p, _i32p, C.c_int, C.c_int, C.c_int, C.POINTER(C.POINTER(TdgProblem))]),
     "tdg_problem_free": (None, [C.POINTER(TdgProblem)]),

@@ -1137,3 +1137,11 @@ extern "C" int tdg_kappa(tdg_ctx *c, const tdg_opts *o, int32_t maxiter, double 
     if (n_iter) *n_iter = iters;
     return kOk;
 }
+
+tdg::CtxView tdg::ctx_view(const tdg_ctx *c) {
+    CtxView v;
+    v.device = c->device;
+    v.stream = c->stream;
+    v.mesh = c->mesh();
+    return v;
+}

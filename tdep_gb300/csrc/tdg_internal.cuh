@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+struct tdg_ctx;
+
 namespace tdg {
 
 // Work item of the three-phonon kernel: one accepted irreducible q-triplet.
@@ -170,5 +172,13 @@ cudaError_t launch_sym_scatmat(const MeshDev &m, const OrbitDev &o, int32_t n_ro
 // K8: buf[r*3+a] = sum_j xi[r, j] * fbb[j*3 + a].
 cudaError_t launch_xi_gemv(const double *xi, int32_t n_row, int64_t n_col, const double *fbb, double *buf,
                            int n_sm, cudaStream_t s);
+
+// What an entry point compiled outside the context's own file needs of a context.
+struct CtxView {
+    int device;
+    cudaStream_t stream;
+    MeshDev mesh;
+};
+CtxView ctx_view(const tdg_ctx *c);
 
 }  // namespace tdg
