@@ -51,6 +51,13 @@ CONFIGS = {
                        workload="rocksalt Na/Cl 2-atom (6 modes), 12x12x12 mesh, adaptive smearing, T=300 K"),
     "perovskite8": dict(synth="perovskite", grid=(8, 8, 8), it=2, temperature=300.0,
                         workload="cubic perovskite 5-atom (15 modes), 8x8x8 mesh, adaptive smearing, T=300 K"),
+    # the smallest cases whose scattering matrix (171 MB, 261 MB) exceeds the 129 MB L2
+    "rocksalt16": dict(synth="rocksalt", grid=(16, 16, 16), it=2, temperature=300.0,
+                       workload="rocksalt Na/Cl 2-atom (6 modes), 16x16x16 mesh, adaptive smearing, T=300 K, "
+                                "full q' grid"),
+    "perovskite12": dict(synth="perovskite", grid=(12, 12, 12), it=2, temperature=300.0, uneven=(200, 1700),
+                         workload="cubic perovskite 5-atom (15 modes), 12x12x12 mesh, adaptive smearing, T=300 K, "
+                                  "seeded per-q1 q' samples of 200-1700 points"),
 }
 
 
