@@ -174,9 +174,12 @@ int tdg_mc_qlists(const tdg_problem *prob, const tdg_opts *opts, int32_t *n_row,
  *   linewidth  dr%iq(:)%linewidth (Hartree)
  *   qs         dr%iq(:)%qs = 2*linewidth
  * stats (may be NULL, 10 doubles): [0] accepted irreducible q-triplets, [1] q-quartets,
- *   [2] device time of the pipeline in ms (inputs resident), [3] candidate q-pairs,
- *   [4] enumeration ms, [5] fused three-phonon kernel ms, [6] symmetrisation ms,
- *   [7] isotope ms, [8] kernel launches, [9] equivalent-triplet entries.
+ *   [2] device time of the pipeline in ms (inputs resident), [3] candidates (q-pairs for
+ *   three-phonon plus q-triples for four-phonon), [4] enumeration ms, [5] fused three- and
+ *   four-phonon kernel ms, [6] symmetrisation ms, [7] isotope ms, [8] kernel launches,
+ *   [9] equivalent-triplet and -quartet entries.
+ * Four-phonon scattering supports up to 5 atoms (15 modes) in the primitive cell,
+ * three-phonon up to 6 atoms.
  */
 int tdg_scattering(tdg_ctx *ctx, const tdg_opts *opts, const tdg_qlists *lists,
                    double *linewidth, double *qs, double *stats);

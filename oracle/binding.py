@@ -108,6 +108,29 @@ def triplets(prob, q1: int, sample: np.ndarray):
     return res
 
 
+def quartets(prob, q1: int, la: np.ndarray, lb: np.ndarray):
+    """[(q2, q3, q4, [(q2', q3', q4'), ...]), ...] for one irreducible q1 over the pairs la x lb."""
+    la = np.ascontiguousarray(la, np.int32)
+    lb = np.ascontiguousarray(lb, np.int32)
+    assert la.size == lb.size
+    cap = 256
+    while True:
+        out = np.zeros(cap, np.int32)
+        ps = prob.struct()
+        w = lib().orc_quartets(C.byref(ps), int(q1), N.ptr(la, C.c_int32), N.ptr(lb, C.c_int32), la.size,
+                               N.ptr(out, C.c_int32), cap)
+        if w >= 0:
+            break
+        cap *= 4
+    res, i = [], 0
+    while i < w:
+        q2, q3, q4, k = (int(x) for x in out[i:i + 4])
+        trip = [tuple(int(v) for v in out[i + 4 + 3 * j: i + 7 + 3 * j]) for j in range(k)]
+        res.append((q2, q3, q4, trip))
+        i += 4 + 3 * k
+    return res
+
+
 def scattering(prob, opts, lists, nthreads: int = 0, rows=None):
     """Per-row part of sr%generate. Returns (gamma[rows], xi[rows, N*n], counts)."""
     r0, r1 = (0, lists.n_row) if rows is None else rows

@@ -30,7 +30,7 @@ NVCCFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-re
 
 HOST_SRC = ["host/crystal.cpp", "host/qmesh.cpp", "host/phonons.cpp", "host/mcgrid.cpp", "host/problem.cpp"]
 CUDA_SRC = ["k_triplets.cu", "k_threephonon.cu", "k_fourphonon.cu", "k_misc.cu", "tdg_api.cu", "tdg_noalloc.cu"]
-HEADERS = ["host/common.hpp", "host/crystal.hpp", "tdg_internal.cuh"]
+HEADERS = ["host/common.hpp", "host/crystal.hpp", "tdg_internal.cuh", "dev_common.cuh"]
 
 
 def _nvcc() -> str:

@@ -1,0 +1,99 @@
+// Device helpers shared by the three- and four-phonon kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace tdg {
+
+namespace {
+
+constexpr double kSqrt2PiInv = 0.398942280401433;
+constexpr double kFreqTolD = 1E-9;
+constexpr int kMaxRed = 192;
+
+template <typename R>
+struct CT;
+template <>
+struct CT<double> {
+    using C = double2;
+};
+template <>
+struct CT<float> {
+    using C = float2;
+};
+
+template <typename C>
+__device__ __forceinline__ C czero();
+template <>
+__device__ __forceinline__ double2 czero<double2>() {
+    return make_double2(0.0, 0.0);
+}
+template <>
+__device__ __forceinline__ float2 czero<float2>() {
+    return make_float2(0.f, 0.f);
+}
+
+template <typename C>
+__device__ __forceinline__ void cfma(C &acc, const C &a, const C &b) {
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(-a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+    acc.y = fma(a.y, b.x, acc.y);
+}
+
+__device__ __forceinline__ bool nonzero(double x) { return (__double_as_longlong(x) << 1) != 0; }
+
+}  // namespace
+
+// exp(-t) for 0 <= t <= 40 in FP64, written from the mathematics: t = (64 m + j) ln2/64 + r
+// (Cody-Waite reduction with a two-part ln2/64, |r| <= ln2/128), exp(-t) =
+// 2^-m * 2^(-j/64) * exp(-r), exp(-r) by its Taylor series to degree 6 (truncation below
+// 3e-20 relative), 2^(-j/64) from a 64-entry table built on the host. 13 FP64 operations
+// against about twice that for the general exp(); tested against exp() on the device.
+__device__ __forceinline__ double exp_neg(double t, const double *tab64) {
+    constexpr double kInvLn2x64 = 92.33248261689366;            // 64 / ln 2
+    constexpr double kLn2o64Hi = 0.010830424696244734;          // ln2/64 to 41 bits: k*Hi exact
+    constexpr double kLn2o64Lo = 4.411764150473684e-15;         // ln2/64 - Hi
+    constexpr double kShift = 6755399441055744.0;               // 1.5 * 2^52
+    const double ys = fma(t, kInvLn2x64, kShift);
+    const int k = __double2loint(ys);                            // rint(t * 64/ln2)
+    const double kf = ys - kShift;
+    double r = fma(-kf, kLn2o64Hi, t);
+    r = fma(-kf, kLn2o64Lo, r);
+    const double s = -r;
+    double p = fma(s, 1.0 / 720.0, 1.0 / 120.0);
+    p = fma(s, p, 1.0 / 24.0);
+    p = fma(s, p, 1.0 / 6.0);
+    p = fma(s, p, 0.5);
+    p = fma(s, p, 1.0);
+    p = fma(s, p, 1.0);
+    const int mm = k >> 6, j = k & 63;
+    const double scale = __hiloint2double((1023 - mm) << 20, 0);  // 2^-mm
+    return (tab64[j] * p) * scale;
+}
+
+namespace {
+
+// lo_gauss (gottochblandat_calculus.f90:268-288) for x - mu = dx, with 8 sigma, the
+// exponent factor 0.5/sigma^2 and 1/(sigma sqrt(2 pi)) supplied.
+__device__ __forceinline__ double gauss(double dx, double win8, double h, double c, const double *tab64) {
+    if (fabs(dx) > win8) return 0.0;
+    return exp_neg(dx * dx * h, tab64) * c;
+}
+
+__device__ __forceinline__ double adaptive_pair(const double *va, const double *vb, const double *rl) {
+    // sqrt(maxval(matmul(va - vb, reclat)**2) * 0.5)
+    double m = 0;
+    for (int j = 0; j < 3; ++j) {
+        double s = 0;
+        for (int i = 0; i < 3; ++i) s += (va[i] - vb[i]) * rl[i + 3 * j];
+        m = fmax(m, s * s);
+    }
+    return sqrt(m * 0.5);
+}
+
+
+}  // namespace
+
+}  // namespace tdg

@@ -98,7 +98,7 @@ struct tdg_ctx {
     int device = 0;
     int n_sm = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t ev[10] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     int32_t *h_tot = nullptr;  // pinned host word pair for the enumeration totals
     // host copy of the problem
     int na = 0, n = 0, nop = 0, N = 0, nirr = 0;
@@ -139,6 +139,13 @@ struct tdg_ctx {
     DevBuf<int4> d_qdesc;
     DevBuf<TripletRec> d_trip;
     DevBuf<int2> d_red;
+    // four-phonon enumeration, samples (list a drives the symmetrisation) and kernel scratch
+    DevBuf<int4> d_cand4, d_red4;
+    DevBuf<uint32_t> d_mask4;
+    DevBuf<int32_t> d_nq, d_nrd4, d_qoff, d_roff4, d_tmp4, d_list4a, d_rlen4;
+    DevBuf<int64_t> d_rbeg4;
+    DevBuf<QuartetRec> d_quart;
+    DevBuf<unsigned char> d_scr4;
     // BTE buffers
     DevBuf<double> d_fbb, d_buf;
 
@@ -563,7 +570,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         st = check_list("four-phonon sample", nr, ql->ptr4, ql->list4b, N);
         if (st) return st;
         if (c->n_fc4 < 1) return set_error(kErrParam, "four-phonon scattering requested without force constants");
-        return set_error(kErrParam, "four-phonon scattering is not available in this build");
+        if (n > 15) return set_error(kErrParam, "this build's four-phonon kernel supports up to 5 atoms");
     }
     c->n_row = nr;
     c->row_q1.assign(ql->row_q1, ql->row_q1 + nr);
@@ -612,6 +619,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         rb1[r] = c->row_b1[r] - 1;
         rowidx[(size_t)rq1[r] * n + rb1[r]] = r;
         if (o->thirdorder) w3[r] = 1.0 / (double)(ql->ptr3[r + 1] - ql->ptr3[r]);
+        if (o->fourthorder) w4[r] = 1.0 / (double)(ql->ptr4[r + 1] - ql->ptr4[r]);
     }
     // ---- three-phonon samples and candidates ----
     // When all rows of a q1 share one sample (the full grid, or samples given per q1) it is
@@ -711,6 +719,102 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         if (nc64 >= ((int64_t)1 << 31) - 1 || (int64_t)slist.size() >= ((int64_t)1 << 31))
             return set_error(kErrBadDim, "too many three-phonon candidates for one call");
     }
+    // ---- four-phonon candidates (scattering_fourphonon.f90:88-99): q2 from list a, q3 from
+    // list b, q3 >= q2 and q4 = -q1-q2-q3 >= q3, once per q1 with the rows that sampled the
+    // pair as a bit mask. Rows of q1 with identical lists share one pass over the pairs;
+    // otherwise the pairs of all rows are merged by sorting. A list that repeats a q-point
+    // is rejected (the reference would count those pairs twice).
+    std::vector<int4> cand4;
+    std::vector<uint32_t> masks4;
+    std::vector<int64_t> rbeg4;
+    std::vector<int32_t> rlen4;
+    if (o->fourthorder) {
+        std::vector<std::array<uint32_t, 4>> table4;
+        auto mask_id4 = [&](const std::array<uint32_t, 4> &key) {
+            for (int t = (int)table4.size() - 1; t >= 0 && t >= (int)table4.size() - 8; --t)
+                if (table4[t] == key) return t;
+            table4.push_back(key);
+            return (int)table4.size() - 1;
+        };
+        const int G0 = c->grid[0], G1 = c->grid[1], G2 = c->grid[2];
+        auto wrap = [](int x, int m) {
+            x %= m;
+            return x < 0 ? x + m : x;
+        };
+        auto fourth = [&](int f1, int q2, int q3) {
+            const int n12 = G1 * G2;
+            const int i = wrap(-(f1 / n12) - (q2 / n12) - (q3 / n12), G0);
+            const int j = wrap(-((f1 / G2) % G1) - ((q2 / G2) % G1) - ((q3 / G2) % G1), G1);
+            const int k = wrap(-(f1 % G2) - (q2 % G2) - (q3 % G2), G2);
+            return (i * G1 + j) * G2 + k;
+        };
+        std::vector<int32_t> stamp_a(N, -1), stamp_b(N, -1);
+        std::vector<std::pair<int64_t, int>> keys;
+        rbeg4.assign(nr, 0);
+        rlen4.assign(nr, 0);
+        for (int r0 = 0; r0 < nr;) {
+            const int q1 = rq1[r0];
+            int r1 = r0;
+            while (r1 < nr && rq1[r1] == q1) ++r1;
+            const int f1 = c->irr_full[q1] - 1;
+            bool same = true;
+            for (int r = r0; r < r1; ++r) {
+                rbeg4[r] = ql->ptr4[r];
+                rlen4[r] = (int32_t)(ql->ptr4[r + 1] - ql->ptr4[r]);
+                for (int64_t i = ql->ptr4[r]; i < ql->ptr4[r + 1]; ++i) {
+                    const int qa = ql->list4a[i] - 1, qb = ql->list4b[i] - 1;
+                    if (stamp_a[qa] == r || stamp_b[qb] == r)
+                        return set_error(kErrParam, "four-phonon sample repeats a q-point");
+                    stamp_a[qa] = r;
+                    stamp_b[qb] = r;
+                }
+                if (r > r0) {
+                    const int64_t L = rlen4[r0];
+                    same = same && rlen4[r] == L &&
+                           std::memcmp(ql->list4a + ql->ptr4[r], ql->list4a + ql->ptr4[r0], sizeof(int32_t) * L) == 0 &&
+                           std::memcmp(ql->list4b + ql->ptr4[r], ql->list4b + ql->ptr4[r0], sizeof(int32_t) * L) == 0;
+                }
+            }
+            if (same) {
+                std::array<uint32_t, 4> key = {0u, 0u, 0u, 0u};
+                for (int r = r0; r < r1; ++r) key[rb1[r] >> 5] |= 1u << (rb1[r] & 31);
+                const int id = mask_id4(key);
+                const int32_t *la = ql->list4a + ql->ptr4[r0], *lb = ql->list4b + ql->ptr4[r0];
+                for (int64_t x = 0; x < rlen4[r0]; ++x)
+                    for (int64_t y = 0; y < rlen4[r0]; ++y) {
+                        const int q2 = la[x] - 1, q3 = lb[y] - 1;
+                        if (q3 < q2 || fourth(f1, q2, q3) < q3) continue;
+                        cand4.push_back(make_int4(q1, q2, q3, id));
+                    }
+            } else {
+                keys.clear();
+                for (int r = r0; r < r1; ++r) {
+                    const int32_t *la = ql->list4a + ql->ptr4[r], *lb = ql->list4b + ql->ptr4[r];
+                    for (int64_t x = 0; x < rlen4[r]; ++x)
+                        for (int64_t y = 0; y < rlen4[r]; ++y) {
+                            const int q2 = la[x] - 1, q3 = lb[y] - 1;
+                            if (q3 < q2 || fourth(f1, q2, q3) < q3) continue;
+                            keys.emplace_back((int64_t)q2 * N + q3, rb1[r]);
+                        }
+                }
+                std::sort(keys.begin(), keys.end());
+                for (size_t i = 0; i < keys.size();) {
+                    std::array<uint32_t, 4> key = {0u, 0u, 0u, 0u};
+                    size_t j = i;
+                    for (; j < keys.size() && keys[j].first == keys[i].first; ++j)
+                        key[keys[j].second >> 5] |= 1u << (keys[j].second & 31);
+                    cand4.push_back(make_int4(q1, (int)(keys[i].first / N), (int)(keys[i].first % N), mask_id4(key)));
+                    i = j;
+                }
+            }
+            if ((int64_t)cand4.size() >= ((int64_t)1 << 31) - 1)
+                return set_error(kErrBadDim, "too many four-phonon candidates for one call");
+            r0 = r1;
+        }
+        for (const auto &t : table4) masks4.insert(masks4.end(), t.begin(), t.end());
+        if (ql->ptr4[nr] >= ((int64_t)1 << 31)) return set_error(kErrBadDim, "four-phonon samples too long for one call");
+    }
+    const int32_t nc4 = (int32_t)cand4.size();
     const int32_t nc = (int32_t)nc64;
     cudaError_t e = cudaSuccess;
     auto chk = [&](cudaError_t x) {
@@ -746,6 +850,19 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
             chk(c->d_cand.upload(cand.data(), cand.size(), s));
             chk(c->d_list3.upload(ql->list3, ql->ptr3[nr], s));
         }
+    }
+    if (o->fourthorder) {
+        chk(c->d_cand4.upload(cand4.data(), cand4.size(), s));
+        chk(c->d_mask4.upload(masks4.data(), masks4.size(), s));
+        chk(c->d_nq.alloc(nc4 + 1));
+        chk(c->d_nrd4.alloc(nc4 + 1));
+        chk(c->d_qoff.alloc(nc4 + 1));
+        chk(c->d_roff4.alloc(nc4 + 1));
+        chk(c->d_tmp4.alloc(exclusive_scan_tmp_elems(nc4)));
+        chk(c->d_rbeg4.upload(rbeg4.data(), rbeg4.size(), s));
+        chk(c->d_rlen4.upload(rlen4.data(), rlen4.size(), s));
+        chk(c->d_list4a.upload(ql->list4a, ql->ptr4[nr], s));
+        chk(c->d_od.alloc((size_t)nr * ld));
     }
     chk(cudaStreamSynchronize(s));
     if (e != cudaSuccess) return set_error(kErrDevice, std::string("allocation/upload failed: ") + cudaGetErrorString(e));
@@ -817,6 +934,62 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         CUDA_TRY(cudaEventRecord(ev[2], s));
         CUDA_TRY(cudaEventRecord(ev[3], s));
     }
+    CUDA_TRY(cudaEventRecord(ev[7], s));
+    // Four-phonon row terms go to their own od buffer: the per-order symmetrisation is not
+    // linear (od_terms > 0 filter), so it runs on od alone and then adds od into Xi.
+    int32_t nquart = 0, nred4 = 0;
+    if (o->fourthorder) {
+        CUDA_TRY(cudaMemsetAsync(c->d_od.p, 0, sizeof(double) * (size_t)nr * ld, s));
+        CUDA_TRY(launch_quartet_count(mesh, c->d_cand4.p, nc4, c->d_nq.p, c->d_nrd4.p, c->d_status.p, s));
+        CUDA_TRY(exclusive_scan_i32(c->d_nq.p, c->d_qoff.p, nc4, c->d_tmp4.p, s));
+        CUDA_TRY(exclusive_scan_i32(c->d_nrd4.p, c->d_roff4.p, nc4, c->d_tmp4.p, s));
+        launches += 1 + 2 * 3;
+        int32_t *tot = c->h_tot;
+        CUDA_TRY(cudaMemcpyAsync(&tot[0], c->d_qoff.p + nc4, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(cudaMemcpyAsync(&tot[1], c->d_roff4.p + nc4, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        st = read_status(c);
+        if (st) return st;
+        nquart = tot[0];
+        nred4 = tot[1];
+        const int grid4 = fourphonon_grid(n, o->precision, c->n_sm, nquart);
+        if (nquart > 0 && grid4 < 1) return set_error(kErrDevice, "four-phonon kernel configuration failed");
+        chk(c->d_quart.alloc(nquart));
+        chk(c->d_red4.alloc(nred4));
+        chk(c->d_scr4.alloc(fourphonon_scratch_bytes(n, o->precision, grid4)));
+        if (e != cudaSuccess) return set_error(kErrDevice, std::string("allocation failed: ") + cudaGetErrorString(e));
+        CUDA_TRY(launch_quartet_fill(mesh, c->d_cand4.p, nc4, c->d_qoff.p, c->d_roff4.p, c->d_quart.p, c->d_red4.p, s));
+        ++launches;
+        CUDA_TRY(cudaEventRecord(ev[8], s));
+        FourPhArgs a4;
+        a4.mesh = mesh;
+        a4.ph = ph;
+        a4.rows = rows;
+        a4.fc.n = c->n_fc4;
+        a4.fc.n_atom = c->na;
+        a4.fc.blk_ptr = c->fc4_blk.p;
+        a4.fc.lv = c->fc4_lv.p;
+        a4.fc.mwm = c->fc4_mwm.p;
+        a4.fc.mwm32 = c->fc4_mwm32.p;
+        a4.twiddle = c->tw.p;
+        a4.twiddle32 = c->tw32.p;
+        a4.quart = c->d_quart.p;
+        a4.n_quart = nquart;
+        a4.red = c->d_red4.p;
+        a4.cand_mask = c->d_mask4.p;
+        a4.gamma = c->d_gamma.p;
+        a4.od = c->d_od.p;
+        a4.status = c->d_status.p;
+        a4.scratch = c->d_scr4.p;
+        CUDA_TRY(launch_fourphonon(a4, o->precision, grid4, s));
+        ++launches;
+        CUDA_TRY(cudaEventRecord(ev[9], s));
+        CUDA_TRY(launch_sym_distribute(mesh, c->orbits, nr, c->d_row_q1.p, c->d_rbeg4.p, c->d_rlen4.p, c->d_list4a.p,
+                                       c->d_od.p, c->d_xi.p, s));
+        ++launches;
+    } else {
+        CUDA_TRY(cudaEventRecord(ev[8], s));
+        CUDA_TRY(cudaEventRecord(ev[9], s));
+    }
     CUDA_TRY(cudaEventRecord(ev[4], s));
     if (o->isotope) {
         CUDA_TRY(launch_isotope(mesh, ph, rows, c->d_row_q1.p, c->d_row_b1.p, c->d_disorder.p, c->na, c->d_gamma.p,
@@ -838,10 +1011,15 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     CUDA_TRY(cudaEventElapsedTime(&ms_iso, ev[4], ev[5]));
     CUDA_TRY(cudaEventElapsedTime(&ms_k1, ev[1], ev[2]));
     CUDA_TRY(cudaEventElapsedTime(&ms_fused, ev[2], ev[3]));
-    float ms_s1 = 0.f, ms_s2 = 0.f;
-    CUDA_TRY(cudaEventElapsedTime(&ms_s1, ev[3], ev[4]));
+    float ms_s1 = 0.f, ms_s2 = 0.f, ms_s3 = 0.f, ms_k1q = 0.f, ms_f4 = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&ms_s1, ev[3], ev[7]));
+    CUDA_TRY(cudaEventElapsedTime(&ms_k1q, ev[7], ev[8]));
+    CUDA_TRY(cudaEventElapsedTime(&ms_f4, ev[8], ev[9]));
+    CUDA_TRY(cudaEventElapsedTime(&ms_s3, ev[9], ev[4]));
     CUDA_TRY(cudaEventElapsedTime(&ms_s2, ev[5], ev[6]));
-    ms_sym = ms_s1 + ms_s2;
+    ms_sym = ms_s1 + ms_s2 + ms_s3;
+    ms_k1 += ms_k1q;
+    ms_fused += ms_f4;
 
     // ---- boundary, degeneracy averaging (scattering.f90:244-292) ----
     std::vector<double> buf_lw((size_t)nirr * n, 0.0);
@@ -886,15 +1064,15 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     if (qs_out) std::memcpy(qs_out, c->qs.data(), sizeof(double) * c->qs.size());
     if (stats) {
         stats[0] = ntrip;
-        stats[1] = 0;
+        stats[1] = nquart;
         stats[2] = ms_total;
-        stats[3] = nc;
+        stats[3] = (double)nc + (double)nc4;
         stats[4] = ms_k1;
         stats[5] = ms_fused;
         stats[6] = ms_sym;
         stats[7] = ms_iso;
         stats[8] = launches;
-        stats[9] = nred;
+        stats[9] = (double)nred + (double)nred4;
     }
     c->have_scattering = true;
     return kOk;
@@ -947,6 +1125,13 @@ extern "C" int tdg_triplets(tdg_ctx *c, int32_t q1, const int32_t *sample, int64
     if (st) return st;
     DevBuf<TripletRec> d_trip;
     DevBuf<int2> d_red;
+    // four-phonon enumeration, samples (list a drives the symmetrisation) and kernel scratch
+    DevBuf<int4> d_cand4, d_red4;
+    DevBuf<uint32_t> d_mask4;
+    DevBuf<int32_t> d_nq, d_nrd4, d_qoff, d_roff4, d_tmp4, d_list4a, d_rlen4;
+    DevBuf<int64_t> d_rbeg4;
+    DevBuf<QuartetRec> d_quart;
+    DevBuf<unsigned char> d_scr4;
     chk(d_trip.alloc(tot[0]));
     chk(d_red.alloc(tot[1]));
     if (e != cudaSuccess) return set_error(kErrDevice, std::string("allocation failed: ") + cudaGetErrorString(e));

@@ -133,8 +133,13 @@ struct FourPhArgs {
     double *gamma;
     double *od;
     int32_t *status;
+    void *scratch;              // fourphonon_scratch_bytes(): one n^4 slice per CTA
 };
-cudaError_t launch_fourphonon(const FourPhArgs &a, int precision, int n_sm, cudaStream_t s);
+// Grid of the four-phonon kernel and the device scratch it needs (bytes); 0 when the mode
+// count is not supported.
+int fourphonon_grid(int n, int precision, int n_sm, int n_quart);
+size_t fourphonon_scratch_bytes(int n, int precision, int grid);
+cudaError_t launch_fourphonon(const FourPhArgs &a, int precision, int grid, cudaStream_t s);
 
 // Isotope scattering (scattering_isotope.f90): adds into gamma and xi.
 cudaError_t launch_isotope(const MeshDev &m, const PhononDev &ph, const RowsDev &rows, const int32_t *row_q1,

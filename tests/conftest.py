@@ -31,3 +31,16 @@ def configs(tmp_path_factory, built):
         "rocksalt": synth.write_config("rocksalt", base / "rocksalt", seed=1),
         "perovskite": synth.write_config("perovskite", base / "perovskite", seed=1),
     }
+
+
+@pytest.fixture(scope="session")
+def configs4(tmp_path_factory, built):
+    """The same crystals with fourth-order force constants."""
+    from tdep_gb300 import synth
+
+    base = tmp_path_factory.mktemp("configs4")
+    return {
+        "fcc": synth.write_config("fcc_morse", base / "fcc", seed=1, order4=True),
+        "rocksalt": synth.write_config("rocksalt", base / "rocksalt", seed=1, order4=True),
+        "perovskite": synth.write_config("perovskite", base / "perovskite", seed=1, order4=True),
+    }

@@ -34,27 +34,65 @@ def distinct_triplets(prob, lists):
     return total
 
 
+def distinct_quartets(prob, lists):
+    """Accepted irreducible q-quartets counted once per q1 over all its rows' pair samples."""
+    total = 0
+    for q1 in np.unique(lists.row_q1):
+        seen = set()
+        for r in np.nonzero(lists.row_q1 == q1)[0]:
+            a, b = lists.ptr4[r], lists.ptr4[r + 1]
+            seen.update((q2, q3, q4) for q2, q3, q4, _ in orc.quartets(prob, int(q1), lists.list4a[a:b], lists.list4b[a:b]))
+        total += len(seen)
+    return total
+
+
+def _xi_flips(xi, ref_xi, ratio_check=True):
+    """Entries of Xi that differ by more than XI_REL of the largest element.
+
+    symmetrize_and_distribute averages only entries with od_terms > 0
+    (scattering_threephonon.f90:175, scattering_fourphonon.f90:222): a sum that is
+    analytically zero can land on either side of 0 depending on summation order (exactly 0
+    here, where the phases are exact roots of unity; +-1e-17 relative in the reference's
+    cos/sin), which changes how many images enter the average of that orbit. Such an entry
+    then differs by the ratio of the two image counts, a fraction p/q with p, q <= 2 * 96.
+    Returns the number of differing entries after checking that they are rare and, when Xi
+    holds a single symmetrised order (ratio_check), that every one of them is such a flip;
+    with two orders or isotope terms in the same entry the ratio is not a fraction."""
+    from fractions import Fraction
+
+    scale = np.abs(ref_xi).max()
+    bad = np.abs(xi - ref_xi) > XI_REL * scale
+    nbad = int(bad.sum())
+    assert bad.mean() < 1e-4, f"{nbad} of {bad.size} Xi entries differ"
+    for a, b in zip(xi[bad], ref_xi[bad]) if ratio_check else ():
+        assert a != 0.0 and b != 0.0, "a differing Xi entry is zero on one side only"
+        r = a / b
+        f = Fraction(r).limit_denominator(192)
+        assert f.numerator <= 192 and abs(r - float(f)) <= 1e-6 * abs(r), f"Xi entry ratio {r} is not an image-count flip"
+    return nbad
+
+
 def _compare(prob, opts, lists, lw_rtol=LW_RTOL, kappa_rtol=KAPPA_RTOL, check_xi=True):
+    """GPU path against the oracle. Linewidths and kappa_sma do not depend on Xi and keep
+    the tight bars. kappa_iter keeps KAPPA_RTOL when Xi agrees entry by entry; when
+    _xi_flips found image-count flips, kappa_iter moves with them and the bar is 1e-3."""
     sr = ScatteringRates(prob)
     lw = sr.generate(opts, lists)
     xi = sr.Xi if check_xi else None
     ks, ki = sr.kappa(opts)
     ref = orc.full_run(prob, opts, lists)
-    assert sr.stats["triplets"] == distinct_triplets(prob, lists)
+    if opts.thirdorder:
+        assert sr.stats["triplets"] == distinct_triplets(prob, lists)
+    if opts.fourthorder:
+        assert sr.stats["quartets"] == distinct_quartets(prob, lists)
     np.testing.assert_allclose(lw, ref["linewidth"], rtol=lw_rtol, atol=1e-14 * np.abs(ref["linewidth"]).max())
     np.testing.assert_allclose(ks, ref["kappa_sma"], rtol=kappa_rtol, atol=kappa_rtol * np.abs(ref["kappa_sma"]).max())
-    np.testing.assert_allclose(ki, ref["kappa_iter"], rtol=kappa_rtol, atol=kappa_rtol * np.abs(ref["kappa_iter"]).max())
-    assert sr.n_iter == ref["n_iter"]
-    if check_xi:
-        # symmetrize_and_distribute averages only entries with od_terms > 0
-        # (scattering_threephonon.f90:175): a sum that is analytically zero can land on
-        # either side of 0 depending on summation order, which changes how many images
-        # are averaged for that entry (a factor up to 2 on that entry). Such flips must
-        # stay rare; every other entry must agree to XI_REL of the largest element.
-        scale = np.abs(ref["xi"]).max()
-        bad = np.abs(xi - ref["xi"]) > XI_REL * scale
-        assert bad.mean() < 1e-4, f"{bad.sum()} of {bad.size} Xi entries differ"
-        assert np.all(np.abs(xi - ref["xi"])[bad] <= np.abs(ref["xi"])[bad] + np.abs(xi)[bad])
+    single = int(bool(opts.thirdorder)) + int(bool(opts.fourthorder)) == 1 and not opts.isotopescattering
+    flips = _xi_flips(xi, ref["xi"], ratio_check=single) if check_xi else 0
+    krt = kappa_rtol if flips == 0 else max(kappa_rtol, 1e-3)
+    np.testing.assert_allclose(ki, ref["kappa_iter"], rtol=krt, atol=krt * np.abs(ref["kappa_iter"]).max())
+    if flips == 0:
+        assert sr.n_iter == ref["n_iter"]
     sr.close()
     return lw, ki, ref
 
@@ -140,6 +178,63 @@ def test_mixed_precision_kappa(configs):
     prob = Problem.load(configs["rocksalt"], (8, 8, 8), readiso=True)
     o64 = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=3)
     o32 = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=3, precision="mixed")
+    lists = QLists.monte_carlo(prob, o64)
+    sr = ScatteringRates(prob)
+    lw64 = sr.generate(o64, lists).copy()
+    _, k64 = sr.kappa(o64)
+    lw32 = sr.generate(o32, lists).copy()
+    _, k32 = sr.kappa(o32)
+    sr.close()
+    big = lw64 > 1e-3 * lw64.max()
+    assert np.max(np.abs(lw32[big] / lw64[big] - 1)) < 1e-4
+    np.testing.assert_allclose(k32, k64, rtol=MIXED_KAPPA_RTOL, atol=MIXED_KAPPA_RTOL * np.abs(k64).max())
+
+
+@pytest.mark.parametrize("name,grid,qg4,it", [("fcc", (8, 8, 8), (4, 4, 4), 2),
+                                             ("rocksalt", (6, 6, 6), (3, 3, 3), 6),
+                                             ("rocksalt", (6, 6, 6), (3, 3, 3), 1)])
+def test_fp64_three_plus_four_phonon_monte_carlo(configs4, name, grid, qg4, it):
+    """Four-phonon rows with their own two stratified samples per row (every row differs)."""
+    prob = Problem.load(configs4[name], grid, fourthorder=True, readiso=True)
+    opts = Options(temperature=300.0, integrationtype=it, sigma=1.0, isotopescattering=False, seed=3,
+                   fourthorder=True, qg4ph=qg4)
+    lists = QLists.monte_carlo(prob, opts)
+    _compare(prob, opts, lists)
+
+
+def test_fp64_four_phonon_only_fcc_monte_carlo(configs4):
+    """The fcc case alone, so that every differing Xi entry must be an image-count flip."""
+    prob = Problem.load(configs4["fcc"], (8, 8, 8), fourthorder=True, readiso=True)
+    opts = Options(temperature=300.0, integrationtype=2, thirdorder=False, isotopescattering=False, seed=3,
+                   fourthorder=True, qg4ph=(4, 4, 4))
+    _compare(prob, opts, QLists.monte_carlo(prob, opts))
+
+
+def test_fp64_four_phonon_perovskite_15_modes(configs4):
+    prob = Problem.load(configs4["perovskite"], (4, 4, 4), fourthorder=True, readiso=True)
+    opts = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=11, fourthorder=True,
+                   qg4ph=(2, 2, 2))
+    _compare(prob, opts, QLists.monte_carlo(prob, opts))
+
+
+def test_fp64_four_phonon_only_uneven_per_q1_samples(configs4):
+    """--nothirdorder with explicit pair samples of uneven size per q1 (shared by its rows)."""
+    prob = Problem.load(configs4["rocksalt"], (6, 6, 6), fourthorder=True, readiso=True)
+    rng = np.random.default_rng(23)
+    samples4 = {}
+    for q in range(1, prob.n_irr + 1):
+        k = int(rng.integers(4, 40))
+        samples4[q] = tuple(np.sort(rng.choice(np.arange(1, prob.n_full + 1), size=k, replace=False)).astype(np.int32)
+                            for _ in range(2))
+    lists = QLists.per_irreducible(prob, samples4=samples4)
+    opts = Options(temperature=500.0, integrationtype=2, thirdorder=False, fourthorder=True, isotopescattering=False)
+    _compare(prob, opts, lists)
+
+
+def test_mixed_precision_four_phonon_kappa(configs4):
+    prob = Problem.load(configs4["rocksalt"], (6, 6, 6), fourthorder=True, readiso=True)
+    kw = dict(temperature=300.0, integrationtype=2, isotopescattering=False, seed=3, fourthorder=True, qg4ph=(3, 3, 3))
+    o64, o32 = Options(**kw), Options(precision="mixed", **kw)
     lists = QLists.monte_carlo(prob, o64)
     sr = ScatteringRates(prob)
     lw64 = sr.generate(o64, lists).copy()
