@@ -217,6 +217,36 @@ int tdg_triplets_static(tdg_ctx *ctx, int32_t q1, const int32_t *sample, int64_t
                         int64_t *written);
 
 /*
+ * Differentiation with respect to the third-order force constants. None of the three entry
+ * points below has a counterpart in the reference; they serve d(kappa)/d(Phi3) and
+ * d(Gamma)/d(Phi3).
+ *
+ * tdg_set_fc3: replace the mass-weighted third-order force constants of a context,
+ * fc3_mwm[n_fc3*27] in the layout of tdg_problem.fc3_mwm (same triplets as at
+ * tdg_create). The scattering state is invalidated (call tdg_scattering again).
+ */
+int tdg_set_fc3(tdg_ctx *ctx, const double *fc3_mwm);
+
+/*
+ * tdg_kappa_sma_vjp: lw_bar[n_irr*n_mode] = (d kappa_sma / d linewidth)^T kappa_bar for the
+ * kappa_sma of tdg_kappa (get_kappa then symmetrize_kappa; lo_chop is taken as the
+ * identity), at the linewidths of the last tdg_scattering. kappa_bar is 3x3 column-major.
+ */
+int tdg_kappa_sma_vjp(tdg_ctx *ctx, const tdg_opts *opts, const double *kappa_bar, double *lw_bar);
+
+/*
+ * tdg_adjoint_fc3: mwm_bar[n_fc3*27] = (d linewidth / d fc3_mwm)^T lw_bar, the vector-Jacobian
+ * product of the three-phonon part of the linewidths (the only part that depends on Phi3)
+ * over the rows, samples and q-triplets of the last tdg_scattering, which must have run with
+ * the same opts (opts->precision may differ). The kernel recomputes Psi per q-triplet
+ * instead of storing it. Layout of mwm_bar as tdg_problem.fc3_mwm; divide by
+ * sqrt(m_i m_j m_k) for the derivative with respect to the unweighted force constants.
+ * stats (may be NULL, 4 doubles): [0] ms of the whole pass, [1] ms of the adjoint kernel,
+ * [2] q-triplets, [3] CTAs.
+ */
+int tdg_adjoint_fc3(tdg_ctx *ctx, const tdg_opts *opts, const double *lw_bar, double *mwm_bar, double *stats);
+
+/*
  * Thermal conductivity from the current scattering state (main.f90:216-244):
  * kappa_sma (get_kappa, kappa.f90:28-75), the iterative BTE (kappa.f90:326-495) with
  * maxiter steps and tolerance tol, kappa_iter, both symmetrised (kappa.f90:308-324).

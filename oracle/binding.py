@@ -43,6 +43,8 @@ def lib():
         L.orc_quartets.argtypes = [P(N.TdgProblem), C.c_int, P(C.c_int32), P(C.c_int32), C.c_int64, P(C.c_int32),
                                    C.c_int64]
         L.orc_quartets.restype = C.c_int64
+        L.orc_adjoint_fc3.argtypes = [P(N.TdgProblem), P(N.TdgOpts), P(N.TdgQlists), P(C.c_double), P(C.c_double),
+                                      C.c_int]
         L.orc_scattering_rows.argtypes = [P(N.TdgProblem), P(N.TdgOpts), P(N.TdgQlists), C.c_int, C.c_int,
                                           P(C.c_double), P(C.c_double), C.c_int, P(C.c_int64)]
         L.orc_scattering_finish.argtypes = [P(N.TdgProblem), P(N.TdgOpts), P(N.TdgQlists), P(C.c_double),
@@ -172,6 +174,16 @@ def kappa(prob, opts, lists, xi, qs, f0, maxiter: int, tol: float):
                     N.ptr(f0, C.c_double), int(maxiter), float(tol), N.ptr(ks, C.c_double), N.ptr(ki, C.c_double),
                     C.byref(nit))
     return ks.reshape(3, 3, order="F"), ki.reshape(3, 3, order="F"), nit.value
+
+
+def adjoint_fc3(prob, opts, lists, lw_bar, nthreads: int = 0):
+    """(d linewidth / d fc3_mwm)^T lw_bar of the three-phonon part: [n_fc3, 27]."""
+    lb = np.ascontiguousarray(lw_bar, np.float64).reshape(-1)
+    out = np.zeros(prob.n_fc3 * 27)
+    ps, os_, qs = prob.struct(), opts.struct(prob.grid), lists.struct()
+    lib().orc_adjoint_fc3(C.byref(ps), C.byref(os_), C.byref(qs), N.ptr(lb, C.c_double), N.ptr(out, C.c_double),
+                          int(nthreads))
+    return out.reshape(prob.n_fc3, 27)
 
 
 def full_run(prob, opts, lists, nthreads: int = 0):

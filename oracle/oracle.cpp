@@ -591,6 +591,89 @@ double threephonon_row(const Ctx &c, const SrInit &sr, int q1, int b1, int it, c
     return g0;
 }
 
+// Reverse mode of threephonon_row's linewidth with respect to fc3_mwm, written from the same
+// loops (scattering_threephonon.f90:72-135): g0 = sum over accepted triplets, (b2,b3) and
+// the k equivalent triplets of f0 + f1, with f = perm * pi/16 |c0|^2 w * plf * d and
+// c0 = sum_l evp2[l] ptf[l], ptf[l] = sum_t mwm_t(i,j,k) e_t. So
+// d g0 / d mwm_t(i,j,k) = sum 2 Re(conj(c0) evp2[l(i,j,k)] e_t) * k * perm * pi/16 w (plf0 d0 + plf1 d1).
+// grad (n_fc3*27) accumulates lam * that derivative.
+void threephonon_row_adjoint(const Ctx &c, const SrInit &sr, int q1, int b1, int it, const int32_t *list,
+                             int64_t npts, double lam, double *grad) {
+    const tdg_problem *p = c.p;
+    const int n = c.n;
+    const int n2 = n * n, n3 = n2 * n;
+    const int qf1 = c.irr_full(q1);
+    const double om1 = c.omega(qf1, b1);
+    const double weight = 1.0 / (double)npts;
+    std::vector<cplx> ptf(n3), evp1(n2), evp2(n3), egv1(n), egv2(n), egv3(n), Q(n3), ph(p->n_fc3);
+    std::vector<int> red;
+    for (int r = 0; r < n; ++r) egv1[r] = c.egv(qf1, b1, r) / std::sqrt(om1);
+    const int dims[3] = {p->grid[0], p->grid[1], p->grid[2]};
+    for (int64_t qi = 0; qi < npts; ++qi) {
+        const int q2 = list[qi];
+        const int q3 = fft_third_grid_index(qf1, q2, dims);
+        if (q3 < q2) continue;
+        if (!triplet_is_irreducible(c, q1, q2, q3, red)) continue;
+        const double perm = (q2 == q3) ? 1.0 : 2.0;
+        const double k = (double)(red.size() / 2);
+        pretransform_phi3(c, q2, q3, ptf);
+        std::fill(Q.begin(), Q.end(), cplx(0, 0));
+        for (int b2 = 1; b2 <= n; ++b2) {
+            const double om2 = c.omega(q2, b2);
+            if (om2 < kFreqTol) continue;
+            if (std::fabs(om1 - om2) < kFreqTol) continue;
+            for (int r = 0; r < n; ++r) egv2[r] = c.egv(q2, b2, r) / std::sqrt(om2);
+            for (int j = 0; j < n; ++j)
+                for (int i = 0; i < n; ++i) evp1[(size_t)j * n + i] = egv2[i] * egv1[j];
+            for (int b3 = 1; b3 <= n; ++b3) {
+                const double om3 = c.omega(q3, b3);
+                if (om3 < kFreqTol) continue;
+                if (std::fabs(om1 - om3) < kFreqTol || std::fabs(om2 - om3) < kFreqTol) continue;
+                for (int r = 0; r < n; ++r) egv3[r] = c.egv(q3, b3, r) / std::sqrt(om3);
+                double sigma = 0;
+                if (it == 1) {
+                    sigma = sr.sigma;
+                } else if (it == 2) {
+                    sigma = std::sqrt(sr.sq(c, q1, b1) + sr.sq(c, c.full_irr(q2), b2) + sr.sq(c, c.full_irr(q3), b3));
+                } else {
+                    sigma = 0.0;
+                    sigma += vsig(c.vel(qf1, b1), c.vel(q2, b2), sr.reclat) / 3.0;
+                    sigma += vsig(c.vel(qf1, b1), c.vel(q3, b3), sr.reclat) / 3.0;
+                    sigma += vsig(c.vel(q2, b2), c.vel(q3, b3), sr.reclat) / 3.0;
+                    sigma += sr.thresh_sigma;
+                }
+                const double d0 = lo_gauss(om1, -om2 + om3, sigma) - lo_gauss(om1, om2 - om3, sigma);
+                const double d1 = lo_gauss(om1, om2 + om3, sigma) - lo_gauss(om1, -om2 - om3, sigma);
+                const double n2v = sr.bose(c, c.full_irr(q2), b2);
+                const double n3v = sr.bose(c, c.full_irr(q3), b3);
+                const double dfd = k * perm * kPi / 16.0 * weight * ((n2v - n3v) * d0 + (n2v + n3v + 1.0) * d1);
+                if (dfd == 0.0) continue;
+                for (int l = 0; l < n2; ++l)
+                    for (int i = 0; i < n; ++i) evp2[(size_t)l * n + i] = egv3[i] * evp1[l];
+                cplx c0 = 0;
+                for (int l = 0; l < n3; ++l) c0 += evp2[l] * ptf[l];
+                const cplx wgt = dfd * std::conj(c0);
+                for (int l = 0; l < n3; ++l) Q[l] += wgt * evp2[l];
+            }
+        }
+        const double *qa = p->q_full + 3 * (q2 - 1);
+        const double *qb = p->q_full + 3 * (q3 - 1);
+        for (int t = 0; t < p->n_fc3; ++t) {
+            const int a1 = p->fc3_atoms[3 * t], a2 = p->fc3_atoms[3 * t + 1], a3 = p->fc3_atoms[3 * t + 2];
+            const double *rv2 = p->fc3_lvcart + 6 * t, *rv3 = rv2 + 3;
+            double iqr = qa[0] * rv2[0] + qa[1] * rv2[1] + qa[2] * rv2[2] + (qb[0] * rv3[0] + qb[1] * rv3[1] + qb[2] * rv3[2]);
+            iqr = -iqr * kTwoPi;
+            const cplx e(std::cos(iqr), std::sin(iqr));
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j)
+                    for (int kk = 0; kk < 3; ++kk) {
+                        const int ia = (a1 - 1) * 3 + i, ib = (a2 - 1) * 3 + j, ic = (a3 - 1) * 3 + kk;
+                        grad[27 * t + i + 3 * j + 9 * kk] += lam * 2.0 * std::real(e * Q[(size_t)ia * n2 + (size_t)ib * n + ic]);
+                    }
+        }
+    }
+}
+
 // compute_fourphonon_scattering (scattering_fourphonon.f90:2-265)
 double fourphonon_row(const Ctx &c, const SrInit &sr, int q1, int b1, int it, const int32_t *la, const int32_t *lb,
                       int64_t npts, double *xi_row, int64_t *nquart) {
@@ -898,6 +981,40 @@ int orc_scattering_rows(const tdg_problem *p, const tdg_opts *o, const tdg_qlist
         counts[0] = nt;
         counts[1] = nq;
     }
+    return 0;
+}
+
+// Vector-Jacobian product of the linewidths (three-phonon part) with respect to fc3_mwm:
+// lw_bar (n_irr*n) -> mwm_bar (n_fc3*27). The degeneracy averaging of scattering.f90:266-277
+// makes each row's cotangent the mean of lw_bar over its degenerate set.
+int orc_adjoint_fc3(const tdg_problem *p, const tdg_opts *o, const tdg_qlists *ql, const double *lw_bar,
+                    double *mwm_bar, int nthreads) {
+    Ctx c;
+    c.init(p);
+    SrInit sr;
+    sr.init(c, o);
+    const int n = c.n, nr = ql->n_row;
+    const size_t nm = (size_t)p->n_fc3 * 27;
+    std::fill(mwm_bar, mwm_bar + nm, 0.0);
+    if (!o->thirdorder) return 0;
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+    const int nt = omp_get_max_threads();
+    std::vector<double> part((size_t)nt * nm, 0.0);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int r = 0; r < nr; ++r) {
+        const int q1 = ql->row_q1[r], b1 = ql->row_b1[r];
+        const int f = c.irr_full(q1);
+        const int dg = p->degen[(size_t)(f - 1) * n + b1 - 1];
+        const int32_t *dm = p->degen_mode + ((size_t)(f - 1) * n + b1 - 1) * n;
+        double lam = 0.0;
+        for (int j = 0; j < dg; ++j) lam += lw_bar[(size_t)(q1 - 1) * n + dm[j] - 1];
+        lam /= (double)dg;
+        if (lam == 0.0) continue;
+        threephonon_row_adjoint(c, sr, q1, b1, o->integrationtype, ql->list3 + ql->ptr3[r],
+                                ql->ptr3[r + 1] - ql->ptr3[r], lam, &part[(size_t)omp_get_thread_num() * nm]);
+    }
+    for (int t = 0; t < nt; ++t)
+        for (size_t i = 0; i < nm; ++i) mwm_bar[i] += part[(size_t)t * nm + i];
     return 0;
 }
 

@@ -115,6 +115,9 @@ SIGNATURES = {
     "tdg_get_xi": (C.c_int, [C.c_void_p, _f64p]),
     "tdg_triplets": (C.c_int, [C.c_void_p, C.c_int32, _i32p, C.c_int64, _i32p, C.c_int64, _i64p]),
     "tdg_triplets_static": (C.c_int, [C.c_void_p, C.c_int32, _i32p, C.c_int64, _i32p, C.c_int64, _i64p]),
+    "tdg_set_fc3": (C.c_int, [C.c_void_p, _f64p]),
+    "tdg_kappa_sma_vjp": (C.c_int, [C.c_void_p, C.POINTER(TdgOpts), _f64p, _f64p]),
+    "tdg_adjoint_fc3": (C.c_int, [C.c_void_p, C.POINTER(TdgOpts), _f64p, _f64p, _f64p]),
     "tdg_kappa": (C.c_int, [C.c_void_p, C.POINTER(TdgOpts), C.c_int32, C.c_double, _f64p, _f64p, _f64p, _i32p]),
     "tdg_problem_load": (C.c_int, [C.c_char_p, _i32p, C.c_int, C.c_int, C.c_int, C.POINTER(C.POINTER(TdgProblem))]),
     "tdg_problem_free": (None, [C.POINTER(TdgProblem)]),

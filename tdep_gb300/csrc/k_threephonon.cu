@@ -72,6 +72,21 @@ __device__ __forceinline__ const float2 *egvs_ptr<float2>(const PhononDev &ph) {
     return ph.egvs32;
 }
 
+// exp(-2 pi i (q2.lv2 + q3.lv3)) of force-constant triplet t as an exact root of unity:
+// q = g/G on the mesh and lv integer, so the phase index is sum_d (g2 lv2 + g3 lv3)_d mod G_d
+// scaled to L = lcm(G).
+template <typename C>
+__device__ __forceinline__ C phase3(const Fc3Dev &fc, const MeshDev &m, const int *gi2, const int *gi3, int t) {
+    const int32_t *lv = fc.lv + (size_t)t * 6;
+    int K = 0;
+    for (int d = 0; d < 3; ++d) {
+        int kd = (gi2[d] * lv[d] + gi3[d] * lv[3 + d]) % m.grid[d];
+        if (kd < 0) kd += m.grid[d];
+        K += kd * m.lmul[d];
+    }
+    return twiddle_at<C>(fc, K % m.L);
+}
+
 // Exclusive scan of one int per thread over the block (blockDim a multiple of 32).
 __device__ __forceinline__ int block_exclusive_scan(int v, int *wsum, int &total) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -153,7 +168,9 @@ __host__ __device__ constexpr int min_blocks_for(int n, bool dbl) {
     return n <= 3 ? 16 : (n <= 6 ? 12 : (n <= 9 ? 6 : (dbl ? (n <= 12 ? 2 : 1) : (n <= 15 ? 3 : 2))));
 }
 
-template <int N, typename R>
+// ADJ = false: Gamma and the Xi row terms. ADJ = true: the adjoint pass, which recomputes
+// the same Psi and delta weights and accumulates d L / d mwm for the row cotangents a.lam.
+template <int N, typename R, bool ADJ>
 __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) == 8)) k_threephonon(ThreePhArgs a) {
     using C = typename CT<R>::C;
     constexpr int N2 = N * N, N3 = N2 * N;
@@ -275,16 +292,7 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
         for (int c0 = 0; c0 < fc.n; c0 += kPhaseChunk) {
             const int cn = min(kPhaseChunk, fc.n - c0);
             __syncthreads();
-            for (int i = tid; i < cn; i += bd) {
-                const int32_t *lv = fc.lv + (size_t)(c0 + i) * 6;
-                int K = 0;
-                for (int d = 0; d < 3; ++d) {
-                    int kd = (gi2[d] * lv[d] + gi3[d] * lv[3 + d]) % m.grid[d];
-                    if (kd < 0) kd += m.grid[d];
-                    K += kd * m.lmul[d];
-                }
-                ph[i] = twiddle_at<C>(fc, K % m.L);
-            }
+            for (int i = tid; i < cn; i += bd) ph[i] = phase3<C>(fc, m, gi2, gi3, c0 + i);
             __syncthreads();
             for (int idx = tid; idx < N3; idx += bd) {
                 const int blk = idx / 27, ijk = idx % 27;
@@ -426,7 +434,8 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
             if (nonzero(d0) || nonzero(d1)) {
                 const C psi = B[idx];
                 const double cr = (double)psi.x, ci = (double)psi.y;
-                const double psisq = kThreePhononPrefactor * (cr * cr + ci * ci) * wrow[b1];
+                // the adjoint keeps d F / d|Psi|^2, i.e. F without |Psi|^2
+                const double psisq = kThreePhononPrefactor * (ADJ ? 1.0 : cr * cr + ci * ci) * wrow[b1];
                 const double n2 = be2[b2], n3 = be3[b3];
                 const double plf0 = n2 - n3;
                 const double plf1 = n2 + n3 + 1.0;
@@ -436,6 +445,92 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
             }
         }
         __syncthreads();
+        if constexpr (ADJ) {
+            // d L / d|Psi_b|^2 = lam[row(b1)] * nred * dF_b/d|Psi_b|^2 (Gamma += nred * sum F);
+            // d|Psi|^2 / d P[abc] = 2 Re(conj(Psi) E1[a][b1] E2[b][b2] E3[c][b3]), so with
+            // W = G conj(Psi):  Q[abc] = sum_b W_b E1[a][b1] E2[b][b2] E3[c][b3] and
+            // d L / d mwm_t(i,j,k) = 2 Re(phase_t Q[3a1+i][3a2+j][3a3+k]).
+            for (int i = tid; i < N3; i += bd) {
+                const int row = rowid[i / N2];
+                const double g = row >= 0 ? a.lam[row] * (double)nred * F[i] : 0.0;
+                const C psi = B[i];
+                C w;
+                w.x = (R)(g * (double)psi.x);
+                w.y = (R)(-g * (double)psi.y);
+                B[i] = w;
+            }
+            // the survivor queue overwrote the eigenvectors: load them again
+            for (int i = tid; i < 3 * N2; i += bd) {
+                const int which = i / N2, e = i % N2;
+                const int r = e / N, b = e % N;
+                const int q = which == 0 ? f1 : (which == 1 ? q2 : q3);
+                C *E = which == 0 ? E1 : (which == 1 ? E2 : E3);
+                E[r * N + b] = egvs[((size_t)q * N + b) * N + r];
+            }
+            __syncthreads();
+            if (tid < N2) {  // A[a][b2b3] = sum_b1 E1[a][b1] W[b1][b2b3]
+                const int bc = tid;
+                C acc[N];
+#pragma unroll
+                for (int x = 0; x < N; ++x) acc[x] = czero<C>();
+#pragma unroll 3
+                for (int b1 = 0; b1 < N; ++b1) {
+                    const C w = B[b1 * N2 + bc];
+#pragma unroll
+                    for (int x = 0; x < N; ++x) cfma(acc[x], E1[x * N + b1], w);
+                }
+#pragma unroll
+                for (int x = 0; x < N; ++x) A[x * N2 + bc] = acc[x];
+            }
+            __syncthreads();
+            if (tid < N2) {  // B[a][b][b3] = sum_b2 E2[b][b2] A[a][b2][b3]
+                const int aa = tid / N, b3 = tid % N;
+                C acc[N];
+#pragma unroll
+                for (int x = 0; x < N; ++x) acc[x] = czero<C>();
+#pragma unroll 3
+                for (int b2 = 0; b2 < N; ++b2) {
+                    const C tv = A[(aa * N + b2) * N + b3];
+#pragma unroll
+                    for (int x = 0; x < N; ++x) cfma(acc[x], E2[x * N + b2], tv);
+                }
+#pragma unroll
+                for (int x = 0; x < N; ++x) B[(aa * N + x) * N + b3] = acc[x];
+            }
+            __syncthreads();
+            if (tid < N2) {  // A[a][b][c] = sum_b3 E3[c][b3] B[a][b][b3]
+                const int ab = tid;
+                C acc[N];
+#pragma unroll
+                for (int x = 0; x < N; ++x) acc[x] = czero<C>();
+#pragma unroll 3
+                for (int b3 = 0; b3 < N; ++b3) {
+                    const C tv = B[ab * N + b3];
+#pragma unroll
+                    for (int x = 0; x < N; ++x) cfma(acc[x], E3[x * N + b3], tv);
+                }
+#pragma unroll
+                for (int x = 0; x < N; ++x) A[ab * N + x] = acc[x];
+            }
+            double *slice = a.mwm_bar + (size_t)blockIdx.x * fc.n * 27;
+            for (int c0 = 0; c0 < fc.n; c0 += kPhaseChunk) {
+                const int cn = min(kPhaseChunk, fc.n - c0);
+                __syncthreads();
+                for (int i = tid; i < cn; i += bd) ph[i] = phase3<C>(fc, m, gi2, gi3, c0 + i);
+                __syncthreads();
+                for (int x = tid; x < cn * 27; x += bd) {
+                    const int tt = c0 + x / 27, ijk = x % 27;
+                    const int blk = fc.blk_of[tt];
+                    const int a1 = blk / (NA * NA), a2 = (blk / NA) % NA, a3 = blk % NA;
+                    const int ii = ijk % 3, jj = (ijk / 3) % 3, kk = ijk / 9;
+                    const C q = A[((3 * a1 + ii) * N + 3 * a2 + jj) * N + 3 * a3 + kk];
+                    const C p = ph[x / 27];
+                    slice[(size_t)tt * 27 + ijk] += 2.0 * ((double)p.x * (double)q.x - (double)p.y * (double)q.y);
+                }
+            }
+            __syncthreads();
+            continue;
+        }
         // ---- R2 = sum over b3, R3 = sum over b2 (into B as doubles) ----
         double *R3 = (double *)B;
         for (int e = tid; e < 2 * N2; e += bd) {
@@ -485,22 +580,72 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
     }
 }
 
+// Persistent grid: resident CTAs per SM times the SM count, at most one CTA per item.
+template <int N, typename R, bool ADJ>
+int grid_n(int n_sm, int n_trip) {
+    const Layout L = make_layout(N, sizeof(typename CT<R>::C));
+    if (cudaFuncSetAttribute(k_threephonon<N, R, ADJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_threephonon<N, R, ADJ>, threads_for(N), L.total) !=
+            cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        return 0;
+    }
+    const int grid = n_sm * per_sm;
+    return grid > n_trip ? (n_trip > 0 ? n_trip : 1) : grid;
+}
+
+template <int N, typename R, bool ADJ>
+cudaError_t launch_grid(const ThreePhArgs &a, int grid, cudaStream_t s) {
+    const Layout L = make_layout(N, sizeof(typename CT<R>::C));
+    k_threephonon<N, R, ADJ><<<grid, threads_for(N), L.total, s>>>(a);
+    return cudaGetLastError();
+}
+
 template <int N, typename R>
 cudaError_t launch_n(const ThreePhArgs &a, int n_sm, cudaStream_t s) {
-    const Layout L = make_layout(N, sizeof(typename CT<R>::C));
-    const int threads = threads_for(N);
-    cudaError_t e = cudaFuncSetAttribute(k_threephonon<N, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)L.total);
-    if (e != cudaSuccess) return e;
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_threephonon<N, R>, threads, L.total);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) return cudaErrorInvalidConfiguration;
-    int grid = n_sm * per_sm;
-    if (grid > a.n_trip) grid = a.n_trip;
-    if (grid < 1) return cudaSuccess;
-    k_threephonon<N, R><<<grid, threads, L.total, s>>>(a);
-    return cudaGetLastError();
+    const int grid = grid_n<N, R, false>(n_sm, a.n_trip);
+    if (grid < 1) return cudaErrorInvalidConfiguration;
+    return launch_grid<N, R, false>(a, grid, s);
+}
+
+template <typename R, bool ADJ>
+int grid_prec(int n, int n_sm, int n_trip) {
+    switch (n) {
+        case 3: return grid_n<3, R, ADJ>(n_sm, n_trip);
+        case 6: return grid_n<6, R, ADJ>(n_sm, n_trip);
+        case 9: return grid_n<9, R, ADJ>(n_sm, n_trip);
+        case 12: return grid_n<12, R, ADJ>(n_sm, n_trip);
+        case 15: return grid_n<15, R, ADJ>(n_sm, n_trip);
+        case 18: return grid_n<18, R, ADJ>(n_sm, n_trip);
+        default: return 0;
+    }
+}
+
+template <typename R>
+cudaError_t launch_adj_prec(const ThreePhArgs &a, int grid, cudaStream_t s) {
+    switch (a.mesh.n_mode) {
+        case 3: return launch_grid<3, R, true>(a, grid, s);
+        case 6: return launch_grid<6, R, true>(a, grid, s);
+        case 9: return launch_grid<9, R, true>(a, grid, s);
+        case 12: return launch_grid<12, R, true>(a, grid, s);
+        case 15: return launch_grid<15, R, true>(a, grid, s);
+        case 18: return launch_grid<18, R, true>(a, grid, s);
+        default: return cudaErrorNotSupported;
+    }
+}
+
+__global__ void k_sum_slices(const double *slices, int32_t n_slice, int64_t n, double *out) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int g = 0; g < n_slice; ++g) acc += slices[(int64_t)g * n + e];
+        out[e] = acc;
+    }
 }
 
 template <typename R>
@@ -539,6 +684,23 @@ cudaError_t launch_threephonon(const ThreePhArgs &a, int precision, int n_sm, cu
     if (a.n_trip <= 0) return cudaSuccess;
     if (precision == 0) return launch_prec<double>(a, n_sm, s);
     return launch_prec<float>(a, n_sm, s);
+}
+
+int threephonon_adjoint_grid(int n, int precision, int n_sm, int n_trip) {
+    return precision == 0 ? grid_prec<double, true>(n, n_sm, n_trip) : grid_prec<float, true>(n, n_sm, n_trip);
+}
+
+cudaError_t launch_threephonon_adjoint(const ThreePhArgs &a, int precision, int grid, cudaStream_t s) {
+    if (a.n_trip <= 0 || grid <= 0) return cudaSuccess;
+    if (precision == 0) return launch_adj_prec<double>(a, grid, s);
+    return launch_adj_prec<float>(a, grid, s);
+}
+
+cudaError_t launch_sum_slices(const double *slices, int32_t n_slice, int64_t n, double *out, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const int64_t blocks = (n + 255) / 256;
+    k_sum_slices<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, s>>>(slices, n_slice, n, out);
+    return cudaGetLastError();
 }
 
 }  // namespace tdg

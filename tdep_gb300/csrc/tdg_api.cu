@@ -112,7 +112,8 @@ struct tdg_ctx {
     DevBuf<double> d_omega, d_vel, d_be, d_sigsq, d_disorder;
     DevBuf<double2> d_egv, d_egvs;
     DevBuf<float2> d_egvs32;
-    DevBuf<int32_t> fc3_blk, fc3_lv, fc4_blk, fc4_lv;
+    DevBuf<int32_t> fc3_blk, fc3_lv, fc4_blk, fc4_lv, fc3_blk_of;
+    std::vector<int> fc3_perm;  // device (block-sorted) position -> index in the problem
     DevBuf<double> fc3_mwm, fc4_mwm;
     DevBuf<float> fc3_mwm32, fc4_mwm32;
     DevBuf<double2> tw;
@@ -148,6 +149,12 @@ struct tdg_ctx {
     DevBuf<unsigned char> d_scr4;
     // BTE buffers
     DevBuf<double> d_fbb, d_buf;
+    // state of the last tdg_scattering that the adjoint pass reuses
+    PhononDev last_ph{};
+    RowsDev last_rows{};
+    int32_t last_ntrip = 0;
+    bool last_third = false;
+    DevBuf<double> d_lam, d_slices, d_mwm_bar;
 
     MeshDev mesh() const {
         MeshDev m;
@@ -361,7 +368,7 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
     }
     // Force constants sorted by atom block (a1,a2,a3).
     const int na = c->na;
-    std::vector<int32_t> blk_ptr3(na * na * na + 1, 0), lv3;
+    std::vector<int32_t> blk_ptr3(na * na * na + 1, 0), lv3, blk_of3;
     std::vector<double> mwm3;
     std::vector<float> mwm3f;
     {
@@ -372,7 +379,9 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
             return ((a[0] - 1) * na + (a[1] - 1)) * na + (a[2] - 1);
         };
         std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return blk(x) < blk(y); });
+        c->fc3_perm = idx;
         for (int t : idx) {
+            blk_of3.push_back(blk(t));
             blk_ptr3[blk(t) + 1]++;
             lv3.insert(lv3.end(), p->fc3_lv + 6 * t, p->fc3_lv + 6 * t + 6);
             for (int k = 0; k < 27; ++k) {
@@ -426,6 +435,7 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
     chk(c->d_egvs32.upload(egvs32.data(), egvs32.size(), s));
     chk(c->d_disorder.upload(c->disorder.data(), c->disorder.size(), s));
     chk(c->fc3_blk.upload(blk_ptr3.data(), blk_ptr3.size(), s));
+    chk(c->fc3_blk_of.upload(blk_of3.data(), blk_of3.size(), s));
     chk(c->fc3_lv.upload(lv3.data(), lv3.size(), s));
     chk(c->fc3_mwm.upload(mwm3.data(), mwm3.size(), s));
     chk(c->fc3_mwm32.upload(mwm3f.data(), mwm3f.size(), s));
@@ -917,6 +927,9 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         a.fc.mwm32 = c->fc3_mwm32.p;
         a.fc.twiddle = c->tw.p;
         a.fc.twiddle32 = c->tw32.p;
+        a.fc.blk_of = c->fc3_blk_of.p;
+        a.lam = nullptr;
+        a.mwm_bar = nullptr;
         a.trip = c->d_trip.p;
         a.n_trip = ntrip;
         a.red = c->d_red.p;
@@ -1074,6 +1087,10 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         stats[8] = launches;
         stats[9] = (double)nred + (double)nred4;
     }
+    c->last_ph = ph;
+    c->last_rows = rows;
+    c->last_ntrip = ntrip;
+    c->last_third = o->thirdorder != 0;
     c->have_scattering = true;
     return kOk;
 }
@@ -1329,4 +1346,159 @@ tdg::CtxView tdg::ctx_view(const tdg_ctx *c) {
     v.stream = c->stream;
     v.mesh = c->mesh();
     return v;
+}
+
+extern "C" int tdg_set_fc3(tdg_ctx *c, const double *fc3_mwm) {
+    if (!c || !fc3_mwm) return set_error(kErrParam, "tdg_set_fc3: null argument");
+    if (c->n_fc3 < 1) return set_error(kErrParam, "tdg_set_fc3: the context has no third-order force constants");
+    const size_t cnt = (size_t)c->n_fc3 * 27;
+    for (size_t i = 0; i < cnt; ++i)
+        if (!std::isfinite(fc3_mwm[i])) return set_error(kErrPhysical, "tdg_set_fc3: non-finite force constant");
+    std::vector<double> m(cnt);
+    std::vector<float> mf(cnt);
+    for (int sidx = 0; sidx < c->n_fc3; ++sidx) {
+        const int t = c->fc3_perm[sidx];
+        for (int k = 0; k < 27; ++k) {
+            m[(size_t)sidx * 27 + k] = fc3_mwm[(size_t)t * 27 + k];
+            mf[(size_t)sidx * 27 + k] = (float)fc3_mwm[(size_t)t * 27 + k];
+        }
+    }
+    CUDA_TRY(cudaSetDevice(c->device));
+    CUDA_TRY(c->fc3_mwm.upload(m.data(), cnt, c->stream));
+    CUDA_TRY(c->fc3_mwm32.upload(mf.data(), cnt, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->have_scattering = false;
+    return kOk;
+}
+
+extern "C" int tdg_kappa_sma_vjp(tdg_ctx *c, const tdg_opts *o, const double *kappa_bar, double *lw_bar) {
+    if (!c || !kappa_bar || !lw_bar) return set_error(kErrParam, "tdg_kappa_sma_vjp: null argument");
+    int st = validate_opts(o);
+    if (st) return st;
+    if (!c->have_scattering) return set_error(kErrParam, "tdg_kappa_sma_vjp: call tdg_scattering first");
+    const int n = c->n;
+    // kappa_sma = S(S(M)) with S(X) = (1/nop) sum_R R X R^T (get_kappa, then symmetrize_kappa;
+    // lo_chop is taken as the identity). The adjoint of S is (1/nop) sum_R R^T X R.
+    auto St = [&](const double *x, double *y) {
+        for (int i = 0; i < 9; ++i) y[i] = 0.0;
+        for (int j = 0; j < c->nop; ++j) {
+            const double *m = &c->op_cart[9 * j];
+            for (int k = 0; k < 3; ++k)
+                for (int l = 0; l < 3; ++l) {
+                    double sum = 0.0;
+                    for (int a = 0; a < 3; ++a)
+                        for (int b = 0; b < 3; ++b) sum += m[a + 3 * k] * x[a + 3 * b] * m[b + 3 * l];
+                    y[k + 3 * l] += sum / c->nop;
+                }
+        }
+    };
+    double t1[9], Mb[9];
+    St(kappa_bar, t1);
+    St(t1, Mb);
+    const double T = o->temperature;
+    for (int q1 = 0; q1 < c->nirr; ++q1) {
+        const int f = c->irr_full[q1] - 1;
+        for (int b1 = 0; b1 < n; ++b1) {
+            double g = 0.0;
+            const double om1 = c->omega[(size_t)f * n + b1];
+            const double lw = c->linewidth[(size_t)q1 * n + b1];
+            if (!(om1 < kFreqTol) && lw > kFreqTol) {
+                // M += w F0 (x) v with F0 = v / (2 lw): d M / d lw = -w v (x) v / (2 lw^2)
+                const double cv = o->classical ? kKbHartree : harmonic_oscillator_cv(T, om1);
+                const double w = cv / c->volume * c->irr_weight[q1];
+                const double *v = &c->vel[((size_t)f * n + b1) * 3];
+                double vmv = 0.0;
+                for (int x = 0; x < 3; ++x)
+                    for (int y = 0; y < 3; ++y) vmv += v[x] * Mb[x + 3 * y] * v[y];
+                g = -w * vmv / (2.0 * lw * lw);
+            }
+            lw_bar[(size_t)q1 * n + b1] = g;
+        }
+    }
+    return kOk;
+}
+
+extern "C" int tdg_adjoint_fc3(tdg_ctx *c, const tdg_opts *o, const double *lw_bar, double *mwm_bar, double *stats) {
+    if (!c || !lw_bar || !mwm_bar) return set_error(kErrParam, "tdg_adjoint_fc3: null argument");
+    int st = validate_opts(o);
+    if (st) return st;
+    if (!c->have_scattering || !c->last_third)
+        return set_error(kErrParam, "tdg_adjoint_fc3: call tdg_scattering with three-phonon scattering first");
+    CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    const int n = c->n, nr = c->n_row;
+    // linewidth_j is the mean of Gamma over the degenerate set of j (scattering.f90:266-277),
+    // so the cotangent of row (q1,b1) collects lw_bar over the set of b1, divided by its size.
+    std::vector<double> lam(nr, 0.0);
+    for (int r = 0; r < nr; ++r) {
+        const int q1 = c->row_q1[r] - 1, b1 = c->row_b1[r] - 1;
+        const int f = c->irr_full[q1] - 1;
+        const int dg = c->degen[(size_t)f * n + b1];
+        const int32_t *dm = &c->degen_mode[((size_t)f * n + b1) * n];
+        double acc = 0.0;
+        for (int j = 0; j < dg; ++j) acc += lw_bar[(size_t)q1 * n + dm[j] - 1];
+        lam[r] = acc / (double)dg;
+    }
+    const int ntrip = c->last_ntrip;
+    const int grid = threephonon_adjoint_grid(n, o->precision, c->n_sm, ntrip);
+    if (ntrip > 0 && grid < 1) return set_error(kErrDevice, "adjoint kernel configuration failed");
+    const int64_t nm = (int64_t)c->n_fc3 * 27;
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t x) {
+        if (e == cudaSuccess) e = x;
+    };
+    chk(c->d_lam.upload(lam.data(), lam.size(), s));
+    chk(c->d_slices.alloc((size_t)std::max(grid, 1) * nm));
+    chk(c->d_mwm_bar.alloc(nm));
+    if (e != cudaSuccess) return set_error(kErrDevice, std::string("allocation failed: ") + cudaGetErrorString(e));
+    cudaEvent_t *ev = c->ev;
+    CUDA_TRY(cudaEventRecord(ev[0], s));
+    CUDA_TRY(cudaMemsetAsync(c->d_slices.p, 0, sizeof(double) * (size_t)std::max(grid, 1) * nm, s));
+    CUDA_TRY(cudaMemsetAsync(c->d_status.p, 0, sizeof(int32_t), s));
+    ThreePhArgs a;
+    a.mesh = c->mesh();
+    a.ph = c->last_ph;
+    a.rows = c->last_rows;
+    a.fc.n = c->n_fc3;
+    a.fc.n_atom = c->na;
+    a.fc.blk_ptr = c->fc3_blk.p;
+    a.fc.lv = c->fc3_lv.p;
+    a.fc.mwm = c->fc3_mwm.p;
+    a.fc.mwm32 = c->fc3_mwm32.p;
+    a.fc.twiddle = c->tw.p;
+    a.fc.twiddle32 = c->tw32.p;
+    a.fc.blk_of = c->fc3_blk_of.p;
+    a.trip = c->d_trip.p;
+    a.n_trip = ntrip;
+    a.red = c->d_red.p;
+    a.cand_mask = c->d_mask.p;
+    a.gamma = nullptr;
+    a.od = nullptr;
+    a.status = c->d_status.p;
+    a.lam = c->d_lam.p;
+    a.mwm_bar = c->d_slices.p;
+    CUDA_TRY(cudaEventRecord(ev[1], s));
+    CUDA_TRY(launch_threephonon_adjoint(a, o->precision, grid, s));
+    CUDA_TRY(cudaEventRecord(ev[2], s));
+    CUDA_TRY(launch_sum_slices(c->d_slices.p, std::max(grid, 1), nm, c->d_mwm_bar.p, s));
+    std::vector<double> dev(nm);
+    CUDA_TRY(cudaMemcpyAsync(dev.data(), c->d_mwm_bar.p, sizeof(double) * nm, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaEventRecord(ev[3], s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    st = read_status(c);
+    if (st) return st;
+    for (int sidx = 0; sidx < c->n_fc3; ++sidx) {
+        const int t = c->fc3_perm[sidx];
+        for (int k = 0; k < 27; ++k) mwm_bar[(size_t)t * 27 + k] = dev[(size_t)sidx * 27 + k];
+    }
+    if (stats) {
+        float ms_all = 0.f, ms_k = 0.f;
+        CUDA_TRY(cudaEventElapsedTime(&ms_all, ev[0], ev[3]));
+        CUDA_TRY(cudaEventElapsedTime(&ms_k, ev[1], ev[2]));
+        stats[0] = ms_all;
+        stats[1] = ms_k;
+        stats[2] = ntrip;
+        stats[3] = grid;
+    }
+    return kOk;
 }

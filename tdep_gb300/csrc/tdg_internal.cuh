@@ -74,6 +74,7 @@ struct Fc3Dev {
     const float *mwm32;       // [n*27]
     const double2 *twiddle;   // [L] exp(-2 pi i K / L)
     const float2 *twiddle32;
+    const int32_t *blk_of;    // [n] atom block (a1,a2,a3) of each triplet
 };
 
 struct Fc4Dev {
@@ -115,8 +116,18 @@ struct ThreePhArgs {
     double *gamma;              // [n_row]
     double *od;                 // [n_row * n_full*n]
     int32_t *status;
+    // adjoint only: cotangent of each row's Gamma and one accumulation slice of
+    // d L / d mwm ([fc.n * 27]) per CTA
+    const double *lam;
+    double *mwm_bar;
 };
 cudaError_t launch_threephonon(const ThreePhArgs &a, int precision, int n_sm, cudaStream_t s);
+// Adjoint of the three-phonon Gamma with respect to mwm: recomputes Psi per q-triplet and
+// accumulates 2 Re(phase * Q) into a.mwm_bar (one slice per CTA of the returned grid).
+int threephonon_adjoint_grid(int n, int precision, int n_sm, int n_trip);
+cudaError_t launch_threephonon_adjoint(const ThreePhArgs &a, int precision, int grid, cudaStream_t s);
+// out[e] = sum over g < n_slice of slices[g * n + e], in slice order.
+cudaError_t launch_sum_slices(const double *slices, int32_t n_slice, int64_t n, double *out, cudaStream_t s);
 size_t threephonon_smem_bytes(int n, int precision, int n_fc);
 
 struct FourPhArgs {

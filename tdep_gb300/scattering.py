@@ -336,6 +336,37 @@ class ScatteringRates:
         self.Fn = fn.reshape(p.n_irr, p.n_mode, 3)
         return ks.reshape(3, 3, order="F"), ki.reshape(3, 3, order="F")
 
+    # ---- differentiation with respect to the third-order force constants ----
+    def set_fc3(self, fc3_mwm: np.ndarray) -> None:
+        """Replace the mass-weighted third-order force constants ([n_fc3, 27], the layout of
+        Problem.fc3_mwm); the next generate() uses them."""
+        m = np.ascontiguousarray(fc3_mwm, dtype=np.float64).reshape(self.prob.n_fc3 * 27)
+        N.check(self._lib.tdg_set_fc3(self._ctx, N.ptr(m, C.c_double)), "tdg_set_fc3")
+
+    def kappa_sma_vjp(self, opts: Options, kappa_bar: np.ndarray) -> np.ndarray:
+        """(d kappa_sma / d linewidth)^T kappa_bar at the last generate(): [n_irr, n_mode]."""
+        p = self.prob
+        kb = np.ascontiguousarray(np.asarray(kappa_bar, dtype=np.float64).reshape(3, 3).ravel(order="F"))
+        out = np.zeros(p.n_irr * p.n_mode)
+        o = opts.struct(p.grid)
+        N.check(self._lib.tdg_kappa_sma_vjp(self._ctx, C.byref(o), N.ptr(kb, C.c_double), N.ptr(out, C.c_double)),
+                "tdg_kappa_sma_vjp")
+        return out.reshape(p.n_irr, p.n_mode)
+
+    def adjoint_fc3(self, opts: Options, lw_bar: np.ndarray) -> np.ndarray:
+        """(d linewidth / d fc3_mwm)^T lw_bar over the q-triplets of the last generate():
+        [n_fc3, 27]. Timing of the pass in self.adjoint_stats."""
+        p = self.prob
+        lb = np.ascontiguousarray(lw_bar, dtype=np.float64).reshape(p.n_irr * p.n_mode)
+        out = np.zeros(p.n_fc3 * 27)
+        st = np.zeros(4)
+        o = opts.struct(p.grid)
+        N.check(self._lib.tdg_adjoint_fc3(self._ctx, C.byref(o), N.ptr(lb, C.c_double), N.ptr(out, C.c_double),
+                                          N.ptr(st, C.c_double)), "tdg_adjoint_fc3")
+        self.adjoint_stats = {"ms": float(st[0]), "kernel_ms": float(st[1]), "triplets": int(st[2]),
+                              "ctas": int(st[3])}
+        return out.reshape(p.n_fc3, 27)
+
 
 def write_outfile(directory, temperature, kappa_sma, kappa_iter, kappa_offdiag=None) -> Path:
     """outfile.thermal_conductivity (main.f90:246-294); tensors in atomic units."""

@@ -1,0 +1,117 @@
+"""Adjoint of the three-phonon linewidths and kappa_sma with respect to Phi3 on the GB300:
+against the oracle's reverse-mode restatement (FP64 reference gradient), against central
+finite differences of the device forward pass, and through torch.autograd."""
+import numpy as np
+import pytest
+
+from oracle import binding as orc
+from tdep_gb300 import Options, Problem, QLists, ScatteringRates, device_count
+
+pytestmark = pytest.mark.gpu
+
+ROCKSALT_AMU = (22.99, 35.45)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _require_gpu(built):
+    assert device_count() > 0, "GPU tests need a CUDA device; the GB300 path has no CPU fallback"
+
+
+@pytest.mark.parametrize("name,grid,it", [("rocksalt", (6, 6, 6), 2), ("perovskite", (4, 4, 4), 6),
+                                          ("fcc", (8, 8, 8), 1)])
+def test_adjoint_fp64_matches_oracle_gradient(configs, name, grid, it):
+    prob = Problem.load(configs[name], grid, readiso=True)
+    opts = Options(temperature=300.0, integrationtype=it, sigma=1.0, isotopescattering=False, seed=13)
+    lists = QLists.monte_carlo(prob, opts)
+    rng = np.random.default_rng(1)
+    lw_bar = rng.normal(size=(prob.n_irr, prob.n_mode))
+    sr = ScatteringRates(prob)
+    sr.generate(opts, lists)
+    g = sr.adjoint_fc3(opts, lw_bar)
+    again = sr.adjoint_fc3(opts, lw_bar)
+    sr.close()
+    ref = orc.adjoint_fc3(prob, opts, lists, lw_bar)
+    np.testing.assert_allclose(g, ref, rtol=1e-9, atol=1e-10 * np.abs(ref).max())
+    np.testing.assert_array_equal(g, again)  # slices are summed in a fixed order
+
+
+def test_adjoint_mixed_close_to_fp64(configs):
+    prob = Problem.load(configs["rocksalt"], (8, 8, 8), readiso=True)
+    o64 = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=2)
+    o32 = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=2, precision="mixed")
+    lists = QLists.monte_carlo(prob, o64)
+    sr = ScatteringRates(prob)
+    sr.generate(o64, lists)
+    sr.kappa(o64, maxiter=0)
+    kb = np.zeros((3, 3))
+    kb[0, 0] = 1.0
+    lw_bar = sr.kappa_sma_vjp(o64, kb)
+    g64 = sr.adjoint_fc3(o64, lw_bar)
+    g32 = sr.adjoint_fc3(o32, lw_bar)
+    sr.close()
+    assert np.linalg.norm(g32 - g64) <= 1e-4 * np.linalg.norm(g64)
+
+
+def test_dkappa_dphi3_against_central_differences(configs):
+    """d kappa_xx(300 K) / d Phi3 on rocksalt 16^3 through ThreePhononKappa, against central
+    differences with a step of 1e-4 eV/A^3 on 20 seeded random force-constant entries."""
+    torch = pytest.importorskip("torch")
+    from tdep_gb300.autograd import FC3_EVA3_TO_AU, linewidth_and_kappa, mass_weights
+
+    prob = Problem.load(configs["rocksalt"], (16, 16, 16), readiso=True)
+    opts = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=1)
+    lists = QLists.monte_carlo(prob, opts)
+    sr = ScatteringRates(prob)
+    m0 = torch.tensor(prob.fc3_mwm, dtype=torch.float64, requires_grad=True)
+    _, ks = linewidth_and_kappa(m0, sr, opts, lists)
+    ks[0, 0].backward()
+    grad_mwm = m0.grad.numpy()
+    w = mass_weights(prob, ROCKSALT_AMU)
+    grad_phi = grad_mwm * (w * FC3_EVA3_TO_AU)[:, None]  # d kappa_xx / d Phi3 [a.u. per eV/A^3]
+    rng = np.random.default_rng(20)
+    h = 1e-4  # eV/A^3
+    base = prob.fc3_mwm.copy()
+    scale = np.abs(grad_phi).max()
+    for _ in range(20):
+        t, e = int(rng.integers(prob.n_fc3)), int(rng.integers(27))
+        vals = []
+        for sgn in (1.0, -1.0):
+            m = base.copy()
+            m[t, e] += sgn * h * FC3_EVA3_TO_AU * w[t]
+            sr.set_fc3(m)
+            sr.generate(opts, lists)
+            vals.append(sr.kappa(opts, maxiter=0)[0][0, 0])
+        fd = (vals[0] - vals[1]) / (2 * h)
+        assert abs(fd - grad_phi[t, e]) <= 2e-6 * scale + 1e-4 * abs(fd), (t, e, fd, grad_phi[t, e])
+    sr.close()
+
+
+def test_autograd_through_a_parameterisation(configs):
+    """Phi3 = Phi3_0 + B x for a random basis B: autograd gives B^T (d kappa / d mwm), and a
+    central difference along x agrees."""
+    torch = pytest.importorskip("torch")
+    from tdep_gb300.autograd import linewidth_and_kappa
+
+    prob = Problem.load(configs["rocksalt"], (6, 6, 6), readiso=True)
+    opts = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=4)
+    lists = QLists.monte_carlo(prob, opts)
+    sr = ScatteringRates(prob)
+    rng = np.random.default_rng(8)
+    B = torch.tensor(rng.normal(size=(prob.n_fc3 * 27, 4)) * np.abs(prob.fc3_mwm).max() * 1e-3)
+    m0 = torch.tensor(prob.fc3_mwm.reshape(-1))
+    x = torch.zeros(4, dtype=torch.float64, requires_grad=True)
+    lw, ks = linewidth_and_kappa((m0 + B @ x).reshape(prob.n_fc3, 27), sr, opts, lists)
+    loss = ks[0, 0] + 1e3 * lw.sum() * ks[0, 0].detach() / lw.sum().detach()
+    loss.backward()
+    gx = x.grad.numpy().copy()
+    h = 1e-3
+    for j in range(4):
+        vals = []
+        for sgn in (1.0, -1.0):
+            xp = torch.zeros(4, dtype=torch.float64)
+            xp[j] = sgn * h
+            lw2, ks2 = linewidth_and_kappa((m0 + B @ xp).reshape(prob.n_fc3, 27), sr, opts, lists)
+            vals.append(float(ks2[0, 0] + 1e3 * lw2.sum() * ks[0, 0].detach() / lw.sum().detach()))
+        fd = (vals[0] - vals[1]) / (2 * h)
+        assert abs(fd - gx[j]) <= 1e-5 * np.abs(gx).max() + 1e-4 * abs(fd)
+    sr.close()

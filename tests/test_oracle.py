@@ -98,3 +98,29 @@ def test_planted_error_is_detected(rs6):
     lw[np.unravel_index(np.argmax(lw), lw.shape)] *= 1 + 1e-7
     with pytest.raises(AssertionError):
         np.testing.assert_allclose(lw, r["linewidth"], rtol=1e-10, atol=1e-14 * np.abs(r["linewidth"]).max())
+
+
+def test_oracle_adjoint_matches_finite_differences(configs):
+    """The oracle's reverse-mode restatement of the three-phonon linewidth with respect to
+    fc3_mwm against central differences of the oracle's own forward pass."""
+    prob = Problem.load(configs["rocksalt"], (4, 4, 4), readiso=True)
+    opts = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=5)
+    lists = QLists.monte_carlo(prob, opts)
+    rng = np.random.default_rng(0)
+    lw_bar = rng.normal(size=(prob.n_irr, prob.n_mode))
+    grad = orc.adjoint_fc3(prob, opts, lists, lw_bar)
+    m0 = prob.fc3_mwm.copy()
+    h = 1e-6 * np.abs(m0).max()
+
+    def loss():
+        return float(np.sum(orc.full_run(prob, opts, lists)["linewidth"] * lw_bar))
+
+    for _ in range(6):
+        t, e = int(rng.integers(prob.n_fc3)), int(rng.integers(27))
+        prob.fc3_mwm[t, e] = m0[t, e] + h
+        lp = loss()
+        prob.fc3_mwm[t, e] = m0[t, e] - h
+        lm = loss()
+        prob.fc3_mwm[t, e] = m0[t, e]
+        fd = (lp - lm) / (2 * h)
+        assert abs(fd - grad[t, e]) <= 1e-6 * abs(grad).max() + 1e-6 * abs(fd)
