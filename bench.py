@@ -88,6 +88,12 @@ def setup(cfg_name, precision="mixed"):
     return cfg, prob, opts, lists
 
 
+# DRAM bytes (read + write) of one launch of the fused kernel, from
+# `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none -k regex:k_threephonon`
+# on `python bench.py --profile --config <name> --steps 1 --warmup 1` (a one-pass capture).
+TRAFFIC_PER_LAUNCH = {"rocksalt16": 40_347_136, "rocksalt24": 458_850_000, "perovskite16": 1_104_760_000}
+
+
 class ClockSampler:
     """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
 
@@ -250,6 +256,21 @@ def run_gb300(args):
     kappa_iters = sr.n_iter
     stats = dict(sr.stats)
 
+    # ---- adjoint pass (d kappa_sma,xx / d Phi3) on the same workload, against the forward ----
+    kb = np.zeros((3, 3))
+    kb[0, 0] = 1.0
+    adj_ms = []
+    for _ in range(max(2, args.steps // 2)):
+        sr.generate(opts, lists)
+        fwd_ms = sr.stats["device_ms"]
+        sr.kappa(opts, maxiter=0)
+        sr.adjoint_fc3(opts, sr.kappa_sma_vjp(opts, kb))
+        adj_ms.append(sr.adjoint_stats["ms"])
+    adjoint = {"ms": float(np.median(adj_ms)), "forward_ms": fwd_ms,
+               "ratio_to_forward": float(np.median(adj_ms)) / fwd_ms,
+               "what": "tdg_adjoint_fc3 after tdg_kappa_sma_vjp: d kappa_xx / d mwm for all "
+                       f"{prob.n_fc3 * 27} third-order entries, mixed precision, Psi recomputed"}
+
     # ---- FP64 path on the same workload: kappa error bar and speedup ----
     o64 = type(opts)(**{**opts.__dict__, "precision": "fp64"})
     sr.generate(o64, lists)
@@ -259,17 +280,22 @@ def run_gb300(args):
     kappa_err = float(np.max(np.abs(ki32 - ki64)) / np.max(np.abs(ki64)))
 
     # ---- end to end through the public API with host buffers ----
-    e2e_s = []
+    e2e_s, parts = [], []
     h2d = d2h = 0
     for _ in range(args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         s2 = ScatteringRates(prob)
+        t1 = time.perf_counter()
         s2.generate(opts, lists)
+        t2 = time.perf_counter()
         s2.kappa(opts)
+        t3 = time.perf_counter()
         s2.close()
         torch.cuda.synchronize()
-        e2e_s.append(time.perf_counter() - t0)
+        t4 = time.perf_counter()
+        e2e_s.append(t4 - t0)
+        parts.append((t1 - t0, t2 - t1, t3 - t2, t4 - t3))
     nrow, ncol = lists.n_row, prob.n_full * n
     h2d = (prob.omega.nbytes + prob.vel.nbytes + prob.egv.nbytes * 3 // 2 + prob.n_op * prob.n_full * 4 +
            prob.fc3_mwm.nbytes * 3 // 2 + prob.fc3_lv.nbytes + lists.list3.nbytes + lists.ptr3.nbytes +
@@ -277,14 +303,29 @@ def run_gb300(args):
     d2h = nrow * 8 + prob.n_irr * n * 8 * 2 + 18 * 8 + kappa_iters * nrow * 3 * 8
 
     # ---- roofline of the dominant kernel (fused pretransform + contraction + epilogue) ----
+    # Per-unit work of a q-triplet: the pretransform streams N_t force-constant triplets
+    # (27 values + 6 lattice indices, 4 bytes each in mixed precision) and writes n^3
+    # complex values (8 bytes); the contraction is 24 n^4 flops. For n <= 6 the kernel is
+    # reported against HBM with the pretransform bytes, for larger n against the tensor
+    # peak with the contraction flops.
     hbm, bf16, src = peaks()
-    flop_per_trip = 24 * n**4 + 4 * 27 * prob.n_fc3
     fused_s = float(np.mean(fused_ms)) / 1e3
-    achieved = flop_per_trip * trip / fused_s / 1e12
-    roof = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16,
-            "traffic": None, "kernel": "k_threephonon (FP32 SIMT)",
-            "per_unit": f"{flop_per_trip} flop per q-triplet (24 n^4 contraction + 108 N_t pretransform)",
-            "peak_source": f"{src} dense bf16"}
+    bytes_per_trip = prob.n_fc3 * 33 * 4 + n**3 * 8
+    flop_per_trip = 24 * n**4
+    gbs = bytes_per_trip * trip / fused_s / 1e9
+    tfs = flop_per_trip * trip / fused_s / 1e12
+    traffic = TRAFFIC_PER_LAUNCH.get(args.config)
+    if n <= 6:
+        roof = {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+                "traffic": traffic, "per_unit": f"{bytes_per_trip} bytes per q-triplet (N_t*33*4 + n^3*8)",
+                "units_per_launch": trip, "peak_source": f"{src} copy bandwidth",
+                "tensor_frac_of_contraction": tfs / bf16}
+    else:
+        roof = {"bound": "tensor", "achieved": tfs, "peak": bf16, "unit": "TFLOP/s", "frac": tfs / bf16,
+                "traffic": traffic, "per_unit": f"{flop_per_trip} flop per q-triplet (24 n^4)",
+                "units_per_launch": trip, "peak_source": f"{src} dense bf16",
+                "hbm_frac_of_pretransform": gbs / hbm}
+    roof["kernel"] = "k_threephonon (fused pretransform, FP32 SIMT contraction, FP64 delta weights)"
 
     cpu_trip, cpu_s, desc, cores = cpu_sample(prob, opts, lists, budget_s=args.cpu_budget)
     value = trip * args.steps / (sum(dev_ms) / 1e3)
@@ -297,7 +338,10 @@ def run_gb300(args):
                    "l2": "256 MB buffer written between steps (L2 flush); Xi+od working set 2x%.2f GB" %
                          (nrow * ncol * 8 / 1e9)},
         "e2e": {"value": trip / float(np.mean(e2e_s)), "unit": "q-triplets/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h), "includes": "context creation, generate, kappa solve"},
+                "d2h_bytes_per_step": int(d2h), "includes": "context creation, generate, kappa solve",
+                "ms": {k: 1e3 * float(np.median([p[i] for p in parts]))
+                       for i, k in enumerate(("create", "generate", "kappa", "destroy"))}},
+        "adjoint": adjoint,
         "roofline": roof,
         "cpu_baseline": {"value": cpu_trip / cpu_s, "unit": "q-triplets/s", "cores": cores, "kind": "port",
                          "sample": desc},

@@ -142,6 +142,11 @@ const char *tdg_version(void);
 /* Number of CUDA devices visible (0 without a GPU); never fails. */
 int tdg_device_count(void);
 
+/* Diagnostic: one 128 x n x 16 tile through the tcgen05 tensor cores with BF16 hi/lo
+ * operand splits, d = a b (a 128 x 16 and b 16 x n row-major floats, n a multiple of 16 up
+ * to 256); variant 0..3 selects the shared-memory operand layout. No reference counterpart. */
+int tdg_check_mma(int32_t variant, int32_t n, const float *a, const float *b, float *d);
+
 /* Diagnostic, no counterpart in the reference: evaluates on the current device the FP64
  * exponential the delta weights use, out[i] = exp(-t[i]) for 0 <= t[i] <= 40 (the range
  * of lo_gauss inside its 8-sigma window), so tests can bound its error. */

@@ -28,6 +28,7 @@ ERRORS = {
 
 _i32p = C.POINTER(C.c_int32)
 _i64p = C.POINTER(C.c_int64)
+_f32p = C.POINTER(C.c_float)
 _f64p = C.POINTER(C.c_double)
 
 
@@ -107,6 +108,7 @@ SIGNATURES = {
     "tdg_version": (C.c_char_p, []),
     "tdg_device_count": (C.c_int, []),
     "tdg_check_exp": (C.c_int, [_f64p, C.c_int32, _f64p]),
+    "tdg_check_mma": (C.c_int, [C.c_int32, C.c_int32, _f32p, _f32p, _f32p]),
     "tdg_create": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(TdgProblem), C.c_int]),
     "tdg_destroy": (None, [C.c_void_p]),
     "tdg_mc_qlists": (C.c_int, [C.POINTER(TdgProblem), C.POINTER(TdgOpts), _i32p, _i32p, _i32p, _i64p, _i32p,

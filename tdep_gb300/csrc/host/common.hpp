@@ -2,10 +2,13 @@
 // small 3x3 linear algebra. Constant values are those of src/libolle/konstanter.f90.
 #pragma once
 
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <complex>
 #include <cstdint>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace tdg {
@@ -62,6 +65,26 @@ enum Status : int {
 
 // Records the message for tdg_last_error() and returns the code.
 int set_error(int code, const std::string &msg);
+
+// f(i) for i in [0, n) on all hardware threads (dynamic assignment, one index at a time);
+// f must be safe to run concurrently for different i.
+template <typename F>
+void parallel_for(int64_t n, F f) {
+    const unsigned nth = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), 64u));
+    if (n <= 1 || nth == 1) {
+        for (int64_t i = 0; i < n; ++i) f(i);
+        return;
+    }
+    std::atomic<int64_t> next{0};
+    auto work = [&]() {
+        for (int64_t i = next++; i < n; i = next++) f(i);
+    };
+    std::vector<std::thread> th;
+    const unsigned used = (unsigned)std::min<int64_t>(n, nth);
+    for (unsigned t = 1; t < used; ++t) th.emplace_back(work);
+    work();
+    for (auto &x : th) x.join();
+}
 const char *last_error();
 
 // ---- 3x3 helpers, column-major like the Fortran arrays: m[i + 3*j] ----

@@ -234,7 +234,22 @@ __global__ void k_xi_gemv(const double *__restrict__ xi, int64_t n_col, const do
     const int r = blockIdx.x;
     const double *row = xi + (int64_t)r * n_col;
     double s0 = 0.0, s1 = 0.0, s2 = 0.0;
-    for (int64_t j = threadIdx.x; j < n_col; j += blockDim.x) {
+    // four independent row loads in flight per thread before they are used
+    const int64_t step = blockDim.x;
+    int64_t j = threadIdx.x;
+    for (; j + 3 * step < n_col; j += 4 * step) {
+        double x[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) x[u] = __ldcs(row + j + u * step);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const double *f = fbb + (j + u * step) * 3;
+            s0 = fma(x[u], __ldg(f), s0);
+            s1 = fma(x[u], __ldg(f + 1), s1);
+            s2 = fma(x[u], __ldg(f + 2), s2);
+        }
+    }
+    for (; j < n_col; j += step) {
         const double x = __ldcs(row + j);
         const double *f = fbb + j * 3;
         s0 = fma(x, __ldg(f), s0);
@@ -311,6 +326,28 @@ cudaError_t launch_sym_scatmat(const MeshDev &m, const OrbitDev &o, int32_t n_ro
     if (n_row <= 0 || o.max_rep <= 0) return cudaSuccess;
     dim3 grid((unsigned)(((int64_t)o.max_rep * m.n_mode + 127) / 128), (unsigned)n_row);
     k_sym_scatmat<<<grid, 128, 0, s>>>(m, o, row_q1, xi);
+    return cudaGetLastError();
+}
+
+// foldout (kappa.f90:382-404): F of every full-mesh point from its irreducible point,
+// Fbb(q, b) = sign(op) * R_|op| Fn(irr(q), b), one thread per (q, b).
+__global__ void k_foldout(int32_t n_full, int32_t n_mode, const int32_t *full_op, const int32_t *full_irr,
+                          const double *op_cart, const double *fn, double *fbb) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)n_full * n_mode) return;
+    const int iq = (int)(i / n_mode), b = (int)(i % n_mode);
+    const int iop = full_op[iq];
+    const double *m = op_cart + 9 * (abs(iop) - 1);
+    const double *v = fn + ((int64_t)full_irr[iq] * n_mode + b) * 3;
+    const double sg = iop > 0 ? 1.0 : -1.0;
+    for (int d = 0; d < 3; ++d) fbb[i * 3 + d] = sg * (m[d] * v[0] + m[d + 3] * v[1] + m[d + 6] * v[2]);
+}
+
+cudaError_t launch_foldout(int32_t n_full, int32_t n_mode, const int32_t *full_op, const int32_t *full_irr,
+                           const double *op_cart, const double *fn, double *fbb, cudaStream_t s) {
+    const int64_t n = (int64_t)n_full * n_mode;
+    if (n <= 0) return cudaSuccess;
+    k_foldout<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n_full, n_mode, full_op, full_irr, op_cart, fn, fbb);
     return cudaGetLastError();
 }
 

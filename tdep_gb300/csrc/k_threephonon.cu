@@ -72,6 +72,31 @@ __device__ __forceinline__ const float2 *egvs_ptr<float2>(const PhononDev &ph) {
     return ph.egvs32;
 }
 
+// One entry of the adjoint's gradient accumulator: FP64 on the FP64 path; on the mixed path
+// a compensated FP32 pair (sum, negated lost low part), because GB300's FP64 pipe runs at
+// 1/64 of the FP32 rate and every q-triplet adds into all n_fc3 * 27 entries.
+template <typename R>
+struct GradAcc;
+template <>
+struct GradAcc<double> {
+    using T = double;
+    __device__ static void add(double &a, double v) { a += v; }
+    __host__ __device__ static double value(double a) { return a; }
+    __device__ static double zero() { return 0.0; }
+};
+template <>
+struct GradAcc<float> {
+    using T = float2;
+    __device__ static void add(float2 &a, float v) {
+        const float y = v - a.y;
+        const float t = a.x + y;
+        a.y = (t - a.x) - y;
+        a.x = t;
+    }
+    __host__ __device__ static double value(float2 a) { return (double)a.x - (double)a.y; }
+    __device__ static float2 zero() { return make_float2(0.f, 0.f); }
+};
+
 // exp(-2 pi i (q2.lv2 + q3.lv3)) of force-constant triplet t as an exact root of unity:
 // q = g/G on the mesh and lv integer, so the phase index is sum_d (g2 lv2 + g3 lv3)_d mod G_d
 // scaled to L = lcm(G).
@@ -215,6 +240,13 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
     const int64_t ld = (int64_t)m.n_full * N;
     const int it = P.integrationtype;
     const float sigfix32 = (float)P.sigma_fixed;
+    using GA = GradAcc<R>;
+    using GT = typename GA::T;
+    GT *acc = (GT *)(smem + L.total);  // ADJ with acc_in_smem: [fc.n * 27]
+    if constexpr (ADJ) {
+        if (a.acc_in_smem)
+            for (int i = tid; i < fc.n * 27; i += bd) acc[i] = GA::zero();
+    }
 
     for (int t = blockIdx.x; t < a.n_trip; t += gridDim.x) {
         const TripletRec rec = a.trip[t];
@@ -512,20 +544,25 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
 #pragma unroll
                 for (int x = 0; x < N; ++x) A[ab * N + x] = acc[x];
             }
-            double *slice = a.mwm_bar + (size_t)blockIdx.x * fc.n * 27;
+            GT *slice = (GT *)a.mwm_bar + (size_t)blockIdx.x * fc.n * 27;
+            // thread -> one (i,j,k) of the 27 and every groups-th force-constant triplet; within a
+            // q-triplet exactly one thread touches each entry, and q-triplets are separated by
+            // barriers
+            const int groups = bd / 27, grp = tid / 27, ijk = tid % 27;
+            const int off = (ijk % 3) * N2 + ((ijk / 3) % 3) * N + ijk / 9;
             for (int c0 = 0; c0 < fc.n; c0 += kPhaseChunk) {
                 const int cn = min(kPhaseChunk, fc.n - c0);
                 __syncthreads();
                 for (int i = tid; i < cn; i += bd) ph[i] = phase3<C>(fc, m, gi2, gi3, c0 + i);
                 __syncthreads();
-                for (int x = tid; x < cn * 27; x += bd) {
-                    const int tt = c0 + x / 27, ijk = x % 27;
-                    const int blk = fc.blk_of[tt];
-                    const int a1 = blk / (NA * NA), a2 = (blk / NA) % NA, a3 = blk % NA;
-                    const int ii = ijk % 3, jj = (ijk / 3) % 3, kk = ijk / 9;
-                    const C q = A[((3 * a1 + ii) * N + 3 * a2 + jj) * N + 3 * a3 + kk];
-                    const C p = ph[x / 27];
-                    slice[(size_t)tt * 27 + ijk] += 2.0 * ((double)p.x * (double)q.x - (double)p.y * (double)q.y);
+                if (grp < groups) {
+                    for (int tl = grp; tl < cn; tl += groups) {
+                        const int tt = c0 + tl;
+                        const C q = A[fc.abase[tt] + off];
+                        const C p = ph[tl];
+                        const R v = (R)2 * (p.x * q.x - p.y * q.y);
+                        GA::add(a.acc_in_smem ? acc[(size_t)tt * 27 + ijk] : slice[(size_t)tt * 27 + ijk], v);
+                    }
                 }
             }
             __syncthreads();
@@ -578,19 +615,29 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
         }
         __syncthreads();
     }
+    if constexpr (ADJ) {
+        if (a.acc_in_smem) {
+            __syncthreads();
+            GT *slice = (GT *)a.mwm_bar + (size_t)blockIdx.x * fc.n * 27;
+            for (int i = tid; i < fc.n * 27; i += bd) slice[i] = acc[i];
+        }
+    }
 }
 
 // Persistent grid: resident CTAs per SM times the SM count, at most one CTA per item.
+// Persistent grid: resident CTAs per SM times the SM count, at most one CTA per item.
+// `extra` bytes of dynamic shared memory follow the kernel's layout (adjoint accumulator).
 template <int N, typename R, bool ADJ>
-int grid_n(int n_sm, int n_trip) {
+int grid_n(int n_sm, int n_trip, size_t extra) {
     const Layout L = make_layout(N, sizeof(typename CT<R>::C));
-    if (cudaFuncSetAttribute(k_threephonon<N, R, ADJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total) !=
+    const size_t bytes = L.total + extra;
+    if (cudaFuncSetAttribute(k_threephonon<N, R, ADJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
         cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_threephonon<N, R, ADJ>, threads_for(N), L.total) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_threephonon<N, R, ADJ>, threads_for(N), bytes) !=
             cudaSuccess ||
         per_sm < 1) {
         cudaGetLastError();
@@ -601,49 +648,50 @@ int grid_n(int n_sm, int n_trip) {
 }
 
 template <int N, typename R, bool ADJ>
-cudaError_t launch_grid(const ThreePhArgs &a, int grid, cudaStream_t s) {
+cudaError_t launch_grid(const ThreePhArgs &a, int grid, size_t extra, cudaStream_t s) {
     const Layout L = make_layout(N, sizeof(typename CT<R>::C));
-    k_threephonon<N, R, ADJ><<<grid, threads_for(N), L.total, s>>>(a);
+    k_threephonon<N, R, ADJ><<<grid, threads_for(N), L.total + extra, s>>>(a);
     return cudaGetLastError();
 }
 
 template <int N, typename R>
 cudaError_t launch_n(const ThreePhArgs &a, int n_sm, cudaStream_t s) {
-    const int grid = grid_n<N, R, false>(n_sm, a.n_trip);
+    const int grid = grid_n<N, R, false>(n_sm, a.n_trip, 0);
     if (grid < 1) return cudaErrorInvalidConfiguration;
-    return launch_grid<N, R, false>(a, grid, s);
+    return launch_grid<N, R, false>(a, grid, 0, s);
 }
 
 template <typename R, bool ADJ>
-int grid_prec(int n, int n_sm, int n_trip) {
+int grid_prec(int n, int n_sm, int n_trip, size_t extra) {
     switch (n) {
-        case 3: return grid_n<3, R, ADJ>(n_sm, n_trip);
-        case 6: return grid_n<6, R, ADJ>(n_sm, n_trip);
-        case 9: return grid_n<9, R, ADJ>(n_sm, n_trip);
-        case 12: return grid_n<12, R, ADJ>(n_sm, n_trip);
-        case 15: return grid_n<15, R, ADJ>(n_sm, n_trip);
-        case 18: return grid_n<18, R, ADJ>(n_sm, n_trip);
+        case 3: return grid_n<3, R, ADJ>(n_sm, n_trip, extra);
+        case 6: return grid_n<6, R, ADJ>(n_sm, n_trip, extra);
+        case 9: return grid_n<9, R, ADJ>(n_sm, n_trip, extra);
+        case 12: return grid_n<12, R, ADJ>(n_sm, n_trip, extra);
+        case 15: return grid_n<15, R, ADJ>(n_sm, n_trip, extra);
+        case 18: return grid_n<18, R, ADJ>(n_sm, n_trip, extra);
         default: return 0;
     }
 }
 
 template <typename R>
-cudaError_t launch_adj_prec(const ThreePhArgs &a, int grid, cudaStream_t s) {
+cudaError_t launch_adj_prec(const ThreePhArgs &a, int grid, size_t extra, cudaStream_t s) {
     switch (a.mesh.n_mode) {
-        case 3: return launch_grid<3, R, true>(a, grid, s);
-        case 6: return launch_grid<6, R, true>(a, grid, s);
-        case 9: return launch_grid<9, R, true>(a, grid, s);
-        case 12: return launch_grid<12, R, true>(a, grid, s);
-        case 15: return launch_grid<15, R, true>(a, grid, s);
-        case 18: return launch_grid<18, R, true>(a, grid, s);
+        case 3: return launch_grid<3, R, true>(a, grid, extra, s);
+        case 6: return launch_grid<6, R, true>(a, grid, extra, s);
+        case 9: return launch_grid<9, R, true>(a, grid, extra, s);
+        case 12: return launch_grid<12, R, true>(a, grid, extra, s);
+        case 15: return launch_grid<15, R, true>(a, grid, extra, s);
+        case 18: return launch_grid<18, R, true>(a, grid, extra, s);
         default: return cudaErrorNotSupported;
     }
 }
 
-__global__ void k_sum_slices(const double *slices, int32_t n_slice, int64_t n, double *out) {
+template <typename R>
+__global__ void k_sum_slices(const typename GradAcc<R>::T *slices, int32_t n_slice, int64_t n, double *out) {
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
         double acc = 0.0;
-        for (int g = 0; g < n_slice; ++g) acc += slices[(int64_t)g * n + e];
+        for (int g = 0; g < n_slice; ++g) acc += GradAcc<R>::value(slices[(int64_t)g * n + e]);
         out[e] = acc;
     }
 }
@@ -686,20 +734,28 @@ cudaError_t launch_threephonon(const ThreePhArgs &a, int precision, int n_sm, cu
     return launch_prec<float>(a, n_sm, s);
 }
 
-int threephonon_adjoint_grid(int n, int precision, int n_sm, int n_trip) {
-    return precision == 0 ? grid_prec<double, true>(n, n_sm, n_trip) : grid_prec<float, true>(n, n_sm, n_trip);
+int threephonon_adjoint_grid(int n, int precision, int n_sm, int n_trip, int n_fc, bool acc_in_smem) {
+    const size_t extra = acc_in_smem ? (size_t)n_fc * 27 * sizeof(double) : 0;
+    return precision == 0 ? grid_prec<double, true>(n, n_sm, n_trip, extra)
+                          : grid_prec<float, true>(n, n_sm, n_trip, extra);
 }
 
 cudaError_t launch_threephonon_adjoint(const ThreePhArgs &a, int precision, int grid, cudaStream_t s) {
     if (a.n_trip <= 0 || grid <= 0) return cudaSuccess;
-    if (precision == 0) return launch_adj_prec<double>(a, grid, s);
-    return launch_adj_prec<float>(a, grid, s);
+    const size_t extra = a.acc_in_smem ? (size_t)a.fc.n * 27 * sizeof(double) : 0;
+    if (precision == 0) return launch_adj_prec<double>(a, grid, extra, s);
+    return launch_adj_prec<float>(a, grid, extra, s);
 }
 
-cudaError_t launch_sum_slices(const double *slices, int32_t n_slice, int64_t n, double *out, cudaStream_t s) {
+cudaError_t launch_sum_slices(const void *slices, int precision, int32_t n_slice, int64_t n, double *out,
+                              cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     const int64_t blocks = (n + 255) / 256;
-    k_sum_slices<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, s>>>(slices, n_slice, n, out);
+    const unsigned g = (unsigned)(blocks < 4096 ? blocks : 4096);
+    if (precision == 0)
+        k_sum_slices<double><<<g, 256, 0, s>>>((const double *)slices, n_slice, n, out);
+    else
+        k_sum_slices<float><<<g, 256, 0, s>>>((const float2 *)slices, n_slice, n, out);
     return cudaGetLastError();
 }
 

@@ -100,6 +100,10 @@ struct tdg_ctx {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[10] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     int32_t *h_tot = nullptr;  // pinned host word pair for the enumeration totals
+    double *h_fn = nullptr, *h_kbuf = nullptr;  // pinned BTE vectors (Fn, Xi.Fbb), grown on demand
+    size_t h_fn_n = 0, h_kbuf_n = 0;
+    DevBuf<int32_t> d_full_op;
+    DevBuf<double> d_op_cart, d_fn;
     // host copy of the problem
     int na = 0, n = 0, nop = 0, N = 0, nirr = 0;
     int grid[3] = {0, 0, 0};
@@ -112,7 +116,7 @@ struct tdg_ctx {
     DevBuf<double> d_omega, d_vel, d_be, d_sigsq, d_disorder;
     DevBuf<double2> d_egv, d_egvs;
     DevBuf<float2> d_egvs32;
-    DevBuf<int32_t> fc3_blk, fc3_lv, fc4_blk, fc4_lv, fc3_blk_of;
+    DevBuf<int32_t> fc3_blk, fc3_lv, fc4_blk, fc4_lv, fc3_abase;
     std::vector<int> fc3_perm;  // device (block-sorted) position -> index in the problem
     DevBuf<double> fc3_mwm, fc4_mwm;
     DevBuf<float> fc3_mwm32, fc4_mwm32;
@@ -173,6 +177,30 @@ struct tdg_ctx {
         return m;
     }
 };
+
+extern "C" int tdg_check_mma(int32_t variant, int32_t n, const float *a, const float *b, float *d) {
+    if (!a || !b || !d || variant < 0 || variant > 3 || n < 16 || n > 256 || n % 16 != 0)
+        return set_error(kErrParam, "tdg_check_mma: bad argument");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return set_error(kErrDevice, "no CUDA device available");
+    }
+    DevBuf<float> da, db, dd;
+    DevBuf<int> dst;
+    CUDA_TRY(da.upload(a, 128 * 16, nullptr));
+    CUDA_TRY(db.upload(b, 16 * (size_t)n, nullptr));
+    CUDA_TRY(dd.alloc(128 * (size_t)n));
+    CUDA_TRY(dst.alloc(1));
+    CUDA_TRY(cudaMemset(dst.p, 0, sizeof(int)));
+    CUDA_TRY(launch_mma_check(variant, n, da.p, db.p, dd.p, dst.p, nullptr));
+    CUDA_TRY(cudaDeviceSynchronize());
+    int st = 0;
+    CUDA_TRY(cudaMemcpy(&st, dst.p, sizeof(int), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(d, dd.p, sizeof(float) * 128 * n, cudaMemcpyDeviceToHost));
+    if (st) return set_error(kErrDevice, "tdg_check_mma: the MMA did not complete in time");
+    return kOk;
+}
 
 extern "C" int tdg_check_exp(const double *t, int32_t n, double *out) {
     if (!t || !out || n < 0) return set_error(kErrParam, "tdg_check_exp: bad argument");
@@ -368,7 +396,7 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
     }
     // Force constants sorted by atom block (a1,a2,a3).
     const int na = c->na;
-    std::vector<int32_t> blk_ptr3(na * na * na + 1, 0), lv3, blk_of3;
+    std::vector<int32_t> blk_ptr3(na * na * na + 1, 0), lv3, abase3;
     std::vector<double> mwm3;
     std::vector<float> mwm3f;
     {
@@ -381,7 +409,10 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
         std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return blk(x) < blk(y); });
         c->fc3_perm = idx;
         for (int t : idx) {
-            blk_of3.push_back(blk(t));
+            {
+                const int32_t *at = p->fc3_atoms + 3 * t;
+                abase3.push_back(((3 * (at[0] - 1)) * c->n + 3 * (at[1] - 1)) * c->n + 3 * (at[2] - 1));
+            }
             blk_ptr3[blk(t) + 1]++;
             lv3.insert(lv3.end(), p->fc3_lv + 6 * t, p->fc3_lv + 6 * t + 6);
             for (int k = 0; k < 27; ++k) {
@@ -435,7 +466,7 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
     chk(c->d_egvs32.upload(egvs32.data(), egvs32.size(), s));
     chk(c->d_disorder.upload(c->disorder.data(), c->disorder.size(), s));
     chk(c->fc3_blk.upload(blk_ptr3.data(), blk_ptr3.size(), s));
-    chk(c->fc3_blk_of.upload(blk_of3.data(), blk_of3.size(), s));
+    chk(c->fc3_abase.upload(abase3.data(), abase3.size(), s));
     chk(c->fc3_lv.upload(lv3.data(), lv3.size(), s));
     chk(c->fc3_mwm.upload(mwm3.data(), mwm3.size(), s));
     chk(c->fc3_mwm32.upload(mwm3f.data(), mwm3f.size(), s));
@@ -504,6 +535,8 @@ extern "C" void tdg_destroy(tdg_ctx *c) {
     for (auto &x : c->ev)
         if (x) cudaEventDestroy(x);
     if (c->h_tot) cudaFreeHost(c->h_tot);
+    if (c->h_fn) cudaFreeHost(c->h_fn);
+    if (c->h_kbuf) cudaFreeHost(c->h_kbuf);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -521,7 +554,8 @@ int validate_opts(const tdg_opts *o) {
     return kOk;
 }
 
-int check_list(const char *what, int n_row, const int64_t *ptr, const int32_t *l, int N) {
+// Row pointers of a CSR sample; with check_values also every entry's range.
+int check_list(const char *what, int n_row, const int64_t *ptr, const int32_t *l, int N, bool check_values = true) {
     if (!ptr) return set_error(kErrParam, std::string(what) + ": missing row pointer");
     if (ptr[0] != 0) return set_error(kErrParam, std::string(what) + ": ptr[0] must be 0");
     for (int r = 0; r < n_row; ++r) {
@@ -529,6 +563,7 @@ int check_list(const char *what, int n_row, const int64_t *ptr, const int32_t *l
         if (ptr[r + 1] == ptr[r]) return set_error(kErrParam, std::string(what) + ": empty q' sample for a row");
     }
     if (ptr[n_row] > 0 && !l) return set_error(kErrParam, std::string(what) + ": missing list");
+    if (!check_values) return kOk;
     for (int64_t i = 0; i < ptr[n_row]; ++i)
         if (l[i] < 1 || l[i] > N) return set_error(kErrParam, std::string(what) + ": q' index out of range");
     return kOk;
@@ -569,7 +604,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
             return set_error(kErrParam, "rows do not match the (q1,b1) set with omega >= lo_freqtol");
     const int nr = ql->n_row;
     if (o->thirdorder) {
-        st = check_list("three-phonon sample", nr, ql->ptr3, ql->list3, N);
+        st = check_list("three-phonon sample", nr, ql->ptr3, ql->list3, N, false);
         if (st) return st;
         if (c->n_fc3 < 1) return set_error(kErrParam, "three-phonon scattering requested without force constants");
         if (n > 18) return set_error(kErrParam, "this build's fused three-phonon kernel supports up to 6 atoms");
@@ -656,15 +691,22 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
             r1 = r0;
             while (r1 < nr && rq1[r1] == q1) ++r1;
         };
-        for (int q1 = 0; q1 < nirr && shared; ++q1) {
+        // rows of a q1 share one sample when every row's list equals the first row's
+        // (compared on all host threads)
+        std::vector<char> same(nirr, 1);
+        parallel_for(nirr, [&](int64_t q1) {
             int r0, r1;
-            rows_of(q1, r0, r1);
-            for (int r = r0 + 1; r < r1 && shared; ++r) {
+            rows_of((int)q1, r0, r1);
+            for (int r = r0 + 1; r < r1; ++r) {
                 const int64_t L = ql->ptr3[r0 + 1] - ql->ptr3[r0];
-                shared = (ql->ptr3[r + 1] - ql->ptr3[r] == L) &&
-                         std::memcmp(ql->list3 + ql->ptr3[r], ql->list3 + ql->ptr3[r0], sizeof(int32_t) * L) == 0;
+                if (ql->ptr3[r + 1] - ql->ptr3[r] != L ||
+                    std::memcmp(ql->list3 + ql->ptr3[r], ql->list3 + ql->ptr3[r0], sizeof(int32_t) * L) != 0) {
+                    same[q1] = 0;
+                    return;
+                }
             }
-        }
+        });
+        for (int q1 = 0; q1 < nirr; ++q1) shared = shared && same[q1];
         std::vector<std::array<uint32_t, 4>> table;
         auto mask_id = [&](const std::array<uint32_t, 4> &key) {
             for (int t = (int)table.size() - 1; t >= 0 && t >= (int)table.size() - 8; --t)
@@ -674,29 +716,59 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         };
         std::vector<int32_t> stamp(N, -1);
         if (shared) {
+            // one list per q1: offsets first, then range and repeat checks and the copy in
+            // parallel (the other rows' lists are byte-equal to it)
             qdesc.assign(nirr, make_int4(0, 0, 0, 0));
+            std::vector<int64_t> start(nirr + 1, 0);
             for (int q1 = 0; q1 < nirr; ++q1) {
                 int r0, r1;
                 rows_of(q1, r0, r1);
+                const int64_t L = r0 == r1 ? 0 : ql->ptr3[r0 + 1] - ql->ptr3[r0];
+                start[q1 + 1] = start[q1] + L;
                 if (r0 == r1) continue;
                 std::array<uint32_t, 4> key = {0u, 0u, 0u, 0u};
                 for (int r = r0; r < r1; ++r) key[rb1[r] >> 5] |= 1u << (rb1[r] & 31);
-                const int64_t L = ql->ptr3[r0 + 1] - ql->ptr3[r0];
-                const int64_t start = (int64_t)slist.size();
-                for (int64_t i = 0; i < L; ++i) {
-                    const int32_t q2 = ql->list3[ql->ptr3[r0] + i];
-                    if (stamp[q2 - 1] == q1) return set_error(kErrParam, "three-phonon sample repeats a q-point");
-                    stamp[q2 - 1] = q1;
-                    slist.push_back(q2);
-                }
-                qdesc[q1] = make_int4((int32_t)start, (int32_t)L, (int32_t)nc64, mask_id(key));
+                qdesc[q1] = make_int4((int32_t)start[q1], (int32_t)L, (int32_t)start[q1], mask_id(key));
                 for (int r = r0; r < r1; ++r) {
-                    rbeg[r] = start;
+                    rbeg[r] = start[q1];
                     rlen[r] = (int32_t)L;
                 }
-                nc64 += L;
             }
+            if (start[nirr] >= ((int64_t)1 << 31) - 1)
+                return set_error(kErrBadDim, "too many three-phonon candidates for one call");
+            slist.resize(start[nirr]);
+            std::atomic<int> bad{0};
+            parallel_for(nirr, [&](int64_t q1) {
+                const int L = (int)(start[q1 + 1] - start[q1]);
+                if (L == 0) return;
+                const int32_t *src = ql->list3 + ql->ptr3[qr0[q1]];
+                std::vector<uint32_t> seen(((size_t)N + 31) / 32, 0u);
+                for (int i = 0; i < L; ++i) {
+                    const int32_t q2 = src[i];
+                    if (q2 < 1 || q2 > N) {
+                        bad.store(1);
+                        return;
+                    }
+                    uint32_t &w = seen[(q2 - 1) >> 5];
+                    const uint32_t bit = 1u << ((q2 - 1) & 31);
+                    if (w & bit) {
+                        bad.store(2);
+                        return;
+                    }
+                    w |= bit;
+                    slist[start[q1] + i] = q2;
+                }
+            });
+            if (bad.load() == 1) return set_error(kErrParam, "three-phonon sample: q' index out of range");
+            if (bad.load() == 2) return set_error(kErrParam, "three-phonon sample repeats a q-point");
+            nc64 = start[nirr];
         } else {
+            std::atomic<int> bad{0};
+            parallel_for(nr, [&](int64_t r) {
+                for (int64_t i = ql->ptr3[r]; i < ql->ptr3[r + 1]; ++i)
+                    if (ql->list3[i] < 1 || ql->list3[i] > N) bad.store(1);
+            });
+            if (bad.load()) return set_error(kErrParam, "three-phonon sample: q' index out of range");
             std::vector<uint32_t> mark((size_t)N * 4, 0u);
             std::vector<int32_t> touched;
             for (int q1 = 0; q1 < nirr; ++q1) {
@@ -927,9 +999,10 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         a.fc.mwm32 = c->fc3_mwm32.p;
         a.fc.twiddle = c->tw.p;
         a.fc.twiddle32 = c->tw32.p;
-        a.fc.blk_of = c->fc3_blk_of.p;
+        a.fc.abase = c->fc3_abase.p;
         a.lam = nullptr;
         a.mwm_bar = nullptr;
+        a.acc_in_smem = 0;
         a.trip = c->d_trip.p;
         a.n_trip = ntrip;
         a.red = c->d_red.p;
@@ -1176,11 +1249,6 @@ extern "C" int tdg_triplets(tdg_ctx *c, int32_t q1, const int32_t *sample, int64
 
 namespace {
 
-// op%m applied to a vector, with an optional sign (time reversal).
-inline void rotate(const double *m, const double *v, double *out, double sg = 1.0) {
-    for (int i = 0; i < 3; ++i) out[i] = sg * (m[i] * v[0] + m[i + 3] * v[1] + m[i + 6] * v[2]);
-}
-
 // get_kappa (kappa.f90:28-75). The reference symmetrises every mode's F (x) v over the
 // operations, (1/nop) sum_R (R F) (x) (R v) = (1/nop) sum_R R (F (x) v) R^T; that map is
 // linear, so the per-mode tensors are summed first and the operations applied once.
@@ -1264,24 +1332,41 @@ extern "C" int tdg_kappa(tdg_ctx *c, const tdg_opts *o, int32_t maxiter, double 
     int iters = 0;
     if (maxiter > 0) {
         const int64_t ncol = (int64_t)N * n;
+        const size_t nfn = (size_t)nirr * n * 3, nbuf = (size_t)nr * 3;
         CUDA_TRY(c->d_fbb.alloc((size_t)ncol * 3));
-        CUDA_TRY(c->d_buf.alloc((size_t)nr * 3));
-        std::vector<double> Fbb((size_t)ncol * 3), buf((size_t)nr * 3), Fnb((size_t)nirr * n * 3);
+        CUDA_TRY(c->d_buf.alloc(nbuf));
+        CUDA_TRY(c->d_fn.alloc(nfn));
+        if (c->d_full_op.n == 0) {
+            CUDA_TRY(c->d_full_op.upload(c->full_op.data(), N, s));
+            CUDA_TRY(c->d_op_cart.upload(c->op_cart.data(), c->op_cart.size(), s));
+        }
+        if (c->h_fn_n < nfn) {
+            if (c->h_fn) cudaFreeHost(c->h_fn);
+            c->h_fn = nullptr;
+            c->h_fn_n = 0;
+            CUDA_TRY(cudaMallocHost(&c->h_fn, sizeof(double) * nfn));
+            c->h_fn_n = nfn;
+        }
+        if (c->h_kbuf_n < nbuf) {
+            if (c->h_kbuf) cudaFreeHost(c->h_kbuf);
+            c->h_kbuf = nullptr;
+            c->h_kbuf_n = 0;
+            CUDA_TRY(cudaMallocHost(&c->h_kbuf, sizeof(double) * nbuf));
+            c->h_kbuf_n = nbuf;
+        }
+        const double *buf = c->h_kbuf;
+        std::vector<double> Fnb((size_t)nirr * n * 3);
         std::vector<double> scf(maxiter, 0.0);
         double mixing = 0.95;
-        double kap[9];
         for (int iter = 1; iter <= maxiter; ++iter) {
             iters = iter;
-            // foldout (kappa.f90:382-404)
-            for (int iq = 0; iq < N; ++iq) {
-                const int iop = c->full_op[iq], jq = c->full_irr[iq] - 1;
-                const double *m = &c->op_cart[9 * (std::abs(iop) - 1)];
-                for (int b1 = 0; b1 < n; ++b1)
-                    rotate(m, &Fn[((size_t)jq * n + b1) * 3], &Fbb[((size_t)iq * n + b1) * 3], iop > 0 ? 1.0 : -1.0);
-            }
-            CUDA_TRY(cudaMemcpyAsync(c->d_fbb.p, Fbb.data(), sizeof(double) * Fbb.size(), cudaMemcpyHostToDevice, s));
+            // foldout (kappa.f90:382-404) and the three Xi products (:411-413) on the device;
+            // only Fn (n_irr*n*3) goes up and Xi.Fbb (n_row*3) comes back
+            std::memcpy(c->h_fn, Fn.data(), sizeof(double) * nfn);
+            CUDA_TRY(cudaMemcpyAsync(c->d_fn.p, c->h_fn, sizeof(double) * nfn, cudaMemcpyHostToDevice, s));
+            CUDA_TRY(launch_foldout(N, n, c->d_full_op.p, c->d_full_irr.p, c->d_op_cart.p, c->d_fn.p, c->d_fbb.p, s));
             CUDA_TRY(launch_xi_gemv(c->d_xi.p, nr, ncol, c->d_fbb.p, c->d_buf.p, c->n_sm, s));
-            CUDA_TRY(cudaMemcpyAsync(buf.data(), c->d_buf.p, sizeof(double) * buf.size(), cudaMemcpyDeviceToHost, s));
+            CUDA_TRY(cudaMemcpyAsync(c->h_kbuf, c->d_buf.p, sizeof(double) * nbuf, cudaMemcpyDeviceToHost, s));
             CUDA_TRY(cudaStreamSynchronize(s));
             // applyXi (kappa.f90:407-426)
             std::fill(Fnb.begin(), Fnb.end(), 0.0);
@@ -1323,7 +1408,6 @@ extern "C" int tdg_kappa(tdg_ctx *c, const tdg_opts *o, int32_t maxiter, double 
                     for (int d = 0; d < 3; ++d) fn[d] = fn[d] * (1.0 - mixing) + mixing * fb[d];
                 }
             scf[iter - 1] = g0 / nirr / n;
-            get_kappa(c, Fn, T, classical, kap);
             if (iter >= 3) {
                 const double g = scf[iter - 3] + scf[iter - 2] + scf[iter - 1];
                 if (g < tol) break;
@@ -1440,7 +1524,9 @@ extern "C" int tdg_adjoint_fc3(tdg_ctx *c, const tdg_opts *o, const double *lw_b
         lam[r] = acc / (double)dg;
     }
     const int ntrip = c->last_ntrip;
-    const int grid = threephonon_adjoint_grid(n, o->precision, c->n_sm, ntrip);
+    // the CTA's gradient slice lives in shared memory when it is small enough
+    const bool acc_smem = (size_t)c->n_fc3 * 27 * sizeof(double) <= 48 * 1024;
+    const int grid = threephonon_adjoint_grid(n, o->precision, c->n_sm, ntrip, c->n_fc3, acc_smem);
     if (ntrip > 0 && grid < 1) return set_error(kErrDevice, "adjoint kernel configuration failed");
     const int64_t nm = (int64_t)c->n_fc3 * 27;
     cudaError_t e = cudaSuccess;
@@ -1453,7 +1539,8 @@ extern "C" int tdg_adjoint_fc3(tdg_ctx *c, const tdg_opts *o, const double *lw_b
     if (e != cudaSuccess) return set_error(kErrDevice, std::string("allocation failed: ") + cudaGetErrorString(e));
     cudaEvent_t *ev = c->ev;
     CUDA_TRY(cudaEventRecord(ev[0], s));
-    CUDA_TRY(cudaMemsetAsync(c->d_slices.p, 0, sizeof(double) * (size_t)std::max(grid, 1) * nm, s));
+    if (!acc_smem || ntrip == 0)
+        CUDA_TRY(cudaMemsetAsync(c->d_slices.p, 0, sizeof(double) * (size_t)std::max(grid, 1) * nm, s));
     CUDA_TRY(cudaMemsetAsync(c->d_status.p, 0, sizeof(int32_t), s));
     ThreePhArgs a;
     a.mesh = c->mesh();
@@ -1467,7 +1554,7 @@ extern "C" int tdg_adjoint_fc3(tdg_ctx *c, const tdg_opts *o, const double *lw_b
     a.fc.mwm32 = c->fc3_mwm32.p;
     a.fc.twiddle = c->tw.p;
     a.fc.twiddle32 = c->tw32.p;
-    a.fc.blk_of = c->fc3_blk_of.p;
+    a.fc.abase = c->fc3_abase.p;
     a.trip = c->d_trip.p;
     a.n_trip = ntrip;
     a.red = c->d_red.p;
@@ -1477,10 +1564,11 @@ extern "C" int tdg_adjoint_fc3(tdg_ctx *c, const tdg_opts *o, const double *lw_b
     a.status = c->d_status.p;
     a.lam = c->d_lam.p;
     a.mwm_bar = c->d_slices.p;
+    a.acc_in_smem = acc_smem ? 1 : 0;
     CUDA_TRY(cudaEventRecord(ev[1], s));
     CUDA_TRY(launch_threephonon_adjoint(a, o->precision, grid, s));
     CUDA_TRY(cudaEventRecord(ev[2], s));
-    CUDA_TRY(launch_sum_slices(c->d_slices.p, std::max(grid, 1), nm, c->d_mwm_bar.p, s));
+    CUDA_TRY(launch_sum_slices(c->d_slices.p, o->precision, std::max(grid, 1), nm, c->d_mwm_bar.p, s));
     std::vector<double> dev(nm);
     CUDA_TRY(cudaMemcpyAsync(dev.data(), c->d_mwm_bar.p, sizeof(double) * nm, cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaEventRecord(ev[3], s));

@@ -74,7 +74,8 @@ struct Fc3Dev {
     const float *mwm32;       // [n*27]
     const double2 *twiddle;   // [L] exp(-2 pi i K / L)
     const float2 *twiddle32;
-    const int32_t *blk_of;    // [n] atom block (a1,a2,a3) of each triplet
+    const int32_t *abase;     // [n] ((3 a1) n + 3 a2) n + 3 a3: element (0,0,0) of the triplet's
+                              // atom block in the n^3 pretransformed tensor
 };
 
 struct Fc4Dev {
@@ -119,15 +120,18 @@ struct ThreePhArgs {
     // adjoint only: cotangent of each row's Gamma and one accumulation slice of
     // d L / d mwm ([fc.n * 27]) per CTA
     const double *lam;
-    double *mwm_bar;
+    double *mwm_bar;            // FP64 slices, or float2 (sum, correction) on the mixed path
+    int32_t acc_in_smem;        // accumulate the CTA's slice in shared memory, store it once
 };
 cudaError_t launch_threephonon(const ThreePhArgs &a, int precision, int n_sm, cudaStream_t s);
 // Adjoint of the three-phonon Gamma with respect to mwm: recomputes Psi per q-triplet and
 // accumulates 2 Re(phase * Q) into a.mwm_bar (one slice per CTA of the returned grid).
-int threephonon_adjoint_grid(int n, int precision, int n_sm, int n_trip);
+int threephonon_adjoint_grid(int n, int precision, int n_sm, int n_trip, int n_fc, bool acc_in_smem);
 cudaError_t launch_threephonon_adjoint(const ThreePhArgs &a, int precision, int grid, cudaStream_t s);
-// out[e] = sum over g < n_slice of slices[g * n + e], in slice order.
-cudaError_t launch_sum_slices(const double *slices, int32_t n_slice, int64_t n, double *out, cudaStream_t s);
+// out[e] = sum over g < n_slice of slices[g * n + e], in slice order; the slices hold FP64
+// (precision 0) or compensated FP32 pairs (mixed), 8 bytes per entry either way.
+cudaError_t launch_sum_slices(const void *slices, int precision, int32_t n_slice, int64_t n, double *out,
+                              cudaStream_t s);
 size_t threephonon_smem_bytes(int n, int precision, int n_fc);
 
 struct FourPhArgs {
@@ -188,6 +192,16 @@ cudaError_t launch_sym_scatmat(const MeshDev &m, const OrbitDev &o, int32_t n_ro
 // K8: buf[r*3+a] = sum_j xi[r, j] * fbb[j*3 + a].
 cudaError_t launch_xi_gemv(const double *xi, int32_t n_row, int64_t n_col, const double *fbb, double *buf,
                            int n_sm, cudaStream_t s);
+
+// One-tile tcgen05 self-check: d (128 x n) = a (128 x 16) b (16 x n) through BF16 hi/lo
+// splits; variant selects the operand layout reading (diagnostic).
+cudaError_t launch_mma_check(int variant, int n, const float *a, const float *b, float *d, int *status,
+                             cudaStream_t s);
+
+// foldout of the BTE: fbb[(q*n + b)*3 + d] = sign * (R fn[(irr(q)*n + b)*3 ..])_d with
+// full_op signed 1-based operations (negative: time reversal) and full_irr 0-based.
+cudaError_t launch_foldout(int32_t n_full, int32_t n_mode, const int32_t *full_op, const int32_t *full_irr,
+                           const double *op_cart, const double *fn, double *fbb, cudaStream_t s);
 
 // What an entry point compiled outside the context's own file needs of a context.
 struct CtxView {
