@@ -112,6 +112,9 @@ typedef struct tdg_opts {
     int32_t qg4ph[3];          /* -qg4ph after defaulting                                     */
     int32_t seed;              /* --seed (> 0)                                                */
     int32_t precision;         /* TDG_PREC_FP64 or TDG_PREC_MIXED                             */
+    int32_t tensor_cores;      /* no reference counterpart: 0 = automatic (the tcgen05
+                                  large-cell contraction for more than 18 modes), 1 = always
+                                  (mixed precision only)                                     */
 } tdg_opts;
 
 /*

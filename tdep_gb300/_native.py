@@ -86,6 +86,7 @@ class TdgOpts(C.Structure):
         ("qg4ph", C.c_int32 * 3),
         ("seed", C.c_int32),
         ("precision", C.c_int32),
+        ("tensor_cores", C.c_int32),
     ]
 
 

@@ -1,0 +1,477 @@
+// Large-cell three-phonon path (n_mode beyond the shared-memory kernel, e.g. a 40-atom cell
+// with 120 modes): the same arithmetic as k_threephonon, restructured for n^3 tensors that
+// do not fit on chip, with the Psi contraction on the tcgen05 tensor cores.
+//
+// Per batch of q-triplets (one slot each):
+//   phases  exp(-2 pi i (q2.lv2 + q3.lv3)) of every force-constant triplet (exact roots of unity)
+//   P       pretransform_phi3 (scattering_threephonon.f90:275-317) into the stage-1 operand
+//   3 GEMM  stages, each contracting the leading component index of the tensor with one
+//           eigenvector matrix: X[(ri,a)][(b,c)] -> Y[(b,c)][(ri',b1)] with the complex product
+//           written as a real one, [Yr | Yi] = [Xr | Xi] [[Er, Ei], [-Ei, Er]]; the epilogue
+//           writes the next stage's operand with the new index last, so that after
+//           contracting a (E1), b (E2) and c (E3) the result is Psi[b1][b2][b3]
+//   delta   get_dirac and the accumulation of Gamma and the Xi row terms
+//           (scattering_threephonon.f90:115-135, 219-271), FP64 weights and sums.
+// GEMM operands are BF16 hi/lo splits of FP32 values (hi*hi + hi*lo + lo*hi into an FP32
+// tensor-memory accumulator, about 16 significant bits per operand) in shared memory as
+// 8 x 16-byte core matrices without swizzle, both operands MN-major; the layout and the
+// descriptor reading (leading byte offset = K-direction core stride, stride byte offset =
+// MN-direction core stride) are the ones the one-tile self-check verifies.
+#include <cuda_bf16.h>
+
+#include "dev_common.cuh"
+#include "tc_common.cuh"
+#include "tdg_internal.cuh"
+
+namespace tdg {
+
+namespace {
+
+constexpr double kLnPrefactor = 3.141592653589793 / 16.0;
+constexpr long long kLnWaitCycles = 4000000000LL;  // about 2 s at 2 GHz
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+__device__ __forceinline__ void store_split(__nv_bfloat16 *hi, __nv_bfloat16 *lo, int64_t i, float v) {
+    unsigned short h, l;
+    tc::split_bf16(v, h, l);
+    hi[i] = __ushort_as_bfloat16(h);
+    lo[i] = __ushort_as_bfloat16(l);
+}
+
+// ---- real-split eigenvector matrices of every mesh point ----
+// bmat[((q*2 + h)*kp + k)*kp + c], h = 0 hi / 1 lo; k = ri*n + a, c = rj*n + b:
+// [[Er, Ei], [-Ei, Er]] with E[a][b] = component a of mode b of egv/sqrt(omega).
+__global__ void k_build_bmat(int n, int kp, int n_q, const float2 *egvs32, __nv_bfloat16 *bmat) {
+    const int64_t per = (int64_t)kp * kp;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)n_q * per) return;
+    const int q = (int)(i / per);
+    const int64_t e = i % per;
+    const int k = (int)(e / kp), c = (int)(e % kp);
+    float v = 0.f;
+    if (k < 2 * n && c < 2 * n) {
+        const int ri = k / n, a = k % n, rj = c / n, b = c % n;
+        const float2 E = egvs32[((size_t)q * n + b) * n + a];
+        v = ri == 0 ? (rj == 0 ? E.x : E.y) : (rj == 0 ? -E.y : E.x);
+    }
+    store_split(bmat + ((int64_t)q * 2) * per, bmat + ((int64_t)q * 2 + 1) * per, e, v);
+}
+
+// ---- phases of the force-constant triplets, per slot ----
+__global__ void k_ln_phases(Fc3Dev fc, MeshDev m, const TripletRec *trip, int nb, float2 *ph) {
+    const int s = blockIdx.y;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nb || t >= fc.n) return;
+    const TripletRec rec = trip[s];
+    const int n12 = m.grid[1] * m.grid[2];
+    const int g2[3] = {rec.q2 / n12, (rec.q2 / m.grid[2]) % m.grid[1], rec.q2 % m.grid[2]};
+    const int g3[3] = {rec.q3 / n12, (rec.q3 / m.grid[2]) % m.grid[1], rec.q3 % m.grid[2]};
+    const int32_t *lv = fc.lv + (size_t)t * 6;
+    int K = 0;
+    for (int d = 0; d < 3; ++d) {
+        int kd = (g2[d] * lv[d] + g3[d] * lv[3 + d]) % m.grid[d];
+        if (kd < 0) kd += m.grid[d];
+        K += kd * m.lmul[d];
+    }
+    ph[(size_t)s * fc.n + t] = fc.twiddle32[K % m.L];
+}
+
+// ---- pretransform into the stage-1 operand: X[k][m], k = ri*n + a, m = b*n + c ----
+__global__ void k_ln_pretransform(int n, int na, Fc3Dev fc, const float2 *ph, int nb, int64_t plane, int mp,
+                                  __nv_bfloat16 *xhi, __nv_bfloat16 *xlo) {
+    const int s = blockIdx.y;
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n3 = (int64_t)n * n * n;
+    if (s >= nb || e >= n3) return;
+    const int nn = n * n;
+    const int a = (int)(e / nn), bc = (int)(e % nn), b = bc / n, c = bc % n;
+    const int blk = ((a / 3) * na + b / 3) * na + c / 3;
+    const int ijk = (a % 3) + 3 * (b % 3) + 9 * (c % 3);
+    float2 acc = make_float2(0.f, 0.f);
+    const float2 *phs = ph + (size_t)s * fc.n;
+    for (int tt = fc.blk_ptr[blk]; tt < fc.blk_ptr[blk + 1]; ++tt) {
+        const float mv = __ldg(fc.mwm32 + (size_t)tt * 27 + ijk);
+        const float2 p = phs[tt];
+        acc.x = fmaf(mv, p.x, acc.x);
+        acc.y = fmaf(mv, p.y, acc.y);
+    }
+    __nv_bfloat16 *hi = xhi + (int64_t)s * plane, *lo = xlo + (int64_t)s * plane;
+    store_split(hi, lo, (int64_t)a * mp + bc, acc.x);
+    store_split(hi, lo, (int64_t)(n + a) * mp + bc, acc.y);
+}
+
+// ---- one contraction stage on the tensor cores ----
+struct LnGemmArgs {
+    const __nv_bfloat16 *xhi, *xlo;  // operand planes, slot s at + s * plane: X[k][m], M stride mp
+    int64_t plane;
+    int mp;
+    const __nv_bfloat16 *bmat;       // k_build_bmat
+    const TripletRec *trip;          // the batch's q-triplets (slot order)
+    const int32_t *irr_full;         // 0-based full index of irreducible q1
+    int stage;                       // 1, 2, 3: contract with E(q1), E(q2), E(q3)
+    int n, kp, kc;                   // modes, padded 2n (multiple of 16), K chunk
+    __nv_bfloat16 *ohi, *olo;        // stages 1-2: next operand planes
+    float2 *psi;                     // stage 3: [slot][n^3]
+    int32_t *status;
+};
+
+// Tile = 128 rows of M = n^2 for one slot, all kp columns. Two shared-memory buffers hold
+// K chunks of both operands (hi and lo); chunk c+1 streams in with cp.async while the MMAs
+// of chunk c run; each buffer's MMAs arrive on its own mbarrier before it is refilled.
+__global__ void __launch_bounds__(128, 1) k_ln_gemm(LnGemmArgs g) {
+    extern __shared__ __align__(1024) unsigned char sm[];
+    __shared__ uint64_t mbar[2];
+    __shared__ uint32_t tbase;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int s = blockIdx.y, m0 = blockIdx.x * 128;
+    const int n = g.n, kp = g.kp, kc = g.kc, M = n * n;
+    const int nch = kp / kc;
+    const uint32_t a_bytes = 128u * kc * 2u, b_bytes = (uint32_t)kc * kp * 2u;
+    const uint32_t buf_bytes = 2u * (a_bytes + b_bytes);
+    const uint32_t a_ck = 16u * 128u, b_ck = 16u * (uint32_t)kp;  // K-direction core strides
+    const uint32_t ncols = kp <= 32 ? 32u : (kp <= 64 ? 64u : (kp <= 128 ? 128u : 256u));
+    const TripletRec rec = g.trip[s];
+    const int q = g.stage == 1 ? g.irr_full[rec.q1] : (g.stage == 2 ? rec.q2 : rec.q3);
+    const int64_t bper = (int64_t)kp * kp;
+    const __nv_bfloat16 *bsrc[2] = {g.bmat + ((int64_t)q * 2) * bper, g.bmat + ((int64_t)q * 2 + 1) * bper};
+    const __nv_bfloat16 *xsrc[2] = {g.xhi + (int64_t)s * g.plane, g.xlo + (int64_t)s * g.plane};
+
+    if (warp == 0) tc::tmem_alloc(&tbase, ncols);
+    if (tid == 0) {
+        tc::mbar_init(&mbar[0], 1);
+        tc::mbar_init(&mbar[1], 1);
+        tc::fence_mbar_init();
+    }
+    auto load_chunk = [&](int c, int buf) {
+        unsigned char *base = sm + buf * buf_bytes;
+        const int k0 = c * kc;
+        // A: 2 planes x kc rows x 16 segments of 8 m
+        for (int i = tid; i < 2 * kc * 16; i += 128) {
+            const int h = i / (kc * 16), r = i % (kc * 16), k = r / 16, mb = r % 16;
+            const uint32_t dst = tc::smem_u32(base + h * a_bytes + mb * 128 + (k >> 3) * a_ck + (k & 7) * 16);
+            cp_async16(dst, xsrc[h] + (int64_t)(k0 + k) * g.mp + m0 + 8 * mb);
+        }
+        // B: 2 planes x kc rows x kp/8 segments
+        const int nbs = kp / 8;
+        for (int i = tid; i < 2 * kc * nbs; i += 128) {
+            const int h = i / (kc * nbs), r = i % (kc * nbs), k = r / nbs, nb = r % nbs;
+            const uint32_t dst =
+                tc::smem_u32(base + 2 * a_bytes + h * b_bytes + nb * 128 + (k >> 3) * b_ck + (k & 7) * 16);
+            cp_async16(dst, bsrc[h] + (int64_t)(k0 + k) * kp + 8 * nb);
+        }
+        cp_async_commit();
+    };
+    load_chunk(0, 0);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t taddr = tbase;
+    const uint32_t idesc = tc::idesc_bf16_f32(128, kp, true, true);
+    // every wait ends within kLnWaitCycles; the outcome is made uniform across the CTA before
+    // any thread acts on it, so that no barrier is skipped by part of the block
+    bool ok = true;
+    for (int c = 0; c < nch; ++c) {
+        const int buf = c & 1;
+        if (c + 1 < nch) {
+            bool w = true;
+            if (c >= 1) w = tc::mbar_wait(&mbar[buf ^ 1], ((c - 1) >> 1) & 1, kLnWaitCycles);
+            ok = __syncthreads_and(w ? 1 : 0) != 0;
+            if (!ok) break;
+            load_chunk(c + 1, buf ^ 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        tc::fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after_sync();
+            unsigned char *base = sm + buf * buf_bytes;
+            const uint32_t ah = tc::smem_u32(base), al = tc::smem_u32(base + a_bytes);
+            const uint32_t bh = tc::smem_u32(base + 2 * a_bytes), bl = tc::smem_u32(base + 2 * a_bytes + b_bytes);
+            for (int k16 = 0; k16 < kc / 16; ++k16) {
+                const uint32_t ao = k16 * 2 * a_ck, bo = k16 * 2 * b_ck;
+                const uint64_t dah = tc::smem_desc(ah + ao, a_ck, 128), dal = tc::smem_desc(al + ao, a_ck, 128);
+                const uint64_t dbh = tc::smem_desc(bh + bo, b_ck, 128), dbl = tc::smem_desc(bl + bo, b_ck, 128);
+                const uint32_t acc0 = (c > 0 || k16 > 0) ? 1u : 0u;
+                tc::mma_bf16(taddr, dah, dbh, idesc, acc0);
+                tc::mma_bf16(taddr, dah, dbl, idesc, 1u);
+                tc::mma_bf16(taddr, dal, dbh, idesc, 1u);
+            }
+            tc::mma_commit(&mbar[buf]);
+        }
+    }
+    if (ok) {
+        const bool w = tc::mbar_wait(&mbar[(nch - 1) & 1], ((nch - 1) >> 1) & 1, kLnWaitCycles);
+        ok = __syncthreads_and(w ? 1 : 0) != 0;
+    }
+    cp_async_wait<0>();
+    if (!ok) {
+        if (tid == 0) atomicExch(g.status, kDevOverflow);
+        // let whatever was issued drain before the tensor memory goes back
+        tc::mbar_wait(&mbar[(nch - 1) & 1], ((nch - 1) >> 1) & 1, kLnWaitCycles);
+    }
+    __syncthreads();
+    tc::fence_after_sync();
+    // ---- epilogue: tensor memory -> shared staging (row stride kp + 1) -> global ----
+    float *stage = (float *)sm;
+    const int ld = kp + 1;
+    if (ok) {
+        for (int c0 = 0; c0 < kp; c0 += 8) {
+            float v[8];
+            tc::tmem_ld8(taddr + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) stage[(32 * warp + lane) * ld + c0 + i] = v[i];
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(taddr, ncols);
+    if (!ok) return;
+    const int rows = min(128, M - m0);
+    if (g.stage < 3) {
+        // D[m = u*n + v][ri*n + w] -> X'[(ri*n + u)*mp + v*n + w]
+        __nv_bfloat16 *hi = g.ohi + (int64_t)s * g.plane, *lo = g.olo + (int64_t)s * g.plane;
+        const int per = 2 * n;
+        for (int i = tid; i < rows * per; i += 128) {
+            const int ml = i / per, r = i % per, ri = r / n, w = r % n;
+            const int m = m0 + ml, u = m / n, v = m % n;
+            store_split(hi, lo, (int64_t)(ri * n + u) * g.mp + v * n + w, stage[ml * ld + r]);
+        }
+    } else {
+        float2 *out = g.psi + (int64_t)s * M * n;
+        for (int i = tid; i < rows * n; i += 128) {
+            const int ml = i / n, w = i % n;
+            out[(int64_t)(m0 + ml) * n + w] = make_float2(stage[ml * ld + w], stage[ml * ld + n + w]);
+        }
+    }
+}
+
+// ---- delta weights and accumulation: one CTA per (slot, b1), 8 warps over b2, lanes over b3 ----
+struct LnDeltaArgs {
+    MeshDev mesh;
+    PhononDev ph;
+    RowsDev rows;
+    const TripletRec *trip;
+    const int2 *red;
+    const uint32_t *cand_mask;
+    const float2 *psi;
+    int n;
+    double *gamma, *od;
+};
+
+__global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    const int n = a.n;
+    const int s = blockIdx.y, b1 = blockIdx.x;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const TripletRec rec = a.trip[s];
+    const MeshDev &m = a.mesh;
+    const PhononDev &P = a.ph;
+    const uint32_t *mask = a.cand_mask + (size_t)rec.cand * 4;
+    if (!((mask[b1 >> 5] >> (b1 & 31)) & 1u)) return;
+    const int row = a.rows.rowidx[(size_t)rec.q1 * n + b1];
+    if (row < 0) return;
+    const int f1 = m.irr_full[rec.q1], q2 = rec.q2, q3 = rec.q3;
+    const int i2 = m.full_irr[q2], i3 = m.full_irr[q3];
+    double *om2 = (double *)sm, *om3 = om2 + n, *be2 = om3 + n, *be3 = be2 + n, *s2 = be3 + n, *s3 = s2 + n;
+    double *v2 = s3 + n, *v3 = v2 + 3 * n, *R2 = v3 + 3 * n, *R3w = R2 + n;  // R3w[8][n]
+    for (int b = tid; b < n; b += blockDim.x) {
+        om2[b] = P.omega[(size_t)q2 * n + b];
+        om3[b] = P.omega[(size_t)q3 * n + b];
+        be2[b] = P.be[(size_t)i2 * n + b];
+        be3[b] = P.be[(size_t)i3 * n + b];
+        s2[b] = P.sigsq[(size_t)i2 * n + b];
+        s3[b] = P.sigsq[(size_t)i3 * n + b];
+        for (int d = 0; d < 3; ++d) {
+            v2[b * 3 + d] = P.vel[((size_t)q2 * n + b) * 3 + d];
+            v3[b * 3 + d] = P.vel[((size_t)q3 * n + b) * 3 + d];
+        }
+    }
+    __syncthreads();
+    const double o1 = P.omega[(size_t)f1 * n + b1];
+    const double s1 = P.sigsq[(size_t)rec.q1 * n + b1];
+    double v1[3];
+    for (int d = 0; d < 3; ++d) v1[d] = P.vel[((size_t)f1 * n + b1) * 3 + d];
+    const double w = a.rows.weight3[row];
+    const double perm = q2 == q3 ? 1.0 : 2.0;
+    const int it = P.integrationtype;
+    const float fo1 = (float)o1, fs1 = (float)s1;
+    const float2 *psi = a.psi + ((int64_t)s * n + b1) * n * n;
+    double r3[4] = {0.0, 0.0, 0.0, 0.0};  // lanes own b3 = lane + 32 j, n <= 128
+    for (int b2 = warp; b2 < n; b2 += 8) {
+        const double o2 = om2[b2];
+        const bool skip2 = o2 < kFreqTolD || fabs(o1 - o2) < kFreqTolD;
+        double r2 = 0.0;
+        for (int j = 0; j < 4; ++j) {
+            const int b3 = lane + 32 * j;
+            if (b3 >= n || skip2) continue;
+            const double o3 = om3[b3];
+            if (o3 < kFreqTolD || fabs(o1 - o3) < kFreqTolD || fabs(o2 - o3) < kFreqTolD) continue;
+            // FP32 screen of the four Gaussians, margin as in the shared-memory kernel
+            uint32_t live = 15u;
+            if (it != 6) {
+                const float f2 = (float)o2, f3 = (float)o3;
+                const float sg = it == 1 ? (float)P.sigma_fixed : sqrtf(fs1 + (float)s2[b2] + (float)s3[b3]);
+                const float win = 8.0f * sg * 1.001f + 1e-6f * (fo1 + f2 + f3);
+                live = (fabsf(fo1 + f2 - f3) <= win ? 1u : 0u) | (fabsf(fo1 - f2 + f3) <= win ? 2u : 0u) |
+                       (fabsf(fo1 - f2 - f3) <= win ? 4u : 0u) | (fo1 + f2 + f3 <= win ? 8u : 0u);
+            }
+            if (!live) continue;
+            double sigma;
+            if (it == 1) {
+                sigma = P.sigma_fixed;
+            } else if (it == 2) {
+                sigma = sqrt(s1 + s2[b2] + s3[b3]);
+            } else {
+                sigma = adaptive_pair(v1, v2 + 3 * b2, P.reclat_g) / 3.0;
+                sigma += adaptive_pair(v1, v3 + 3 * b3, P.reclat_g) / 3.0;
+                sigma += adaptive_pair(v2 + 3 * b2, v3 + 3 * b3, P.reclat_g) / 3.0;
+                sigma += P.thresh_sigma;
+            }
+            const double invsig = 1.0 / sigma;
+            const double win8 = 8.0 * sigma, h = 0.5 * invsig * invsig, cg = kSqrt2PiInv * invsig;
+            const double *tab = P.exp2tab;
+            const double ga = (live & 1u) ? gauss(o1 - (-o2 + o3), win8, h, cg, tab) : 0.0;
+            const double gb = (live & 2u) ? gauss(o1 - (o2 - o3), win8, h, cg, tab) : 0.0;
+            const double gc = (live & 4u) ? gauss(o1 - (o2 + o3), win8, h, cg, tab) : 0.0;
+            const double gd = (live & 8u) ? gauss(o1 - (-o2 - o3), win8, h, cg, tab) : 0.0;
+            const double d0 = ga - gb, d1 = gc - gd;
+            if (!nonzero(d0) && !nonzero(d1)) continue;
+            const float2 ps = psi[b2 * n + b3];
+            const double cr = ps.x, ci = ps.y;
+            const double psisq = kLnPrefactor * (cr * cr + ci * ci) * w;
+            const double n2 = be2[b2], n3 = be3[b3];
+            const double f = perm * psisq * (n2 - n3) * d0 + perm * psisq * (n2 + n3 + 1.0) * d1;
+            r2 += f;
+            r3[j] += f;
+        }
+        for (int o = 16; o > 0; o >>= 1) r2 += __shfl_down_sync(0xffffffffu, r2, o);
+        if (lane == 0) R2[b2] = r2;
+    }
+    for (int j = 0; j < 4; ++j) {
+        const int b3 = lane + 32 * j;
+        if (b3 < n) R3w[warp * n + b3] = r3[j];
+    }
+    __syncthreads();
+    for (int b3 = tid; b3 < n; b3 += blockDim.x) {
+        double sum = 0.0;
+        for (int x = 0; x < 8; ++x) sum += R3w[x * n + b3];
+        R3w[b3] = sum;  // row 0 of R3w now holds R3 (each b3 written by its own thread)
+    }
+    __syncthreads();
+    const int nred = rec.red_cnt;
+    if (tid == 0) {
+        double gsum = 0.0;
+        for (int b2 = 0; b2 < n; ++b2) gsum += R2[b2];
+        if (nonzero(gsum)) atomicAdd(a.gamma + row, (double)nred * gsum);
+    }
+    const double inv1 = 1.0 / o1;
+    const int64_t ldx = (int64_t)m.n_full * n;
+    for (int i = tid; i < 2 * n * nred; i += blockDim.x) {
+        const int r = i / (2 * n), e = i % (2 * n);
+        const int2 pr = a.red[rec.red_off + r];
+        if (e < n) {
+            const double v = R2[e];
+            if (nonzero(v)) atomicAdd(a.od + row * ldx + (int64_t)pr.x * n + e, 2.0 * v * om2[e] * inv1);
+        } else {
+            const int b3 = e - n;
+            const double v = R3w[b3];
+            if (nonzero(v)) atomicAdd(a.od + row * ldx + (int64_t)pr.y * n + b3, 2.0 * v * om3[b3] * inv1);
+        }
+    }
+}
+
+}  // namespace
+
+int ln_kp(int n) { return ((2 * n + 15) / 16) * 16; }
+
+int ln_kc(int kp) {
+    for (int kc : {64, 48, 32, 16})
+        if (kp % kc == 0) return kc;
+    return 16;
+}
+
+size_t ln_gemm_smem(int kp) {
+    const int kc = ln_kc(kp);
+    const size_t bufs = 2 * 2 * ((size_t)128 * kc * 2 + (size_t)kc * kp * 2);
+    const size_t stage = (size_t)128 * (kp + 1) * sizeof(float);
+    return bufs > stage ? bufs : stage;
+}
+
+cudaError_t launch_ln_bmat(int n, int n_q, const float2 *egvs32, __nv_bfloat16 *bmat, cudaStream_t s) {
+    const int kp = ln_kp(n);
+    const int64_t total = (int64_t)n_q * kp * kp;
+    if (total <= 0) return cudaSuccess;
+    k_build_bmat<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(n, kp, n_q, egvs32, bmat);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ln_batch(const LnBatch &b, cudaStream_t s) {
+    const int n = b.n, kp = ln_kp(n), kc = ln_kc(kp), M = n * n;
+    if (b.nb <= 0) return cudaSuccess;
+    if (kp > 256) return cudaErrorNotSupported;
+    cudaError_t e;
+    {
+        dim3 grid((unsigned)((b.fc.n + 255) / 256), (unsigned)b.nb);
+        k_ln_phases<<<grid, 256, 0, s>>>(b.fc, b.mesh, b.trip, b.nb, b.phase);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    {
+        const int64_t n3 = (int64_t)n * n * n;
+        dim3 grid((unsigned)((n3 + 255) / 256), (unsigned)b.nb);
+        k_ln_pretransform<<<grid, 256, 0, s>>>(n, n / 3, b.fc, b.phase, b.nb, b.plane, b.mp, b.xa_hi, b.xa_lo);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    const size_t smem = ln_gemm_smem(kp);
+    if ((e = cudaFuncSetAttribute(k_ln_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+        return e;
+    LnGemmArgs g;
+    g.plane = b.plane;
+    g.mp = b.mp;
+    g.bmat = b.bmat;
+    g.trip = b.trip;
+    g.irr_full = b.mesh.irr_full;
+    g.n = n;
+    g.kp = kp;
+    g.kc = kc;
+    g.psi = b.psi;
+    g.status = b.status;
+    dim3 grid((unsigned)((M + 127) / 128), (unsigned)b.nb);
+    for (int stage = 1; stage <= 3; ++stage) {
+        const bool from_a = stage != 2;
+        g.stage = stage;
+        g.xhi = from_a ? b.xa_hi : b.xb_hi;
+        g.xlo = from_a ? b.xa_lo : b.xb_lo;
+        g.ohi = from_a ? b.xb_hi : b.xa_hi;
+        g.olo = from_a ? b.xb_lo : b.xa_lo;
+        k_ln_gemm<<<grid, 128, smem, s>>>(g);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    LnDeltaArgs d;
+    d.mesh = b.mesh;
+    d.ph = b.ph;
+    d.rows = b.rows;
+    d.trip = b.trip;
+    d.red = b.red;
+    d.cand_mask = b.cand_mask;
+    d.psi = b.psi;
+    d.n = n;
+    d.gamma = b.gamma;
+    d.od = b.od;
+    const size_t dsm = sizeof(double) * ((size_t)n * 12 + (size_t)n + 8 * (size_t)n);
+    if ((e = cudaFuncSetAttribute(k_ln_delta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm)) != cudaSuccess)
+        return e;
+    k_ln_delta<<<dim3((unsigned)n, (unsigned)b.nb), 256, dsm, s>>>(d);
+    return cudaGetLastError();
+}
+
+}  // namespace tdg

@@ -159,6 +159,10 @@ struct tdg_ctx {
     int32_t last_ntrip = 0;
     bool last_third = false;
     DevBuf<double> d_lam, d_slices, d_mwm_bar;
+    // large-cell path: real-split eigenvector matrices (built once), operand planes, Psi, phases
+    DevBuf<__nv_bfloat16> d_bmat, d_lnx;
+    DevBuf<float2> d_psi, d_lnph;
+    bool bmat_ready = false;
 
     MeshDev mesh() const {
         MeshDev m;
@@ -551,6 +555,9 @@ int validate_opts(const tdg_opts *o) {
     if (o->integrationtype == 1 && !(o->sigma > 0)) return set_error(kErrParam, "sigma must be positive");
     if (o->precision != TDG_PREC_FP64 && o->precision != TDG_PREC_MIXED)
         return set_error(kErrParam, "precision must be TDG_PREC_FP64 or TDG_PREC_MIXED");
+    if (o->tensor_cores != 0 && o->tensor_cores != 1) return set_error(kErrParam, "tensor_cores must be 0 or 1");
+    if (o->tensor_cores == 1 && o->precision != TDG_PREC_MIXED)
+        return set_error(kErrParam, "the tensor-core contraction needs precision TDG_PREC_MIXED");
     return kOk;
 }
 
@@ -607,7 +614,10 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         st = check_list("three-phonon sample", nr, ql->ptr3, ql->list3, N, false);
         if (st) return st;
         if (c->n_fc3 < 1) return set_error(kErrParam, "three-phonon scattering requested without force constants");
-        if (n > 18) return set_error(kErrParam, "this build's fused three-phonon kernel supports up to 6 atoms");
+        if (n > 18 && o->precision != TDG_PREC_MIXED)
+            return set_error(kErrParam, "beyond 18 modes the three-phonon contraction runs on the tensor cores, "
+                                        "which needs precision TDG_PREC_MIXED");
+        if (ln_kp(n) > 256) return set_error(kErrParam, "the tensor-core contraction supports up to 128 modes");
     }
     if (o->fourthorder) {
         st = check_list("four-phonon sample", nr, ql->ptr4, ql->list4a, N);
@@ -1010,8 +1020,60 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         a.gamma = c->d_gamma.p;
         a.od = c->d_xi.p;
         a.status = c->d_status.p;
-        CUDA_TRY(launch_threephonon(a, o->precision, c->n_sm, s));
-        ++launches;
+        if (n > 18 || o->tensor_cores) {
+            // large-cell path: batches of q-triplets through the tcgen05 contraction
+            const int kp = ln_kp(n), mp = ((n * n + 127) / 128) * 128;
+            const int64_t plane = (int64_t)kp * mp;
+            const size_t per_slot = 4 * (size_t)plane * sizeof(__nv_bfloat16) + (size_t)n * n * n * sizeof(float2) +
+                                    (size_t)c->n_fc3 * sizeof(float2);
+            int nbmax = (int)std::max<size_t>(1, std::min<size_t>(256, ((size_t)2 << 30) / per_slot));
+            nbmax = std::max(1, std::min(nbmax, ntrip));
+            if (!c->bmat_ready) {
+                chk(c->d_bmat.alloc((size_t)N * 2 * kp * kp));
+                if (e != cudaSuccess)
+                    return set_error(kErrDevice, std::string("allocation failed: ") + cudaGetErrorString(e));
+                CUDA_TRY(launch_ln_bmat(n, N, c->d_egvs32.p, c->d_bmat.p, s));
+                c->bmat_ready = true;
+            }
+            const __nv_bfloat16 *old = c->d_lnx.p;
+            chk(c->d_lnx.alloc(4 * (size_t)plane * nbmax));
+            chk(c->d_psi.alloc((size_t)nbmax * n * n * n));
+            chk(c->d_lnph.alloc((size_t)nbmax * c->n_fc3));
+            if (e != cudaSuccess) return set_error(kErrDevice, std::string("allocation failed: ") + cudaGetErrorString(e));
+            // padding rows (k >= 2n) of the operand planes must read as zero; no kernel writes them
+            if (c->d_lnx.p != old)
+                CUDA_TRY(cudaMemsetAsync(c->d_lnx.p, 0, sizeof(__nv_bfloat16) * c->d_lnx.n, s));
+            const size_t slots = c->d_lnx.n / (4 * (size_t)plane);
+            LnBatch b;
+            b.mesh = mesh;
+            b.ph = ph;
+            b.rows = rows;
+            b.fc = a.fc;
+            b.red = c->d_red.p;
+            b.cand_mask = c->d_mask.p;
+            b.n = n;
+            b.plane = plane;
+            b.mp = mp;
+            b.xa_hi = c->d_lnx.p;
+            b.xa_lo = b.xa_hi + plane * slots;
+            b.xb_hi = b.xa_lo + plane * slots;
+            b.xb_lo = b.xb_hi + plane * slots;
+            b.bmat = c->d_bmat.p;
+            b.phase = c->d_lnph.p;
+            b.psi = c->d_psi.p;
+            b.gamma = c->d_gamma.p;
+            b.od = c->d_xi.p;
+            b.status = c->d_status.p;
+            for (int t0 = 0; t0 < ntrip; t0 += nbmax) {
+                b.trip = c->d_trip.p + t0;
+                b.nb = std::min(nbmax, ntrip - t0);
+                CUDA_TRY(launch_ln_batch(b, s));
+                launches += 6;
+            }
+        } else {
+            CUDA_TRY(launch_threephonon(a, o->precision, c->n_sm, s));
+            ++launches;
+        }
         CUDA_TRY(cudaEventRecord(ev[3], s));
         CUDA_TRY(launch_sym_distribute(mesh, c->orbits, nr, c->d_row_q1.p, c->d_rbeg.p, c->d_rlen.p, c->d_list3.p,
                                        c->d_xi.p, nullptr, s));

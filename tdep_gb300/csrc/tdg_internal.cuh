@@ -1,6 +1,7 @@
 // Internal device-side declarations shared by the kernels and the C-ABI layer.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -155,6 +156,33 @@ struct FourPhArgs {
 int fourphonon_grid(int n, int precision, int n_sm, int n_quart);
 size_t fourphonon_scratch_bytes(int n, int precision, int grid);
 cudaError_t launch_fourphonon(const FourPhArgs &a, int precision, int grid, cudaStream_t s);
+
+// Large-cell three-phonon path (tcgen05 contraction), one batch of q-triplets.
+struct LnBatch {
+    MeshDev mesh;
+    PhononDev ph;
+    RowsDev rows;
+    Fc3Dev fc;
+    const TripletRec *trip;  // first q-triplet of the batch
+    int nb;                  // q-triplets (slots) in the batch
+    const int2 *red;
+    const uint32_t *cand_mask;
+    int n;
+    int64_t plane;           // elements of one operand plane per slot: ln_kp(n) * mp
+    int mp;                  // M stride: n^2 rounded up to 128
+    __nv_bfloat16 *xa_hi, *xa_lo, *xb_hi, *xb_lo;  // operand planes (hi/lo), zero-initialised
+    const __nv_bfloat16 *bmat;                     // launch_ln_bmat
+    float2 *phase;           // [nb * fc.n]
+    float2 *psi;             // [nb * n^3]
+    double *gamma, *od;
+    int32_t *status;
+};
+int ln_kp(int n);
+int ln_kc(int kp);
+size_t ln_gemm_smem(int kp);
+// Real-split eigenvector matrices of every mesh point: n_q * 2 * ln_kp(n)^2 BF16 (hi, lo).
+cudaError_t launch_ln_bmat(int n, int n_q, const float2 *egvs32, __nv_bfloat16 *bmat, cudaStream_t s);
+cudaError_t launch_ln_batch(const LnBatch &b, cudaStream_t s);
 
 // Isotope scattering (scattering_isotope.f90): adds into gamma and xi.
 cudaError_t launch_isotope(const MeshDev &m, const PhononDev &ph, const RowsDev &rows, const int32_t *row_q1,

@@ -142,6 +142,7 @@ class Options:
     qg4ph: tuple = (-1, -1, -1)
     seed: int = 1
     precision: str = "fp64"  # "fp64" or "mixed"
+    tensor_cores: bool = False  # force the tcgen05 large-cell contraction (automatic beyond 18 modes)
     itertol: float = 1e-5
     itermaxsteps: int = 200
 
@@ -169,6 +170,7 @@ class Options:
         if self.precision not in ("fp64", "mixed"):
             raise ValueError("precision must be 'fp64' or 'mixed'")
         o.precision = N.TDG_PREC_FP64 if self.precision == "fp64" else N.TDG_PREC_MIXED
+        o.tensor_cores = int(bool(self.tensor_cores))
         return o
 
 

@@ -311,3 +311,27 @@ def test_device_exponential_accuracy(built):
     ref = np.array([math.exp(-x) for x in t])
     ulp = np.spacing(ref)
     assert np.max(np.abs(out - ref) / ulp) <= 2.0
+
+
+@pytest.mark.parametrize("name,grid,it", [("rocksalt", (6, 6, 6), 2), ("perovskite", (4, 4, 4), 2),
+                                          ("fcc", (8, 8, 8), 6)])
+def test_tensor_core_contraction_matches_fp64(configs, name, grid, it):
+    """The large-cell path (tcgen05 BF16x3 contraction of n^3 tensors in HBM, batched
+    q-triplets), forced at small n, against the FP64 shared-memory path: the spec bar
+    for mixed precision (kappa within 1e-4)."""
+    prob = Problem.load(configs[name], grid, readiso=True)
+    kw = dict(temperature=300.0, integrationtype=it, isotopescattering=False, seed=21)
+    o64 = Options(**kw)
+    otc = Options(precision="mixed", tensor_cores=True, **kw)
+    lists = QLists.monte_carlo(prob, o64)
+    sr = ScatteringRates(prob)
+    lw64 = sr.generate(o64, lists).copy()
+    n64 = sr.stats["triplets"]
+    _, k64 = sr.kappa(o64)
+    lwtc = sr.generate(otc, lists).copy()
+    assert sr.stats["triplets"] == n64
+    _, ktc = sr.kappa(otc)
+    sr.close()
+    big = lw64 > 1e-3 * lw64.max()
+    assert np.max(np.abs(lwtc[big] / lw64[big] - 1)) < 1e-4
+    np.testing.assert_allclose(ktc, k64, rtol=MIXED_KAPPA_RTOL, atol=MIXED_KAPPA_RTOL * np.abs(k64).max())
