@@ -681,8 +681,10 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     // uploaded once per q1 and the candidates (q1, q2, mask of every row of q1) are formed
     // on the device, in sample order. Otherwise the candidates are, per q1, the union of
     // its rows' samples, with the set of rows that sampled q2 as a bit mask. Masks are
-    // stored once in a table of distinct masks. A sample that repeats a q-point is
-    // rejected: the reference would count that point twice.
+    // stored once in a table of distinct masks. A q-point that a row samples k times (the
+    // reference's sampler only avoids repeating the previous point, so this happens when the
+    // Monte-Carlo grid does not divide the mesh) is counted k times, as the reference does:
+    // the j-th copy of a candidate carries the rows that sampled the point at least j times.
     std::vector<int4> cand;                 // union path
     std::vector<uint32_t> masks;            // distinct row masks (4 words each)
     std::vector<int64_t> rbeg(nr, 0);       // per row: start of its sample in the uploaded list
@@ -726,8 +728,9 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         };
         std::vector<int32_t> stamp(N, -1);
         if (shared) {
-            // one list per q1: offsets first, then range and repeat checks and the copy in
-            // parallel (the other rows' lists are byte-equal to it)
+            // one list per q1: offsets first, then range checks and the copy in parallel (the
+            // other rows' lists are byte-equal to it); a repeated entry becomes a repeated
+            // candidate
             qdesc.assign(nirr, make_int4(0, 0, 0, 0));
             std::vector<int64_t> start(nirr + 1, 0);
             for (int q1 = 0; q1 < nirr; ++q1) {
@@ -752,25 +755,16 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
                 const int L = (int)(start[q1 + 1] - start[q1]);
                 if (L == 0) return;
                 const int32_t *src = ql->list3 + ql->ptr3[qr0[q1]];
-                std::vector<uint32_t> seen(((size_t)N + 31) / 32, 0u);
                 for (int i = 0; i < L; ++i) {
                     const int32_t q2 = src[i];
                     if (q2 < 1 || q2 > N) {
                         bad.store(1);
                         return;
                     }
-                    uint32_t &w = seen[(q2 - 1) >> 5];
-                    const uint32_t bit = 1u << ((q2 - 1) & 31);
-                    if (w & bit) {
-                        bad.store(2);
-                        return;
-                    }
-                    w |= bit;
                     slist[start[q1] + i] = q2;
                 }
             });
             if (bad.load() == 1) return set_error(kErrParam, "three-phonon sample: q' index out of range");
-            if (bad.load() == 2) return set_error(kErrParam, "three-phonon sample repeats a q-point");
             nc64 = start[nirr];
         } else {
             std::atomic<int> bad{0};
@@ -780,29 +774,47 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
             });
             if (bad.load()) return set_error(kErrParam, "three-phonon sample: q' index out of range");
             std::vector<uint32_t> mark((size_t)N * 4, 0u);
-            std::vector<int32_t> touched;
+            std::vector<int32_t> touched, occ(N, 0), row_touched;
+            std::vector<std::array<int, 3>> extra;  // (q2, copy index >= 2, b1)
             for (int q1 = 0; q1 < nirr; ++q1) {
                 int r0, r1;
                 rows_of(q1, r0, r1);
                 touched.clear();
+                extra.clear();
                 for (int r = r0; r < r1; ++r) {
                     const int b1 = rb1[r];
                     rbeg[r] = ql->ptr3[r];
                     rlen[r] = (int32_t)(ql->ptr3[r + 1] - ql->ptr3[r]);
+                    row_touched.clear();
                     for (int64_t i = ql->ptr3[r]; i < ql->ptr3[r + 1]; ++i) {
                         const int q2 = ql->list3[i] - 1;
-                        if (stamp[q2] == r) return set_error(kErrParam, "three-phonon sample repeats a q-point");
+                        if (stamp[q2] == r) {
+                            extra.push_back({q2, ++occ[q2], b1});
+                            continue;
+                        }
                         stamp[q2] = r;
+                        occ[q2] = 1;
+                        row_touched.push_back(q2);
                         uint32_t *mk = &mark[(size_t)q2 * 4];
                         if (!(mk[0] | mk[1] | mk[2] | mk[3])) touched.push_back(q2);
                         mk[b1 >> 5] |= 1u << (b1 & 31);
                     }
+                    for (int q2 : row_touched) occ[q2] = 0;
                 }
                 std::sort(touched.begin(), touched.end());
                 for (int q2 : touched) {
                     uint32_t *mk = &mark[(size_t)q2 * 4];
                     cand.push_back(make_int4(q1, q2, mask_id({mk[0], mk[1], mk[2], mk[3]}), 0));
                     mk[0] = mk[1] = mk[2] = mk[3] = 0u;
+                }
+                std::sort(extra.begin(), extra.end());
+                for (size_t i = 0; i < extra.size();) {
+                    std::array<uint32_t, 4> key = {0u, 0u, 0u, 0u};
+                    size_t j = i;
+                    for (; j < extra.size() && extra[j][0] == extra[i][0] && extra[j][1] == extra[i][1]; ++j)
+                        key[extra[j][2] >> 5] |= 1u << (extra[j][2] & 31);
+                    cand.push_back(make_int4(q1, extra[i][0], mask_id(key), 0));
+                    i = j;
                 }
             }
             nc64 = (int64_t)cand.size();
@@ -814,8 +826,8 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     // ---- four-phonon candidates (scattering_fourphonon.f90:88-99): q2 from list a, q3 from
     // list b, q3 >= q2 and q4 = -q1-q2-q3 >= q3, once per q1 with the rows that sampled the
     // pair as a bit mask. Rows of q1 with identical lists share one pass over the pairs;
-    // otherwise the pairs of all rows are merged by sorting. A list that repeats a q-point
-    // is rejected (the reference would count those pairs twice).
+    // otherwise the pairs of all rows are merged by sorting. A pair that a row forms k times
+    // (repeated points in its lists) is counted k times, as in the reference's double loop.
     std::vector<int4> cand4;
     std::vector<uint32_t> masks4;
     std::vector<int64_t> rbeg4;
@@ -840,7 +852,6 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
             const int k = wrap(-(f1 % G2) - (q2 % G2) - (q3 % G2), G2);
             return (i * G1 + j) * G2 + k;
         };
-        std::vector<int32_t> stamp_a(N, -1), stamp_b(N, -1);
         std::vector<std::pair<int64_t, int>> keys;
         rbeg4.assign(nr, 0);
         rlen4.assign(nr, 0);
@@ -853,13 +864,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
             for (int r = r0; r < r1; ++r) {
                 rbeg4[r] = ql->ptr4[r];
                 rlen4[r] = (int32_t)(ql->ptr4[r + 1] - ql->ptr4[r]);
-                for (int64_t i = ql->ptr4[r]; i < ql->ptr4[r + 1]; ++i) {
-                    const int qa = ql->list4a[i] - 1, qb = ql->list4b[i] - 1;
-                    if (stamp_a[qa] == r || stamp_b[qb] == r)
-                        return set_error(kErrParam, "four-phonon sample repeats a q-point");
-                    stamp_a[qa] = r;
-                    stamp_b[qb] = r;
-                }
+
                 if (r > r0) {
                     const int64_t L = rlen4[r0];
                     same = same && rlen4[r] == L &&
@@ -891,11 +896,26 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
                 }
                 std::sort(keys.begin(), keys.end());
                 for (size_t i = 0; i < keys.size();) {
-                    std::array<uint32_t, 4> key = {0u, 0u, 0u, 0u};
                     size_t j = i;
-                    for (; j < keys.size() && keys[j].first == keys[i].first; ++j)
-                        key[keys[j].second >> 5] |= 1u << (keys[j].second & 31);
-                    cand4.push_back(make_int4(q1, (int)(keys[i].first / N), (int)(keys[i].first % N), mask_id4(key)));
+                    while (j < keys.size() && keys[j].first == keys[i].first) ++j;
+                    // entries i..j-1: the rows (sorted) that formed this pair, a row once per time
+                    // it formed it; copy k goes to the rows with at least k entries
+                    for (int k = 1;; ++k) {
+                        std::array<uint32_t, 4> key = {0u, 0u, 0u, 0u};
+                        bool any = false;
+                        for (size_t x = i; x < j;) {
+                            size_t y = x;
+                            while (y < j && keys[y].second == keys[x].second) ++y;
+                            if ((int)(y - x) >= k) {
+                                key[keys[x].second >> 5] |= 1u << (keys[x].second & 31);
+                                any = true;
+                            }
+                            x = y;
+                        }
+                        if (!any) break;
+                        cand4.push_back(
+                            make_int4(q1, (int)(keys[i].first / N), (int)(keys[i].first % N), mask_id4(key)));
+                    }
                     i = j;
                 }
             }

@@ -316,10 +316,43 @@ def config_perovskite(seed=1, cutoff=6.0):
     return cell, pot, cutoff
 
 
+def supercell(cell: Cell, reps, rng=None, disp=0.0) -> Cell:
+    """reps[0] x reps[1] x reps[2] supercell, atoms grouped by species in first-appearance
+    order, optional Gaussian displacements of standard deviation disp (A)."""
+    reps = np.asarray(reps, int)
+    lat = cell.lattice * reps[:, None]
+    order = []
+    for sp in cell.species:
+        if sp not in order:
+            order.append(sp)
+    frac, species, masses = [], [], []
+    for sp in order:
+        for ijk in itertools.product(*[range(r) for r in reps]):
+            for a in range(cell.na):
+                if cell.species[a] == sp:
+                    frac.append((cell.frac[a] + np.array(ijk)) / reps)
+                    species.append(sp)
+                    masses.append(cell.masses[a])
+    frac = np.array(frac)
+    if disp > 0.0:
+        frac = frac + rng.normal(0.0, disp, frac.shape) @ np.linalg.inv(lat)
+    return Cell(lat, frac, species, np.array(masses))
+
+
+def config_perovskite_supercell(seed=1, reps=(2, 2, 2), disp=0.05, cutoff=5.0):
+    """Supercell of the cubic perovskite (2x2x2: 40 atoms, 120 modes) with seeded Gaussian
+    atomic displacements, so that only the identity survives as a symmetry operation; the
+    pair potentials of config_perovskite, evaluated at the displaced positions."""
+    rng = np.random.default_rng(seed + 1000)
+    base, pot, _ = config_perovskite(seed=seed)
+    return supercell(base, reps, rng, disp), pot, cutoff
+
+
 CONFIGS = {
     "fcc_morse": config_fcc_morse,
     "rocksalt": config_rocksalt,
     "perovskite": config_perovskite,
+    "perovskite_supercell": config_perovskite_supercell,
 }
 
 

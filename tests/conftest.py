@@ -30,6 +30,8 @@ def configs(tmp_path_factory, built):
         "fcc": synth.write_config("fcc_morse", base / "fcc", seed=1),
         "rocksalt": synth.write_config("rocksalt", base / "rocksalt", seed=1),
         "perovskite": synth.write_config("perovskite", base / "perovskite", seed=1),
+        # 10 atoms, 30 modes, no symmetry: the tensor-core path is taken automatically
+        "supercell": synth.write_config("perovskite_supercell", base / "supercell", seed=1, reps=(2, 1, 1)),
     }
 
 

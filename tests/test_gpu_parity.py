@@ -25,24 +25,34 @@ def _require_gpu(built):
 
 def distinct_triplets(prob, lists):
     """Accepted irreducible q-triplets counted once per q1 over the union of its rows' samples
-    (the oracle, like the reference, revisits each of them once per row)."""
+    (the oracle, like the reference, revisits each of them once per row). A q2 that a row
+    samples k times counts k times, as it does in the reference's row loop."""
     total = 0
     for q1 in np.unique(lists.row_q1):
-        rows = np.nonzero(lists.row_q1 == q1)[0]
-        union = np.unique(np.concatenate([lists.list3[lists.ptr3[r]:lists.ptr3[r + 1]] for r in rows]))
-        total += len(orc.triplets(prob, int(q1), union.astype(np.int32)))
+        mult = {}
+        for r in np.nonzero(lists.row_q1 == q1)[0]:
+            vals, counts = np.unique(lists.list3[lists.ptr3[r]:lists.ptr3[r + 1]], return_counts=True)
+            for v, c in zip(vals.tolist(), counts.tolist()):
+                mult[v] = max(mult.get(v, 0), c)
+        union = np.array(sorted(mult), dtype=np.int32)
+        total += sum(mult[q2] for q2, _, _ in orc.triplets(prob, int(q1), union))
     return total
 
 
 def distinct_quartets(prob, lists):
-    """Accepted irreducible q-quartets counted once per q1 over all its rows' pair samples."""
+    """Accepted irreducible q-quartets counted once per q1 over all its rows' pair samples; a
+    pair that a row forms k times counts k times."""
     total = 0
     for q1 in np.unique(lists.row_q1):
-        seen = set()
+        mult = {}
         for r in np.nonzero(lists.row_q1 == q1)[0]:
             a, b = lists.ptr4[r], lists.ptr4[r + 1]
-            seen.update((q2, q3, q4) for q2, q3, q4, _ in orc.quartets(prob, int(q1), lists.list4a[a:b], lists.list4b[a:b]))
-        total += len(seen)
+            cnt = {}
+            for q2, q3, q4, _ in orc.quartets(prob, int(q1), lists.list4a[a:b], lists.list4b[a:b]):
+                cnt[(q2, q3, q4)] = cnt.get((q2, q3, q4), 0) + 1
+            for k, c in cnt.items():
+                mult[k] = max(mult.get(k, 0), c)
+        total += sum(mult.values())
     return total
 
 
@@ -164,6 +174,18 @@ def test_fp64_monte_carlo_rows_differ(configs):
     _compare(prob, opts, lists)
 
 
+def test_fp64_monte_carlo_grid_not_dividing_the_mesh(configs):
+    """-qg3ph 5 5 5 on a 6x6x6 mesh: the reference's sampler only avoids repeating the
+    previous point, so rows sample some q-points twice and count them twice."""
+    prob = Problem.load(configs["rocksalt"], (6, 6, 6), readiso=True)
+    opts = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=8, qg3ph=(5, 5, 5))
+    lists = QLists.monte_carlo(prob, opts)
+    r = 0
+    assert any(np.unique(lists.list3[lists.ptr3[r]:lists.ptr3[r + 1]]).size < lists.ptr3[r + 1] - lists.ptr3[r]
+               for r in range(lists.n_row))
+    _compare(prob, opts, lists)
+
+
 def test_fp64_classical_uneven_per_q1_samples(configs):
     prob = Problem.load(configs["perovskite"], (4, 4, 4), readiso=True)
     rng = np.random.default_rng(17)
@@ -207,6 +229,14 @@ def test_fp64_four_phonon_only_fcc_monte_carlo(configs4):
     prob = Problem.load(configs4["fcc"], (8, 8, 8), fourthorder=True, readiso=True)
     opts = Options(temperature=300.0, integrationtype=2, thirdorder=False, isotopescattering=False, seed=3,
                    fourthorder=True, qg4ph=(4, 4, 4))
+    _compare(prob, opts, QLists.monte_carlo(prob, opts))
+
+
+def test_fp64_four_phonon_grid_not_dividing_the_mesh(configs4):
+    """-qg4ph 4 4 4 on a 6x6x6 mesh: repeated points in the pair lists count once per pair."""
+    prob = Problem.load(configs4["rocksalt"], (6, 6, 6), fourthorder=True, readiso=True)
+    opts = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=9, fourthorder=True,
+                   qg4ph=(4, 4, 4), qg3ph=(4, 4, 4))
     _compare(prob, opts, QLists.monte_carlo(prob, opts))
 
 
@@ -335,3 +365,37 @@ def test_tensor_core_contraction_matches_fp64(configs, name, grid, it):
     big = lw64 > 1e-3 * lw64.max()
     assert np.max(np.abs(lwtc[big] / lw64[big] - 1)) < 1e-4
     np.testing.assert_allclose(ktc, k64, rtol=MIXED_KAPPA_RTOL, atol=MIXED_KAPPA_RTOL * np.abs(k64).max())
+
+
+def test_large_cell_tensor_core_path_matches_oracle(configs):
+    """A displaced 2x1x1 perovskite supercell (30 modes, identity only): beyond 18 modes the
+    contraction runs on the tensor cores in mixed precision; against the oracle's FP64
+    restatement at the mixed-precision bar."""
+    prob = Problem.load(configs["supercell"], (3, 3, 3), readiso=True)
+    assert prob.n_mode == 30 and prob.n_op == 1
+    opts = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=6, precision="mixed",
+                   qg3ph=(2, 2, 2))
+    lists = QLists.monte_carlo(prob, opts)
+    sr = ScatteringRates(prob)
+    lw = sr.generate(opts, lists)
+    ks, ki = sr.kappa(opts)
+    trip = sr.stats["triplets"]
+    sr.close()
+    ref = orc.full_run(prob, opts, lists)
+    assert trip == distinct_triplets(prob, lists)
+    big = ref["linewidth"] > 1e-3 * ref["linewidth"].max()
+    assert np.max(np.abs(lw[big] / ref["linewidth"][big] - 1)) < 1e-4
+    np.testing.assert_allclose(ks, ref["kappa_sma"], rtol=MIXED_KAPPA_RTOL, atol=MIXED_KAPPA_RTOL * np.abs(ks).max())
+    np.testing.assert_allclose(ki, ref["kappa_iter"], rtol=MIXED_KAPPA_RTOL, atol=MIXED_KAPPA_RTOL * np.abs(ki).max())
+
+
+def test_large_cell_needs_mixed_precision(configs):
+    from tdep_gb300._native import TdgError
+
+    prob = Problem.load(configs["supercell"], (3, 3, 3), readiso=True)
+    opts = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=6, precision="fp64")
+    sr = ScatteringRates(prob)
+    with pytest.raises(TdgError) as e:
+        sr.generate(opts, QLists.monte_carlo(prob, opts))
+    assert e.value.code == 5
+    sr.close()
