@@ -255,7 +255,15 @@ __global__ void __launch_bounds__(128, 1) k_ln_gemm(LnGemmArgs g) {
     }
 }
 
-// ---- delta weights and accumulation: one CTA per (slot, b1), 8 warps over b2, lanes over b3 ----
+// ---- delta weights and accumulation: one CTA per (slot, b1) ----
+// GB300's FP64 pipe is 1/64 of FP32, and only a fraction of the n^2 mode pairs (b2, b3) has a
+// Gaussian inside its 8-sigma window. In blocks of kLnBB rows b2: (A) every pair is screened
+// in FP32 (window with a margin far above FP32 rounding, degeneracy skips pre-checked in
+// FP32), the survivors are compacted into a queue with a block scan; (B) full warps evaluate
+// the queue with the reference's FP64 window test, weights and occupations into a dense F;
+// (C) R2[b2] = sum_b3 F and R3[b3] += sum_b2 F.
+constexpr int kLnBB = 32;
+
 struct LnDeltaArgs {
     MeshDev mesh;
     PhononDev ph;
@@ -268,11 +276,16 @@ struct LnDeltaArgs {
     double *gamma, *od;
 };
 
+__host__ __device__ inline size_t ln_delta_smem(int n) {
+    return sizeof(double) * ((size_t)14 * n + (size_t)kLnBB * n) + sizeof(uint32_t) * (size_t)kLnBB * n +
+           sizeof(int) * 33 + 16;
+}
+
 __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
     extern __shared__ __align__(16) unsigned char sm[];
     const int n = a.n;
     const int s = blockIdx.y, b1 = blockIdx.x;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tid = threadIdx.x, bd = blockDim.x;
     const TripletRec rec = a.trip[s];
     const MeshDev &m = a.mesh;
     const PhononDev &P = a.ph;
@@ -283,8 +296,10 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
     const int f1 = m.irr_full[rec.q1], q2 = rec.q2, q3 = rec.q3;
     const int i2 = m.full_irr[q2], i3 = m.full_irr[q3];
     double *om2 = (double *)sm, *om3 = om2 + n, *be2 = om3 + n, *be3 = be2 + n, *s2 = be3 + n, *s3 = s2 + n;
-    double *v2 = s3 + n, *v3 = v2 + 3 * n, *R2 = v3 + 3 * n, *R3w = R2 + n;  // R3w[8][n]
-    for (int b = tid; b < n; b += blockDim.x) {
+    double *v2 = s3 + n, *v3 = v2 + 3 * n, *R2 = v3 + 3 * n, *R3 = R2 + n, *F = R3 + n;
+    uint32_t *Q = (uint32_t *)(F + (size_t)kLnBB * n);
+    int *wsum = (int *)(Q + (size_t)kLnBB * n);
+    for (int b = tid; b < n; b += bd) {
         om2[b] = P.omega[(size_t)q2 * n + b];
         om3[b] = P.omega[(size_t)q3 * n + b];
         be2[b] = P.be[(size_t)i2 * n + b];
@@ -295,6 +310,7 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
             v2[b * 3 + d] = P.vel[((size_t)q2 * n + b) * 3 + d];
             v3[b * 3 + d] = P.vel[((size_t)q3 * n + b) * 3 + d];
         }
+        R3[b] = 0.0;
     }
     __syncthreads();
     const double o1 = P.omega[(size_t)f1 * n + b1];
@@ -306,26 +322,49 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
     const int it = P.integrationtype;
     const float fo1 = (float)o1, fs1 = (float)s1;
     const float2 *psi = a.psi + ((int64_t)s * n + b1) * n * n;
-    double r3[4] = {0.0, 0.0, 0.0, 0.0};  // lanes own b3 = lane + 32 j, n <= 128
-    for (int b2 = warp; b2 < n; b2 += 8) {
-        const double o2 = om2[b2];
-        const bool skip2 = o2 < kFreqTolD || fabs(o1 - o2) < kFreqTolD;
-        double r2 = 0.0;
-        for (int j = 0; j < 4; ++j) {
-            const int b3 = lane + 32 * j;
-            if (b3 >= n || skip2) continue;
-            const double o3 = om3[b3];
-            if (o3 < kFreqTolD || fabs(o1 - o3) < kFreqTolD || fabs(o2 - o3) < kFreqTolD) continue;
-            // FP32 screen of the four Gaussians, margin as in the shared-memory kernel
-            uint32_t live = 15u;
-            if (it != 6) {
-                const float f2 = (float)o2, f3 = (float)o3;
-                const float sg = it == 1 ? (float)P.sigma_fixed : sqrtf(fs1 + (float)s2[b2] + (float)s3[b3]);
-                const float win = 8.0f * sg * 1.001f + 1e-6f * (fo1 + f2 + f3);
-                live = (fabsf(fo1 + f2 - f3) <= win ? 1u : 0u) | (fabsf(fo1 - f2 + f3) <= win ? 2u : 0u) |
-                       (fabsf(fo1 - f2 - f3) <= win ? 4u : 0u) | (fo1 + f2 + f3 <= win ? 8u : 0u);
-            }
-            if (!live) continue;
+    // 4-bit live mask of the Gaussians of pair (b2, b3), 0 when a skip rule applies
+    // (scattering_threephonon.f90:90-101) or no Gaussian can reach its window
+    auto screen = [&](int b2, int b3) -> uint32_t {
+        const double o2 = om2[b2], o3 = om3[b3];
+        const float f2 = (float)o2, f3 = (float)o3;
+        // |x - y| < 1e-9 in FP64 needs |fx - fy| below 1e-8 in FP32 at these magnitudes
+        if (o2 < kFreqTolD || o3 < kFreqTolD) return 0u;
+        if (fabsf(fo1 - f2) < 1e-8f && fabs(o1 - o2) < kFreqTolD) return 0u;
+        if (fabsf(fo1 - f3) < 1e-8f && fabs(o1 - o3) < kFreqTolD) return 0u;
+        if (fabsf(f2 - f3) < 1e-8f && fabs(o2 - o3) < kFreqTolD) return 0u;
+        if (it == 6) return 15u;  // the velocity-difference width can cancel in FP32: not screened
+        const float sg = it == 1 ? (float)P.sigma_fixed : sqrtf(fs1 + (float)s2[b2] + (float)s3[b3]);
+        const float win = 8.0f * sg * 1.001f + 1e-6f * (fo1 + f2 + f3);
+        return (fabsf(fo1 + f2 - f3) <= win ? 1u : 0u) | (fabsf(fo1 - f2 + f3) <= win ? 2u : 0u) |
+               (fabsf(fo1 - f2 - f3) <= win ? 4u : 0u) | (fo1 + f2 + f3 <= win ? 8u : 0u);
+    };
+    for (int bb = 0; bb < n; bb += kLnBB) {
+        const int nbb = min(kLnBB, n - bb), cnt = nbb * n;
+        // (A) contiguous chunk per thread (at most 16 entries: kLnBB * 128 / 256)
+        const int per = (cnt + bd - 1) / bd;
+        const int e0 = min(cnt, tid * per), e1 = min(cnt, e0 + per);
+        uint64_t lives = 0;
+        int ns = 0;
+        for (int e = e0; e < e1; ++e) {
+            const uint32_t l = screen(bb + e / n, e % n);
+            lives |= (uint64_t)l << (4 * (e - e0));
+            ns += l != 0u;
+        }
+        for (int e = tid; e < cnt; e += bd) F[e] = 0.0;
+        int total = 0;
+        int k = block_exclusive_scan(ns, wsum, total);  // contains __syncthreads
+        for (int e = e0; e < e1; ++e) {
+            const uint32_t l = (uint32_t)(lives >> (4 * (e - e0))) & 15u;
+            if (l) Q[k++] = (uint32_t)e | (l << 16);
+        }
+        __syncthreads();
+        // (B) FP64 delta weights and occupations of the survivors, full warps
+        for (int i = tid; i < total; i += bd) {
+            const uint32_t qv = Q[i];
+            const int e = (int)(qv & 0xffffu);
+            const uint32_t live = qv >> 16;
+            const int b2 = bb + e / n, b3 = e % n;
+            const double o2 = om2[b2], o3 = om3[b3];
             double sigma;
             if (it == 1) {
                 sigma = P.sigma_fixed;
@@ -350,24 +389,28 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
             const double cr = ps.x, ci = ps.y;
             const double psisq = kLnPrefactor * (cr * cr + ci * ci) * w;
             const double n2 = be2[b2], n3 = be3[b3];
-            const double f = perm * psisq * (n2 - n3) * d0 + perm * psisq * (n2 + n3 + 1.0) * d1;
-            r2 += f;
-            r3[j] += f;
+            F[e] = perm * psisq * (n2 - n3) * d0 + perm * psisq * (n2 + n3 + 1.0) * d1;
         }
-        for (int o = 16; o > 0; o >>= 1) r2 += __shfl_down_sync(0xffffffffu, r2, o);
-        if (lane == 0) R2[b2] = r2;
+        __syncthreads();
+        // (C) row sums of the block and running column sums
+        for (int r = tid; r < nbb; r += bd) {
+            double sum = 0.0;
+            for (int b3 = 0; b3 < n; ++b3) {
+                const double f = F[r * n + b3];
+                if (nonzero(f)) sum += f;
+            }
+            R2[bb + r] = sum;
+        }
+        for (int b3 = tid; b3 < n; b3 += bd) {
+            double sum = R3[b3];
+            for (int r = 0; r < nbb; ++r) {
+                const double f = F[r * n + b3];
+                if (nonzero(f)) sum += f;
+            }
+            R3[b3] = sum;
+        }
+        __syncthreads();
     }
-    for (int j = 0; j < 4; ++j) {
-        const int b3 = lane + 32 * j;
-        if (b3 < n) R3w[warp * n + b3] = r3[j];
-    }
-    __syncthreads();
-    for (int b3 = tid; b3 < n; b3 += blockDim.x) {
-        double sum = 0.0;
-        for (int x = 0; x < 8; ++x) sum += R3w[x * n + b3];
-        R3w[b3] = sum;  // row 0 of R3w now holds R3 (each b3 written by its own thread)
-    }
-    __syncthreads();
     const int nred = rec.red_cnt;
     if (tid == 0) {
         double gsum = 0.0;
@@ -376,7 +419,7 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
     }
     const double inv1 = 1.0 / o1;
     const int64_t ldx = (int64_t)m.n_full * n;
-    for (int i = tid; i < 2 * n * nred; i += blockDim.x) {
+    for (int i = tid; i < 2 * n * nred; i += bd) {
         const int r = i / (2 * n), e = i % (2 * n);
         const int2 pr = a.red[rec.red_off + r];
         if (e < n) {
@@ -384,7 +427,7 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
             if (nonzero(v)) atomicAdd(a.od + row * ldx + (int64_t)pr.x * n + e, 2.0 * v * om2[e] * inv1);
         } else {
             const int b3 = e - n;
-            const double v = R3w[b3];
+            const double v = R3[b3];
             if (nonzero(v)) atomicAdd(a.od + row * ldx + (int64_t)pr.y * n + b3, 2.0 * v * om3[b3] * inv1);
         }
     }
@@ -467,7 +510,7 @@ cudaError_t launch_ln_batch(const LnBatch &b, cudaStream_t s) {
     d.n = n;
     d.gamma = b.gamma;
     d.od = b.od;
-    const size_t dsm = sizeof(double) * ((size_t)n * 12 + (size_t)n + 8 * (size_t)n);
+    const size_t dsm = ln_delta_smem(n);
     if ((e = cudaFuncSetAttribute(k_ln_delta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm)) != cudaSuccess)
         return e;
     k_ln_delta<<<dim3((unsigned)n, (unsigned)b.nb), 256, dsm, s>>>(d);

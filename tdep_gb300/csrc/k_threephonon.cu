@@ -112,30 +112,6 @@ __device__ __forceinline__ C phase3(const Fc3Dev &fc, const MeshDev &m, const in
     return twiddle_at<C>(fc, K % m.L);
 }
 
-// Exclusive scan of one int per thread over the block (blockDim a multiple of 32).
-__device__ __forceinline__ int block_exclusive_scan(int v, int *wsum, int &total) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    int x = v;
-    for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) wsum[w] = x;
-    __syncthreads();
-    if (w == 0) {
-        int s = lane < nw ? wsum[lane] : 0;
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, s, o);
-            if (lane >= o) s += y;
-        }
-        if (lane < nw) wsum[lane] = s;
-    }
-    __syncthreads();
-    total = wsum[nw - 1];
-    const int res = (w > 0 ? wsum[w - 1] : 0) + x - v;
-    __syncthreads();
-    return res;
-}
 
 // Shared-memory layout (bytes) for mode count n and complex size cs.
 struct Layout {
