@@ -117,25 +117,40 @@ struct LnGemmArgs {
     const TripletRec *trip;          // the batch's q-triplets (slot order)
     const int32_t *irr_full;         // 0-based full index of irreducible q1
     int stage;                       // 1, 2, 3: contract with E(q1), E(q2), E(q3)
-    int n, kp, kc;                   // modes, padded 2n (multiple of 16), K chunk
+    int n, kp;                       // modes, padded 2n (multiple of 16)
     __nv_bfloat16 *ohi, *olo;        // stages 1-2: next operand planes
     float2 *psi;                     // stage 3: [slot][n^3]
     int32_t *status;
 };
 
-// Tile = 128 rows of M = n^2 for one slot, all kp columns. Two shared-memory buffers hold
-// K chunks of both operands (hi and lo); chunk c+1 streams in with cp.async while the MMAs
-// of chunk c run; each buffer's MMAs arrive on its own mbarrier before it is refilled.
-__global__ void __launch_bounds__(128, 1) k_ln_gemm(LnGemmArgs g) {
+// Tile = 128 rows of M = n^2 for one slot, all kp columns. kLnStages shared-memory stages
+// hold K chunks of 16 of both operands (hi and lo); cp.async keeps kLnStages - 1 chunks in
+// flight ahead of the MMAs, and a stage is refilled only after the MMAs that read it have
+// arrived on its mbarrier. The epilogue reads tensor memory straight into registers: warps
+// w and w + 4 share TMEM lane group w and split the columns.
+constexpr int kLnStages = 4;
+constexpr int kLnThreads = 256;
+
+__device__ __forceinline__ uint4 pack8(const unsigned short (&h)[8]) {
+    uint4 r;
+    r.x = (uint32_t)h[0] | ((uint32_t)h[1] << 16);
+    r.y = (uint32_t)h[2] | ((uint32_t)h[3] << 16);
+    r.z = (uint32_t)h[4] | ((uint32_t)h[5] << 16);
+    r.w = (uint32_t)h[6] | ((uint32_t)h[7] << 16);
+    return r;
+}
+
+__global__ void __launch_bounds__(kLnThreads, 1) k_ln_gemm(LnGemmArgs g) {
     extern __shared__ __align__(1024) unsigned char sm[];
-    __shared__ uint64_t mbar[2];
+    __shared__ uint64_t mbar[kLnStages];
     __shared__ uint32_t tbase;
+    constexpr int S = kLnStages;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int s = blockIdx.y, m0 = blockIdx.x * 128;
-    const int n = g.n, kp = g.kp, kc = g.kc, M = n * n;
-    const int nch = kp / kc;
-    const uint32_t a_bytes = 128u * kc * 2u, b_bytes = (uint32_t)kc * kp * 2u;
-    const uint32_t buf_bytes = 2u * (a_bytes + b_bytes);
+    const int n = g.n, kp = g.kp, M = n * n;
+    const int nch = kp / 16;
+    const uint32_t a_bytes = 128u * 16u * 2u, b_bytes = 16u * (uint32_t)kp * 2u;
+    const uint32_t stage_bytes = 2u * (a_bytes + b_bytes);
     const uint32_t a_ck = 16u * 128u, b_ck = 16u * (uint32_t)kp;  // K-direction core strides
     const uint32_t ncols = kp <= 32 ? 32u : (kp <= 64 ? 64u : (kp <= 128 ? 128u : 256u));
     const TripletRec rec = g.trip[s];
@@ -146,113 +161,119 @@ __global__ void __launch_bounds__(128, 1) k_ln_gemm(LnGemmArgs g) {
 
     if (warp == 0) tc::tmem_alloc(&tbase, ncols);
     if (tid == 0) {
-        tc::mbar_init(&mbar[0], 1);
-        tc::mbar_init(&mbar[1], 1);
+        for (int i = 0; i < S; ++i) tc::mbar_init(&mbar[i], 1);
         tc::fence_mbar_init();
     }
-    auto load_chunk = [&](int c, int buf) {
-        unsigned char *base = sm + buf * buf_bytes;
-        const int k0 = c * kc;
-        // A: 2 planes x kc rows x 16 segments of 8 m
-        for (int i = tid; i < 2 * kc * 16; i += 128) {
-            const int h = i / (kc * 16), r = i % (kc * 16), k = r / 16, mb = r % 16;
-            const uint32_t dst = tc::smem_u32(base + h * a_bytes + mb * 128 + (k >> 3) * a_ck + (k & 7) * 16);
-            cp_async16(dst, xsrc[h] + (int64_t)(k0 + k) * g.mp + m0 + 8 * mb);
-        }
-        // B: 2 planes x kc rows x kp/8 segments
-        const int nbs = kp / 8;
-        for (int i = tid; i < 2 * kc * nbs; i += 128) {
-            const int h = i / (kc * nbs), r = i % (kc * nbs), k = r / nbs, nb = r % nbs;
-            const uint32_t dst =
-                tc::smem_u32(base + 2 * a_bytes + h * b_bytes + nb * 128 + (k >> 3) * b_ck + (k & 7) * 16);
-            cp_async16(dst, bsrc[h] + (int64_t)(k0 + k) * kp + 8 * nb);
+    // one cp.async group per chunk (an empty group past the end keeps the count uniform)
+    auto load_chunk = [&](int c) {
+        if (c < nch) {
+            unsigned char *base = sm + (c % S) * stage_bytes;
+            const int k0 = c * 16;
+            for (int i = tid; i < 2 * 16 * 16; i += kLnThreads) {  // A: 2 planes x 16 k x 16 m-blocks
+                const int h = i >> 8, k = (i >> 4) & 15, mb = i & 15;
+                const uint32_t dst = tc::smem_u32(base + h * a_bytes + mb * 128 + (k >> 3) * a_ck + (k & 7) * 16);
+                cp_async16(dst, xsrc[h] + (int64_t)(k0 + k) * g.mp + m0 + 8 * mb);
+            }
+            const int nbs = kp / 8;
+            for (int i = tid; i < 2 * 16 * nbs; i += kLnThreads) {  // B: 2 planes x 16 k x kp/8 blocks
+                const int h = i / (16 * nbs), r = i % (16 * nbs), k = r / nbs, nb = r % nbs;
+                const uint32_t dst =
+                    tc::smem_u32(base + 2 * a_bytes + h * b_bytes + nb * 128 + (k >> 3) * b_ck + (k & 7) * 16);
+                cp_async16(dst, bsrc[h] + (int64_t)(k0 + k) * kp + 8 * nb);
+            }
         }
         cp_async_commit();
     };
-    load_chunk(0, 0);
+    for (int c = 0; c < S - 1; ++c) load_chunk(c);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t taddr = tbase;
     const uint32_t idesc = tc::idesc_bf16_f32(128, kp, true, true);
-    // every wait ends within kLnWaitCycles; the outcome is made uniform across the CTA before
-    // any thread acts on it, so that no barrier is skipped by part of the block
+    // every wait ends within kLnWaitCycles; its outcome is made uniform across the CTA
+    // before any thread acts on it, so that no barrier is skipped by part of the block
     bool ok = true;
     for (int c = 0; c < nch; ++c) {
-        const int buf = c & 1;
-        if (c + 1 < nch) {
-            bool w = true;
-            if (c >= 1) w = tc::mbar_wait(&mbar[buf ^ 1], ((c - 1) >> 1) & 1, kLnWaitCycles);
+        const int pf = c + S - 1;  // refills the stage chunk c - 1 used
+        if (pf < nch && c >= 1) {
+            const bool w = tc::mbar_wait(&mbar[(c - 1) % S], ((c - 1) / S) & 1, kLnWaitCycles);
             ok = __syncthreads_and(w ? 1 : 0) != 0;
             if (!ok) break;
-            load_chunk(c + 1, buf ^ 1);
-            cp_async_wait<1>();
-        } else {
-            cp_async_wait<0>();
         }
+        load_chunk(pf);
+        cp_async_wait<S - 1>();  // chunk c has landed
         tc::fence_async_smem();
         __syncthreads();
         if (tid == 0) {
             tc::fence_after_sync();
-            unsigned char *base = sm + buf * buf_bytes;
+            unsigned char *base = sm + (c % S) * stage_bytes;
             const uint32_t ah = tc::smem_u32(base), al = tc::smem_u32(base + a_bytes);
             const uint32_t bh = tc::smem_u32(base + 2 * a_bytes), bl = tc::smem_u32(base + 2 * a_bytes + b_bytes);
-            for (int k16 = 0; k16 < kc / 16; ++k16) {
-                const uint32_t ao = k16 * 2 * a_ck, bo = k16 * 2 * b_ck;
-                const uint64_t dah = tc::smem_desc(ah + ao, a_ck, 128), dal = tc::smem_desc(al + ao, a_ck, 128);
-                const uint64_t dbh = tc::smem_desc(bh + bo, b_ck, 128), dbl = tc::smem_desc(bl + bo, b_ck, 128);
-                const uint32_t acc0 = (c > 0 || k16 > 0) ? 1u : 0u;
-                tc::mma_bf16(taddr, dah, dbh, idesc, acc0);
-                tc::mma_bf16(taddr, dah, dbl, idesc, 1u);
-                tc::mma_bf16(taddr, dal, dbh, idesc, 1u);
-            }
-            tc::mma_commit(&mbar[buf]);
+            const uint64_t dah = tc::smem_desc(ah, a_ck, 128), dal = tc::smem_desc(al, a_ck, 128);
+            const uint64_t dbh = tc::smem_desc(bh, b_ck, 128), dbl = tc::smem_desc(bl, b_ck, 128);
+            tc::mma_bf16(taddr, dah, dbh, idesc, c > 0 ? 1u : 0u);
+            tc::mma_bf16(taddr, dah, dbl, idesc, 1u);
+            tc::mma_bf16(taddr, dal, dbh, idesc, 1u);
+            tc::mma_commit(&mbar[c % S]);
         }
     }
     if (ok) {
-        const bool w = tc::mbar_wait(&mbar[(nch - 1) & 1], ((nch - 1) >> 1) & 1, kLnWaitCycles);
+        const bool w = tc::mbar_wait(&mbar[(nch - 1) % S], ((nch - 1) / S) & 1, kLnWaitCycles);
         ok = __syncthreads_and(w ? 1 : 0) != 0;
     }
     cp_async_wait<0>();
     if (!ok) {
         if (tid == 0) atomicExch(g.status, kDevOverflow);
         // let whatever was issued drain before the tensor memory goes back
-        tc::mbar_wait(&mbar[(nch - 1) & 1], ((nch - 1) >> 1) & 1, kLnWaitCycles);
+        tc::mbar_wait(&mbar[(nch - 1) % S], ((nch - 1) / S) & 1, kLnWaitCycles);
     }
     __syncthreads();
     tc::fence_after_sync();
-    // ---- epilogue: tensor memory -> shared staging (row stride kp + 1) -> global ----
-    float *stage = (float *)sm;
-    const int ld = kp + 1;
-    if (ok) {
-        for (int c0 = 0; c0 < kp; c0 += 8) {
-            float v[8];
-            tc::tmem_ld8(taddr + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
+    // ---- epilogue ----
+    const int lg = warp & 3, half = warp >> 2;
+    const int ml = 32 * lg + lane, m = m0 + ml;
+    const uint32_t trow = taddr + ((uint32_t)(32 * lg) << 16);
+    if (ok && g.stage < 3) {
+        // D[m = u*n + v][ri*n + w] -> X'[(ri*n + u)*mp + v*n + w]
+        __nv_bfloat16 *hi = g.ohi + (int64_t)s * g.plane, *lo = g.olo + (int64_t)s * g.plane;
+        const int u = m / n, v = m % n;
+        const int c_lo = half * (kp / 2), c_hi = c_lo + kp / 2;
+        for (int c0 = c_lo; c0 < c_hi; c0 += 8) {
+            float x[8];
+            tc::tmem_ld8(trow + (uint32_t)c0, x);
+            if (m >= M) continue;
+            if (n % 8 == 0 && c0 + 8 <= 2 * n) {
+                const int ri = c0 / n, w0 = c0 % n;
+                unsigned short h[8], l[8];
 #pragma unroll
-            for (int i = 0; i < 8; ++i) stage[(32 * warp + lane) * ld + c0 + i] = v[i];
+                for (int i = 0; i < 8; ++i) tc::split_bf16(x[i], h[i], l[i]);
+                const int64_t o = (int64_t)(ri * n + u) * g.mp + v * n + w0;
+                *reinterpret_cast<uint4 *>(hi + o) = pack8(h);
+                *reinterpret_cast<uint4 *>(lo + o) = pack8(l);
+            } else {
+                for (int i = 0; i < 8; ++i) {
+                    const int c = c0 + i;
+                    if (c >= 2 * n) break;
+                    store_split(hi, lo, (int64_t)((c / n) * n + u) * g.mp + v * n + c % n, x[i]);
+                }
+            }
+        }
+    } else if (ok) {
+        // Psi[m][w] = (D[m][w], D[m][n + w]); the two halves take the w ranges
+        float2 *out = g.psi + (int64_t)s * M * n;
+        const int wh = ((n + 15) / 16) * 8;  // w range of half 0, a multiple of 8
+        const int w_lo = half * wh, w_hi = min(n, w_lo + wh);
+        for (int w0 = w_lo; w0 < w_hi; w0 += 8) {
+            float re[8], im[8];
+            tc::tmem_ld8(trow + (uint32_t)w0, re);
+            tc::tmem_ld8(trow + (uint32_t)(n + w0), im);
+            if (m >= M) continue;
+            for (int i = 0; i < 8 && w0 + i < w_hi; ++i) out[(int64_t)m * n + w0 + i] = make_float2(re[i], im[i]);
         }
     }
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(taddr, ncols);
-    if (!ok) return;
-    const int rows = min(128, M - m0);
-    if (g.stage < 3) {
-        // D[m = u*n + v][ri*n + w] -> X'[(ri*n + u)*mp + v*n + w]
-        __nv_bfloat16 *hi = g.ohi + (int64_t)s * g.plane, *lo = g.olo + (int64_t)s * g.plane;
-        const int per = 2 * n;
-        for (int i = tid; i < rows * per; i += 128) {
-            const int ml = i / per, r = i % per, ri = r / n, w = r % n;
-            const int m = m0 + ml, u = m / n, v = m % n;
-            store_split(hi, lo, (int64_t)(ri * n + u) * g.mp + v * n + w, stage[ml * ld + r]);
-        }
-    } else {
-        float2 *out = g.psi + (int64_t)s * M * n;
-        for (int i = tid; i < rows * n; i += 128) {
-            const int ml = i / n, w = i % n;
-            out[(int64_t)(m0 + ml) * n + w] = make_float2(stage[ml * ld + w], stage[ml * ld + n + w]);
-        }
-    }
 }
 
 // ---- delta weights and accumulation: one CTA per (slot, b1) ----
@@ -437,18 +458,7 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
 
 int ln_kp(int n) { return ((2 * n + 15) / 16) * 16; }
 
-int ln_kc(int kp) {
-    for (int kc : {64, 48, 32, 16})
-        if (kp % kc == 0) return kc;
-    return 16;
-}
-
-size_t ln_gemm_smem(int kp) {
-    const int kc = ln_kc(kp);
-    const size_t bufs = 2 * 2 * ((size_t)128 * kc * 2 + (size_t)kc * kp * 2);
-    const size_t stage = (size_t)128 * (kp + 1) * sizeof(float);
-    return bufs > stage ? bufs : stage;
-}
+size_t ln_gemm_smem(int kp) { return (size_t)kLnStages * 2 * ((size_t)128 * 16 * 2 + (size_t)16 * kp * 2); }
 
 cudaError_t launch_ln_bmat(int n, int n_q, const float2 *egvs32, __nv_bfloat16 *bmat, cudaStream_t s) {
     const int kp = ln_kp(n);
@@ -459,7 +469,7 @@ cudaError_t launch_ln_bmat(int n, int n_q, const float2 *egvs32, __nv_bfloat16 *
 }
 
 cudaError_t launch_ln_batch(const LnBatch &b, cudaStream_t s) {
-    const int n = b.n, kp = ln_kp(n), kc = ln_kc(kp), M = n * n;
+    const int n = b.n, kp = ln_kp(n), M = n * n;
     if (b.nb <= 0) return cudaSuccess;
     if (kp > 256) return cudaErrorNotSupported;
     cudaError_t e;
@@ -485,7 +495,6 @@ cudaError_t launch_ln_batch(const LnBatch &b, cudaStream_t s) {
     g.irr_full = b.mesh.irr_full;
     g.n = n;
     g.kp = kp;
-    g.kc = kc;
     g.psi = b.psi;
     g.status = b.status;
     dim3 grid((unsigned)((M + 127) / 128), (unsigned)b.nb);
@@ -496,7 +505,7 @@ cudaError_t launch_ln_batch(const LnBatch &b, cudaStream_t s) {
         g.xlo = from_a ? b.xa_lo : b.xb_lo;
         g.ohi = from_a ? b.xb_hi : b.xa_hi;
         g.olo = from_a ? b.xb_lo : b.xa_lo;
-        k_ln_gemm<<<grid, 128, smem, s>>>(g);
+        k_ln_gemm<<<grid, kLnThreads, smem, s>>>(g);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     LnDeltaArgs d;

@@ -178,7 +178,6 @@ struct LnBatch {
     int32_t *status;
 };
 int ln_kp(int n);
-int ln_kc(int kp);
 size_t ln_gemm_smem(int kp);
 // Real-split eigenvector matrices of every mesh point: n_q * 2 * ln_kp(n)^2 BF16 (hi, lo).
 cudaError_t launch_ln_bmat(int n, int n_q, const float2 *egvs32, __nv_bfloat16 *bmat, cudaStream_t s);
