@@ -107,6 +107,32 @@ __device__ __forceinline__ double gauss(double dx, double win8, double h, double
     return exp_neg(dx * dx * h, tab64) * c;
 }
 
+// d0 = g(om1; -om2+om3) - g(om1; om2-om3), d1 = g(om1; om2+om3) - g(om1; -om2-om3)
+// (get_dirac, scattering_threephonon.f90:262-267), evaluating only the Gaussians whose bit
+// (0..3 in that order) is set in live; the others are 0 (outside their window). One
+// Gaussian per loop trip, so a warp runs as many trips as its lane with the most live bits
+// instead of every branch some lane needs. The centre is (+-om2) + (+-om3) with the signs
+// applied to the bit patterns: the same rounding as the reference's expressions.
+__device__ __forceinline__ void dirac3(uint32_t live, double o1, double o2, double o3, double win8, double h,
+                                       double c, const double *tab, double &d0, double &d1) {
+    double g0 = 0.0, g1 = 0.0, g2 = 0.0, g3 = 0.0;
+    const long long b2 = __double_as_longlong(o2), b3 = __double_as_longlong(o3);
+    constexpr long long kSign = (long long)0x8000000000000000ULL;
+    while (live) {
+        const int j = __ffs(live) - 1;
+        live &= live - 1;
+        const double m2 = __longlong_as_double((j == 1 || j == 2) ? b2 : (b2 ^ kSign));
+        const double m3 = __longlong_as_double((j == 0 || j == 2) ? b3 : (b3 ^ kSign));
+        const double g = gauss(o1 - (m2 + m3), win8, h, c, tab);
+        g0 = j == 0 ? g : g0;
+        g1 = j == 1 ? g : g1;
+        g2 = j == 2 ? g : g2;
+        g3 = j == 3 ? g : g3;
+    }
+    d0 = g0 - g1;
+    d1 = g2 - g3;
+}
+
 __device__ __forceinline__ double adaptive_pair(const double *va, const double *vb, const double *rl) {
     // sqrt(maxval(matmul(va - vb, reclat)**2) * 0.5)
     double m = 0;

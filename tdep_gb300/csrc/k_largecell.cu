@@ -386,25 +386,25 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
             const uint32_t live = qv >> 16;
             const int b2 = bb + e / n, b3 = e % n;
             const double o2 = om2[b2], o3 = om3[b3];
-            double sigma;
+            double sigma, invsig;
             if (it == 1) {
                 sigma = P.sigma_fixed;
+                invsig = 1.0 / sigma;
             } else if (it == 2) {
-                sigma = sqrt(s1 + s2[b2] + s3[b3]);
+                const double sq = s1 + s2[b2] + s3[b3];
+                invsig = rsqrt(sq);
+                sigma = sq * invsig;
             } else {
                 sigma = adaptive_pair(v1, v2 + 3 * b2, P.reclat_g) / 3.0;
                 sigma += adaptive_pair(v1, v3 + 3 * b3, P.reclat_g) / 3.0;
                 sigma += adaptive_pair(v2 + 3 * b2, v3 + 3 * b3, P.reclat_g) / 3.0;
                 sigma += P.thresh_sigma;
+                invsig = 1.0 / sigma;
             }
-            const double invsig = 1.0 / sigma;
             const double win8 = 8.0 * sigma, h = 0.5 * invsig * invsig, cg = kSqrt2PiInv * invsig;
             const double *tab = P.exp2tab;
-            const double ga = (live & 1u) ? gauss(o1 - (-o2 + o3), win8, h, cg, tab) : 0.0;
-            const double gb = (live & 2u) ? gauss(o1 - (o2 - o3), win8, h, cg, tab) : 0.0;
-            const double gc = (live & 4u) ? gauss(o1 - (o2 + o3), win8, h, cg, tab) : 0.0;
-            const double gd = (live & 8u) ? gauss(o1 - (-o2 - o3), win8, h, cg, tab) : 0.0;
-            const double d0 = ga - gb, d1 = gc - gd;
+            double d0, d1;
+            dirac3(live, o1, o2, o3, win8, h, cg, tab, d0, d1);
             if (!nonzero(d0) && !nonzero(d1)) continue;
             const float2 ps = psi[b2 * n + b3];
             const double cr = ps.x, ci = ps.y;

@@ -139,7 +139,7 @@ __host__ __device__ inline Layout make_layout(int n, int cs) {
     L.wrow = o; o += dn;
     L.r2 = o; o += align16(sizeof(double) * n2);
     L.f32 = o; o += align16(sizeof(float) * n * 6);            // om1..3, s1..3 in FP32
-    L.masks = o; o += align16(sizeof(uint32_t) * (3 * n + 2));  // m12, m13, m23, z2, z3
+    L.masks = o; o += align16(sizeof(uint32_t) * (3 * n + 2 + 2 * n2));  // m12, m13, m23, z2, z3, row/col bits
     // E1..E3 and the phase chunk are dead once Psi is formed: the survivor queue reuses them.
     const size_t ez = align16(cs * n2);
     L.E1 = o;
@@ -197,6 +197,9 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
     float *fo2 = fo1 + N, *fo3 = fo2 + N, *fs1 = fo3 + N, *fs2 = fs1 + N, *fs3 = fs2 + N;
     uint32_t *m12 = (uint32_t *)(smem + L.masks);
     uint32_t *m13 = m12 + N, *m23 = m13 + N, *zmask = m23 + N;  // zmask[0]: omega2 < tol, zmask[1]: omega3 < tol
+    // b3 with a non-zero F for each (b1, b2), and b2 for each (b1, b3): the row and column sums
+    // then add only those terms (adding an exact zero changes nothing)
+    uint32_t *rowbits = zmask + 2, *colbits = rowbits + N2;
     C *E1 = (C *)(smem + L.E1);
     C *E2 = (C *)(smem + L.E2);
     C *E3 = (C *)(smem + L.E3);
@@ -237,18 +240,18 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
             om1[b] = P.omega[(size_t)f1 * N + b];
             om2[b] = P.omega[(size_t)q2 * N + b];
             om3[b] = P.omega[(size_t)q3 * N + b];
-            inv1[b] = om1[b] > 0.0 ? 1.0 / om1[b] : 0.0;
+            inv1[b] = P.inv_omega[(size_t)f1 * N + b];
             be2[b] = P.be[(size_t)i2 * N + b];
             be3[b] = P.be[(size_t)i3 * N + b];
             s1[b] = P.sigsq[(size_t)rec.q1 * N + b];
             s2[b] = P.sigsq[(size_t)i2 * N + b];
             s3[b] = P.sigsq[(size_t)i3 * N + b];
-            fo1[b] = (float)om1[b];
-            fo2[b] = (float)om2[b];
-            fo3[b] = (float)om3[b];
-            fs1[b] = (float)s1[b];
-            fs2[b] = (float)s2[b];
-            fs3[b] = (float)s3[b];
+            fo1[b] = P.omega32[(size_t)f1 * N + b];
+            fo2[b] = P.omega32[(size_t)q2 * N + b];
+            fo3[b] = P.omega32[(size_t)q3 * N + b];
+            fs1[b] = P.sigsq32[(size_t)rec.q1 * N + b];
+            fs2[b] = P.sigsq32[(size_t)i2 * N + b];
+            fs3[b] = P.sigsq32[(size_t)i3 * N + b];
             for (int d = 0; d < 3; ++d) {
                 v1[b * 3 + d] = P.vel[((size_t)f1 * N + b) * 3 + d];
                 v2[b * 3 + d] = P.vel[((size_t)q2 * N + b) * 3 + d];
@@ -266,6 +269,7 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
             zmask[0] = 0u;
             zmask[1] = 0u;
         }
+        for (int i = tid; i < 2 * N2; i += bd) rowbits[i] = 0u;
         for (int i = tid; i < nred && i < kMaxRed; i += bd) red[i] = a.red[rec.red_off + i];
         for (int i = tid; i < 3 * N2; i += bd) {
             const int which = i / N2, e = i % N2;
@@ -282,8 +286,11 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
                 const int which = i / N2, x = (i % N2) / N, y = i % N;
                 const double *pa = which == 2 ? om2 : om1;
                 const double *pb = which == 0 ? om2 : om3;
+                const float *fa = which == 2 ? fo2 : fo1;
+                const float *fb = which == 0 ? fo2 : fo3;
                 uint32_t *mk = which == 0 ? m12 : (which == 1 ? m13 : m23);
-                if (fabs(pa[x] - pb[y]) < kFreqTolD) atomicOr(mk + x, 1u << y);
+                // |x - y| < 1e-9 in FP64 needs |fx - fy| below 1e-8 in FP32 at these magnitudes
+                if (fabsf(fa[x] - fb[y]) < 1e-8f && fabs(pa[x] - pb[y]) < kFreqTolD) atomicOr(mk + x, 1u << y);
             } else {
                 const int j = i - 3 * N2, which = j / N, b = j % N;
                 const double w = which == 0 ? om2[b] : om3[b];
@@ -433,12 +440,8 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
             }
             const double win8 = 8.0 * sigma, h = 0.5 * invsig * invsig, cg = kSqrt2PiInv * invsig;
             const double *tab = P.exp2tab;
-            const double ga = (live & 1u) ? gauss(o1 - (-o2 + o3), win8, h, cg, tab) : 0.0;
-            const double gb = (live & 2u) ? gauss(o1 - (o2 - o3), win8, h, cg, tab) : 0.0;
-            const double gc = (live & 4u) ? gauss(o1 - (o2 + o3), win8, h, cg, tab) : 0.0;
-            const double gd = (live & 8u) ? gauss(o1 - (-o2 - o3), win8, h, cg, tab) : 0.0;
-            const double d0 = ga - gb;
-            const double d1 = gc - gd;
+            double d0, d1;
+            dirac3(live, o1, o2, o3, win8, h, cg, tab, d0, d1);
             if (nonzero(d0) || nonzero(d1)) {
                 const C psi = B[idx];
                 const double cr = (double)psi.x, ci = (double)psi.y;
@@ -449,7 +452,12 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
                 const double plf1 = n2 + n3 + 1.0;
                 const double f0 = perm * psisq * plf0 * d0;
                 const double f1 = perm * psisq * plf1 * d1;
-                F[idx] = f0 + f1;
+                const double fsum = f0 + f1;
+                F[idx] = fsum;
+                if (nonzero(fsum)) {
+                    atomicOr(rowbits + b1 * N + b2, 1u << b3);
+                    atomicOr(colbits + b1 * N + b3, 1u << b2);
+                }
             }
         }
         __syncthreads();
@@ -549,17 +557,12 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
         for (int e = tid; e < 2 * N2; e += bd) {
             double sum = 0.0;
             if (e < N2) {
-                for (int b3 = 0; b3 < N; ++b3) {
-                    const double f = F[e * N + b3];
-                    if (nonzero(f)) sum += f;
-                }
+                for (uint32_t bits = rowbits[e]; bits; bits &= bits - 1) sum += F[e * N + __ffs(bits) - 1];
                 R2[e] = sum;
             } else {
                 const int e3 = e - N2, b1 = e3 / N, b3 = e3 % N;
-                for (int b2 = 0; b2 < N; ++b2) {
-                    const double f = F[(b1 * N + b2) * N + b3];
-                    if (nonzero(f)) sum += f;
-                }
+                for (uint32_t bits = colbits[e3]; bits; bits &= bits - 1)
+                    sum += F[(b1 * N + __ffs(bits) - 1) * N + b3];
                 R3[e3] = sum;
             }
         }
@@ -572,6 +575,20 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
                 if (nonzero(g)) atomicAdd(a.gamma + row, (double)nred * g);
             }
         }
+        // the Xi row terms 2 F om/om1 of each entry, computed once for all equivalent triplets
+        // (after Gamma has read R2)
+        __syncthreads();
+        for (int e = tid; e < 2 * N2; e += bd) {
+            if (e < N2) {
+                const double v = R2[e];
+                R2[e] = nonzero(v) ? 2.0 * v * om2[e % N] * inv1[e / N] : 0.0;
+            } else {
+                const int e3 = e - N2;
+                const double v = R3[e3];
+                R3[e3] = nonzero(v) ? 2.0 * v * om3[e3 % N] * inv1[e3 / N] : 0.0;
+            }
+        }
+        __syncthreads();
         for (int i = tid; i < 2 * N2 * nred; i += bd) {
             const int r = i / (2 * N2), e = i % (2 * N2);
             const int2 pr = red[r];
@@ -579,14 +596,12 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
                 const int b1 = e / N, b2 = e % N;
                 const int row = rowid[b1];
                 const double v = R2[e];
-                if (row >= 0 && nonzero(v))
-                    atomicAdd(a.od + row * ld + (int64_t)pr.x * N + b2, 2.0 * v * om2[b2] * inv1[b1]);
+                if (row >= 0 && nonzero(v)) atomicAdd(a.od + row * ld + (int64_t)pr.x * N + b2, v);
             } else {
                 const int e3 = e - N2, b1 = e3 / N, b3 = e3 % N;
                 const int row = rowid[b1];
                 const double v = R3[e3];
-                if (row >= 0 && nonzero(v))
-                    atomicAdd(a.od + row * ld + (int64_t)pr.y * N + b3, 2.0 * v * om3[b3] * inv1[b1]);
+                if (row >= 0 && nonzero(v)) atomicAdd(a.od + row * ld + (int64_t)pr.y * N + b3, v);
             }
         }
         __syncthreads();

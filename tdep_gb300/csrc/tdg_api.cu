@@ -122,7 +122,8 @@ struct tdg_ctx {
     DevBuf<float> fc3_mwm32, fc4_mwm32;
     DevBuf<double2> tw;
     DevBuf<float2> tw32;
-    DevBuf<double> d_exp2tab;
+    DevBuf<double> d_exp2tab, d_invom;
+    DevBuf<float> d_om32, d_sigsq32;
     int L = 1, lmul[3] = {1, 1, 1};
     // scattering state
     int n_row = 0;
@@ -482,6 +483,17 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
     chk(c->tw32.upload(tw32.data(), tw32.size(), s));
     const std::vector<double> e2t = exp2_table();
     chk(c->d_exp2tab.upload(e2t.data(), e2t.size(), s));
+    {
+        // per-mode tables of the kernels' screens: omega in FP32 and 1/omega
+        std::vector<float> om32(c->omega.size());
+        std::vector<double> invom(c->omega.size());
+        for (size_t i = 0; i < c->omega.size(); ++i) {
+            om32[i] = (float)c->omega[i];
+            invom[i] = c->omega[i] > 0.0 ? 1.0 / c->omega[i] : 0.0;
+        }
+        chk(c->d_om32.upload(om32.data(), om32.size(), s));
+        chk(c->d_invom.upload(invom.data(), invom.size(), s));
+    }
     chk(c->d_status.alloc(1));
     chk(cudaStreamSynchronize(s));
     if (e != cudaSuccess) return fail(set_error(kErrDevice, std::string("upload failed: ") + cudaGetErrorString(e)));
@@ -666,6 +678,8 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     ph.thresh_sigma = maxavg * 1e-4;
     ph.integrationtype = o->integrationtype;
     ph.exp2tab = c->d_exp2tab.p;
+    ph.inv_omega = c->d_invom.p;
+    ph.omega32 = c->d_om32.p;
 
     std::vector<int32_t> rowidx((size_t)nirr * n, -1), rq1(nr), rb1(nr);
     std::vector<double> w3(nr, 0.0), w4(nr, 0.0);
@@ -934,6 +948,8 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     };
     chk(c->d_be.upload(be.data(), be.size(), s));
     chk(c->d_sigsq.upload(sigsq.data(), sigsq.size(), s));
+    std::vector<float> sigsq32(sigsq.begin(), sigsq.end());
+    chk(c->d_sigsq32.upload(sigsq32.data(), sigsq32.size(), s));
     chk(c->d_rowidx.upload(rowidx.data(), rowidx.size(), s));
     chk(c->d_row_q1.upload(rq1.data(), rq1.size(), s));
     chk(c->d_row_b1.upload(rb1.data(), rb1.size(), s));
@@ -980,6 +996,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     if (e != cudaSuccess) return set_error(kErrDevice, std::string("allocation/upload failed: ") + cudaGetErrorString(e));
     ph.be = c->d_be.p;
     ph.sigsq = c->d_sigsq.p;
+    ph.sigsq32 = c->d_sigsq32.p;
     RowsDev rows;
     rows.n_row = nr;
     rows.rowidx = c->d_rowidx.p;

@@ -53,6 +53,9 @@ struct PhononDev {
     double thresh_sigma;     // integrationtype 6
     int32_t integrationtype;
     const double *exp2tab;   // [64] 2^(-j/64), the table of exp_neg
+    const double *inv_omega; // [n_full*n] 1/omega, 0 where omega <= 0
+    const float *omega32;    // [n_full*n] omega in FP32 (screens)
+    const float *sigsq32;    // [n_irr*n] sigsq in FP32 (screens)
 };
 
 // exp(-t), 0 <= t <= 40, on the device (diagnostic for tests): out[i] = exp_neg(t[i]).
