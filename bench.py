@@ -333,16 +333,12 @@ def run_gb300(args):
         t2 = time.perf_counter()
         s2.kappa(opts)
         t3 = time.perf_counter()
+        h2d, d2h = s2.transfer_bytes()
         s2.close()
         torch.cuda.synchronize()
         t4 = time.perf_counter()
         e2e_s.append(t4 - t0)
         parts.append((t1 - t0, t2 - t1, t3 - t2, t4 - t3))
-    nrow, ncol = lists.n_row, prob.n_full * n
-    h2d = (prob.omega.nbytes + prob.vel.nbytes + prob.egv.nbytes * 3 // 2 + prob.n_op * prob.n_full * 4 +
-           prob.fc3_mwm.nbytes * 3 // 2 + prob.fc3_lv.nbytes + lists.list3.nbytes + lists.ptr3.nbytes +
-           stats["candidates"] * 16 + 2 * prob.n_irr * n * 8 + kappa_iters * ncol * 3 * 8)
-    d2h = nrow * 8 + prob.n_irr * n * 8 * 2 + 18 * 8 + kappa_iters * nrow * 3 * 8
 
     # ---- roofline of the dominant kernel (fused pretransform + contraction + epilogue) ----
     # Per-unit work of a q-triplet: the pretransform streams N_t force-constant triplets
@@ -385,7 +381,7 @@ def run_gb300(args):
                                  if small else "mixed: FP32 pretransform, BF16x3 tensor-core contraction with FP32 "
                                                "accumulation, FP64 delta weights/occupations/accumulation"),
                    "l2": "256 MB buffer written between steps (L2 flush); Xi+od working set 2x%.2f GB" %
-                         (nrow * ncol * 8 / 1e9)},
+                         (lists.n_row * prob.n_full * n * 8 / 1e9)},
         "e2e": {"value": trip / float(np.mean(e2e_s)), "unit": "q-triplets/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "includes": "context creation, generate, kappa solve",
                 "ms": {k: 1e3 * float(np.median([p[i] for p in parts]))

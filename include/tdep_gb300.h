@@ -196,6 +196,13 @@ int tdg_scattering(tdg_ctx *ctx, const tdg_opts *opts, const tdg_qlists *lists,
 int tdg_get_xi(tdg_ctx *ctx, double *xi);
 
 /*
+ * Bytes copied host-to-device (*h2d) and device-to-host (*d2h) by all calls on this context
+ * since tdg_create, that call included. Instrumentation with no reference counterpart: the
+ * reference keeps everything in host memory.
+ */
+int tdg_transfer_bytes(tdg_ctx *ctx, int64_t *h2d, int64_t *d2h);
+
+/*
  * Irreducible q-triplets of one sample, enumerated on the device (kernel K1). Replaces the
  * per-candidate q3 index and triplet_is_irreducible of scattering_threephonon.f90:72-77,
  * 319-448. q1 is the irreducible index (1-based) and sample holds full-mesh indices

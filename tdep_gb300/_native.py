@@ -116,6 +116,7 @@ SIGNATURES = {
                                 _i64p, _i32p, _i32p]),
     "tdg_scattering": (C.c_int, [C.c_void_p, C.POINTER(TdgOpts), C.POINTER(TdgQlists), _f64p, _f64p, _f64p]),
     "tdg_get_xi": (C.c_int, [C.c_void_p, _f64p]),
+    "tdg_transfer_bytes": (C.c_int, [C.c_void_p, _i64p, _i64p]),
     "tdg_triplets": (C.c_int, [C.c_void_p, C.c_int32, _i32p, C.c_int64, _i32p, C.c_int64, _i64p]),
     "tdg_triplets_static": (C.c_int, [C.c_void_p, C.c_int32, _i32p, C.c_int64, _i32p, C.c_int64, _i64p]),
     "tdg_set_fc3": (C.c_int, [C.c_void_p, _f64p]),

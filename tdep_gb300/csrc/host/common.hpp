@@ -66,6 +66,22 @@ enum Status : int {
 // Records the message for tdg_last_error() and returns the code.
 int set_error(int code, const std::string &msg);
 
+// Host-phase timing for diagnostics: when the environment variable TDG_TRACE is set, the
+// time between successive mark() calls is summed per label and printed to stderr when the
+// timer goes out of scope. Costs one clock read per mark otherwise.
+class PhaseTimer {
+  public:
+    explicit PhaseTimer(const char *scope);
+    ~PhaseTimer();
+    void mark(const char *label);
+
+  private:
+    const char *scope_;
+    bool on_;
+    double t_;
+    std::vector<std::pair<const char *, double>> sums_;
+};
+
 // f(i) for i in [0, n) on all hardware threads (dynamic assignment, one index at a time);
 // f must be safe to run concurrently for different i.
 template <typename F>

@@ -1,6 +1,8 @@
 // Host stage of thermal_conductivity: reading the input files and building the flattened
 // problem (main.f90:42-181), error reporting and the output file (main.f90:246-294).
+#include <chrono>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <memory>
@@ -12,6 +14,32 @@ namespace tdg {
 
 namespace {
 thread_local std::string g_last_error;
+}
+
+namespace {
+double now_ms() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+}  // namespace
+
+PhaseTimer::PhaseTimer(const char *scope) : scope_(scope), on_(std::getenv("TDG_TRACE") != nullptr), t_(now_ms()) {}
+
+PhaseTimer::~PhaseTimer() {
+    if (!on_) return;
+    for (const auto &x : sums_) std::fprintf(stderr, "[tdg] %s %s %.3f ms\n", scope_, x.first, x.second);
+}
+
+void PhaseTimer::mark(const char *label) {
+    if (!on_) return;
+    const double t = now_ms();
+    for (auto &x : sums_)
+        if (std::strcmp(x.first, label) == 0) {
+            x.second += t - t_;
+            t_ = t;
+            return;
+        }
+    sums_.emplace_back(label, t - t_);
+    t_ = t;
 }
 
 int set_error(int code, const std::string &msg) {

@@ -227,52 +227,218 @@ __global__ void k_sym_scatmat(MeshDev m, OrbitDev o, const int32_t *row_q1, doub
 }
 
 // K8: three dot products per row of Xi (kappa.f90:411-413, the lo_gemv calls).
-// Xi streams from HBM once; F (3 x n_col) stays in L2.
-__global__ void k_xi_gemv(const double *__restrict__ xi, int64_t n_col, const double *__restrict__ fbb,
-                          double *buf) {
-    __shared__ double sh[3][32];
-    const int r = blockIdx.x;
-    const double *row = xi + (int64_t)r * n_col;
-    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
-    // four independent row loads in flight per thread before they are used
+// Xi streams from HBM once per BTE iteration; F (3 x n_col) stays in L2. GB300's FP64 pipe
+// (2 FMA per SM and clock) would make an FP64 product with three right-hand sides
+// compute-bound at ~1.2 TB/s of Xi, so the product runs on the FP32 pipe in one of two
+// element formats, converted once per kappa call (k_split_xi) and per iteration for F
+// (k_foldout):
+//  - FP64 runs: Xi and F as (hi, lo) float pairs with hi + lo = x to ~2^-48, each term
+//    accumulated in double-float (exact leading product by FMA, cross terms, TwoSum of the
+//    high parts); ~1e-14 relative. Same bytes per element as FP64.
+//  - mixed-precision runs: Xi and F as floats, the 2^-24 rounding of the FP32 contraction
+//    that produced Xi; chains of kChain products by FMA are added into double-float
+//    accumulators, so the sum over 10^5 columns adds no error of its own. Half the bytes.
+// A CTA takes kGemvRows rows and one of gemv_split() column ranges (gridDim.y): each F value
+// read from L2 serves kGemvRows rows. Partial sums go to part[row][range][3] (FP64) and are
+// added in range order by k_xi_reduce, so the result does not depend on scheduling. The
+// in-CTA reduction stays in double-float too: FP64 shuffles and adds in every CTA's epilogue
+// cost more than the product itself once there are more than a few ranges.
+constexpr int kGemvRows = 4;
+constexpr int kGemvMaxSplit = 32;
+constexpr int kChain = 4;
+
+// Ranges of at most 32768 columns, and enough CTAs for about two waves of 4 per SM.
+int gemv_split(int32_t n_row, int64_t n_col, int n_sm) {
+    const int64_t groups = (n_row + kGemvRows - 1) / kGemvRows;
+    int64_t k = (n_col + 32767) / 32768;
+    const int64_t w = (8 * (int64_t)n_sm + groups - 1) / groups;
+    if (w > k) k = w;
+    if (k > n_col / 256) k = n_col / 256;
+    return (int)(k < 1 ? 1 : (k > kGemvMaxSplit ? kGemvMaxSplit : k));
+}
+
+// x = hi + lo by integer operations on the bits (double <-> float conversions run on the
+// FP64 pipe): hi keeps the leading 24 significant bits of x, lo the remaining 29 rounded to
+// 24, so hi + lo = x to 2^-48 relative. Zero and subnormal doubles give 0; magnitudes
+// outside [2^-74, 2^127) take the FP64 conversions.
+__device__ __forceinline__ float2 split_df(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7FF);
+    if (e == 0) return make_float2(0.f, 0.f);
+    if (e < 949 || e > 1150) {
+        const float h = (float)x;
+        return make_float2(h, (float)(x - (double)h));
+    }
+    const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+    const float hi = __uint_as_float(sign | ((unsigned int)(e - 896) << 23) | (unsigned int)((b >> 29) & 0x7FFFFFu));
+    // remainder r * 2^(e - 1075), r < 2^29; the power of two is a normal float for e >= 949
+    const float lo = __uint2float_rn((unsigned int)(b & 0x1FFFFFFFu)) * __uint_as_float((unsigned int)(e - 948) << 23);
+    return make_float2(hi, sign ? -lo : lo);
+}
+
+// x rounded to float (ties away from zero) by integer operations; magnitudes outside
+// [2^-126, 2^127) take the FP64 conversion.
+__device__ __forceinline__ float round_f32(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7FF);
+    if (e == 0) return 0.f;
+    if (e < 897 || e > 1149) return (float)x;
+    const unsigned int v = ((unsigned int)(b >> 32) & 0x80000000u) | ((unsigned int)(e - 896) << 23) |
+                           (unsigned int)((b >> 29) & 0x7FFFFFu);
+    return __uint_as_float(v + (unsigned int)((b >> 28) & 1u));  // a carry moves into the exponent
+}
+
+// (a.x + a.y) + (b.x + b.y) in double-float (TwoSum of the high parts)
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+    const float t = a.x + b.x;
+    const float bb = t - a.x;
+    const float e = (a.x - (t - bb)) + (b.x - bb);
+    return make_float2(t, a.y + b.y + e);
+}
+
+// s += p in double-float
+__device__ __forceinline__ void df_add1(float2 &s, float p) {
+    const float t = s.x + p;
+    const float bb = t - s.x;
+    s.y += (s.x - (t - bb)) + (p - bb);
+    s.x = t;
+}
+
+// s += a * b in double-float
+__device__ __forceinline__ void df_fma(float2 &s, float2 a, float2 b) {
+    const float p = a.x * b.x;
+    const float pe = fmaf(a.x, b.x, -p);
+    const float cross = fmaf(a.x, b.y, a.y * b.x);
+    const float t = s.x + p;
+    const float bb = t - s.x;
+    const float e = (s.x - (t - bb)) + (p - bb);
+    s.x = t;
+    s.y += e + pe + cross;
+}
+
+template <bool DF>
+__global__ void k_split_xi(const double *xi, int64_t n, void *out) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if constexpr (DF)
+            static_cast<float2 *>(out)[i] = split_df(__ldcs(xi + i));
+        else
+            static_cast<float *>(out)[i] = round_f32(__ldcs(xi + i));
+    }
+}
+
+// DF: xi, fbb as float2 (FP64 runs); otherwise as float (mixed precision).
+template <bool DF>
+__global__ void __launch_bounds__(256) k_xi_gemv(const void *__restrict__ xi_, int32_t n_row, int64_t n_col,
+                                                 const void *__restrict__ fbb_, double *part) {
+    __shared__ float2 sh[kGemvRows * 3][8];
+    const int r0 = blockIdx.x * kGemvRows;
+    const int nr = min(kGemvRows, n_row - r0);
+    const int64_t per = (n_col + gridDim.y - 1) / gridDim.y;
+    const int64_t c0 = per * blockIdx.y, c1 = min(n_col, c0 + per);
+    float2 acc[kGemvRows][3];
+#pragma unroll
+    for (int k = 0; k < kGemvRows; ++k) acc[k][0] = acc[k][1] = acc[k][2] = make_float2(0.f, 0.f);
     const int64_t step = blockDim.x;
-    int64_t j = threadIdx.x;
-    for (; j + 3 * step < n_col; j += 4 * step) {
-        double x[4];
+    int64_t j = c0 + threadIdx.x;
+    if constexpr (DF) {
+        const float2 *xi = static_cast<const float2 *>(xi_);
+        const float2 *fbb = static_cast<const float2 *>(fbb_);
+        for (; j + step < c1; j += 2 * step) {
+            float2 x[2][kGemvRows];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) x[u] = __ldcs(row + j + u * step);
+            for (int u = 0; u < 2; ++u)
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const double *f = fbb + (j + u * step) * 3;
-            s0 = fma(x[u], __ldg(f), s0);
-            s1 = fma(x[u], __ldg(f + 1), s1);
-            s2 = fma(x[u], __ldg(f + 2), s2);
+                for (int k = 0; k < kGemvRows; ++k)
+                    x[u][k] = k < nr ? __ldcs(xi + (int64_t)(r0 + k) * n_col + j + u * step) : make_float2(0.f, 0.f);
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const float2 *f = fbb + (j + u * step) * 3;
+                const float2 f0 = __ldg(f), f1 = __ldg(f + 1), f2 = __ldg(f + 2);
+#pragma unroll
+                for (int k = 0; k < kGemvRows; ++k) {
+                    df_fma(acc[k][0], x[u][k], f0);
+                    df_fma(acc[k][1], x[u][k], f1);
+                    df_fma(acc[k][2], x[u][k], f2);
+                }
+            }
+        }
+        for (; j < c1; j += step) {
+            const float2 *f = fbb + j * 3;
+            const float2 f0 = __ldg(f), f1 = __ldg(f + 1), f2 = __ldg(f + 2);
+#pragma unroll
+            for (int k = 0; k < kGemvRows; ++k) {
+                const float2 x = k < nr ? __ldcs(xi + (int64_t)(r0 + k) * n_col + j) : make_float2(0.f, 0.f);
+                df_fma(acc[k][0], x, f0);
+                df_fma(acc[k][1], x, f1);
+                df_fma(acc[k][2], x, f2);
+            }
+        }
+    } else {
+        const float *xi = static_cast<const float *>(xi_);
+        const float *fbb = static_cast<const float *>(fbb_);
+        for (; j + (kChain - 1) * step < c1; j += kChain * step) {
+            float x[kChain][kGemvRows], f[kChain][3];
+#pragma unroll
+            for (int u = 0; u < kChain; ++u)
+#pragma unroll
+                for (int k = 0; k < kGemvRows; ++k)
+                    x[u][k] = k < nr ? __ldcs(xi + (int64_t)(r0 + k) * n_col + j + u * step) : 0.f;
+#pragma unroll
+            for (int u = 0; u < kChain; ++u)
+#pragma unroll
+                for (int d = 0; d < 3; ++d) f[u][d] = __ldg(fbb + (j + u * step) * 3 + d);
+#pragma unroll
+            for (int k = 0; k < kGemvRows; ++k)
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    float c = x[0][k] * f[0][d];
+#pragma unroll
+                    for (int u = 1; u < kChain; ++u) c = fmaf(x[u][k], f[u][d], c);
+                    df_add1(acc[k][d], c);
+                }
+        }
+        for (; j < c1; j += step) {
+            const float *f = fbb + j * 3;
+            const float f0 = __ldg(f), f1 = __ldg(f + 1), f2 = __ldg(f + 2);
+#pragma unroll
+            for (int k = 0; k < kGemvRows; ++k) {
+                const float x = k < nr ? __ldcs(xi + (int64_t)(r0 + k) * n_col + j) : 0.f;
+                df_add1(acc[k][0], x * f0);
+                df_add1(acc[k][1], x * f1);
+                df_add1(acc[k][2], x * f2);
+            }
         }
     }
-    for (; j < n_col; j += step) {
-        const double x = __ldcs(row + j);
-        const double *f = fbb + j * 3;
-        s0 = fma(x, __ldg(f), s0);
-        s1 = fma(x, __ldg(f + 1), s1);
-        s2 = fma(x, __ldg(f + 2), s2);
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        s0 += __shfl_down_sync(0xffffffffu, s0, o);
-        s1 += __shfl_down_sync(0xffffffffu, s1, o);
-        s2 += __shfl_down_sync(0xffffffffu, s2, o);
-    }
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (lane == 0) {
-        sh[0][w] = s0;
-        sh[1][w] = s1;
-        sh[2][w] = s2;
-    }
+#pragma unroll
+    for (int k = 0; k < kGemvRows; ++k)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            float2 v = acc[k][d];
+            for (int o = 16; o > 0; o >>= 1) {
+                float2 u;
+                u.x = __shfl_down_sync(0xffffffffu, v.x, o);
+                u.y = __shfl_down_sync(0xffffffffu, v.y, o);
+                v = df_add(v, u);
+            }
+            if (lane == 0) sh[k * 3 + d][w] = v;
+        }
     __syncthreads();
-    if (threadIdx.x < 3) {
-        double s = 0.0;
-        for (int i = 0; i < (int)(blockDim.x / 32); ++i) s += sh[threadIdx.x][i];
-        buf[(int64_t)r * 3 + threadIdx.x] = s;
+    if (threadIdx.x < nr * 3) {
+        float2 v = sh[threadIdx.x][0];
+        for (int i = 1; i < 8; ++i) v = df_add(v, sh[threadIdx.x][i]);
+        const int k = threadIdx.x / 3, d = threadIdx.x % 3;
+        part[((int64_t)(r0 + k) * gridDim.y + blockIdx.y) * 3 + d] = (double)v.x + (double)v.y;
     }
+}
+
+__global__ void k_xi_reduce(const double *part, int32_t n_row, int split, double *buf) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_row * 3) return;
+    const int r = i / 3, d = i % 3;
+    double v = 0.0;
+    for (int c = 0; c < split; ++c) v += part[((int64_t)r * split + c) * 3 + d];
+    buf[i] = v;
 }
 
 }  // namespace
@@ -331,8 +497,9 @@ cudaError_t launch_sym_scatmat(const MeshDev &m, const OrbitDev &o, int32_t n_ro
 
 // foldout (kappa.f90:382-404): F of every full-mesh point from its irreducible point,
 // Fbb(q, b) = sign(op) * R_|op| Fn(irr(q), b), one thread per (q, b).
+template <bool DF>
 __global__ void k_foldout(int32_t n_full, int32_t n_mode, const int32_t *full_op, const int32_t *full_irr,
-                          const double *op_cart, const double *fn, double *fbb) {
+                          const double *op_cart, const double *fn, void *fbb) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (int64_t)n_full * n_mode) return;
     const int iq = (int)(i / n_mode), b = (int)(i % n_mode);
@@ -340,22 +507,49 @@ __global__ void k_foldout(int32_t n_full, int32_t n_mode, const int32_t *full_op
     const double *m = op_cart + 9 * (abs(iop) - 1);
     const double *v = fn + ((int64_t)full_irr[iq] * n_mode + b) * 3;
     const double sg = iop > 0 ? 1.0 : -1.0;
-    for (int d = 0; d < 3; ++d) fbb[i * 3 + d] = sg * (m[d] * v[0] + m[d + 3] * v[1] + m[d + 6] * v[2]);
+    for (int d = 0; d < 3; ++d) {
+        const double y = sg * (m[d] * v[0] + m[d + 3] * v[1] + m[d + 6] * v[2]);
+        if constexpr (DF)
+            static_cast<float2 *>(fbb)[i * 3 + d] = split_df(y);
+        else
+            static_cast<float *>(fbb)[i * 3 + d] = round_f32(y);
+    }
 }
 
 cudaError_t launch_foldout(int32_t n_full, int32_t n_mode, const int32_t *full_op, const int32_t *full_irr,
-                           const double *op_cart, const double *fn, double *fbb, cudaStream_t s) {
+                           const double *op_cart, const double *fn, bool df, void *fbb, cudaStream_t s) {
     const int64_t n = (int64_t)n_full * n_mode;
     if (n <= 0) return cudaSuccess;
-    k_foldout<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n_full, n_mode, full_op, full_irr, op_cart, fn, fbb);
+    if (df)
+        k_foldout<true><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n_full, n_mode, full_op, full_irr, op_cart, fn, fbb);
+    else
+        k_foldout<false><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n_full, n_mode, full_op, full_irr, op_cart, fn, fbb);
     return cudaGetLastError();
 }
 
-cudaError_t launch_xi_gemv(const double *xi, int32_t n_row, int64_t n_col, const double *fbb, double *buf,
-                           int n_sm, cudaStream_t s) {
-    (void)n_sm;
+size_t xi_gemv_part_elems(int32_t n_row) { return (size_t)n_row * kGemvMaxSplit * 3; }
+
+cudaError_t launch_split_xi(const double *xi, int64_t n, bool df, void *out, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const int64_t blocks = (n + 255) / 256;
+    const unsigned g = (unsigned)(blocks < 65536 ? blocks : 65536);
+    if (df)
+        k_split_xi<true><<<g, 256, 0, s>>>(xi, n, out);
+    else
+        k_split_xi<false><<<g, 256, 0, s>>>(xi, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_xi_gemv(const void *xi, int32_t n_row, int64_t n_col, bool df, const void *fbb, double *part,
+                           double *buf, int n_sm, cudaStream_t s) {
     if (n_row <= 0) return cudaSuccess;
-    k_xi_gemv<<<n_row, 256, 0, s>>>(xi, n_col, fbb, buf);
+    const int split = gemv_split(n_row, n_col, n_sm);
+    dim3 grid((unsigned)((n_row + kGemvRows - 1) / kGemvRows), (unsigned)split);
+    if (df)
+        k_xi_gemv<true><<<grid, 256, 0, s>>>(xi, n_row, n_col, fbb, part);
+    else
+        k_xi_gemv<false><<<grid, 256, 0, s>>>(xi, n_row, n_col, fbb, part);
+    k_xi_reduce<<<(n_row * 3 + 255) / 256, 256, 0, s>>>(part, n_row, split, buf);
     return cudaGetLastError();
 }
 

@@ -72,30 +72,11 @@ __device__ __forceinline__ const float2 *egvs_ptr<float2>(const PhononDev &ph) {
     return ph.egvs32;
 }
 
-// One entry of the adjoint's gradient accumulator: FP64 on the FP64 path; on the mixed path
-// a compensated FP32 pair (sum, negated lost low part), because GB300's FP64 pipe runs at
-// 1/64 of the FP32 rate and every q-triplet adds into all n_fc3 * 27 entries.
-template <typename R>
-struct GradAcc;
-template <>
-struct GradAcc<double> {
-    using T = double;
-    __device__ static void add(double &a, double v) { a += v; }
-    __host__ __device__ static double value(double a) { return a; }
-    __device__ static double zero() { return 0.0; }
-};
-template <>
-struct GradAcc<float> {
-    using T = float2;
-    __device__ static void add(float2 &a, float v) {
-        const float y = v - a.y;
-        const float t = a.x + y;
-        a.y = (t - a.x) - y;
-        a.x = t;
-    }
-    __host__ __device__ static double value(float2 a) { return (double)a.x - (double)a.y; }
-    __device__ static float2 zero() { return make_float2(0.f, 0.f); }
-};
+// The adjoint accumulates d L / d mwm per CTA in shared memory in the precision of the
+// contraction (FP64 or FP32) and adds it into the CTA's FP64 slice in global memory every
+// kAdjFlush q-triplets, which bounds the FP32 rounding on the mixed path (GB300's FP64 pipe
+// runs at 1/64 of the FP32 rate and every q-triplet adds into all n_fc3 * 27 entries).
+constexpr int kAdjFlush = 64;
 
 // exp(-2 pi i (q2.lv2 + q3.lv3)) of force-constant triplet t as an exact root of unity:
 // q = g/G on the mesh and lv integer, so the phase index is sum_d (g2 lv2 + g3 lv3)_d mod G_d
@@ -219,12 +200,11 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
     const int64_t ld = (int64_t)m.n_full * N;
     const int it = P.integrationtype;
     const float sigfix32 = (float)P.sigma_fixed;
-    using GA = GradAcc<R>;
-    using GT = typename GA::T;
-    GT *acc = (GT *)(smem + L.total);  // ADJ with acc_in_smem: [fc.n * 27]
+    R *acc = (R *)(smem + L.total);  // ADJ with acc_in_smem: [fc.n * 27]
+    int since_flush = 0;
     if constexpr (ADJ) {
         if (a.acc_in_smem)
-            for (int i = tid; i < fc.n * 27; i += bd) acc[i] = GA::zero();
+            for (int i = tid; i < fc.n * 27; i += bd) acc[i] = (R)0;
     }
 
     for (int t = blockIdx.x; t < a.n_trip; t += gridDim.x) {
@@ -528,7 +508,7 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
 #pragma unroll
                 for (int x = 0; x < N; ++x) A[ab * N + x] = acc[x];
             }
-            GT *slice = (GT *)a.mwm_bar + (size_t)blockIdx.x * fc.n * 27;
+            double *slice = a.mwm_bar + (size_t)blockIdx.x * fc.n * 27;
             // thread -> one (i,j,k) of the 27 and every groups-th force-constant triplet; within a
             // q-triplet exactly one thread touches each entry, and q-triplets are separated by
             // barriers
@@ -545,11 +525,22 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
                         const C q = A[fc.abase[tt] + off];
                         const C p = ph[tl];
                         const R v = (R)2 * (p.x * q.x - p.y * q.y);
-                        GA::add(a.acc_in_smem ? acc[(size_t)tt * 27 + ijk] : slice[(size_t)tt * 27 + ijk], v);
+                        if (a.acc_in_smem)
+                            acc[(size_t)tt * 27 + ijk] += v;
+                        else
+                            slice[(size_t)tt * 27 + ijk] += (double)v;
                     }
                 }
             }
             __syncthreads();
+            if (a.acc_in_smem && ++since_flush == kAdjFlush) {
+                for (int i = tid; i < fc.n * 27; i += bd) {
+                    slice[i] += (double)acc[i];
+                    acc[i] = (R)0;
+                }
+                since_flush = 0;
+                __syncthreads();
+            }
             continue;
         }
         // ---- R2 = sum over b3, R3 = sum over b2 (into B as doubles) ----
@@ -609,8 +600,8 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
     if constexpr (ADJ) {
         if (a.acc_in_smem) {
             __syncthreads();
-            GT *slice = (GT *)a.mwm_bar + (size_t)blockIdx.x * fc.n * 27;
-            for (int i = tid; i < fc.n * 27; i += bd) slice[i] = acc[i];
+            double *slice = a.mwm_bar + (size_t)blockIdx.x * fc.n * 27;
+            for (int i = tid; i < fc.n * 27; i += bd) slice[i] += (double)acc[i];
         }
     }
 }
@@ -678,11 +669,10 @@ cudaError_t launch_adj_prec(const ThreePhArgs &a, int grid, size_t extra, cudaSt
     }
 }
 
-template <typename R>
-__global__ void k_sum_slices(const typename GradAcc<R>::T *slices, int32_t n_slice, int64_t n, double *out) {
+__global__ void k_sum_slices(const double *slices, int32_t n_slice, int64_t n, double *out) {
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
         double acc = 0.0;
-        for (int g = 0; g < n_slice; ++g) acc += GradAcc<R>::value(slices[(int64_t)g * n + e]);
+        for (int g = 0; g < n_slice; ++g) acc += slices[(int64_t)g * n + e];
         out[e] = acc;
     }
 }
@@ -726,27 +716,23 @@ cudaError_t launch_threephonon(const ThreePhArgs &a, int precision, int n_sm, cu
 }
 
 int threephonon_adjoint_grid(int n, int precision, int n_sm, int n_trip, int n_fc, bool acc_in_smem) {
-    const size_t extra = acc_in_smem ? (size_t)n_fc * 27 * sizeof(double) : 0;
+    const size_t extra = acc_in_smem ? (size_t)n_fc * 27 * (precision == 0 ? sizeof(double) : sizeof(float)) : 0;
     return precision == 0 ? grid_prec<double, true>(n, n_sm, n_trip, extra)
                           : grid_prec<float, true>(n, n_sm, n_trip, extra);
 }
 
 cudaError_t launch_threephonon_adjoint(const ThreePhArgs &a, int precision, int grid, cudaStream_t s) {
     if (a.n_trip <= 0 || grid <= 0) return cudaSuccess;
-    const size_t extra = a.acc_in_smem ? (size_t)a.fc.n * 27 * sizeof(double) : 0;
+    const size_t extra =
+        a.acc_in_smem ? (size_t)a.fc.n * 27 * (precision == 0 ? sizeof(double) : sizeof(float)) : 0;
     if (precision == 0) return launch_adj_prec<double>(a, grid, extra, s);
     return launch_adj_prec<float>(a, grid, extra, s);
 }
 
-cudaError_t launch_sum_slices(const void *slices, int precision, int32_t n_slice, int64_t n, double *out,
-                              cudaStream_t s) {
+cudaError_t launch_sum_slices(const double *slices, int32_t n_slice, int64_t n, double *out, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     const int64_t blocks = (n + 255) / 256;
-    const unsigned g = (unsigned)(blocks < 4096 ? blocks : 4096);
-    if (precision == 0)
-        k_sum_slices<double><<<g, 256, 0, s>>>((const double *)slices, n_slice, n, out);
-    else
-        k_sum_slices<float><<<g, 256, 0, s>>>((const float2 *)slices, n_slice, n, out);
+    k_sum_slices<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, s>>>(slices, n_slice, n, out);
     return cudaGetLastError();
 }
 

@@ -60,7 +60,7 @@ struct DevBuf {
         cudaError_t e = alloc(count);
         if (e != cudaSuccess) return e;
         if (count == 0) return cudaSuccess;
-        return cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s);
+        return copy_async(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s);
     }
 };
 
@@ -94,14 +94,18 @@ double lo_chop(double x, double tol) {
 
 }  // namespace
 
+namespace tdg {
+thread_local int64_t *tl_xfer = nullptr;
+}
+
 struct tdg_ctx {
     int device = 0;
+    int64_t xfer[2] = {0, 0};  // host-to-device and device-to-host bytes of calls on this context
     int n_sm = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[10] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-    int32_t *h_tot = nullptr;  // pinned host word pair for the enumeration totals
-    double *h_fn = nullptr, *h_kbuf = nullptr;  // pinned BTE vectors (Fn, Xi.Fbb), grown on demand
-    size_t h_fn_n = 0, h_kbuf_n = 0;
+    int32_t h_tot[2] = {0, 0};  // enumeration totals (a pinned allocation costs more than it saves)
+    std::vector<double> h_kbuf;  // Xi.Fbb of a BTE iteration
     DevBuf<int32_t> d_full_op;
     DevBuf<double> d_op_cart, d_fn;
     // host copy of the problem
@@ -153,7 +157,8 @@ struct tdg_ctx {
     DevBuf<QuartetRec> d_quart;
     DevBuf<unsigned char> d_scr4;
     // BTE buffers
-    DevBuf<double> d_fbb, d_buf;
+    DevBuf<double> d_buf, d_part;
+    DevBuf<float2> d_fbb, d_xi_df;  // F and Xi as double-float pairs for the BTE product
     // state of the last tdg_scattering that the adjoint pass reuses
     PhononDev last_ph{};
     RowsDev last_rows{};
@@ -164,6 +169,7 @@ struct tdg_ctx {
     DevBuf<__nv_bfloat16> d_bmat, d_lnx;
     DevBuf<float2> d_psi, d_lnph;
     bool bmat_ready = false;
+    int xi_fmt = -1;  // d_xi_df holds the current Xi as float pairs (1), floats (0), or nothing (-1)
 
     MeshDev mesh() const {
         MeshDev m;
@@ -294,28 +300,31 @@ void build_rot_table(const tdg_problem *p, int L, std::vector<int32_t> &rot) {
     const int N = p->n_full;
     const int *g = p->grid;
     rot.assign((size_t)p->n_op * N, -1);
-    for (int o = 0; o < p->n_op; ++o) {
+    // one operation per task; (R q)_i = sum_j R_ij g_j / N_j = num / L with |num| < 3 L max(N),
+    // in 32-bit integers
+    parallel_for(p->n_op, [&](int64_t o) {
         const int32_t *R = p->op_recfrac + 9 * o;
+        int32_t *dst = rot.data() + (size_t)o * N;
+        const int m0 = L / g[0], m1 = L / g[1], m2 = L / g[2];
         for (int q = 0; q < N; ++q) {
-            const int gi[3] = {q / (g[1] * g[2]), (q / g[2]) % g[1], q % g[2]};
+            const int gi0 = q / (g[1] * g[2]), gi1 = (q / g[2]) % g[1], gi2 = q % g[2];
             int out[3];
             bool ok = true;
             for (int i = 0; i < 3 && ok; ++i) {
-                // (R q)_i = sum_j R_ij g_j / N_j = num / L
-                int64_t num = 0;
-                for (int j = 0; j < 3; ++j) num += (int64_t)R[i + 3 * j] * gi[j] * (L / g[j]);
-                const int64_t t = num * g[i];
-                if (t % L != 0) {
+                const int num = R[i] * gi0 * m0 + R[i + 3] * gi1 * m1 + R[i + 6] * gi2 * m2;
+                // num / L must be a multiple of 1 / g_i
+                const int step = L / g[i];
+                if (num % step != 0) {
                     ok = false;
                     break;
                 }
-                int64_t v = (t / L) % g[i];
+                int v = (num / step) % g[i];
                 if (v < 0) v += g[i];
-                out[i] = (int)v;
+                out[i] = v;
             }
-            if (ok) rot[(size_t)o * N + q] = (out[0] * g[1] + out[1]) * g[2] + out[2];
+            if (ok) dst[q] = (out[0] * g[1] + out[1]) * g[2] + out[2];
         }
-    }
+    });
 }
 
 }  // namespace
@@ -331,23 +340,24 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
         return set_error(kErrDevice, "no CUDA device available: the GB300 path has no CPU fallback");
     }
     if (device < 0 || device >= ndev) return set_error(kErrParam, "device index out of range");
+    PhaseTimer pt("tdg_create");
     CUDA_TRY(cudaSetDevice(device));
     auto *c = new tdg_ctx();
     c->device = device;
+    XferScope xs(c->xfer);
     auto fail = [&](int code) {
         delete c;
         return code;
     };
-    cudaDeviceProp prop;
-    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return fail(set_error(kErrDevice, "device query failed"));
-    if (prop.major < 10) return fail(set_error(kErrDevice, "device is not Blackwell (sm_100 family required)"));
-    c->n_sm = prop.multiProcessorCount;
+    int major = 0;
+    if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+        return fail(set_error(kErrDevice, "device query failed"));
+    if (major < 10) return fail(set_error(kErrDevice, "device is not Blackwell (sm_100 family required)"));
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
         return fail(set_error(kErrDevice, "stream creation failed"));
     for (auto &x : c->ev)
         if (cudaEventCreate(&x) != cudaSuccess) return fail(set_error(kErrDevice, "event creation failed"));
-    if (cudaMallocHost(&c->h_tot, 2 * sizeof(int32_t)) != cudaSuccess)
-        return fail(set_error(kErrDevice, "pinned allocation failed"));
     c->na = p->n_atom;
     c->n = p->n_mode;
     c->nop = p->n_op;
@@ -378,9 +388,11 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
     for (int i = 0; i < 3; ++i) c->L = c->L / gcd_i(c->L, c->grid[i]) * c->grid[i];
     for (int i = 0; i < 3; ++i) c->lmul[i] = c->L / c->grid[i];
 
+    pt.mark("device and host copies");
     cudaStream_t s = c->stream;
     std::vector<int32_t> rot;
     build_rot_table(p, c->L, rot);
+    pt.mark("rotation table");
     std::vector<int32_t> irr_full0(c->nirr), full_irr0(c->N), irr_ops0((size_t)c->nirr * c->nop, 0);
     for (int i = 0; i < c->nirr; ++i) irr_full0[i] = c->irr_full[i] - 1;
     for (int i = 0; i < c->N; ++i) full_irr0[i] = c->full_irr[i] - 1;
@@ -399,6 +411,7 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
             egvs32[i] = make_float2((float)egvs[i].x, (float)egvs[i].y);
         }
     }
+    pt.mark("eigenvector copies");
     // Force constants sorted by atom block (a1,a2,a3).
     const int na = c->na;
     std::vector<int32_t> blk_ptr3(na * na * na + 1, 0), lv3, abase3;
@@ -496,6 +509,7 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
     }
     chk(c->d_status.alloc(1));
     chk(cudaStreamSynchronize(s));
+    pt.mark("force constants, tables, uploads");
     if (e != cudaSuccess) return fail(set_error(kErrDevice, std::string("upload failed: ") + cudaGetErrorString(e)));
     {
         // Orbit tables: flags, global scan over (q1, q2), fill; representatives per q1.
@@ -512,7 +526,7 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
         chk(launch_orbit_flag(mesh, flag.p, s));
         chk(exclusive_scan_i32(flag.p, scan.p, nflag, tmp.p, s));
         int32_t nrep = 0;
-        chk(cudaMemcpyAsync(&nrep, scan.p + nflag, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        chk(copy_async(&nrep, scan.p + nflag, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         chk(cudaStreamSynchronize(s));
         chk(c->d_orb_rep.alloc(nrep));
         chk(c->d_orb_img.alloc((size_t)nrep * c->nop));
@@ -533,13 +547,14 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
         c->orbits.orb_of = c->d_orb_of.p;
         chk(launch_orbit_fill(mesh, flag.p, scan.p, c->orbits, s));
         std::vector<int32_t> rp(c->nirr + 1);
-        chk(cudaMemcpyAsync(rp.data(), c->d_orb_rep_ptr.p, sizeof(int32_t) * rp.size(), cudaMemcpyDeviceToHost, s));
+        chk(copy_async(rp.data(), c->d_orb_rep_ptr.p, sizeof(int32_t) * rp.size(), cudaMemcpyDeviceToHost, s));
         chk(cudaStreamSynchronize(s));
         if (e != cudaSuccess) return fail(set_error(kErrDevice, std::string("orbit tables: ") + cudaGetErrorString(e)));
         int mx = 0;
         for (int q = 0; q < c->nirr; ++q) mx = std::max(mx, rp[q + 1] - rp[q]);
         c->orbits.max_rep = mx;
     }
+    pt.mark("orbit tables");
     *out = c;
     return kOk;
 }
@@ -550,9 +565,6 @@ extern "C" void tdg_destroy(tdg_ctx *c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (auto &x : c->ev)
         if (x) cudaEventDestroy(x);
-    if (c->h_tot) cudaFreeHost(c->h_tot);
-    if (c->h_fn) cudaFreeHost(c->h_fn);
-    if (c->h_kbuf) cudaFreeHost(c->h_kbuf);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -590,7 +602,7 @@ int check_list(const char *what, int n_row, const int64_t *ptr, const int32_t *l
 
 int read_status(tdg_ctx *c) {
     int32_t st = 0;
-    CUDA_TRY(cudaMemcpyAsync(&st, c->d_status.p, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(copy_async(&st, c->d_status.p, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(cudaStreamSynchronize(c->stream));
     if (st != kDevOk) return set_error(kErrDevice, "device-side index check failed (status " + std::to_string(st) + ")");
     return kOk;
@@ -600,6 +612,7 @@ int read_status(tdg_ctx *c) {
 
 extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *ql, double *linewidth, double *qs_out,
                               double *stats) {
+    XferScope xs(c ? c->xfer : nullptr);
     if (!c || !ql || !linewidth) return set_error(kErrParam, "tdg_scattering: null argument");
     int st = validate_opts(o);
     if (st) return st;
@@ -1012,6 +1025,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     // isotope terms, which the reference adds unsymmetrised, come after it.
     CUDA_TRY(cudaEventRecord(ev[0], s));
     CUDA_TRY(cudaMemsetAsync(c->d_xi.p, 0, sizeof(double) * (size_t)nr * ld, s));
+    c->xi_fmt = -1;
     CUDA_TRY(cudaMemsetAsync(c->d_gamma.p, 0, sizeof(double) * nr, s));
     CUDA_TRY(cudaMemsetAsync(c->d_status.p, 0, sizeof(int32_t), s));
     CUDA_TRY(cudaEventRecord(ev[1], s));
@@ -1022,8 +1036,8 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         CUDA_TRY(exclusive_scan_i32(c->d_nrd.p, c->d_roff.p, nc, c->d_tmp.p, s));
         launches += 1 + 2 * 3;
         int32_t *tot = c->h_tot;
-        CUDA_TRY(cudaMemcpyAsync(&tot[0], c->d_toff.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-        CUDA_TRY(cudaMemcpyAsync(&tot[1], c->d_roff.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(copy_async(&tot[0], c->d_toff.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(copy_async(&tot[1], c->d_roff.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         st = read_status(c);
         if (st) return st;
         ntrip = tot[0];
@@ -1130,8 +1144,8 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         CUDA_TRY(exclusive_scan_i32(c->d_nrd4.p, c->d_roff4.p, nc4, c->d_tmp4.p, s));
         launches += 1 + 2 * 3;
         int32_t *tot = c->h_tot;
-        CUDA_TRY(cudaMemcpyAsync(&tot[0], c->d_qoff.p + nc4, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-        CUDA_TRY(cudaMemcpyAsync(&tot[1], c->d_roff4.p + nc4, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(copy_async(&tot[0], c->d_qoff.p + nc4, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(copy_async(&tot[1], c->d_roff4.p + nc4, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         st = read_status(c);
         if (st) return st;
         nquart = tot[0];
@@ -1184,7 +1198,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     CUDA_TRY(cudaEventRecord(ev[5], s));
     // ---- gamma to host; symmetrize_scatmat on the device meanwhile ----
     std::vector<double> gamma(nr);
-    CUDA_TRY(cudaMemcpyAsync(gamma.data(), c->d_gamma.p, sizeof(double) * nr, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(copy_async(gamma.data(), c->d_gamma.p, sizeof(double) * nr, cudaMemcpyDeviceToHost, s));
     CUDA_TRY(launch_sym_scatmat(mesh, c->orbits, nr, c->d_row_q1.p, c->d_xi.p, s));
     ++launches;
     CUDA_TRY(cudaEventRecord(ev[6], s));
@@ -1268,17 +1282,19 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
 }
 
 extern "C" int tdg_get_xi(tdg_ctx *c, double *xi) {
+    XferScope xs(c ? c->xfer : nullptr);
     if (!c || !xi) return set_error(kErrParam, "tdg_get_xi: null argument");
     if (!c->have_scattering) return set_error(kErrParam, "tdg_get_xi: call tdg_scattering first");
     CUDA_TRY(cudaSetDevice(c->device));
     const size_t cnt = (size_t)c->n_row * c->N * c->n;
-    CUDA_TRY(cudaMemcpyAsync(xi, c->d_xi.p, sizeof(double) * cnt, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(copy_async(xi, c->d_xi.p, sizeof(double) * cnt, cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(cudaStreamSynchronize(c->stream));
     return kOk;
 }
 
 extern "C" int tdg_triplets(tdg_ctx *c, int32_t q1, const int32_t *sample, int64_t n, int32_t *out, int64_t cap,
                             int64_t *written) {
+    XferScope xs(c ? c->xfer : nullptr);
     if (!c || !sample || !out || !written) return set_error(kErrParam, "tdg_triplets: null argument");
     if (q1 < 1 || q1 > c->nirr) return set_error(kErrParam, "tdg_triplets: q1 out of range");
     if (n < 0 || n > (int64_t)1 << 30) return set_error(kErrParam, "tdg_triplets: bad sample length");
@@ -1308,8 +1324,8 @@ extern "C" int tdg_triplets(tdg_ctx *c, int32_t q1, const int32_t *sample, int64
     CUDA_TRY(exclusive_scan_i32(d_nt.p, d_toff.p, nc, d_tmp.p, s));
     CUDA_TRY(exclusive_scan_i32(d_nrd.p, d_roff.p, nc, d_tmp.p, s));
     int32_t tot[2] = {0, 0};
-    CUDA_TRY(cudaMemcpyAsync(&tot[0], d_toff.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(cudaMemcpyAsync(&tot[1], d_roff.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(copy_async(&tot[0], d_toff.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(copy_async(&tot[1], d_roff.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     int st = read_status(c);
     if (st) return st;
     DevBuf<TripletRec> d_trip;
@@ -1328,8 +1344,8 @@ extern "C" int tdg_triplets(tdg_ctx *c, int32_t q1, const int32_t *sample, int64
     std::vector<TripletRec> trip(tot[0]);
     std::vector<int2> red(tot[1]);
     if (tot[0] > 0)
-        CUDA_TRY(cudaMemcpyAsync(trip.data(), d_trip.p, sizeof(TripletRec) * tot[0], cudaMemcpyDeviceToHost, s));
-    if (tot[1] > 0) CUDA_TRY(cudaMemcpyAsync(red.data(), d_red.p, sizeof(int2) * tot[1], cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(copy_async(trip.data(), d_trip.p, sizeof(TripletRec) * tot[0], cudaMemcpyDeviceToHost, s));
+    if (tot[1] > 0) CUDA_TRY(copy_async(red.data(), d_red.p, sizeof(int2) * tot[1], cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
     int64_t w = 0;
     for (const auto &t : trip) {
@@ -1410,6 +1426,7 @@ void symmetrize_kappa(const tdg_ctx *c, double *kappa) {
 
 extern "C" int tdg_kappa(tdg_ctx *c, const tdg_opts *o, int32_t maxiter, double tol, double *kappa_sma,
                          double *kappa_iter, double *fn_out, int32_t *n_iter) {
+    XferScope xs(c ? c->xfer : nullptr);
     if (!c || !kappa_sma || !kappa_iter) return set_error(kErrParam, "tdg_kappa: null argument");
     int st = validate_opts(o);
     if (st) return st;
@@ -1433,40 +1450,38 @@ extern "C" int tdg_kappa(tdg_ctx *c, const tdg_opts *o, int32_t maxiter, double 
         const int64_t ncol = (int64_t)N * n;
         const size_t nfn = (size_t)nirr * n * 3, nbuf = (size_t)nr * 3;
         CUDA_TRY(c->d_fbb.alloc((size_t)ncol * 3));
+        // element format of the Xi.F products: float pairs for FP64 runs, floats for mixed
+        const bool df = o->precision == TDG_PREC_FP64;
+        if (c->xi_fmt != (int)df) {
+            CUDA_TRY(c->d_xi_df.alloc(df ? (size_t)nr * ncol : ((size_t)nr * ncol + 1) / 2));
+            CUDA_TRY(launch_split_xi(c->d_xi.p, (int64_t)nr * ncol, df, c->d_xi_df.p, s));
+            c->xi_fmt = (int)df;
+        }
         CUDA_TRY(c->d_buf.alloc(nbuf));
+        CUDA_TRY(c->d_part.alloc(xi_gemv_part_elems(nr)));
         CUDA_TRY(c->d_fn.alloc(nfn));
         if (c->d_full_op.n == 0) {
             CUDA_TRY(c->d_full_op.upload(c->full_op.data(), N, s));
             CUDA_TRY(c->d_op_cart.upload(c->op_cart.data(), c->op_cart.size(), s));
         }
-        if (c->h_fn_n < nfn) {
-            if (c->h_fn) cudaFreeHost(c->h_fn);
-            c->h_fn = nullptr;
-            c->h_fn_n = 0;
-            CUDA_TRY(cudaMallocHost(&c->h_fn, sizeof(double) * nfn));
-            c->h_fn_n = nfn;
-        }
-        if (c->h_kbuf_n < nbuf) {
-            if (c->h_kbuf) cudaFreeHost(c->h_kbuf);
-            c->h_kbuf = nullptr;
-            c->h_kbuf_n = 0;
-            CUDA_TRY(cudaMallocHost(&c->h_kbuf, sizeof(double) * nbuf));
-            c->h_kbuf_n = nbuf;
-        }
-        const double *buf = c->h_kbuf;
+        c->h_kbuf.resize(nbuf);
+        const double *buf = c->h_kbuf.data();
         std::vector<double> Fnb((size_t)nirr * n * 3);
         std::vector<double> scf(maxiter, 0.0);
         double mixing = 0.95;
+        PhaseTimer pt("tdg_kappa");
         for (int iter = 1; iter <= maxiter; ++iter) {
             iters = iter;
+            pt.mark("host");
             // foldout (kappa.f90:382-404) and the three Xi products (:411-413) on the device;
             // only Fn (n_irr*n*3) goes up and Xi.Fbb (n_row*3) comes back
-            std::memcpy(c->h_fn, Fn.data(), sizeof(double) * nfn);
-            CUDA_TRY(cudaMemcpyAsync(c->d_fn.p, c->h_fn, sizeof(double) * nfn, cudaMemcpyHostToDevice, s));
-            CUDA_TRY(launch_foldout(N, n, c->d_full_op.p, c->d_full_irr.p, c->d_op_cart.p, c->d_fn.p, c->d_fbb.p, s));
-            CUDA_TRY(launch_xi_gemv(c->d_xi.p, nr, ncol, c->d_fbb.p, c->d_buf.p, c->n_sm, s));
-            CUDA_TRY(cudaMemcpyAsync(c->h_kbuf, c->d_buf.p, sizeof(double) * nbuf, cudaMemcpyDeviceToHost, s));
+            CUDA_TRY(copy_async(c->d_fn.p, Fn.data(), sizeof(double) * nfn, cudaMemcpyHostToDevice, s));
+            pt.mark("upload");
+            CUDA_TRY(launch_foldout(N, n, c->d_full_op.p, c->d_full_irr.p, c->d_op_cart.p, c->d_fn.p, df, c->d_fbb.p, s));
+            CUDA_TRY(launch_xi_gemv(c->d_xi_df.p, nr, ncol, df, c->d_fbb.p, c->d_part.p, c->d_buf.p, c->n_sm, s));
+            CUDA_TRY(copy_async(c->h_kbuf.data(), c->d_buf.p, sizeof(double) * nbuf, cudaMemcpyDeviceToHost, s));
             CUDA_TRY(cudaStreamSynchronize(s));
+            pt.mark("foldout, Xi.F and download (device)");
             // applyXi (kappa.f90:407-426)
             std::fill(Fnb.begin(), Fnb.end(), 0.0);
             for (int r = 0; r < nr; ++r) {
@@ -1523,15 +1538,17 @@ extern "C" int tdg_kappa(tdg_ctx *c, const tdg_opts *o, int32_t maxiter, double 
     return kOk;
 }
 
-tdg::CtxView tdg::ctx_view(const tdg_ctx *c) {
+tdg::CtxView tdg::ctx_view(tdg_ctx *c) {
     CtxView v;
     v.device = c->device;
     v.stream = c->stream;
     v.mesh = c->mesh();
+    v.xfer = c->xfer;
     return v;
 }
 
 extern "C" int tdg_set_fc3(tdg_ctx *c, const double *fc3_mwm) {
+    XferScope xs(c ? c->xfer : nullptr);
     if (!c || !fc3_mwm) return set_error(kErrParam, "tdg_set_fc3: null argument");
     if (c->n_fc3 < 1) return set_error(kErrParam, "tdg_set_fc3: the context has no third-order force constants");
     const size_t cnt = (size_t)c->n_fc3 * 27;
@@ -1555,6 +1572,7 @@ extern "C" int tdg_set_fc3(tdg_ctx *c, const double *fc3_mwm) {
 }
 
 extern "C" int tdg_kappa_sma_vjp(tdg_ctx *c, const tdg_opts *o, const double *kappa_bar, double *lw_bar) {
+    XferScope xs(c ? c->xfer : nullptr);
     if (!c || !kappa_bar || !lw_bar) return set_error(kErrParam, "tdg_kappa_sma_vjp: null argument");
     int st = validate_opts(o);
     if (st) return st;
@@ -1602,6 +1620,7 @@ extern "C" int tdg_kappa_sma_vjp(tdg_ctx *c, const tdg_opts *o, const double *ka
 }
 
 extern "C" int tdg_adjoint_fc3(tdg_ctx *c, const tdg_opts *o, const double *lw_bar, double *mwm_bar, double *stats) {
+    XferScope xs(c ? c->xfer : nullptr);
     if (!c || !lw_bar || !mwm_bar) return set_error(kErrParam, "tdg_adjoint_fc3: null argument");
     int st = validate_opts(o);
     if (st) return st;
@@ -1638,8 +1657,7 @@ extern "C" int tdg_adjoint_fc3(tdg_ctx *c, const tdg_opts *o, const double *lw_b
     if (e != cudaSuccess) return set_error(kErrDevice, std::string("allocation failed: ") + cudaGetErrorString(e));
     cudaEvent_t *ev = c->ev;
     CUDA_TRY(cudaEventRecord(ev[0], s));
-    if (!acc_smem || ntrip == 0)
-        CUDA_TRY(cudaMemsetAsync(c->d_slices.p, 0, sizeof(double) * (size_t)std::max(grid, 1) * nm, s));
+    CUDA_TRY(cudaMemsetAsync(c->d_slices.p, 0, sizeof(double) * (size_t)std::max(grid, 1) * nm, s));
     CUDA_TRY(cudaMemsetAsync(c->d_status.p, 0, sizeof(int32_t), s));
     ThreePhArgs a;
     a.mesh = c->mesh();
@@ -1667,9 +1685,9 @@ extern "C" int tdg_adjoint_fc3(tdg_ctx *c, const tdg_opts *o, const double *lw_b
     CUDA_TRY(cudaEventRecord(ev[1], s));
     CUDA_TRY(launch_threephonon_adjoint(a, o->precision, grid, s));
     CUDA_TRY(cudaEventRecord(ev[2], s));
-    CUDA_TRY(launch_sum_slices(c->d_slices.p, o->precision, std::max(grid, 1), nm, c->d_mwm_bar.p, s));
+    CUDA_TRY(launch_sum_slices(c->d_slices.p, std::max(grid, 1), nm, c->d_mwm_bar.p, s));
     std::vector<double> dev(nm);
-    CUDA_TRY(cudaMemcpyAsync(dev.data(), c->d_mwm_bar.p, sizeof(double) * nm, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(copy_async(dev.data(), c->d_mwm_bar.p, sizeof(double) * nm, cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaEventRecord(ev[3], s));
     CUDA_TRY(cudaStreamSynchronize(s));
     st = read_status(c);
@@ -1687,5 +1705,12 @@ extern "C" int tdg_adjoint_fc3(tdg_ctx *c, const tdg_opts *o, const double *lw_b
         stats[2] = ntrip;
         stats[3] = grid;
     }
+    return kOk;
+}
+
+extern "C" int tdg_transfer_bytes(tdg_ctx *c, int64_t *h2d, int64_t *d2h) {
+    if (!c) return set_error(kErrParam, "tdg_transfer_bytes: null context");
+    if (h2d) *h2d = c->xfer[0];
+    if (d2h) *d2h = c->xfer[1];
     return kOk;
 }

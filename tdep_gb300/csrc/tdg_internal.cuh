@@ -9,6 +9,26 @@ struct tdg_ctx;
 
 namespace tdg {
 
+// Host<->device byte counter of the context whose entry point runs on this thread
+// ([0] host to device, [1] device to host); XferScope sets it for the span of a call.
+extern thread_local int64_t *tl_xfer;
+
+struct XferScope {
+    int64_t *prev;
+    explicit XferScope(int64_t *counter) : prev(tl_xfer) { tl_xfer = counter; }
+    ~XferScope() { tl_xfer = prev; }
+};
+
+// cudaMemcpyAsync that adds host<->device bytes to the active counter.
+inline cudaError_t copy_async(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind, cudaStream_t s) {
+    if (tl_xfer) {
+        if (kind == cudaMemcpyHostToDevice) tl_xfer[0] += (int64_t)bytes;
+        if (kind == cudaMemcpyDeviceToHost) tl_xfer[1] += (int64_t)bytes;
+    }
+    return cudaMemcpyAsync(dst, src, bytes, kind, s);
+}
+
+
 // Work item of the three-phonon kernel: one accepted irreducible q-triplet.
 struct TripletRec {
     int32_t q1;       // irreducible index of q1 (0-based)
@@ -124,7 +144,7 @@ struct ThreePhArgs {
     // adjoint only: cotangent of each row's Gamma and one accumulation slice of
     // d L / d mwm ([fc.n * 27]) per CTA
     const double *lam;
-    double *mwm_bar;            // FP64 slices, or float2 (sum, correction) on the mixed path
+    double *mwm_bar;            // FP64 slices, zeroed before the launch
     int32_t acc_in_smem;        // accumulate the CTA's slice in shared memory, store it once
 };
 cudaError_t launch_threephonon(const ThreePhArgs &a, int precision, int n_sm, cudaStream_t s);
@@ -132,10 +152,8 @@ cudaError_t launch_threephonon(const ThreePhArgs &a, int precision, int n_sm, cu
 // accumulates 2 Re(phase * Q) into a.mwm_bar (one slice per CTA of the returned grid).
 int threephonon_adjoint_grid(int n, int precision, int n_sm, int n_trip, int n_fc, bool acc_in_smem);
 cudaError_t launch_threephonon_adjoint(const ThreePhArgs &a, int precision, int grid, cudaStream_t s);
-// out[e] = sum over g < n_slice of slices[g * n + e], in slice order; the slices hold FP64
-// (precision 0) or compensated FP32 pairs (mixed), 8 bytes per entry either way.
-cudaError_t launch_sum_slices(const void *slices, int precision, int32_t n_slice, int64_t n, double *out,
-                              cudaStream_t s);
+// out[e] = sum over g < n_slice of slices[g * n + e], in slice order.
+cudaError_t launch_sum_slices(const double *slices, int32_t n_slice, int64_t n, double *out, cudaStream_t s);
 size_t threephonon_smem_bytes(int n, int precision, int n_fc);
 
 struct FourPhArgs {
@@ -219,26 +237,33 @@ cudaError_t launch_build_candidates(const int4 *desc, int32_t n_irr, int32_t max
 // K5b: symmetrize_scatmat (scattering.f90:296-357).
 cudaError_t launch_sym_scatmat(const MeshDev &m, const OrbitDev &o, int32_t n_row, const int32_t *row_q1, double *xi,
                                cudaStream_t s);
-// K8: buf[r*3+a] = sum_j xi[r, j] * fbb[j*3 + a].
-cudaError_t launch_xi_gemv(const double *xi, int32_t n_row, int64_t n_col, const double *fbb, double *buf,
-                           int n_sm, cudaStream_t s);
+// K8: buf[r*3+a] = sum_j xi[r, j] * fbb[j*3 + a] on the FP32 pipe; xi and fbb as (hi, lo)
+// float pairs accumulated in double-float when df (FP64 runs), else as floats with FMA chains
+// added into double-float accumulators (mixed precision). launch_split_xi converts the FP64
+// Xi; part: xi_gemv_part_elems(n_row) doubles.
+cudaError_t launch_split_xi(const double *xi, int64_t n, bool df, void *out, cudaStream_t s);
+size_t xi_gemv_part_elems(int32_t n_row);
+cudaError_t launch_xi_gemv(const void *xi, int32_t n_row, int64_t n_col, bool df, const void *fbb, double *part,
+                           double *buf, int n_sm, cudaStream_t s);
 
 // One-tile tcgen05 self-check: d (128 x n) = a (128 x 16) b (16 x n) through BF16 hi/lo
 // splits; variant selects the operand layout reading (diagnostic).
 cudaError_t launch_mma_check(int variant, int n, const float *a, const float *b, float *d, int *status,
                              cudaStream_t s);
 
-// foldout of the BTE: fbb[(q*n + b)*3 + d] = sign * (R fn[(irr(q)*n + b)*3 ..])_d with
-// full_op signed 1-based operations (negative: time reversal) and full_irr 0-based.
+// foldout of the BTE: fbb[(q*n + b)*3 + d] = sign * (R fn[(irr(q)*n + b)*3 ..])_d, with
+// full_op signed 1-based operations (negative: time reversal) and full_irr 0-based; stored
+// as (hi, lo) float pairs when df, else as floats (the Xi.F element format).
 cudaError_t launch_foldout(int32_t n_full, int32_t n_mode, const int32_t *full_op, const int32_t *full_irr,
-                           const double *op_cart, const double *fn, double *fbb, cudaStream_t s);
+                           const double *op_cart, const double *fn, bool df, void *fbb, cudaStream_t s);
 
 // What an entry point compiled outside the context's own file needs of a context.
 struct CtxView {
     int device;
     cudaStream_t stream;
     MeshDev mesh;
+    int64_t *xfer;  // the context's transfer counter
 };
-CtxView ctx_view(const tdg_ctx *c);
+CtxView ctx_view(tdg_ctx *c);
 
 }  // namespace tdg

@@ -110,6 +110,7 @@ extern "C" int tdg_triplets_static(tdg_ctx *c, int32_t q1, const int32_t *sample
         return set_error(kErrParam, "tdg_triplets_static: sample of " + std::to_string(n) +
                                         " q-points exceeds the static scratch limit of " + std::to_string(kMaxSample));
     const CtxView v = ctx_view(c);
+    XferScope xs(v.xfer);
     if (q1 < 1 || q1 > v.mesh.n_irr) return set_error(kErrParam, "tdg_triplets_static: q1 out of range");
     for (int64_t i = 0; i < n; ++i)
         if (sample[i] < 1 || sample[i] > v.mesh.n_full)
@@ -135,16 +136,16 @@ extern "C" int tdg_triplets_static(tdg_ctx *c, int32_t q1, const int32_t *sample
     int32_t *d_out = reinterpret_cast<int32_t *>(base + kOffOut);
 
     CUDA_TRY(cudaMemsetAsync(d_status, 0, sizeof(int32_t), s));
-    CUDA_TRY(cudaMemcpyAsync(d_sample, sample, sizeof(int32_t) * nc, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(copy_async(d_sample, sample, sizeof(int32_t) * nc, cudaMemcpyHostToDevice, s));
     k_sample_candidates<<<(nc + 255) / 256, 256, 0, s>>>(q1 - 1, d_sample, nc, d_cand);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(launch_triplet_count(v.mesh, d_cand, nc, d_nt, d_nrd, d_status, s));
     CUDA_TRY(exclusive_scan_i32(d_nt, d_toff, nc, d_tmp, s));
     CUDA_TRY(exclusive_scan_i32(d_nrd, d_roff, nc, d_tmp, s));
     int32_t h[3] = {0, 0, 0};
-    CUDA_TRY(cudaMemcpyAsync(&h[0], d_toff + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(cudaMemcpyAsync(&h[1], d_roff + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(cudaMemcpyAsync(&h[2], d_status, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(copy_async(&h[0], d_toff + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(copy_async(&h[1], d_roff + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(copy_async(&h[2], d_status, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
     if (h[2] != kDevOk)
         return set_error(kErrDevice, "device-side index check failed (status " + std::to_string(h[2]) + ")");
@@ -158,7 +159,7 @@ extern "C" int tdg_triplets_static(tdg_ctx *c, int32_t q1, const int32_t *sample
     if (h[0] > 0) {
         k_format_triplets<<<(h[0] + 127) / 128, 128, 0, s>>>(d_trip, h[0], d_red, d_out);
         CUDA_TRY(cudaGetLastError());
-        CUDA_TRY(cudaMemcpyAsync(out, d_out, sizeof(int32_t) * w, cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(copy_async(out, d_out, sizeof(int32_t) * w, cudaMemcpyDeviceToHost, s));
     }
     CUDA_TRY(cudaStreamSynchronize(s));
     *written = w;

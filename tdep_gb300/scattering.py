@@ -322,6 +322,12 @@ class ScatteringRates:
         N.check(self._lib.tdg_get_xi(self._ctx, N.ptr(xi, C.c_double)), "tdg_get_xi")
         return xi
 
+    def transfer_bytes(self) -> tuple[int, int]:
+        """(host-to-device, device-to-host) bytes copied by this object's calls so far."""
+        h, d = C.c_int64(0), C.c_int64(0)
+        N.check(self._lib.tdg_transfer_bytes(self._ctx, C.byref(h), C.byref(d)), "tdg_transfer_bytes")
+        return int(h.value), int(d.value)
+
     def kappa(self, opts: Options, maxiter: int | None = None, tol: float | None = None):
         """get_kappa (SMA), iterative_solution, symmetrize_kappa. Returns a.u. 3x3 tensors."""
         p = self.prob

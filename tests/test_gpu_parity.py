@@ -291,6 +291,31 @@ def test_repeat_calls_are_stable(configs):
     np.testing.assert_allclose(ka, kb, rtol=1e-12, atol=0)
 
 
+def test_transfer_counter_counts_the_copies(configs):
+    """tdg_transfer_bytes: a Xi download adds exactly its size; once the first kappa call has
+    uploaded the symmetry tables, a BTE iteration is one Fn upload and one Xi.F download."""
+    prob = Problem.load(configs["rocksalt"], (6, 6, 6), readiso=True)
+    opts = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=9)
+    lists = QLists.monte_carlo(prob, opts)
+    sr = ScatteringRates(prob)
+    h0, d0 = sr.transfer_bytes()
+    assert h0 > prob.egv.nbytes and d0 >= 0
+    sr.generate(opts, lists)
+    h1, d1 = sr.transfer_bytes()
+    assert h1 > h0 and d1 >= d0 + lists.n_row * 8
+    xi = sr.Xi
+    h2, d2 = sr.transfer_bytes()
+    assert (h2, d2) == (h1, d1 + xi.nbytes)
+    n = prob.n_mode
+    sr.kappa(opts, maxiter=1, tol=0.0)
+    h2, d2 = sr.transfer_bytes()
+    sr.kappa(opts, maxiter=1, tol=0.0)
+    h3, d3 = sr.transfer_bytes()
+    assert h3 - h2 == prob.n_irr * n * 3 * 8
+    assert d3 - d2 == lists.n_row * 3 * 8
+    sr.close()
+
+
 def test_fp64_reference_mgo_fixture(built):
     """The reference's own MgO inputs (tests/infiles of the reference; polar long-range
     term not applied) through both paths, 5x5x5 mesh as in the reference's test."""
