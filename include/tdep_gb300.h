@@ -96,6 +96,18 @@ typedef struct tdg_problem {
     const int32_t *fc4_lv;     /* [n_fc4*9] lv2, lv3, lv4, integer fractional                */
     const double *fc4_lvcart;  /* [n_fc4*9] lv2, lv3, lv4 Cartesian, Bohr                    */
     const double *fc4_mwm;     /* [n_fc4*81] mwm(i,j,k,l) at i + 3j + 9k + 27l               */
+    /* off-diagonal (coherence) kappa, get_kappa_offdiag (kappa.f90:77-306); only
+       tdg_kappa_offdiag reads these, and they may be NULL when it is not called            */
+    const double *irr_dyngrad; /* [n_irr*3*n_mode*n_mode*2] gradient of the mass-weighted
+                                  dynamical matrix at the irreducible points
+                                  (fc%dynamicalmatrix(..., dynamical_matrix_gradient), d/d(2*pi*q),
+                                  Cartesian): element (r, c) of direction x of point i at
+                                  (((i*3 + x)*n_mode + c)*n_mode + r)*2 (+1 imaginary part)       */
+    const int32_t *op_fmap;    /* [n_op*n_atom] op%fmap: operation o takes atom a onto atom
+                                  op_fmap[o*n_atom + a] (1-based)                                */
+    const double *atom_shift;  /* [n_op*n_atom*3] lattice vector op^-1(r(fmap(a)) - tr) - r(a),
+                                  Cartesian Bohr (the v0 of lo_eigenvector_transformation_matrix,
+                                  type_symmetryoperation.f90:243-290)                           */
 } tdg_problem;
 
 /* The hot-path subset of lo_opts (src/thermal_conductivity/options.f90). */
@@ -270,6 +282,19 @@ int tdg_adjoint_fc3(tdg_ctx *ctx, const tdg_opts *opts, const double *lw_bar, do
  */
 int tdg_kappa(tdg_ctx *ctx, const tdg_opts *opts, int32_t maxiter, double tol,
               double *kappa_sma, double *kappa_iter, double *fn_out, int32_t *n_iter);
+
+/*
+ * Off-diagonal (coherence) thermal conductivity, get_kappa_offdiag (kappa.f90:77-306)
+ * followed by symmetrize_kappa (main.f90:243), from the linewidths of the last
+ * tdg_scattering: per irreducible point the off-diagonal group velocities
+ * Re <e_i|dD/dq|e_j> / (2 sqrt(w_i w_j)) averaged over the little group with the eigenvector
+ * transformation matrices, rotated over the star, and summed with the Lorentzian
+ * (G_i + G_j) / ((G_i + G_j)^2 + (w_i - w_j)^2). Needs irr_dyngrad, op_fmap and atom_shift
+ * in the problem given to tdg_create. kappa_offdiag: 3x3 column-major, atomic units.
+ * The reference keeps only the real part of each velocity matrix element, which depends on
+ * the phases of the eigenvectors: the result is that formula on the problem's eigenvectors.
+ */
+int tdg_kappa_offdiag(tdg_ctx *ctx, const tdg_opts *opts, double *kappa_offdiag);
 
 /*
  * Host stage of thermal_conductivity (main.f90:42-181) for the C++ driver and tests:

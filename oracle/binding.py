@@ -51,6 +51,7 @@ def lib():
                                             P(C.c_double), P(C.c_double), P(C.c_double), P(C.c_double)]
         L.orc_kappa.argtypes = [P(N.TdgProblem), P(N.TdgOpts), P(N.TdgQlists), P(C.c_double), P(C.c_double),
                                 P(C.c_double), C.c_int, C.c_double, P(C.c_double), P(C.c_double), P(C.c_int32)]
+        L.orc_kappa_offdiag.argtypes = [P(N.TdgProblem), P(N.TdgOpts), P(C.c_double), P(C.c_double)]
         _L = L
     return _L
 
@@ -174,6 +175,16 @@ def kappa(prob, opts, lists, xi, qs, f0, maxiter: int, tol: float):
                     N.ptr(f0, C.c_double), int(maxiter), float(tol), N.ptr(ks, C.c_double), N.ptr(ki, C.c_double),
                     C.byref(nit))
     return ks.reshape(3, 3, order="F"), ki.reshape(3, 3, order="F"), nit.value
+
+
+def kappa_offdiag(prob, opts, linewidth):
+    """get_kappa_offdiag + symmetrize_kappa (kappa.f90:77-306, main.f90:243) from the given
+    irreducible-point linewidths ([n_irr, n_mode]); a.u. 3x3."""
+    lw = np.ascontiguousarray(linewidth, np.float64).reshape(-1)
+    out = np.zeros(9)
+    ps, os_ = prob.struct(), opts.struct(prob.grid)
+    lib().orc_kappa_offdiag(C.byref(ps), C.byref(os_), N.ptr(lw, C.c_double), N.ptr(out, C.c_double))
+    return out.reshape(3, 3, order="F")
 
 
 def adjoint_fc3(prob, opts, lists, lw_bar, nthreads: int = 0):

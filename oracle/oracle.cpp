@@ -12,7 +12,8 @@
 //   src/thermal_conductivity/scattering_isotope.f90:1-91
 //   src/thermal_conductivity/scattering_threephonon.f90:2-448
 //   src/thermal_conductivity/scattering_fourphonon.f90:2-506
-//   src/thermal_conductivity/kappa.f90:28-75, 308-495
+//   src/thermal_conductivity/kappa.f90:28-75, 77-306, 308-495
+//   src/libolle/type_symmetryoperation.f90:243-290 (eigenvector transformation matrix)
 //   src/libolle/type_qpointmesh_gridgeneration.f90:612-662 (on-grid test, index)
 //   src/libolle/gottochblandat_calculus.f90:268-288 (lo_gauss)
 //   src/libolle/gottochblandat_physics.f90:160-186, 331-366 (planck, cv)
@@ -1093,6 +1094,129 @@ int orc_scattering_finish(const tdg_problem *p, const tdg_opts *o, const tdg_qli
 }
 
 // get_kappa (SMA with Fn = F0), iterative_solution and symmetrize_kappa.
+// get_kappa_offdiag (kappa.f90:77-306) with the n^2 x n^2 Kronecker sum of eigenvector
+// products (:171-197) and its product with the flattened dD/dq (:146-158, 200), then
+// symmetrize_kappa as main.f90:243 applies it. The problem carries the mass-weighted
+// gradient; the reference divides it by invsqrtmass(a1)*invsqrtmass(a2) (:156) and multiplies
+// the rotated eigenvectors by invsqrtmass(a) (:180-186), factors that cancel and are left out.
+int orc_kappa_offdiag(const tdg_problem *p, const tdg_opts *o, const double *linewidth, double *kappa_offdiag) {
+    Ctx c;
+    c.init(p);
+    const int n = c.n, na = p->n_atom, nn = n * n;
+    const double T = o->temperature;
+    const bool classical = o->classical != 0;
+    const double chop_tol = 1E-10 / ((0.52917721067E-10 / kHbarHartree) / 1000.0);
+    double kap[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    std::vector<cplx> cm1((size_t)nn * 3), cm2((size_t)nn * 3), kron((size_t)nn * nn), gm((size_t)nn), egw((size_t)nn);
+    std::vector<double> vel((size_t)nn * 3), velsq((size_t)nn * 9);
+    for (int iq = 1; iq <= p->n_irr; ++iq) {
+        const int f = c.irr_full(iq);
+        const double *qv = p->q_full + (size_t)(f - 1) * 3;
+        const double *grad = p->irr_dyngrad + (size_t)(iq - 1) * 3 * nn * 2;
+        // flatten the gradient: cm1((Q-1)*n + P, iz) = grad(Q, P, iz)
+        for (int iz = 0; iz < 3; ++iz)
+            for (int a1 = 1; a1 <= na; ++a1)
+                for (int a2 = 1; a2 <= na; ++a2)
+                    for (int ix = 1; ix <= 3; ++ix)
+                        for (int iy = 1; iy <= 3; ++iy) {
+                            const int ib = (a1 - 1) * 3 + ix, ia = (a2 - 1) * 3 + iy;
+                            const int ic = (ia - 1) * n + ib;
+                            const size_t g = ((size_t)iz * nn + (size_t)(ib - 1) * n + (ia - 1)) * 2;
+                            cm1[(size_t)iz * nn + ic - 1] = cplx(grad[g], grad[g + 1]);
+                        }
+        std::fill(kron.begin(), kron.end(), cplx(0, 0));
+        const int nop = p->irr_nop[iq - 1];
+        for (int k = 1; k <= nop; ++k) {
+            const int iop = p->irr_ops[(size_t)(iq - 1) * p->n_op + k - 1];
+            const int o0 = std::abs(iop) - 1;
+            const double *m = p->op_cart + 9 * o0;
+            std::fill(gm.begin(), gm.end(), cplx(0, 0));
+            for (int a2 = 1; a2 <= na; ++a2) {
+                const int a1 = p->op_fmap[(size_t)o0 * na + a2 - 1];
+                const double *v0 = p->atom_shift + ((size_t)o0 * na + a2 - 1) * 3;
+                const double iqvv = -(v0[0] * qv[0] + v0[1] * qv[1] + v0[2] * qv[2]) * kTwoPi;
+                const cplx e(std::cos(iqvv), std::sin(iqvv));
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) gm[(size_t)((a2 - 1) * 3 + j) * n + (a1 - 1) * 3 + i] = m[i + 3 * j] * e;
+            }
+            // egw = gm * egv (columns are modes), conjugated for time-reversed operations
+            for (int b = 1; b <= n; ++b)
+                for (int r = 0; r < n; ++r) {
+                    cplx s = 0;
+                    for (int cc = 0; cc < n; ++cc) s += gm[(size_t)cc * n + r] * c.egv(f, b, cc);
+                    egw[(size_t)(b - 1) * n + r] = iop < 0 ? std::conj(s) : s;
+                }
+            for (int b = 1; b <= n; ++b) {
+                const double om = c.omega(f, b);
+                for (int r = 0; r < n; ++r)
+                    egw[(size_t)(b - 1) * n + r] = om > kFreqTol ? egw[(size_t)(b - 1) * n + r] / std::sqrt(om * 2.0) : 0.0;
+            }
+            for (int i = 1; i <= n; ++i)
+                for (int j = 1; j <= n; ++j) {
+                    const cplx cj = std::conj(egw[(size_t)(i - 1) * n + j - 1]);  // conjg(buf_egw(j, i))
+                    for (int ii = 1; ii <= n; ++ii)
+                        for (int jj = 1; jj <= n; ++jj) {
+                            const int ia = (i - 1) * n + ii, ib = (j - 1) * n + jj;
+                            kron[(size_t)(ib - 1) * nn + ia - 1] += egw[(size_t)(ii - 1) * n + jj - 1] * cj;
+                        }
+                }
+        }
+        for (auto &x : kron) x /= (double)nop;
+        for (int iz = 0; iz < 3; ++iz)
+            for (int ia = 0; ia < nn; ++ia) {
+                cplx s = 0;
+                for (int ib = 0; ib < nn; ++ib) s += kron[(size_t)ib * nn + ia] * cm1[(size_t)iz * nn + ib];
+                cm2[(size_t)iz * nn + ia] = s;
+            }
+        for (int i = 1; i <= n; ++i)
+            for (int j = 1; j <= n; ++j)
+                for (int iz = 0; iz < 3; ++iz) {
+                    double re = cm2[(size_t)iz * nn + (size_t)(i - 1) * n + j - 1].real();
+                    if (std::fabs(re) < chop_tol) re = 0.0;
+                    vel[((size_t)(i - 1) * n + j - 1) * 3 + iz] = re;
+                }
+        std::fill(velsq.begin(), velsq.end(), 0.0);
+        int nstar = 0;
+        for (int fq = 1; fq <= c.N; ++fq) {
+            if (p->full_irr[fq - 1] != iq) continue;
+            ++nstar;
+            const double *m = p->op_cart + 9 * (std::abs(p->full_op[fq - 1]) - 1);
+            for (size_t ij = 0; ij < (size_t)nn; ++ij) {
+                const double *v0 = &vel[ij * 3];
+                double v1[3];
+                for (int x = 0; x < 3; ++x) v1[x] = m[x] * v0[0] + m[x + 3] * v0[1] + m[x + 6] * v0[2];
+                for (int x = 0; x < 3; ++x)
+                    for (int y = 0; y < 3; ++y) velsq[ij * 9 + x + 3 * y] += v1[x] * v1[y];
+            }
+        }
+        for (auto &x : velsq) x /= (double)nstar;
+        const double pref = p->irr_weight[iq - 1] / p->volume;
+        for (int jm = 1; jm <= n; ++jm) {
+            const double om1 = c.omega(f, jm);
+            if (om1 < kFreqTol) continue;
+            const double tau1 = linewidth[(size_t)(iq - 1) * n + jm - 1];
+            if (tau1 < kFreqTol) continue;
+            for (int km = 1; km <= n; ++km) {
+                if (jm == km) continue;
+                const double om2 = c.omega(f, km);
+                if (om2 < kFreqTol) continue;
+                const double tau2 = linewidth[(size_t)(iq - 1) * n + km - 1];
+                if (tau2 < kFreqTol) continue;
+                const double f0 = classical ? kKbHartree : 0.5 * (lo_cv(T, om1) + lo_cv(T, om2));
+                const double tau = (tau1 + tau2) / ((tau1 + tau2) * (tau1 + tau2) + (om1 - om2) * (om1 - om2));
+                const double *vs = &velsq[((size_t)(jm - 1) * n + km - 1) * 9];
+                for (int k = 0; k < 9; ++k) kap[k] += vs[k] * tau * f0 * pref;
+            }
+        }
+    }
+    double tol = 0;
+    for (int k = 0; k < 9; ++k) tol += std::fabs(kap[k]);
+    for (int k = 0; k < 9; ++k) kap[k] = lo_chop(kap[k], tol * 1e-6);
+    symmetrize_kappa(p, kap);
+    std::memcpy(kappa_offdiag, kap, sizeof(kap));
+    return 0;
+}
+
 int orc_kappa(const tdg_problem *p, const tdg_opts *o, const tdg_qlists *ql, const double *xi, const double *qs,
               const double *F0, int maxiter, double tol, double *kappa_sma, double *kappa_iter, int32_t *n_iter) {
     Ctx c;

@@ -69,6 +69,9 @@ class TdgProblem(C.Structure):
         ("fc4_lv", _i32p),
         ("fc4_lvcart", _f64p),
         ("fc4_mwm", _f64p),
+        ("irr_dyngrad", _f64p),
+        ("op_fmap", _i32p),
+        ("atom_shift", _f64p),
     ]
 
 
@@ -117,6 +120,7 @@ SIGNATURES = {
     "tdg_scattering": (C.c_int, [C.c_void_p, C.POINTER(TdgOpts), C.POINTER(TdgQlists), _f64p, _f64p, _f64p]),
     "tdg_get_xi": (C.c_int, [C.c_void_p, _f64p]),
     "tdg_transfer_bytes": (C.c_int, [C.c_void_p, _i64p, _i64p]),
+    "tdg_kappa_offdiag": (C.c_int, [C.c_void_p, C.POINTER(TdgOpts), _f64p]),
     "tdg_triplets": (C.c_int, [C.c_void_p, C.c_int32, _i32p, C.c_int64, _i32p, C.c_int64, _i64p]),
     "tdg_triplets_static": (C.c_int, [C.c_void_p, C.c_int32, _i32p, C.c_int64, _i32p, C.c_int64, _i64p]),
     "tdg_set_fc3": (C.c_int, [C.c_void_p, _f64p]),

@@ -10,6 +10,7 @@ namespace {
 
 constexpr double kSqrt2PiInv = 0.398942280401433;
 constexpr double kFreqTolD = 1E-9;
+constexpr double kTwoPiD = 6.283185307179586;
 constexpr int kMaxRed = 192;
 
 template <typename R>

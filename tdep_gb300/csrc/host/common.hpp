@@ -40,6 +40,7 @@ constexpr double kFc4EvAToHaBohr = kEvToHartree / (kAToBohr * kAToBohr * kAToBoh
 constexpr double kFreqHartreeToTHz = 1E-12 / kTwoPi / kHbarHartree;
 constexpr double kFreqTHzToHartree = 1.0 / kFreqHartreeToTHz;
 constexpr double kKappaAuToSI = kHartreeToJoule / kTimeAuToS / kBohrToM;
+constexpr double kGroupVelAuToMs = kBohrToM / kTimeAuToS;  // lo_groupvel_Hartreebohr_to_ms
 constexpr double kMToBohr = 1.0 / kBohrToM;
 
 // ---- tolerances (konstanter.f90:113-140) ----

@@ -399,4 +399,35 @@ int read_fc4(const std::string &path, const Crystal &c, FC4 &fc) {
     return kOk;
 }
 
+int op_atom_maps(const Crystal &c, std::vector<int32_t> &fmap, std::vector<double> &shift) {
+    const int na = c.na, no = (int)c.ops.size();
+    fmap.assign((size_t)no * na, -1);
+    shift.assign((size_t)no * na * 3, 0.0);
+    for (int o = 0; o < no; ++o) {
+        const SymOp &op = c.ops[o];
+        M3 W;
+        for (int k = 0; k < 9; ++k) W.a[k] = op.fm[k];
+        const M3 Wi = inverse(W);
+        for (int a = 0; a < na; ++a) {
+            const V3 img = mul(W, c.frac[a]);
+            int hit = -1;
+            for (int b = 0; b < na && hit < 0; ++b) {
+                if (c.species[b] != c.species[a]) continue;
+                V3 d;
+                for (int i = 0; i < 3; ++i) d[i] = img[i] + op.tr[i] - c.frac[b][i];
+                if (frac_dist(c, d) < 1e-4) hit = b;
+            }
+            if (hit < 0) return set_error(kErrSymmetry, "an operation does not map the crystal onto itself");
+            fmap[(size_t)o * na + a] = hit;
+            V3 u;
+            for (int i = 0; i < 3; ++i) u[i] = c.frac[hit][i] - op.tr[i];
+            V3 v = mul(Wi, u);
+            for (int i = 0; i < 3; ++i) v[i] = anint(v[i] - c.frac[a][i]);
+            const V3 w = c.frac_to_cart(v);
+            for (int i = 0; i < 3; ++i) shift[((size_t)o * na + a) * 3 + i] = w[i];
+        }
+    }
+    return kOk;
+}
+
 }  // namespace tdg

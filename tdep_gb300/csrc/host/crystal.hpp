@@ -41,6 +41,12 @@ int read_isotopes(const std::string &path, Crystal &c);
 // itself with some fractional translation. Identity first.
 int find_symmetry(Crystal &c);
 
+// Atom maps of the operations (op%fmap, type_symmetryoperation.f90:811-900): operation o
+// takes atom a onto atom fmap[o*na + a] (0-based), and shift[o*na + a] is the lattice vector
+// op^-1(r(fmap(a)) - tr) - r(a) in Cartesian Bohr, the vector whose phase enters
+// lo_eigenvector_transformation_matrix (type_symmetryoperation.f90:243-290).
+int op_atom_maps(const Crystal &c, std::vector<int32_t> &fmap, std::vector<double> &shift);
+
 struct FC2Pair {
     int a1, a2;        // 0-based
     V3 lv;             // Cartesian lattice vector, Bohr
@@ -100,6 +106,11 @@ struct Phonons {
 // D(q) (type_forceconstant_secondorder_dynamicalmatrix.f90:484-788), Hermitian
 // diagonalisation, group velocities and degeneracy tables at every mesh point.
 int build_phonons(const Crystal &c, const FC2 &fc, const QMesh &qp, Phonons &ph);
+
+// Gradient of the mass-weighted dynamical matrix at the Cartesian point q (1/Bohr without
+// 2*pi, as QMesh::q_full) (type_forceconstant_secondorder_dynamicalmatrix.f90:484-788,
+// non-polar branch), derivative with respect to 2*pi*q: g[(x*nb + c)*nb + r] = dD(r, c)/dq_x.
+void dyn_gradient(const Crystal &c, const FC2 &fc, const V3 &qr, int nb, cplx *g);
 
 // Complex Hermitian Jacobi eigensolver: a is n x n column-major, overwritten.
 // Eigenvalues unsorted in w, eigenvectors as columns of v.

@@ -78,15 +78,16 @@ namespace {
 
 double negsqrt(double x) { return x >= 0 ? std::sqrt(x) : -std::sqrt(-x); }
 
-int solve_point(const Crystal &c, const FC2 &fc, const V3 &qr, int nb, double *omega, double *egv,
-                double *vel) {
-    // D((a2,j),(a1,i)) = sum_pairs exp(i q.R) m(i,j) / sqrt(m1 m2), q with 2*pi.
+// D((a2,j),(a1,i)) = sum_pairs exp(i q.R) m(i,j) / sqrt(m1 m2) and its q gradient G, q
+// with 2*pi; D and G column-major, G direction-major.
+void dyn_matrix(const Crystal &c, const FC2 &fc, const V3 &qr, int nb, cplx *D, cplx *G) {
     V3 qv;
     for (int d = 0; d < 3; ++d) {
         qv[d] = qr[d] * kTwoPi;
         if (std::fabs(qv[d]) < 1e-13) qv[d] = 0.0;
     }
-    std::vector<cplx> D((size_t)nb * nb, 0.0), G((size_t)3 * nb * nb, 0.0);
+    std::fill(D, D + (size_t)nb * nb, cplx(0, 0));
+    std::fill(G, G + (size_t)3 * nb * nb, cplx(0, 0));
     for (const auto &p : fc.pairs) {
         const double qdotr = p.lv[0] * qv[0] + p.lv[1] * qv[1] + p.lv[2] * qv[2];
         const cplx e(std::cos(qdotr), std::sin(qdotr));
@@ -99,6 +100,12 @@ int solve_point(const Crystal &c, const FC2 &fc, const V3 &qr, int nb, double *o
                 for (int d = 0; d < 3; ++d) G[(size_t)d * nb * nb + ii + (size_t)nb * jj] += cplx(0, p.lv[d]) * val;
             }
     }
+}
+
+int solve_point(const Crystal &c, const FC2 &fc, const V3 &qr, int nb, double *omega, double *egv,
+                double *vel) {
+    std::vector<cplx> D((size_t)nb * nb), G((size_t)3 * nb * nb);
+    dyn_matrix(c, fc, qr, nb, D.data(), G.data());
     // Hermitise against rounding before diagonalising.
     for (int i = 0; i < nb; ++i)
         for (int j = i; j < nb; ++j) {
@@ -193,6 +200,11 @@ int solve_point(const Crystal &c, const FC2 &fc, const V3 &qr, int nb, double *o
 }
 
 }  // namespace
+
+void dyn_gradient(const Crystal &c, const FC2 &fc, const V3 &qr, int nb, cplx *g) {
+    std::vector<cplx> D((size_t)nb * nb);
+    dyn_matrix(c, fc, qr, nb, D.data(), g);
+}
 
 int build_phonons(const Crystal &c, const FC2 &fc, const QMesh &qp, Phonons &ph) {
     const int nb = 3 * c.na;

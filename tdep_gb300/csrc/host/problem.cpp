@@ -81,6 +81,8 @@ struct ProblemHolder {
     std::vector<double> op_cart;
     std::vector<int32_t> op_recfrac;
     std::vector<double> q_full;
+    std::vector<double> irr_dyngrad, atom_shift;
+    std::vector<int32_t> op_fmap;
 };
 
 }  // namespace
@@ -122,6 +124,22 @@ extern "C" int tdg_problem_load(const char *dir, const int32_t grid[3], int four
     if (st) return st;
     st = build_phonons(h->c, fc2, h->q, h->ph);
     if (st) return st;
+    // off-diagonal kappa inputs: dD/dq at the irreducible points and the atom maps
+    {
+        const int nb = 3 * h->c.na, ni = h->q.n_irr;
+        h->irr_dyngrad.assign((size_t)ni * 3 * nb * nb * 2, 0.0);
+        parallel_for(ni, [&](int64_t i) {
+            std::vector<cplx> g((size_t)3 * nb * nb);
+            dyn_gradient(h->c, fc2, h->q.q_full[h->q.irr_full[i] - 1], nb, g.data());
+            for (size_t k = 0; k < g.size(); ++k) {
+                h->irr_dyngrad[((size_t)i * 3 * nb * nb + k) * 2] = g[k].real();
+                h->irr_dyngrad[((size_t)i * 3 * nb * nb + k) * 2 + 1] = g[k].imag();
+            }
+        });
+        st = op_atom_maps(h->c, h->op_fmap, h->atom_shift);
+        if (st) return st;
+        for (auto &x : h->op_fmap) x += 1;
+    }
 
     tdg_problem &p = h->p;
     std::memset(&p, 0, sizeof(p));
@@ -165,6 +183,9 @@ extern "C" int tdg_problem_load(const char *dir, const int32_t grid[3], int four
     p.fc4_lv = h->f4.lv.data();
     p.fc4_lvcart = h->f4.lvcart.data();
     p.fc4_mwm = h->f4.mwm.data();
+    p.irr_dyngrad = h->irr_dyngrad.data();
+    p.op_fmap = h->op_fmap.data();
+    p.atom_shift = h->atom_shift.data();
     *out = &h.release()->p;
     return kOk;
 }

@@ -170,6 +170,12 @@ struct tdg_ctx {
     DevBuf<float2> d_psi, d_lnph;
     bool bmat_ready = false;
     int xi_fmt = -1;  // d_xi_df holds the current Xi as float pairs (1), floats (0), or nothing (-1)
+    // off-diagonal kappa inputs (host copies; uploaded by the first tdg_kappa_offdiag)
+    std::vector<double> irr_dyngrad, atom_shift, q_full;
+    std::vector<int32_t> op_fmap;
+    DevBuf<double2> d_grad, d_odwork;
+    DevBuf<double> d_shift, d_qfull, d_lwcv, d_odS, d_irr_weight;
+    DevBuf<int32_t> d_fmap;
 
     MeshDev mesh() const {
         MeshDev m;
@@ -384,6 +390,16 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
     c->degen_mode.assign(p->degen_mode, p->degen_mode + nm * c->n);
     c->n_fc3 = p->n_fc3;
     c->n_fc4 = p->n_fc4;
+    c->q_full.assign(p->q_full, p->q_full + 3 * (size_t)c->N);
+    if (p->irr_dyngrad && p->op_fmap && p->atom_shift) {
+        c->irr_dyngrad.assign(p->irr_dyngrad, p->irr_dyngrad + (size_t)c->nirr * 3 * c->n * c->n * 2);
+        c->atom_shift.assign(p->atom_shift, p->atom_shift + (size_t)c->nop * c->na * 3);
+        c->op_fmap.resize((size_t)c->nop * c->na);
+        for (size_t i = 0; i < c->op_fmap.size(); ++i) {
+            c->op_fmap[i] = p->op_fmap[i] - 1;
+            if (c->op_fmap[i] < 0 || c->op_fmap[i] >= c->na) return fail(set_error(kErrParam, "op_fmap out of range"));
+        }
+    }
     c->L = 1;
     for (int i = 0; i < 3; ++i) c->L = c->L / gcd_i(c->L, c->grid[i]) * c->grid[i];
     for (int i = 0; i < 3; ++i) c->lmul[i] = c->L / c->grid[i];
@@ -562,11 +578,14 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
 extern "C" void tdg_destroy(tdg_ctx *c) {
     if (!c) return;
     cudaSetDevice(c->device);
+    PhaseTimer pt("tdg_destroy");
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (auto &x : c->ev)
         if (x) cudaEventDestroy(x);
     if (c->stream) cudaStreamDestroy(c->stream);
+    pt.mark("stream and events");
     delete c;
+    pt.mark("device buffers");
 }
 
 namespace {
@@ -614,6 +633,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
                               double *stats) {
     XferScope xs(c ? c->xfer : nullptr);
     if (!c || !ql || !linewidth) return set_error(kErrParam, "tdg_scattering: null argument");
+    PhaseTimer pt("tdg_scattering");
     int st = validate_opts(o);
     if (st) return st;
     CUDA_TRY(cudaSetDevice(c->device));
@@ -655,6 +675,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     c->n_row = nr;
     c->row_q1.assign(ql->row_q1, ql->row_q1 + nr);
     c->row_b1.assign(ql->row_b1, ql->row_b1 + nr);
+    pt.mark("argument checks");
 
     // ---- init block (scattering.f90:126-168) ----
     std::vector<double> be((size_t)nirr * n, 0.0), sigsq((size_t)nirr * n, 0.0), sigavg(n, 0.0);
@@ -703,6 +724,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         if (o->thirdorder) w3[r] = 1.0 / (double)(ql->ptr3[r + 1] - ql->ptr3[r]);
         if (o->fourthorder) w4[r] = 1.0 / (double)(ql->ptr4[r + 1] - ql->ptr4[r]);
     }
+    pt.mark("init block");
     // ---- three-phonon samples and candidates ----
     // When all rows of a q1 share one sample (the full grid, or samples given per q1) it is
     // uploaded once per q1 and the candidates (q1, q2, mask of every row of q1) are formed
@@ -850,6 +872,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         if (nc64 >= ((int64_t)1 << 31) - 1 || (int64_t)slist.size() >= ((int64_t)1 << 31))
             return set_error(kErrBadDim, "too many three-phonon candidates for one call");
     }
+    pt.mark("three-phonon candidates (host)");
     // ---- four-phonon candidates (scattering_fourphonon.f90:88-99): q2 from list a, q3 from
     // list b, q3 >= q2 and q4 = -q1-q2-q3 >= q3, once per q1 with the rows that sampled the
     // pair as a bit mask. Rows of q1 with identical lists share one pass over the pairs;
@@ -1006,6 +1029,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         chk(c->d_od.alloc((size_t)nr * ld));
     }
     chk(cudaStreamSynchronize(s));
+    pt.mark("allocations and uploads");
     if (e != cudaSuccess) return set_error(kErrDevice, std::string("allocation/upload failed: ") + cudaGetErrorString(e));
     ph.be = c->d_be.p;
     ph.sigsq = c->d_sigsq.p;
@@ -1203,6 +1227,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     ++launches;
     CUDA_TRY(cudaEventRecord(ev[6], s));
     CUDA_TRY(cudaStreamSynchronize(s));
+    pt.mark("device pipeline");
     st = read_status(c);
     if (st) return st;
     float ms_total = 0.f, ms_iso = 0.f, ms_k1 = 0.f, ms_fused = 0.f, ms_sym = 0.f;
@@ -1278,6 +1303,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     c->last_ntrip = ntrip;
     c->last_third = o->thirdorder != 0;
     c->have_scattering = true;
+    pt.mark("linewidths and F0 (host)");
     return kOk;
 }
 
@@ -1712,5 +1738,94 @@ extern "C" int tdg_transfer_bytes(tdg_ctx *c, int64_t *h2d, int64_t *d2h) {
     if (!c) return set_error(kErrParam, "tdg_transfer_bytes: null context");
     if (h2d) *h2d = c->xfer[0];
     if (d2h) *d2h = c->xfer[1];
+    return kOk;
+}
+
+extern "C" int tdg_kappa_offdiag(tdg_ctx *c, const tdg_opts *o, double *kappa_offdiag) {
+    XferScope xs(c ? c->xfer : nullptr);
+    if (!c || !kappa_offdiag) return set_error(kErrParam, "tdg_kappa_offdiag: null argument");
+    int st = validate_opts(o);
+    if (st) return st;
+    if (!c->have_scattering) return set_error(kErrParam, "tdg_kappa_offdiag: call tdg_scattering first");
+    if (c->irr_dyngrad.empty())
+        return set_error(kErrParam, "tdg_kappa_offdiag: the problem has no irr_dyngrad/op_fmap/atom_shift");
+    CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    const int n = c->n, nirr = c->nirr;
+    const size_t nn = (size_t)n * n;
+    if (c->d_grad.n == 0) {
+        CUDA_TRY(c->d_grad.upload(reinterpret_cast<const double2 *>(c->irr_dyngrad.data()), (size_t)nirr * 3 * nn, s));
+        CUDA_TRY(c->d_shift.upload(c->atom_shift.data(), c->atom_shift.size(), s));
+        CUDA_TRY(c->d_fmap.upload(c->op_fmap.data(), c->op_fmap.size(), s));
+        CUDA_TRY(c->d_qfull.upload(c->q_full.data(), c->q_full.size(), s));
+        CUDA_TRY(c->d_irr_weight.upload(c->irr_weight.data(), c->irr_weight.size(), s));
+        if (c->d_op_cart.n == 0) CUDA_TRY(c->d_op_cart.upload(c->op_cart.data(), c->op_cart.size(), s));
+        const size_t w = offdiag_work_elems(n, nirr);
+        if (w) CUDA_TRY(c->d_odwork.alloc(w));
+        CUDA_TRY(c->d_odS.alloc((size_t)nirr * 9));
+    }
+    // linewidths and heat capacities of the irreducible modes (kappa.f90:252-278)
+    std::vector<double> lwcv(2 * (size_t)nirr * n);
+    for (int q = 0; q < nirr; ++q) {
+        const int f = c->irr_full[q] - 1;
+        for (int b = 0; b < n; ++b) {
+            lwcv[(size_t)q * n + b] = c->linewidth[(size_t)q * n + b];
+            lwcv[(size_t)nirr * n + (size_t)q * n + b] =
+                o->classical ? kKbHartree : harmonic_oscillator_cv(o->temperature, c->omega[(size_t)f * n + b]);
+        }
+    }
+    CUDA_TRY(c->d_lwcv.upload(lwcv.data(), lwcv.size(), s));
+    OffdiagArgs a{};
+    a.n = n;
+    a.na = c->na;
+    a.n_op = c->nop;
+    a.egv = c->d_egv.p;
+    a.grad = c->d_grad.p;
+    a.omega = c->d_omega.p;
+    a.q_full = c->d_qfull.p;
+    a.irr_full = c->d_irr_full.p;
+    a.irr_nop = c->d_irr_nop.p;
+    a.irr_ops = c->d_irr_ops.p;
+    a.op_cart = c->d_op_cart.p;
+    a.fmap = c->d_fmap.p;
+    a.shift = c->d_shift.p;
+    a.lw = c->d_lwcv.p;
+    a.cv = c->d_lwcv.p + (size_t)nirr * n;
+    a.irr_weight = c->d_irr_weight.p;
+    a.inv_volume = 1.0 / c->volume;
+    a.chop_tol = 1E-10 / (kGroupVelAuToMs / 1000.0);
+    a.work = c->d_odwork.p;
+    a.vel = nullptr;
+    a.S = c->d_odS.p;
+    CUDA_TRY(launch_offdiag(a, nirr, s));
+    std::vector<double> S((size_t)nirr * 9);
+    CUDA_TRY(copy_async(S.data(), c->d_odS.p, sizeof(double) * S.size(), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    // star of each irreducible point: (1/n_star) sum_R R S R^T (kappa.f90:221-231)
+    std::vector<double> K((size_t)nirr * 9, 0.0);
+    std::vector<int> nstar(nirr, 0);
+    for (int f = 0; f < c->N; ++f) {
+        const int q = c->full_irr[f] - 1;
+        const double *m = &c->op_cart[9 * (std::abs(c->full_op[f]) - 1)];
+        const double *Sq = &S[(size_t)q * 9];
+        double *Kq = &K[(size_t)q * 9];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                double v = 0.0;
+                for (int k = 0; k < 3; ++k)
+                    for (int l = 0; l < 3; ++l) v += m[i + 3 * k] * Sq[k + 3 * l] * m[j + 3 * l];
+                Kq[i + 3 * j] += v;
+            }
+        ++nstar[q];
+    }
+    double kap[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int q = 0; q < nirr; ++q)
+        for (int k = 0; k < 9; ++k) kap[k] += K[(size_t)q * 9 + k] / nstar[q];
+    double tol = 0.0;
+    for (int k = 0; k < 9; ++k) tol += std::fabs(kap[k]);
+    tol *= 1e-6;
+    for (int k = 0; k < 9; ++k) kap[k] = lo_chop(kap[k], tol);
+    symmetrize_kappa(c, kap);
+    std::memcpy(kappa_offdiag, kap, sizeof(kap));
     return kOk;
 }

@@ -258,6 +258,32 @@ cudaError_t launch_foldout(int32_t n_full, int32_t n_mode, const int32_t *full_o
                            const double *op_cart, const double *fn, bool df, void *fbb, cudaStream_t s);
 
 // What an entry point compiled outside the context's own file needs of a context.
+// Off-diagonal kappa (k_offdiag.cu), one CTA per irreducible point. Index tables 0-based.
+constexpr int kOffdiagSmemModes = 18;  // up to this many modes the work arrays live in shared memory
+struct OffdiagArgs {
+    int32_t n, na, n_op;
+    const double2 *egv;       // full-mesh eigenvectors, element r of mode b of point f at (f*n + b)*n + r
+    const double2 *grad;      // [n_irr][3][n][n] dD/dq, element (r, c) at (x*n + c)*n + r
+    const double *omega;      // [n_full][n]
+    const double *q_full;     // [n_full][3] Cartesian, 1/Bohr without 2*pi
+    const int32_t *irr_full;  // [n_irr]
+    const int32_t *irr_nop;   // [n_irr]
+    const int32_t *irr_ops;   // [n_irr][n_op]
+    const double *op_cart;    // [n_op][9]
+    const int32_t *fmap;      // [n_op][na]
+    const double *shift;      // [n_op][na][3]
+    const double *lw;         // [n_irr][n] linewidths
+    const double *cv;         // [n_irr][n] heat capacities (k_B when classical)
+    const double *irr_weight; // [n_irr]
+    double inv_volume;
+    double chop_tol;          // velocity components below this become 0 (kappa.f90:209)
+    double2 *work;            // offdiag_work_elems(n, n_irr) beyond kOffdiagSmemModes modes
+    double *vel;              // optional [n_irr][n][n][3] off-diagonal velocities
+    double *S;                // [n_irr][9] sum over mode pairs of w v v^T, column-major
+};
+size_t offdiag_work_elems(int n, int n_irr);
+cudaError_t launch_offdiag(const OffdiagArgs &a, int n_irr, cudaStream_t s);
+
 struct CtxView {
     int device;
     cudaStream_t stream;

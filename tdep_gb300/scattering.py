@@ -39,6 +39,8 @@ _FIELDS_F64 = {
     "fc3_mwm": ("n_fc3", 27),
     "fc4_lvcart": ("n_fc4", 9),
     "fc4_mwm": ("n_fc4", 81),
+    "irr_dyngrad": ("n_irr", 3, "n_mode", "n_mode", 2),
+    "atom_shift": ("n_op", "n_atom", 3),
 }
 _FIELDS_I32 = {
     "op_recfrac": ("n_op", 9),
@@ -53,6 +55,7 @@ _FIELDS_I32 = {
     "fc3_lv": ("n_fc3", 6),
     "fc4_atoms": ("n_fc4", 4),
     "fc4_lv": ("n_fc4", 9),
+    "op_fmap": ("n_op", "n_atom"),
 }
 _SCALARS = ("n_atom", "n_mode", "n_op", "n_full", "n_irr", "n_fc3", "n_fc4")
 
@@ -321,6 +324,14 @@ class ScatteringRates:
         xi = np.zeros((self.lists.n_row, p.n_full * p.n_mode))
         N.check(self._lib.tdg_get_xi(self._ctx, N.ptr(xi, C.c_double)), "tdg_get_xi")
         return xi
+
+    def kappa_offdiag(self, opts: Options) -> np.ndarray:
+        """get_kappa_offdiag (kappa.f90:77-306) + symmetrize_kappa from the linewidths of the
+        last generate(). Returns the a.u. 3x3 off-diagonal (coherence) tensor."""
+        o = opts.struct(self.prob.grid)
+        k = np.zeros(9)
+        N.check(self._lib.tdg_kappa_offdiag(self._ctx, C.byref(o), N.ptr(k, C.c_double)), "tdg_kappa_offdiag")
+        return k.reshape(3, 3, order="F")
 
     def transfer_bytes(self) -> tuple[int, int]:
         """(host-to-device, device-to-host) bytes copied by this object's calls so far."""

@@ -346,9 +346,11 @@ def test_driver_matches_api(configs, tmp_path):
     sr = ScatteringRates(prob)
     sr.generate(opts)
     ks, ki = sr.kappa(opts)
+    ko = sr.kappa_offdiag(opts)
     sr.close()
     np.testing.assert_allclose(vals[0][:3], np.diag(ks) * KAPPA_AU_TO_SI, rtol=1e-9)
-    np.testing.assert_allclose(vals[3][:3], np.diag(ki) * KAPPA_AU_TO_SI, rtol=1e-9)
+    np.testing.assert_allclose(vals[2][:3], np.diag(ko) * KAPPA_AU_TO_SI, rtol=1e-9)
+    np.testing.assert_allclose(vals[3][:3], np.diag(ki + ko) * KAPPA_AU_TO_SI, rtol=1e-9)
 
 
 def test_device_exponential_accuracy(built):
@@ -424,3 +426,35 @@ def test_large_cell_needs_mixed_precision(configs):
         sr.generate(opts, QLists.monte_carlo(prob, opts))
     assert e.value.code == 5
     sr.close()
+
+
+@pytest.mark.parametrize("name,grid,classical", [("rocksalt", (6, 6, 6), False), ("perovskite", (4, 4, 4), False),
+                                                 ("fcc", (8, 8, 8), True)])
+def test_offdiag_kappa_matches_oracle(configs, name, grid, classical):
+    """get_kappa_offdiag on the device (little-group sandwich per point, shared-memory work
+    arrays) against the oracle's literal Kronecker form, from the same linewidths."""
+    prob = Problem.load(configs[name], grid, readiso=True)
+    opts = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=5, classical=classical)
+    lists = QLists.monte_carlo(prob, opts)
+    sr = ScatteringRates(prob)
+    lw = sr.generate(opts, lists)
+    kod = sr.kappa_offdiag(opts)
+    sr.close()
+    ref = orc.kappa_offdiag(prob, opts, lw)
+    assert np.abs(ref).max() > 0
+    np.testing.assert_allclose(kod, ref, rtol=1e-10, atol=1e-10 * np.abs(ref).max())
+
+
+def test_offdiag_kappa_large_cell_matches_oracle(configs):
+    """30 modes: the work arrays live in global memory."""
+    prob = Problem.load(configs["supercell"], (3, 3, 3), readiso=True)
+    opts = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=6, precision="mixed",
+                   qg3ph=(2, 2, 2))
+    lists = QLists.monte_carlo(prob, opts)
+    sr = ScatteringRates(prob)
+    lw = sr.generate(opts, lists)
+    kod = sr.kappa_offdiag(opts)
+    sr.close()
+    ref = orc.kappa_offdiag(prob, opts, lw)
+    assert np.abs(ref).max() > 0
+    np.testing.assert_allclose(kod, ref, rtol=1e-10, atol=1e-10 * np.abs(ref).max())

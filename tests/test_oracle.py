@@ -124,3 +124,72 @@ def test_oracle_adjoint_matches_finite_differences(configs):
         prob.fc3_mwm[t, e] = m0[t, e]
         fd = (lp - lm) / (2 * h)
         assert abs(fd - grad[t, e]) <= 1e-6 * abs(grad).max() + 1e-6 * abs(fd)
+
+
+def _offdiag_sandwich(prob, opts, lw):
+    """get_kappa_offdiag written as per-operation sandwiches egw^H (dD/dq) egw in numpy,
+    an independent form of the oracle's n^2 x n^2 Kronecker product (kappa.f90:171-200)."""
+    n, na = prob.n_mode, prob.n_atom
+    kb = 8.6173303e-5 / 27.21138602
+    hbar = 6.582119514e-16 / 27.21138602
+    chop = 1e-10 / ((0.52917721067e-10 / hbar) / 1000.0)
+
+    def cv(T, om):
+        x = om / T / kb
+        if x > 200:
+            return 0.0
+        if x > 21:
+            return kb * x * x * np.exp(-x)
+        if x < 2e-2:
+            return kb * (1 - x * x / 12 + x**4 / 240)
+        return kb * x * x * np.exp(x) / (np.exp(x) - 1) ** 2
+
+    K = np.zeros((3, 3))
+    for q in range(prob.n_irr):
+        f = prob.irr_full[q] - 1
+        E = prob.egv[f][..., 0] + 1j * prob.egv[f][..., 1]
+        G = prob.irr_dyngrad[q][..., 0] + 1j * prob.irr_dyngrad[q][..., 1]
+        om = prob.omega[f]
+        V = np.zeros((3, n, n), complex)
+        for k in range(prob.irr_nop[q]):
+            o = prob.irr_ops[q, k] - 1
+            R = prob.op_cart[o].reshape(3, 3, order="F")
+            egw = np.zeros((n, n), complex)
+            for a2 in range(na):
+                a1 = prob.op_fmap[o, a2] - 1
+                ph = np.exp(-2j * np.pi * prob.atom_shift[o, a2] @ prob.q_full[f])
+                egw[:, 3 * a1:3 * a1 + 3] = (E[:, 3 * a2:3 * a2 + 3] @ R.T) * ph
+            egw *= np.where(om > 1e-9, 1 / np.sqrt(2 * np.maximum(om, 1e-300)), 0.0)[:, None]
+            for x in range(3):
+                V[x] += egw.conj() @ G[x].T @ egw.T
+        v = (V.real / prob.irr_nop[q]).transpose(1, 2, 0)
+        v[np.abs(v) < chop] = 0
+        S = np.zeros((3, 3))
+        for j in range(n):
+            for kk in range(n):
+                if j == kk or min(om[j], om[kk], lw[q, j], lw[q, kk]) < 1e-9:
+                    continue
+                t = lw[q, j] + lw[q, kk]
+                f0 = 0.5 * (cv(opts.temperature, om[j]) + cv(opts.temperature, om[kk]))
+                S += t / (t * t + (om[j] - om[kk]) ** 2) * f0 * np.outer(v[j, kk], v[j, kk])
+        star = np.nonzero(prob.full_irr == q + 1)[0]
+        for fq in star:
+            R = prob.op_cart[abs(prob.full_op[fq]) - 1].reshape(3, 3, order="F")
+            K += R @ S @ R.T * prob.irr_weight[q] / prob.volume / len(star)
+    Ks = sum(prob.op_cart[o].reshape(3, 3, order="F") @ K @ prob.op_cart[o].reshape(3, 3, order="F").T
+             for o in range(prob.n_op))
+    return Ks / prob.n_op
+
+
+@pytest.mark.parametrize("name,grid", [("rocksalt", (4, 4, 4)), ("perovskite", (3, 3, 3))])
+def test_offdiag_kronecker_form_equals_sandwich_form(configs, name, grid):
+    """The oracle's off-diagonal kappa (kappa.f90:77-306, literal Kronecker form) equals the
+    per-operation sandwich form the device kernel uses, and is isotropic for cubic cells."""
+    p = Problem.load(configs[name], grid, readiso=True)
+    opts = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=3)
+    lw = orc.full_run(p, opts, QLists.monte_carlo(p, opts), nthreads=4)["linewidth"]
+    ko = orc.kappa_offdiag(p, opts, lw)
+    ks = _offdiag_sandwich(p, opts, lw)
+    assert ko[0, 0] > 0
+    np.testing.assert_allclose(ko, ks, rtol=1e-12, atol=1e-12 * np.abs(ko).max())
+    np.testing.assert_allclose(np.diag(ko), ko[0, 0], rtol=1e-10)
