@@ -1,6 +1,7 @@
 // Isotope scattering, the two scattering-matrix symmetrisations and the BTE product.
 #include <cuda_runtime.h>
 
+#include "dev_common.cuh"
 #include "tdg_internal.cuh"
 
 namespace tdg {
@@ -8,8 +9,6 @@ namespace tdg {
 namespace {
 
 constexpr double kIsotopePrefactor = 3.141592653589793 / 4.0;
-constexpr double kSqrt2PiInv = 0.398942280401433;
-constexpr double kFreqTolD = 1E-9;
 
 __device__ __forceinline__ double lo_gauss(double x, double mu, double sigma) {
     if (fabs(x - mu) > 8.0 * sigma) return 0.0;
@@ -193,37 +192,106 @@ __global__ void k_sym_distribute(MeshDev m, OrbitDev o, const int32_t *row_q1, c
     for (int64_t j = threadIdx.x; j < ld; j += blockDim.x) xr[j] += odr[j];
 }
 
-// symmetrize_scatmat (scattering.f90:296-357): one thread per (row, orbit, mode).
-__global__ void k_sym_scatmat(MeshDev m, OrbitDev o, const int32_t *row_q1, double *xi) {
-    const int n = m.n_mode;
-    const int r = blockIdx.y;
-    const int q1 = row_q1[r];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nrep = o.rep_ptr[q1 + 1] - o.rep_ptr[q1];
-    if (i >= nrep * n) return;
-    const int k = o.rep_ptr[q1] + i / n, b2 = i % n;
-    const int cnt = o.cnt[k];
-    if (cnt == 0) return;
-    const int nu = o.nuniq[k];
-    const int32_t *im = o.img + (size_t)k * m.n_op;
-    const int32_t *mu = o.mult + (size_t)k * m.n_op;
+// Both row symmetrisations on tiles of whole orbits: symmetrize_and_distribute of the
+// three-phonon terms (scattering_threephonon.f90:143-205; only orbits whose representative
+// the row sampled, entries > 0 averaged) and symmetrize_scatmat (scattering.f90:296-357;
+// every orbit, all entries). A CTA takes K = min(256, T / |G_q1|) consecutive orbits of its
+// row's q1 (at most T points), gathers their images' n modes into shared memory with
+// independent loads, averages there in the reference's summation order (each image added
+// mult times, in first-appearance order) and writes the images back. With both passes in
+// one kernel Xi crosses HBM once instead of twice. q1 whose little group is the identity
+// alone are skipped: every orbit is one point with count 1, and both averages return it.
+__global__ void __launch_bounds__(256) k_sym_tile(MeshDev m, OrbitDev o, const int32_t *row_q1, double *xi,
+                                                  const uint32_t *sbits, int do_dist, int do_scat) {
+    extern __shared__ double sym_sm[];
+    __shared__ int wsum[8];
+    const int n = m.n_mode, T = o.tile_pts;
+    const int r = blockIdx.y, q1 = row_q1[r];
+    const int nop = m.irr_nop[q1];
+    if (nop <= 1) return;
+    const int K = min(256, T / nop);
+    const int kb = o.rep_ptr[q1], ke = o.rep_ptr[q1 + 1];
+    const int k0 = kb + blockIdx.x * K;
+    if (k0 >= ke) return;
+    const int nk = min(K, ke - k0);
+    double *vals = sym_sm;                                 // [T][n]
+    int *pts = (int *)(vals + (size_t)T * n);              // [T] image of each position
+    int *pmu = pts + T;                                    // [T] its multiplicity
+    int *off = pmu + T;                                    // [257] first position of each orbit
+    const int tid = threadIdx.x;
+    const int nu_t = tid < nk ? o.nuniq[k0 + tid] : 0;
+    int P = 0;
+    const int my = block_exclusive_scan(nu_t, wsum, P);
+    if (tid < nk) {
+        off[tid] = my;
+        const int32_t *im = o.img + (size_t)(k0 + tid) * m.n_op;
+        const int32_t *mu = o.mult + (size_t)(k0 + tid) * m.n_op;
+        for (int u = 0; u < nu_t; ++u) {
+            pts[my + u] = im[u];
+            pmu[my + u] = mu[u];
+        }
+    }
+    if (tid == 0) off[nk] = P;
+    __syncthreads();
     double *xr = xi + (int64_t)r * m.n_full * n;
-    double buf = 0.0;
-    int u = 0;
-    for (; u + 4 <= nu; u += 4) {
-        const double x0 = xr[(int64_t)im[u] * n + b2], x1 = xr[(int64_t)im[u + 1] * n + b2];
-        const double x2 = xr[(int64_t)im[u + 2] * n + b2], x3 = xr[(int64_t)im[u + 3] * n + b2];
-        for (int rep = 0; rep < mu[u]; ++rep) buf += x0;
-        for (int rep = 0; rep < mu[u + 1]; ++rep) buf += x1;
-        for (int rep = 0; rep < mu[u + 2]; ++rep) buf += x2;
-        for (int rep = 0; rep < mu[u + 3]; ++rep) buf += x3;
+    for (int e = tid; e < P * n; e += blockDim.x) {
+        const int p = e / n, b2 = e - p * n;
+        vals[e] = xr[(int64_t)pts[p] * n + b2];
     }
-    for (; u < nu; ++u) {
-        const double x = xr[(int64_t)im[u] * n + b2];
-        for (int rep = 0; rep < mu[u]; ++rep) buf += x;
+    __syncthreads();
+    const uint32_t *bits = sbits ? sbits + (size_t)r * ((m.n_full + 31) / 32) : nullptr;
+    for (int it = tid; it < nk * n; it += blockDim.x) {
+        const int t = it / n, b2 = it - t * n, k = k0 + t;
+        const int p0 = off[t], p1 = off[t + 1];
+        if (do_dist) {
+            const int q2 = o.rep[k];
+            if ((bits[q2 >> 5] >> (q2 & 31)) & 1u) {
+                double buf = 0.0;
+                int nn = 0;
+                for (int p = p0; p < p1; ++p) {
+                    const double v = vals[p * n + b2];
+                    if (__double_as_longlong(v) > 0) {  // v > 0, v not NaN
+                        nn += pmu[p];
+                        for (int rep = 0; rep < pmu[p]; ++rep) buf += v;
+                    }
+                }
+                if (nn) {
+                    const double avg = buf * o.rcp[nn];
+                    for (int p = p0; p < p1; ++p) vals[p * n + b2] = avg;
+                }
+            }
+        }
+        if (do_scat) {
+            const int cnt = o.cnt[k];
+            if (cnt) {
+                double buf = 0.0;
+                for (int p = p0; p < p1; ++p) {
+                    const double v = vals[p * n + b2];
+                    for (int rep = 0; rep < pmu[p]; ++rep) buf += v;
+                }
+                buf *= o.rcp[cnt];
+                for (int p = p0; p < p1; ++p) vals[p * n + b2] = buf;
+            }
+        }
     }
-    buf *= o.rcp[cnt];
-    for (u = 0; u < nu; ++u) xr[(int64_t)im[u] * n + b2] = buf;
+    __syncthreads();
+    for (int e = tid; e < P * n; e += blockDim.x) {
+        const int p = e / n, b2 = e - p * n;
+        xr[(int64_t)pts[p] * n + b2] = vals[e];
+    }
+}
+
+// Bitmap of the q-points each row sampled, [n_row][ceil(n_full/32)] words.
+__global__ void k_sample_bits(int32_t n_full, const int64_t *rbeg, const int32_t *rlen, const int32_t *list,
+                              uint32_t *bits) {
+    const int r = blockIdx.x, nw = (n_full + 31) / 32;
+    uint32_t *br = bits + (size_t)r * nw;
+    for (int i = threadIdx.x; i < nw; i += blockDim.x) br[i] = 0u;
+    __syncthreads();
+    for (int64_t i = rbeg[r] + threadIdx.x; i < rbeg[r] + rlen[r]; i += blockDim.x) {
+        const int q2 = list[i] - 1;
+        atomicOr(br + (q2 >> 5), 1u << (q2 & 31));
+    }
 }
 
 // K8: three dot products per row of Xi (kappa.f90:411-413, the lo_gemv calls).
@@ -487,11 +555,40 @@ cudaError_t launch_sym_distribute(const MeshDev &m, const OrbitDev &o, int32_t n
     return cudaGetLastError();
 }
 
-cudaError_t launch_sym_scatmat(const MeshDev &m, const OrbitDev &o, int32_t n_row, const int32_t *row_q1, double *xi,
-                               cudaStream_t s) {
-    if (n_row <= 0 || o.max_rep <= 0) return cudaSuccess;
-    dim3 grid((unsigned)(((int64_t)o.max_rep * m.n_mode + 127) / 128), (unsigned)n_row);
-    k_sym_scatmat<<<grid, 128, 0, s>>>(m, o, row_q1, xi);
+int sym_tile_points(int n_mode) {
+    const int t = 4096 / (n_mode > 0 ? n_mode : 1);
+    return t < 64 ? 64 : (t > 1024 ? 1024 : t);
+}
+
+size_t sym_tile_smem(int n_mode) {
+    const int T = sym_tile_points(n_mode);
+    return sizeof(double) * (size_t)T * n_mode + sizeof(int) * (2 * (size_t)T + 257);
+}
+
+int sym_tile_count(int n_rep, int n_ops, int n_mode) {
+    if (n_ops <= 1 || n_rep <= 0) return 0;
+    int K = sym_tile_points(n_mode) / n_ops;
+    K = K > 256 ? 256 : K;
+    return (n_rep + K - 1) / K;
+}
+
+cudaError_t launch_sample_bits(int32_t n_full, int32_t n_row, const int64_t *rbeg, const int32_t *rlen,
+                               const int32_t *list, uint32_t *bits, cudaStream_t s) {
+    if (n_row <= 0) return cudaSuccess;
+    k_sample_bits<<<n_row, 256, 0, s>>>(n_full, rbeg, rlen, list, bits);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sym_tile(const MeshDev &m, const OrbitDev &o, int32_t n_row, const int32_t *row_q1, double *xi,
+                            const uint32_t *sbits, bool dist, bool scat, cudaStream_t s) {
+    if (n_row <= 0 || o.max_tiles <= 0 || (!dist && !scat)) return cudaSuccess;
+    const size_t sm = sym_tile_smem(m.n_mode);
+    if (sm > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_sym_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+    }
+    dim3 grid((unsigned)o.max_tiles, (unsigned)n_row);
+    k_sym_tile<<<grid, 256, sm, s>>>(m, o, row_q1, xi, sbits, dist ? 1 : 0, scat ? 1 : 0);
     return cudaGetLastError();
 }
 

@@ -139,6 +139,7 @@ struct tdg_ctx {
     DevBuf<double> d_rcp;
     OrbitDev orbits{};
     DevBuf<int32_t> d_status;
+    DevBuf<uint32_t> d_sbits;  // per row: bitmap of its sampled q-points (three-phonon)
     bool have_scattering = false;
     std::vector<double> linewidth, qs, F0, Fn;  // irr-point arrays
     // enumeration and sample buffers, kept across calls (they only grow)
@@ -566,9 +567,14 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
         chk(copy_async(rp.data(), c->d_orb_rep_ptr.p, sizeof(int32_t) * rp.size(), cudaMemcpyDeviceToHost, s));
         chk(cudaStreamSynchronize(s));
         if (e != cudaSuccess) return fail(set_error(kErrDevice, std::string("orbit tables: ") + cudaGetErrorString(e)));
-        int mx = 0;
-        for (int q = 0; q < c->nirr; ++q) mx = std::max(mx, rp[q + 1] - rp[q]);
+        int mx = 0, mt = 0;
+        for (int q = 0; q < c->nirr; ++q) {
+            mx = std::max(mx, rp[q + 1] - rp[q]);
+            mt = std::max(mt, sym_tile_count(rp[q + 1] - rp[q], c->irr_nop[q], c->n));
+        }
         c->orbits.max_rep = mx;
+        c->orbits.tile_pts = sym_tile_points(c->n);
+        c->orbits.max_tiles = mt;
     }
     pt.mark("orbit tables");
     *out = c;
@@ -992,6 +998,8 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     chk(c->d_w3.upload(w3.data(), w3.size(), s));
     chk(c->d_w4.upload(w4.data(), w4.size(), s));
     const int64_t ld = (int64_t)N * n;
+    const bool fuse_sym = o->thirdorder && !o->fourthorder && !o->isotope;
+    if (o->thirdorder) chk(c->d_sbits.alloc((size_t)nr * ((N + 31) / 32)));
     chk(c->d_xi.alloc((size_t)nr * ld));
     chk(c->d_gamma.alloc(nr));
     if (o->thirdorder) {
@@ -1150,9 +1158,14 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
             ++launches;
         }
         CUDA_TRY(cudaEventRecord(ev[3], s));
-        CUDA_TRY(launch_sym_distribute(mesh, c->orbits, nr, c->d_row_q1.p, c->d_rbeg.p, c->d_rlen.p, c->d_list3.p,
-                                       c->d_xi.p, nullptr, s));
+        CUDA_TRY(launch_sample_bits(N, nr, c->d_rbeg.p, c->d_rlen.p, c->d_list3.p, c->d_sbits.p, s));
         ++launches;
+        // without four-phonon or isotope terms in between, the three-phonon distribution
+        // runs in the same pass as symmetrize_scatmat below
+        if (!fuse_sym) {
+            CUDA_TRY(launch_sym_tile(mesh, c->orbits, nr, c->d_row_q1.p, c->d_xi.p, c->d_sbits.p, true, false, s));
+            ++launches;
+        }
     } else {
         CUDA_TRY(cudaEventRecord(ev[2], s));
         CUDA_TRY(cudaEventRecord(ev[3], s));
@@ -1223,7 +1236,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     // ---- gamma to host; symmetrize_scatmat on the device meanwhile ----
     std::vector<double> gamma(nr);
     CUDA_TRY(copy_async(gamma.data(), c->d_gamma.p, sizeof(double) * nr, cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(launch_sym_scatmat(mesh, c->orbits, nr, c->d_row_q1.p, c->d_xi.p, s));
+    CUDA_TRY(launch_sym_tile(mesh, c->orbits, nr, c->d_row_q1.p, c->d_xi.p, c->d_sbits.p, fuse_sym, true, s));
     ++launches;
     CUDA_TRY(cudaEventRecord(ev[6], s));
     CUDA_TRY(cudaStreamSynchronize(s));

@@ -220,6 +220,8 @@ struct OrbitDev {
     const int32_t *orb_of;   // [n_irr * n_full] representative index of q2, -1 otherwise
     const double *rcp;       // [n_op+1] 1/i, replaces the FP64 divisions by counts
     int32_t max_rep;         // largest number of representatives of one q1
+    int32_t tile_pts;        // sym_tile_points(n_mode)
+    int32_t max_tiles;       // largest sym_tile_count over the q1
 };
 cudaError_t launch_orbit_flag(const MeshDev &m, int32_t *flag, cudaStream_t s);
 cudaError_t launch_orbit_fill(const MeshDev &m, const int32_t *flag, const int32_t *scan, OrbitDev &o,
@@ -234,9 +236,15 @@ cudaError_t launch_sym_distribute(const MeshDev &m, const OrbitDev &o, int32_t n
 // first candidate, mask id); cand[desc.z + i] = (q1, list[desc.x + i] - 1, desc.w, 0).
 cudaError_t launch_build_candidates(const int4 *desc, int32_t n_irr, int32_t max_len, const int32_t *list, int4 *cand,
                                     cudaStream_t s);
-// K5b: symmetrize_scatmat (scattering.f90:296-357).
-cudaError_t launch_sym_scatmat(const MeshDev &m, const OrbitDev &o, int32_t n_row, const int32_t *row_q1, double *xi,
-                               cudaStream_t s);
+// K5b: symmetrize_and_distribute of the three-phonon terms in place on xi (dist, orbits
+// whose representative the row sampled per sbits, launch_sample_bits) and/or
+// symmetrize_scatmat (scat, scattering.f90:296-357), on tiles of whole orbits.
+int sym_tile_points(int n_mode);
+int sym_tile_count(int n_rep, int n_ops, int n_mode);
+cudaError_t launch_sample_bits(int32_t n_full, int32_t n_row, const int64_t *rbeg, const int32_t *rlen,
+                               const int32_t *list, uint32_t *bits, cudaStream_t s);
+cudaError_t launch_sym_tile(const MeshDev &m, const OrbitDev &o, int32_t n_row, const int32_t *row_q1, double *xi,
+                            const uint32_t *sbits, bool dist, bool scat, cudaStream_t s);
 // K8: buf[r*3+a] = sum_j xi[r, j] * fbb[j*3 + a] on the FP32 pipe; xi and fbb as (hi, lo)
 // float pairs accumulated in double-float when df (FP64 runs), else as floats with FMA chains
 // added into double-float accumulators (mixed precision). launch_split_xi converts the FP64
