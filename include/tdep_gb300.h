@@ -174,6 +174,14 @@ int tdg_create(tdg_ctx **out, const tdg_problem *prob, int device);
 void tdg_destroy(tdg_ctx *ctx);
 
 /*
+ * Device memory of the contexts comes from a stream-ordered pool per device that keeps the
+ * blocks tdg_destroy frees, so that later contexts reuse them (a caching allocator; no
+ * reference counterpart). This returns the cached blocks of `device` to the driver; call it
+ * when no context of that device is alive.
+ */
+int tdg_release_cached_memory(int device);
+
+/*
  * Rows and Monte-Carlo q' samples, generated on the host exactly as the reference does:
  * MT19937-64 seeded by init_genrand64(iseed=0, rseed=1/seed) (lo_randomnumbers.f90:203-236),
  * one stratified sample per row and order (lo_fftgrid_helper.f90:56-99), consumed row by

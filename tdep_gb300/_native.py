@@ -121,6 +121,7 @@ SIGNATURES = {
     "tdg_get_xi": (C.c_int, [C.c_void_p, _f64p]),
     "tdg_transfer_bytes": (C.c_int, [C.c_void_p, _i64p, _i64p]),
     "tdg_kappa_offdiag": (C.c_int, [C.c_void_p, C.POINTER(TdgOpts), _f64p]),
+    "tdg_release_cached_memory": (C.c_int, [C.c_int]),
     "tdg_triplets": (C.c_int, [C.c_void_p, C.c_int32, _i32p, C.c_int64, _i32p, C.c_int64, _i64p]),
     "tdg_triplets_static": (C.c_int, [C.c_void_p, C.c_int32, _i32p, C.c_int64, _i32p, C.c_int64, _i64p]),
     "tdg_set_fc3": (C.c_int, [C.c_void_p, _f64p]),

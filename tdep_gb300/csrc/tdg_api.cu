@@ -16,6 +16,7 @@
 #include <array>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -35,25 +36,85 @@ namespace {
             return set_error(kErrDevice, std::string(#expr) + ": " + cudaGetErrorString(e_));          \
     } while (0)
 
+// Device memory of a context comes from one stream-ordered pool per device that keeps freed
+// blocks (unlimited release threshold): a context created after another one reuses its
+// buffers instead of mapping new memory, as a caching allocator does.
+// tdg_release_cached_memory returns the cached blocks to the driver. Allocation and free are
+// ordered on the stream of the context whose call is running on this thread (PoolScope);
+// outside such a call DevBuf falls back to cudaMalloc / cudaFree.
+thread_local cudaStream_t tl_stream = nullptr;
+thread_local cudaMemPool_t tl_pool = nullptr;
+
+struct PoolScope {
+    cudaStream_t ps;
+    cudaMemPool_t pp;
+    PoolScope(cudaStream_t s, cudaMemPool_t p) : ps(tl_stream), pp(tl_pool) {
+        tl_stream = s;
+        tl_pool = p;
+    }
+    ~PoolScope() {
+        tl_stream = ps;
+        tl_pool = pp;
+    }
+};
+
+std::mutex g_pool_mu;
+cudaMemPool_t g_pools[64] = {};
+
+cudaMemPool_t device_pool(int dev) {
+    if (dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> g(g_pool_mu);
+    if (!g_pools[dev]) {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        if (cudaMemPoolCreate(&g_pools[dev], &props) != cudaSuccess) {
+            cudaGetLastError();
+            g_pools[dev] = nullptr;
+            return nullptr;
+        }
+        uint64_t keep = UINT64_MAX;
+        cudaMemPoolSetAttribute(g_pools[dev], cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    return g_pools[dev];
+}
+
 template <typename T>
 struct DevBuf {
     T *p = nullptr;
     size_t n = 0;
+    cudaStream_t st = nullptr;  // stream of a pool allocation, nullptr for cudaMalloc
     DevBuf() = default;
     DevBuf(const DevBuf &) = delete;
     DevBuf &operator=(const DevBuf &) = delete;
     ~DevBuf() { release(); }
     void release() {
-        if (p) cudaFree(p);
+        if (p) {
+            if (st)
+                cudaFreeAsync(p, st);
+            else
+                cudaFree(p);
+        }
         p = nullptr;
         n = 0;
+        st = nullptr;
     }
     cudaError_t alloc(size_t count) {
         if (count <= n && p) return cudaSuccess;
         release();
         if (count == 0) count = 1;
-        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
-        if (e == cudaSuccess) n = count;
+        cudaError_t e;
+        if (tl_pool && tl_stream) {
+            e = cudaMallocFromPoolAsync(reinterpret_cast<void **>(&p), count * sizeof(T), tl_pool, tl_stream);
+            if (e == cudaSuccess) st = tl_stream;
+        } else {
+            e = cudaMalloc(&p, count * sizeof(T));
+        }
+        if (e == cudaSuccess)
+            n = count;
+        else
+            p = nullptr;
         return e;
     }
     cudaError_t upload(const T *h, size_t count, cudaStream_t s) {
@@ -101,6 +162,7 @@ thread_local int64_t *tl_xfer = nullptr;
 struct tdg_ctx {
     int device = 0;
     int64_t xfer[2] = {0, 0};  // host-to-device and device-to-host bytes of calls on this context
+    cudaMemPool_t pool = nullptr;  // device_pool(device)
     int n_sm = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[10] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -336,6 +398,39 @@ void build_rot_table(const tdg_problem *p, int L, std::vector<int32_t> &rot) {
 
 }  // namespace
 
+namespace {
+// Buffers go back to the pool in the order of the context's stream, which is destroyed last.
+void destroy_ctx(tdg_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    PhaseTimer pt("tdg_destroy");
+    cudaStream_t s = c->stream;
+    if (s) cudaStreamSynchronize(s);
+    for (auto &x : c->ev)
+        if (x) cudaEventDestroy(x);
+    delete c;
+    pt.mark("device buffers");
+    if (s) {
+        cudaStreamSynchronize(s);
+        cudaStreamDestroy(s);
+    }
+    pt.mark("stream");
+}
+}  // namespace
+
+extern "C" int tdg_release_cached_memory(int device) {
+    cudaMemPool_t pool = device_pool(device);
+    if (!pool) return set_error(kErrParam, "tdg_release_cached_memory: no pool for this device");
+    int prev = 0;
+    CUDA_TRY(cudaGetDevice(&prev));
+    CUDA_TRY(cudaSetDevice(device));
+    CUDA_TRY(cudaDeviceSynchronize());
+    const cudaError_t e = cudaMemPoolTrimTo(pool, 0);
+    cudaSetDevice(prev);
+    CUDA_TRY(e);
+    return kOk;
+}
+
 extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
     if (!out) return set_error(kErrParam, "tdg_create: null output");
     *out = nullptr;
@@ -353,7 +448,7 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
     c->device = device;
     XferScope xs(c->xfer);
     auto fail = [&](int code) {
-        delete c;
+        destroy_ctx(c);
         return code;
     };
     int major = 0;
@@ -363,6 +458,8 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
     if (major < 10) return fail(set_error(kErrDevice, "device is not Blackwell (sm_100 family required)"));
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
         return fail(set_error(kErrDevice, "stream creation failed"));
+    c->pool = device_pool(device);
+    PoolScope pscope(c->stream, c->pool);
     for (auto &x : c->ev)
         if (cudaEventCreate(&x) != cudaSuccess) return fail(set_error(kErrDevice, "event creation failed"));
     c->na = p->n_atom;
@@ -581,18 +678,7 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
     return kOk;
 }
 
-extern "C" void tdg_destroy(tdg_ctx *c) {
-    if (!c) return;
-    cudaSetDevice(c->device);
-    PhaseTimer pt("tdg_destroy");
-    if (c->stream) cudaStreamSynchronize(c->stream);
-    for (auto &x : c->ev)
-        if (x) cudaEventDestroy(x);
-    if (c->stream) cudaStreamDestroy(c->stream);
-    pt.mark("stream and events");
-    delete c;
-    pt.mark("device buffers");
-}
+extern "C" void tdg_destroy(tdg_ctx *c) { destroy_ctx(c); }
 
 namespace {
 
@@ -638,6 +724,7 @@ int read_status(tdg_ctx *c) {
 extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *ql, double *linewidth, double *qs_out,
                               double *stats) {
     XferScope xs(c ? c->xfer : nullptr);
+    PoolScope pscope(c ? c->stream : nullptr, c ? c->pool : nullptr);
     if (!c || !ql || !linewidth) return set_error(kErrParam, "tdg_scattering: null argument");
     PhaseTimer pt("tdg_scattering");
     int st = validate_opts(o);
@@ -1322,6 +1409,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
 
 extern "C" int tdg_get_xi(tdg_ctx *c, double *xi) {
     XferScope xs(c ? c->xfer : nullptr);
+    PoolScope pscope(c ? c->stream : nullptr, c ? c->pool : nullptr);
     if (!c || !xi) return set_error(kErrParam, "tdg_get_xi: null argument");
     if (!c->have_scattering) return set_error(kErrParam, "tdg_get_xi: call tdg_scattering first");
     CUDA_TRY(cudaSetDevice(c->device));
@@ -1334,6 +1422,7 @@ extern "C" int tdg_get_xi(tdg_ctx *c, double *xi) {
 extern "C" int tdg_triplets(tdg_ctx *c, int32_t q1, const int32_t *sample, int64_t n, int32_t *out, int64_t cap,
                             int64_t *written) {
     XferScope xs(c ? c->xfer : nullptr);
+    PoolScope pscope(c ? c->stream : nullptr, c ? c->pool : nullptr);
     if (!c || !sample || !out || !written) return set_error(kErrParam, "tdg_triplets: null argument");
     if (q1 < 1 || q1 > c->nirr) return set_error(kErrParam, "tdg_triplets: q1 out of range");
     if (n < 0 || n > (int64_t)1 << 30) return set_error(kErrParam, "tdg_triplets: bad sample length");
@@ -1466,6 +1555,7 @@ void symmetrize_kappa(const tdg_ctx *c, double *kappa) {
 extern "C" int tdg_kappa(tdg_ctx *c, const tdg_opts *o, int32_t maxiter, double tol, double *kappa_sma,
                          double *kappa_iter, double *fn_out, int32_t *n_iter) {
     XferScope xs(c ? c->xfer : nullptr);
+    PoolScope pscope(c ? c->stream : nullptr, c ? c->pool : nullptr);
     if (!c || !kappa_sma || !kappa_iter) return set_error(kErrParam, "tdg_kappa: null argument");
     int st = validate_opts(o);
     if (st) return st;
@@ -1588,6 +1678,7 @@ tdg::CtxView tdg::ctx_view(tdg_ctx *c) {
 
 extern "C" int tdg_set_fc3(tdg_ctx *c, const double *fc3_mwm) {
     XferScope xs(c ? c->xfer : nullptr);
+    PoolScope pscope(c ? c->stream : nullptr, c ? c->pool : nullptr);
     if (!c || !fc3_mwm) return set_error(kErrParam, "tdg_set_fc3: null argument");
     if (c->n_fc3 < 1) return set_error(kErrParam, "tdg_set_fc3: the context has no third-order force constants");
     const size_t cnt = (size_t)c->n_fc3 * 27;
@@ -1612,6 +1703,7 @@ extern "C" int tdg_set_fc3(tdg_ctx *c, const double *fc3_mwm) {
 
 extern "C" int tdg_kappa_sma_vjp(tdg_ctx *c, const tdg_opts *o, const double *kappa_bar, double *lw_bar) {
     XferScope xs(c ? c->xfer : nullptr);
+    PoolScope pscope(c ? c->stream : nullptr, c ? c->pool : nullptr);
     if (!c || !kappa_bar || !lw_bar) return set_error(kErrParam, "tdg_kappa_sma_vjp: null argument");
     int st = validate_opts(o);
     if (st) return st;
@@ -1660,6 +1752,7 @@ extern "C" int tdg_kappa_sma_vjp(tdg_ctx *c, const tdg_opts *o, const double *ka
 
 extern "C" int tdg_adjoint_fc3(tdg_ctx *c, const tdg_opts *o, const double *lw_bar, double *mwm_bar, double *stats) {
     XferScope xs(c ? c->xfer : nullptr);
+    PoolScope pscope(c ? c->stream : nullptr, c ? c->pool : nullptr);
     if (!c || !lw_bar || !mwm_bar) return set_error(kErrParam, "tdg_adjoint_fc3: null argument");
     int st = validate_opts(o);
     if (st) return st;
@@ -1756,6 +1849,7 @@ extern "C" int tdg_transfer_bytes(tdg_ctx *c, int64_t *h2d, int64_t *d2h) {
 
 extern "C" int tdg_kappa_offdiag(tdg_ctx *c, const tdg_opts *o, double *kappa_offdiag) {
     XferScope xs(c ? c->xfer : nullptr);
+    PoolScope pscope(c ? c->stream : nullptr, c ? c->pool : nullptr);
     if (!c || !kappa_offdiag) return set_error(kErrParam, "tdg_kappa_offdiag: null argument");
     int st = validate_opts(o);
     if (st) return st;

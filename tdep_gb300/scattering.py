@@ -398,5 +398,10 @@ def write_outfile(directory, temperature, kappa_sma, kappa_iter, kappa_offdiag=N
     return Path(directory) / "outfile.thermal_conductivity"
 
 
+def release_cached_memory(device: int = 0) -> None:
+    """Return the device memory the library keeps for reuse after contexts close."""
+    N.check(N.lib().tdg_release_cached_memory(int(device)), "tdg_release_cached_memory")
+
+
 def device_count() -> int:
     return int(N.lib().tdg_device_count())

@@ -458,3 +458,25 @@ def test_offdiag_kappa_large_cell_matches_oracle(configs):
     ref = orc.kappa_offdiag(prob, opts, lw)
     assert np.abs(ref).max() > 0
     np.testing.assert_allclose(kod, ref, rtol=1e-10, atol=1e-10 * np.abs(ref).max())
+
+
+def test_contexts_reuse_pooled_memory_and_release_it(configs):
+    """A context created after another one reuses the pooled device memory and gives the
+    same results (up to the order of atomic additions); the cache can be released once no
+    context is alive."""
+    from tdep_gb300 import release_cached_memory
+
+    prob = Problem.load(configs["rocksalt"], (6, 6, 6), readiso=True)
+    opts = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=9)
+    lists = QLists.monte_carlo(prob, opts)
+    out = []
+    for _ in range(3):
+        sr = ScatteringRates(prob)
+        lw = sr.generate(opts, lists).copy()
+        _, ki = sr.kappa(opts)
+        out.append((lw, ki))
+        sr.close()
+    release_cached_memory(0)
+    for lw, ki in out[1:]:  # equal up to the order of FP64 atomic additions
+        np.testing.assert_allclose(lw, out[0][0], rtol=1e-12, atol=0)
+        np.testing.assert_allclose(ki, out[0][1], rtol=1e-12, atol=0)
