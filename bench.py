@@ -98,7 +98,9 @@ def setup(cfg_name, precision="mixed"):
 # DRAM bytes (read + write) of one launch of the fused kernel, from
 # `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none -k regex:k_threephonon`
 # on `python bench.py --profile --config <name> --steps 1 --warmup 1` (a one-pass capture).
-TRAFFIC_PER_LAUNCH = {"rocksalt16": 40_347_136, "rocksalt24": 458_850_000, "perovskite16": 1_104_760_000}
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_threephonon launch (ncu, one pass), from
+# the launch lists summarised in profiles/
+TRAFFIC_PER_LAUNCH = {"rocksalt16": 40_693_760, "rocksalt24": 456_200_000, "perovskite16": 1_098_700_000}
 
 
 class ClockSampler:
@@ -246,14 +248,24 @@ def run_reference(args):
 
 
 def run_profile(args):
-    """--profile: warm-up passes then `steps` scattering passes, nothing else (for ncu)."""
+    """--profile: warm-up passes then `steps` passes of one stage, nothing else (for ncu):
+    scattering (generate), kappa (one generate, then BTE solves) or offdiag (one generate,
+    then off-diagonal kappa)."""
     from tdep_gb300 import ScatteringRates
 
     cfg, prob, opts, lists = setup(args.config, precision=args.precision)
     sr = ScatteringRates(prob)
-    for _ in range(args.warmup + args.steps):
+    if args.stage == "scattering":
+        for _ in range(args.warmup + args.steps):
+            sr.generate(opts, lists)
+    else:
         sr.generate(opts, lists)
-    log(f"[bench] profile: {sr.stats}")
+        for _ in range(args.warmup + args.steps):
+            if args.stage == "kappa":
+                sr.kappa(opts)
+            else:
+                sr.kappa_offdiag(opts)
+    log(f"[bench] profile ({args.stage}): {sr.stats}")
     sr.close()
 
 
@@ -411,8 +423,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="rocksalt24", choices=sorted(CONFIGS))
     ap.add_argument("--cpu-budget", type=float, default=12.0)
-    ap.add_argument("--profile", action="store_true", help="only run scattering passes (for ncu captures)")
+    ap.add_argument("--profile", action="store_true", help="only run passes of one stage, see --stage (for ncu captures)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"], help="with --profile")
+    ap.add_argument("--stage", default="scattering", choices=["scattering", "kappa", "offdiag"], help="with --profile")
     args = ap.parse_args()
     if args.profile:
         run_profile(args)

@@ -281,17 +281,21 @@ __global__ void __launch_bounds__(256) k_sym_tile(MeshDev m, OrbitDev o, const i
     }
 }
 
-// Bitmap of the q-points each row sampled, [n_row][ceil(n_full/32)] words.
+// Bitmap of the q-points each row sampled, [n_row][ceil(n_full/32)] words, built in shared
+// memory (dynamic, nw words) and written out once.
 __global__ void k_sample_bits(int32_t n_full, const int64_t *rbeg, const int32_t *rlen, const int32_t *list,
                               uint32_t *bits) {
+    extern __shared__ uint32_t sb[];
     const int r = blockIdx.x, nw = (n_full + 31) / 32;
-    uint32_t *br = bits + (size_t)r * nw;
-    for (int i = threadIdx.x; i < nw; i += blockDim.x) br[i] = 0u;
+    for (int i = threadIdx.x; i < nw; i += blockDim.x) sb[i] = 0u;
     __syncthreads();
     for (int64_t i = rbeg[r] + threadIdx.x; i < rbeg[r] + rlen[r]; i += blockDim.x) {
         const int q2 = list[i] - 1;
-        atomicOr(br + (q2 >> 5), 1u << (q2 & 31));
+        atomicOr(sb + (q2 >> 5), 1u << (q2 & 31));
     }
+    __syncthreads();
+    uint32_t *br = bits + (size_t)r * nw;
+    for (int i = threadIdx.x; i < nw; i += blockDim.x) br[i] = sb[i];
 }
 
 // K8: three dot products per row of Xi (kappa.f90:411-413, the lo_gemv calls).
@@ -394,7 +398,8 @@ __global__ void k_split_xi(const double *xi, int64_t n, void *out) {
     }
 }
 
-// DF: xi, fbb as float2 (FP64 runs); otherwise as float (mixed precision).
+// DF: xi, fbb as float2 (FP64 runs); otherwise as float (mixed precision). Loads of four
+// consecutive columns per thread (16 bytes) measured slower than these 4-byte coalesced loads.
 template <bool DF>
 __global__ void __launch_bounds__(256) k_xi_gemv(const void *__restrict__ xi_, int32_t n_row, int64_t n_col,
                                                  const void *__restrict__ fbb_, double *part) {
@@ -402,7 +407,7 @@ __global__ void __launch_bounds__(256) k_xi_gemv(const void *__restrict__ xi_, i
     const int r0 = blockIdx.x * kGemvRows;
     const int nr = min(kGemvRows, n_row - r0);
     const int64_t per = (n_col + gridDim.y - 1) / gridDim.y;
-    const int64_t c0 = per * blockIdx.y, c1 = min(n_col, c0 + per);
+    const int64_t c0 = min(n_col, per * blockIdx.y), c1 = min(n_col, c0 + per);
     float2 acc[kGemvRows][3];
 #pragma unroll
     for (int k = 0; k < kGemvRows; ++k) acc[k][0] = acc[k][1] = acc[k][2] = make_float2(0.f, 0.f);
@@ -575,7 +580,12 @@ int sym_tile_count(int n_rep, int n_ops, int n_mode) {
 cudaError_t launch_sample_bits(int32_t n_full, int32_t n_row, const int64_t *rbeg, const int32_t *rlen,
                                const int32_t *list, uint32_t *bits, cudaStream_t s) {
     if (n_row <= 0) return cudaSuccess;
-    k_sample_bits<<<n_row, 256, 0, s>>>(n_full, rbeg, rlen, list, bits);
+    const size_t sm = sizeof(uint32_t) * (size_t)((n_full + 31) / 32);
+    if (sm > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_sample_bits, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+    }
+    k_sample_bits<<<n_row, 256, sm, s>>>(n_full, rbeg, rlen, list, bits);
     return cudaGetLastError();
 }
 
