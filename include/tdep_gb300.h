@@ -273,11 +273,14 @@ int tdg_kappa_sma_vjp(tdg_ctx *ctx, const tdg_opts *opts, const double *kappa_ba
  * tdg_adjoint_fc3: mwm_bar[n_fc3*27] = (d linewidth / d fc3_mwm)^T lw_bar, the vector-Jacobian
  * product of the three-phonon part of the linewidths (the only part that depends on Phi3)
  * over the rows, samples and q-triplets of the last tdg_scattering, which must have run with
- * the same opts (opts->precision may differ). The kernel recomputes Psi per q-triplet
- * instead of storing it. Layout of mwm_bar as tdg_problem.fc3_mwm; divide by
- * sqrt(m_i m_j m_k) for the derivative with respect to the unweighted force constants.
- * stats (may be NULL, 4 doubles): [0] ms of the whole pass, [1] ms of the adjoint kernel,
- * [2] q-triplets, [3] CTAs.
+ * the same opts (opts->precision may differ). Psi is recomputed per q-triplet instead of
+ * stored. After a large-cell pass (the tensor-core contraction: more than 18 modes, or
+ * forced with opts->tensor_cores) the adjoint runs per batch on the same path, with the
+ * back-contraction on the tensor cores and the gradient accumulated in double-float.
+ * Layout of mwm_bar as tdg_problem.fc3_mwm; divide by sqrt(m_i m_j m_k) for the derivative
+ * with respect to the unweighted force constants. stats (may be NULL, 4 doubles): [0] ms of
+ * the whole pass, [1] ms of the adjoint kernels, [2] q-triplets, [3] CTAs of the shared-
+ * memory kernel or batches of the large-cell path.
  */
 int tdg_adjoint_fc3(tdg_ctx *ctx, const tdg_opts *opts, const double *lw_bar, double *mwm_bar, double *stats);
 

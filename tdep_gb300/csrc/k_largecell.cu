@@ -49,7 +49,9 @@ __device__ __forceinline__ void store_split(__nv_bfloat16 *hi, __nv_bfloat16 *lo
 // ---- real-split eigenvector matrices of every mesh point ----
 // bmat[((q*2 + h)*kp + k)*kp + c], h = 0 hi / 1 lo; k = ri*n + a, c = rj*n + b:
 // [[Er, Ei], [-Ei, Er]] with E[a][b] = component a of mode b of egv/sqrt(omega).
-__global__ void k_build_bmat(int n, int kp, int n_q, const float2 *egvs32, __nv_bfloat16 *bmat) {
+// With transpose, E is replaced by its transpose (E^T[a][b] = E[b][a]): the matrices of the
+// adjoint's back-contraction, which turns a mode index back into a component index.
+__global__ void k_build_bmat(int n, int kp, int n_q, const float2 *egvs32, __nv_bfloat16 *bmat, int transpose) {
     const int64_t per = (int64_t)kp * kp;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (int64_t)n_q * per) return;
@@ -59,7 +61,7 @@ __global__ void k_build_bmat(int n, int kp, int n_q, const float2 *egvs32, __nv_
     float v = 0.f;
     if (k < 2 * n && c < 2 * n) {
         const int ri = k / n, a = k % n, rj = c / n, b = c % n;
-        const float2 E = egvs32[((size_t)q * n + b) * n + a];
+        const float2 E = transpose ? egvs32[((size_t)q * n + a) * n + b] : egvs32[((size_t)q * n + b) * n + a];
         v = ri == 0 ? (rj == 0 ? E.x : E.y) : (rj == 0 ? -E.y : E.x);
     }
     store_split(bmat + ((int64_t)q * 2) * per, bmat + ((int64_t)q * 2 + 1) * per, e, v);
@@ -295,6 +297,9 @@ struct LnDeltaArgs {
     const float2 *psi;
     int n;
     double *gamma, *od;
+    // adjoint: cotangents of the rows; W = G conj(Psi) is written over psi
+    const double *lam;
+    float2 *w;
 };
 
 __host__ __device__ inline size_t ln_delta_smem(int n) {
@@ -302,6 +307,10 @@ __host__ __device__ inline size_t ln_delta_smem(int n) {
            sizeof(int) * 33 + 16;
 }
 
+// ADJ: the adjoint's weights. F holds G_b = lam(row) * nred * dF_b/d|Psi_b|^2 of the
+// survivors (F without |Psi|^2), and W_b = G_b conj(Psi_b) replaces Psi_b for every (b2, b3)
+// of the row mode b1, zero where nothing survives or the row is not sampled.
+template <bool ADJ>
 __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
     extern __shared__ __align__(16) unsigned char sm[];
     const int n = a.n;
@@ -311,9 +320,14 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
     const MeshDev &m = a.mesh;
     const PhononDev &P = a.ph;
     const uint32_t *mask = a.cand_mask + (size_t)rec.cand * 4;
-    if (!((mask[b1 >> 5] >> (b1 & 31)) & 1u)) return;
     const int row = a.rows.rowidx[(size_t)rec.q1 * n + b1];
-    if (row < 0) return;
+    if (!((mask[b1 >> 5] >> (b1 & 31)) & 1u) || row < 0) {
+        if (ADJ) {
+            float2 *wr = a.w + ((int64_t)s * n + b1) * n * n;
+            for (int e = tid; e < n * n; e += bd) wr[e] = make_float2(0.f, 0.f);
+        }
+        return;
+    }
     const int f1 = m.irr_full[rec.q1], q2 = rec.q2, q3 = rec.q3;
     const int i2 = m.full_irr[q2], i3 = m.full_irr[q3];
     double *om2 = (double *)sm, *om3 = om2 + n, *be2 = om3 + n, *be3 = be2 + n, *s2 = be3 + n, *s3 = s2 + n;
@@ -406,13 +420,28 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
             double d0, d1;
             dirac3(live, o1, o2, o3, win8, h, cg, tab, d0, d1);
             if (!nonzero(d0) && !nonzero(d1)) continue;
+            const double n2 = be2[b2], n3 = be3[b3];
+            if (ADJ) {
+                F[e] = a.lam[row] * (double)rec.red_cnt * perm * kLnPrefactor * w *
+                       ((n2 - n3) * d0 + (n2 + n3 + 1.0) * d1);
+                continue;
+            }
             const float2 ps = psi[b2 * n + b3];
             const double cr = ps.x, ci = ps.y;
             const double psisq = kLnPrefactor * (cr * cr + ci * ci) * w;
-            const double n2 = be2[b2], n3 = be3[b3];
             F[e] = perm * psisq * (n2 - n3) * d0 + perm * psisq * (n2 + n3 + 1.0) * d1;
         }
         __syncthreads();
+        if (ADJ) {
+            float2 *wr = a.w + ((int64_t)s * n + b1) * n * n + (int64_t)bb * n;
+            for (int e = tid; e < cnt; e += bd) {
+                const float g = (float)F[e];
+                const float2 ps = wr[e];
+                wr[e] = make_float2(g * ps.x, -g * ps.y);
+            }
+            __syncthreads();
+            continue;
+        }
         // (C) row sums of the block and running column sums
         for (int r = tid; r < nbb; r += bd) {
             double sum = 0.0;
@@ -432,6 +461,7 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
         }
         __syncthreads();
     }
+    if (ADJ) return;
     const int nred = rec.red_cnt;
     if (tid == 0) {
         double gsum = 0.0;
@@ -454,43 +484,72 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
     }
 }
 
+// ---- adjoint: W[b1][b2][b3] into the stage-1 operand planes X[(ri, b1)][b2 n + b3] ----
+__global__ void k_ln_pack(int n, const float2 *w, int nb, int64_t plane, int mp, __nv_bfloat16 *xhi,
+                          __nv_bfloat16 *xlo) {
+    const int s = blockIdx.y;
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n3 = (int64_t)n * n * n;
+    if (s >= nb || e >= n3) return;
+    const int nn = n * n;
+    const int b1 = (int)(e / nn), bc = (int)(e % nn);
+    const float2 v = w[(int64_t)s * n3 + e];
+    __nv_bfloat16 *hi = xhi + (int64_t)s * plane, *lo = xlo + (int64_t)s * plane;
+    store_split(hi, lo, (int64_t)b1 * mp + bc, v.x);
+    store_split(hi, lo, (int64_t)(n + b1) * mp + bc, v.y);
+}
+
+// ---- adjoint: d L / d mwm_t(i,j,k) += 2 Re(phase_t Q[3a1+i][3a2+j][3a3+k]) over the batch ----
+// One thread per (force-constant triplet t, ijk), summing the batch's slots in FP32 and adding
+// the sum into a double-float accumulator (hi, lo): GB300's FP64 pipe would make one FP64
+// add per entry and batch the most expensive part of the pass.
+__global__ void k_ln_grad(int n, Fc3Dev fc, const float2 *ph, const float2 *q, int nb, float *ghi, float *glo) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)fc.n * 27) return;
+    const int t = (int)(i / 27), ijk = (int)(i % 27);
+    const int64_t n3 = (int64_t)n * n * n;
+    const int64_t off = fc.abase[t] + (int64_t)(ijk % 3) * n * n + ((ijk / 3) % 3) * n + ijk / 9;
+    float acc = 0.f;
+    for (int s = 0; s < nb; ++s) {
+        const float2 p = ph[(size_t)s * fc.n + t];
+        const float2 v = q[(int64_t)s * n3 + off];
+        acc = fmaf(p.x, v.x, fmaf(-p.y, v.y, acc));
+    }
+    acc *= 2.f;
+    const float h = ghi[i];
+    const float tsum = h + acc, bb = tsum - h;
+    glo[i] += (h - (tsum - bb)) + (acc - bb);
+    ghi[i] = tsum;
+}
+
 }  // namespace
 
 int ln_kp(int n) { return ((2 * n + 15) / 16) * 16; }
 
 size_t ln_gemm_smem(int kp) { return (size_t)kLnStages * 2 * ((size_t)128 * 16 * 2 + (size_t)16 * kp * 2); }
 
-cudaError_t launch_ln_bmat(int n, int n_q, const float2 *egvs32, __nv_bfloat16 *bmat, cudaStream_t s) {
+cudaError_t launch_ln_bmat(int n, int n_q, const float2 *egvs32, __nv_bfloat16 *bmat, bool transpose,
+                           cudaStream_t s) {
     const int kp = ln_kp(n);
     const int64_t total = (int64_t)n_q * kp * kp;
     if (total <= 0) return cudaSuccess;
-    k_build_bmat<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(n, kp, n_q, egvs32, bmat);
+    k_build_bmat<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(n, kp, n_q, egvs32, bmat, transpose ? 1 : 0);
     return cudaGetLastError();
 }
 
-cudaError_t launch_ln_batch(const LnBatch &b, cudaStream_t s) {
+namespace {
+// The three tcgen05 stages from the operand in the xa planes to b.psi, with the real-split
+// matrices bmat (forward: E; adjoint: E^T).
+cudaError_t ln_contract(const LnBatch &b, const __nv_bfloat16 *bmat, cudaStream_t s) {
     const int n = b.n, kp = ln_kp(n), M = n * n;
-    if (b.nb <= 0) return cudaSuccess;
-    if (kp > 256) return cudaErrorNotSupported;
     cudaError_t e;
-    {
-        dim3 grid((unsigned)((b.fc.n + 255) / 256), (unsigned)b.nb);
-        k_ln_phases<<<grid, 256, 0, s>>>(b.fc, b.mesh, b.trip, b.nb, b.phase);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    }
-    {
-        const int64_t n3 = (int64_t)n * n * n;
-        dim3 grid((unsigned)((n3 + 255) / 256), (unsigned)b.nb);
-        k_ln_pretransform<<<grid, 256, 0, s>>>(n, n / 3, b.fc, b.phase, b.nb, b.plane, b.mp, b.xa_hi, b.xa_lo);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    }
     const size_t smem = ln_gemm_smem(kp);
     if ((e = cudaFuncSetAttribute(k_ln_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
         return e;
     LnGemmArgs g;
     g.plane = b.plane;
     g.mp = b.mp;
-    g.bmat = b.bmat;
+    g.bmat = bmat;
     g.trip = b.trip;
     g.irr_full = b.mesh.irr_full;
     g.n = n;
@@ -508,6 +567,10 @@ cudaError_t launch_ln_batch(const LnBatch &b, cudaStream_t s) {
         k_ln_gemm<<<grid, kLnThreads, smem, s>>>(g);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
+    return cudaSuccess;
+}
+
+LnDeltaArgs delta_args(const LnBatch &b) {
     LnDeltaArgs d;
     d.mesh = b.mesh;
     d.ph = b.ph;
@@ -516,13 +579,71 @@ cudaError_t launch_ln_batch(const LnBatch &b, cudaStream_t s) {
     d.red = b.red;
     d.cand_mask = b.cand_mask;
     d.psi = b.psi;
-    d.n = n;
+    d.n = b.n;
     d.gamma = b.gamma;
     d.od = b.od;
+    d.lam = b.lam;
+    d.w = b.psi;
+    return d;
+}
+}  // namespace
+
+cudaError_t launch_ln_adjoint_batch(const LnBatch &b, cudaStream_t s) {
+    const int n = b.n, kp = ln_kp(n);
+    if (b.nb <= 0) return cudaSuccess;
+    if (kp > 256) return cudaErrorNotSupported;
+    cudaError_t e;
+    const int64_t n3 = (int64_t)n * n * n;
+    {
+        dim3 grid((unsigned)((b.fc.n + 255) / 256), (unsigned)b.nb);
+        k_ln_phases<<<grid, 256, 0, s>>>(b.fc, b.mesh, b.trip, b.nb, b.phase);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        dim3 g2((unsigned)((n3 + 255) / 256), (unsigned)b.nb);
+        k_ln_pretransform<<<g2, 256, 0, s>>>(n, n / 3, b.fc, b.phase, b.nb, b.plane, b.mp, b.xa_hi, b.xa_lo);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    if ((e = ln_contract(b, b.bmat, s)) != cudaSuccess) return e;  // Psi
+    const LnDeltaArgs d = delta_args(b);
     const size_t dsm = ln_delta_smem(n);
-    if ((e = cudaFuncSetAttribute(k_ln_delta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm)) != cudaSuccess)
+    if ((e = cudaFuncSetAttribute(k_ln_delta<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm)) !=
+        cudaSuccess)
         return e;
-    k_ln_delta<<<dim3((unsigned)n, (unsigned)b.nb), 256, dsm, s>>>(d);
+    k_ln_delta<true><<<dim3((unsigned)n, (unsigned)b.nb), 256, dsm, s>>>(d);  // W over Psi
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    {
+        dim3 grid((unsigned)((n3 + 255) / 256), (unsigned)b.nb);
+        k_ln_pack<<<grid, 256, 0, s>>>(n, b.psi, b.nb, b.plane, b.mp, b.xa_hi, b.xa_lo);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    if ((e = ln_contract(b, b.bmat_t, s)) != cudaSuccess) return e;  // Q over W
+    const int64_t ne = (int64_t)b.fc.n * 27;
+    k_ln_grad<<<(unsigned)((ne + 255) / 256), 256, 0, s>>>(n, b.fc, b.phase, b.psi, b.nb, b.grad_hi, b.grad_lo);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ln_batch(const LnBatch &b, cudaStream_t s) {
+    const int n = b.n, kp = ln_kp(n);
+    if (b.nb <= 0) return cudaSuccess;
+    if (kp > 256) return cudaErrorNotSupported;
+    cudaError_t e;
+    {
+        dim3 grid((unsigned)((b.fc.n + 255) / 256), (unsigned)b.nb);
+        k_ln_phases<<<grid, 256, 0, s>>>(b.fc, b.mesh, b.trip, b.nb, b.phase);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    {
+        const int64_t n3 = (int64_t)n * n * n;
+        dim3 grid((unsigned)((n3 + 255) / 256), (unsigned)b.nb);
+        k_ln_pretransform<<<grid, 256, 0, s>>>(n, n / 3, b.fc, b.phase, b.nb, b.plane, b.mp, b.xa_hi, b.xa_lo);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    if ((e = ln_contract(b, b.bmat, s)) != cudaSuccess) return e;
+    const LnDeltaArgs d = delta_args(b);
+    const size_t dsm = ln_delta_smem(n);
+    if ((e = cudaFuncSetAttribute(k_ln_delta<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm)) !=
+        cudaSuccess)
+        return e;
+    k_ln_delta<false><<<dim3((unsigned)n, (unsigned)b.nb), 256, dsm, s>>>(d);
     return cudaGetLastError();
 }
 

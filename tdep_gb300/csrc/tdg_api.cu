@@ -232,6 +232,9 @@ struct tdg_ctx {
     DevBuf<__nv_bfloat16> d_bmat, d_lnx;
     DevBuf<float2> d_psi, d_lnph;
     bool bmat_ready = false;
+    bool last_ln = false;  // the last tdg_scattering took the large-cell (tensor-core) path
+    DevBuf<__nv_bfloat16> d_bmat_t;  // transposed real-split matrices (adjoint)
+    DevBuf<float> d_ghi, d_glo;      // double-float gradient accumulator (large-cell adjoint)
     int xi_fmt = -1;  // d_xi_df holds the current Xi as float pairs (1), floats (0), or nothing (-1)
     // off-diagonal kappa inputs (host copies; uploaded by the first tdg_kappa_offdiag)
     std::vector<double> irr_dyngrad, atom_shift, q_full;
@@ -721,6 +724,56 @@ int read_status(tdg_ctx *c) {
 
 }  // namespace
 
+namespace {
+// Buffers and the batch descriptor of the large-cell path (real-split eigenvector matrices
+// built once per context; operand planes, Psi and phases for nbmax q-triplets, bounded to
+// 2 GB).
+int ln_batch_setup(tdg_ctx *c, const MeshDev &mesh, const PhononDev &ph, const RowsDev &rows, const Fc3Dev &fc,
+                   int ntrip, LnBatch &b, int &nbmax) {
+    cudaStream_t s = c->stream;
+    const int n = c->n, N = c->N;
+    const int kp = ln_kp(n), mp = ((n * n + 127) / 128) * 128;
+    const int64_t plane = (int64_t)kp * mp;
+    const size_t per_slot = 4 * (size_t)plane * sizeof(__nv_bfloat16) + (size_t)n * n * n * sizeof(float2) +
+                            (size_t)c->n_fc3 * sizeof(float2);
+    nbmax = (int)std::max<size_t>(1, std::min<size_t>(256, ((size_t)2 << 30) / per_slot));
+    nbmax = std::max(1, std::min(nbmax, ntrip));
+    if (!c->bmat_ready) {
+        CUDA_TRY(c->d_bmat.alloc((size_t)N * 2 * kp * kp));
+        CUDA_TRY(launch_ln_bmat(n, N, c->d_egvs32.p, c->d_bmat.p, false, s));
+        c->bmat_ready = true;
+    }
+    const __nv_bfloat16 *old = c->d_lnx.p;
+    CUDA_TRY(c->d_lnx.alloc(4 * (size_t)plane * nbmax));
+    CUDA_TRY(c->d_psi.alloc((size_t)nbmax * n * n * n));
+    CUDA_TRY(c->d_lnph.alloc((size_t)nbmax * c->n_fc3));
+    // padding rows (k >= 2n) of the operand planes must read as zero; no kernel writes them
+    if (c->d_lnx.p != old) CUDA_TRY(cudaMemsetAsync(c->d_lnx.p, 0, sizeof(__nv_bfloat16) * c->d_lnx.n, s));
+    const size_t slots = c->d_lnx.n / (4 * (size_t)plane);
+    b = LnBatch{};
+    b.mesh = mesh;
+    b.ph = ph;
+    b.rows = rows;
+    b.fc = fc;
+    b.red = c->d_red.p;
+    b.cand_mask = c->d_mask.p;
+    b.n = n;
+    b.plane = plane;
+    b.mp = mp;
+    b.xa_hi = c->d_lnx.p;
+    b.xa_lo = b.xa_hi + plane * slots;
+    b.xb_hi = b.xa_lo + plane * slots;
+    b.xb_lo = b.xb_hi + plane * slots;
+    b.bmat = c->d_bmat.p;
+    b.phase = c->d_lnph.p;
+    b.psi = c->d_psi.p;
+    b.gamma = c->d_gamma.p;
+    b.od = c->d_xi.p;
+    b.status = c->d_status.p;
+    return kOk;
+}
+}  // namespace
+
 extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *ql, double *linewidth, double *qs_out,
                               double *stats) {
     XferScope xs(c ? c->xfer : nullptr);
@@ -1190,50 +1243,13 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         a.gamma = c->d_gamma.p;
         a.od = c->d_xi.p;
         a.status = c->d_status.p;
-        if (n > 18 || o->tensor_cores) {
+        c->last_ln = n > 18 || o->tensor_cores;
+        if (c->last_ln) {
             // large-cell path: batches of q-triplets through the tcgen05 contraction
-            const int kp = ln_kp(n), mp = ((n * n + 127) / 128) * 128;
-            const int64_t plane = (int64_t)kp * mp;
-            const size_t per_slot = 4 * (size_t)plane * sizeof(__nv_bfloat16) + (size_t)n * n * n * sizeof(float2) +
-                                    (size_t)c->n_fc3 * sizeof(float2);
-            int nbmax = (int)std::max<size_t>(1, std::min<size_t>(256, ((size_t)2 << 30) / per_slot));
-            nbmax = std::max(1, std::min(nbmax, ntrip));
-            if (!c->bmat_ready) {
-                chk(c->d_bmat.alloc((size_t)N * 2 * kp * kp));
-                if (e != cudaSuccess)
-                    return set_error(kErrDevice, std::string("allocation failed: ") + cudaGetErrorString(e));
-                CUDA_TRY(launch_ln_bmat(n, N, c->d_egvs32.p, c->d_bmat.p, s));
-                c->bmat_ready = true;
-            }
-            const __nv_bfloat16 *old = c->d_lnx.p;
-            chk(c->d_lnx.alloc(4 * (size_t)plane * nbmax));
-            chk(c->d_psi.alloc((size_t)nbmax * n * n * n));
-            chk(c->d_lnph.alloc((size_t)nbmax * c->n_fc3));
-            if (e != cudaSuccess) return set_error(kErrDevice, std::string("allocation failed: ") + cudaGetErrorString(e));
-            // padding rows (k >= 2n) of the operand planes must read as zero; no kernel writes them
-            if (c->d_lnx.p != old)
-                CUDA_TRY(cudaMemsetAsync(c->d_lnx.p, 0, sizeof(__nv_bfloat16) * c->d_lnx.n, s));
-            const size_t slots = c->d_lnx.n / (4 * (size_t)plane);
+            int nbmax = 0;
             LnBatch b;
-            b.mesh = mesh;
-            b.ph = ph;
-            b.rows = rows;
-            b.fc = a.fc;
-            b.red = c->d_red.p;
-            b.cand_mask = c->d_mask.p;
-            b.n = n;
-            b.plane = plane;
-            b.mp = mp;
-            b.xa_hi = c->d_lnx.p;
-            b.xa_lo = b.xa_hi + plane * slots;
-            b.xb_hi = b.xa_lo + plane * slots;
-            b.xb_lo = b.xb_hi + plane * slots;
-            b.bmat = c->d_bmat.p;
-            b.phase = c->d_lnph.p;
-            b.psi = c->d_psi.p;
-            b.gamma = c->d_gamma.p;
-            b.od = c->d_xi.p;
-            b.status = c->d_status.p;
+            st = ln_batch_setup(c, mesh, ph, rows, a.fc, ntrip, b, nbmax);
+            if (st) return st;
             for (int t0 = 0; t0 < ntrip; t0 += nbmax) {
                 b.trip = c->d_trip.p + t0;
                 b.nb = std::min(nbmax, ntrip - t0);
@@ -1750,6 +1766,80 @@ extern "C" int tdg_kappa_sma_vjp(tdg_ctx *c, const tdg_opts *o, const double *ka
     return kOk;
 }
 
+namespace {
+// tdg_adjoint_fc3 after a large-cell (tensor-core) scattering pass: per batch the forward
+// contraction again, W = G conj(Psi) from the delta kernel, the back-contraction with the
+// transposed eigenvector matrices into Q, and 2 Re(phase Q) accumulated per force-constant
+// entry in double-float.
+int adjoint_large_cell(tdg_ctx *c, const std::vector<double> &lam, double *mwm_bar, double *stats) {
+    cudaStream_t s = c->stream;
+    const int n = c->n, N = c->N, ntrip = c->last_ntrip;
+    const int64_t nm = (int64_t)c->n_fc3 * 27;
+    CUDA_TRY(c->d_lam.upload(lam.data(), lam.size(), s));
+    if (c->d_bmat_t.n == 0) {
+        const int kp = ln_kp(n);
+        CUDA_TRY(c->d_bmat_t.alloc((size_t)N * 2 * kp * kp));
+        CUDA_TRY(launch_ln_bmat(n, N, c->d_egvs32.p, c->d_bmat_t.p, true, s));
+    }
+    CUDA_TRY(c->d_ghi.alloc(nm));
+    CUDA_TRY(c->d_glo.alloc(nm));
+    cudaEvent_t *ev = c->ev;
+    CUDA_TRY(cudaEventRecord(ev[0], s));
+    CUDA_TRY(cudaMemsetAsync(c->d_ghi.p, 0, sizeof(float) * nm, s));
+    CUDA_TRY(cudaMemsetAsync(c->d_glo.p, 0, sizeof(float) * nm, s));
+    CUDA_TRY(cudaMemsetAsync(c->d_status.p, 0, sizeof(int32_t), s));
+    Fc3Dev fc;
+    fc.n = c->n_fc3;
+    fc.n_atom = c->na;
+    fc.blk_ptr = c->fc3_blk.p;
+    fc.lv = c->fc3_lv.p;
+    fc.mwm = c->fc3_mwm.p;
+    fc.mwm32 = c->fc3_mwm32.p;
+    fc.twiddle = c->tw.p;
+    fc.twiddle32 = c->tw32.p;
+    fc.abase = c->fc3_abase.p;
+    LnBatch b;
+    int nbmax = 0, batches = 0;
+    int st = ln_batch_setup(c, c->mesh(), c->last_ph, c->last_rows, fc, std::max(ntrip, 1), b, nbmax);
+    if (st) return st;
+    b.gamma = nullptr;
+    b.od = nullptr;
+    b.bmat_t = c->d_bmat_t.p;
+    b.lam = c->d_lam.p;
+    b.grad_hi = c->d_ghi.p;
+    b.grad_lo = c->d_glo.p;
+    CUDA_TRY(cudaEventRecord(ev[1], s));
+    for (int t0 = 0; t0 < ntrip; t0 += nbmax, ++batches) {
+        b.trip = c->d_trip.p + t0;
+        b.nb = std::min(nbmax, ntrip - t0);
+        CUDA_TRY(launch_ln_adjoint_batch(b, s));
+    }
+    CUDA_TRY(cudaEventRecord(ev[2], s));
+    std::vector<float> hi(nm), lo(nm);
+    CUDA_TRY(copy_async(hi.data(), c->d_ghi.p, sizeof(float) * nm, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(copy_async(lo.data(), c->d_glo.p, sizeof(float) * nm, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaEventRecord(ev[3], s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    st = read_status(c);
+    if (st) return st;
+    for (int sidx = 0; sidx < c->n_fc3; ++sidx) {
+        const int t = c->fc3_perm[sidx];
+        for (int k = 0; k < 27; ++k)
+            mwm_bar[(size_t)t * 27 + k] = (double)hi[(size_t)sidx * 27 + k] + (double)lo[(size_t)sidx * 27 + k];
+    }
+    if (stats) {
+        float ms_all = 0.f, ms_k = 0.f;
+        CUDA_TRY(cudaEventElapsedTime(&ms_all, ev[0], ev[3]));
+        CUDA_TRY(cudaEventElapsedTime(&ms_k, ev[1], ev[2]));
+        stats[0] = ms_all;
+        stats[1] = ms_k;
+        stats[2] = ntrip;
+        stats[3] = batches;
+    }
+    return kOk;
+}
+}  // namespace
+
 extern "C" int tdg_adjoint_fc3(tdg_ctx *c, const tdg_opts *o, const double *lw_bar, double *mwm_bar, double *stats) {
     XferScope xs(c ? c->xfer : nullptr);
     PoolScope pscope(c ? c->stream : nullptr, c ? c->pool : nullptr);
@@ -1774,6 +1864,7 @@ extern "C" int tdg_adjoint_fc3(tdg_ctx *c, const tdg_opts *o, const double *lw_b
         lam[r] = acc / (double)dg;
     }
     const int ntrip = c->last_ntrip;
+    if (c->last_ln) return adjoint_large_cell(c, lam, mwm_bar, stats);
     // the CTA's gradient slice lives in shared memory when it is small enough
     const bool acc_smem = (size_t)c->n_fc3 * 27 * sizeof(double) <= 48 * 1024;
     const int grid = threephonon_adjoint_grid(n, o->precision, c->n_sm, ntrip, c->n_fc3, acc_smem);

@@ -197,12 +197,22 @@ struct LnBatch {
     float2 *psi;             // [nb * n^3]
     double *gamma, *od;
     int32_t *status;
+    // adjoint (launch_ln_adjoint_batch): transposed matrices, row cotangents and the
+    // double-float gradient accumulator [n_fc * 27] in block-sorted order
+    const __nv_bfloat16 *bmat_t = nullptr;
+    const double *lam = nullptr;
+    float *grad_hi = nullptr, *grad_lo = nullptr;
 };
 int ln_kp(int n);
 size_t ln_gemm_smem(int kp);
-// Real-split eigenvector matrices of every mesh point: n_q * 2 * ln_kp(n)^2 BF16 (hi, lo).
-cudaError_t launch_ln_bmat(int n, int n_q, const float2 *egvs32, __nv_bfloat16 *bmat, cudaStream_t s);
+// Real-split eigenvector matrices of every mesh point: n_q * 2 * ln_kp(n)^2 BF16 (hi, lo);
+// transposed for the adjoint's back-contraction.
+cudaError_t launch_ln_bmat(int n, int n_q, const float2 *egvs32, __nv_bfloat16 *bmat, bool transpose,
+                           cudaStream_t s);
 cudaError_t launch_ln_batch(const LnBatch &b, cudaStream_t s);
+// Adjoint of one batch: forward contraction, W = G conj(Psi), back-contraction with E^T into Q,
+// gradient of the mass-weighted force constants added into grad_hi/grad_lo.
+cudaError_t launch_ln_adjoint_batch(const LnBatch &b, cudaStream_t s);
 
 // Isotope scattering (scattering_isotope.f90): adds into gamma and xi.
 cudaError_t launch_isotope(const MeshDev &m, const PhononDev &ph, const RowsDev &rows, const int32_t *row_q1,

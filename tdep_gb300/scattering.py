@@ -383,7 +383,7 @@ class ScatteringRates:
         N.check(self._lib.tdg_adjoint_fc3(self._ctx, C.byref(o), N.ptr(lb, C.c_double), N.ptr(out, C.c_double),
                                           N.ptr(st, C.c_double)), "tdg_adjoint_fc3")
         self.adjoint_stats = {"ms": float(st[0]), "kernel_ms": float(st[1]), "triplets": int(st[2]),
-                              "ctas": int(st[3])}
+                              "batches_or_ctas": int(st[3])}
         return out.reshape(p.n_fc3, 27)
 
 

@@ -115,3 +115,42 @@ def test_autograd_through_a_parameterisation(configs):
         fd = (vals[0] - vals[1]) / (2 * h)
         assert abs(fd - gx[j]) <= 1e-5 * np.abs(gx).max() + 1e-4 * abs(fd)
     sr.close()
+
+
+@pytest.mark.parametrize("name,grid,it", [("rocksalt", (6, 6, 6), 2), ("perovskite", (4, 4, 4), 2)])
+def test_adjoint_tensor_core_path_matches_fp64(configs, name, grid, it):
+    """After a pass on the large-cell path (forced at small n), the adjoint runs per batch on
+    the tensor cores (back-contraction with the transposed eigenvector matrices); against the
+    FP64 shared-memory adjoint of the same samples, at the mixed-precision bar."""
+    prob = Problem.load(configs[name], grid, readiso=True)
+    kw = dict(temperature=300.0, integrationtype=it, isotopescattering=False, seed=17)
+    o64 = Options(**kw)
+    otc = Options(precision="mixed", tensor_cores=True, **kw)
+    lists = QLists.monte_carlo(prob, o64)
+    rng = np.random.default_rng(4)
+    lw_bar = rng.normal(size=(prob.n_irr, prob.n_mode))
+    sr = ScatteringRates(prob)
+    sr.generate(o64, lists)
+    g64 = sr.adjoint_fc3(o64, lw_bar)
+    sr.generate(otc, lists)
+    gtc = sr.adjoint_fc3(otc, lw_bar)
+    assert sr.adjoint_stats["batches_or_ctas"] >= 1
+    sr.close()
+    assert np.linalg.norm(gtc - g64) <= 1e-3 * np.linalg.norm(g64)
+
+
+def test_adjoint_large_cell_matches_oracle(configs):
+    """30 modes (displaced 2x1x1 supercell, identity only): the large-cell adjoint against the
+    oracle's FP64 reverse-mode restatement."""
+    prob = Problem.load(configs["supercell"], (3, 3, 3), readiso=True)
+    opts = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=6, precision="mixed",
+                   qg3ph=(2, 2, 2))
+    lists = QLists.monte_carlo(prob, opts)
+    rng = np.random.default_rng(5)
+    lw_bar = rng.normal(size=(prob.n_irr, prob.n_mode))
+    sr = ScatteringRates(prob)
+    sr.generate(opts, lists)
+    g = sr.adjoint_fc3(opts, lw_bar)
+    sr.close()
+    ref = orc.adjoint_fc3(prob, opts, lists, lw_bar)
+    assert np.linalg.norm(g - ref) <= 1e-3 * np.linalg.norm(ref)
