@@ -660,4 +660,64 @@ cudaError_t launch_xi_gemv(const void *xi, int32_t n_row, int64_t n_col, bool df
     return cudaGetLastError();
 }
 
+namespace {
+// rot[o][q] = full-mesh index of R_o q, -1 when R_o q is off the mesh: (R q)_i = num / L with
+// num = sum_j R_ij g_j (L / N_j) in 32-bit integers (|num| < 3 L max N), on the mesh when
+// num is a multiple of L / N_i.
+__global__ void k_rot_table(int g0, int g1, int g2, int L, int n_full, const int32_t *op_recfrac, int32_t *rot) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int o = blockIdx.y;
+    if (q >= n_full) return;
+    const int32_t *R = op_recfrac + 9 * o;
+    const int g[3] = {g0, g1, g2};
+    const int gi[3] = {q / (g1 * g2), (q / g2) % g1, q % g2};
+    int out[3];
+    for (int i = 0; i < 3; ++i) {
+        const int num = R[i] * gi[0] * (L / g0) + R[i + 3] * gi[1] * (L / g1) + R[i + 6] * gi[2] * (L / g2);
+        const int step = L / g[i];
+        if (num % step != 0) {
+            rot[(size_t)o * n_full + q] = -1;
+            return;
+        }
+        int v = (num / step) % g[i];
+        if (v < 0) v += g[i];
+        out[i] = v;
+    }
+    rot[(size_t)o * n_full + q] = (out[0] * g1 + out[1]) * g2 + out[2];
+}
+
+// Eigenvectors scaled by 1/sqrt(omega) (scattering_threephonon.f90:67,93,102), FP64 and FP32,
+// zero for omega < lo_freqtol; IEEE sqrt and division as on the host.
+__global__ void k_egv_scaled(int64_t nm, int n, const double2 *egv, const double *omega, double2 *egvs,
+                             float2 *egvs32) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nm * n) return;
+    const double om = omega[i / n];
+    double2 v = make_double2(0.0, 0.0);
+    if (!(om < kFreqTolD)) {
+        const double sq = sqrt(om);
+        const double2 e = egv[i];
+        v = make_double2(e.x / sq, e.y / sq);
+    }
+    egvs[i] = v;
+    egvs32[i] = make_float2((float)v.x, (float)v.y);
+}
+}  // namespace
+
+cudaError_t launch_rot_table(const int32_t grid[3], int L, int n_full, int n_op, const int32_t *op_recfrac,
+                             int32_t *rot, cudaStream_t s) {
+    if (n_full <= 0 || n_op <= 0) return cudaSuccess;
+    dim3 g((unsigned)((n_full + 255) / 256), (unsigned)n_op);
+    k_rot_table<<<g, 256, 0, s>>>(grid[0], grid[1], grid[2], L, n_full, op_recfrac, rot);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_egv_scaled(int64_t nm, int n, const double2 *egv, const double *omega, double2 *egvs,
+                              float2 *egvs32, cudaStream_t s) {
+    const int64_t total = nm * n;
+    if (total <= 0) return cudaSuccess;
+    k_egv_scaled<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(nm, n, egv, omega, egvs, egvs32);
+    return cudaGetLastError();
+}
+
 }  // namespace tdg

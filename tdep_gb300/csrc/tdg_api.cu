@@ -366,39 +366,6 @@ int check_problem(const tdg_problem *p) {
     return kOk;
 }
 
-// Image of every mesh point under every operation, in exact integer arithmetic on the
-// grid coordinates; -1 when the rotated point is not on the mesh.
-void build_rot_table(const tdg_problem *p, int L, std::vector<int32_t> &rot) {
-    const int N = p->n_full;
-    const int *g = p->grid;
-    rot.assign((size_t)p->n_op * N, -1);
-    // one operation per task; (R q)_i = sum_j R_ij g_j / N_j = num / L with |num| < 3 L max(N),
-    // in 32-bit integers
-    parallel_for(p->n_op, [&](int64_t o) {
-        const int32_t *R = p->op_recfrac + 9 * o;
-        int32_t *dst = rot.data() + (size_t)o * N;
-        const int m0 = L / g[0], m1 = L / g[1], m2 = L / g[2];
-        for (int q = 0; q < N; ++q) {
-            const int gi0 = q / (g[1] * g[2]), gi1 = (q / g[2]) % g[1], gi2 = q % g[2];
-            int out[3];
-            bool ok = true;
-            for (int i = 0; i < 3 && ok; ++i) {
-                const int num = R[i] * gi0 * m0 + R[i + 3] * gi1 * m1 + R[i + 6] * gi2 * m2;
-                // num / L must be a multiple of 1 / g_i
-                const int step = L / g[i];
-                if (num % step != 0) {
-                    ok = false;
-                    break;
-                }
-                int v = (num / step) % g[i];
-                if (v < 0) v += g[i];
-                out[i] = v;
-            }
-            if (ok) dst[q] = (out[0] * g[1] + out[1]) * g[2] + out[2];
-        }
-    });
-}
-
 }  // namespace
 
 namespace {
@@ -507,27 +474,13 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
 
     pt.mark("device and host copies");
     cudaStream_t s = c->stream;
-    std::vector<int32_t> rot;
-    build_rot_table(p, c->L, rot);
     pt.mark("rotation table");
     std::vector<int32_t> irr_full0(c->nirr), full_irr0(c->N), irr_ops0((size_t)c->nirr * c->nop, 0);
     for (int i = 0; i < c->nirr; ++i) irr_full0[i] = c->irr_full[i] - 1;
     for (int i = 0; i < c->N; ++i) full_irr0[i] = c->full_irr[i] - 1;
     for (size_t i = 0; i < irr_ops0.size(); ++i) irr_ops0[i] = c->irr_ops[i] > 0 ? c->irr_ops[i] - 1 : -1;
-    // Eigenvectors as stored, and scaled by 1/sqrt(omega) as the scattering routines use
-    // them (egv(:,b)/sqrt(om), scattering_threephonon.f90:67,93,102), once per mode.
-    std::vector<double2> egv(nm * c->n), egvs(nm * c->n);
-    std::vector<float2> egvs32(nm * c->n);
-    for (size_t qb = 0; qb < nm; ++qb) {
-        const double om = c->omega[qb];
-        const double sq = om < kFreqTol ? 0.0 : std::sqrt(om);
-        for (int r = 0; r < c->n; ++r) {
-            const size_t i = qb * c->n + r;
-            egv[i] = make_double2(p->egv[2 * i], p->egv[2 * i + 1]);
-            egvs[i] = om < kFreqTol ? make_double2(0.0, 0.0) : make_double2(egv[i].x / sq, egv[i].y / sq);
-            egvs32[i] = make_float2((float)egvs[i].x, (float)egvs[i].y);
-        }
-    }
+    // the eigenvectors go up as stored; the scaled copies (egv(:,b)/sqrt(om),
+    // scattering_threephonon.f90:67,93,102) and the rotation table are built on the device
     pt.mark("eigenvector copies");
     // Force constants sorted by atom block (a1,a2,a3).
     const int na = c->na;
@@ -589,16 +542,23 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
     auto chk = [&](cudaError_t x) {
         if (e == cudaSuccess) e = x;
     };
-    chk(c->rot.upload(rot.data(), rot.size(), s));
+    {
+        DevBuf<int32_t> orf;
+        chk(orf.upload(p->op_recfrac, (size_t)9 * c->nop, s));
+        chk(c->rot.alloc((size_t)c->nop * c->N));
+        if (e == cudaSuccess) chk(launch_rot_table(c->grid, c->L, c->N, c->nop, orf.p, c->rot.p, s));
+    }
     chk(c->d_irr_full.upload(irr_full0.data(), irr_full0.size(), s));
     chk(c->d_full_irr.upload(full_irr0.data(), full_irr0.size(), s));
     chk(c->d_irr_nop.upload(c->irr_nop.data(), c->irr_nop.size(), s));
     chk(c->d_irr_ops.upload(irr_ops0.data(), irr_ops0.size(), s));
     chk(c->d_omega.upload(c->omega.data(), c->omega.size(), s));
     chk(c->d_vel.upload(c->vel.data(), c->vel.size(), s));
-    chk(c->d_egv.upload(egv.data(), egv.size(), s));
-    chk(c->d_egvs.upload(egvs.data(), egvs.size(), s));
-    chk(c->d_egvs32.upload(egvs32.data(), egvs32.size(), s));
+    chk(c->d_egv.upload(reinterpret_cast<const double2 *>(p->egv), nm * c->n, s));
+    chk(c->d_egvs.alloc(nm * c->n));
+    chk(c->d_egvs32.alloc(nm * c->n));
+    if (e == cudaSuccess)
+        chk(launch_egv_scaled((int64_t)nm, c->n, c->d_egv.p, c->d_omega.p, c->d_egvs.p, c->d_egvs32.p, s));
     chk(c->d_disorder.upload(c->disorder.data(), c->disorder.size(), s));
     chk(c->fc3_blk.upload(blk_ptr3.data(), blk_ptr3.size(), s));
     chk(c->fc3_abase.upload(abase3.data(), abase3.size(), s));

@@ -219,6 +219,14 @@ cudaError_t launch_isotope(const MeshDev &m, const PhononDev &ph, const RowsDev 
                            const int32_t *row_b1, const double *disorder, int32_t n_atom, double *gamma,
                            double *xi, cudaStream_t s);
 
+// Context tables built on the device: the rotation table rot[op][q] (integer rotation of
+// fractional reciprocal coordinates on the mesh, -1 off the mesh) and the eigenvectors
+// scaled by 1/sqrt(omega) in FP64 and FP32.
+cudaError_t launch_rot_table(const int32_t grid[3], int L, int n_full, int n_op, const int32_t *op_recfrac,
+                             int32_t *rot, cudaStream_t s);
+cudaError_t launch_egv_scaled(int64_t nm, int n, const double2 *egv, const double *omega, double2 *egvs,
+                              float2 *egvs32, cudaStream_t s);
+
 // Orbits of the little group of every irreducible q1 on the mesh (built once per context).
 struct OrbitDev {
     const int32_t *rep_ptr;  // [n_irr+1] first representative of q1
