@@ -8,6 +8,7 @@
 #include <complex>
 #include <cstdint>
 #include <string>
+#include <functional>
 #include <thread>
 #include <vector>
 
@@ -84,23 +85,20 @@ class PhaseTimer {
 };
 
 // f(i) for i in [0, n) on all hardware threads (dynamic assignment, one index at a time);
-// f must be safe to run concurrently for different i.
+// f must be safe to run concurrently for different i. Runs on a fixed pool of worker threads
+// created on first use (one job at a time; a call made while another runs, or in a child
+// process after fork, runs serially in the caller).
+bool pool_run(int64_t n, const std::function<void(int64_t)> &f);
+
 template <typename F>
 void parallel_for(int64_t n, F f) {
-    const unsigned nth = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), 64u));
-    if (n <= 1 || nth == 1) {
+    if (n <= 1) {
         for (int64_t i = 0; i < n; ++i) f(i);
         return;
     }
-    std::atomic<int64_t> next{0};
-    auto work = [&]() {
-        for (int64_t i = next++; i < n; i = next++) f(i);
-    };
-    std::vector<std::thread> th;
-    const unsigned used = (unsigned)std::min<int64_t>(n, nth);
-    for (unsigned t = 1; t < used; ++t) th.emplace_back(work);
-    work();
-    for (auto &x : th) x.join();
+    const std::function<void(int64_t)> fn = f;
+    if (!pool_run(n, fn))
+        for (int64_t i = 0; i < n; ++i) f(i);
 }
 const char *last_error();
 

@@ -4,8 +4,12 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <condition_variable>
 #include <fstream>
 #include <memory>
+#include <mutex>
+
+#include <unistd.h>
 
 #include "../../../include/tdep_gb300.h"
 #include "crystal.hpp"
@@ -67,6 +71,71 @@ double harmonic_oscillator_cv(double temp, double omega) {
     if (x < 2E-2) return kKbHartree * (1.0 - x * x / 12.0 + x * x * x * x / 240.0);
     const double em1 = std::exp(x) - 1.0;
     return kKbHartree * x * x * std::exp(x) / (em1 * em1);
+}
+
+namespace {
+
+// Worker threads of parallel_for, created once (hardware threads - 1; the caller is the last
+// one). One job at a time; a job finishes only after every worker has taken part in it.
+struct Pool {
+    std::mutex mu;
+    std::condition_variable cv_start, cv_done;
+    std::atomic<bool> busy{false};
+    const std::function<void(int64_t)> *fn = nullptr;
+    int64_t n = 0;
+    std::atomic<int64_t> next{0};
+    uint64_t gen = 0;
+    unsigned active = 0, nw = 0;
+    pid_t pid = 0;
+    Pool() {
+        pid = getpid();
+        const unsigned hc = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), 64u));
+        nw = hc - 1;
+        for (unsigned t = 0; t < nw; ++t) std::thread([this] { loop(); }).detach();
+    }
+    void work() {
+        for (int64_t i = next++; i < n; i = next++) (*fn)(i);
+    }
+    void loop() {
+        uint64_t seen = 0;
+        for (;;) {
+            std::unique_lock<std::mutex> lk(mu);
+            cv_start.wait(lk, [&] { return gen != seen; });
+            seen = gen;
+            lk.unlock();
+            work();
+            lk.lock();
+            if (--active == 0) cv_done.notify_one();
+        }
+    }
+    bool run(int64_t count, const std::function<void(int64_t)> &f) {
+        if (nw == 0 || getpid() != pid) return false;
+        bool idle = false;
+        if (!busy.compare_exchange_strong(idle, true)) return false;
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            fn = &f;
+            n = count;
+            next = 0;
+            active = nw;
+            ++gen;
+        }
+        cv_start.notify_all();
+        work();
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            cv_done.wait(lk, [&] { return active == 0; });
+        }
+        busy = false;
+        return true;
+    }
+};
+
+}  // namespace
+
+bool pool_run(int64_t n, const std::function<void(int64_t)> &f) {
+    static Pool *pool = new Pool();  // never destroyed: its threads live as long as the process
+    return pool->run(n, f);
 }
 
 namespace {

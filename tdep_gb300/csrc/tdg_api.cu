@@ -16,6 +16,7 @@
 #include <array>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <numeric>
 #include <string>
@@ -42,6 +43,8 @@ namespace {
 // tdg_release_cached_memory returns the cached blocks to the driver. Allocation and free are
 // ordered on the stream of the context whose call is running on this thread (PoolScope);
 // outside such a call DevBuf falls back to cudaMalloc / cudaFree.
+thread_local std::unique_ptr<int32_t[]> tl_slist;  // shared three-phonon samples (tdg_scattering)
+thread_local size_t tl_slist_cap = 0;
 thread_local cudaStream_t tl_stream = nullptr;
 thread_local cudaMemPool_t tl_pool = nullptr;
 
@@ -844,7 +847,9 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     std::vector<uint32_t> masks;            // distinct row masks (4 words each)
     std::vector<int64_t> rbeg(nr, 0);       // per row: start of its sample in the uploaded list
     std::vector<int32_t> rlen(nr, 0);
-    std::vector<int32_t> slist;             // shared path: one sample per q1
+    // shared path: one sample per q1, in this thread's grow-only host buffer (not zero-filled;
+    // the upload from pageable memory has copied it when the call returns)
+    size_t slist_n = 0;
     std::vector<int4> qdesc;                // shared path: per q1 (list start, length, first candidate, mask)
     bool shared = true;
     int64_t nc64 = 0;
@@ -874,6 +879,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
             }
         });
         for (int q1 = 0; q1 < nirr; ++q1) shared = shared && same[q1];
+        pt.mark("three-phonon sharing test (host)");
         std::vector<std::array<uint32_t, 4>> table;
         auto mask_id = [&](const std::array<uint32_t, 4> &key) {
             for (int t = (int)table.size() - 1; t >= 0 && t >= (int)table.size() - 8; --t)
@@ -904,7 +910,12 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
             }
             if (start[nirr] >= ((int64_t)1 << 31) - 1)
                 return set_error(kErrBadDim, "too many three-phonon candidates for one call");
-            slist.resize(start[nirr]);
+            slist_n = (size_t)start[nirr];
+            if (tl_slist_cap < slist_n) {
+                tl_slist.reset(new int32_t[slist_n]);
+                tl_slist_cap = slist_n;
+            }
+            int32_t *slist = tl_slist.get();
             std::atomic<int> bad{0};
             parallel_for(nirr, [&](int64_t q1) {
                 const int L = (int)(start[q1 + 1] - start[q1]);
@@ -921,6 +932,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
             });
             if (bad.load() == 1) return set_error(kErrParam, "three-phonon sample: q' index out of range");
             nc64 = start[nirr];
+            pt.mark("three-phonon shared samples (host)");
         } else {
             std::atomic<int> bad{0};
             parallel_for(nr, [&](int64_t r) {
@@ -975,7 +987,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
             nc64 = (int64_t)cand.size();
         }
         for (const auto &t : table) masks.insert(masks.end(), t.begin(), t.end());
-        if (nc64 >= ((int64_t)1 << 31) - 1 || (int64_t)slist.size() >= ((int64_t)1 << 31))
+        if (nc64 >= ((int64_t)1 << 31) - 1 || (int64_t)slist_n >= ((int64_t)1 << 31))
             return set_error(kErrBadDim, "too many three-phonon candidates for one call");
     }
     pt.mark("three-phonon candidates (host)");
@@ -1112,7 +1124,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         chk(c->d_rbeg.upload(rbeg.data(), rbeg.size(), s));
         chk(c->d_rlen.upload(rlen.data(), rlen.size(), s));
         if (shared) {
-            chk(c->d_list3.upload(slist.data(), slist.size(), s));
+            chk(c->d_list3.upload(tl_slist.get(), slist_n, s));
             chk(c->d_qdesc.upload(qdesc.data(), qdesc.size(), s));
             chk(c->d_cand.alloc(nc));
             int maxL = 0;
