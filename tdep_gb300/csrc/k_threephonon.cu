@@ -145,15 +145,17 @@ __host__ __device__ inline Layout make_layout(int n, int cs) {
 
 __host__ __device__ constexpr int threads_for(int n) { return ((n * n + 31) / 32) * 32; }
 // Resident CTAs per SM the register budget is sized for; FP64 buffers at n >= 12 already
-// limit residency through shared memory.
-__host__ __device__ constexpr int min_blocks_for(int n, bool dbl) {
-    return n <= 3 ? 16 : (n <= 6 ? 12 : (n <= 9 ? 6 : (dbl ? (n <= 12 ? 2 : 1) : (n <= 15 ? 3 : 2))));
+// limit residency through shared memory. At n = 6 the forward pass runs faster with 16
+// CTAs of 64 threads at 64 registers (a few spills) than with 12; the adjoint, with its
+// larger live state, keeps 12.
+__host__ __device__ constexpr int min_blocks_for(int n, bool dbl, bool adj) {
+    return n <= 3 ? 16 : (n <= 6 ? (adj ? 12 : 16) : (n <= 9 ? 6 : (dbl ? (n <= 12 ? 2 : 1) : (n <= 15 ? 3 : 2))));
 }
 
 // ADJ = false: Gamma and the Xi row terms. ADJ = true: the adjoint pass, which recomputes
 // the same Psi and delta weights and accumulates d L / d mwm for the row cotangents a.lam.
 template <int N, typename R, bool ADJ>
-__global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) == 8)) k_threephonon(ThreePhArgs a) {
+__global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) == 8, ADJ)) k_threephonon(ThreePhArgs a) {
     using C = typename CT<R>::C;
     constexpr int N2 = N * N, N3 = N2 * N;
     constexpr int NA = N / 3;

@@ -695,7 +695,7 @@ int ln_batch_setup(tdg_ctx *c, const MeshDev &mesh, const PhononDev &ph, const R
                    int ntrip, LnBatch &b, int &nbmax) {
     cudaStream_t s = c->stream;
     const int n = c->n, N = c->N;
-    const int kp = ln_kp(n), mp = ((n * n + 127) / 128) * 128;
+    const int kp = ln_kp(n), mp = ln_mp(n);
     const int64_t plane = (int64_t)kp * mp;
     const size_t per_slot = 4 * (size_t)plane * sizeof(__nv_bfloat16) + (size_t)n * n * n * sizeof(float2) +
                             (size_t)c->n_fc3 * sizeof(float2);
@@ -710,7 +710,8 @@ int ln_batch_setup(tdg_ctx *c, const MeshDev &mesh, const PhononDev &ph, const R
     CUDA_TRY(c->d_lnx.alloc(4 * (size_t)plane * nbmax));
     CUDA_TRY(c->d_psi.alloc((size_t)nbmax * n * n * n));
     CUDA_TRY(c->d_lnph.alloc((size_t)nbmax * c->n_fc3));
-    // padding rows (k >= 2n) of the operand planes must read as zero; no kernel writes them
+    // padding of the operand planes (component rows a >= n, positions with an index >= n)
+    // must read as zero; no kernel writes it
     if (c->d_lnx.p != old) CUDA_TRY(cudaMemsetAsync(c->d_lnx.p, 0, sizeof(__nv_bfloat16) * c->d_lnx.n, s));
     const size_t slots = c->d_lnx.n / (4 * (size_t)plane);
     b = LnBatch{};
@@ -723,6 +724,7 @@ int ln_batch_setup(tdg_ctx *c, const MeshDev &mesh, const PhononDev &ph, const R
     b.n = n;
     b.plane = plane;
     b.mp = mp;
+    b.n_sm = c->n_sm;
     b.xa_hi = c->d_lnx.p;
     b.xa_lo = b.xa_hi + plane * slots;
     b.xb_hi = b.xa_lo + plane * slots;

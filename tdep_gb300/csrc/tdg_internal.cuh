@@ -190,7 +190,8 @@ struct LnBatch {
     const uint32_t *cand_mask;
     int n;
     int64_t plane;           // elements of one operand plane per slot: ln_kp(n) * mp
-    int mp;                  // M stride: n^2 rounded up to 128
+    int mp;                  // ln_mp(n): M tiles of 128 rows (8 x by 16 y) times 128
+    int n_sm = 0;            // SMs of the device (persistent GEMM grid)
     __nv_bfloat16 *xa_hi, *xa_lo, *xb_hi, *xb_lo;  // operand planes (hi/lo), zero-initialised
     const __nv_bfloat16 *bmat;                     // launch_ln_bmat
     float2 *phase;           // [nb * fc.n]
@@ -204,6 +205,7 @@ struct LnBatch {
     float *grad_hi = nullptr, *grad_lo = nullptr;
 };
 int ln_kp(int n);
+int ln_mp(int n);
 size_t ln_gemm_smem(int kp);
 // Real-split eigenvector matrices of every mesh point: n_q * 2 * ln_kp(n)^2 BF16 (hi, lo);
 // transposed for the adjoint's back-contraction.
