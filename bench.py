@@ -265,7 +265,9 @@ def run_profile(args):
                 sr.kappa(opts)
             else:
                 sr.kappa_offdiag(opts)
-    log(f"[bench] profile ({args.stage}): {sr.stats}")
+    from tdep_gb300._native import autotune_table
+
+    log(f"[bench] profile ({args.stage}): {sr.stats} launch shapes {autotune_table()} graphs {sr.graph_counts()}")
     sr.close()
 
 
@@ -273,6 +275,7 @@ def run_gb300(args):
     import torch
 
     from tdep_gb300 import ScatteringRates
+    from tdep_gb300._native import autotune_table
 
     cfg, prob, opts, lists = setup(args.config, precision="mixed")
     n = prob.n_mode
@@ -298,6 +301,7 @@ def run_gb300(args):
         trip = st["triplets"]
     torch.cuda.synchronize()
     clk = clocks.stop()
+    graphs = sr.graph_counts()
     lw_mixed = sr.linewidth.copy()
     t0 = time.perf_counter()
     ks32, ki32 = sr.kappa(opts)
@@ -325,6 +329,7 @@ def run_gb300(args):
     if small:
         # ---- FP64 path on the same workload: kappa error bar and speedup ----
         o64 = type(opts)(**{**opts.__dict__, "precision": "fp64"})
+        sr.generate(o64, lists)  # warm-up: the first FP64 call also runs the launch-shape trials
         sr.generate(o64, lists)
         fp64_ms = sr.stats["device_ms"]
         _, ki64 = sr.kappa(o64)
@@ -405,6 +410,10 @@ def run_gb300(args):
                          "sample": desc},
         "clocks": clk,
         "gpu_launches": int(launches),
+        "launch_shapes": {"autotuned": autotune_table(),
+                          "graph_counts_direct_recorded_replayed": graphs,
+                          "note": "warm-up calls run the autotuner trials and record the CUDA graph of the "
+                                  "three-phonon kernels; timed calls replay it"},
         "stage_ms": {k: stats[k] for k in ("enumerate_ms", "threephonon_ms", "symmetrize_ms", "device_ms")},
         "mode_triplets_per_s": value * n**3,
         "kappa_wall_ms": kappa_ms, "kappa_iterations": kappa_iters,

@@ -182,6 +182,37 @@ void tdg_destroy(tdg_ctx *ctx);
 int tdg_release_cached_memory(int device);
 
 /*
+ * CUDA graphs (no reference counterpart): the three-phonon kernels of tdg_scattering (the
+ * fused kernel, or the launches of the large-cell batches) run directly on the first call
+ * with a given configuration, are recorded as a CUDA graph on the
+ * second and replayed on later calls with the same configuration and device buffers (the
+ * data in the buffers may change). TDG_GRAPHS=0 runs it directly every time. counts[0..2]
+ * receive the context's direct runs, recordings and replays of that part.
+ */
+int tdg_graph_counts(tdg_ctx *ctx, int64_t *counts);
+
+/*
+ * Launch-shape autotuner (no reference counterpart). The first scattering call that needs a
+ * launch shape for its mode count, precision and device (the persistent grid of the fused
+ * three-phonon kernel; the delta kernel's row block and the GEMM pipeline depth of the
+ * large-cell path) times each candidate on its own work and keeps the fastest in a
+ * process-wide table; results do not depend on the choice beyond floating-point summation
+ * order. Environment: TDG_AUTOTUNE=0 turns the trials off (defaults, or decisions already
+ * in the table); TDG_TUNE_CACHE=<file> is read before the first decision and rewritten
+ * after each new one.
+ *   tdg_autotune_load   adds the "key value" lines of a file to the table (TDG_ERR_IO if
+ *                       it cannot be read or a line is malformed);
+ *   tdg_autotune_save   writes the table to a file;
+ *   tdg_autotune_report writes the table as text ("key value\n" lines, NUL-terminated,
+ *                       truncated to cap bytes); *needed (if not NULL) gets the full size;
+ *   tdg_autotune_clear  empties the table.
+ */
+int tdg_autotune_load(const char *path);
+int tdg_autotune_save(const char *path);
+int tdg_autotune_report(char *buf, int64_t cap, int64_t *needed);
+int tdg_autotune_clear(void);
+
+/*
  * Rows and Monte-Carlo q' samples, generated on the host exactly as the reference does:
  * MT19937-64 seeded by init_genrand64(iseed=0, rseed=1/seed) (lo_randomnumbers.f90:203-236),
  * one stratified sample per row and order (lo_fftgrid_helper.f90:56-99), consumed row by

@@ -122,6 +122,11 @@ SIGNATURES = {
     "tdg_transfer_bytes": (C.c_int, [C.c_void_p, _i64p, _i64p]),
     "tdg_kappa_offdiag": (C.c_int, [C.c_void_p, C.POINTER(TdgOpts), _f64p]),
     "tdg_release_cached_memory": (C.c_int, [C.c_int]),
+    "tdg_autotune_load": (C.c_int, [C.c_char_p]),
+    "tdg_autotune_save": (C.c_int, [C.c_char_p]),
+    "tdg_autotune_report": (C.c_int, [C.c_char_p, C.c_int64, _i64p]),
+    "tdg_autotune_clear": (C.c_int, []),
+    "tdg_graph_counts": (C.c_int, [C.c_void_p, _i64p]),
     "tdg_triplets": (C.c_int, [C.c_void_p, C.c_int32, _i32p, C.c_int64, _i32p, C.c_int64, _i64p]),
     "tdg_triplets_static": (C.c_int, [C.c_void_p, C.c_int32, _i32p, C.c_int64, _i32p, C.c_int64, _i64p]),
     "tdg_set_fc3": (C.c_int, [C.c_void_p, _f64p]),
@@ -168,3 +173,17 @@ def ptr(a: np.ndarray | None, ctype):
         return None
     assert a.flags["C_CONTIGUOUS"], "array must be C-contiguous"
     return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def autotune_table() -> dict[str, int]:
+    """The launch-shape decisions of the autotuner in this process (key -> value)."""
+    L = lib()
+    need = C.c_int64(0)
+    check(L.tdg_autotune_report(None, 0, C.byref(need)), "tdg_autotune_report")
+    buf = C.create_string_buffer(int(need.value) + 1)
+    check(L.tdg_autotune_report(buf, len(buf), C.byref(need)), "tdg_autotune_report")
+    out = {}
+    for line in buf.value.decode().splitlines():
+        k, v = line.split()
+        out[k] = int(v)
+    return out

@@ -425,12 +425,11 @@ __global__ void __launch_bounds__(kLnGemmThreads, 1) k_ln_gemm(LnGemmArgs g) {
 
 // ---- delta weights and accumulation: one CTA per (slot, b1) ----
 // GB300's FP64 pipe is 1/64 of FP32, and only a fraction of the n^2 mode pairs (b2, b3) has a
-// Gaussian inside its 8-sigma window. In blocks of kLnBB rows b2: (A) every pair is screened
+// Gaussian inside its 8-sigma window. In blocks of BB rows b2 (16 or 32, autotuned): (A) every pair is screened
 // in FP32 (window with a margin far above FP32 rounding, degeneracy skips pre-checked in
 // FP32), the survivors are compacted into a queue with a block scan; (B) full warps evaluate
 // the queue with the reference's FP64 window test, weights and occupations into a dense F;
 // (C) R2[b2] = sum_b3 F and R3[b3] += sum_b2 F.
-constexpr int kLnBB = 32;
 
 struct LnDeltaArgs {
     MeshDev mesh;
@@ -447,15 +446,15 @@ struct LnDeltaArgs {
     float2 *w;
 };
 
-__host__ __device__ inline size_t ln_delta_smem(int n) {
-    return sizeof(double) * ((size_t)14 * n + (size_t)kLnBB * n) + sizeof(uint32_t) * (size_t)kLnBB * n +
+__host__ __device__ inline size_t ln_delta_smem(int n, int bb) {
+    return sizeof(double) * ((size_t)14 * n + (size_t)bb * n) + sizeof(uint32_t) * (size_t)bb * n +
            sizeof(int) * 33 + sizeof(float) * 4 * (size_t)n + 16;
 }
 
 // ADJ: the adjoint's weights. F holds G_b = lam(row) * nred * dF_b/d|Psi_b|^2 of the
 // survivors (F without |Psi|^2), and W_b = G_b conj(Psi_b) replaces Psi_b for every (b2, b3)
 // of the row mode b1, zero where nothing survives or the row is not sampled.
-template <bool ADJ>
+template <bool ADJ, int BB>
 __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
     extern __shared__ __align__(16) unsigned char sm[];
     const int n = a.n;
@@ -477,8 +476,8 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
     const int i2 = m.full_irr[q2], i3 = m.full_irr[q3];
     double *om2 = (double *)sm, *om3 = om2 + n, *be2 = om3 + n, *be3 = be2 + n, *s2 = be3 + n, *s3 = s2 + n;
     double *v2 = s3 + n, *v3 = v2 + 3 * n, *R2 = v3 + 3 * n, *R3 = R2 + n, *F = R3 + n;
-    uint32_t *Q = (uint32_t *)(F + (size_t)kLnBB * n);
-    int *wsum = (int *)(Q + (size_t)kLnBB * n);
+    uint32_t *Q = (uint32_t *)(F + (size_t)BB * n);
+    int *wsum = (int *)(Q + (size_t)BB * n);
     // FP32 copies for the screen (double -> float conversions run on the FP64 pipe, so they
     // are made once per mode here instead of once per pair); NaN marks omega < 1e-9 Ha.
     float *g2 = (float *)(wsum + 33), *g3 = g2 + n, *t2 = g3 + n, *t3 = t2 + n;
@@ -506,6 +505,10 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
     for (int d = 0; d < 3; ++d) v1[d] = P.vel[((size_t)f1 * n + b1) * 3 + d];
     const double w = a.rows.weight3[row];
     const double perm = q2 == q3 ? 1.0 : 2.0;
+    // F = perm * (pi/16) |Psi|^2 w * ((n2 - n3) d0 + (n2 + n3 + 1) d1), constants folded;
+    // the adjoint's G = lambda(row) * k * dF/d|Psi|^2
+    const double pw = perm * kLnPrefactor * w;
+    const double fadj = ADJ ? a.lam[row] * (double)rec.red_cnt * pw : 0.0;
     const int it = P.integrationtype;
     const float fo1 = (float)o1, fs1 = (float)s1, fsig = (float)P.sigma_fixed;
     const float2 *psi = a.psi + ((int64_t)s * n + b1) * n * n;
@@ -525,9 +528,9 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
         return (fabsf(fo1 + f2 - f3) <= win ? 1u : 0u) | (fabsf(fo1 - f2 + f3) <= win ? 2u : 0u) |
                (fabsf(fo1 - f2 - f3) <= win ? 4u : 0u) | (fo1 + f2 + f3 <= win ? 8u : 0u);
     };
-    for (int bb = 0; bb < n; bb += kLnBB) {
-        const int nbb = min(kLnBB, n - bb), cnt = nbb * n;
-        // (A) contiguous chunk per thread (at most 16 entries: kLnBB * 128 / 256)
+    for (int bb = 0; bb < n; bb += BB) {
+        const int nbb = min(BB, n - bb), cnt = nbb * n;
+        // (A) contiguous chunk per thread (at most 16 entries: BB * 128 / 256)
         const int per = (cnt + bd - 1) / bd;
         const int e0 = min(cnt, tid * per), e1 = min(cnt, e0 + per);
         uint64_t lives = 0;
@@ -573,15 +576,14 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
             dirac3(live, o1, o2, o3, win8, h, cg, tab, d0, d1);
             if (!nonzero(d0) && !nonzero(d1)) continue;
             const double n2 = be2[b2], n3 = be3[b3];
+            const double occ = (n2 - n3) * d0 + (n2 + n3 + 1.0) * d1;
             if (ADJ) {
-                F[e] = a.lam[row] * (double)rec.red_cnt * perm * kLnPrefactor * w *
-                       ((n2 - n3) * d0 + (n2 + n3 + 1.0) * d1);
+                F[e] = fadj * occ;
                 continue;
             }
             const float2 ps = psi[b2 * n + b3];
             const double cr = ps.x, ci = ps.y;
-            const double psisq = kLnPrefactor * (cr * cr + ci * ci) * w;
-            F[e] = perm * psisq * (n2 - n3) * d0 + perm * psisq * (n2 + n3 + 1.0) * d1;
+            F[e] = (pw * (cr * cr + ci * ci)) * occ;
         }
         __syncthreads();
         if (ADJ) {
@@ -594,22 +596,32 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
             __syncthreads();
             continue;
         }
-        // (C) row sums of the block and running column sums
-        for (int r = tid; r < nbb; r += bd) {
-            double sum = 0.0;
-            for (int b3 = 0; b3 < n; ++b3) {
-                const double f = F[r * n + b3];
-                if (nonzero(f)) sum += f;
+        // (C) row sums of the block and running column sums, spread over the whole block: a
+        // warp per row with the columns split over its lanes, two threads per column
+        {
+            const int lane = tid & 31, wid = tid >> 5, nw = bd >> 5;
+            for (int r = wid; r < nbb; r += nw) {
+                double sum = 0.0;
+                for (int b3 = lane; b3 < n; b3 += 32) {
+                    const double f = F[r * n + b3];
+                    if (nonzero(f)) sum += f;
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+                if (lane == 0) R2[bb + r] = sum;
             }
-            R2[bb + r] = sum;
-        }
-        for (int b3 = tid; b3 < n; b3 += bd) {
-            double sum = R3[b3];
-            for (int r = 0; r < nbb; ++r) {
-                const double f = F[r * n + b3];
-                if (nonzero(f)) sum += f;
+            const int n2c = ((2 * n + 31) / 32) * 32;
+            for (int t = tid; t < n2c; t += bd) {  // warp-uniform trip count
+                const int b3 = t >> 1, h = t & 1;
+                double sum = 0.0;
+                if (b3 < n)
+                    for (int r = h; r < nbb; r += 2) {
+                        const double f = F[r * n + b3];
+                        if (nonzero(f)) sum += f;
+                    }
+                sum += __shfl_xor_sync(0xffffffffu, sum, 1);
+                if (h == 0 && b3 < n) R3[b3] += sum;
             }
-            R3[b3] = sum;
         }
         __syncthreads();
     }
@@ -737,7 +749,7 @@ cudaError_t ln_contract(const LnBatch &b, const __nv_bfloat16 *bmat, cudaStream_
     g.irr_full = b.mesh.irr_full;
     g.n = n;
     g.kp = kp;
-    g.n_stage = ln_gemm_stages(kp);
+    g.n_stage = b.gemm_stages > 0 ? std::min(b.gemm_stages, ln_gemm_stages(kp)) : ln_gemm_stages(kp);
     g.acc_cols = kp <= 32 ? 32u : (kp <= 64 ? 64u : (kp <= 128 ? 128u : 256u));
     g.psi = b.psi;
     g.status = b.status;
@@ -772,6 +784,27 @@ LnDeltaArgs delta_args(const LnBatch &b) {
     d.w = b.psi;
     return d;
 }
+
+template <bool ADJ>
+cudaError_t launch_ln_delta(const LnBatch &b, cudaStream_t s) {
+    const LnDeltaArgs d = delta_args(b);
+    const int bb = b.delta_bb == 16 ? 16 : 32;
+    const size_t dsm = ln_delta_smem(b.n, bb);
+    const dim3 grid((unsigned)b.n, (unsigned)b.nb);
+    cudaError_t e;
+    if (bb == 16) {
+        if ((e = cudaFuncSetAttribute(k_ln_delta<ADJ, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm)) !=
+            cudaSuccess)
+            return e;
+        k_ln_delta<ADJ, 16><<<grid, 256, dsm, s>>>(d);
+    } else {
+        if ((e = cudaFuncSetAttribute(k_ln_delta<ADJ, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm)) !=
+            cudaSuccess)
+            return e;
+        k_ln_delta<ADJ, 32><<<grid, 256, dsm, s>>>(d);
+    }
+    return cudaGetLastError();
+}
 }  // namespace
 
 cudaError_t launch_ln_adjoint_batch(const LnBatch &b, cudaStream_t s) {
@@ -789,13 +822,7 @@ cudaError_t launch_ln_adjoint_batch(const LnBatch &b, cudaStream_t s) {
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     if ((e = ln_contract(b, b.bmat, s)) != cudaSuccess) return e;  // Psi
-    const LnDeltaArgs d = delta_args(b);
-    const size_t dsm = ln_delta_smem(n);
-    if ((e = cudaFuncSetAttribute(k_ln_delta<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm)) !=
-        cudaSuccess)
-        return e;
-    k_ln_delta<true><<<dim3((unsigned)n, (unsigned)b.nb), 256, dsm, s>>>(d);  // W over Psi
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = launch_ln_delta<true>(b, s)) != cudaSuccess) return e;  // W over Psi
     {
         dim3 grid((unsigned)((pack_threads(n) + 255) / 256), (unsigned)b.nb);
         k_ln_pack<<<grid, 256, 0, s>>>(n, b.psi, b.nb, b.plane, kp / 16, (n + 15) / 16, b.xa_hi, b.xa_lo);
@@ -824,13 +851,7 @@ cudaError_t launch_ln_batch(const LnBatch &b, cudaStream_t s) {
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     if ((e = ln_contract(b, b.bmat, s)) != cudaSuccess) return e;
-    const LnDeltaArgs d = delta_args(b);
-    const size_t dsm = ln_delta_smem(n);
-    if ((e = cudaFuncSetAttribute(k_ln_delta<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm)) !=
-        cudaSuccess)
-        return e;
-    k_ln_delta<false><<<dim3((unsigned)n, (unsigned)b.nb), 256, dsm, s>>>(d);
-    return cudaGetLastError();
+    return launch_ln_delta<false>(b, s);
 }
 
 }  // namespace tdg

@@ -145,11 +145,13 @@ __host__ __device__ inline Layout make_layout(int n, int cs) {
 
 __host__ __device__ constexpr int threads_for(int n) { return ((n * n + 31) / 32) * 32; }
 // Resident CTAs per SM the register budget is sized for; FP64 buffers at n >= 12 already
-// limit residency through shared memory. At n = 6 the forward pass runs faster with 16
-// CTAs of 64 threads at 64 registers (a few spills) than with 12; the adjoint, with its
-// larger live state, keeps 12.
+// limit residency through shared memory. At n = 6 the FP32 forward pass runs faster with 16
+// CTAs of 64 threads at 64 registers (a few spills) than with 12; the FP64 pass and the
+// adjoint, with their larger live state, keep 12.
 __host__ __device__ constexpr int min_blocks_for(int n, bool dbl, bool adj) {
-    return n <= 3 ? 16 : (n <= 6 ? (adj ? 12 : 16) : (n <= 9 ? 6 : (dbl ? (n <= 12 ? 2 : 1) : (n <= 15 ? 3 : 2))));
+    return n <= 3 ? 16
+                  : (n <= 6 ? (adj || dbl ? 12 : 16)
+                            : (n <= 9 ? 6 : (dbl ? (n <= 12 ? 2 : 1) : (n <= 15 ? 3 : 2))));
 }
 
 // ADJ = false: Gamma and the Xi row terms. ADJ = true: the adjoint pass, which recomputes
@@ -612,7 +614,7 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
 // Persistent grid: resident CTAs per SM times the SM count, at most one CTA per item.
 // `extra` bytes of dynamic shared memory follow the kernel's layout (adjoint accumulator).
 template <int N, typename R, bool ADJ>
-int grid_n(int n_sm, int n_trip, size_t extra) {
+int grid_n(int n_sm, int n_trip, size_t extra, int ctas_per_sm = 0) {
     const Layout L = make_layout(N, sizeof(typename CT<R>::C));
     const size_t bytes = L.total + extra;
     if (cudaFuncSetAttribute(k_threephonon<N, R, ADJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
@@ -627,6 +629,7 @@ int grid_n(int n_sm, int n_trip, size_t extra) {
         cudaGetLastError();
         return 0;
     }
+    if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
     const int grid = n_sm * per_sm;
     return grid > n_trip ? (n_trip > 0 ? n_trip : 1) : grid;
 }
@@ -639,8 +642,8 @@ cudaError_t launch_grid(const ThreePhArgs &a, int grid, size_t extra, cudaStream
 }
 
 template <int N, typename R>
-cudaError_t launch_n(const ThreePhArgs &a, int n_sm, cudaStream_t s) {
-    const int grid = grid_n<N, R, false>(n_sm, a.n_trip, 0);
+cudaError_t launch_n(const ThreePhArgs &a, int n_sm, int ctas_per_sm, cudaStream_t s) {
+    const int grid = grid_n<N, R, false>(n_sm, a.n_trip, 0, ctas_per_sm);
     if (grid < 1) return cudaErrorInvalidConfiguration;
     return launch_grid<N, R, false>(a, grid, 0, s);
 }
@@ -680,14 +683,14 @@ __global__ void k_sum_slices(const double *slices, int32_t n_slice, int64_t n, d
 }
 
 template <typename R>
-cudaError_t launch_prec(const ThreePhArgs &a, int n_sm, cudaStream_t s) {
+cudaError_t launch_prec(const ThreePhArgs &a, int n_sm, int ctas_per_sm, cudaStream_t s) {
     switch (a.mesh.n_mode) {
-        case 3: return launch_n<3, R>(a, n_sm, s);
-        case 6: return launch_n<6, R>(a, n_sm, s);
-        case 9: return launch_n<9, R>(a, n_sm, s);
-        case 12: return launch_n<12, R>(a, n_sm, s);
-        case 15: return launch_n<15, R>(a, n_sm, s);
-        case 18: return launch_n<18, R>(a, n_sm, s);
+        case 3: return launch_n<3, R>(a, n_sm, ctas_per_sm, s);
+        case 6: return launch_n<6, R>(a, n_sm, ctas_per_sm, s);
+        case 9: return launch_n<9, R>(a, n_sm, ctas_per_sm, s);
+        case 12: return launch_n<12, R>(a, n_sm, ctas_per_sm, s);
+        case 15: return launch_n<15, R>(a, n_sm, ctas_per_sm, s);
+        case 18: return launch_n<18, R>(a, n_sm, ctas_per_sm, s);
         default: return cudaErrorNotSupported;
     }
 }
@@ -711,10 +714,15 @@ size_t threephonon_smem_bytes(int n, int precision, int) {
     return make_layout(n, precision == 0 ? sizeof(double2) : sizeof(float2)).total;
 }
 
-cudaError_t launch_threephonon(const ThreePhArgs &a, int precision, int n_sm, cudaStream_t s) {
+cudaError_t launch_threephonon(const ThreePhArgs &a, int precision, int n_sm, int ctas_per_sm, cudaStream_t s) {
     if (a.n_trip <= 0) return cudaSuccess;
-    if (precision == 0) return launch_prec<double>(a, n_sm, s);
-    return launch_prec<float>(a, n_sm, s);
+    if (precision == 0) return launch_prec<double>(a, n_sm, ctas_per_sm, s);
+    return launch_prec<float>(a, n_sm, ctas_per_sm, s);
+}
+
+int threephonon_max_per_sm(int n, int precision) {
+    // grid_n with one SM and an unbounded item count gives the CTAs that fit on one SM
+    return precision == 0 ? grid_prec<double, false>(n, 1, 1 << 30, 0) : grid_prec<float, false>(n, 1, 1 << 30, 0);
 }
 
 int threephonon_adjoint_grid(int n, int precision, int n_sm, int n_trip, int n_fc, bool acc_in_smem) {

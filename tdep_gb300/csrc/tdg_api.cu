@@ -13,12 +13,15 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <array>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <memory>
 #include <mutex>
 #include <numeric>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -235,7 +238,18 @@ struct tdg_ctx {
     DevBuf<__nv_bfloat16> d_bmat, d_lnx;
     DevBuf<float2> d_psi, d_lnph;
     bool bmat_ready = false;
+    // The three-phonon kernels of the pipeline (the fused kernel, or the large-cell batches)
+    // as a CUDA graph: recorded on the second call with the same key
+    // (the first runs it directly, which also sets the kernels' attributes), replayed after.
+    struct GraphSlot {
+        std::string key;
+        int seen = 0;
+        bool failed = false;  // capture refused: this key runs directly
+        cudaGraphExec_t exec = nullptr;
+    } graph3;
+    int64_t graph_counts[3] = {0, 0, 0};  // direct runs, recordings, replays
     bool last_ln = false;  // the last tdg_scattering took the large-cell (tensor-core) path
+    int last_ln_tune = 324;  // its launch shape (delta row block * 10 + GEMM stages)
     DevBuf<__nv_bfloat16> d_bmat_t;  // transposed real-split matrices (adjoint)
     DevBuf<float> d_ghi, d_glo;      // double-float gradient accumulator (large-cell adjoint)
     int xi_fmt = -1;  // d_xi_df holds the current Xi as float pairs (1), floats (0), or nothing (-1)
@@ -248,6 +262,7 @@ struct tdg_ctx {
 
     MeshDev mesh() const {
         MeshDev m;
+        std::memset(&m, 0, sizeof m);  // kernel-argument bytes are compared as graph keys
         m.n_full = N;
         m.n_irr = nirr;
         m.n_op = nop;
@@ -381,6 +396,7 @@ void destroy_ctx(tdg_ctx *c) {
     if (s) cudaStreamSynchronize(s);
     for (auto &x : c->ev)
         if (x) cudaEventDestroy(x);
+    if (c->graph3.exec) cudaGraphExecDestroy(c->graph3.exec);
     delete c;
     pt.mark("device buffers");
     if (s) {
@@ -390,6 +406,12 @@ void destroy_ctx(tdg_ctx *c) {
     pt.mark("stream");
 }
 }  // namespace
+
+extern "C" int tdg_graph_counts(tdg_ctx *c, int64_t *counts) {
+    if (!c || !counts) return set_error(kErrParam, "tdg_graph_counts: null argument");
+    for (int i = 0; i < 3; ++i) counts[i] = c->graph_counts[i];
+    return kOk;
+}
 
 extern "C" int tdg_release_cached_memory(int device) {
     cudaMemPool_t pool = device_pool(device);
@@ -714,7 +736,8 @@ int ln_batch_setup(tdg_ctx *c, const MeshDev &mesh, const PhononDev &ph, const R
     // must read as zero; no kernel writes it
     if (c->d_lnx.p != old) CUDA_TRY(cudaMemsetAsync(c->d_lnx.p, 0, sizeof(__nv_bfloat16) * c->d_lnx.n, s));
     const size_t slots = c->d_lnx.n / (4 * (size_t)plane);
-    b = LnBatch{};
+    std::memset(&b, 0, sizeof b);  // kernel-argument bytes are compared as graph keys
+    b.delta_bb = 32;
     b.mesh = mesh;
     b.ph = ph;
     b.rows = rows;
@@ -738,6 +761,72 @@ int ln_batch_setup(tdg_ctx *c, const MeshDev &mesh, const PhononDev &ph, const R
     return kOk;
 }
 }  // namespace
+
+// Launch shape of the large-cell path packed as one tuning value: delta row block * 10 +
+// GEMM pipeline stages.
+constexpr int kLnTuneDefault = 324;
+void ln_apply_tune(LnBatch &b, int v) {
+    b.delta_bb = v / 10 == 16 ? 16 : 32;
+    b.gemm_stages = v % 10;
+}
+
+bool graphs_enabled() {
+    const char *p = std::getenv("TDG_GRAPHS");
+    return !(p && std::strcmp(p, "0") == 0);
+}
+
+// Runs body on stream s directly, or as the context's recorded graph for this key (see
+// tdg_ctx::GraphSlot). A capture the runtime refuses leaves the key on direct runs.
+cudaError_t run_graph_region(tdg_ctx *c, const std::string &key, cudaStream_t s,
+                             const std::function<cudaError_t()> &body) {
+    auto &g = c->graph3;
+    if (g.key != key) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+        g.key = key;
+        g.seen = 0;
+        g.failed = false;
+    }
+    if (g.exec) {
+        ++c->graph_counts[2];
+        return cudaGraphLaunch(g.exec, s);
+    }
+    if (g.seen == 0 || g.failed || !graphs_enabled()) {
+        ++g.seen;
+        ++c->graph_counts[0];
+        return body();
+    }
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        g.failed = true;
+        ++c->graph_counts[0];
+        return body();
+    }
+    const cudaError_t eb = body();
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(s, &graph);
+    cudaGraphExec_t exec = nullptr;
+    if (eb == cudaSuccess && ee == cudaSuccess && graph) e = cudaGraphInstantiate(&exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (eb != cudaSuccess || ee != cudaSuccess || e != cudaSuccess || !exec) {
+        // nothing of a failed capture ran: run the work directly from now on
+        cudaGetLastError();
+        g.failed = true;
+        ++c->graph_counts[0];
+        return body();
+    }
+    g.exec = exec;
+    ++c->graph_counts[1];
+    return cudaGraphLaunch(g.exec, s);
+}
+
+// Autotuning trials ran on the call's own work: Gamma and Xi start again from zero.
+cudaError_t rezero_outputs(tdg_ctx *c, int64_t nr, int64_t ld, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(c->d_xi.p, 0, sizeof(double) * (size_t)nr * ld, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_gamma.p, 0, sizeof(double) * nr, s);
+    return e;
+}
 
 extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *ql, double *linewidth, double *qs_out,
                               double *stats) {
@@ -813,6 +902,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     const double maxavg = *std::max_element(sigavg.begin(), sigavg.end());
     for (double &x : sigsq) x += maxavg * 1e-4;
     PhononDev ph;
+    std::memset(&ph, 0, sizeof ph);
     ph.omega = c->d_omega.p;
     ph.egv = c->d_egv.p;
     ph.egvs = c->d_egvs.p;
@@ -1157,6 +1247,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     ph.sigsq = c->d_sigsq.p;
     ph.sigsq32 = c->d_sigsq32.p;
     RowsDev rows;
+    std::memset(&rows, 0, sizeof rows);
     rows.n_row = nr;
     rows.rowidx = c->d_rowidx.p;
     rows.weight3 = c->d_w3.p;
@@ -1195,6 +1286,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         ++launches;
         CUDA_TRY(cudaEventRecord(ev[2], s));
         ThreePhArgs a;
+        std::memset(&a, 0, sizeof a);
         a.mesh = mesh;
         a.ph = ph;
         a.rows = rows;
@@ -1218,22 +1310,70 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         a.od = c->d_xi.p;
         a.status = c->d_status.p;
         c->last_ln = n > 18 || o->tensor_cores;
+        // the launch shape comes first (autotuner trials run outside any graph), then the
+        // three-phonon part of the pipeline runs directly or as the context's graph
+        // graph key: every value the recorded launches bake in (kernel-argument bytes, with
+        // the device buffers' addresses, and the launch shape)
+        std::function<cudaError_t()> body3;
+        std::ostringstream gk;
+        gk << n << '/' << ntrip << '/' << o->precision << '/' << c->n_sm << '/';
+        LnBatch b;
+        int nbmax = 0, cps = 0;
         if (c->last_ln) {
             // large-cell path: batches of q-triplets through the tcgen05 contraction
-            int nbmax = 0;
-            LnBatch b;
             st = ln_batch_setup(c, mesh, ph, rows, a.fc, ntrip, b, nbmax);
             if (st) return st;
-            for (int t0 = 0; t0 < ntrip; t0 += nbmax) {
-                b.trip = c->d_trip.p + t0;
-                b.nb = std::min(nbmax, ntrip - t0);
-                CUDA_TRY(launch_ln_batch(b, s));
-                launches += 6;
+            // launch shape (delta row block, GEMM pipeline depth), timed on the first slots
+            {
+                const std::string key = tune_key("largecell", n, o->precision, c->device);
+                int v = kLnTuneDefault;
+                bool tuned = false;
+                LnBatch tb = b;
+                tb.trip = c->d_trip.p;
+                tb.nb = std::min(std::min(nbmax, ntrip), 16);
+                CUDA_TRY(tune_pick(key, {324, 164, 323, 163}, kLnTuneDefault,
+                                   [&](int cand) {
+                                       ln_apply_tune(tb, cand);
+                                       return launch_ln_batch(tb, s);
+                                   },
+                                   s, v, tuned));
+                if (tuned) CUDA_TRY(rezero_outputs(c, nr, ld, s));
+                ln_apply_tune(b, v);
+                c->last_ln_tune = v;
             }
+            gk << "ln" << c->last_ln_tune << '/' << nbmax << '/' << (const void *)c->d_trip.p << '/'
+               << std::string(reinterpret_cast<const char *>(&b), sizeof b);
+            body3 = [&]() -> cudaError_t {
+                for (int t0 = 0; t0 < ntrip; t0 += nbmax) {
+                    LnBatch bt = b;
+                    bt.trip = c->d_trip.p + t0;
+                    bt.nb = std::min(nbmax, ntrip - t0);
+                    const cudaError_t e = launch_ln_batch(bt, s);
+                    if (e != cudaSuccess) return e;
+                }
+                return cudaSuccess;
+            };
+            launches += 6 * ((ntrip + nbmax - 1) / std::max(nbmax, 1));
         } else {
-            CUDA_TRY(launch_threephonon(a, o->precision, c->n_sm, s));
+            // persistent grid (CTAs per SM), timed on a prefix of the q-triplets
+            const int maxps = threephonon_max_per_sm(n, o->precision);
+            std::vector<int> cand;
+            for (int v : {maxps, (3 * maxps + 3) / 4, (maxps + 1) / 2})
+                if (v >= 1 && std::find(cand.begin(), cand.end(), v) == cand.end()) cand.push_back(v);
+            const std::string key = tune_key("threephonon", n, o->precision, c->device);
+            bool tuned = false;
+            ThreePhArgs ta = a;
+            ta.n_trip = std::min(ntrip, std::max(ntrip / 8, 64 * c->n_sm * std::max(maxps, 1)));
+            CUDA_TRY(tune_pick(key, cand, 0,
+                               [&](int v) { return launch_threephonon(ta, o->precision, c->n_sm, v, s); }, s, cps,
+                               tuned));
+            if (tuned) CUDA_TRY(rezero_outputs(c, nr, ld, s));
+            gk << "f" << cps << '/' << std::string(reinterpret_cast<const char *>(&a), sizeof a);
+            body3 = [&]() { return launch_threephonon(a, o->precision, c->n_sm, cps, s); };
             ++launches;
         }
+        CUDA_TRY(run_graph_region(c, gk.str(), s, body3));
+        // (events recorded inside a graph cannot be timed against the others: ev[3] stays out)
         CUDA_TRY(cudaEventRecord(ev[3], s));
         CUDA_TRY(launch_sample_bits(N, nr, c->d_rbeg.p, c->d_rlen.p, c->d_list3.p, c->d_sbits.p, s));
         ++launches;
@@ -1776,6 +1916,7 @@ int adjoint_large_cell(tdg_ctx *c, const std::vector<double> &lam, double *mwm_b
     int nbmax = 0, batches = 0;
     int st = ln_batch_setup(c, c->mesh(), c->last_ph, c->last_rows, fc, std::max(ntrip, 1), b, nbmax);
     if (st) return st;
+    ln_apply_tune(b, c->last_ln_tune);
     b.gamma = nullptr;
     b.od = nullptr;
     b.bmat_t = c->d_bmat_t.p;

@@ -5,6 +5,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <functional>
+#include <string>
+#include <vector>
+
 struct tdg_ctx;
 
 namespace tdg {
@@ -147,7 +151,10 @@ struct ThreePhArgs {
     double *mwm_bar;            // FP64 slices, zeroed before the launch
     int32_t acc_in_smem;        // accumulate the CTA's slice in shared memory, store it once
 };
-cudaError_t launch_threephonon(const ThreePhArgs &a, int precision, int n_sm, cudaStream_t s);
+// ctas_per_sm: persistent grid of n_sm * ctas_per_sm CTAs (0 or more than fit: as many as fit).
+cudaError_t launch_threephonon(const ThreePhArgs &a, int precision, int n_sm, int ctas_per_sm, cudaStream_t s);
+// CTAs of the fused kernel that fit on one SM (0 if the configuration is not supported).
+int threephonon_max_per_sm(int n, int precision);
 // Adjoint of the three-phonon Gamma with respect to mwm: recomputes Psi per q-triplet and
 // accumulates 2 Re(phase * Q) into a.mwm_bar (one slice per CTA of the returned grid).
 int threephonon_adjoint_grid(int n, int precision, int n_sm, int n_trip, int n_fc, bool acc_in_smem);
@@ -192,6 +199,8 @@ struct LnBatch {
     int64_t plane;           // elements of one operand plane per slot: ln_kp(n) * mp
     int mp;                  // ln_mp(n): M tiles of 128 rows (8 x by 16 y) times 128
     int n_sm = 0;            // SMs of the device (persistent GEMM grid)
+    int delta_bb = 32;       // rows b2 per block of the delta kernel (16 or 32)
+    int gemm_stages = 0;     // shared-memory pipeline stages of the GEMM (0: the most that fit, at most 4)
     __nv_bfloat16 *xa_hi, *xa_lo, *xb_hi, *xb_lo;  // operand planes (hi/lo), zero-initialised
     const __nv_bfloat16 *bmat;                     // launch_ln_bmat
     float2 *phase;           // [nb * fc.n]
@@ -319,5 +328,17 @@ struct CtxView {
     int64_t *xfer;  // the context's transfer counter
 };
 CtxView ctx_view(tdg_ctx *c);
+
+
+// ---- launch-shape autotuner (autotune.cu) ----
+// Key of a decision: kernel name, mode count, precision, SM count and device name.
+std::string tune_key(const char *kernel, int n, int precision, int device);
+// The table's decision for key, or dflt.
+int tune_lookup(const std::string &key, int dflt);
+// The decision for key: from the table, or (trials enabled, two or more candidates) the
+// candidate whose trial(c) ran fastest on stream s, which is then recorded; otherwise dflt.
+// tuned is true when trials ran (their outputs are the caller's to discard).
+cudaError_t tune_pick(const std::string &key, const std::vector<int> &cand, int dflt,
+                      const std::function<cudaError_t(int)> &trial, cudaStream_t s, int &choice, bool &tuned);
 
 }  // namespace tdg

@@ -333,6 +333,13 @@ class ScatteringRates:
         N.check(self._lib.tdg_kappa_offdiag(self._ctx, C.byref(o), N.ptr(k, C.c_double)), "tdg_kappa_offdiag")
         return k.reshape(3, 3, order="F")
 
+    def graph_counts(self) -> list[int]:
+        """Direct runs, CUDA-graph recordings and replays of the three-phonon kernels on this
+        context (tdg_graph_counts)."""
+        c = np.zeros(3, dtype=np.int64)
+        N.check(self._lib.tdg_graph_counts(self._ctx, N.ptr(c, C.c_int64)), "tdg_graph_counts")
+        return [int(x) for x in c]
+
     def transfer_bytes(self) -> tuple[int, int]:
         """(host-to-device, device-to-host) bytes copied by this object's calls so far."""
         h, d = C.c_int64(0), C.c_int64(0)

@@ -109,3 +109,30 @@ def test_outfile_layout_matches_reference(built, tmp_path):
             np.testing.assert_allclose([float(x) for x in a.split()], [float(x) for x in b.split()], rtol=1e-10,
                                        atol=1e-14)
             assert len(a) == len(b)
+
+
+def test_autotune_table_round_trip(built, tmp_path):
+    """The autotuner's decision table loads, reports and saves its text format (no GPU)."""
+    L = N.lib()
+    N.check(L.tdg_autotune_clear(), "clear")
+    f = tmp_path / "tune.txt"
+    f.write_text("# comment\nthreephonon/n6/p1/sm152/NVIDIA_GB300 12\n\nlargecell/n120/p1/sm152/NVIDIA_GB300 164\n")
+    N.check(L.tdg_autotune_load(str(f).encode()), "load")
+    t = N.autotune_table()
+    assert t == {"threephonon/n6/p1/sm152/NVIDIA_GB300": 12, "largecell/n120/p1/sm152/NVIDIA_GB300": 164}
+    g = tmp_path / "saved.txt"
+    N.check(L.tdg_autotune_save(str(g).encode()), "save")
+    N.check(L.tdg_autotune_clear(), "clear")
+    assert N.autotune_table() == {}
+    N.check(L.tdg_autotune_load(str(g).encode()), "reload")
+    assert N.autotune_table() == t
+    # truncated report stays NUL-terminated and reports the full size
+    need = C.c_int64(0)
+    buf = C.create_string_buffer(8)
+    N.check(L.tdg_autotune_report(buf, 8, C.byref(need)), "report")
+    assert len(buf.value) == 7 and need.value > 8
+    bad = tmp_path / "bad.txt"
+    bad.write_text("key notanumber\n")
+    assert L.tdg_autotune_load(str(bad).encode()) == 6
+    assert L.tdg_autotune_load(str(tmp_path / "missing.txt").encode()) == 6
+    N.check(L.tdg_autotune_clear(), "clear")
