@@ -1,6 +1,8 @@
 // Isotope scattering, the two scattering-matrix symmetrisations and the BTE product.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "dev_common.cuh"
 #include "tdg_internal.cuh"
 
@@ -402,8 +404,9 @@ __global__ void k_split_xi(const double *xi, int64_t n, void *out) {
 // consecutive columns per thread (16 bytes) measured slower than these 4-byte coalesced loads.
 template <bool DF>
 __global__ void __launch_bounds__(256) k_xi_gemv(const void *__restrict__ xi_, int32_t n_row, int64_t n_col,
-                                                 const void *__restrict__ fbb_, double *part) {
+                                                 const void *__restrict__ fbb_, double *part, const int32_t *skip) {
     __shared__ float2 sh[kGemvRows * 3][8];
+    if (skip && *skip) return;
     const int r0 = blockIdx.x * kGemvRows;
     const int nr = min(kGemvRows, n_row - r0);
     const int64_t per = (n_col + gridDim.y - 1) / gridDim.y;
@@ -505,7 +508,8 @@ __global__ void __launch_bounds__(256) k_xi_gemv(const void *__restrict__ xi_, i
     }
 }
 
-__global__ void k_xi_reduce(const double *part, int32_t n_row, int split, double *buf) {
+__global__ void k_xi_reduce(const double *part, int32_t n_row, int split, double *buf, const int32_t *skip) {
+    if (skip && *skip) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_row * 3) return;
     const int r = i / 3, d = i % 3;
@@ -606,7 +610,8 @@ cudaError_t launch_sym_tile(const MeshDev &m, const OrbitDev &o, int32_t n_row, 
 // Fbb(q, b) = sign(op) * R_|op| Fn(irr(q), b), one thread per (q, b).
 template <bool DF>
 __global__ void k_foldout(int32_t n_full, int32_t n_mode, const int32_t *full_op, const int32_t *full_irr,
-                          const double *op_cart, const double *fn, void *fbb) {
+                          const double *op_cart, const double *fn, void *fbb, const int32_t *skip) {
+    if (skip && *skip) return;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (int64_t)n_full * n_mode) return;
     const int iq = (int)(i / n_mode), b = (int)(i % n_mode);
@@ -624,13 +629,16 @@ __global__ void k_foldout(int32_t n_full, int32_t n_mode, const int32_t *full_op
 }
 
 cudaError_t launch_foldout(int32_t n_full, int32_t n_mode, const int32_t *full_op, const int32_t *full_irr,
-                           const double *op_cart, const double *fn, bool df, void *fbb, cudaStream_t s) {
+                           const double *op_cart, const double *fn, bool df, void *fbb, cudaStream_t s,
+                           const int32_t *skip) {
     const int64_t n = (int64_t)n_full * n_mode;
     if (n <= 0) return cudaSuccess;
     if (df)
-        k_foldout<true><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n_full, n_mode, full_op, full_irr, op_cart, fn, fbb);
+        k_foldout<true><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n_full, n_mode, full_op, full_irr, op_cart, fn, fbb,
+                                                                     skip);
     else
-        k_foldout<false><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n_full, n_mode, full_op, full_irr, op_cart, fn, fbb);
+        k_foldout<false><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n_full, n_mode, full_op, full_irr, op_cart, fn,
+                                                                      fbb, skip);
     return cudaGetLastError();
 }
 
@@ -647,16 +655,140 @@ cudaError_t launch_split_xi(const double *xi, int64_t n, bool df, void *out, cud
     return cudaGetLastError();
 }
 
+int xi_gemv_default_split(int32_t n_row, int64_t n_col, int n_sm) { return gemv_split(n_row, n_col, n_sm); }
+
+int xi_gemv_max_split(int64_t n_col) {
+    const int64_t k = n_col / 256;
+    return (int)(k < 1 ? 1 : (k > kGemvMaxSplit ? kGemvMaxSplit : k));
+}
+
 cudaError_t launch_xi_gemv(const void *xi, int32_t n_row, int64_t n_col, bool df, const void *fbb, double *part,
-                           double *buf, int n_sm, cudaStream_t s) {
+                           double *buf, int n_sm, cudaStream_t s, const int32_t *skip, int split) {
     if (n_row <= 0) return cudaSuccess;
-    const int split = gemv_split(n_row, n_col, n_sm);
+    if (split <= 0) split = gemv_split(n_row, n_col, n_sm);
+    split = std::min(split, xi_gemv_max_split(n_col));
     dim3 grid((unsigned)((n_row + kGemvRows - 1) / kGemvRows), (unsigned)split);
     if (df)
-        k_xi_gemv<true><<<grid, 256, 0, s>>>(xi, n_row, n_col, fbb, part);
+        k_xi_gemv<true><<<grid, 256, 0, s>>>(xi, n_row, n_col, fbb, part, skip);
     else
-        k_xi_gemv<false><<<grid, 256, 0, s>>>(xi, n_row, n_col, fbb, part);
-    k_xi_reduce<<<(n_row * 3 + 255) / 256, 256, 0, s>>>(part, n_row, split, buf);
+        k_xi_gemv<false><<<grid, 256, 0, s>>>(xi, n_row, n_col, fbb, part, skip);
+    k_xi_reduce<<<(n_row * 3 + 255) / 256, 256, 0, s>>>(part, n_row, split, buf, skip);
+    return cudaGetLastError();
+}
+
+namespace {
+// One BTE iteration's scalar part (kappa.f90:407-490) after the products buf = Xi . Fbb, in
+// three kernels spread over the SMs (GB300's FP64 rate on a single SM, 2 operations per
+// clock, made a one-CTA version take 80 us for the divisions alone):
+//   k_bte_apply  applyXi: Fnb = -buf / qs for every (q1, b1) with a row, else 0;
+//   k_bte_mix    per q1 (8 per CTA): distributeF (degeneracy average in the reference's in-place order,
+//                then + F0) and addandcheck (relative change, mixing into Fn), partial sums
+//                of the change per CTA;
+//   k_bte_check  the change summed in a fixed order into scf, the convergence test on the
+//                last three values, the mixing schedule, the done flag.
+// Every kernel of an iteration returns at once when done is set.
+// q1 per CTA of k_bte_mix (one warp, the other lanes idle): few per CTA spreads the FP64
+// divisions over many SMs.
+constexpr int kBteMixQ = 8;
+
+__global__ void k_bte_apply(BteDev d, const double *buf) {
+    if (d.ctl->done) return;
+    const int n = d.n_mode;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n_irr * n) return;
+    const int r = d.rowidx[i];
+    const double q = d.qs[i];
+    for (int x = 0; x < 3; ++x)
+        d.fnb[(size_t)i * 3 + x] = (r < 0 || q < kFreqTolD) ? 0.0 : -buf[(size_t)r * 3 + x] / q;
+}
+
+__global__ void k_bte_mix(BteDev d) {
+    __shared__ double red[32];
+    extern __shared__ double sm_mix[];  // Fnb, F0 and Fn of the CTA's kBteMixQ points
+    if (d.ctl->done) return;
+    const int n = d.n_mode, tid = threadIdx.x, bd = blockDim.x;
+    const int q0 = blockIdx.x * kBteMixQ, nq = min(kBteMixQ, d.n_irr - q0);
+    const int m = nq * n * 3;
+    double *fbs = sm_mix, *f0s = sm_mix + kBteMixQ * n * 3, *fns = f0s + kBteMixQ * n * 3;
+    const size_t base = (size_t)q0 * n * 3;
+    for (int i = tid; i < m; i += bd) {
+        fbs[i] = d.fnb[base + i];
+        f0s[i] = d.F0[base + i];
+        fns[i] = d.fn[base + i];
+    }
+    __syncthreads();
+    const double mixing = d.ctl->mixing;
+    double g0 = 0.0;
+    if (tid < nq) {
+        const int q1 = q0 + tid;
+        double *fb = fbs + tid * n * 3;
+        const double *f0 = f0s + tid * n * 3;
+        for (int b1 = 0; b1 < n; ++b1) {
+            const int dg = d.degen[q1 * n + b1];
+            const int32_t *dm = d.degen_mode + ((size_t)q1 * n + b1) * n;
+            double v0[3] = {0.0, 0.0, 0.0};
+            for (int j = 0; j < dg; ++j)
+                for (int x = 0; x < 3; ++x) v0[x] += fb[(dm[j] - 1) * 3 + x];
+            if (dg != 1)
+                for (int x = 0; x < 3; ++x) v0[x] /= (double)dg;
+            for (int j = 0; j < dg; ++j)
+                for (int x = 0; x < 3; ++x) fb[(dm[j] - 1) * 3 + x] = v0[x];
+            for (int x = 0; x < 3; ++x) fb[b1 * 3 + x] = f0[b1 * 3 + x] + fb[b1 * 3 + x];
+        }
+        double *fn = fns + tid * n * 3;
+        for (int b1 = 0; b1 < n; ++b1) {
+            double *v = fn + b1 * 3;
+            const double *f = fb + b1 * 3;
+            double g1 = 0.0, g2 = 0.0;
+            for (int x = 0; x < 3; ++x) {
+                g1 += (v[x] - f[x]) * (v[x] - f[x]);
+                g2 += v[x] * v[x];
+            }
+            if (g2 > d.sqtol) g0 += g1 / g2;
+            for (int x = 0; x < 3; ++x) v[x] = v[x] * (1.0 - mixing) + mixing * f[x];
+        }
+    }
+    __syncthreads();
+    for (int i = tid; i < m; i += bd) d.fn[base + i] = fns[i];
+    for (int o = 16; o > 0; o >>= 1) g0 += __shfl_xor_sync(0xffffffffu, g0, o);
+    if ((tid & 31) == 0) red[tid >> 5] = g0;
+    __syncthreads();
+    if (tid == 0) {
+        double g = 0.0;
+        for (int w = 0; w < (bd >> 5); ++w) g += red[w];
+        d.part[blockIdx.x] = g;
+    }
+}
+
+__global__ void k_bte_check(BteDev d, int n_part) {
+    BteCtl *c = d.ctl;
+    if (c->done) return;
+    double g = 0.0;
+    for (int i = threadIdx.x; i < n_part; i += 32) g += d.part[i];
+    for (int o = 16; o > 0; o >>= 1) g += __shfl_xor_sync(0xffffffffu, g, o);
+    if (threadIdx.x != 0) return;
+    const int iter = c->iter + 1;
+    const double mixing = c->mixing;
+    d.scf[iter - 1] = g / d.n_irr / d.n_mode;
+    bool stop = false;
+    if (iter >= 3) stop = d.scf[iter - 3] + d.scf[iter - 2] + d.scf[iter - 1] < d.tol;
+    if (!stop && iter > 15 && mixing > 0.50) c->mixing = mixing * 0.98;
+    c->iter = iter;
+    if (stop || iter >= d.maxiter) c->done = 1;
+}
+}  // namespace
+
+int bte_part_elems(int32_t n_irr) { return (n_irr + kBteMixQ - 1) / kBteMixQ; }
+
+cudaError_t launch_bte_update(const BteDev &d, const double *buf, cudaStream_t s) {
+    const int ne = d.n_irr * d.n_mode;
+    k_bte_apply<<<(ne + 127) / 128, 128, 0, s>>>(d, buf);
+    const int nb = bte_part_elems(d.n_irr);
+    const size_t mix_smem = sizeof(double) * 3 * kBteMixQ * 3 * (size_t)d.n_mode;
+    cudaError_t e = cudaFuncSetAttribute(k_bte_mix, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mix_smem);
+    if (e != cudaSuccess) return e;
+    k_bte_mix<<<nb, 64, mix_smem, s>>>(d);
+    k_bte_check<<<1, 32, 0, s>>>(d, nb);
     return cudaGetLastError();
 }
 

@@ -173,7 +173,6 @@ struct tdg_ctx {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[10] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     int32_t h_tot[2] = {0, 0};  // enumeration totals (a pinned allocation costs more than it saves)
-    std::vector<double> h_kbuf;  // Xi.Fbb of a BTE iteration
     DevBuf<int32_t> d_full_op;
     DevBuf<double> d_op_cart, d_fn;
     // host copy of the problem
@@ -246,8 +245,14 @@ struct tdg_ctx {
         int seen = 0;
         bool failed = false;  // capture refused: this key runs directly
         cudaGraphExec_t exec = nullptr;
+        int64_t counts[3] = {0, 0, 0};  // direct runs, recordings, replays
     } graph3;
-    int64_t graph_counts[3] = {0, 0, 0};  // direct runs, recordings, replays
+    GraphSlot graph_bte;                  // a chunk of BTE iterations (tdg_kappa)
+    int kappa_calls = 0;
+    // BTE iteration state on the device
+    DevBuf<double> d_fnb, d_scf, d_qs_bte, d_F0, d_bte_part;
+    DevBuf<int32_t> d_deg_irr, d_dm_irr;
+    DevBuf<BteCtl> d_ctl;
     bool last_ln = false;  // the last tdg_scattering took the large-cell (tensor-core) path
     int last_ln_tune = 324;  // its launch shape (delta row block * 10 + GEMM stages)
     DevBuf<__nv_bfloat16> d_bmat_t;  // transposed real-split matrices (adjoint)
@@ -397,6 +402,7 @@ void destroy_ctx(tdg_ctx *c) {
     for (auto &x : c->ev)
         if (x) cudaEventDestroy(x);
     if (c->graph3.exec) cudaGraphExecDestroy(c->graph3.exec);
+    if (c->graph_bte.exec) cudaGraphExecDestroy(c->graph_bte.exec);
     delete c;
     pt.mark("device buffers");
     if (s) {
@@ -409,7 +415,7 @@ void destroy_ctx(tdg_ctx *c) {
 
 extern "C" int tdg_graph_counts(tdg_ctx *c, int64_t *counts) {
     if (!c || !counts) return set_error(kErrParam, "tdg_graph_counts: null argument");
-    for (int i = 0; i < 3; ++i) counts[i] = c->graph_counts[i];
+    for (int i = 0; i < 3; ++i) counts[i] = c->graph3.counts[i];
     return kOk;
 }
 
@@ -777,9 +783,8 @@ bool graphs_enabled() {
 
 // Runs body on stream s directly, or as the context's recorded graph for this key (see
 // tdg_ctx::GraphSlot). A capture the runtime refuses leaves the key on direct runs.
-cudaError_t run_graph_region(tdg_ctx *c, const std::string &key, cudaStream_t s,
-                             const std::function<cudaError_t()> &body) {
-    auto &g = c->graph3;
+cudaError_t run_graph_region(tdg_ctx *c, tdg_ctx::GraphSlot &g, const std::string &key, cudaStream_t s,
+                             const std::function<cudaError_t()> &body, bool may_record = true) {
     if (g.key != key) {
         if (g.exec) cudaGraphExecDestroy(g.exec);
         g.exec = nullptr;
@@ -788,19 +793,19 @@ cudaError_t run_graph_region(tdg_ctx *c, const std::string &key, cudaStream_t s,
         g.failed = false;
     }
     if (g.exec) {
-        ++c->graph_counts[2];
+        ++g.counts[2];
         return cudaGraphLaunch(g.exec, s);
     }
-    if (g.seen == 0 || g.failed || !graphs_enabled()) {
+    if (g.seen == 0 || g.failed || !may_record || !graphs_enabled()) {
         ++g.seen;
-        ++c->graph_counts[0];
+        ++g.counts[0];
         return body();
     }
     cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) {
         cudaGetLastError();
         g.failed = true;
-        ++c->graph_counts[0];
+        ++g.counts[0];
         return body();
     }
     const cudaError_t eb = body();
@@ -813,13 +818,17 @@ cudaError_t run_graph_region(tdg_ctx *c, const std::string &key, cudaStream_t s,
         // nothing of a failed capture ran: run the work directly from now on
         cudaGetLastError();
         g.failed = true;
-        ++c->graph_counts[0];
+        ++g.counts[0];
         return body();
     }
     g.exec = exec;
-    ++c->graph_counts[1];
+    ++g.counts[1];
     return cudaGraphLaunch(g.exec, s);
 }
+
+// BTE iterations enqueued between two host checks of the convergence flag; iterations after
+// convergence in a chunk return at once.
+constexpr int kBteChunk = 8;
 
 // Autotuning trials ran on the call's own work: Gamma and Xi start again from zero.
 cudaError_t rezero_outputs(tdg_ctx *c, int64_t nr, int64_t ld, cudaStream_t s) {
@@ -1372,7 +1381,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
             body3 = [&]() { return launch_threephonon(a, o->precision, c->n_sm, cps, s); };
             ++launches;
         }
-        CUDA_TRY(run_graph_region(c, gk.str(), s, body3));
+        CUDA_TRY(run_graph_region(c, c->graph3, gk.str(), s, body3));
         // (events recorded inside a graph cannot be timed against the others: ev[3] stays out)
         CUDA_TRY(cudaEventRecord(ev[3], s));
         CUDA_TRY(launch_sample_bits(N, nr, c->d_rbeg.p, c->d_rlen.p, c->d_list3.p, c->d_sbits.p, s));
@@ -1701,6 +1710,7 @@ extern "C" int tdg_kappa(tdg_ctx *c, const tdg_opts *o, int32_t maxiter, double 
         if (n_iter) *n_iter = 0;
         return kOk;
     }
+    ++c->kappa_calls;
     // Every call starts from Fn = F0, the state sr%generate leaves (scattering.f90:288-289).
     std::vector<double> Fn = c->F0;
     get_kappa(c, Fn, T, classical, kappa_sma);
@@ -1723,70 +1733,103 @@ extern "C" int tdg_kappa(tdg_ctx *c, const tdg_opts *o, int32_t maxiter, double 
             CUDA_TRY(c->d_full_op.upload(c->full_op.data(), N, s));
             CUDA_TRY(c->d_op_cart.upload(c->op_cart.data(), c->op_cart.size(), s));
         }
-        c->h_kbuf.resize(nbuf);
-        const double *buf = c->h_kbuf.data();
-        std::vector<double> Fnb((size_t)nirr * n * 3);
-        std::vector<double> scf(maxiter, 0.0);
-        double mixing = 0.95;
-        PhaseTimer pt("tdg_kappa");
-        for (int iter = 1; iter <= maxiter; ++iter) {
-            iters = iter;
-            pt.mark("host");
-            // foldout (kappa.f90:382-404) and the three Xi products (:411-413) on the device;
-            // only Fn (n_irr*n*3) goes up and Xi.Fbb (n_row*3) comes back
-            CUDA_TRY(copy_async(c->d_fn.p, Fn.data(), sizeof(double) * nfn, cudaMemcpyHostToDevice, s));
-            pt.mark("upload");
-            CUDA_TRY(launch_foldout(N, n, c->d_full_op.p, c->d_full_irr.p, c->d_op_cart.p, c->d_fn.p, df, c->d_fbb.p, s));
-            CUDA_TRY(launch_xi_gemv(c->d_xi_df.p, nr, ncol, df, c->d_fbb.p, c->d_part.p, c->d_buf.p, c->n_sm, s));
-            CUDA_TRY(copy_async(c->h_kbuf.data(), c->d_buf.p, sizeof(double) * nbuf, cudaMemcpyDeviceToHost, s));
-            CUDA_TRY(cudaStreamSynchronize(s));
-            pt.mark("foldout, Xi.F and download (device)");
-            // applyXi (kappa.f90:407-426)
-            std::fill(Fnb.begin(), Fnb.end(), 0.0);
-            for (int r = 0; r < nr; ++r) {
-                const int q1 = c->row_q1[r] - 1, b1 = c->row_b1[r] - 1;
-                const double q = c->qs[(size_t)q1 * n + b1];
-                for (int d = 0; d < 3; ++d)
-                    Fnb[((size_t)q1 * n + b1) * 3 + d] = q < kFreqTol ? 0.0 : -buf[(size_t)r * 3 + d] / q;
-            }
-            // distributeF (kappa.f90:429-448), in place as in the reference
+        // The whole iteration runs on the device (kappa.f90:382-490): foldout, the three Xi
+        // products and the scalar recurrences (k_bte_update), in chunks of kBteChunk
+        // iterations between host checks of the done flag; a chunk is replayed as a CUDA
+        // graph from its second use. Fn goes up once and comes back once.
+        if (c->d_deg_irr.n == 0) {
+            std::vector<int32_t> dg((size_t)nirr * n), dm((size_t)nirr * n * n);
             for (int q1 = 0; q1 < nirr; ++q1) {
                 const int f = c->irr_full[q1] - 1;
                 for (int b1 = 0; b1 < n; ++b1) {
-                    const int dg = c->degen[(size_t)f * n + b1];
-                    const int32_t *dm = &c->degen_mode[((size_t)f * n + b1) * n];
-                    double v0[3] = {0, 0, 0};
-                    for (int j = 0; j < dg; ++j)
-                        for (int d = 0; d < 3; ++d) v0[d] += Fnb[((size_t)q1 * n + dm[j] - 1) * 3 + d];
-                    for (int d = 0; d < 3; ++d) v0[d] /= (double)dg;
-                    for (int j = 0; j < dg; ++j)
-                        for (int d = 0; d < 3; ++d) Fnb[((size_t)q1 * n + dm[j] - 1) * 3 + d] = v0[d];
-                    for (int d = 0; d < 3; ++d)
-                        Fnb[((size_t)q1 * n + b1) * 3 + d] =
-                            c->F0[((size_t)q1 * n + b1) * 3 + d] + Fnb[((size_t)q1 * n + b1) * 3 + d];
+                    dg[(size_t)q1 * n + b1] = c->degen[(size_t)f * n + b1];
+                    for (int j = 0; j < n; ++j)
+                        dm[((size_t)q1 * n + b1) * n + j] = c->degen_mode[((size_t)f * n + b1) * n + j];
                 }
             }
-            // addandcheck (kappa.f90:451-490)
-            double g0 = 0.0;
-            for (int q = 0; q < nirr; ++q)
-                for (int j = 0; j < n; ++j) {
-                    double *fn = &Fn[((size_t)q * n + j) * 3];
-                    const double *fb = &Fnb[((size_t)q * n + j) * 3];
-                    double g1 = 0.0, g2 = 0.0;
-                    for (int d = 0; d < 3; ++d) {
-                        g1 += (fn[d] - fb[d]) * (fn[d] - fb[d]);
-                        g2 += fn[d] * fn[d];
-                    }
-                    if (g2 > kSqTol) g0 += g1 / g2;
-                    for (int d = 0; d < 3; ++d) fn[d] = fn[d] * (1.0 - mixing) + mixing * fb[d];
-                }
-            scf[iter - 1] = g0 / nirr / n;
-            if (iter >= 3) {
-                const double g = scf[iter - 3] + scf[iter - 2] + scf[iter - 1];
-                if (g < tol) break;
-            }
-            if (iter > 15 && mixing > 0.50) mixing *= 0.98;
+            CUDA_TRY(c->d_deg_irr.upload(dg.data(), dg.size(), s));
+            CUDA_TRY(c->d_dm_irr.upload(dm.data(), dm.size(), s));
         }
+        CUDA_TRY(c->d_fnb.alloc(nfn));
+        CUDA_TRY(c->d_scf.alloc((size_t)maxiter));
+        CUDA_TRY(c->d_ctl.alloc(1));
+        CUDA_TRY(c->d_bte_part.alloc((size_t)bte_part_elems(nirr)));
+        CUDA_TRY(c->d_qs_bte.upload(c->qs.data(), c->qs.size(), s));
+        CUDA_TRY(c->d_F0.upload(c->F0.data(), nfn, s));
+        CUDA_TRY(copy_async(c->d_fn.p, Fn.data(), sizeof(double) * nfn, cudaMemcpyHostToDevice, s));
+        const BteCtl ctl0{0, 0, 0.95};
+        CUDA_TRY(copy_async(c->d_ctl.p, &ctl0, sizeof(BteCtl), cudaMemcpyHostToDevice, s));
+        BteDev bd;
+        std::memset(&bd, 0, sizeof bd);
+        bd.n_irr = nirr;
+        bd.n_mode = n;
+        bd.n_row = nr;
+        bd.maxiter = maxiter;
+        bd.tol = tol;
+        bd.sqtol = kSqTol;
+        bd.rowidx = c->d_rowidx.p;
+        bd.part = c->d_bte_part.p;
+        bd.qs = c->d_qs_bte.p;
+        bd.F0 = c->d_F0.p;
+        bd.degen = c->d_deg_irr.p;
+        bd.degen_mode = c->d_dm_irr.p;
+        bd.fn = c->d_fn.p;
+        bd.fnb = c->d_fnb.p;
+        bd.scf = c->d_scf.p;
+        bd.ctl = c->d_ctl.p;
+        const int32_t *done = &c->d_ctl.p->done;
+        // column split of the Xi products, autotuned per problem size on F0's foldout
+        int split = 0;
+        {
+            CUDA_TRY(launch_foldout(N, n, c->d_full_op.p, c->d_full_irr.p, c->d_op_cart.p, c->d_fn.p, df, c->d_fbb.p,
+                                    s));
+            const int s0 = xi_gemv_default_split(nr, ncol, c->n_sm), smax = xi_gemv_max_split(ncol);
+            std::vector<int> cand;
+            for (int v : {s0, 2 * s0, 4 * s0, 8 * s0})
+                if (v <= smax && std::find(cand.begin(), cand.end(), v) == cand.end()) cand.push_back(v);
+            std::ostringstream key;
+            key << "xigemv/r" << nr << "/c" << ncol;
+            bool tuned = false;
+            CUDA_TRY(tune_pick(tune_key(key.str().c_str(), n, df ? 0 : 1, c->device), cand, s0,
+                               [&](int v) {
+                                   return launch_xi_gemv(c->d_xi_df.p, nr, ncol, df, c->d_fbb.p, c->d_part.p,
+                                                         c->d_buf.p, c->n_sm, s, nullptr, v);
+                               },
+                               s, split, tuned));
+        }
+        auto iterations = [&](int k) -> cudaError_t {
+            for (int j = 0; j < k; ++j) {
+                cudaError_t e = launch_foldout(N, n, c->d_full_op.p, c->d_full_irr.p, c->d_op_cart.p, c->d_fn.p, df,
+                                               c->d_fbb.p, s, done);
+                if (e == cudaSuccess)
+                    e = launch_xi_gemv(c->d_xi_df.p, nr, ncol, df, c->d_fbb.p, c->d_part.p, c->d_buf.p, c->n_sm, s,
+                                       done, split);
+                if (e == cudaSuccess) e = launch_bte_update(bd, c->d_buf.p, s);
+                if (e != cudaSuccess) return e;
+            }
+            return cudaSuccess;
+        };
+        BteCtl ctl = ctl0;
+        PhaseTimer pt("tdg_kappa");
+        for (int it0 = 0; it0 < maxiter; it0 += kBteChunk) {
+            const int k = std::min(kBteChunk, maxiter - it0);
+            std::ostringstream key;
+            key << k << '/' << df << '/' << split << '/' << std::string(reinterpret_cast<const char *>(&bd), sizeof bd)
+                << '/'
+                << (const void *)c->d_xi_df.p << (const void *)c->d_fbb.p << (const void *)c->d_part.p
+                << (const void *)c->d_buf.p << (const void *)c->d_fn.p << ncol;
+            // recorded only from the context's second kappa call on: a context that solves
+            // once would pay for the recording without replaying it much
+            CUDA_TRY(run_graph_region(c, c->graph_bte, key.str(), s, [&]() { return iterations(k); },
+                                      c->kappa_calls > 1));
+            CUDA_TRY(copy_async(&ctl, c->d_ctl.p, sizeof(BteCtl), cudaMemcpyDeviceToHost, s));
+            CUDA_TRY(cudaStreamSynchronize(s));
+            pt.mark("iterations (device)");
+            if (ctl.done) break;
+        }
+        iters = ctl.iter;
+        CUDA_TRY(copy_async(Fn.data(), c->d_fn.p, sizeof(double) * nfn, cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(cudaStreamSynchronize(s));
     }
     get_kappa(c, Fn, T, classical, kappa_iter);
     symmetrize_kappa(c, kappa_iter);

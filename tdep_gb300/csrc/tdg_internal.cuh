@@ -280,8 +280,11 @@ cudaError_t launch_sym_tile(const MeshDev &m, const OrbitDev &o, int32_t n_row, 
 // Xi; part: xi_gemv_part_elems(n_row) doubles.
 cudaError_t launch_split_xi(const double *xi, int64_t n, bool df, void *out, cudaStream_t s);
 size_t xi_gemv_part_elems(int32_t n_row);
+// split: column ranges per row group (0: a default sized for about two waves).
 cudaError_t launch_xi_gemv(const void *xi, int32_t n_row, int64_t n_col, bool df, const void *fbb, double *part,
-                           double *buf, int n_sm, cudaStream_t s);
+                           double *buf, int n_sm, cudaStream_t s, const int32_t *skip = nullptr, int split = 0);
+int xi_gemv_default_split(int32_t n_row, int64_t n_col, int n_sm);
+int xi_gemv_max_split(int64_t n_col);
 
 // One-tile tcgen05 self-check: d (128 x n) = a (128 x 16) b (16 x n) through BF16 hi/lo
 // splits; variant selects the operand layout reading (diagnostic).
@@ -292,7 +295,30 @@ cudaError_t launch_mma_check(int variant, int n, const float *a, const float *b,
 // full_op signed 1-based operations (negative: time reversal) and full_irr 0-based; stored
 // as (hi, lo) float pairs when df, else as floats (the Xi.F element format).
 cudaError_t launch_foldout(int32_t n_full, int32_t n_mode, const int32_t *full_op, const int32_t *full_irr,
-                           const double *op_cart, const double *fn, bool df, void *fbb, cudaStream_t s);
+                           const double *op_cart, const double *fn, bool df, void *fbb, cudaStream_t s,
+                           const int32_t *skip = nullptr);
+
+// Device state of the BTE iteration (kappa.f90:326-495): the iteration counter, the mixing
+// factor and the done flag, which every kernel of an iteration checks first.
+struct BteCtl {
+    int32_t done, iter;
+    double mixing;
+};
+struct BteDev {
+    int32_t n_irr, n_mode, n_row, maxiter;
+    double tol, sqtol;
+    const int32_t *rowidx;            // [n_irr*n] row of (q1, b1), -1 without one
+    const double *qs;                 // [n_irr*n]
+    const double *F0;                 // [n_irr*n*3]
+    const int32_t *degen;             // [n_irr*n] degenerate-subspace sizes at the irreducible points
+    const int32_t *degen_mode;        // [n_irr*n*n] its modes, 1-based
+    double *fn, *fnb;                 // [n_irr*n*3] current F and the new one
+    double *scf;                      // [maxiter] relative changes
+    double *part;                     // [bte_part_elems(n_irr)] partial sums of the change
+    BteCtl *ctl;
+};
+cudaError_t launch_bte_update(const BteDev &d, const double *buf, cudaStream_t s);
+int bte_part_elems(int32_t n_irr);
 
 // What an entry point compiled outside the context's own file needs of a context.
 // Off-diagonal kappa (k_offdiag.cu), one CTA per irreducible point. Index tables 0-based.

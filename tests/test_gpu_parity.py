@@ -293,7 +293,9 @@ def test_repeat_calls_are_stable(configs):
 
 def test_transfer_counter_counts_the_copies(configs):
     """tdg_transfer_bytes: a Xi download adds exactly its size; once the first kappa call has
-    uploaded the symmetry tables, a BTE iteration is one Fn upload and one Xi.F download."""
+    uploaded the symmetry and degeneracy tables, a kappa call uploads qs, F0, Fn and the
+    16-byte control word of the device iteration once, and downloads the control word per
+    chunk of iterations and Fn once."""
     prob = Problem.load(configs["rocksalt"], (6, 6, 6), readiso=True)
     opts = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=9)
     lists = QLists.monte_carlo(prob, opts)
@@ -311,8 +313,9 @@ def test_transfer_counter_counts_the_copies(configs):
     h2, d2 = sr.transfer_bytes()
     sr.kappa(opts, maxiter=1, tol=0.0)
     h3, d3 = sr.transfer_bytes()
-    assert h3 - h2 == prob.n_irr * n * 3 * 8
-    assert d3 - d2 == lists.n_row * 3 * 8
+    m = prob.n_irr * n
+    assert h3 - h2 == m * 8 + 2 * m * 3 * 8 + 16
+    assert d3 - d2 == 16 + m * 3 * 8
     sr.close()
 
 
