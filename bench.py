@@ -271,6 +271,55 @@ def run_profile(args):
     sr.close()
 
 
+def fourphonon_leg(cfg_name, steps):
+    """Three- plus four-phonon scattering on the C3 perovskite (its batched configuration):
+    the same uneven three-phonon samples plus seeded four-phonon pair samples per
+    irreducible point (two lists of 27 points, the size of the reference's -qg4ph 3 3 3),
+    mixed precision and FP64. Returns q-quartets/s of the added four-phonon work and the
+    pass and kappa times."""
+    from tdep_gb300 import Options, Problem, QLists, ScatteringRates, synth
+
+    cfg = CONFIGS[cfg_name]
+    tmp = tempfile.mkdtemp(prefix="tdg_bench4_")
+    d = synth.write_config(cfg["synth"], Path(tmp) / cfg["synth"], seed=1, order4=True)
+    prob = Problem.load(d, cfg["grid"], fourthorder=True, readiso=True)
+    lo, hi = cfg["uneven"]
+    rng = np.random.default_rng(1)
+    s3 = {q: np.sort(rng.choice(np.arange(1, prob.n_full + 1), size=int(rng.integers(lo, hi + 1)),
+                                replace=False)).astype(np.int32) for q in range(1, prob.n_irr + 1)}
+    rng4 = np.random.default_rng(2)
+    s4 = {q: tuple(np.sort(rng4.choice(np.arange(1, prob.n_full + 1), size=27, replace=False)).astype(np.int32)
+                   for _ in range(2)) for q in range(1, prob.n_irr + 1)}
+    lists = QLists.per_irreducible(prob, samples3=s3, samples4=s4)
+    out = {"workload": cfg["workload"] + "; plus four-phonon: seeded pair samples of 27 x 27 points per irreducible q"}
+    sr = ScatteringRates(prob)
+    for prec in ("mixed", "fp64"):
+        o34 = Options(temperature=cfg["temperature"], integrationtype=cfg["it"], isotopescattering=False, seed=1,
+                      precision=prec, fourthorder=True, itertol=1e-6, itermaxsteps=200)
+        o3 = Options(**{**o34.__dict__, "fourthorder": False})
+        ms34, ms3 = [], []
+        for i in range(steps + 1):  # the first of each is a warm-up
+            sr.generate(o3, lists)
+            if i:
+                ms3.append(sr.stats["device_ms"])
+            sr.generate(o34, lists)
+            if i:
+                ms34.append(sr.stats["device_ms"])
+        quart = sr.stats["quartets"]
+        t0 = time.perf_counter()
+        _, ki = sr.kappa(o34)
+        kms = 1e3 * (time.perf_counter() - t0)
+        d4 = float(np.median(ms34)) - float(np.median(ms3))
+        out[prec] = {"q_quartets": int(quart), "pass_ms_3ph_4ph": float(np.median(ms34)),
+                     "pass_ms_3ph_only": float(np.median(ms3)), "fourphonon_ms": d4,
+                     "q_quartets_per_s": quart / (d4 / 1e3) if d4 > 0 else None, "kappa_wall_ms": kms,
+                     "kappa_xx": float(ki[0, 0])}
+    sr.close()
+    out["mixed_speedup_3ph_4ph"] = out["fp64"]["pass_ms_3ph_4ph"] / out["mixed"]["pass_ms_3ph_4ph"]
+    out["kappa_rel_err_mixed_vs_fp64"] = abs(out["mixed"]["kappa_xx"] / out["fp64"]["kappa_xx"] - 1)
+    return out
+
+
 def run_gb300(args):
     import torch
 
@@ -421,6 +470,8 @@ def run_gb300(args):
                                                               "tensor cores (mixed precision)"},
         "linewidth_max_hartree": float(lw_mixed.max()),
     }
+    if "uneven" in cfg and args.config == "perovskite16":
+        line["three_plus_four_phonon"] = fourphonon_leg(args.config, max(2, args.steps // 2))
     print(json.dumps(line))
 
 
