@@ -62,7 +62,7 @@ __device__ __forceinline__ const float2 *egvs4_ptr<float2>(const PhononDev &ph) 
 }
 
 struct Layout4 {
-    size_t om, be, sg, vel, fo, inv1, wrow, rowid, red, R, E, ph, A, B, total;
+    size_t om, be, sg, vel, fo, inv1, wrow, rowid, red, R, occ, E, ph, A, B, total;
 };
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~size_t(15); }
 __host__ __device__ inline Layout4 make_layout4(int n, int cs) {
@@ -79,6 +79,7 @@ __host__ __device__ inline Layout4 make_layout4(int n, int cs) {
     L.rowid = o; o += al16(sizeof(int) * n);
     L.red = o; o += al16(sizeof(int4) * kMaxRed);
     L.R = o; o += al16(sizeof(double) * 3 * n);
+    L.occ = o; o += al16(sizeof(double) * (2 * n * n + 4 * n));  // occupation products (see below)
     L.E = o; o += al16((size_t)cs * 4 * n2);
     L.ph = o; o += al16((size_t)cs * kPhaseChunk4);
     const size_t csz = (size_t)cs > sizeof(double) ? (size_t)cs : sizeof(double);
@@ -109,6 +110,13 @@ __global__ void __launch_bounds__(threads4_for(N)) k_fourphonon(FourPhArgs a) {
     int *rowid = (int *)(smem + L.rowid);
     int4 *red = (int4 *)(smem + L.red);
     double *Rs = (double *)(smem + L.R);    // R2, R3, R4 of the current b1
+    // Occupation products of the quartet, so that the four polynomials of the weights
+    // (scattering_fourphonon.f90:161-186) cost 10 FP64 operations per mode quadruplet
+    // instead of 26: per (b3, b4) P00 = n3 n4 and P11 = (n3+1)(n4+1), with n3 (n4+1) =
+    // P00 + n3 and (n3+1) n4 = P00 + n4; per b2 n2, n2+1, 3 n2, 3 (n2+1). Two tables of n^2
+    // keep three CTAs per SM at n = 15.
+    double *P00 = (double *)(smem + L.occ), *P11 = P00 + N * N;
+    double *N2v = P11 + N * N, *N2p = N2v + N, *N2x3 = N2p + N, *N2px3 = N2x3 + N;
     C *E = (C *)(smem + L.E);               // E[k*N2 + r*N + b], k = 0..3
     C *ph = (C *)(smem + L.ph);
     C *A = (C *)(smem + L.A);
@@ -151,7 +159,9 @@ __global__ void __launch_bounds__(threads4_for(N)) k_fourphonon(FourPhArgs a) {
             om[i] = w;
             sg[i] = P.sigsq[(size_t)qi[k] * N + b];
             be[i] = k > 0 ? P.be[(size_t)qi[k] * N + b] : 0.0;
-            fo[i] = (float)w;
+            // NaN marks omega < 1e-9 Ha: the skip test then runs in FP32 (double compares and
+            // conversions per mode quadruplet would occupy GB300's narrow FP64 pipe)
+            fo[i] = w < kFreqTolD ? __int_as_float(0x7fc00000) : (float)w;
             fo[4 * N + i] = (float)sg[i];
             for (int d = 0; d < 3; ++d) vel[i * 3 + d] = P.vel[((size_t)qf[k] * N + b) * 3 + d];
             if (k == 0) {
@@ -167,6 +177,19 @@ __global__ void __launch_bounds__(threads4_for(N)) k_fourphonon(FourPhArgs a) {
             const int k = i / N2, e = i % N2;
             const int r = e / N, b = e % N;
             E[i] = egvs[((size_t)qf[k] * N + b) * N + r];
+        }
+        __syncthreads();  // be[] of q2..q4 is in shared memory
+        for (int i = tid; i < N * N; i += bd) {
+            const double n3 = be[2 * N + i / N], n4 = be[3 * N + i % N];
+            P00[i] = n3 * n4;
+            P11[i] = (n3 + 1.0) * (n4 + 1.0);
+        }
+        for (int b = tid; b < N; b += bd) {
+            const double n2 = be[N + b];
+            N2v[b] = n2;
+            N2p[b] = n2 + 1.0;
+            N2x3[b] = 3.0 * n2;
+            N2px3[b] = 3.0 * (n2 + 1.0);
         }
         int g[3][3];
         {
@@ -221,7 +244,6 @@ __global__ void __launch_bounds__(threads4_for(N)) k_fourphonon(FourPhArgs a) {
         __syncthreads();
         const C *E2 = E + N2, *E3 = E + 2 * N2, *E4 = E + 3 * N2;
         const double *om1 = om, *om2 = om + N, *om3 = om + 2 * N, *om4 = om + 3 * N;
-        const double *be2 = be + N, *be3 = be + 2 * N, *be4 = be + 3 * N;
         const float *fo1 = fo, *fo2 = fo + N, *fo3 = fo + 2 * N, *fo4 = fo + 3 * N;
         const float *fs1 = fo + 4 * N, *fs2 = fo + 5 * N, *fs3 = fo + 6 * N, *fs4 = fo + 7 * N;
         for (int b1 = 0; b1 < N; ++b1) {
@@ -259,13 +281,14 @@ __global__ void __launch_bounds__(threads4_for(N)) k_fourphonon(FourPhArgs a) {
             // ---- delta weights, occupations (FP64); F in A as doubles ----
             double *F = (double *)A;
             const double o1 = om1[b1], w1 = wrow[b1];
+            const double pw4 = kFourPhononPrefactor * w1 * w1;
             const float f_o1 = fo1[b1];
             for (int o = tid; o < N3; o += bd) {
                 const int b2 = o / N2, b3 = (o / N) % N, b4 = o % N;
                 double fall = 0.0;
-                const double o2 = om2[b2], o3 = om3[b3], o4 = om4[b4];
-                if (!(o2 < kFreqTolD || o3 < kFreqTolD || o4 < kFreqTolD)) {
-                    const float f2 = fo2[b2], f3 = fo3[b3], f4 = fo4[b4];
+                const float f2 = fo2[b2], f3 = fo3[b3], f4 = fo4[b4];
+                if (f2 == f2 && f3 == f3 && f4 == f4) {  // no omega below 1e-9 Ha
+                    const double o2 = om2[b2], o3 = om3[b3], o4 = om4[b4];
                     uint32_t live = 0xffu;  // the -it 6 width can cancel in FP32: not screened
                     if (it != 6) {
                         float sgf = sigfix32;
@@ -281,11 +304,14 @@ __global__ void __launch_bounds__(threads4_for(N)) k_fourphonon(FourPhArgs a) {
                                (fabsf(f_o1 - (-f2 - f3 + f4)) <= win ? 128u : 0u);
                     }
                     if (live) {
-                        double sigma;
+                        double sigma, invsig;
                         if (it == 1) {
                             sigma = P.sigma_fixed;
+                            invsig = 1.0 / sigma;
                         } else if (it == 2) {
-                            sigma = sqrt(sg[b1] + sg[N + b2] + sg[2 * N + b3] + sg[3 * N + b4]);
+                            const double sq = sg[b1] + sg[N + b2] + sg[2 * N + b3] + sg[3 * N + b4];
+                            invsig = rsqrt(sq);
+                            sigma = sq * invsig;
                         } else {
                             const double *v1 = vel + 3 * b1, *v2 = vel + 3 * (N + b2), *v3 = vel + 3 * (2 * N + b3),
                                          *v4 = vel + 3 * (3 * N + b4);
@@ -297,32 +323,41 @@ __global__ void __launch_bounds__(threads4_for(N)) k_fourphonon(FourPhArgs a) {
                             sigma += adaptive_pair(v2, v4, P.reclat_g) / 6.0;
                             sigma += adaptive_pair(v3, v4, P.reclat_g) / 6.0;
                             sigma += P.thresh_sigma;
+                            invsig = 1.0 / sigma;
                         }
-                        const double invsig = 1.0 / sigma;
                         const double win8 = 8.0 * sigma, h = 0.5 * invsig * invsig, cg = kSqrt2PiInv * invsig;
                         const double *tab = P.exp2tab;
-                        auto gs = [&](uint32_t bit, double mu) {
-                            return (live & bit) ? gauss(o1 - mu, win8, h, cg, tab) : 0.0;
-                        };
-                        const double d0 = gs(1u, o2 + o3 + o4) - gs(2u, -o2 - o3 - o4);
-                        const double d1 = gs(4u, -o2 + o3 + o4) - gs(8u, o2 - o3 - o4);
-                        const double d2 = gs(16u, o2 - o3 + o4) - gs(32u, -o2 + o3 - o4);
-                        const double d3 = gs(64u, o2 + o3 - o4) - gs(128u, -o2 - o3 + o4);
+                        // a centre is formed only for a Gaussian that the screen left live
+                        const double d0 = ((live & 1u) ? gauss(o1 - (o2 + o3 + o4), win8, h, cg, tab) : 0.0) -
+                                          ((live & 2u) ? gauss(o1 - (-o2 - o3 - o4), win8, h, cg, tab) : 0.0);
+                        const double d1 = ((live & 4u) ? gauss(o1 - (-o2 + o3 + o4), win8, h, cg, tab) : 0.0) -
+                                          ((live & 8u) ? gauss(o1 - (o2 - o3 - o4), win8, h, cg, tab) : 0.0);
+                        const double d2 = ((live & 16u) ? gauss(o1 - (o2 - o3 + o4), win8, h, cg, tab) : 0.0) -
+                                          ((live & 32u) ? gauss(o1 - (-o2 + o3 - o4), win8, h, cg, tab) : 0.0);
+                        const double d3 = ((live & 64u) ? gauss(o1 - (o2 + o3 - o4), win8, h, cg, tab) : 0.0) -
+                                          ((live & 128u) ? gauss(o1 - (-o2 - o3 + o4), win8, h, cg, tab) : 0.0);
                         if (nonzero(d0) || nonzero(d1) || nonzero(d2) || nonzero(d3)) {
                             const C psi = B[o];
-                            const double cr = (double)psi.x, ci = (double)psi.y;
-                            const double psisq = kFourPhononPrefactor * (cr * cr + ci * ci) * w1 * w1;
-                            const double n2 = be2[b2], n3 = be3[b3], n4 = be4[b4];
-                            const double n2p = n2 + 1.0, n3p = n3 + 1.0, n4p = n4 + 1.0;
-                            const double plf0 = n2p * n3p * n4p - n2 * n3 * n4;
-                            const double plf1 = 3.0 * n2 * n3p * n4p - n2p * n3 * n4;
-                            const double plf2 = 3.0 * n3 * n2p * n4p - n3p * n2 * n4;
-                            const double plf3 = 3.0 * n4 * n3p * n2p - n4p * n3 * n2;
-                            const double f0 = mult0 * psisq * plf0 * d0;
-                            const double f1 = mult1 * psisq * plf1 * d1;
-                            const double f2d = mult1 * psisq * plf2 * d2;
-                            const double f3d = mult1 * psisq * plf3 * d3;
-                            fall = f0 + f1 + f2d + f3d;
+                            double ps;
+                            if constexpr (sizeof(R) == 4) {
+                                ps = (double)fmaf(psi.x, psi.x, psi.y * psi.y);  // |Psi|^2 of an FP32 Psi
+                            } else {
+                                ps = psi.x * psi.x + psi.y * psi.y;
+                            }
+                            // plf0 = (n2+1)(n3+1)(n4+1) - n2 n3 n4, plf1 = 3 n2 (n3+1)(n4+1) - (n2+1) n3 n4,
+                            // plf2 = 3 n3 (n2+1)(n4+1) - (n3+1) n2 n4, plf3 = 3 n4 (n2+1)(n3+1) - (n4+1) n2 n3
+                            const int k34 = b3 * N + b4;
+                            const double n2 = N2v[b2], n2p = N2p[b2], p00 = P00[k34], p11 = P11[k34];
+                            double acc = 0.0;
+                            if (nonzero(d0)) acc = mult0 * fma(n2p, p11, -n2 * p00) * d0;
+                            double a1 = 0.0;
+                            if (nonzero(d1)) a1 = fma(N2x3[b2], p11, -n2p * p00) * d1;
+                            if (nonzero(d2) || nonzero(d3)) {
+                                const double q1 = p00 + be[2 * N + b3], q2 = p00 + be[3 * N + b4];
+                                if (nonzero(d2)) a1 = fma(N2px3[b2], q1, -n2 * q2) * d2 + a1;
+                                if (nonzero(d3)) a1 = fma(N2px3[b2], q2, -n2 * q1) * d3 + a1;
+                            }
+                            fall = pw4 * ps * fma(mult1, a1, acc);
                         }
                     }
                 }
