@@ -196,24 +196,25 @@ __global__ void __launch_bounds__(threads4_for(N)) k_fourphonon(FourPhArgs a) {
             const int n12 = m.grid[1] * m.grid[2];
             for (int k = 0; k < 3; ++k) {
                 const int q = qf[k + 1];
-                g[k][0] = q / n12;
-                g[k][1] = (q / m.grid[2]) % m.grid[1];
-                g[k][2] = q % m.grid[2];
+                g[k][0] = (q / n12) * m.lmul[0];  // g_d L/N_d
+                g[k][1] = ((q / m.grid[2]) % m.grid[1]) * m.lmul[1];
+                g[k][2] = (q % m.grid[2]) * m.lmul[2];
             }
         }
         // ---- T1 = E1^T . ptf for the row modes, in chunks of phases ----
         for (int c0 = 0; c0 < fc.n; c0 += kPhaseChunk4) {
             const int cn = min(kPhaseChunk4, fc.n - c0);
             __syncthreads();
+            // K = sum_d ((g2 lv2 + g3 lv3 + g4 lv4)_d mod N_d) L/N_d mod L, evaluated as
+            // (sum_d (g2 L/N_d) lv2 + ...) mod L: the same integer with one division
             for (int i = tid; i < cn; i += bd) {
                 const int32_t *lv = fc.lv + (size_t)(c0 + i) * 9;
-                int K = 0;
-                for (int d = 0; d < 3; ++d) {
-                    int kd = (g[0][d] * lv[d] + g[1][d] * lv[3 + d] + g[2][d] * lv[6 + d]) % m.grid[d];
-                    if (kd < 0) kd += m.grid[d];
-                    K += kd * m.lmul[d];
-                }
-                ph[i] = twiddle4<C>(a, K % m.L);
+                int S = 0;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) S += g[0][d] * lv[d] + g[1][d] * lv[3 + d] + g[2][d] * lv[6 + d];
+                int K = S % m.L;
+                if (K < 0) K += m.L;
+                ph[i] = twiddle4<C>(a, K);
             }
             __syncthreads();
             for (int o = tid; o < N * N3; o += bd) {

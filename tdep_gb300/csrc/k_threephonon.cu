@@ -79,18 +79,20 @@ __device__ __forceinline__ const float2 *egvs_ptr<float2>(const PhononDev &ph) {
 constexpr int kAdjFlush = 64;
 
 // exp(-2 pi i (q2.lv2 + q3.lv3)) of force-constant triplet t as an exact root of unity:
-// q = g/G on the mesh and lv integer, so the phase index is sum_d (g2 lv2 + g3 lv3)_d mod G_d
-// scaled to L = lcm(G).
+// q = g/N on the mesh and lv integer, so the phase is twiddle[K] with
+// K = sum_d ((g2_d lv2_d + g3_d lv3_d) mod N_d) L/N_d mod L, L = lcm(N). Since N_d (L/N_d) = L
+// the inner reductions can be dropped: K = (sum_d (g2_d L/N_d) lv2_d + (g3_d L/N_d) lv3_d)
+// mod L, the same integer with one division instead of four; u2, u3 hold g_d L/N_d of the
+// q-triplet.
 template <typename C>
-__device__ __forceinline__ C phase3(const Fc3Dev &fc, const MeshDev &m, const int *gi2, const int *gi3, int t) {
+__device__ __forceinline__ C phase3(const Fc3Dev &fc, const MeshDev &m, const int *u2, const int *u3, int t) {
     const int32_t *lv = fc.lv + (size_t)t * 6;
-    int K = 0;
-    for (int d = 0; d < 3; ++d) {
-        int kd = (gi2[d] * lv[d] + gi3[d] * lv[3 + d]) % m.grid[d];
-        if (kd < 0) kd += m.grid[d];
-        K += kd * m.lmul[d];
-    }
-    return twiddle_at<C>(fc, K % m.L);
+    int S = 0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) S += u2[d] * lv[d] + u3[d] * lv[3 + d];
+    int K = S % m.L;
+    if (K < 0) K += m.L;
+    return twiddle_at<C>(fc, K);
 }
 
 
@@ -287,6 +289,10 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
             const int n12 = m.grid[1] * m.grid[2];
             gi2[0] = q2 / n12; gi2[1] = (q2 / m.grid[2]) % m.grid[1]; gi2[2] = q2 % m.grid[2];
             gi3[0] = q3 / n12; gi3[1] = (q3 / m.grid[2]) % m.grid[1]; gi3[2] = q3 % m.grid[2];
+            for (int d = 0; d < 3; ++d) {  // g_d L/N_d (phase3)
+                gi2[d] *= m.lmul[d];
+                gi3[d] *= m.lmul[d];
+            }
         }
         for (int c0 = 0; c0 < fc.n; c0 += kPhaseChunk) {
             const int cn = min(kPhaseChunk, fc.n - c0);
