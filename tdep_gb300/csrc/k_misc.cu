@@ -312,8 +312,8 @@ __global__ void k_sample_bits(int32_t n_full, const int64_t *rbeg, const int32_t
 //  - mixed-precision runs: Xi and F as floats, the 2^-24 rounding of the FP32 contraction
 //    that produced Xi; chains of kChain products by FMA are added into double-float
 //    accumulators, so the sum over 10^5 columns adds no error of its own. Half the bytes.
-// A CTA takes kGemvRows rows and one of gemv_split() column ranges (gridDim.y): each F value
-// read from L2 serves kGemvRows rows. Partial sums go to part[row][range][3] (FP64) and are
+// A CTA takes ROWS rows (4 or 8, autotuned) and one of the column ranges (gridDim.y): each F
+// value read from L2 serves ROWS rows. Partial sums go to part[row][range][3] (FP64) and are
 // added in range order by k_xi_reduce, so the result does not depend on scheduling. The
 // in-CTA reduction stays in double-float too: FP64 shuffles and adds in every CTA's epilogue
 // cost more than the product itself once there are more than a few ranges.
@@ -402,36 +402,36 @@ __global__ void k_split_xi(const double *xi, int64_t n, void *out) {
 
 // DF: xi, fbb as float2 (FP64 runs); otherwise as float (mixed precision). Loads of four
 // consecutive columns per thread (16 bytes) measured slower than these 4-byte coalesced loads.
-template <bool DF>
+template <bool DF, int ROWS>
 __global__ void __launch_bounds__(256) k_xi_gemv(const void *__restrict__ xi_, int32_t n_row, int64_t n_col,
                                                  const void *__restrict__ fbb_, double *part, const int32_t *skip) {
-    __shared__ float2 sh[kGemvRows * 3][8];
+    __shared__ float2 sh[ROWS * 3][8];
     if (skip && *skip) return;
-    const int r0 = blockIdx.x * kGemvRows;
-    const int nr = min(kGemvRows, n_row - r0);
+    const int r0 = blockIdx.x * ROWS;
+    const int nr = min(ROWS, n_row - r0);
     const int64_t per = (n_col + gridDim.y - 1) / gridDim.y;
     const int64_t c0 = min(n_col, per * blockIdx.y), c1 = min(n_col, c0 + per);
-    float2 acc[kGemvRows][3];
+    float2 acc[ROWS][3];
 #pragma unroll
-    for (int k = 0; k < kGemvRows; ++k) acc[k][0] = acc[k][1] = acc[k][2] = make_float2(0.f, 0.f);
+    for (int k = 0; k < ROWS; ++k) acc[k][0] = acc[k][1] = acc[k][2] = make_float2(0.f, 0.f);
     const int64_t step = blockDim.x;
     int64_t j = c0 + threadIdx.x;
     if constexpr (DF) {
         const float2 *xi = static_cast<const float2 *>(xi_);
         const float2 *fbb = static_cast<const float2 *>(fbb_);
         for (; j + step < c1; j += 2 * step) {
-            float2 x[2][kGemvRows];
+            float2 x[2][ROWS];
 #pragma unroll
             for (int u = 0; u < 2; ++u)
 #pragma unroll
-                for (int k = 0; k < kGemvRows; ++k)
+                for (int k = 0; k < ROWS; ++k)
                     x[u][k] = k < nr ? __ldcs(xi + (int64_t)(r0 + k) * n_col + j + u * step) : make_float2(0.f, 0.f);
 #pragma unroll
             for (int u = 0; u < 2; ++u) {
                 const float2 *f = fbb + (j + u * step) * 3;
                 const float2 f0 = __ldg(f), f1 = __ldg(f + 1), f2 = __ldg(f + 2);
 #pragma unroll
-                for (int k = 0; k < kGemvRows; ++k) {
+                for (int k = 0; k < ROWS; ++k) {
                     df_fma(acc[k][0], x[u][k], f0);
                     df_fma(acc[k][1], x[u][k], f1);
                     df_fma(acc[k][2], x[u][k], f2);
@@ -442,7 +442,7 @@ __global__ void __launch_bounds__(256) k_xi_gemv(const void *__restrict__ xi_, i
             const float2 *f = fbb + j * 3;
             const float2 f0 = __ldg(f), f1 = __ldg(f + 1), f2 = __ldg(f + 2);
 #pragma unroll
-            for (int k = 0; k < kGemvRows; ++k) {
+            for (int k = 0; k < ROWS; ++k) {
                 const float2 x = k < nr ? __ldcs(xi + (int64_t)(r0 + k) * n_col + j) : make_float2(0.f, 0.f);
                 df_fma(acc[k][0], x, f0);
                 df_fma(acc[k][1], x, f1);
@@ -453,18 +453,18 @@ __global__ void __launch_bounds__(256) k_xi_gemv(const void *__restrict__ xi_, i
         const float *xi = static_cast<const float *>(xi_);
         const float *fbb = static_cast<const float *>(fbb_);
         for (; j + (kChain - 1) * step < c1; j += kChain * step) {
-            float x[kChain][kGemvRows], f[kChain][3];
+            float x[kChain][ROWS], f[kChain][3];
 #pragma unroll
             for (int u = 0; u < kChain; ++u)
 #pragma unroll
-                for (int k = 0; k < kGemvRows; ++k)
+                for (int k = 0; k < ROWS; ++k)
                     x[u][k] = k < nr ? __ldcs(xi + (int64_t)(r0 + k) * n_col + j + u * step) : 0.f;
 #pragma unroll
             for (int u = 0; u < kChain; ++u)
 #pragma unroll
                 for (int d = 0; d < 3; ++d) f[u][d] = __ldg(fbb + (j + u * step) * 3 + d);
 #pragma unroll
-            for (int k = 0; k < kGemvRows; ++k)
+            for (int k = 0; k < ROWS; ++k)
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {
                     float c = x[0][k] * f[0][d];
@@ -477,7 +477,7 @@ __global__ void __launch_bounds__(256) k_xi_gemv(const void *__restrict__ xi_, i
             const float *f = fbb + j * 3;
             const float f0 = __ldg(f), f1 = __ldg(f + 1), f2 = __ldg(f + 2);
 #pragma unroll
-            for (int k = 0; k < kGemvRows; ++k) {
+            for (int k = 0; k < ROWS; ++k) {
                 const float x = k < nr ? __ldcs(xi + (int64_t)(r0 + k) * n_col + j) : 0.f;
                 df_add1(acc[k][0], x * f0);
                 df_add1(acc[k][1], x * f1);
@@ -487,7 +487,7 @@ __global__ void __launch_bounds__(256) k_xi_gemv(const void *__restrict__ xi_, i
     }
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
-    for (int k = 0; k < kGemvRows; ++k)
+    for (int k = 0; k < ROWS; ++k)
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             float2 v = acc[k][d];
@@ -663,15 +663,22 @@ int xi_gemv_max_split(int64_t n_col) {
 }
 
 cudaError_t launch_xi_gemv(const void *xi, int32_t n_row, int64_t n_col, bool df, const void *fbb, double *part,
-                           double *buf, int n_sm, cudaStream_t s, const int32_t *skip, int split) {
+                           double *buf, int n_sm, cudaStream_t s, const int32_t *skip, int shape) {
     if (n_row <= 0) return cudaSuccess;
+    // shape = rows per CTA * 100 + column ranges; 0: 4 rows and the default split
+    int rows = shape / 100, split = shape % 100;
+    if (rows != 8) rows = 4;
     if (split <= 0) split = gemv_split(n_row, n_col, n_sm);
     split = std::min(split, xi_gemv_max_split(n_col));
-    dim3 grid((unsigned)((n_row + kGemvRows - 1) / kGemvRows), (unsigned)split);
-    if (df)
-        k_xi_gemv<true><<<grid, 256, 0, s>>>(xi, n_row, n_col, fbb, part, skip);
+    dim3 grid((unsigned)((n_row + rows - 1) / rows), (unsigned)split);
+    if (df && rows == 8)
+        k_xi_gemv<true, 8><<<grid, 256, 0, s>>>(xi, n_row, n_col, fbb, part, skip);
+    else if (df)
+        k_xi_gemv<true, 4><<<grid, 256, 0, s>>>(xi, n_row, n_col, fbb, part, skip);
+    else if (rows == 8)
+        k_xi_gemv<false, 8><<<grid, 256, 0, s>>>(xi, n_row, n_col, fbb, part, skip);
     else
-        k_xi_gemv<false><<<grid, 256, 0, s>>>(xi, n_row, n_col, fbb, part, skip);
+        k_xi_gemv<false, 4><<<grid, 256, 0, s>>>(xi, n_row, n_col, fbb, part, skip);
     k_xi_reduce<<<(n_row * 3 + 255) / 256, 256, 0, s>>>(part, n_row, split, buf, skip);
     return cudaGetLastError();
 }

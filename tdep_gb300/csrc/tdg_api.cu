@@ -1783,14 +1783,17 @@ extern "C" int tdg_kappa(tdg_ctx *c, const tdg_opts *o, int32_t maxiter, double 
         {
             CUDA_TRY(launch_foldout(N, n, c->d_full_op.p, c->d_full_irr.p, c->d_op_cart.p, c->d_fn.p, df, c->d_fbb.p,
                                     s));
+            // shapes: rows per CTA (4, 8) * 100 + column ranges (the default, twice it)
             const int s0 = xi_gemv_default_split(nr, ncol, c->n_sm), smax = xi_gemv_max_split(ncol);
             std::vector<int> cand;
-            for (int v : {s0, 2 * s0, 4 * s0, 8 * s0})
-                if (v <= smax && std::find(cand.begin(), cand.end(), v) == cand.end()) cand.push_back(v);
+            for (int rows : {4, 8})
+                for (int v : {s0, 2 * s0})
+                    if (v <= smax && std::find(cand.begin(), cand.end(), rows * 100 + v) == cand.end())
+                        cand.push_back(rows * 100 + v);
             std::ostringstream key;
             key << "xigemv/r" << nr << "/c" << ncol;
             bool tuned = false;
-            CUDA_TRY(tune_pick(tune_key(key.str().c_str(), n, df ? 0 : 1, c->device), cand, s0,
+            CUDA_TRY(tune_pick(tune_key(key.str().c_str(), n, df ? 0 : 1, c->device), cand, 400 + s0,
                                [&](int v) {
                                    return launch_xi_gemv(c->d_xi_df.p, nr, ncol, df, c->d_fbb.p, c->d_part.p,
                                                          c->d_buf.p, c->n_sm, s, nullptr, v);

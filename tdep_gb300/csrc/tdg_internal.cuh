@@ -280,9 +280,10 @@ cudaError_t launch_sym_tile(const MeshDev &m, const OrbitDev &o, int32_t n_row, 
 // Xi; part: xi_gemv_part_elems(n_row) doubles.
 cudaError_t launch_split_xi(const double *xi, int64_t n, bool df, void *out, cudaStream_t s);
 size_t xi_gemv_part_elems(int32_t n_row);
-// split: column ranges per row group (0: a default sized for about two waves).
+// shape: rows per CTA (4 or 8) * 100 + column ranges per row group (0: 4 rows and a default
+// split sized for about two waves).
 cudaError_t launch_xi_gemv(const void *xi, int32_t n_row, int64_t n_col, bool df, const void *fbb, double *part,
-                           double *buf, int n_sm, cudaStream_t s, const int32_t *skip = nullptr, int split = 0);
+                           double *buf, int n_sm, cudaStream_t s, const int32_t *skip = nullptr, int shape = 0);
 int xi_gemv_default_split(int32_t n_row, int64_t n_col, int n_sm);
 int xi_gemv_max_split(int64_t n_col);
 
