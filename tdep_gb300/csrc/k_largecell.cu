@@ -575,15 +575,21 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
             double d0, d1;
             dirac3(live, o1, o2, o3, win8, h, cg, tab, d0, d1);
             if (!nonzero(d0) && !nonzero(d1)) continue;
+            // (n2 - n3) d0 + (n2 + n3 + 1) d1, forming only the terms whose weight is non-zero
+            // (usually one: a mode triplet rarely sits in a window of both kinds)
             const double n2 = be2[b2], n3 = be3[b3];
-            const double occ = (n2 - n3) * d0 + (n2 + n3 + 1.0) * d1;
+            double occ = 0.0;
+            if (nonzero(d0)) occ = (n2 - n3) * d0;
+            if (nonzero(d1)) occ = fma(n2 + n3 + 1.0, d1, occ);
             if (ADJ) {
                 F[e] = fadj * occ;
                 continue;
             }
             const float2 ps = psi[b2 * n + b3];
-            const double cr = ps.x, ci = ps.y;
-            F[e] = (pw * (cr * cr + ci * ci)) * occ;
+            // |Psi|^2 of the FP32 contraction result in FP32 (one conversion instead of two
+            // plus two FP64 operations); the weights and sums stay FP64
+            const double p2 = (double)fmaf(ps.x, ps.x, ps.y * ps.y);
+            F[e] = (pw * p2) * occ;
         }
         __syncthreads();
         if (ADJ) {
