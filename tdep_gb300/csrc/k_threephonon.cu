@@ -38,6 +38,16 @@ namespace {
 
 constexpr double kThreePhononPrefactor = 3.141592653589793 / 16.0;
 constexpr int kPhaseChunk = 512;
+// Phase factors held in shared memory at a time: at least kPhaseChunk, more when the survivor
+// queue, which later reuses the eigenvector and phase region, is larger anyway (n = 15 in
+// FP32: 1008, so that 1115 force-constant triplets take two passes instead of three at no
+// cost in shared memory).
+__host__ __device__ constexpr int phase_chunk(int n, int cs) {
+    const int ez = (cs * n * n + 15) / 16 * 16;
+    const int qsz = (4 * n * n * n + 15) / 16 * 16;
+    const int room = (qsz - 3 * ez) / cs / 16 * 16;
+    return room > kPhaseChunk ? room : kPhaseChunk;
+}
 
 template <typename R>
 __device__ __forceinline__ const R *mwm_ptr(const Fc3Dev &fc);
@@ -129,7 +139,7 @@ __host__ __device__ inline Layout make_layout(int n, int cs) {
     L.E2 = o + ez;
     L.E3 = o + 2 * ez;
     L.ph = o + 3 * ez;
-    const size_t eph = 3 * ez + align16((size_t)cs * kPhaseChunk);
+    const size_t eph = 3 * ez + align16((size_t)cs * phase_chunk(n, cs));
     const size_t qsz = align16(sizeof(uint32_t) * n3);
     L.Q = o;
     o += eph > qsz ? eph : qsz;
@@ -294,8 +304,9 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
                 gi3[d] *= m.lmul[d];
             }
         }
-        for (int c0 = 0; c0 < fc.n; c0 += kPhaseChunk) {
-            const int cn = min(kPhaseChunk, fc.n - c0);
+        constexpr int PC = phase_chunk(N, sizeof(C));
+        for (int c0 = 0; c0 < fc.n; c0 += PC) {
+            const int cn = min(PC, fc.n - c0);
             __syncthreads();
             for (int i = tid; i < cn; i += bd) ph[i] = phase3<C>(fc, m, gi2, gi3, c0 + i);
             __syncthreads();
@@ -524,8 +535,9 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
             // barriers
             const int groups = bd / 27, grp = tid / 27, ijk = tid % 27;
             const int off = (ijk % 3) * N2 + ((ijk / 3) % 3) * N + ijk / 9;
-            for (int c0 = 0; c0 < fc.n; c0 += kPhaseChunk) {
-                const int cn = min(kPhaseChunk, fc.n - c0);
+            constexpr int PCA = phase_chunk(N, sizeof(C));
+            for (int c0 = 0; c0 < fc.n; c0 += PCA) {
+                const int cn = min(PCA, fc.n - c0);
                 __syncthreads();
                 for (int i = tid; i < cn; i += bd) ph[i] = phase3<C>(fc, m, gi2, gi3, c0 + i);
                 __syncthreads();
