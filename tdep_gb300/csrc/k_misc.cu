@@ -409,7 +409,8 @@ __global__ void __launch_bounds__(256) k_xi_gemv(const void *__restrict__ xi_, i
     if (skip && *skip) return;
     const int r0 = blockIdx.x * ROWS;
     const int nr = min(ROWS, n_row - r0);
-    const int64_t per = (n_col + gridDim.y - 1) / gridDim.y;
+    // column ranges start on multiples of 8 (16-byte float4 loads of Xi and F)
+    const int64_t per = ((n_col + gridDim.y - 1) / gridDim.y + 7) / 8 * 8;
     const int64_t c0 = min(n_col, per * blockIdx.y), c1 = min(n_col, c0 + per);
     float2 acc[ROWS][3];
 #pragma unroll
@@ -448,6 +449,73 @@ __global__ void __launch_bounds__(256) k_xi_gemv(const void *__restrict__ xi_, i
                 df_fma(acc[k][1], x, f1);
                 df_fma(acc[k][2], x, f2);
             }
+        }
+    } else if (n_col % 4 == 0) {
+        // float4 loads: a thread takes groups of 4 consecutive columns (rows 16-byte aligned
+        // since n_col % 4 == 0; F of 4 columns is 12 floats, three float4), two groups per
+        // trip, and adds each 8-product FP32 chain into the double-float accumulators
+        const float *xi = static_cast<const float *>(xi_);
+        const float4 *fbb4 = static_cast<const float4 *>(fbb_);
+        const float4 *xr[ROWS];
+#pragma unroll
+        for (int k = 0; k < ROWS; ++k) xr[k] = reinterpret_cast<const float4 *>(xi + (int64_t)(r0 + min(k, nr - 1)) * n_col);
+        const int64_t g1 = c1 / 4;
+        int64_t g = c0 / 4 + threadIdx.x;
+        for (; g + step < g1; g += 2 * step) {
+            float4 x[2][ROWS];
+#pragma unroll
+            for (int u = 0; u < 2; ++u)
+#pragma unroll
+                for (int k = 0; k < ROWS; ++k) x[u][k] = __ldcs(xr[k] + g + u * step);
+            float f[2][12];
+#pragma unroll
+            for (int u = 0; u < 2; ++u)
+#pragma unroll
+                for (int v = 0; v < 3; ++v) {
+                    const float4 t = __ldg(fbb4 + 3 * (g + u * step) + v);
+                    f[u][4 * v] = t.x;
+                    f[u][4 * v + 1] = t.y;
+                    f[u][4 * v + 2] = t.z;
+                    f[u][4 * v + 3] = t.w;
+                }
+#pragma unroll
+            for (int k = 0; k < ROWS; ++k)
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    float c = x[0][k].x * f[0][d];
+                    c = fmaf(x[0][k].y, f[0][3 + d], c);
+                    c = fmaf(x[0][k].z, f[0][6 + d], c);
+                    c = fmaf(x[0][k].w, f[0][9 + d], c);
+                    c = fmaf(x[1][k].x, f[1][d], c);
+                    c = fmaf(x[1][k].y, f[1][3 + d], c);
+                    c = fmaf(x[1][k].z, f[1][6 + d], c);
+                    c = fmaf(x[1][k].w, f[1][9 + d], c);
+                    if (k < nr) df_add1(acc[k][d], c);
+                }
+        }
+        for (; g < g1; g += step) {
+            float4 x[ROWS];
+#pragma unroll
+            for (int k = 0; k < ROWS; ++k) x[k] = __ldcs(xr[k] + g);
+            float f[12];
+#pragma unroll
+            for (int v = 0; v < 3; ++v) {
+                const float4 t = __ldg(fbb4 + 3 * g + v);
+                f[4 * v] = t.x;
+                f[4 * v + 1] = t.y;
+                f[4 * v + 2] = t.z;
+                f[4 * v + 3] = t.w;
+            }
+#pragma unroll
+            for (int k = 0; k < ROWS; ++k)
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    float c = x[k].x * f[d];
+                    c = fmaf(x[k].y, f[3 + d], c);
+                    c = fmaf(x[k].z, f[6 + d], c);
+                    c = fmaf(x[k].w, f[9 + d], c);
+                    if (k < nr) df_add1(acc[k][d], c);
+                }
         }
     } else {
         const float *xi = static_cast<const float *>(xi_);
