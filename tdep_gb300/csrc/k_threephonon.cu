@@ -223,8 +223,12 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
             for (int i = tid; i < fc.n * 27; i += bd) acc[i] = (R)0;
     }
 
+    // the next q-triplet's record is loaded one iteration ahead, so that the per-mode loads
+    // of an iteration wait for one round trip to memory instead of two
+    TripletRec rec_next = blockIdx.x < a.n_trip ? a.trip[blockIdx.x] : TripletRec{};
     for (int t = blockIdx.x; t < a.n_trip; t += gridDim.x) {
-        const TripletRec rec = a.trip[t];
+        const TripletRec rec = rec_next;
+        if (t + (int)gridDim.x < a.n_trip) rec_next = a.trip[t + gridDim.x];
         const int f1 = m.irr_full[rec.q1];
         const int q2 = rec.q2, q3 = rec.q3;
         const int i2 = m.full_irr[q2], i3 = m.full_irr[q3];
@@ -256,7 +260,7 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
             const int r = a.rows.rowidx[(size_t)rec.q1 * N + b];
             const bool on = (mask[b >> 5] >> (b & 31)) & 1u;
             rowid[b] = on ? r : -1;
-            wrow[b] = r >= 0 ? a.rows.weight3[r] : 0.0;
+            wrow[b] = a.rows.w3q[(size_t)rec.q1 * N + b];
             m12[b] = 0u;
             m13[b] = 0u;
             m23[b] = 0u;

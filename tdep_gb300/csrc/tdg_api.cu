@@ -200,7 +200,7 @@ struct tdg_ctx {
     int n_row = 0;
     std::vector<int32_t> row_q1, row_b1;
     DevBuf<int32_t> d_row_q1, d_row_b1, d_rowidx;
-    DevBuf<double> d_w3, d_w4, d_gamma, d_xi, d_od;
+    DevBuf<double> d_w3, d_w4, d_w3q, d_gamma, d_xi, d_od;
     // orbits of the little groups (built once per context)
     DevBuf<int32_t> d_orb_rep_ptr, d_orb_rep, d_orb_img, d_orb_mult, d_orb_nuniq, d_orb_cnt, d_orb_of;
     DevBuf<double> d_rcp;
@@ -926,13 +926,14 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     ph.omega32 = c->d_om32.p;
 
     std::vector<int32_t> rowidx((size_t)nirr * n, -1), rq1(nr), rb1(nr);
-    std::vector<double> w3(nr, 0.0), w4(nr, 0.0);
+    std::vector<double> w3(nr, 0.0), w4(nr, 0.0), w3q((size_t)nirr * n, 0.0);
     for (int r = 0; r < nr; ++r) {
         rq1[r] = c->row_q1[r] - 1;
         rb1[r] = c->row_b1[r] - 1;
         rowidx[(size_t)rq1[r] * n + rb1[r]] = r;
         if (o->thirdorder) w3[r] = 1.0 / (double)(ql->ptr3[r + 1] - ql->ptr3[r]);
         if (o->fourthorder) w4[r] = 1.0 / (double)(ql->ptr4[r + 1] - ql->ptr4[r]);
+        w3q[(size_t)rq1[r] * n + rb1[r]] = w3[r];
     }
     pt.mark("init block");
     // ---- three-phonon samples and candidates ----
@@ -1209,6 +1210,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     chk(c->d_row_q1.upload(rq1.data(), rq1.size(), s));
     chk(c->d_row_b1.upload(rb1.data(), rb1.size(), s));
     chk(c->d_w3.upload(w3.data(), w3.size(), s));
+    chk(c->d_w3q.upload(w3q.data(), w3q.size(), s));
     chk(c->d_w4.upload(w4.data(), w4.size(), s));
     const int64_t ld = (int64_t)N * n;
     const bool fuse_sym = o->thirdorder && !o->fourthorder && !o->isotope;
@@ -1260,6 +1262,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     rows.n_row = nr;
     rows.rowidx = c->d_rowidx.p;
     rows.weight3 = c->d_w3.p;
+    rows.w3q = c->d_w3q.p;
     rows.weight4 = c->d_w4.p;
     const MeshDev mesh = c->mesh();
 

@@ -91,6 +91,7 @@ struct RowsDev {
     const int32_t *rowidx;    // [n_irr*n] row of (q1,b1), -1 when absent
     const double *weight3;    // [n_row] 1/len of the row's three-phonon sample
     const double *weight4;    // [n_row] 1/len of the row's four-phonon sample
+    const double *w3q;        // [n_irr*n] weight3 of the row of (q1,b1), 0 when absent
 };
 
 struct Fc3Dev {
