@@ -100,7 +100,7 @@ def setup(cfg_name, precision="mixed"):
 # on `python bench.py --profile --config <name> --steps 1 --warmup 1` (a one-pass capture).
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_threephonon launch (ncu, one pass), from
 # the launch lists summarised in profiles/
-TRAFFIC_PER_LAUNCH = {"rocksalt16": 40_693_760, "rocksalt24": 456_200_000, "perovskite16": 1_098_700_000}
+TRAFFIC_PER_LAUNCH = {"rocksalt16": 40_693_760, "rocksalt24": 460_600_000, "perovskite16": 1_098_100_000}
 
 
 class ClockSampler:
