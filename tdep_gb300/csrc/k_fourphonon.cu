@@ -7,9 +7,10 @@
 //   get_dirac (:267-327), multiplicities (:104-122), accumulation (:161-186).
 // The reference rebuilds the n^4 ptf per row and contracts it per (b2,b3,b4) (2 n^4
 // complex MACs per mode quadruplet, n^8 per row). Here, per q-quartet:
-//   T1[b1][b][c][d] = sum_{a1,i} E1[3a1+i][b1] sum_t mwm_t(i,j,k,l) phase_t
-// is built once for every row mode b1 (n_fc4 * 81 * n complex MACs) into a per-CTA slice of
-// device scratch, and for each row b1 the n^3 slice of T1 is contracted with E2, E3, E4 in
+//   T1[b1][b][c][d] = sum_a E1[a][b1] ptf[a][b][c][d], ptf = sum_t mwm_t(i,j,k,l) phase_t
+// is built once for every row mode b1 into a per-CTA slice of device scratch: first the
+// pretransform ptf (n_fc4 * 81 real x complex MACs), then its contraction with E1 in place
+// (n^5 complex MACs); for each row b1 the n^3 slice of T1 is contracted with E2, E3, E4 in
 // shared memory (3 n^4 complex MACs per b1): 4 n^5 complex MACs per q-quartet in all.
 // Phases are exact roots of unity from integer lattice vectors, as in the three-phonon
 // kernel. Delta weights, occupations and accumulation are FP64 with the reference's
@@ -93,8 +94,12 @@ __host__ __device__ constexpr int threads4_for(int n) {
     return n * n * n >= 256 ? 256 : ((n * n * n + 31) / 32) * 32;
 }
 
+// Resident CTAs the register budget is sized for: at n = 15 in FP32 shared memory admits
+// three per SM, which the in-place E1 contraction's registers would otherwise reduce to two.
+__host__ __device__ constexpr int min_blocks4(int n, bool dbl) { return (n == 15 && !dbl) ? 3 : 1; }
+
 template <int N, typename R>
-__global__ void __launch_bounds__(threads4_for(N)) k_fourphonon(FourPhArgs a) {
+__global__ void __launch_bounds__(threads4_for(N), min_blocks4(N, sizeof(R) == 8)) k_fourphonon(FourPhArgs a) {
     using C = typename CT<R>::C;
     constexpr int N2 = N * N, N3 = N2 * N;
     constexpr int NA = N / 3;
@@ -201,45 +206,64 @@ __global__ void __launch_bounds__(threads4_for(N)) k_fourphonon(FourPhArgs a) {
                 g[k][2] = (q % m.grid[2]) * m.lmul[2];
             }
         }
-        // ---- T1 = E1^T . ptf for the row modes, in chunks of phases ----
-        for (int c0 = 0; c0 < fc.n; c0 += kPhaseChunk4) {
-            const int cn = min(kPhaseChunk4, fc.n - c0);
-            __syncthreads();
-            // K = sum_d ((g2 lv2 + g3 lv3 + g4 lv4)_d mod N_d) L/N_d mod L, evaluated as
-            // (sum_d (g2 L/N_d) lv2 + ...) mod L: the same integer with one division
-            for (int i = tid; i < cn; i += bd) {
-                const int32_t *lv = fc.lv + (size_t)(c0 + i) * 9;
-                int S = 0;
-#pragma unroll
-                for (int d = 0; d < 3; ++d) S += g[0][d] * lv[d] + g[1][d] * lv[3 + d] + g[2][d] * lv[6 + d];
-                int K = S % m.L;
-                if (K < 0) K += m.L;
-                ph[i] = twiddle4<C>(a, K);
+        // ---- ptf[a][bcd] (pretransform_phi4) into the T1 slice, one atom a1 at a time: the
+        // force-constant quartets are sorted by atom block with a1 leading, so the phase
+        // chunks of one a1 serve exactly its 3 n^3 outputs a = 3 a1 + i (n_fc4 * 81 real x
+        // complex multiply-adds per q-quartet) ----
+        constexpr int NA3 = NA * NA * NA;
+        for (int a1 = 0; a1 < NA; ++a1) {
+            C *P = T1 + (size_t)(3 * a1) * N3;
+            const int t0 = fc.blk_ptr[a1 * NA3], t1 = fc.blk_ptr[(a1 + 1) * NA3];
+            if (t0 >= t1) {
+                for (int o = tid; o < 3 * N3; o += bd) P[o] = czero<C>();
+                continue;
             }
-            __syncthreads();
-            for (int o = tid; o < N * N3; o += bd) {
-                const int b1 = o / N3;
-                if (rowid[b1] < 0) continue;
-                const int bcd = o % N3;
-                const int b = bcd / N2, c = (bcd / N) % N, d = bcd % N;
-                const int a2 = b / 3, a3 = c / 3, a4 = d / 3;
-                const int jkl = (b % 3) * 3 + (c % 3) * 9 + (d % 3) * 27;
-                C acc = c0 == 0 ? czero<C>() : T1[o];
-                for (int a1 = 0; a1 < NA; ++a1) {
-                    const int blk = ((a1 * NA + a2) * NA + a3) * NA + a4;
-                    const int lo = max(fc.blk_ptr[blk], c0), hi = min(fc.blk_ptr[blk + 1], c0 + cn);
-                    if (lo >= hi) continue;
-                    const C e0 = E[(3 * a1) * N + b1], e1 = E[(3 * a1 + 1) * N + b1], e2 = E[(3 * a1 + 2) * N + b1];
-                    for (int tt = lo; tt < hi; ++tt) {
-                        const R *mm = mwm + (size_t)tt * 81 + jkl;
-                        const R m0 = __ldg(mm), m1 = __ldg(mm + 1), m2 = __ldg(mm + 2);
-                        C u;
-                        u.x = fma(m0, e0.x, fma(m1, e1.x, m2 * e2.x));
-                        u.y = fma(m0, e0.y, fma(m1, e1.y, m2 * e2.y));
-                        cfma(acc, u, ph[tt - c0]);
-                    }
+            for (int c0 = t0; c0 < t1; c0 += kPhaseChunk4) {
+                const int cn = min(kPhaseChunk4, t1 - c0);
+                __syncthreads();
+                // K = sum_d ((g2 lv2 + g3 lv3 + g4 lv4)_d mod N_d) L/N_d mod L, evaluated as
+                // (sum_d (g2 L/N_d) lv2 + ...) mod L: the same integer with one division
+                for (int i = tid; i < cn; i += bd) {
+                    const int32_t *lv = fc.lv + (size_t)(c0 + i) * 9;
+                    int S = 0;
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) S += g[0][d] * lv[d] + g[1][d] * lv[3 + d] + g[2][d] * lv[6 + d];
+                    int K = S % m.L;
+                    if (K < 0) K += m.L;
+                    ph[i] = twiddle4<C>(a, K);
                 }
-                T1[o] = acc;
+                __syncthreads();
+                for (int o = tid; o < 3 * N3; o += bd) {
+                    const int i = o / N3, bcd = o % N3;
+                    const int b = bcd / N2, c = (bcd / N) % N, d = bcd % N;
+                    const int blk = ((a1 * NA + b / 3) * NA + c / 3) * NA + d / 3;
+                    const int ijkl = i + (b % 3) * 3 + (c % 3) * 9 + (d % 3) * 27;
+                    C acc = c0 == t0 ? czero<C>() : P[o];
+                    const int lo = max(fc.blk_ptr[blk], c0), hi = min(fc.blk_ptr[blk + 1], c0 + cn);
+                    for (int tt = lo; tt < hi; ++tt) {
+                        const R mv = __ldg(mwm + (size_t)tt * 81 + ijkl);
+                        const C p = ph[tt - c0];
+                        acc.x = fma(mv, p.x, acc.x);
+                        acc.y = fma(mv, p.y, acc.y);
+                    }
+                    P[o] = acc;
+                }
+            }
+        }
+        __syncthreads();
+        // ---- T1[b1][bcd] = sum_a E1[a][b1] ptf[a][bcd], column by column in place (n^5
+        // complex multiply-adds, against n_fc4 * 81 * n when E1 is folded into every
+        // force-constant term) ----
+        for (int col = tid; col < N3; col += bd) {
+            C v[N];
+#pragma unroll
+            for (int x = 0; x < N; ++x) v[x] = T1[(size_t)x * N3 + col];
+            for (int b1 = 0; b1 < N; ++b1) {
+                if (rowid[b1] < 0) continue;
+                C acc = czero<C>();
+#pragma unroll
+                for (int x = 0; x < N; ++x) cfma(acc, E[x * N + b1], v[x]);
+                T1[(size_t)b1 * N3 + col] = acc;
             }
         }
         __syncthreads();
