@@ -407,6 +407,14 @@ __global__ void __launch_bounds__(threads4_for(N), min_blocks4(N, sizeof(R) == 8
                 for (int b2 = 0; b2 < N; ++b2) gsum += Rs[b2];
                 if (nonzero(gsum)) atomicAdd(a.gamma + row, (double)nred * gsum);
             }
+            // the row terms 2 R om / om1, formed once for all equivalent quartets (after Gamma
+            // has read R2)
+            __syncthreads();
+            for (int e = tid; e < 3 * N; e += bd) {
+                const double v = Rs[e];
+                Rs[e] = nonzero(v) ? 2.0 * v * om[(e / N + 1) * N + e % N] * inv1[b1] : 0.0;
+            }
+            __syncthreads();
             for (int i = tid; i < 3 * N * nred; i += bd) {
                 const int r = i / (3 * N), e = i % (3 * N);
                 const int which = e / N, b = e % N;
@@ -414,8 +422,7 @@ __global__ void __launch_bounds__(threads4_for(N), min_blocks4(N, sizeof(R) == 8
                 if (!nonzero(v)) continue;
                 const int4 pr = red[r];
                 const int qp = which == 0 ? pr.x : (which == 1 ? pr.y : pr.z);
-                const double omb = om[(which + 1) * N + b];
-                atomicAdd(a.od + row * ld + (int64_t)qp * N + b, 2.0 * v * omb * inv1[b1]);
+                atomicAdd(a.od + row * ld + (int64_t)qp * N + b, v);
             }
             __syncthreads();
         }
