@@ -349,6 +349,17 @@ int tdg_problem_load(const char *dir, const int32_t grid[3], int fourthorder, in
                      int timereversal, tdg_problem **out);
 void tdg_problem_free(tdg_problem *prob);
 
+/*
+ * Harmonic frequencies (Hartree, ascending) at nq Cartesian points q[3*k..] (1/Bohr,
+ * without 2*pi) from infile.ucposcar and infile.forceconstant in `dir`, polar
+ * force constants included: the per-point stage of phonon_dispersion_relations
+ * (lo_phonon_bandstructure_on_path.f90:203-217 -> type_phonon_dispersions.f90:1083-1190).
+ * At Gamma the non-analytic term is taken along qdir[3*k..] (NULL: [1,0,0] for every
+ * point; a zero direction leaves it out). omega holds nq*3*na values. Host only.
+ */
+int tdg_phonon_frequencies(const char *dir, int32_t nq, const double *q, const double *qdir,
+                           double *omega);
+
 /* Writes outfile.thermal_conductivity (main.f90:246-294) into `dir`. Tensors in a.u. */
 int tdg_write_outfile(const char *dir, double temperature, const double *kappa_sma,
                       const double *kappa_iter, const double *kappa_offdiag);

@@ -136,6 +136,7 @@ SIGNATURES = {
     "tdg_problem_load": (C.c_int, [C.c_char_p, _i32p, C.c_int, C.c_int, C.c_int, C.POINTER(C.POINTER(TdgProblem))]),
     "tdg_problem_free": (None, [C.POINTER(TdgProblem)]),
     "tdg_write_outfile": (C.c_int, [C.c_char_p, C.c_double, _f64p, _f64p, _f64p]),
+    "tdg_phonon_frequencies": (C.c_int, [C.c_char_p, C.c_int32, _f64p, _f64p, _f64p]),
 }
 
 _LIB = None

@@ -29,6 +29,20 @@ const std::map<std::string, double> &atomic_weights() {
     return w;
 }
 
+// Natural isotope distributions (abundance, mass in amu; the IUPAC/NIST isotopic
+// compositions) of the elements of the reference's test cells. As in the reference
+// (type_crystalstructure.f90:645-656, 1505-1519), an atom without infile.isotopes takes
+// the mean mass of its element's distribution and the mass-disorder parameter
+// sum_i c_i (m_i - <m>)^2 / <m>^2 that isotope scattering uses. Elements outside this
+// table fall back to the standard atomic weight with no disorder.
+const std::map<std::string, std::vector<std::pair<double, double>>> &natural_isotopes() {
+    static const std::map<std::string, std::vector<std::pair<double, double>>> t = {
+        {"O", {{0.99757, 15.99491461956}, {0.00038, 16.9991317}, {0.00205, 17.999161}}},
+        {"Mg", {{0.7899, 23.9850417}, {0.1000, 24.98583692}, {0.1101, 25.982592929}}},
+    };
+    return t;
+}
+
 std::vector<std::string> split_ws(const std::string &s) {
     std::istringstream is(s);
     std::vector<std::string> out;
@@ -112,6 +126,20 @@ int read_poscar(const std::string &path, Crystal &c) {
     c.disorder.assign(c.na, 0.0);
     for (int a = 0; a < c.na; ++a) {
         c.rcart[a] = c.frac_to_cart(c.frac[a]);
+        const auto &nat = natural_isotopes();
+        auto nt = nat.find(c.symbols[c.species[a]]);
+        if (nt != nat.end()) {
+            double mean = 0, g = 0;
+            for (const auto &ci : nt->second) mean += ci.first * ci.second * kAmuToEmu;
+            for (const auto &ci : nt->second) {
+                const double dm = ci.second * kAmuToEmu - mean;
+                g += ci.first * dm * dm;
+            }
+            c.mass[a] = mean;
+            c.invsqrtmass[a] = 1.0 / std::sqrt(mean);
+            c.disorder[a] = g / (mean * mean);
+            continue;
+        }
         const auto &w = atomic_weights();
         auto it = w.find(c.symbols[c.species[a]]);
         if (it != w.end()) {
@@ -263,8 +291,107 @@ int read_fc2(const std::string &path, const Crystal &c, FC2 &fc) {
             fc.pairs.push_back(p);
         }
     }
-    // Polar correction flag; the long-range block itself is not used by this build.
+    // Polar block (type_forceconstant_secondorder_io.f90:172-196).
+    fc.polar = 0;
     if (first_tokens(1, v)) fc.polar = (int)v[0];
+    if (fc.polar == 0) return kOk;
+    if (fc.polar == 1 || fc.polar == 2)
+        return set_error(kErrIo, "This polar correction type is deprecated (" + path + ")");
+    if (fc.polar != 3) return set_error(kErrIo, "Undefined polar correction type in " + path);
+    for (int col = 0; col < 3; ++col) {  // eps(:, col), one line each
+        if (!first_tokens(3, v)) return set_error(kErrIo, "truncated " + path);
+        for (int r = 0; r < 3; ++r) fc.eps(r, col) = v[r];
+    }
+    if (!first_tokens(1, v)) return set_error(kErrIo, "truncated " + path);
+    fc.lambda = v[0];
+    if (!first_tokens(1, v)) return set_error(kErrIo, "truncated " + path);
+    const int nx = (int)v[0];
+    if (nx < 0) return set_error(kErrIo, "bad number of Born-charge components in " + path);
+    std::vector<double> x(nx), coeff((size_t)9 * fc.na * nx);
+    for (int i = 0; i < nx; ++i) {
+        if (!first_tokens(1, v)) return set_error(kErrIo, "truncated " + path);
+        x[i] = v[0];
+    }
+    for (int r = 0; r < 9 * fc.na; ++r) {
+        if (nx > 0 && !first_tokens(nx, v)) return set_error(kErrIo, "truncated " + path);
+        for (int i = 0; i < nx; ++i) coeff[(size_t)r * nx + i] = v[i];
+    }
+    // Zflat = coeff_Z x_Z, unflattened row by row (gottochblandat_tensors.f90:191-203).
+    fc.Z.assign((size_t)9 * fc.na, 0.0);
+    double tot[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int a = 0; a < fc.na; ++a)
+        for (int l = 0; l < 9; ++l) {
+            double zf = 0;
+            for (int i = 0; i < nx; ++i) zf += coeff[(size_t)(a * 9 + l) * nx + i] * x[i];
+            const int i = l / 3, j = l % 3;
+            fc.Z[(size_t)a * 9 + i + 3 * j] = zf;
+            tot[i + 3 * j] += zf;
+        }
+    double s = 0;
+    for (double t : tot) s += std::fabs(t);
+    if (s > kSqTol) return set_error(kErrSymmetry, "Born charges do not add up to zero");
+
+    // Reciprocal vectors of the Ewald sum. The reference fixes the radius by a root search
+    // on the Gaussian tail (lo_longrange_electrostatics.f90:392-480, tolerance 1e-20) plus
+    // the bounding sphere of the reciprocal cell; this takes every vector whose Gaussian
+    // factor exp(-|K|^2_eps / 4 lambda^2) |K|^2_eps can exceed 1e-30, plus the sum of the
+    // reciprocal basis lengths, a superset whose extra terms are below that bound.
+    std::vector<cplx> em(9);
+    for (int i = 0; i < 9; ++i) em[i] = fc.eps.a[i];
+    std::vector<double> ew;
+    std::vector<cplx> evec;
+    int st = hermitian_jacobi(3, em, ew, evec);
+    if (st) return st;
+    const double emin = std::min({ew[0], ew[1], ew[2]}), emax = std::max({ew[0], ew[1], ew[2]});
+    if (!(emin > 0) || !(fc.lambda > 0))
+        return set_error(kErrIo, "polar block needs a positive-definite dielectric tensor and lambda > 0");
+    const double inv4l2 = 1.0 / (4.0 * fc.lambda * fc.lambda);
+    double r0 = 0;
+    for (;;) {
+        r0 += 1e-3;
+        const double kk = kTwoPi * kTwoPi * r0 * r0;
+        if (std::exp(-kk * emin * inv4l2) * kk * emax < 1e-30) break;
+    }
+    double krad = r0;
+    for (int i = 0; i < 3; ++i)
+        krad += std::sqrt(c.reclat(0, i) * c.reclat(0, i) + c.reclat(1, i) * c.reclat(1, i) +
+                          c.reclat(2, i) * c.reclat(2, i));
+    int bd[3];
+    for (int i = 0; i < 3; ++i) {
+        const double al = std::sqrt(c.lat(0, i) * c.lat(0, i) + c.lat(1, i) * c.lat(1, i) + c.lat(2, i) * c.lat(2, i));
+        bd[i] = (int)std::ceil(krad * al) + 1;
+    }
+    std::vector<std::pair<double, V3>> gl;
+    for (int i = -bd[0]; i <= bd[0]; ++i)
+        for (int j = -bd[1]; j <= bd[1]; ++j)
+            for (int k = -bd[2]; k <= bd[2]; ++k) {
+                V3 f;
+                f[0] = i;
+                f[1] = j;
+                f[2] = k;
+                const V3 g = mul(c.reclat, f);
+                const double n2 = sqnorm(g);
+                if (n2 < krad * krad) gl.push_back({n2, g});
+            }
+    // Longest first, as the reference stores them.
+    std::stable_sort(gl.begin(), gl.end(), [](const auto &a, const auto &b) { return a.first > b.first; });
+    fc.G.clear();
+    for (const auto &e : gl) fc.G.push_back(e.second);
+
+    // Onsite correction: minus the row sums of the real long-range matrix at Gamma,
+    // chopped at 1e-13 (type_forceconstant_secondorder_loto.f90:76-96).
+    fc.Zonsite.assign((size_t)9 * fc.na, 0.0);
+    std::vector<cplx> dc((size_t)9 * fc.na * fc.na);
+    longrange_dm(c, fc, V3(), false, dc.data(), nullptr);
+    double im = 0;
+    for (const auto &z : dc) im += std::fabs(z.imag());
+    if (im > kSqTol * fc.na * fc.na) return set_error(kErrSymmetry, "Dynamical matrix at gamma not real.");
+    for (int a1 = 0; a1 < fc.na; ++a1)
+        for (int e = 0; e < 9; ++e) {
+            double m = 0;
+            for (int a2 = 0; a2 < fc.na; ++a2) m += dc[((size_t)a1 * fc.na + a2) * 9 + e].real();
+            fc.Zonsite[(size_t)a1 * 9 + e] = std::fabs(m) < 1e-13 ? 0.0 : -m;
+        }
     return kOk;
 }
 

@@ -55,10 +55,32 @@ struct FC2Pair {
 struct FC2 {
     int na = 0;
     std::vector<FC2Pair> pairs;
-    int polar = 0;
+    int polar = 0;                 // loto%correctiontype: 0 none, 3 reciprocal-space Ewald sum
+    M3 eps;                        // dielectric tensor
+    double lambda = 0;             // Ewald coupling parameter
+    std::vector<double> Z;         // Born charges Z(i,j,a) at a*9 + i + 3j
+    std::vector<double> Zonsite;   // onsite correction, same layout
+    std::vector<V3> G;             // reciprocal lattice vectors (1/Bohr, no 2*pi) in the Ewald sphere
 };
-// type_forceconstant_secondorder_io.f90:136-200. The polar block is read and ignored.
+// type_forceconstant_secondorder_io.f90:136-246. For polar materials (correction type 3,
+// the only one the reference accepts) it also reads the dielectric tensor, the Ewald
+// parameter and the Born charges, and sets up the long-range term
+// (type_forceconstant_secondorder_loto.f90:10-99).
 int read_fc2(const std::string &path, const Crystal &c, FC2 &fc);
+
+// Long-range dipole-dipole dynamical matrix, reciprocal-space sum only
+// (lo_longrange_electrostatics_dynmat.f90:12-360 with reconly): P(i,j,a1,a2) at
+// ((a1*na + a2)*9 + i + 3j), Hartree/Bohr^2, no masses; q Cartesian in 1/Bohr without 2*pi.
+// With pg != nullptr also its gradient with respect to 2*pi*q, direction-major.
+void longrange_dm(const Crystal &c, const FC2 &fc, const V3 &q, bool onsite, cplx *p, cplx *pg);
+// Non-analytic term at Gamma along qdir (type_forceconstant_secondorder_loto.f90:130-163),
+// same layout as longrange_dm, real.
+void nonanalytic_dm(const Crystal &c, const FC2 &fc, const V3 &qdir, double *p);
+
+// Frequencies (Hartree) at arbitrary Cartesian points q (1/Bohr, no 2*pi); at Gamma the
+// non-analytic term is taken along qdir[k] unless qdir[k] is zero
+// (type_phonon_dispersions.f90:1083-1190). omega is nq*3*na.
+int phonon_frequencies(const Crystal &c, const FC2 &fc, int nq, const V3 *q, const V3 *qdir, double *omega);
 
 struct FC3 {
     std::vector<int32_t> atoms;    // n*3, 1-based

@@ -1,5 +1,6 @@
 // Harmonic phonons on every point of the mesh: dynamical matrix and its gradient
-// (type_forceconstant_secondorder_dynamicalmatrix.f90:484-788, non-polar branch),
+// (type_forceconstant_secondorder_dynamicalmatrix.f90:484-788, with the polar
+// correction type 3 of :654-714: reciprocal-space Ewald sum and the non-analytic term),
 // Hermitian diagonalisation (:113-164), group velocities (:167-200) and the degeneracy
 // tables (type_phonon_dispersions.f90:1190-1212).
 //
@@ -75,12 +76,135 @@ int hermitian_jacobi(int n, std::vector<cplx> &a, std::vector<double> &w, std::v
 }
 
 namespace {
+inline cplx chop(const cplx &z, double tol) {
+    return cplx(std::fabs(z.real()) < tol ? 0.0 : z.real(), std::fabs(z.imag()) < tol ? 0.0 : z.imag());
+}
+}  // namespace
+
+void longrange_dm(const Crystal &c, const FC2 &fc, const V3 &q, bool onsite, cplx *p, cplx *pg) {
+    const int na = fc.na;
+    const size_t blk = (size_t)9 * na * na;
+    // Pairs a1 <= a2 with tau = r(a2) - r(a1); the reciprocal sum accumulates
+    // K K^T exp(-|K|^2_eps / 4 lambda^2) / |K|^2_eps exp(-i K.tau) over K = 2 pi (G + q).
+    std::vector<int> pa1, pa2;
+    std::vector<V3> tau;
+    for (int a1 = 0; a1 < na; ++a1)
+        for (int a2 = a1; a2 < na; ++a2) {
+            V3 t;
+            for (int d = 0; d < 3; ++d) {
+                t[d] = c.rcart[a2][d] - c.rcart[a1][d];
+                if (std::fabs(t[d]) < kSqTol) t[d] = 0.0;
+            }
+            pa1.push_back(a1);
+            pa2.push_back(a2);
+            tau.push_back(t);
+        }
+    const size_t np = tau.size();
+    std::vector<cplx> dl(np * 9, 0.0), dq(pg ? np * 27 : 0, 0.0);
+    const double inv4l2 = 1.0 / (4.0 * fc.lambda * fc.lambda);
+    for (const V3 &g : fc.G) {
+        double K[3];
+        for (int d = 0; d < 3; ++d) {
+            K[d] = (g[d] + q[d]) * kTwoPi;
+            if (std::fabs(K[d]) < kSqTol) K[d] = 0.0;
+        }
+        if (K[0] * K[0] + K[1] * K[1] + K[2] * K[2] < kSqTol * kSqTol) continue;
+        double eK[3];
+        for (int i = 0; i < 3; ++i) eK[i] = fc.eps(i, 0) * K[0] + fc.eps(i, 1) * K[1] + fc.eps(i, 2) * K[2];
+        const double knorm = K[0] * eK[0] + K[1] * eK[1] + K[2] * eK[2];
+        const double inv = 1.0 / knorm;
+        const double pchi = std::exp(-knorm * inv4l2) * inv;
+        double keps[3];  // d|K|^2_eps/dK (1/|K|^2_eps + 1/4 lambda^2): K^T eps, doubled
+        for (int i = 0; i < 3; ++i)
+            keps[i] = 2.0 * (K[0] * fc.eps(0, i) + K[1] * fc.eps(1, i) + K[2] * fc.eps(2, i)) * (inv + inv4l2);
+        for (size_t ip = 0; ip < np; ++ip) {
+            const double kr = -(K[0] * tau[ip][0] + K[1] * tau[ip][1] + K[2] * tau[ip][2]);
+            const cplx chi = pchi * cplx(std::cos(kr), std::sin(kr));
+            for (int j = 0; j < 3; ++j)
+                for (int i = 0; i < 3; ++i) dl[ip * 9 + i + 3 * j] += K[i] * K[j] * chi;
+            if (!pg) continue;
+            for (int d = 0; d < 3; ++d) {
+                const cplx v0 = cplx(-keps[d], -tau[ip][d]);  // i*(-tau_d) - keps_d
+                for (int j = 0; j < 3; ++j)
+                    for (int i = 0; i < 3; ++i) {
+                        const double dkk = (i == d ? K[j] : 0.0) + (j == d ? K[i] : 0.0);
+                        dq[(ip * 3 + d) * 9 + i + 3 * j] += (K[i] * K[j] * v0 + dkk) * chi;
+                    }
+            }
+        }
+    }
+    const double f0 = 4.0 * kPi / c.volume;
+    // Hermitian completion of the pair blocks, then the Born charges on both sides.
+    std::vector<cplx> d0(blk), g0(pg ? 3 * blk : 0);
+    for (size_t ip = 0; ip < np; ++ip) {
+        const int a1 = pa1[ip], a2 = pa2[ip];
+        for (int j = 0; j < 3; ++j)
+            for (int i = 0; i < 3; ++i) {
+                const cplx v = dl[ip * 9 + i + 3 * j] * f0;
+                d0[((size_t)a1 * na + a2) * 9 + i + 3 * j] = v;
+                if (a1 != a2) d0[((size_t)a2 * na + a1) * 9 + j + 3 * i] = std::conj(v);
+                if (!pg) continue;
+                for (int d = 0; d < 3; ++d) {
+                    const cplx w = dq[(ip * 3 + d) * 9 + i + 3 * j] * f0;
+                    g0[d * blk + ((size_t)a1 * na + a2) * 9 + i + 3 * j] = w;
+                    if (a1 != a2) g0[d * blk + ((size_t)a2 * na + a1) * 9 + j + 3 * i] = std::conj(w);
+                }
+            }
+    }
+    const double *Z = fc.Z.data();
+    auto zz = [&](const cplx *src, cplx *dst, int a1, int a2) {
+        const cplx *s = src + ((size_t)a1 * na + a2) * 9;
+        for (int j = 0; j < 3; ++j)
+            for (int i = 0; i < 3; ++i) {
+                cplx acc = 0;
+                for (int jj = 0; jj < 3; ++jj)
+                    for (int ii = 0; ii < 3; ++ii)
+                        acc += Z[(size_t)a1 * 9 + i + 3 * ii] * Z[(size_t)a2 * 9 + j + 3 * jj] * s[ii + 3 * jj];
+                dst[((size_t)a1 * na + a2) * 9 + i + 3 * j] = acc;
+            }
+    };
+    for (int a1 = 0; a1 < na; ++a1)
+        for (int a2 = 0; a2 < na; ++a2) {
+            zz(d0.data(), p, a1, a2);
+            if (pg)
+                for (int d = 0; d < 3; ++d) zz(g0.data() + d * blk, pg + d * blk, a1, a2);
+        }
+    if (onsite)
+        for (int a = 0; a < na; ++a)
+            for (int e = 0; e < 9; ++e) p[((size_t)a * na + a) * 9 + e] += fc.Zonsite[(size_t)a * 9 + e];
+    for (size_t e = 0; e < blk; ++e) p[e] = chop(p[e], kSqTol);
+}
+
+void nonanalytic_dm(const Crystal &c, const FC2 &fc, const V3 &qdir, double *p) {
+    const int na = fc.na;
+    const double nq = std::sqrt(sqnorm(qdir));
+    double u[3] = {qdir[0] / nq, qdir[1] / nq, qdir[2] / nq};
+    double qeq = 0;
+    for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i) qeq += u[i] * fc.eps(i, j) * u[j];
+    const double f0 = (1.0 / qeq) * 4.0 * kPi / c.volume;
+    std::vector<double> zq((size_t)3 * na);  // zq(i, a) = sum_k u_k Z(i,k,a)
+    for (int a = 0; a < na; ++a)
+        for (int i = 0; i < 3; ++i) {
+            double s = 0;
+            for (int k = 0; k < 3; ++k) s += u[k] * fc.Z[(size_t)a * 9 + i + 3 * k];
+            zq[(size_t)a * 3 + i] = s;
+        }
+    for (int a1 = 0; a1 < na; ++a1)
+        for (int a2 = 0; a2 < na; ++a2)
+            for (int j = 0; j < 3; ++j)
+                for (int i = 0; i < 3; ++i)
+                    p[((size_t)a1 * na + a2) * 9 + i + 3 * j] = zq[(size_t)a1 * 3 + i] * zq[(size_t)a2 * 3 + j] * f0;
+}
+
+namespace {
 
 double negsqrt(double x) { return x >= 0 ? std::sqrt(x) : -std::sqrt(-x); }
 
 // D((a2,j),(a1,i)) = sum_pairs exp(i q.R) m(i,j) / sqrt(m1 m2) and its q gradient G, q
-// with 2*pi; D and G column-major, G direction-major.
-void dyn_matrix(const Crystal &c, const FC2 &fc, const V3 &qr, int nb, cplx *D, cplx *G) {
+// with 2*pi; D and G column-major, G direction-major. Polar force constants add the
+// long-range matrix and, at Gamma with qdir given, the non-analytic term along qdir.
+void dyn_matrix(const Crystal &c, const FC2 &fc, const V3 &qr, const V3 *qdir, int nb, cplx *D, cplx *G) {
     V3 qv;
     for (int d = 0; d < 3; ++d) {
         qv[d] = qr[d] * kTwoPi;
@@ -100,12 +224,33 @@ void dyn_matrix(const Crystal &c, const FC2 &fc, const V3 &qr, int nb, cplx *D, 
                 for (int d = 0; d < 3; ++d) G[(size_t)d * nb * nb + ii + (size_t)nb * jj] += cplx(0, p.lv[d]) * val;
             }
     }
+    if (fc.polar != 3) return;
+    const int na = fc.na;
+    const size_t blk = (size_t)9 * na * na;
+    std::vector<cplx> P(blk), PG(3 * blk);
+    longrange_dm(c, fc, qr, true, P.data(), PG.data());
+    std::vector<double> NA;
+    if (qdir && sqnorm(qr) < kSqTol && sqnorm(*qdir) > kSqTol) {
+        NA.resize(blk);
+        nonanalytic_dm(c, fc, *qdir, NA.data());
+    }
+    for (int a1 = 0; a1 < na; ++a1)
+        for (int a2 = 0; a2 < na; ++a2) {
+            const double ms = c.invsqrtmass[a1] * c.invsqrtmass[a2];
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) {
+                    const size_t e = ((size_t)a1 * na + a2) * 9 + i + 3 * j;
+                    const size_t at = (size_t)(a2 * 3 + j) + (size_t)nb * (a1 * 3 + i);
+                    D[at] += (P[e] + (NA.empty() ? 0.0 : NA[e])) * ms;
+                    for (int d = 0; d < 3; ++d) G[(size_t)d * nb * nb + at] += PG[d * blk + e] * ms;
+                }
+        }
 }
 
-int solve_point(const Crystal &c, const FC2 &fc, const V3 &qr, int nb, double *omega, double *egv,
+int solve_point(const Crystal &c, const FC2 &fc, const V3 &qr, const V3 *qdir, int nb, double *omega, double *egv,
                 double *vel) {
     std::vector<cplx> D((size_t)nb * nb), G((size_t)3 * nb * nb);
-    dyn_matrix(c, fc, qr, nb, D.data(), G.data());
+    dyn_matrix(c, fc, qr, qdir, nb, D.data(), G.data());
     // Hermitise against rounding before diagonalising.
     for (int i = 0; i < nb; ++i)
         for (int j = i; j < nb; ++j) {
@@ -203,10 +348,25 @@ int solve_point(const Crystal &c, const FC2 &fc, const V3 &qr, int nb, double *o
 
 void dyn_gradient(const Crystal &c, const FC2 &fc, const V3 &qr, int nb, cplx *g) {
     std::vector<cplx> D((size_t)nb * nb);
-    dyn_matrix(c, fc, qr, nb, D.data(), g);
+    dyn_matrix(c, fc, qr, nullptr, nb, D.data(), g);
+}
+
+int phonon_frequencies(const Crystal &c, const FC2 &fc, int nq, const V3 *q, const V3 *qdir, double *omega) {
+    const int nb = 3 * c.na;
+    std::vector<int> status(nq, kOk);
+    parallel_for(nq, [&](int64_t k) {
+        std::vector<double> egv((size_t)nb * nb * 2), vel((size_t)nb * 3);
+        status[k] = solve_point(c, fc, q[k], qdir ? &qdir[k] : nullptr, nb, omega + (size_t)k * nb, egv.data(),
+                                vel.data());
+    });
+    for (int st : status)
+        if (st) return st;
+    return kOk;
 }
 
 int build_phonons(const Crystal &c, const FC2 &fc, const QMesh &qp, Phonons &ph) {
+    V3 kDefaultDir;
+    kDefaultDir[0] = 1.0;
     const int nb = 3 * c.na;
     const int np = qp.n_full;
     ph.n_mode = nb;
@@ -222,7 +382,9 @@ int build_phonons(const Crystal &c, const FC2 &fc, const QMesh &qp, Phonons &ph)
     for (unsigned t = 0; t < nth; ++t)
         th.emplace_back([&, t]() {
             for (int q = (int)t; q < np; q += (int)nth) {
-                int st = solve_point(c, fc, qp.q_full[q], nb, &ph.omega[(size_t)q * nb],
+                // The mesh takes the default direction [1,0,0] at Gamma
+                // (type_phonon_dispersions.f90:1099, 1148).
+                int st = solve_point(c, fc, qp.q_full[q], &kDefaultDir, nb, &ph.omega[(size_t)q * nb],
                                      &ph.egv[(size_t)q * nb * nb * 2], &ph.vel[(size_t)q * nb * 3]);
                 if (st) {
                     status[t] = st;

@@ -296,6 +296,29 @@ std::string fortran_e(double x, int w, int d) {
 }
 }  // namespace
 
+extern "C" int tdg_phonon_frequencies(const char *dir, int32_t nq, const double *q, const double *qdir,
+                                      double *omega) {
+    using namespace tdg;
+    if (!dir || nq < 0 || (nq > 0 && (!q || !omega)))
+        return set_error(kErrParam, "tdg_phonon_frequencies: null argument");
+    const std::string d = std::string(dir) + "/";
+    Crystal c;
+    int st = read_poscar(d + "infile.ucposcar", c);
+    if (st) return st;
+    for (int a = 0; a < c.na; ++a)
+        if (!(c.mass[a] > 0)) return set_error(kErrParam, "unknown element mass for atom " + std::to_string(a + 1));
+    FC2 fc2;
+    st = read_fc2(d + "infile.forceconstant", c, fc2);
+    if (st) return st;
+    std::vector<V3> qv(nq), dv(nq);
+    for (int k = 0; k < nq; ++k)
+        for (int x = 0; x < 3; ++x) {
+            qv[k][x] = q[3 * k + x];
+            dv[k][x] = qdir ? qdir[3 * k + x] : (x == 0 ? 1.0 : 0.0);
+        }
+    return phonon_frequencies(c, fc2, nq, qv.data(), dv.data(), omega);
+}
+
 extern "C" int tdg_write_outfile(const char *dir, double temperature, const double *ksma, const double *kiter,
                                  const double *koff) {
     using namespace tdg;

@@ -405,6 +405,27 @@ def write_outfile(directory, temperature, kappa_sma, kappa_iter, kappa_offdiag=N
     return Path(directory) / "outfile.thermal_conductivity"
 
 
+def phonon_frequencies(directory, q, qdir=None) -> np.ndarray:
+    """Harmonic frequencies in Hartree, ascending, at Cartesian points q (1/Bohr, no 2*pi),
+    from infile.ucposcar and infile.forceconstant in `directory`, polar force constants
+    included (type_phonon_dispersions.f90:1083-1190). At Gamma the non-analytic term is
+    taken along qdir (default [1,0,0]; a zero row leaves it out). Host-side computation."""
+    L = N.lib()
+    qa = np.ascontiguousarray(np.asarray(q, dtype=np.float64).reshape(-1, 3))
+    da = None if qdir is None else np.ascontiguousarray(np.asarray(qdir, dtype=np.float64).reshape(-1, 3))
+    if da is not None and da.shape != qa.shape:
+        raise ValueError("qdir must have the shape of q")
+    nq = qa.shape[0]
+    # The mode count is known only after reading the cell: 3 * number of atoms.
+    first = Path(directory, "infile.ucposcar").read_text().split("\n")
+    na = sum(int(x) for x in first[6].split())
+    om = np.zeros((nq, 3 * na))
+    N.check(L.tdg_phonon_frequencies(str(directory).encode(), nq, N.ptr(qa, C.c_double),
+                                     None if da is None else N.ptr(da, C.c_double), N.ptr(om, C.c_double)),
+            "tdg_phonon_frequencies")
+    return om
+
+
 def release_cached_memory(device: int = 0) -> None:
     """Return the device memory the library keeps for reuse after contexts close."""
     N.check(N.lib().tdg_release_cached_memory(int(device)), "tdg_release_cached_memory")

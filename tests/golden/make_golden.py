@@ -8,6 +8,7 @@ Copied data files (the reference's own test inputs and expected output, unmodifi
   mgo/infile.forceconstant               tests/infiles/infile.forceconstant        (polar MgO FC2)
   mgo/infile.forceconstant_thirdorder    tests/infiles/infile.forceconstant_thirdorder
   mgo/outfile.thermal_conductivity.ref   tests/thermal_conductivity/reference/outfile.thermal_conductivity
+  mgo/outfile.dispersion_relations.ref   tests/phonon_dispersion_relations/reference/outfile.dispersion_relations
 A SHA-256 manifest of the sources is written to mgo/MANIFEST.
 """
 import hashlib
@@ -20,6 +21,7 @@ FILES = {
     "infile.forceconstant": "tests/infiles/infile.forceconstant",
     "infile.forceconstant_thirdorder": "tests/infiles/infile.forceconstant_thirdorder",
     "outfile.thermal_conductivity.ref": "tests/thermal_conductivity/reference/outfile.thermal_conductivity",
+    "outfile.dispersion_relations.ref": "tests/phonon_dispersion_relations/reference/outfile.dispersion_relations",
 }
 
 

@@ -320,8 +320,9 @@ def test_transfer_counter_counts_the_copies(configs):
 
 
 def test_fp64_reference_mgo_fixture(built):
-    """The reference's own MgO inputs (tests/infiles of the reference; polar long-range
-    term not applied) through both paths, 5x5x5 mesh as in the reference's test."""
+    """The reference's own MgO inputs (tests/infiles of the reference: polar force
+    constants with the long-range Ewald term, natural-isotope masses and disorder)
+    through both paths, 5x5x5 mesh as in the reference's test."""
     from pathlib import Path
 
     prob = Problem.load(Path(__file__).parent / "golden" / "mgo", (5, 5, 5))
