@@ -181,6 +181,17 @@ void tdg_destroy(tdg_ctx *ctx);
  */
 int tdg_release_cached_memory(int device);
 
+/* Bytes of that pool in use by live buffers and reserved from the driver (diagnostic, no
+ * reference counterpart). */
+int tdg_pool_usage(int device, uint64_t *used, uint64_t *reserved);
+
+/* Natural isotope composition of an element (replaces naturaldistribution,
+ * src/libolle/type_crystalstructure.f90:1522): returns the number of isotopes and fills
+ * abundance[] and mass[] (amu) when cap allows, -count when cap is too small, 0 when the
+ * library has no table entry for the symbol (such an atom needs infile.isotopes for
+ * isotope scattering). */
+int tdg_natural_isotopes(const char *symbol, int32_t cap, double *abundance, double *mass);
+
 /*
  * CUDA graphs (no reference counterpart): the three-phonon kernels of tdg_scattering (the
  * fused kernel, or the launches of the large-cell batches) run directly on the first call
@@ -270,9 +281,13 @@ int tdg_triplets(tdg_ctx *ctx, int32_t q1, const int32_t *sample, int64_t n, int
  * cannot call cudaMalloc at the time of the call. Its device scratch is one fixed
  * file-scope array (about 4.3 MiB per device) instead of per-call allocations, so it
  * calls no cudaMalloc, cudaFree or other allocating routine.
- * Limits: n <= 32768 q-points, and at most 131072 equivalent triplets in the result
- * (always met on meshes of up to 131072 points); beyond either, TDG_ERR_PARAM with a
- * message naming the limit, before any device work on the result.
+ * Limits: n <= 32768 q-points, and at most 131072 equivalent triplets in the result.
+ * A sample without repeated q-points meets the second limit on every mesh of up to 131072
+ * points: the equivalent triplets of distinct irreducible triplets are distinct pairs
+ * (q2', q3'), and q3' follows from q2'. Repeated q-points (Monte Carlo samples may repeat
+ * one) add their images once per repeat, so in general the count is bounded only by n times
+ * the largest image count. Beyond either limit: TDG_ERR_PARAM with a message naming the
+ * limit, before any device work on the result.
  * The first call on each device looks the array up (cudaGetSymbolAddress, which loads the
  * module); make that first call before any stream capture. Only the status word of the
  * scratch must start at zero, and each call clears it itself. All calls on one device

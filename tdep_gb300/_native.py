@@ -122,6 +122,8 @@ SIGNATURES = {
     "tdg_transfer_bytes": (C.c_int, [C.c_void_p, _i64p, _i64p]),
     "tdg_kappa_offdiag": (C.c_int, [C.c_void_p, C.POINTER(TdgOpts), _f64p]),
     "tdg_release_cached_memory": (C.c_int, [C.c_int]),
+    "tdg_pool_usage": (C.c_int, [C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "tdg_natural_isotopes": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "tdg_autotune_load": (C.c_int, [C.c_char_p]),
     "tdg_autotune_save": (C.c_int, [C.c_char_p]),
     "tdg_autotune_report": (C.c_int, [C.c_char_p, C.c_int64, _i64p]),

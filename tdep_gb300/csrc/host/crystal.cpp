@@ -3,6 +3,9 @@
 
 #include <algorithm>
 #include <fstream>
+#include <cmath>
+#include <cstring>
+#include <limits>
 #include <map>
 #include <sstream>
 
@@ -29,16 +32,73 @@ const std::map<std::string, double> &atomic_weights() {
     return w;
 }
 
-// Natural isotope distributions (abundance, mass in amu; the IUPAC/NIST isotopic
-// compositions) of the elements of the reference's test cells. As in the reference
-// (type_crystalstructure.f90:645-656, 1505-1519), an atom without infile.isotopes takes
-// the mean mass of its element's distribution and the mass-disorder parameter
-// sum_i c_i (m_i - <m>)^2 / <m>^2 that isotope scattering uses. Elements outside this
-// table fall back to the standard atomic weight with no disorder.
-const std::map<std::string, std::vector<std::pair<double, double>>> &natural_isotopes() {
-    static const std::map<std::string, std::vector<std::pair<double, double>>> t = {
+// Natural isotope distributions (abundance, mass in amu): the NIST isotopic compositions
+// and relative atomic masses, the public data the reference also tabulates for every
+// element (type_crystalstructure.f90:1522, naturaldistribution). As in the reference
+// (type_crystalstructure.f90:645-656, 1505-1519), an atom without infile.isotopes takes the
+// mean mass of its element's distribution and the mass-disorder parameter
+// sum_i c_i (m_i - <m>)^2 / <m>^2 that isotope scattering uses. An element outside this
+// table gets its standard atomic weight and an unknown disorder (NaN): isotope scattering
+// then stops with an error instead of silently using zero (give infile.isotopes or switch
+// isotope scattering off).
+using IsoTable = std::map<std::string, std::vector<std::pair<double, double>>>;
+const IsoTable &natural_isotopes() {
+    static const IsoTable t = {
+        {"H", {{0.999885, 1.00782503207}, {0.000115, 2.0141017778}}},
+        {"Li", {{0.0759, 6.015122795}, {0.9241, 7.01600455}}},
+        {"Be", {{1.0, 9.0121822}}},
+        {"B", {{0.199, 10.0129370}, {0.801, 11.0093054}}},
+        {"C", {{0.9893, 12.0}, {0.0107, 13.0033548378}}},
+        {"N", {{0.99636, 14.0030740048}, {0.00364, 15.0001088982}}},
         {"O", {{0.99757, 15.99491461956}, {0.00038, 16.9991317}, {0.00205, 17.999161}}},
+        {"F", {{1.0, 18.99840322}}},
+        {"Na", {{1.0, 22.9897692809}}},
         {"Mg", {{0.7899, 23.9850417}, {0.1000, 24.98583692}, {0.1101, 25.982592929}}},
+        {"Al", {{1.0, 26.98153863}}},
+        {"Si", {{0.92223, 27.9769265325}, {0.04685, 28.976494700}, {0.03092, 29.97377017}}},
+        {"P", {{1.0, 30.97376163}}},
+        {"S", {{0.9499, 31.97207100}, {0.0075, 32.97145876}, {0.0425, 33.96786690}, {0.0001, 35.96708076}}},
+        {"Cl", {{0.7576, 34.96885268}, {0.2424, 36.96590259}}},
+        {"K", {{0.932581, 38.96370668}, {0.000117, 39.96399848}, {0.067302, 40.96182576}}},
+        {"Ca", {{0.96941, 39.96259098}, {0.00647, 41.95861801}, {0.00135, 42.9587666}, {0.02086, 43.9554818},
+                {0.00004, 45.9536926}, {0.00187, 47.952534}}},
+        {"Sc", {{1.0, 44.9559119}}},
+        {"Ti", {{0.0825, 45.9526316}, {0.0744, 46.9517631}, {0.7372, 47.9479463}, {0.0541, 48.9478700},
+                {0.0518, 49.9447912}}},
+        {"V", {{0.00250, 49.9471585}, {0.99750, 50.9439595}}},
+        {"Cr", {{0.04345, 49.9460442}, {0.83789, 51.9405075}, {0.09501, 52.9406494}, {0.02365, 53.9388804}}},
+        {"Mn", {{1.0, 54.9380451}}},
+        {"Fe", {{0.05845, 53.9396105}, {0.91754, 55.9349375}, {0.02119, 56.9353940}, {0.00282, 57.9332756}}},
+        {"Co", {{1.0, 58.9331950}}},
+        {"Ni", {{0.680769, 57.9353429}, {0.262231, 59.9307864}, {0.011399, 60.9310560}, {0.036345, 61.9283451},
+                {0.009256, 63.9279660}}},
+        {"Cu", {{0.6915, 62.9295975}, {0.3085, 64.9277895}}},
+        {"Zn", {{0.48268, 63.9291422}, {0.27975, 65.9260334}, {0.04102, 66.9271273}, {0.19024, 67.9248442},
+                {0.00631, 69.9253193}}},
+        {"Ga", {{0.60108, 68.9255736}, {0.39892, 70.9247013}}},
+        {"Ge", {{0.2038, 69.9242474}, {0.2731, 71.9220758}, {0.0776, 72.9234589}, {0.3672, 73.9211778},
+                {0.0783, 75.9214026}}},
+        {"As", {{1.0, 74.9215965}}},
+        {"Se", {{0.0089, 73.9224764}, {0.0937, 75.9192136}, {0.0763, 76.9199140}, {0.2377, 77.9173091},
+                {0.4961, 79.9165213}, {0.0873, 81.9166994}}},
+        {"Br", {{0.5069, 78.9183371}, {0.4931, 80.9162906}}},
+        {"Sr", {{0.0056, 83.913425}, {0.0986, 85.9092602}, {0.0700, 86.9088771}, {0.8258, 87.9056121}}},
+        {"Y", {{1.0, 88.9058483}}},
+        {"Zr", {{0.5145, 89.9047044}, {0.1122, 90.9056458}, {0.1715, 91.9050408}, {0.1738, 93.9063152},
+                {0.0280, 95.9082734}}},
+        {"Nb", {{1.0, 92.9063781}}},
+        {"Ag", {{0.51839, 106.905097}, {0.48161, 108.904752}}},
+        {"In", {{0.0429, 112.904058}, {0.9571, 114.903878}}},
+        {"Sb", {{0.5721, 120.9038157}, {0.4279, 122.9042140}}},
+        {"Te", {{0.0009, 119.904020}, {0.0255, 121.9030439}, {0.0089, 122.9042700}, {0.0474, 123.9028179},
+                {0.0707, 124.9044307}, {0.1884, 125.9033117}, {0.3174, 127.9044631}, {0.3408, 129.9062244}}},
+        {"I", {{1.0, 126.904473}}},
+        {"Cs", {{1.0, 132.905451933}}},
+        {"Ba", {{0.00106, 129.9063208}, {0.00101, 131.9050613}, {0.02417, 133.9045084}, {0.06592, 134.9056886},
+                {0.07854, 135.9045759}, {0.11232, 136.9058274}, {0.71698, 137.9052472}}},
+        {"Au", {{1.0, 196.9665687}}},
+        {"Pb", {{0.014, 203.9730436}, {0.241, 205.9744653}, {0.221, 206.9758969}, {0.524, 207.9766521}}},
+        {"Bi", {{1.0, 208.9803987}}},
     };
     return t;
 }
@@ -146,6 +206,8 @@ int read_poscar(const std::string &path, Crystal &c) {
             c.mass[a] = it->second * kAmuToEmu;
             c.invsqrtmass[a] = 1.0 / std::sqrt(c.mass[a]);
         }
+        // no natural distribution: the disorder is unknown until infile.isotopes gives it
+        c.disorder[a] = std::numeric_limits<double>::quiet_NaN();
     }
     return kOk;
 }
@@ -558,3 +620,17 @@ int op_atom_maps(const Crystal &c, std::vector<int32_t> &fmap, std::vector<doubl
 }
 
 }  // namespace tdg
+
+extern "C" int tdg_natural_isotopes(const char *symbol, int32_t cap, double *abundance, double *mass) {
+    if (!symbol) return tdg::set_error(tdg::kErrParam, "tdg_natural_isotopes: null symbol");
+    const auto &t = tdg::natural_isotopes();
+    auto it = t.find(symbol);
+    if (it == t.end()) return 0;
+    const int32_t n = (int32_t)it->second.size();
+    if (cap < n || !abundance || !mass) return -n;
+    for (int32_t i = 0; i < n; ++i) {
+        abundance[i] = it->second[i].first;
+        mass[i] = it->second[i].second;
+    }
+    return n;
+}

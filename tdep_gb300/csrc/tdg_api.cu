@@ -432,6 +432,18 @@ extern "C" int tdg_release_cached_memory(int device) {
     return kOk;
 }
 
+extern "C" int tdg_pool_usage(int device, uint64_t *used, uint64_t *reserved) {
+    if (!used || !reserved) return set_error(kErrParam, "tdg_pool_usage: null argument");
+    cudaMemPool_t pool = device_pool(device);
+    if (!pool) return set_error(kErrParam, "tdg_pool_usage: no pool for this device");
+    uint64_t u = 0, r = 0;
+    CUDA_TRY(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &u));
+    CUDA_TRY(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &r));
+    *used = (uint64_t)u;
+    *reserved = (uint64_t)r;
+    return kOk;
+}
+
 extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
     if (!out) return set_error(kErrParam, "tdg_create: null output");
     *out = nullptr;
@@ -873,6 +885,12 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
                                         "which needs precision TDG_PREC_MIXED");
         if (ln_kp(n) > 256) return set_error(kErrParam, "the tensor-core contraction supports up to 128 modes");
     }
+    if (o->isotope)
+        for (int a = 0; a < c->na; ++a)
+            if (std::isnan(c->disorder[a]))
+                return set_error(kErrParam, "isotope scattering: atom " + std::to_string(a + 1) +
+                                                " has no natural isotope distribution in the library's table; "
+                                                "give infile.isotopes or switch isotope scattering off");
     if (o->fourthorder) {
         st = check_list("four-phonon sample", nr, ql->ptr4, ql->list4a, N);
         if (st) return st;

@@ -4,11 +4,13 @@
 // allocating routine; the array is created with the module and found once per device with
 // cudaGetSymbolAddress.
 //
-// Limits (checked on the host before any device work): a sample of at most
+// Limits (checked on the host before any device work on the result): a sample of at most
 // kMaxSample = 32768 q-points, and at most kMaxPairs = 131072 equivalent triplets in the
-// result (the equivalent triplets of distinct irreducible triplets are distinct mesh
-// pairs, so any mesh of up to 131072 points stays within it). Scratch: about 4.3 MiB per
-// device.
+// result. A sample without repeated q-points on a mesh of up to 131072 points always stays
+// within the second limit (the equivalent triplets of distinct irreducible triplets are
+// distinct pairs (q2', q3'), and q3' follows from q2'); a repeated q-point adds its images
+// once per repeat, so heavily repeated samples can exceed it and get TDG_ERR_PARAM from
+// the check on the count pass. Scratch: about 4.3 MiB per device.
 //
 // Only the status word must start at zero; every call clears it before the count pass.
 // Every other region is written in full before it is read. All calls on one device share

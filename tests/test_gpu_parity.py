@@ -65,7 +65,7 @@ def _xi_flips(xi, ref_xi, ratio_check=True, max_frac=1e-4):
     here, where the phases are exact roots of unity; +-1e-17 relative in the reference's
     cos/sin), which changes how many images enter the average of that orbit. Such an entry
     then differs by the ratio of the two image counts, a fraction p/q with p, q <= 2 * 96.
-    Returns the number of differing entries after checking that they are rare and, when Xi
+    Returns the mask of differing entries after checking that they are rare and, when Xi
     holds a single symmetrised order (ratio_check), that every one of them is such a flip;
     with two orders or isotope terms in the same entry the ratio is not a fraction."""
     from fractions import Fraction
@@ -79,13 +79,15 @@ def _xi_flips(xi, ref_xi, ratio_check=True, max_frac=1e-4):
         r = a / b
         f = Fraction(r).limit_denominator(192)
         assert f.numerator <= 192 and abs(r - float(f)) <= 1e-6 * abs(r), f"Xi entry ratio {r} is not an image-count flip"
-    return nbad
+    return bad
 
 
 def _compare(prob, opts, lists, lw_rtol=LW_RTOL, kappa_rtol=KAPPA_RTOL, check_xi=True, xi_max_frac=1e-4):
     """GPU path against the oracle. Linewidths and kappa_sma do not depend on Xi and keep
     the tight bars. kappa_iter keeps KAPPA_RTOL when Xi agrees entry by entry; when
-    _xi_flips found image-count flips, kappa_iter moves with them and the bar is 1e-3."""
+    _xi_flips found image-count flips, kappa_iter moves with them and the bar is 1e-3.
+    Returns the linewidths, kappa_iter, the oracle's results and the mask of differing Xi
+    entries (None without the Xi check)."""
     sr = ScatteringRates(prob)
     lw = sr.generate(opts, lists)
     xi = sr.Xi if check_xi else None
@@ -98,13 +100,14 @@ def _compare(prob, opts, lists, lw_rtol=LW_RTOL, kappa_rtol=KAPPA_RTOL, check_xi
     np.testing.assert_allclose(lw, ref["linewidth"], rtol=lw_rtol, atol=1e-14 * np.abs(ref["linewidth"]).max())
     np.testing.assert_allclose(ks, ref["kappa_sma"], rtol=kappa_rtol, atol=kappa_rtol * np.abs(ref["kappa_sma"]).max())
     single = int(bool(opts.thirdorder)) + int(bool(opts.fourthorder)) == 1 and not opts.isotopescattering
-    flips = _xi_flips(xi, ref["xi"], ratio_check=single, max_frac=xi_max_frac) if check_xi else 0
+    bad = _xi_flips(xi, ref["xi"], ratio_check=single, max_frac=xi_max_frac) if check_xi else None
+    flips = int(bad.sum()) if bad is not None else 0
     krt = kappa_rtol if flips == 0 else max(kappa_rtol, 1e-3)
     np.testing.assert_allclose(ki, ref["kappa_iter"], rtol=krt, atol=krt * np.abs(ref["kappa_iter"]).max())
     if flips == 0:
         assert sr.n_iter == ref["n_iter"]
     sr.close()
-    return lw, ki, ref
+    return lw, ki, ref, bad
 
 
 @pytest.mark.parametrize("name,grid", [("fcc", (8, 8, 8)), ("rocksalt", (6, 6, 6)), ("perovskite", (4, 4, 4))])
@@ -329,12 +332,16 @@ def test_fp64_reference_mgo_fixture(built):
     # The polar eigenvectors have irrational components, so more od_terms sums that are
     # analytically zero round to either sign than in the non-polar cells (about 1e-3 of
     # the Xi entries). Without isotope terms every differing entry must be shown to be
-    # such an image-count flip (ratio p/q); with them, linewidths and kappa_SMA keep the
-    # tight bars and the differing fraction stays as rare.
+    # such an image-count flip (ratio p/q). With them the ratio is not a fraction, so the
+    # isotope-on run (same seed, hence the same samples) must differ only at positions where
+    # the isotope-off run was shown to flip: the isotope terms are added outside the
+    # od_terms > 0 filter and cannot create a flip of their own.
     opts0 = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=42)
-    _compare(prob, opts0, QLists.monte_carlo(prob, opts0), xi_max_frac=2e-3)
+    bad0 = _compare(prob, opts0, QLists.monte_carlo(prob, opts0), xi_max_frac=2e-3)[3]
     opts = Options(temperature=300.0, integrationtype=2, isotopescattering=True, seed=42)
-    _compare(prob, opts, QLists.monte_carlo(prob, opts), xi_max_frac=2e-3)
+    bad1 = _compare(prob, opts, QLists.monte_carlo(prob, opts), xi_max_frac=2e-3)[3]
+    extra = bad1 & ~bad0
+    assert not extra.any(), f"{int(extra.sum())} Xi entries differ with isotope terms that were not flips without them"
 
 
 def test_driver_matches_api(configs, tmp_path):

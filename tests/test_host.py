@@ -137,3 +137,51 @@ def test_full_grid_sample_is_the_mesh_in_order(fcc8):
     a = QLists.monte_carlo(fcc8, Options(seed=3))
     for r in range(a.n_row):
         assert np.array_equal(a.list3[a.ptr3[r]:a.ptr3[r + 1]], np.arange(1, fcc8.n_full + 1))
+
+
+def test_natural_isotope_table_matches_the_reference():
+    """Every element of the library's natural-isotope table (abundances and isotope masses)
+    against the reference's own table, extracted into tests/golden/isotopes.json by
+    tests/golden/make_isotopes.py; the elements of the synthetic cells and the reference's
+    MgO fixture must be there."""
+    import ctypes as C
+    import json
+
+    from tdep_gb300 import _native as N
+
+    ref = json.loads((GOLDEN / "isotopes.json").read_text())
+    lib = N.lib()
+    lib.tdg_natural_isotopes.restype = C.c_int
+    lib.tdg_natural_isotopes.argtypes = [C.c_char_p, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    have = []
+    for sym, iso in ref.items():
+        ab = (C.c_double * 16)()
+        ms = (C.c_double * 16)()
+        n = lib.tdg_natural_isotopes(sym.encode(), 16, ab, ms)
+        if n == 0:
+            continue
+        have.append(sym)
+        assert n == len(iso), sym
+        np.testing.assert_allclose(list(ab[:n]), [c for c, _ in iso], rtol=0, atol=1e-12, err_msg=sym)
+        np.testing.assert_allclose(list(ms[:n]), [m for _, m in iso], rtol=1e-10, err_msg=sym)
+    assert {"Al", "Na", "Cl", "Ti", "O", "Ba", "Mg", "Si"} <= set(have)
+    assert len(have) >= 45
+    assert lib.tdg_natural_isotopes(b"Xx", 16, None, None) == 0
+
+
+def test_unknown_isotope_disorder_is_nan(configs, tmp_path):
+    """An element without a tabulated natural distribution keeps its standard weight and
+    an unknown (NaN) disorder, so isotope scattering fails loudly instead of using zero;
+    infile.isotopes supplies it."""
+    import shutil
+
+    d = tmp_path / "hf"
+    shutil.copytree(configs["fcc"], d)
+    pos = (d / "infile.ucposcar").read_text().splitlines()
+    sym_line = next(i for i, ln in enumerate(pos) if ln.split() and ln.split()[0] == "Al")
+    pos[sym_line] = pos[sym_line].replace("Al", "Hf")
+    (d / "infile.ucposcar").write_text("\n".join(pos) + "\n")
+    prob = Problem.load(d, (4, 4, 4))
+    assert np.isnan(prob.mass_disorder).all()
+    prob = Problem.load(d, (4, 4, 4), readiso=True)  # the synthetic cells ship infile.isotopes
+    assert np.isfinite(prob.mass_disorder).all()

@@ -88,3 +88,47 @@ def test_static_rejects_and_edges(configs):
     ref, got = _both(sr, 2, full)
     np.testing.assert_array_equal(got, ref)
     sr.close()
+
+
+def test_static_repeated_sample_over_the_pair_limit(configs):
+    """A q-point sampled k times adds its equivalent triplets k times: a sample of one
+    q-point with at least 5 images, repeated 32768 times, goes over the 131072-pair limit
+    and gets the limit error; the next call is still correct."""
+    prob = Problem.load(configs["rocksalt"], (6, 6, 6))
+    sr = ScatteringRates(prob)
+    full = np.arange(1, prob.n_full + 1, dtype=np.int32)
+    trip = sr.triplets(1, full)
+    q2, _, k = max(((t[0], t[1], len(t[2])) for t in trip), key=lambda x: x[2])
+    assert k >= 5, "the Gamma row of the rocksalt mesh has q-triplets with many images"
+    rc, got = _call(sr, "tdg_triplets_static", 1, np.full(MAX_SAMPLE, q2, np.int32), cap=16)
+    assert rc == 5 and got.size == 0
+    assert b"131072" in N.lib().tdg_last_error()
+    ref, got = _both(sr, 1, full)
+    np.testing.assert_array_equal(got, ref)
+    sr.close()
+
+
+def test_static_allocates_nothing(configs):
+    """The property the entry point exists for: around a call on a warmed-up context, the
+    device's free memory and the library pool's used and reserved bytes stay the same."""
+    import torch
+
+    prob = Problem.load(configs["perovskite"], (4, 4, 4))
+    sr = ScatteringRates(prob)
+    full = np.arange(1, prob.n_full + 1, dtype=np.int32)
+    rc, first = _call(sr, "tdg_triplets_static", 2, full)  # warm-up: module and symbol lookup
+    assert rc == 0
+
+    def usage():
+        torch.cuda.synchronize()
+        used, res = C.c_uint64(), C.c_uint64()
+        N.check(N.lib().tdg_pool_usage(0, C.byref(used), C.byref(res)), "tdg_pool_usage")
+        return torch.cuda.mem_get_info(0)[0], used.value, res.value
+
+    before = usage()
+    for _ in range(3):
+        rc, got = _call(sr, "tdg_triplets_static", 2, full)
+        assert rc == 0
+        np.testing.assert_array_equal(got, first)
+    assert usage() == before
+    sr.close()
