@@ -1,9 +1,12 @@
 """Benchmark of the GB300 three-phonon scattering path.
 
-Default workload (the configuration the headline metric is quoted on): 2-atom rocksalt,
-24x24x24 Gamma-centred mesh, adaptive Gaussian smearing, T = 300 K, full q' grid (the
-reference's default -qg3ph), seeded Born-Mayer + spring force constants, mixed precision
-(FP32 pretransform and contraction, FP64 delta weights and accumulation).
+Default workload (the configuration the benchmark spec's targets are stated on): 5-atom cubic
+perovskite (15 modes), 16x16x16 Gamma-centred mesh, adaptive Gaussian smearing, T = 300 K,
+seeded per-q1 q' samples of uneven sizes (200-4000 points) in one persistent launch,
+seeded Lennard-Jones + Born-Mayer force constants, mixed precision (tensor-core or FP32
+contraction, FP64 delta weights and accumulation). The same line carries the
+three-plus-four-phonon leg, the adjoint ratio and, as a sub-record, the 2-atom rocksalt
+24x24x24 configuration.
 
 One step = one pass of the scattering path (sr%generate: triplet enumeration, fused
 pretransform/contraction/accumulation, symmetrisation) over the whole mesh.
@@ -14,6 +17,8 @@ pretransform/contraction/accumulation, symmetrisation) over the whole mesh.
           linewidths) and the kappa solve, per step
   cpu_baseline / --impl reference : the oracle's restatement of the reference on the host
           cores (OpenMP), timed on complete q1 groups of the same workload.
+  parity : the oracle's linewidths and Xi rows of those q1 groups against the GPU's FP64 and
+          mixed-precision results of the same run.
 
   python bench.py [--gpus 1] [--steps K] [--warmup W] [--impl gb300|reference] [--config NAME]
 """
@@ -161,9 +166,10 @@ def peaks():
     return 6800.0, 1900.0, "fallback"
 
 
-def cpu_sample(prob, opts, lists, budget_s=12.0, nthreads=None):
+def cpu_sample(prob, opts, lists, budget_s=12.0, nthreads=None, keep=False):
     """Time the oracle on complete q1 groups until the budget is used; returns
-    (distinct q-triplets covered, seconds, description, threads)."""
+    (distinct q-triplets covered, seconds, description, threads, rows) where rows holds the
+    oracle's (r0, r1, gamma, xi) of every block when keep is set."""
     from oracle import binding as orc
 
     nthreads = nthreads or os.cpu_count() or 1
@@ -172,7 +178,7 @@ def cpu_sample(prob, opts, lists, budget_s=12.0, nthreads=None):
     # every thread busy; each block is whole rows of whole q1 groups
     per_block = max(1, -(-nthreads // max(1, prob.n_mode)))
     start = len(q1s) // 2
-    done_trip, done_s, used = 0, 0.0, []
+    done_trip, done_s, used, kept = 0, 0.0, [], []
     for b0 in range(start, start + len(q1s), per_block):
         block = [q1s[i % len(q1s)] for i in range(b0, b0 + per_block)]
         if len(set(block)) < len(block) or any(q in used for q in block):
@@ -182,8 +188,10 @@ def cpu_sample(prob, opts, lists, budget_s=12.0, nthreads=None):
         if r1 - r0 != rows.size:
             break
         t0 = time.perf_counter()
-        orc.scattering(prob, opts, lists, nthreads=nthreads, rows=(r0, r1))
+        gamma, xi, _ = orc.scattering(prob, opts, lists, nthreads=nthreads, rows=(r0, r1))
         done_s += time.perf_counter() - t0
+        if keep:
+            kept.append((r0, r1, gamma, xi))
         for q1 in block:
             rr = np.nonzero(lists.row_q1 == q1)[0]
             union = np.unique(np.concatenate([lists.list3[lists.ptr3[r]:lists.ptr3[r + 1]] for r in rr]))
@@ -193,32 +201,83 @@ def cpu_sample(prob, opts, lists, budget_s=12.0, nthreads=None):
             break
     desc = (f"oracle restatement (per-row zgeru/dot_product contraction as in scattering_threephonon.f90), "
             f"{len(used)} complete irreducible q1 groups ({done_trip} q-triplets) of the same workload")
-    return done_trip, done_s, desc, nthreads
+    return done_trip, done_s, desc, nthreads, kept
+
+
+def large_sample_lists(prob, lists):
+    """Large cells: one accepted q-triplet (q1 from the middle of the wedge, its first
+    accepted q2) sampled by every row; returns (sample lists, q1, its rows)."""
+    from oracle import binding as orc
+    from tdep_gb300 import QLists
+
+    q1s = np.unique(lists.row_q1)
+    q1 = int(q1s[len(q1s) // 2])
+    rows = np.nonzero(lists.row_q1 == q1)[0]
+    full = lists.list3[lists.ptr3[rows[0]]:lists.ptr3[rows[0] + 1]]
+    q2 = next(int(q) for q in full if orc.triplets(prob, q1, np.array([q], np.int32)))
+    one = np.full(lists.n_row, q2, np.int32)
+    return QLists(lists.row_q1, lists.row_b1, np.arange(lists.n_row + 1, dtype=np.int64), one), q1, rows
 
 
 def cpu_sample_large(prob, opts, lists, nthreads=None):
     """Large cells: one accepted q-triplet per row for as many rows of one q1 as there are
     host threads (the oracle's cost per q-triplet and row grows as n^5); a GPU q-triplet
-    covers all rows of its q1, so the rate is scaled by the rows of that q1."""
+    covers all rows of its q1, so the rate is scaled by the rows of that q1. Returns
+    (q-triplet equivalents, seconds, description, threads, rows) with rows = [(r0, r1,
+    gamma, xi)] of the oracle."""
     from oracle import binding as orc
-    from tdep_gb300 import QLists
 
     nthreads = nthreads or os.cpu_count() or 1
-    q1 = int(np.unique(lists.row_q1)[len(np.unique(lists.row_q1)) // 2])
-    rows = np.nonzero(lists.row_q1 == q1)[0]
-    full = lists.list3[lists.ptr3[rows[0]]:lists.ptr3[rows[0] + 1]]
-    q2 = next(int(q) for q in full if orc.triplets(prob, q1, np.array([q], np.int32)))
-    one = np.full(lists.n_row, q2, np.int32)
-    sample = QLists(lists.row_q1, lists.row_b1, np.arange(lists.n_row + 1, dtype=np.int64), one)
+    sample, q1, rows = large_sample_lists(prob, lists)
     r0 = int(rows[0])
     r1 = min(int(rows[-1]) + 1, r0 + nthreads)
     t0 = time.perf_counter()
-    orc.scattering(prob, opts, sample, nthreads=nthreads, rows=(r0, r1))
+    gamma, xi, _ = orc.scattering(prob, opts, sample, nthreads=nthreads, rows=(r0, r1))
     secs = time.perf_counter() - t0
     done = (r1 - r0) / rows.size  # q-triplet equivalents: (rows done) / (rows per q-triplet)
     desc = (f"oracle restatement on {r1 - r0} of the {rows.size} rows of one q1, one accepted q-triplet each "
             f"(one q-triplet of the GPU covers all {rows.size} rows)")
-    return done, secs, desc, nthreads
+    return done, secs, desc, nthreads, [(r0, r1, gamma, xi)]
+
+
+def oracle_rows_finish(prob, opts, lists, kept):
+    """Boundary term, degeneracy averaging and symmetrize_scatmat of the oracle's rows (whole
+    q1 groups): returns (row indices, linewidths [n_irr, n_mode] with only those q1 filled,
+    symmetrised Xi rows)."""
+    from oracle import binding as orc
+    from tdep_gb300 import QLists
+
+    idx = np.concatenate([np.arange(r0, r1) for r0, r1, _, _ in kept])
+    gamma = np.concatenate([g for _, _, g, _ in kept])
+    xi = np.concatenate([x for _, _, _, x in kept])
+    sub = QLists(lists.row_q1[idx], lists.row_b1[idx])
+    lw, _, _ = orc.finish(prob, opts, sub, gamma, xi)
+    return idx, lw, xi
+
+
+def parity_record(prob, lists, idx, lw_ref, xi_ref, runs):
+    """Largest relative linewidth difference over the rows' q1 groups and the Xi entry
+    differences (relative to the largest |Xi| of those rows) of each GPU run against the
+    oracle. Xi entries that differ beyond 1e-9 of the largest are counted as flips of the
+    od_terms > 0 filter (an analytically zero sum rounded to either side of 0 changes how
+    many images enter an orbit average); their fraction is reported beside the largest
+    difference of the other entries."""
+    q1s = np.unique(lists.row_q1[idx]) - 1
+    ref = lw_ref[q1s]
+    mask = np.abs(ref) > 1e-12 * np.abs(ref).max()
+    out = {"rows": int(idx.size), "q1_groups": int(q1s.size)}
+    for name, (lw, xi) in runs.items():
+        got = lw[q1s]
+        out[f"lw_max_rel_{name}"] = float(np.max(np.abs(got[mask] - ref[mask]) / np.abs(ref[mask])))
+        if xi is not None and xi_ref is not None:
+            d = np.abs(xi - xi_ref) / float(np.abs(xi_ref).max())
+            if name == "fp64":
+                flips = d > 1e-9
+                out["xi_max_rel_fp64"] = float(d[~flips].max()) if (~flips).any() else 0.0
+                out["xi_flip_frac_fp64"] = float(flips.mean())
+            else:
+                out[f"xi_max_rel_{name}"] = float(d.max())
+    return out
 
 
 def run_reference(args):
@@ -232,9 +291,9 @@ def run_reference(args):
     desc, cores = "", os.cpu_count()
     for _ in range(args.steps if not large else 1):
         if large:
-            t, s, desc, cores = cpu_sample_large(prob, opts, lists)
+            t, s, desc, cores, _ = cpu_sample_large(prob, opts, lists)
         else:
-            t, s, desc, cores = cpu_sample(prob, opts, lists, budget_s=per_step)
+            t, s, desc, cores, _ = cpu_sample(prob, opts, lists, budget_s=per_step)
         trip += t
         secs += s
     value = trip / secs
@@ -320,16 +379,18 @@ def fourphonon_leg(cfg_name, steps):
     return out
 
 
-def run_gb300(args):
+def measure(cfg_name, args, cpu_budget, with_adjoint=True):
+    """Device passes, FP64 leg, adjoint ratio, e2e, CPU sample and parity rows of one
+    configuration; returns a dict (the bench line's fields for that configuration)."""
     import torch
 
     from tdep_gb300 import ScatteringRates
     from tdep_gb300._native import autotune_table
 
-    cfg, prob, opts, lists = setup(args.config, precision="mixed")
+    cfg, prob, opts, lists = setup(cfg_name, precision="mixed")
     n = prob.n_mode
-    torch.cuda.init()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > 129 MB L2
+    small = n <= 18  # the FP64 path exists
 
     sr = ScatteringRates(prob)
     for _ in range(args.warmup):
@@ -352,35 +413,39 @@ def run_gb300(args):
     clk = clocks.stop()
     graphs = sr.graph_counts()
     lw_mixed = sr.linewidth.copy()
+    xi_mixed = sr.Xi if small else None
     t0 = time.perf_counter()
     ks32, ki32 = sr.kappa(opts)
     kappa_ms = 1e3 * (time.perf_counter() - t0)
     kappa_iters = sr.n_iter
     stats = dict(sr.stats)
 
-    small = n <= 18  # the shared-memory kernel: the FP64 path exists
     adjoint = fp64 = None
-    # ---- adjoint pass (d kappa_sma,xx / d Phi3) on the same workload, against the forward ----
-    kb = np.zeros((3, 3))
-    kb[0, 0] = 1.0
-    adj_ms = []
-    for _ in range(max(2, args.steps // 2) if small else 1):
-        sr.generate(opts, lists)
-        fwd_ms = sr.stats["device_ms"]
-        sr.kappa(opts, maxiter=0)
-        sr.adjoint_fc3(opts, sr.kappa_sma_vjp(opts, kb))
-        adj_ms.append(sr.adjoint_stats["ms"])
-    adjoint = {"ms": float(np.median(adj_ms)), "forward_ms": fwd_ms,
-               "ratio_to_forward": float(np.median(adj_ms)) / fwd_ms,
-               "what": "tdg_adjoint_fc3 after tdg_kappa_sma_vjp: d kappa_xx / d mwm for all "
-                       f"{prob.n_fc3 * 27} third-order entries, mixed precision, Psi recomputed"
-                       + ("" if small else "; large-cell path: back-contraction on the tensor cores")}
+    if with_adjoint:
+        # ---- adjoint pass (d kappa_sma,xx / d Phi3) on the same workload, against the forward ----
+        kb = np.zeros((3, 3))
+        kb[0, 0] = 1.0
+        adj_ms = []
+        for _ in range(max(2, args.steps // 2) if small else 1):
+            sr.generate(opts, lists)
+            fwd_ms = sr.stats["device_ms"]
+            sr.kappa(opts, maxiter=0)
+            sr.adjoint_fc3(opts, sr.kappa_sma_vjp(opts, kb))
+            adj_ms.append(sr.adjoint_stats["ms"])
+        adjoint = {"ms": float(np.median(adj_ms)), "forward_ms": fwd_ms,
+                   "ratio_to_forward": float(np.median(adj_ms)) / fwd_ms,
+                   "what": "tdg_adjoint_fc3 after tdg_kappa_sma_vjp: d kappa_xx / d mwm for all "
+                           f"{prob.n_fc3 * 27} third-order entries, mixed precision, Psi recomputed"
+                           + ("" if small else "; large-cell path: back-contraction on the tensor cores")}
+    lw64 = xi64 = None
+    o64 = type(opts)(**{**opts.__dict__, "precision": "fp64"})
     if small:
         # ---- FP64 path on the same workload: kappa error bar and speedup ----
-        o64 = type(opts)(**{**opts.__dict__, "precision": "fp64"})
         sr.generate(o64, lists)  # warm-up: the first FP64 call also runs the launch-shape trials
         sr.generate(o64, lists)
         fp64_ms = sr.stats["device_ms"]
+        lw64 = sr.linewidth.copy()
+        xi64 = sr.Xi
         _, ki64 = sr.kappa(o64)
         kappa_err = float(np.max(np.abs(ki32 - ki64)) / np.max(np.abs(ki64)))
         fp64 = {"value": trip / (fp64_ms / 1e3), "ms_per_step": fp64_ms,
@@ -388,24 +453,33 @@ def run_gb300(args):
     sr.close()
 
     # ---- end to end through the public API with host buffers ----
-    e2e_s, parts = [], []
-    h2d = d2h = 0
-    for _ in range(args.steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        s2 = ScatteringRates(prob)
-        t1 = time.perf_counter()
-        s2.generate(opts, lists)
-        t2 = time.perf_counter()
-        s2.kappa_offdiag(opts)
-        s2.kappa(opts)
-        t3 = time.perf_counter()
-        h2d, d2h = s2.transfer_bytes()
-        s2.close()
-        torch.cuda.synchronize()
-        t4 = time.perf_counter()
-        e2e_s.append(t4 - t0)
-        parts.append((t1 - t0, t2 - t1, t3 - t2, t4 - t3))
+    def e2e_run(o, steps):
+        e2e_s, parts = [], []
+        h2d = d2h = 0
+        for _ in range(steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s2 = ScatteringRates(prob)
+            t1 = time.perf_counter()
+            s2.generate(o, lists)
+            t2 = time.perf_counter()
+            s2.kappa_offdiag(o)
+            s2.kappa(o)
+            t3 = time.perf_counter()
+            h2d, d2h = s2.transfer_bytes()
+            s2.close()
+            torch.cuda.synchronize()
+            t4 = time.perf_counter()
+            e2e_s.append(t4 - t0)
+            parts.append((t1 - t0, t2 - t1, t3 - t2, t4 - t3))
+        return {"value": trip / float(np.mean(e2e_s)), "unit": "q-triplets/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "includes": "context creation, generate, off-diagonal kappa, kappa solve",
+                "ms": {k: 1e3 * float(np.median([p[i] for p in parts]))
+                       for i, k in enumerate(("create", "generate", "kappa", "destroy"))}}
+
+    e2e = e2e_run(opts, args.steps)
+    if fp64 is not None:
+        fp64["e2e"] = e2e_run(o64, max(2, args.steps // 2))
 
     # ---- roofline of the dominant kernel (fused pretransform + contraction + epilogue) ----
     # Per-unit work of a q-triplet: the pretransform streams N_t force-constant triplets
@@ -419,7 +493,7 @@ def run_gb300(args):
     flop_per_trip = 24 * n**4
     gbs = bytes_per_trip * trip / fused_s / 1e9
     tfs = flop_per_trip * trip / fused_s / 1e12
-    traffic = TRAFFIC_PER_LAUNCH.get(args.config)
+    traffic = TRAFFIC_PER_LAUNCH.get(cfg_name)
     if n <= 6:
         roof = {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
                 "traffic": traffic, "per_unit": f"{bytes_per_trip} bytes per q-triplet (N_t*33*4 + n^3*8)",
@@ -430,48 +504,89 @@ def run_gb300(args):
                 "traffic": traffic, "per_unit": f"{flop_per_trip} flop per q-triplet (24 n^4)",
                 "units_per_launch": trip, "peak_source": f"{src} dense bf16",
                 "hbm_frac_of_pretransform": gbs / hbm}
-    roof["kernel"] = ("k_threephonon (fused pretransform, FP32 SIMT contraction, FP64 delta weights)" if small else
-                      "large-cell stage: phases, pretransform, 3 tcgen05 BF16x3 GEMM stages, FP64 delta kernel "
-                      "(time of the whole stage)")
+    roof["kernel"] = stats.get("threephonon_kernel") or (
+        "k_threephonon (fused pretransform, FP32 SIMT contraction, FP64 delta weights)" if small else
+        "large-cell stage: phases, pretransform, 3 tcgen05 BF16x3 GEMM stages, FP64 delta kernel "
+        "(time of the whole stage)")
 
+    # ---- CPU baseline sample and parity of its rows against the GPU runs ----
     if small:
-        cpu_trip, cpu_s, desc, cores = cpu_sample(prob, opts, lists, budget_s=args.cpu_budget)
+        cpu_trip, cpu_s, desc, cores, kept = cpu_sample(prob, opts, lists, budget_s=cpu_budget, keep=True)
+        idx, lw_ref, xi_ref = oracle_rows_finish(prob, o64, lists, kept)
+        runs = {"fp64": (lw64, xi64[idx]), "mixed": (lw_mixed, xi_mixed[idx])}
+        parity = parity_record(prob, lists, idx, lw_ref, xi_ref, runs)
     else:
-        cpu_trip, cpu_s, desc, cores = cpu_sample_large(prob, opts, lists)
+        cpu_trip, cpu_s, desc, cores, kept = cpu_sample_large(prob, opts, lists)
+        sample, q1, rows = large_sample_lists(prob, lists)
+        s3 = ScatteringRates(prob)
+        lw_gpu = s3.generate(opts, sample)
+        s3.close()
+        r0, r1, gamma, _ = kept[0]
+        b1 = lists.row_b1[r0:r1] - 1
+        f = prob.irr_full[q1 - 1] - 1
+        nondeg = prob.degen[f, b1] == 1  # linewidths without degeneracy averaging equal gamma
+        ref = gamma[nondeg]
+        got = lw_gpu[q1 - 1, b1[nondeg]]
+        mask = np.abs(ref) > 1e-12 * np.abs(ref).max()
+        parity = {"rows": int(nondeg.sum()), "q1_groups": 1, "what": "one q-triplet per row, rows of one q1 "
+                  "without degenerate partners: tensor-core mixed path against the FP64 oracle",
+                  "lw_max_rel_mixed": float(np.max(np.abs(got[mask] - ref[mask]) / np.abs(ref[mask])))}
     value = trip * args.steps / (sum(dev_ms) / 1e3)
+    return {
+        "cfg": cfg, "n": n, "small": small, "value": value, "ms_per_step": float(np.mean(dev_ms)),
+        "trip": trip, "xi_gb": lists.n_row * prob.n_full * n * 8 / 1e9, "e2e": e2e, "adjoint": adjoint,
+        "roofline": roof, "clocks": clk, "launches": launches, "graphs": graphs, "stats": stats,
+        "kappa_ms": kappa_ms, "kappa_iters": kappa_iters, "fp64": fp64, "lw_max": float(lw_mixed.max()),
+        "cpu": {"value": cpu_trip / cpu_s, "unit": "q-triplets/s", "cores": cores, "kind": "port", "sample": desc},
+        "parity": parity, "tune": autotune_table(),
+    }
+
+
+def run_gb300(args):
+    import torch
+
+    torch.cuda.init()
+    m = measure(args.config, args, args.cpu_budget)
+    n, small = m["n"], m["small"]
+    cfg = m["cfg"]
     line = {
-        "metric": METRIC, "value": value, "unit": "q-triplets/s", "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": float(np.mean(dev_ms)), "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": m["value"], "unit": "q-triplets/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": m["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": cfg["workload"], "mesh": list(cfg["grid"]), "n_mode": n, "q_triplets_per_step": trip,
-                   "precision": ("mixed: FP32 pretransform+contraction, FP64 delta weights/occupations/accumulation"
-                                 if small else "mixed: FP32 pretransform, BF16x3 tensor-core contraction with FP32 "
-                                               "accumulation, FP64 delta weights/occupations/accumulation"),
-                   "l2": "256 MB buffer written between steps (L2 flush); Xi+od working set 2x%.2f GB" %
-                         (lists.n_row * prob.n_full * n * 8 / 1e9)},
-        "e2e": {"value": trip / float(np.mean(e2e_s)), "unit": "q-triplets/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h), "includes": "context creation, generate, off-diagonal kappa, kappa solve",
-                "ms": {k: 1e3 * float(np.median([p[i] for p in parts]))
-                       for i, k in enumerate(("create", "generate", "kappa", "destroy"))}},
-        "adjoint": adjoint,
-        "roofline": roof,
-        "cpu_baseline": {"value": cpu_trip / cpu_s, "unit": "q-triplets/s", "cores": cores, "kind": "port",
-                         "sample": desc},
-        "clocks": clk,
-        "gpu_launches": int(launches),
-        "launch_shapes": {"autotuned": autotune_table(),
-                          "graph_counts_direct_recorded_replayed": graphs,
+        "config": {"workload": cfg["workload"], "mesh": list(cfg["grid"]), "n_mode": n, "q_triplets_per_step": m["trip"],
+                   "precision": m["stats"].get("precision_note") or (
+                       "mixed: FP32 pretransform+contraction, FP64 delta weights/occupations/accumulation" if small
+                       else "mixed: FP32 pretransform, BF16x3 tensor-core contraction with FP32 accumulation, FP64 "
+                            "delta weights/occupations/accumulation"),
+                   "l2": "256 MB buffer written between steps (L2 flush); Xi+od working set 2x%.2f GB" % m["xi_gb"]},
+        "e2e": m["e2e"],
+        "adjoint": m["adjoint"],
+        "roofline": m["roofline"],
+        "cpu_baseline": m["cpu"],
+        "parity": m["parity"],
+        "clocks": m["clocks"],
+        "gpu_launches": int(m["launches"]),
+        "launch_shapes": {"autotuned": m["tune"],
+                          "graph_counts_direct_recorded_replayed": m["graphs"],
                           "note": "warm-up calls run the autotuner trials and record the CUDA graph of the "
                                   "three-phonon kernels; timed calls replay it"},
-        "stage_ms": {k: stats[k] for k in ("enumerate_ms", "threephonon_ms", "symmetrize_ms", "device_ms")},
-        "mode_triplets_per_s": value * n**3,
-        "kappa_wall_ms": kappa_ms, "kappa_iterations": kappa_iters,
-        "fp64": fp64 if small else {"value": None, "reason": "beyond 18 modes the contraction runs only on the "
-                                                              "tensor cores (mixed precision)"},
-        "linewidth_max_hartree": float(lw_mixed.max()),
+        "stage_ms": {k: m["stats"][k] for k in ("enumerate_ms", "threephonon_ms", "symmetrize_ms", "device_ms")},
+        "mode_triplets_per_s": m["value"] * n**3,
+        "kappa_wall_ms": m["kappa_ms"], "kappa_iterations": m["kappa_iters"],
+        "fp64": m["fp64"] if small else {"value": None, "reason": "beyond 18 modes the contraction runs only on the "
+                                                                   "tensor cores (mixed precision)"},
+        "linewidth_max_hartree": m["lw_max"],
     }
     if "uneven" in cfg and args.config == "perovskite16":
         line["three_plus_four_phonon"] = fourphonon_leg(args.config, max(2, args.steps // 2))
+    if args.config == "perovskite16" and not args.no_sub:
+        # the 2-atom rocksalt 24^3 configuration (6 modes, full q' grid) measured in the same run
+        r = measure("rocksalt24", args, min(6.0, args.cpu_budget), with_adjoint=True)
+        line["rocksalt24"] = {
+            "workload": r["cfg"]["workload"], "value": r["value"], "unit": "q-triplets/s",
+            "ms_per_step": r["ms_per_step"], "q_triplets_per_step": r["trip"], "e2e": r["e2e"], "fp64": r["fp64"],
+            "adjoint": r["adjoint"], "roofline": r["roofline"], "cpu_baseline": r["cpu"], "parity": r["parity"],
+            "clocks": r["clocks"], "gpu_launches": int(r["launches"]), "kappa_wall_ms": r["kappa_ms"]}
     print(json.dumps(line))
 
 
@@ -481,7 +596,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="rocksalt24", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="perovskite16", choices=sorted(CONFIGS))
+    ap.add_argument("--no-sub", action="store_true", help="skip the rocksalt 24^3 sub-record of the default run")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--profile", action="store_true", help="only run passes of one stage, see --stage (for ncu captures)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"], help="with --profile")

@@ -124,9 +124,11 @@ typedef struct tdg_opts {
     int32_t qg4ph[3];          /* -qg4ph after defaulting                                     */
     int32_t seed;              /* --seed (> 0)                                                */
     int32_t precision;         /* TDG_PREC_FP64 or TDG_PREC_MIXED                             */
-    int32_t tensor_cores;      /* no reference counterpart: 0 = automatic (the tcgen05
+    int32_t tensor_cores;      /* no reference counterpart: 0 = automatic (mixed precision:
+                                  the tcgen05 fused kernel for 9, 12 and 15 modes, the tcgen05
                                   large-cell contraction for more than 18 modes), 1 = always
-                                  (mixed precision only)                                     */
+                                  the large-cell contraction (mixed precision only), 2 = the
+                                  FP32 SIMT fused kernel up to 18 modes                       */
 } tdg_opts;
 
 /*
@@ -201,6 +203,12 @@ int tdg_natural_isotopes(const char *symbol, int32_t cap, double *abundance, dou
  * receive the context's direct runs, recordings and replays of that part.
  */
 int tdg_graph_counts(tdg_ctx *ctx, int64_t *counts);
+
+/* Which three-phonon path the context's last tdg_scattering took (no reference
+ * counterpart): 0 the SIMT fused kernel (FP64, or FP32 contraction), 1 the tcgen05 fused
+ * kernel (9, 12 or 15 modes, mixed precision), 2 the large-cell batches (tcgen05), -1 none
+ * yet. The environment variable TDG_TC_SMALL=0 turns path 1 off. */
+int tdg_last_path(tdg_ctx *ctx, int32_t *path);
 
 /*
  * Launch-shape autotuner (no reference counterpart). The first scattering call that needs a
@@ -374,6 +382,18 @@ void tdg_problem_free(tdg_problem *prob);
  */
 int tdg_phonon_frequencies(const char *dir, int32_t nq, const double *q, const double *qdir,
                            double *omega);
+
+/*
+ * outfile.thermal_conductivity_grid.hdf5 (type_phonon_dispersions.f90:316-641, written by
+ * main.f90:339): the per-mode data of the full mesh in HDF5, without libhdf5 (the library
+ * writes the file format itself). linewidth [n_irr*n_mode] as tdg_scattering returns it
+ * (Hartree); fn [n_irr*n_mode*3] the final Fn of tdg_kappa, or NULL for the relaxation-time
+ * form of the per-mode conductivity. The dataset thermal_conductivity summed over points and
+ * modes and divided by number_of_qpoints is kappa_iter (W/m/K), as the reference's own test
+ * checks (tests/thermal_conductivity/test_thermal_conductivity.py:24-40).
+ */
+int tdg_write_grid_hdf5(const char *path, const tdg_problem *prob, double temperature, const double *linewidth,
+                        const double *fn);
 
 /* Writes outfile.thermal_conductivity (main.f90:246-294) into `dir`. Tensors in a.u. */
 int tdg_write_outfile(const char *dir, double temperature, const double *kappa_sma,

@@ -5,7 +5,8 @@ Python users drive it through tdep_gb300.scattering (Problem, Options, QLists,
 ScatteringRates); Fortran or C callers bind the C-ABI directly.
 """
 from .scattering import (KAPPA_AU_TO_SI, Options, Problem, QLists, ScatteringRates, device_count,  # noqa: F401
-                         release_cached_memory, write_outfile)
+                         release_cached_memory, write_grid_hdf5, write_outfile)
 
-__all__ = ["Problem", "Options", "QLists", "ScatteringRates", "write_outfile", "device_count", "release_cached_memory",
+__all__ = ["Problem", "Options", "QLists", "ScatteringRates", "write_outfile", "write_grid_hdf5", "device_count",
+           "release_cached_memory",
            "KAPPA_AU_TO_SI"]

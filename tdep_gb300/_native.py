@@ -122,6 +122,8 @@ SIGNATURES = {
     "tdg_transfer_bytes": (C.c_int, [C.c_void_p, _i64p, _i64p]),
     "tdg_kappa_offdiag": (C.c_int, [C.c_void_p, C.POINTER(TdgOpts), _f64p]),
     "tdg_release_cached_memory": (C.c_int, [C.c_int]),
+    "tdg_write_grid_hdf5": (C.c_int, [C.c_char_p, C.POINTER(TdgProblem), C.c_double, _f64p, _f64p]),
+    "tdg_last_path": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "tdg_pool_usage": (C.c_int, [C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "tdg_natural_isotopes": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "tdg_autotune_load": (C.c_int, [C.c_char_p]),

@@ -1,0 +1,270 @@
+// Per-q-triplet stages shared by the two fused three-phonon kernels (the SIMT kernel of
+// k_threephonon.cu and the tensor-core kernel of k_threephonon_tc.cu): loading the mode
+// scalars, the skip rules as bit masks, the FP32 screen of the Gaussians, the FP64 delta
+// weights of the survivors, and the row/column sums with the Gamma and Xi scatter.
+//
+// Reference (src/thermal_conductivity/scattering_threephonon.f90):
+//   skip rules (:90-101), get_dirac (:219-271), accumulation into Gamma and the Xi row
+//   terms for every equivalent triplet (:115-135).
+#pragma once
+
+#include "dev_common.cuh"
+#include "tdg_internal.cuh"
+
+namespace tdg {
+
+namespace {
+
+constexpr double kThreePhononPrefactor = 3.141592653589793 / 16.0;
+
+// Shared-memory arrays of one q-triplet (all length n unless noted).
+struct K3Smem {
+    double *om1, *om2, *om3, *inv1, *be2, *be3, *s1, *s2, *s3;
+    double *v1, *v2, *v3;  // [3n]
+    double *wrow;
+    double *R2;            // [n^2] row sums, then Xi row terms
+    double *R3;            // [n^2] column sums, then Xi row terms
+    double *F;             // [n^3] dense F (zero where no survivor)
+    float *fo1, *fo2, *fo3, *fs1, *fs2, *fs3;
+    uint32_t *m12, *m13, *m23;
+    uint32_t *zmask;       // [2]: omega2 < tol, omega3 < tol
+    uint32_t *rowbits;     // [n^2] b3 with a non-zero F for each (b1, b2)
+    uint32_t *colbits;     // [n^2] b2 with a non-zero F for each (b1, b3)
+    uint32_t *Q;           // survivor queue: (b1 b2 b3 index) | live bits << 16
+    int *rowid;            // row of (q1, b1), -1 when the row does not sample q2
+    int2 *red;             // [kMaxRed] equivalent triplets
+    int *wsum;             // [33] block scan
+};
+
+// Per-mode scalars of the q-triplet, row ids of the rows that sample it, cleared masks and
+// the equivalent triplets. Caller: a barrier before the next stage.
+template <int N>
+__device__ __forceinline__ void k3_load_modes(const K3Smem &S, const ThreePhArgs &a, const TripletRec &rec,
+                                              int f1, int q2, int q3, int i2, int i3) {
+    constexpr int N2 = N * N;
+    const PhononDev &P = a.ph;
+    const int tid = threadIdx.x, bd = blockDim.x;
+    const uint32_t *mask = a.cand_mask + (size_t)rec.cand * 4;
+    for (int b = tid; b < N; b += bd) {
+        S.om1[b] = P.omega[(size_t)f1 * N + b];
+        S.om2[b] = P.omega[(size_t)q2 * N + b];
+        S.om3[b] = P.omega[(size_t)q3 * N + b];
+        S.inv1[b] = P.inv_omega[(size_t)f1 * N + b];
+        S.be2[b] = P.be[(size_t)i2 * N + b];
+        S.be3[b] = P.be[(size_t)i3 * N + b];
+        S.s1[b] = P.sigsq[(size_t)rec.q1 * N + b];
+        S.s2[b] = P.sigsq[(size_t)i2 * N + b];
+        S.s3[b] = P.sigsq[(size_t)i3 * N + b];
+        S.fo1[b] = P.omega32[(size_t)f1 * N + b];
+        S.fo2[b] = P.omega32[(size_t)q2 * N + b];
+        S.fo3[b] = P.omega32[(size_t)q3 * N + b];
+        S.fs1[b] = P.sigsq32[(size_t)rec.q1 * N + b];
+        S.fs2[b] = P.sigsq32[(size_t)i2 * N + b];
+        S.fs3[b] = P.sigsq32[(size_t)i3 * N + b];
+        for (int d = 0; d < 3; ++d) {
+            S.v1[b * 3 + d] = P.vel[((size_t)f1 * N + b) * 3 + d];
+            S.v2[b * 3 + d] = P.vel[((size_t)q2 * N + b) * 3 + d];
+            S.v3[b * 3 + d] = P.vel[((size_t)q3 * N + b) * 3 + d];
+        }
+        const int r = a.rows.rowidx[(size_t)rec.q1 * N + b];
+        const bool on = (mask[b >> 5] >> (b & 31)) & 1u;
+        S.rowid[b] = on ? r : -1;
+        S.wrow[b] = a.rows.w3q[(size_t)rec.q1 * N + b];
+        S.m12[b] = 0u;
+        S.m13[b] = 0u;
+        S.m23[b] = 0u;
+    }
+    if (tid == 0) {
+        S.zmask[0] = 0u;
+        S.zmask[1] = 0u;
+    }
+    for (int i = tid; i < 2 * N2; i += bd) S.rowbits[i] = 0u;
+    for (int i = tid; i < rec.red_cnt && i < kMaxRed; i += bd) S.red[i] = a.red[rec.red_off + i];
+}
+
+// Skip rules of scattering_threephonon.f90:90-101 as bit masks (after a barrier that made
+// the mode scalars visible).
+template <int N>
+__device__ __forceinline__ void k3_skip_masks(const K3Smem &S) {
+    constexpr int N2 = N * N;
+    const int tid = threadIdx.x, bd = blockDim.x;
+    for (int i = tid; i < 3 * N2 + 2 * N; i += bd) {
+        if (i < 3 * N2) {
+            const int which = i / N2, x = (i % N2) / N, y = i % N;
+            const double *pa = which == 2 ? S.om2 : S.om1;
+            const double *pb = which == 0 ? S.om2 : S.om3;
+            const float *fa = which == 2 ? S.fo2 : S.fo1;
+            const float *fb = which == 0 ? S.fo2 : S.fo3;
+            uint32_t *mk = which == 0 ? S.m12 : (which == 1 ? S.m13 : S.m23);
+            // |x - y| < 1e-9 in FP64 needs |fx - fy| below 1e-8 in FP32 at these magnitudes
+            if (fabsf(fa[x] - fb[y]) < 1e-8f && fabs(pa[x] - pb[y]) < kFreqTolD) atomicOr(mk + x, 1u << y);
+        } else {
+            const int j = i - 3 * N2, which = j / N, b = j % N;
+            const double w = which == 0 ? S.om2[b] : S.om3[b];
+            if (w < kFreqTolD) atomicOr(S.zmask + which, 1u << b);
+        }
+    }
+}
+
+// Live bits of the four Gaussians of every b3 of one (b1, b2): the FP32 screen against
+// the 8-sigma window of lo_gauss with a relative margin of 1e-3 and an absolute margin far
+// above FP32 rounding (a Gaussian the screen drops is exactly 0 in the reference). Returns
+// the number of surviving mode triplets; the live bits of b3 are packed 4 per b3 into
+// lo (b3 < 8), hi (b3 < 16) and x (b3 < 18).
+template <int N>
+__device__ __forceinline__ int k3_screen(const K3Smem &S, int it, float sigfix32, int b1, int b2, uint32_t &live_lo,
+                                         uint32_t &live_hi, uint32_t &live_x) {
+    constexpr uint32_t kAll = (N >= 32) ? 0xffffffffu : ((1u << N) - 1u);
+    live_lo = live_hi = live_x = 0u;
+    int nsurv = 0;
+    const bool skip12 = S.rowid[b1] < 0 || ((S.zmask[0] | S.m12[b1]) >> b2) & 1u;
+    const uint32_t allowed = skip12 ? 0u : (kAll & ~(S.zmask[1] | S.m13[b1] | S.m23[b2]));
+    const float f_o1 = S.fo1[b1], f_o2 = S.fo2[b2];
+#pragma unroll
+    for (int b3 = 0; b3 < N; ++b3) {
+        if (!((allowed >> b3) & 1u)) continue;
+        const float f_o3 = S.fo3[b3];
+        float sg = 0.f;
+        if (it == 1) sg = sigfix32;
+        else if (it == 2) sg = sqrtf(S.fs1[b1] + S.fs2[b2] + S.fs3[b3]);
+        const float win = 8.0f * sg * 1.001f + 1e-6f * (f_o1 + f_o2 + f_o3);
+        uint32_t live = 15u;  // the -it 6 width can cancel in FP32: not screened
+        if (it != 6) {
+            live = (fabsf(f_o1 + f_o2 - f_o3) <= win ? 1u : 0u) | (fabsf(f_o1 - f_o2 + f_o3) <= win ? 2u : 0u) |
+                   (fabsf(f_o1 - f_o2 - f_o3) <= win ? 4u : 0u) | (f_o1 + f_o2 + f_o3 <= win ? 8u : 0u);
+        }
+        if (live) {
+            ++nsurv;
+            if (b3 < 8) live_lo |= live << (4 * b3);
+            else if (b3 < 16) live_hi |= live << (4 * (b3 - 8));
+            else live_x |= live << (4 * (b3 - 16));
+        }
+    }
+    return nsurv;
+}
+
+// Queue entries of one (b1, b2) from its live bits, starting at position k.
+template <int N>
+__device__ __forceinline__ void k3_enqueue(const K3Smem &S, int b1b2, int k, uint32_t live_lo, uint32_t live_hi,
+                                           uint32_t live_x) {
+#pragma unroll
+    for (int b3 = 0; b3 < N; ++b3) {
+        const uint32_t live = b3 < 8 ? (live_lo >> (4 * b3)) & 15u
+                                     : (b3 < 16 ? (live_hi >> (4 * (b3 - 8))) & 15u : (live_x >> (4 * (b3 - 16))) & 15u);
+        if (live) S.Q[k++] = (uint32_t)(b1b2 * N + b3) | (live << 16);
+    }
+}
+
+// FP64 delta weights and occupations of the nq queued survivors, by full warps: F[idx] =
+// perm |Psi|^2 ((n2 - n3) d0 + (n2 + n3 + 1) d1) (the adjoint keeps dF/d|Psi|^2: psisq(idx)
+// returns 1) and the row/column bits of the non-zero entries. F must be zero beforehand.
+template <int N, typename PsiSq>
+__device__ __forceinline__ void k3_survivors(const K3Smem &S, const PhononDev &P, int nq, double perm,
+                                             PsiSq psisq) {
+    constexpr int N2 = N * N;
+    const int it = P.integrationtype;
+    for (int s = threadIdx.x; s < nq; s += blockDim.x) {
+        const uint32_t qv = S.Q[s];
+        const int idx = (int)(qv & 0xffffu);
+        const uint32_t live = qv >> 16;
+        const int b1 = idx / N2, b2 = (idx / N) % N, b3 = idx % N;
+        const double o1 = S.om1[b1], o2 = S.om2[b2], o3 = S.om3[b3];
+        double sigma, invsig;
+        if (it == 1) {
+            sigma = P.sigma_fixed;
+            invsig = 1.0 / sigma;
+        } else if (it == 2) {
+            const double sq = S.s1[b1] + S.s2[b2] + S.s3[b3];
+            invsig = rsqrt(sq);
+            sigma = sq * invsig;
+        } else {
+            sigma = adaptive_pair(S.v1 + 3 * b1, S.v2 + 3 * b2, P.reclat_g) / 3.0;
+            sigma += adaptive_pair(S.v1 + 3 * b1, S.v3 + 3 * b3, P.reclat_g) / 3.0;
+            sigma += adaptive_pair(S.v2 + 3 * b2, S.v3 + 3 * b3, P.reclat_g) / 3.0;
+            sigma += P.thresh_sigma;
+            invsig = 1.0 / sigma;
+        }
+        const double win8 = 8.0 * sigma, h = 0.5 * invsig * invsig, cg = kSqrt2PiInv * invsig;
+        double d0, d1;
+        dirac3(live, o1, o2, o3, win8, h, cg, P.exp2tab, d0, d1);
+        if (nonzero(d0) || nonzero(d1)) {
+            const double pq = kThreePhononPrefactor * psisq(idx) * S.wrow[b1];
+            const double n2 = S.be2[b2], n3 = S.be3[b3];
+            const double f0 = perm * pq * (n2 - n3) * d0;
+            const double f1 = perm * pq * (n2 + n3 + 1.0) * d1;
+            const double fsum = f0 + f1;
+            S.F[idx] = fsum;
+            if (nonzero(fsum)) {
+                atomicOr(S.rowbits + b1 * N + b2, 1u << b3);
+                atomicOr(S.colbits + b1 * N + b3, 1u << b2);
+            }
+        }
+    }
+}
+
+// Row sums over b3 (R2) and column sums over b2 (R3) of the non-zero F, Gamma of every
+// sampling row times the nred equivalent triplets, then the Xi row terms 2 F om/om1 added
+// for each equivalent triplet (scattering_threephonon.f90:115-135). Starts and ends with
+// barriers of its own.
+template <int N>
+__device__ __forceinline__ void k3_sums_scatter(const K3Smem &S, const ThreePhArgs &a, int nred) {
+    constexpr int N2 = N * N;
+    const int tid = threadIdx.x, bd = blockDim.x;
+    const int64_t ld = (int64_t)a.mesh.n_full * N;
+    __syncthreads();
+    for (int e = tid; e < 2 * N2; e += bd) {
+        double sum = 0.0;
+        if (e < N2) {
+            for (uint32_t bits = S.rowbits[e]; bits; bits &= bits - 1) sum += S.F[e * N + __ffs(bits) - 1];
+            S.R2[e] = sum;
+        } else {
+            const int e3 = e - N2, b1 = e3 / N, b3 = e3 % N;
+            for (uint32_t bits = S.colbits[e3]; bits; bits &= bits - 1)
+                sum += S.F[(b1 * N + __ffs(bits) - 1) * N + b3];
+            S.R3[e3] = sum;
+        }
+    }
+    __syncthreads();
+    if (tid < N) {
+        const int row = S.rowid[tid];
+        if (row >= 0) {
+            double g = 0.0;
+            for (int b2 = 0; b2 < N; ++b2) g += S.R2[tid * N + b2];
+            if (nonzero(g)) atomicAdd(a.gamma + row, (double)nred * g);
+        }
+    }
+    // the Xi row terms 2 F om/om1 of each entry, computed once for all equivalent triplets
+    // (after Gamma has read R2)
+    __syncthreads();
+    for (int e = tid; e < 2 * N2; e += bd) {
+        if (e < N2) {
+            const double v = S.R2[e];
+            S.R2[e] = nonzero(v) ? 2.0 * v * S.om2[e % N] * S.inv1[e / N] : 0.0;
+        } else {
+            const int e3 = e - N2;
+            const double v = S.R3[e3];
+            S.R3[e3] = nonzero(v) ? 2.0 * v * S.om3[e3 % N] * S.inv1[e3 / N] : 0.0;
+        }
+    }
+    __syncthreads();
+    for (int i = tid; i < 2 * N2 * nred; i += bd) {
+        const int r = i / (2 * N2), e = i % (2 * N2);
+        const int2 pr = S.red[r];
+        if (e < N2) {
+            const int b1 = e / N, b2 = e % N;
+            const int row = S.rowid[b1];
+            const double v = S.R2[e];
+            if (row >= 0 && nonzero(v)) atomicAdd(a.od + row * ld + (int64_t)pr.x * N + b2, v);
+        } else {
+            const int e3 = e - N2, b1 = e3 / N, b3 = e3 % N;
+            const int row = S.rowid[b1];
+            const double v = S.R3[e3];
+            if (row >= 0 && nonzero(v)) atomicAdd(a.od + row * ld + (int64_t)pr.y * N + b3, v);
+        }
+    }
+    __syncthreads();
+}
+
+}  // namespace
+
+}  // namespace tdg

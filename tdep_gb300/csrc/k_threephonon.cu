@@ -30,13 +30,13 @@
 #include <cuda_runtime.h>
 
 #include "dev_common.cuh"
+#include "k3_parts.cuh"
 #include "tdg_internal.cuh"
 
 namespace tdg {
 
 namespace {
 
-constexpr double kThreePhononPrefactor = 3.141592653589793 / 16.0;
 constexpr int kPhaseChunk = 512;
 // Phase factors held in shared memory at a time: at least kPhaseChunk, more when the survivor
 // queue, which later reuses the eigenvector and phase region, is larger anyway (n = 15 in
@@ -207,6 +207,13 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
     int *rowid = (int *)(smem + L.rowid);
     int2 *red = (int2 *)(smem + L.red);
     int *wsum = (int *)(smem + L.wsum);
+    K3Smem S;
+    S.om1 = om1; S.om2 = om2; S.om3 = om3; S.inv1 = inv1; S.be2 = be2; S.be3 = be3;
+    S.s1 = s1; S.s2 = s2; S.s3 = s3; S.v1 = v1; S.v2 = v2; S.v3 = v3; S.wrow = wrow;
+    S.R2 = R2; S.R3 = (double *)B; S.F = (double *)A;
+    S.fo1 = fo1; S.fo2 = fo2; S.fo3 = fo3; S.fs1 = fs1; S.fs2 = fs2; S.fs3 = fs3;
+    S.m12 = m12; S.m13 = m13; S.m23 = m23; S.zmask = zmask; S.rowbits = rowbits; S.colbits = colbits;
+    S.Q = Q; S.rowid = rowid; S.red = red; S.wsum = wsum;
     const int tid = threadIdx.x, bd = blockDim.x;
     const MeshDev &m = a.mesh;
     const PhononDev &P = a.ph;
@@ -232,45 +239,9 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
         const int f1 = m.irr_full[rec.q1];
         const int q2 = rec.q2, q3 = rec.q3;
         const int i2 = m.full_irr[q2], i3 = m.full_irr[q3];
-        const uint32_t *mask = a.cand_mask + (size_t)rec.cand * 4;
         const int nred = rec.red_cnt;
         const double perm = (q2 == q3) ? 1.0 : 2.0;
-        // ---- per-mode scalars ----
-        for (int b = tid; b < N; b += bd) {
-            om1[b] = P.omega[(size_t)f1 * N + b];
-            om2[b] = P.omega[(size_t)q2 * N + b];
-            om3[b] = P.omega[(size_t)q3 * N + b];
-            inv1[b] = P.inv_omega[(size_t)f1 * N + b];
-            be2[b] = P.be[(size_t)i2 * N + b];
-            be3[b] = P.be[(size_t)i3 * N + b];
-            s1[b] = P.sigsq[(size_t)rec.q1 * N + b];
-            s2[b] = P.sigsq[(size_t)i2 * N + b];
-            s3[b] = P.sigsq[(size_t)i3 * N + b];
-            fo1[b] = P.omega32[(size_t)f1 * N + b];
-            fo2[b] = P.omega32[(size_t)q2 * N + b];
-            fo3[b] = P.omega32[(size_t)q3 * N + b];
-            fs1[b] = P.sigsq32[(size_t)rec.q1 * N + b];
-            fs2[b] = P.sigsq32[(size_t)i2 * N + b];
-            fs3[b] = P.sigsq32[(size_t)i3 * N + b];
-            for (int d = 0; d < 3; ++d) {
-                v1[b * 3 + d] = P.vel[((size_t)f1 * N + b) * 3 + d];
-                v2[b * 3 + d] = P.vel[((size_t)q2 * N + b) * 3 + d];
-                v3[b * 3 + d] = P.vel[((size_t)q3 * N + b) * 3 + d];
-            }
-            const int r = a.rows.rowidx[(size_t)rec.q1 * N + b];
-            const bool on = (mask[b >> 5] >> (b & 31)) & 1u;
-            rowid[b] = on ? r : -1;
-            wrow[b] = a.rows.w3q[(size_t)rec.q1 * N + b];
-            m12[b] = 0u;
-            m13[b] = 0u;
-            m23[b] = 0u;
-        }
-        if (tid == 0) {
-            zmask[0] = 0u;
-            zmask[1] = 0u;
-        }
-        for (int i = tid; i < 2 * N2; i += bd) rowbits[i] = 0u;
-        for (int i = tid; i < nred && i < kMaxRed; i += bd) red[i] = a.red[rec.red_off + i];
+        k3_load_modes<N>(S, a, rec, f1, q2, q3, i2, i3);
         for (int i = tid; i < 3 * N2; i += bd) {
             const int which = i / N2, e = i % N2;
             const int r = e / N, b = e % N;  // element (r) of mode b
@@ -281,22 +252,7 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
         for (int i = tid; i < N3; i += bd) A[i] = czero<C>();
         __syncthreads();
         // ---- skip rules of scattering_threephonon.f90:90-101 as bit masks ----
-        for (int i = tid; i < 3 * N2 + 2 * N; i += bd) {
-            if (i < 3 * N2) {
-                const int which = i / N2, x = (i % N2) / N, y = i % N;
-                const double *pa = which == 2 ? om2 : om1;
-                const double *pb = which == 0 ? om2 : om3;
-                const float *fa = which == 2 ? fo2 : fo1;
-                const float *fb = which == 0 ? fo2 : fo3;
-                uint32_t *mk = which == 0 ? m12 : (which == 1 ? m13 : m23);
-                // |x - y| < 1e-9 in FP64 needs |fx - fy| below 1e-8 in FP32 at these magnitudes
-                if (fabsf(fa[x] - fb[y]) < 1e-8f && fabs(pa[x] - pb[y]) < kFreqTolD) atomicOr(mk + x, 1u << y);
-            } else {
-                const int j = i - 3 * N2, which = j / N, b = j % N;
-                const double w = which == 0 ? om2[b] : om3[b];
-                if (w < kFreqTolD) atomicOr(zmask + which, 1u << b);
-            }
-        }
+        k3_skip_masks<N>(S);
         // ---- K2: pretransform into A ----
         int gi2[3], gi3[3];
         {
@@ -364,7 +320,6 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
         }
         __syncthreads();
         // ---- Psi into B; FP32 screen of the Gaussians, survivors counted per thread ----
-        uint32_t allowed = 0u;  // b3 that pass the reference's skip rules
         uint32_t live_lo = 0u, live_hi = 0u;  // 4-bit live masks of b3 = 0..7 and 8..15
         uint32_t live_x = 0u;                 // b3 = 16, 17
         int nsurv = 0;
@@ -381,90 +336,27 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
             }
 #pragma unroll
             for (int b3 = 0; b3 < N; ++b3) B[(b1 * N + b2) * N + b3] = acc[b3];
-            const bool skip12 = rowid[b1] < 0 || ((zmask[0] | m12[b1]) >> b2) & 1u;
-            allowed = skip12 ? 0u : (kAll & ~(zmask[1] | m13[b1] | m23[b2]));
-            const float f_o1 = fo1[b1], f_o2 = fo2[b2];
-#pragma unroll
-            for (int b3 = 0; b3 < N; ++b3) {
-                if (!((allowed >> b3) & 1u)) continue;
-                const float f_o3 = fo3[b3];
-                float sg = 0.f;
-                if (it == 1) sg = sigfix32;
-                else if (it == 2) sg = sqrtf(fs1[b1] + fs2[b2] + fs3[b3]);
-                const float win = 8.0f * sg * 1.001f + 1e-6f * (f_o1 + f_o2 + f_o3);
-                uint32_t live = 15u;  // the -it 6 width can cancel in FP32: not screened
-                if (it != 6) {
-                    live = (fabsf(f_o1 + f_o2 - f_o3) <= win ? 1u : 0u) | (fabsf(f_o1 - f_o2 + f_o3) <= win ? 2u : 0u) |
-                           (fabsf(f_o1 - f_o2 - f_o3) <= win ? 4u : 0u) | (f_o1 + f_o2 + f_o3 <= win ? 8u : 0u);
-                }
-                if (live) {
-                    ++nsurv;
-                    if (b3 < 8) live_lo |= live << (4 * b3);
-                    else if (b3 < 16) live_hi |= live << (4 * (b3 - 8));
-                    else live_x |= live << (4 * (b3 - 16));
-                }
-            }
+            nsurv = k3_screen<N>(S, it, sigfix32, b1, b2, live_lo, live_hi, live_x);
         }
         int nq = 0;
         const int off = block_exclusive_scan(nsurv, wsum, nq);  // contains __syncthreads
         // E1..E3 and the phases are dead: the queue overwrites them.
-        if (tid < N2 && nsurv) {
-            int k = off;
-#pragma unroll
-            for (int b3 = 0; b3 < N; ++b3) {
-                const uint32_t live = b3 < 8 ? (live_lo >> (4 * b3)) & 15u
-                                             : (b3 < 16 ? (live_hi >> (4 * (b3 - 8))) & 15u : (live_x >> (4 * (b3 - 16))) & 15u);
-                if (live) Q[k++] = (uint32_t)(tid * N + b3) | (live << 16);
-            }
-        }
+        if (tid < N2 && nsurv) k3_enqueue<N>(S, tid, off, live_lo, live_hi, live_x);
         // dense F (doubles) in A, zero where no survivor
         double *F = (double *)A;
         for (int i = tid; i < N3; i += bd) F[i] = 0.0;
         __syncthreads();
         // ---- FP64 delta weights and occupations for the survivors, full warps ----
-        for (int s = tid; s < nq; s += bd) {
-            const uint32_t qv = Q[s];
-            const int idx = (int)(qv & 0xffffu);
-            const uint32_t live = qv >> 16;
-            const int b1 = idx / N2, b2 = (idx / N) % N, b3 = idx % N;
-            const double o1 = om1[b1], o2 = om2[b2], o3 = om3[b3];
-            double sigma, invsig;
-            if (it == 1) {
-                sigma = P.sigma_fixed;
-                invsig = 1.0 / sigma;
-            } else if (it == 2) {
-                const double sq = s1[b1] + s2[b2] + s3[b3];
-                invsig = rsqrt(sq);
-                sigma = sq * invsig;
+        // (the adjoint keeps d F / d|Psi|^2, i.e. F without |Psi|^2)
+        k3_survivors<N>(S, P, nq, perm, [&](int idx) -> double {
+            if constexpr (ADJ) {
+                return 1.0;
             } else {
-                sigma = adaptive_pair(v1 + 3 * b1, v2 + 3 * b2, P.reclat_g) / 3.0;
-                sigma += adaptive_pair(v1 + 3 * b1, v3 + 3 * b3, P.reclat_g) / 3.0;
-                sigma += adaptive_pair(v2 + 3 * b2, v3 + 3 * b3, P.reclat_g) / 3.0;
-                sigma += P.thresh_sigma;
-                invsig = 1.0 / sigma;
-            }
-            const double win8 = 8.0 * sigma, h = 0.5 * invsig * invsig, cg = kSqrt2PiInv * invsig;
-            const double *tab = P.exp2tab;
-            double d0, d1;
-            dirac3(live, o1, o2, o3, win8, h, cg, tab, d0, d1);
-            if (nonzero(d0) || nonzero(d1)) {
                 const C psi = B[idx];
                 const double cr = (double)psi.x, ci = (double)psi.y;
-                // the adjoint keeps d F / d|Psi|^2, i.e. F without |Psi|^2
-                const double psisq = kThreePhononPrefactor * (ADJ ? 1.0 : cr * cr + ci * ci) * wrow[b1];
-                const double n2 = be2[b2], n3 = be3[b3];
-                const double plf0 = n2 - n3;
-                const double plf1 = n2 + n3 + 1.0;
-                const double f0 = perm * psisq * plf0 * d0;
-                const double f1 = perm * psisq * plf1 * d1;
-                const double fsum = f0 + f1;
-                F[idx] = fsum;
-                if (nonzero(fsum)) {
-                    atomicOr(rowbits + b1 * N + b2, 1u << b3);
-                    atomicOr(colbits + b1 * N + b3, 1u << b2);
-                }
+                return cr * cr + ci * ci;
             }
-        }
+        });
         __syncthreads();
         if constexpr (ADJ) {
             // d L / d|Psi_b|^2 = lam[row(b1)] * nred * dF_b/d|Psi_b|^2 (Gamma += nred * sum F);
@@ -569,59 +461,8 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
             }
             continue;
         }
-        // ---- R2 = sum over b3, R3 = sum over b2 (into B as doubles) ----
-        double *R3 = (double *)B;
-        for (int e = tid; e < 2 * N2; e += bd) {
-            double sum = 0.0;
-            if (e < N2) {
-                for (uint32_t bits = rowbits[e]; bits; bits &= bits - 1) sum += F[e * N + __ffs(bits) - 1];
-                R2[e] = sum;
-            } else {
-                const int e3 = e - N2, b1 = e3 / N, b3 = e3 % N;
-                for (uint32_t bits = colbits[e3]; bits; bits &= bits - 1)
-                    sum += F[(b1 * N + __ffs(bits) - 1) * N + b3];
-                R3[e3] = sum;
-            }
-        }
-        __syncthreads();
-        if (tid < N) {
-            const int row = rowid[tid];
-            if (row >= 0) {
-                double g = 0.0;
-                for (int b2 = 0; b2 < N; ++b2) g += R2[tid * N + b2];
-                if (nonzero(g)) atomicAdd(a.gamma + row, (double)nred * g);
-            }
-        }
-        // the Xi row terms 2 F om/om1 of each entry, computed once for all equivalent triplets
-        // (after Gamma has read R2)
-        __syncthreads();
-        for (int e = tid; e < 2 * N2; e += bd) {
-            if (e < N2) {
-                const double v = R2[e];
-                R2[e] = nonzero(v) ? 2.0 * v * om2[e % N] * inv1[e / N] : 0.0;
-            } else {
-                const int e3 = e - N2;
-                const double v = R3[e3];
-                R3[e3] = nonzero(v) ? 2.0 * v * om3[e3 % N] * inv1[e3 / N] : 0.0;
-            }
-        }
-        __syncthreads();
-        for (int i = tid; i < 2 * N2 * nred; i += bd) {
-            const int r = i / (2 * N2), e = i % (2 * N2);
-            const int2 pr = red[r];
-            if (e < N2) {
-                const int b1 = e / N, b2 = e % N;
-                const int row = rowid[b1];
-                const double v = R2[e];
-                if (row >= 0 && nonzero(v)) atomicAdd(a.od + row * ld + (int64_t)pr.x * N + b2, v);
-            } else {
-                const int e3 = e - N2, b1 = e3 / N, b3 = e3 % N;
-                const int row = rowid[b1];
-                const double v = R3[e3];
-                if (row >= 0 && nonzero(v)) atomicAdd(a.od + row * ld + (int64_t)pr.y * N + b3, v);
-            }
-        }
-        __syncthreads();
+        // ---- R2 = sum over b3, R3 = sum over b2 (into B as doubles), Gamma and Xi ----
+        k3_sums_scatter<N>(S, a, nred);
     }
     if constexpr (ADJ) {
         if (a.acc_in_smem) {

@@ -1,0 +1,472 @@
+// Fused three-phonon kernel with the Psi contraction on the tcgen05 tensor cores, for
+// small cells (9, 12 or 15 modes; mixed precision). One CTA of 256 threads takes one
+// accepted irreducible q-triplet at a time (persistent grid-stride loop, several CTAs per
+// SM so that one CTA's SIMT stages overlap another's tensor-core stages).
+//
+// Reference (src/thermal_conductivity/scattering_threephonon.f90):
+//   pretransform_phi3 (:275-317)      P(a,b,c) = sum_t mwm_t(i,j,k) exp(-2 pi i (q2.lv2 + q3.lv3))
+//   zgeru x2 + dot_product (:93-113)   Psi(b1,b2,b3) = sum_abc E1(a,b1) E2(b,b2) E3(c,b3) P(a,b,c)
+//   get_dirac (:219-271) and accumulation (:115-135), shared with the SIMT kernel (k3_parts.cuh).
+//
+// Contraction. With the modes padded to 16, each of the three stages contracts one
+// component index of a 16^3 complex tensor with one eigenvector matrix E (16 x 16 complex,
+// e/sqrt(omega), not conjugated), as a real GEMM with M = 256 rows (the two uncontracted
+// indices, two M = 128 tiles), K = 32 and N = 32:
+//   [Yr | Yi] = [Xr | Xi] [[Er, Ei], [-Ei, Er]]
+//   stage 1: rows (b, c), k = a   -> T1 columns b1
+//   stage 2: rows (b1, c), k = b  -> T2 columns b2
+//   stage 3: rows (b1, b2), k = c -> Psi columns b3
+// Operands are BF16 hi/lo splits of FP32 values (x = hi + lo, about 16 significant bits);
+// a product is hi*hi + hi*lo + lo*hi accumulated in FP32 in tensor memory (2 accumulators
+// of 32 columns). The B operands (the real-split E of every mesh point, 4 KB each) are
+// built once per context and brought into shared memory by bulk copies on an mbarrier;
+// each stage's accumulator rows are read by the thread of that row (tcgen05.ld), split and
+// stored as the next stage's A operand, with the index rotation of the table above, in
+// 8 x 16-byte core matrices without swizzle (stage 1 and 2 MN-major, stage 3 K-major). The
+// padding (modes and components 15, or 9-15 / 12-15) is zero in P and E and stays exactly
+// zero through the stages.
+//
+// Pretransform. The force constants are read in a per-block transposed copy (block = atom
+// triple, triplets of a block consecutive and padded to 4), so that the thread of one
+// output element reads its block's values with 16-byte loads; the phase factors are exact
+// roots of unity from the mesh table, computed once per q-triplet into shared memory.
+//
+// Every wait is bounded: an MMA or copy that does not complete within about 1 s makes all
+// threads leave together (the decision is a barrier reduction), after waiting for their
+// copies and MMAs in flight (bounded as well); the tensor memory is freed and the status
+// word reports the timeout.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstring>
+
+#include "dev_common.cuh"
+#include "k3_parts.cuh"
+#include "tc_common.cuh"
+#include "tdg_internal.cuh"
+
+namespace tdg {
+
+namespace {
+
+constexpr int kTcThreads = 256;
+constexpr int kEImgBytes = 4096;           // one real-split E: hi plane + lo plane, 32 x 32 BF16 each
+constexpr int kAPlane = 16384;             // one A plane: 256 rows x 32 k x 2 bytes
+constexpr long long kTcWait = 2000000000LL;  // about 1 s at 2 GHz
+
+// Shared-memory layout (bytes) of the tensor-core kernel for mode count n and nt
+// force-constant triplets. Region X holds the A operand (hi, lo), the three E images and
+// the phase factors while Psi is formed; afterwards the survivor queue and the dense F
+// reuse it.
+struct TcLayout {
+    size_t A, E, ph, Q, F, psq, om, f32, v, masks, rowid, red, wsum, mbar, tslot, total;
+};
+__host__ __device__ inline size_t tc_al(size_t x, size_t a = 16) { return (x + a - 1) / a * a; }
+__host__ __device__ inline TcLayout tc_layout(int n, int nt) {
+    TcLayout L;
+    const size_t n2 = (size_t)n * n, n3 = n2 * n;
+    L.A = 0;
+    L.E = 2 * kAPlane;
+    L.ph = L.E + 3 * kEImgBytes;
+    const size_t x_end = L.ph + tc_al(sizeof(float2) * ((size_t)nt + 4));
+    L.Q = 0;
+    L.F = tc_al(sizeof(uint32_t) * n3);
+    const size_t y_end = L.F + sizeof(double) * n3;
+    size_t o = tc_al(x_end > y_end ? x_end : y_end, 128);
+    L.psq = o; o += tc_al(sizeof(float) * n3);  // |Psi|^2, then the row and column sums (2 n^2 doubles)
+    L.om = o; o += 9 * tc_al(sizeof(double) * n) + tc_al(sizeof(double) * n);  // om1..3 inv1 be2 be3 s1..3, wrow
+    L.v = o; o += 3 * tc_al(sizeof(double) * 3 * n);
+    L.f32 = o; o += tc_al(sizeof(float) * 6 * n);
+    L.masks = o; o += tc_al(sizeof(uint32_t) * (3 * n + 2 + 2 * n2));
+    L.rowid = o; o += tc_al(sizeof(int) * n);
+    L.red = o; o += tc_al(sizeof(int2) * kMaxRed);
+    L.wsum = o; o += tc_al(sizeof(int) * 33);
+    L.mbar = o; o += 16;
+    L.tslot = o; o += 16;
+    L.total = o;
+    return L;
+}
+
+// Byte offset of element (m, k) in a 256 x 32 A plane: core matrices of 8 rows x 16 bytes,
+// M groups 128 bytes apart, K groups 4096 bytes apart. MN-major: a core's 8 rows are 8 k,
+// each 8 consecutive m; K-major: its rows are 8 m, each 8 consecutive k.
+__device__ __forceinline__ uint32_t a_off_mn(int m, int k) {
+    return (uint32_t)(((m >> 3) << 7) + ((k >> 3) << 12) + ((k & 7) << 4) + ((m & 7) << 1));
+}
+
+__device__ __forceinline__ void st_split(unsigned char *plane_hi, uint32_t off, float x) {
+    unsigned short h, l;
+    tc::split_bf16(x, h, l);
+    *(unsigned short *)(plane_hi + off) = h;
+    *(unsigned short *)(plane_hi + kAPlane + off) = l;
+}
+
+// 32 lanes x 32 consecutive columns: thread i of the warp gets lane (base lane + i).
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// exp(-2 pi i (q2.lv2 + q3.lv3)) of force-constant triplet t as an exact root of unity
+// (see the SIMT kernel): u2, u3 hold g_d L/N_d of q2 and q3.
+__device__ __forceinline__ float2 tc_phase(const Fc3Dev &fc, const MeshDev &m, const int *u2, const int *u3, int t) {
+    const int32_t *lv = fc.lv + (size_t)t * 6;
+    int S = 0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) S += u2[d] * lv[d] + u3[d] * lv[3 + d];
+    int K = S % m.L;
+    if (K < 0) K += m.L;
+    return fc.twiddle32[K];
+}
+
+// One stage: 2 tiles x 2 K chunks x 3 split products of 128 x 32 x 16, issued by one thread.
+__device__ __forceinline__ void issue_stage(uint32_t tbase, uint32_t a_base, uint32_t e_base, bool a_mn) {
+    const uint32_t idesc = tc::idesc_bf16_f32(128, 32, a_mn, true);
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+#pragma unroll
+            for (int p = 0; p < 3; ++p) {
+                const uint32_t pa = p == 2 ? kAPlane : 0u, pb = p == 1 ? 2048u : 0u;
+                const uint64_t ad = tc::smem_desc(a_base + pa + 2048u * t + 8192u * j, 4096u, 128u);
+                const uint64_t bd = tc::smem_desc(e_base + pb + 1024u * j, 512u, 128u);
+                tc::mma_bf16(tbase + 32u * t, ad, bd, idesc, (j | p) ? 1u : 0u);
+            }
+        }
+    }
+}
+
+template <int N>
+__global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a) {
+    constexpr int N2 = N * N, N3 = N2 * N;
+    constexpr int NA = N / 3;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const Fc3Dev &fc = a.fc;
+    const MeshDev &m = a.mesh;
+    const PhononDev &P = a.ph;
+    const TcLayout L = tc_layout(N, fc.n);
+    unsigned char *Aop = smem + L.A;
+    unsigned char *Eimg = smem + L.E;
+    float2 *ph = (float2 *)(smem + L.ph);
+    float *psq = (float *)(smem + L.psq);
+    uint64_t *mb = (uint64_t *)(smem + L.mbar);  // [0] E-image copies, [1] MMA completion
+    uint32_t *tslot = (uint32_t *)(smem + L.tslot);
+    K3Smem S;
+    {
+        double *d = (double *)(smem + L.om);
+        const size_t dn = tc_al(sizeof(double) * N) / sizeof(double);
+        S.om1 = d; S.om2 = d + dn; S.om3 = d + 2 * dn; S.inv1 = d + 3 * dn; S.be2 = d + 4 * dn; S.be3 = d + 5 * dn;
+        S.s1 = d + 6 * dn; S.s2 = d + 7 * dn; S.s3 = d + 8 * dn; S.wrow = d + 9 * dn;
+        double *v = (double *)(smem + L.v);
+        const size_t dv = tc_al(sizeof(double) * 3 * N) / sizeof(double);
+        S.v1 = v; S.v2 = v + dv; S.v3 = v + 2 * dv;
+        float *f = (float *)(smem + L.f32);
+        S.fo1 = f; S.fo2 = f + N; S.fo3 = f + 2 * N; S.fs1 = f + 3 * N; S.fs2 = f + 4 * N; S.fs3 = f + 5 * N;
+        uint32_t *mk = (uint32_t *)(smem + L.masks);
+        S.m12 = mk; S.m13 = mk + N; S.m23 = mk + 2 * N; S.zmask = mk + 3 * N;
+        S.rowbits = S.zmask + 2; S.colbits = S.rowbits + N2;
+        S.R2 = (double *)(smem + L.psq);  // |Psi|^2 is dead when the sums start
+        S.R3 = S.R2 + N2;
+        S.F = (double *)(smem + L.F);
+        S.Q = (uint32_t *)(smem + L.Q);
+        S.rowid = (int *)(smem + L.rowid);
+        S.red = (int2 *)(smem + L.red);
+        S.wsum = (int *)(smem + L.wsum);
+    }
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int it = P.integrationtype;
+    const float sigfix32 = (float)P.sigma_fixed;
+
+    if (warp == 0) tc::tmem_alloc(tslot, 64);
+    if (tid == 0) {
+        tc::mbar_init(&mb[0], 1);
+        tc::mbar_init(&mb[1], 1);
+        tc::fence_mbar_init();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tbase = *tslot;
+    // this thread's accumulator row: tile t = warp / 4, lane 32 (warp % 4) + lane
+    const int tile = warp >> 2;
+    const int row = tid & 127;
+    const int mrow = 128 * tile + row;  // row of the 256-row operand (two uncontracted indices, 16 x 16)
+    const uint32_t taddr = tbase + ((uint32_t)(32 * (warp & 3)) << 16) + 32u * (uint32_t)tile;
+    const uint32_t a_u = tc::smem_u32(Aop), e_u = tc::smem_u32(Eimg);
+    uint32_t e_ph = 0, m_ph = 0;
+    bool ok = true;
+
+    for (int t = blockIdx.x; t < a.n_trip && ok; t += gridDim.x) {
+        const TripletRec rec = a.trip[t];
+        const int f1 = m.irr_full[rec.q1];
+        const int q2 = rec.q2, q3 = rec.q3;
+        const int i2 = m.full_irr[q2], i3 = m.full_irr[q3];
+        const int nred = rec.red_cnt;
+        const double perm = (q2 == q3) ? 1.0 : 2.0;
+        // E images of q1, q2, q3 into shared memory (the region was last read by the previous
+        // q-triplet's MMAs and reused by its F, both finished before the last barrier)
+        if (tid == 0) {
+            tc::fence_async_smem();  // the generic accesses of the region (ordered by the last barrier) come first
+            tc::mbar_arrive_expect_tx(&mb[0], 3u * kEImgBytes);
+            tc::bulk_g2s(e_u, a.tc_eimg + (size_t)f1 * kEImgBytes, kEImgBytes, &mb[0]);
+            tc::bulk_g2s(e_u + kEImgBytes, a.tc_eimg + (size_t)q2 * kEImgBytes, kEImgBytes, &mb[0]);
+            tc::bulk_g2s(e_u + 2 * kEImgBytes, a.tc_eimg + (size_t)q3 * kEImgBytes, kEImgBytes, &mb[0]);
+        }
+        k3_load_modes<N>(S, a, rec, f1, q2, q3, i2, i3);
+        // A operand zeroed (padding must be exact zeros), phase factors of all triplets
+        for (int i = tid; i < 2 * kAPlane / 16; i += kTcThreads) ((uint4 *)Aop)[i] = make_uint4(0u, 0u, 0u, 0u);
+        {
+            int u2[3], u3[3];
+            const int n12 = m.grid[1] * m.grid[2];
+            u2[0] = q2 / n12; u2[1] = (q2 / m.grid[2]) % m.grid[1]; u2[2] = q2 % m.grid[2];
+            u3[0] = q3 / n12; u3[1] = (q3 / m.grid[2]) % m.grid[1]; u3[2] = q3 % m.grid[2];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                u2[d] *= m.lmul[d];
+                u3[d] *= m.lmul[d];
+            }
+            for (int i = tid; i < fc.n + 4; i += kTcThreads)
+                ph[i] = i < fc.n ? tc_phase(fc, m, u2, u3, i) : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+        k3_skip_masks<N>(S);
+        // ---- pretransform into the stage-1 operand: rows (b, c), k = a (re) and 16 + a (im) ----
+        for (int idx = tid; idx < N3; idx += kTcThreads) {
+            const int blk = idx / 27, ijk = idx - 27 * blk;
+            const int lo = fc.blk_ptr[blk];
+            const int o0 = a.tc_toff[blk], pc = (a.tc_toff[blk + 1] - o0) / 27;
+            const float4 *mr = (const float4 *)(a.tc_fct + o0 + ijk * pc);
+            float ar = 0.f, ai = 0.f;
+            for (int j = 0; j < pc; j += 4) {
+                const float4 mv = __ldg(mr + (j >> 2));
+                const float2 p0 = ph[lo + j], p1 = ph[lo + j + 1], p2 = ph[lo + j + 2], p3 = ph[lo + j + 3];
+                ar = fmaf(mv.x, p0.x, ar); ai = fmaf(mv.x, p0.y, ai);
+                ar = fmaf(mv.y, p1.x, ar); ai = fmaf(mv.y, p1.y, ai);
+                ar = fmaf(mv.z, p2.x, ar); ai = fmaf(mv.z, p2.y, ai);
+                ar = fmaf(mv.w, p3.x, ar); ai = fmaf(mv.w, p3.y, ai);
+            }
+            const int a1 = blk / (NA * NA), a2 = (blk / NA) % NA, a3 = blk % NA;
+            const int pa = 3 * a1 + ijk % 3, pb = 3 * a2 + (ijk / 3) % 3, pcc = 3 * a3 + ijk / 9;
+            const uint32_t off = a_off_mn(16 * pb + pcc, pa);
+            st_split(Aop, off, ar);
+            st_split(Aop, off + 8192u, ai);
+        }
+        // ---- three contraction stages ----
+#pragma unroll 1
+        for (int stage = 0; stage < 3; ++stage) {
+            tc::fence_async_smem();
+            tc::fence_before_sync();
+            __syncthreads();
+            if (tid == 0) {
+                tc::fence_after_sync();
+                bool go = true;
+                if (stage == 0) {
+                    go = tc::mbar_wait(&mb[0], e_ph, kTcWait);
+                    if (go) e_ph ^= 1u;  // else the abort path waits on the same phase again
+                }
+                if (go) {
+                    issue_stage(tbase, a_u, e_u + (uint32_t)stage * kEImgBytes, stage < 2);
+                    tc::mma_commit(&mb[1]);
+                }
+            }
+            const bool done = tc::mbar_wait(&mb[1], m_ph, kTcWait);
+            ok = __syncthreads_and(done) != 0;
+            if (!ok) break;  // m_ph unchanged: the abort path waits on that phase again
+            m_ph ^= 1u;
+            tc::fence_after_sync();
+            float v[32];
+            tmem_ld32(taddr, v);
+            if (stage == 0) {
+                // row (b, c) of T1 over b1 -> stage-2 operand rows (b1, c), k = b (MN-major)
+                const int b = mrow >> 4, c = mrow & 15;
+                const uint32_t base = (uint32_t)(((c >> 3) << 7) + ((b >> 3) << 12) + ((b & 7) << 4) + ((c & 7) << 1));
+#pragma unroll
+                for (int b1 = 0; b1 < 16; ++b1) {
+                    st_split(Aop, base + 256u * b1, v[b1]);
+                    st_split(Aop, base + 256u * b1 + 8192u, v[16 + b1]);
+                }
+            } else if (stage == 1) {
+                // row (b1, c) of T2 over b2 -> stage-3 operand rows (b1, b2), k = c (K-major)
+                const int b1 = mrow >> 4, c = mrow & 15;
+                const uint32_t base = (uint32_t)(256 * b1 + ((c >> 3) << 12) + ((c & 7) << 1));
+#pragma unroll
+                for (int b2 = 0; b2 < 16; ++b2) {
+                    st_split(Aop, base + 16u * b2, v[b2]);
+                    st_split(Aop, base + 16u * b2 + 8192u, v[16 + b2]);
+                }
+            } else {
+                // row (b1, b2) of Psi over b3 -> |Psi|^2 of the valid modes
+                const int b1 = mrow >> 4, b2 = mrow & 15;
+                if (b1 < N && b2 < N) {
+#pragma unroll
+                    for (int b3 = 0; b3 < N; ++b3) psq[(b1 * N + b2) * N + b3] = v[b3] * v[b3] + v[16 + b3] * v[16 + b3];
+                }
+            }
+        }
+        if (!ok) break;
+        tc::fence_before_sync();
+        // ---- FP32 screen of the Gaussians, survivors queued, FP64 weights ----
+        uint32_t live_lo = 0u, live_hi = 0u, live_x = 0u;
+        int nsurv = 0;
+        const int b1 = mrow >> 4, b2 = mrow & 15;
+        const bool mine = b1 < N && b2 < N;
+        if (mine) nsurv = k3_screen<N>(S, it, sigfix32, b1, b2, live_lo, live_hi, live_x);
+        int nq = 0;
+        const int off = block_exclusive_scan(nsurv, S.wsum, nq);  // contains barriers: the operands are dead
+        if (mine && nsurv) k3_enqueue<N>(S, b1 * N + b2, off, live_lo, live_hi, live_x);
+        for (int i = tid; i < N3; i += kTcThreads) S.F[i] = 0.0;
+        __syncthreads();
+        k3_survivors<N>(S, P, nq, perm, [&](int idx) -> double { return (double)psq[idx]; });
+        k3_sums_scatter<N>(S, a, nred);
+    }
+    if (!ok) {
+        // a wait ran out: record it, let the copies and MMAs in flight finish (bounded), free
+        // the tensor memory
+        if (tid == 0) {
+            atomicExch(a.status, (int32_t)kDevTimeout);
+            tc::mbar_wait(&mb[0], e_ph, kTcWait);
+            tc::mbar_wait(&mb[1], m_ph, kTcWait);
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::tmem_dealloc(tbase, 64);
+}
+
+// Per-block transposed copy of the FP32 force constants: block b (atom triple) holds its
+// triplets' 27 values as [ijk][triplet], the triplet count padded to 4 with zeros; toff[b]
+// is the block's first float and toff[n_blk] the total. One CTA.
+__global__ void k_tc_prep_fc(const int32_t *blk_ptr, int32_t n_blk, const float *mwm32, int32_t *toff, float *out) {
+    __shared__ int32_t s_off[256 + 1];
+    if (threadIdx.x == 0) {
+        int32_t o = 0;
+        for (int b = 0; b < n_blk; ++b) {
+            s_off[b] = o;
+            const int32_t c = blk_ptr[b + 1] - blk_ptr[b];
+            o += 27 * ((c + 3) & ~3);
+        }
+        s_off[n_blk] = o;
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b <= n_blk; b += blockDim.x) toff[b] = s_off[b];
+    for (int b = 0; b < n_blk; ++b) {
+        const int32_t lo = blk_ptr[b], c = blk_ptr[b + 1] - lo, pc = (c + 3) & ~3;
+        for (int e = threadIdx.x; e < 27 * pc; e += blockDim.x) {
+            const int ijk = e / pc, j = e - ijk * pc;
+            out[s_off[b] + e] = j < c ? mwm32[(size_t)(lo + j) * 27 + ijk] : 0.f;
+        }
+    }
+}
+
+// Real-split eigenvector images of every mesh point: B = [[Er, Ei], [-Ei, Er]] (32 x 32,
+// row k = component a (re) / 16 + a, column = mode b (re) / 16 + b), E = egvs32 padded with
+// zeros, split into BF16 hi and lo planes, MN-major core matrices (N groups 128 bytes apart,
+// K groups 512 bytes apart).
+__global__ void k_tc_eimg(int32_t n_full, int32_t n, const float2 *egvs32, unsigned char *out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)n_full * 1024) return;
+    const int q = (int)(i >> 10), e = (int)(i & 1023);
+    const int k = e >> 5, c = e & 31;
+    const int aa = k & 15, b = c & 15;
+    const bool kim = k >= 16, cim = c >= 16;
+    float2 z = make_float2(0.f, 0.f);
+    if (aa < n && b < n) z = egvs32[((size_t)q * n + b) * n + aa];
+    const float x = (kim == cim) ? z.x : (kim ? -z.y : z.y);
+    unsigned short h, l;
+    tc::split_bf16(x, h, l);
+    const uint32_t off = (uint32_t)(((c >> 3) << 7) + ((k >> 3) << 9) + ((k & 7) << 4) + ((c & 7) << 1));
+    unsigned char *img = out + (size_t)q * kEImgBytes;
+    *(unsigned short *)(img + off) = h;
+    *(unsigned short *)(img + 2048 + off) = l;
+}
+
+template <int N>
+int tc_grid(const ThreePhArgs &a, int n_sm, int ctas_per_sm) {
+    const size_t bytes = tc_layout(N, a.fc.n).total;
+    if (cudaFuncSetAttribute(k_threephonon_tc<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_threephonon_tc<N>, kTcThreads, bytes) !=
+            cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        return 0;
+    }
+    // tensor memory: 64 columns per CTA, 512 per SM
+    if (per_sm > 8) per_sm = 8;
+    if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
+    const int grid = n_sm * per_sm;
+    return grid > a.n_trip ? (a.n_trip > 0 ? a.n_trip : 1) : grid;
+}
+
+template <int N>
+cudaError_t tc_launch(const ThreePhArgs &a, int n_sm, int ctas_per_sm, cudaStream_t s) {
+    const int grid = tc_grid<N>(a, n_sm, ctas_per_sm);
+    if (grid < 1) return cudaErrorInvalidConfiguration;
+    k_threephonon_tc<N><<<grid, kTcThreads, tc_layout(N, a.fc.n).total, s>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+bool threephonon_tc_supported(int n, int precision, int n_fc) {
+    if (precision == 0 || (n != 9 && n != 12 && n != 15)) return false;
+    return tc_layout(n, n_fc).total <= 110 * 1024;  // at least two CTAs per SM
+}
+
+int threephonon_tc_max_per_sm(int n, int n_fc) {
+    ThreePhArgs a;
+    memset(&a, 0, sizeof a);
+    a.fc.n = n_fc;
+    a.n_trip = 1 << 30;
+    switch (n) {
+        case 9: return tc_grid<9>(a, 1, 0);
+        case 12: return tc_grid<12>(a, 1, 0);
+        case 15: return tc_grid<15>(a, 1, 0);
+        default: return 0;
+    }
+}
+
+cudaError_t launch_threephonon_tc(const ThreePhArgs &a, int n_sm, int ctas_per_sm, cudaStream_t s) {
+    if (a.n_trip <= 0) return cudaSuccess;
+    switch (a.mesh.n_mode) {
+        case 9: return tc_launch<9>(a, n_sm, ctas_per_sm, s);
+        case 12: return tc_launch<12>(a, n_sm, ctas_per_sm, s);
+        case 15: return tc_launch<15>(a, n_sm, ctas_per_sm, s);
+        default: return cudaErrorNotSupported;
+    }
+}
+
+size_t tc_fct_floats(int n_fc, int n_blk) { return 27 * ((size_t)n_fc + 3 * (size_t)n_blk); }
+
+cudaError_t launch_tc_prep_fc(const int32_t *blk_ptr, int32_t n_blk, const float *mwm32, int32_t *toff, float *out,
+                              cudaStream_t s) {
+    if (n_blk > 256) return cudaErrorInvalidValue;
+    k_tc_prep_fc<<<1, 256, 0, s>>>(blk_ptr, n_blk, mwm32, toff, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tc_eimg(int32_t n_full, int32_t n, const float2 *egvs32, unsigned char *out, cudaStream_t s) {
+    if (n > 16) return cudaErrorInvalidValue;
+    const int64_t total = (int64_t)n_full * 1024;
+    k_tc_eimg<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(n_full, n, egvs32, out);
+    return cudaGetLastError();
+}
+
+}  // namespace tdg

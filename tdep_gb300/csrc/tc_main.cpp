@@ -172,7 +172,8 @@ int main(int argc, char **argv) {
     // main.f90:219-244: single-mode, off-diagonal (coherence) and collective contributions
     st = tdg_kappa_offdiag(ctx, &o, koff);
     if (st) return die(st);
-    st = tdg_kappa(ctx, &o, itermax, itertol, ksma, kiter, nullptr, &nit);
+    std::vector<double> fn((size_t)cap * 3);
+    st = tdg_kappa(ctx, &o, itermax, itertol, ksma, kiter, fn.data(), &nit);
     if (st) return die(st);
     const auto t3 = std::chrono::steady_clock::now();
     std::printf(" ... iterative solution: %d iterations\n", nit);
@@ -180,6 +181,10 @@ int main(int argc, char **argv) {
                 (kiter[0] + koff[0]) * kKappaAuToSI, (kiter[4] + koff[4]) * kKappaAuToSI,
                 (kiter[8] + koff[8]) * kKappaAuToSI);
     st = tdg_write_outfile(dir.c_str(), o.temperature, ksma, kiter, koff);
+    if (st) return die(st);
+    // main.f90:339: the per-mode data of the full mesh
+    st = tdg_write_grid_hdf5((dir + "/outfile.thermal_conductivity_grid.hdf5").c_str(), prob, o.temperature, lw.data(),
+                             fn.data());
     if (st) return die(st);
     auto ms = [](auto a, auto b) { return std::chrono::duration<double, std::milli>(b - a).count(); };
     std::printf(" Timings (ms): init %.1f  scattering %.1f  kappa %.1f\n", ms(t0, t1), ms(t1, t2), ms(t2, t3));

@@ -191,6 +191,13 @@ struct tdg_ctx {
     std::vector<int> fc3_perm;  // device (block-sorted) position -> index in the problem
     DevBuf<double> fc3_mwm, fc4_mwm;
     DevBuf<float> fc3_mwm32, fc4_mwm32;
+    // tensor-core fused kernel (9-15 modes, mixed): eigenvector images built on first use,
+    // transposed force constants rebuilt by every call (tdg_set_fc3 may change them)
+    DevBuf<unsigned char> d_tc_eimg;
+    DevBuf<float> d_tc_fct;
+    DevBuf<int32_t> d_tc_toff;
+    bool tc_eimg_ready = false;
+    int last_path = -1;  // 0 SIMT fused kernel, 1 tensor-core fused kernel, 2 large-cell batches
     DevBuf<double2> tw;
     DevBuf<float2> tw32;
     DevBuf<double> d_exp2tab, d_invom;
@@ -412,6 +419,12 @@ void destroy_ctx(tdg_ctx *c) {
     pt.mark("stream");
 }
 }  // namespace
+
+extern "C" int tdg_last_path(tdg_ctx *c, int32_t *path) {
+    if (!c || !path) return set_error(kErrParam, "tdg_last_path: null argument");
+    *path = c->last_path;
+    return kOk;
+}
 
 extern "C" int tdg_graph_counts(tdg_ctx *c, int64_t *counts) {
     if (!c || !counts) return set_error(kErrParam, "tdg_graph_counts: null argument");
@@ -696,7 +709,7 @@ int validate_opts(const tdg_opts *o) {
     if (o->integrationtype == 1 && !(o->sigma > 0)) return set_error(kErrParam, "sigma must be positive");
     if (o->precision != TDG_PREC_FP64 && o->precision != TDG_PREC_MIXED)
         return set_error(kErrParam, "precision must be TDG_PREC_FP64 or TDG_PREC_MIXED");
-    if (o->tensor_cores != 0 && o->tensor_cores != 1) return set_error(kErrParam, "tensor_cores must be 0 or 1");
+    if (o->tensor_cores < 0 || o->tensor_cores > 2) return set_error(kErrParam, "tensor_cores must be 0, 1 or 2");
     if (o->tensor_cores == 1 && o->precision != TDG_PREC_MIXED)
         return set_error(kErrParam, "the tensor-core contraction needs precision TDG_PREC_MIXED");
     return kOk;
@@ -1339,7 +1352,26 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         a.gamma = c->d_gamma.p;
         a.od = c->d_xi.p;
         a.status = c->d_status.p;
-        c->last_ln = n > 18 || o->tensor_cores;
+        c->last_ln = n > 18 || o->tensor_cores == 1;
+        const char *tc_env = std::getenv("TDG_TC_SMALL");
+        const bool use_tc = !c->last_ln && o->tensor_cores != 2 && !(tc_env && tc_env[0] == '0') &&
+                            threephonon_tc_supported(n, o->precision, c->n_fc3);
+        c->last_path = c->last_ln ? 2 : (use_tc ? 1 : 0);
+        if (use_tc) {
+            if (!c->tc_eimg_ready) {
+                chk(c->d_tc_eimg.alloc((size_t)N * 4096));
+                if (e != cudaSuccess)
+                    return set_error(kErrDevice, std::string("allocation failed: ") + cudaGetErrorString(e));
+                CUDA_TRY(launch_tc_eimg(N, n, c->d_egvs32.p, c->d_tc_eimg.p, s));
+                c->tc_eimg_ready = true;
+            }
+            chk(c->d_tc_fct.alloc(tc_fct_floats(c->n_fc3, c->na * c->na * c->na)));
+            chk(c->d_tc_toff.alloc((size_t)c->na * c->na * c->na + 1));
+            if (e != cudaSuccess) return set_error(kErrDevice, std::string("allocation failed: ") + cudaGetErrorString(e));
+            a.tc_eimg = c->d_tc_eimg.p;
+            a.tc_fct = c->d_tc_fct.p;
+            a.tc_toff = c->d_tc_toff.p;
+        }
         // the launch shape comes first (autotuner trials run outside any graph), then the
         // three-phonon part of the pipeline runs directly or as the context's graph
         // graph key: every value the recorded launches bake in (kernel-argument bytes, with
@@ -1386,21 +1418,26 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
             launches += 6 * ((ntrip + nbmax - 1) / std::max(nbmax, 1));
         } else {
             // persistent grid (CTAs per SM), timed on a prefix of the q-triplets
-            const int maxps = threephonon_max_per_sm(n, o->precision);
+            const int maxps = use_tc ? threephonon_tc_max_per_sm(n, c->n_fc3) : threephonon_max_per_sm(n, o->precision);
             std::vector<int> cand;
             for (int v : {maxps, (3 * maxps + 3) / 4, (maxps + 1) / 2})
                 if (v >= 1 && std::find(cand.begin(), cand.end(), v) == cand.end()) cand.push_back(v);
-            const std::string key = tune_key("threephonon", n, o->precision, c->device);
+            const std::string key = tune_key(use_tc ? "threephonon_tc" : "threephonon", n, o->precision, c->device);
+            auto fused = [&, use_tc](const ThreePhArgs &x, int v) -> cudaError_t {
+                if (!use_tc) return launch_threephonon(x, o->precision, c->n_sm, v, s);
+                const cudaError_t ep = launch_tc_prep_fc(c->fc3_blk.p, c->na * c->na * c->na, c->fc3_mwm32.p,
+                                                         c->d_tc_toff.p, c->d_tc_fct.p, s);
+                if (ep != cudaSuccess) return ep;
+                return launch_threephonon_tc(x, c->n_sm, v, s);
+            };
             bool tuned = false;
             ThreePhArgs ta = a;
             ta.n_trip = std::min(ntrip, std::max(ntrip / 8, 64 * c->n_sm * std::max(maxps, 1)));
-            CUDA_TRY(tune_pick(key, cand, 0,
-                               [&](int v) { return launch_threephonon(ta, o->precision, c->n_sm, v, s); }, s, cps,
-                               tuned));
+            CUDA_TRY(tune_pick(key, cand, 0, [&](int v) { return fused(ta, v); }, s, cps, tuned));
             if (tuned) CUDA_TRY(rezero_outputs(c, nr, ld, s));
-            gk << "f" << cps << '/' << std::string(reinterpret_cast<const char *>(&a), sizeof a);
-            body3 = [&]() { return launch_threephonon(a, o->precision, c->n_sm, cps, s); };
-            ++launches;
+            gk << (use_tc ? "t" : "f") << cps << '/' << std::string(reinterpret_cast<const char *>(&a), sizeof a);
+            body3 = [&, fused]() { return fused(a, cps); };
+            launches += use_tc ? 2 : 1;
         }
         CUDA_TRY(run_graph_region(c, c->graph3, gk.str(), s, body3));
         // (events recorded inside a graph cannot be timed against the others: ev[3] stays out)

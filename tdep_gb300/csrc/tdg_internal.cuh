@@ -117,7 +117,7 @@ struct Fc4Dev {
 };
 
 // Device status word: kernels record the first failed check here.
-enum DevStatus : int32_t { kDevOk = 0, kDevBadIndex = 1, kDevOverflow = 2 };
+enum DevStatus : int32_t { kDevOk = 0, kDevBadIndex = 1, kDevOverflow = 2, kDevTimeout = 3 };
 
 // ---- launch wrappers (each returns cudaError_t of the launch) ----
 // K1: count/fill passes of the irreducible-triplet enumeration.
@@ -151,6 +151,11 @@ struct ThreePhArgs {
     const double *lam;
     double *mwm_bar;            // FP64 slices, zeroed before the launch
     int32_t acc_in_smem;        // accumulate the CTA's slice in shared memory, store it once
+    // tensor-core kernel only (k_threephonon_tc): real-split eigenvector images of every mesh
+    // point (4 KB each), the per-block transposed FP32 force constants and their offsets
+    const unsigned char *tc_eimg;
+    const float *tc_fct;
+    const int32_t *tc_toff;
 };
 // ctas_per_sm: persistent grid of n_sm * ctas_per_sm CTAs (0 or more than fit: as many as fit).
 cudaError_t launch_threephonon(const ThreePhArgs &a, int precision, int n_sm, int ctas_per_sm, cudaStream_t s);
@@ -163,6 +168,16 @@ cudaError_t launch_threephonon_adjoint(const ThreePhArgs &a, int precision, int 
 // out[e] = sum over g < n_slice of slices[g * n + e], in slice order.
 cudaError_t launch_sum_slices(const double *slices, int32_t n_slice, int64_t n, double *out, cudaStream_t s);
 size_t threephonon_smem_bytes(int n, int precision, int n_fc);
+// Tensor-core fused kernel for 9, 12 or 15 modes in mixed precision (k_threephonon_tc.cu).
+bool threephonon_tc_supported(int n, int precision, int n_fc);
+int threephonon_tc_max_per_sm(int n, int n_fc);
+cudaError_t launch_threephonon_tc(const ThreePhArgs &a, int n_sm, int ctas_per_sm, cudaStream_t s);
+// Floats of the transposed force-constant copy, its builder (one CTA, n_blk <= 256) and the
+// eigenvector images (n <= 16).
+size_t tc_fct_floats(int n_fc, int n_blk);
+cudaError_t launch_tc_prep_fc(const int32_t *blk_ptr, int32_t n_blk, const float *mwm32, int32_t *toff, float *out,
+                              cudaStream_t s);
+cudaError_t launch_tc_eimg(int32_t n_full, int32_t n, const float2 *egvs32, unsigned char *out, cudaStream_t s);
 
 struct FourPhArgs {
     MeshDev mesh;

@@ -145,7 +145,7 @@ class Options:
     qg4ph: tuple = (-1, -1, -1)
     seed: int = 1
     precision: str = "fp64"  # "fp64" or "mixed"
-    tensor_cores: bool = False  # force the tcgen05 large-cell contraction (automatic beyond 18 modes)
+    tensor_cores: int = 0  # 0 automatic, 1 (or True) force the tcgen05 large-cell contraction, 2 SIMT fused kernel
     itertol: float = 1e-5
     itermaxsteps: int = 200
 
@@ -173,7 +173,7 @@ class Options:
         if self.precision not in ("fp64", "mixed"):
             raise ValueError("precision must be 'fp64' or 'mixed'")
         o.precision = N.TDG_PREC_FP64 if self.precision == "fp64" else N.TDG_PREC_MIXED
-        o.tensor_cores = int(bool(self.tensor_cores))
+        o.tensor_cores = int(self.tensor_cores)
         return o
 
 
@@ -333,6 +333,13 @@ class ScatteringRates:
         N.check(self._lib.tdg_kappa_offdiag(self._ctx, C.byref(o), N.ptr(k, C.c_double)), "tdg_kappa_offdiag")
         return k.reshape(3, 3, order="F")
 
+    def last_path(self) -> int:
+        """Three-phonon path of the last generate(): 0 SIMT fused kernel, 1 tcgen05 fused
+        kernel, 2 large-cell tcgen05 batches (tdg_last_path)."""
+        v = C.c_int32(-1)
+        N.check(self._lib.tdg_last_path(self._ctx, C.byref(v)), "tdg_last_path")
+        return int(v.value)
+
     def graph_counts(self) -> list[int]:
         """Direct runs, CUDA-graph recordings and replays of the three-phonon kernels on this
         context (tdg_graph_counts)."""
@@ -403,6 +410,18 @@ def write_outfile(directory, temperature, kappa_sma, kappa_iter, kappa_offdiag=N
     N.check(L.tdg_write_outfile(str(directory).encode(), float(temperature), N.ptr(ks, C.c_double),
                                 N.ptr(ki, C.c_double), N.ptr(ko, C.c_double)), "tdg_write_outfile")
     return Path(directory) / "outfile.thermal_conductivity"
+
+
+def write_grid_hdf5(path, prob: "Problem", temperature, linewidth, fn=None) -> Path:
+    """outfile.thermal_conductivity_grid.hdf5 (type_phonon_dispersions.f90:316-641): per-mode
+    data of the full mesh from the linewidths (n_irr, n_mode) of generate() and the final Fn
+    (n_irr, n_mode, 3) of kappa(), or fn=None for the relaxation-time form."""
+    lw = np.ascontiguousarray(np.asarray(linewidth, np.float64).reshape(-1))
+    f = None if fn is None else np.ascontiguousarray(np.asarray(fn, np.float64).reshape(-1))
+    ps = prob.struct()
+    N.check(N.lib().tdg_write_grid_hdf5(str(path).encode(), C.byref(ps), float(temperature), N.ptr(lw, C.c_double),
+                                        N.ptr(f, C.c_double) if f is not None else None), "tdg_write_grid_hdf5")
+    return Path(path)
 
 
 def phonon_frequencies(directory, q, qdir=None) -> np.ndarray:

@@ -23,7 +23,8 @@ from pathlib import Path
 
 import numpy as np
 
-AMU = {"Al": 26.98, "Na": 22.99, "Cl": 35.45, "Ti": 47.9, "O": 16.0, "Ba": 137.3}
+AMU = {"Al": 26.98, "Na": 22.99, "Cl": 35.45, "Ti": 47.9, "O": 16.0, "Ba": 137.3, "Ca": 40.08, "F": 19.0,
+       "Cu": 63.55, "Au": 196.97}
 
 
 # ---------------------------------------------------------------- pair potentials
@@ -118,6 +119,22 @@ def perovskite(a):
     frac = np.array([[0.0, 0.0, 0.0], [0.5, 0.5, 0.5], [0.5, 0.5, 0.0], [0.5, 0.0, 0.5], [0.0, 0.5, 0.5]])
     sp = ["Ba", "Ti", "O", "O", "O"]
     return Cell(lat, frac, sp, np.array([AMU[s] for s in sp]))
+
+
+def fluorite(a, s1, s2):
+    """AX2 fluorite (3 atoms, fcc lattice): A at 0, X at +-(1/4, 1/4, 1/4)."""
+    lat = np.array([[0, a / 2, a / 2], [a / 2, 0, a / 2], [a / 2, a / 2, 0]])
+    frac = np.array([[0.0, 0.0, 0.0], [0.25, 0.25, 0.25], [0.75, 0.75, 0.75]])
+    sp = [s1, s2, s2]
+    return Cell(lat, frac, sp, np.array([AMU[x] for x in sp]))
+
+
+def l12(a, s1, s2):
+    """AB3 L1_2 (4 atoms, simple cubic lattice): A at the corner, B at the face centres."""
+    lat = np.eye(3) * a
+    frac = np.array([[0.0, 0.0, 0.0], [0.0, 0.5, 0.5], [0.5, 0.0, 0.5], [0.5, 0.5, 0.0]])
+    sp = [s1, s2, s2, s2]
+    return Cell(lat, frac, sp, np.array([AMU[x] for x in sp]))
 
 
 def neighbours(cell, cutoff):
@@ -316,6 +333,40 @@ def config_perovskite(seed=1, cutoff=6.0):
     return cell, pot, cutoff
 
 
+def config_fluorite(seed=1):
+    """Fluorite CaF2 (a = 5.46 A, 9 modes), seeded Born-Mayer pairs plus nearest-neighbour
+    springs, cutoff between the third and fourth shells."""
+    rng = np.random.default_rng(seed)
+    a = 5.46
+    cell = fluorite(a, "Ca", "F")
+    r_cf, r_ff = a * np.sqrt(3) / 4, a / 2
+    bm = {k: born_mayer(rng.uniform(1000.0, 3000.0), _jitter(rng, 0.3)) for k in ("CaF", "FF", "CaCa")}
+    sp = {"CaF": spring(_jitter(rng, 1.5), r_cf - 0.5), "FF": spring(_jitter(rng, 0.5), r_ff - 0.5),
+          "CaCa": spring(_jitter(rng, 0.3), a / np.sqrt(2) - 0.6)}
+
+    def pot(s1, s2):
+        key = "CaF" if s1 != s2 else s1 + s2
+        return combine(bm[key], sp[key])
+
+    return cell, pot, 0.5 * (a / np.sqrt(2) + a * np.sqrt(11) / 4)
+
+
+def config_l12(seed=1):
+    """L1_2 Cu3Au (a = 3.75 A, 12 modes), seeded Morse pairs, cutoff between the second and
+    third shells."""
+    rng = np.random.default_rng(seed)
+    a = 3.75
+    cell = l12(a, "Au", "Cu")
+    r1 = a / np.sqrt(2)
+    ms = {k: morse(_jitter(rng, 0.3), _jitter(rng, 1.4), _jitter(rng, r1)) for k in ("AuCu", "CuCu", "AuAu")}
+
+    def pot(s1, s2):
+        key = "AuCu" if s1 != s2 else s1 + s2
+        return ms[key]
+
+    return cell, pot, 0.5 * (a + a * np.sqrt(1.5))
+
+
 def supercell(cell: Cell, reps, rng=None, disp=0.0) -> Cell:
     """reps[0] x reps[1] x reps[2] supercell, atoms grouped by species in first-appearance
     order, optional Gaussian displacements of standard deviation disp (A)."""
@@ -353,6 +404,8 @@ CONFIGS = {
     "rocksalt": config_rocksalt,
     "perovskite": config_perovskite,
     "perovskite_supercell": config_perovskite_supercell,
+    "fluorite": config_fluorite,
+    "l12": config_l12,
 }
 
 

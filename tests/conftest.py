@@ -32,6 +32,9 @@ def configs(tmp_path_factory, built):
         "perovskite": synth.write_config("perovskite", base / "perovskite", seed=1),
         # 10 atoms, 30 modes, no symmetry: the tensor-core path is taken automatically
         "supercell": synth.write_config("perovskite_supercell", base / "supercell", seed=1, reps=(2, 1, 1)),
+        # 3 and 4 atoms (9 and 12 modes): the tcgen05 fused kernel's other mode counts
+        "fluorite": synth.write_config("fluorite", base / "fluorite", seed=1),
+        "l12": synth.write_config("l12", base / "l12", seed=1),
     }
 
 

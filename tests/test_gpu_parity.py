@@ -498,3 +498,102 @@ def test_contexts_reuse_pooled_memory_and_release_it(configs):
     for lw, ki in out[1:]:  # equal up to the order of FP64 atomic additions
         np.testing.assert_allclose(lw, out[0][0], rtol=1e-12, atol=0)
         np.testing.assert_allclose(ki, out[0][1], rtol=1e-12, atol=0)
+
+
+def test_rocksalt16_rows_against_the_oracle(configs):
+    """Parity at a benchmarked mesh size (rocksalt 16^3, the adjoint configuration's mesh,
+    full q' grid): the oracle runs a few whole q1 groups, the GPU the whole mesh; their
+    linewidths (after degeneracy averaging) and symmetrised Xi rows must agree with the FP64
+    bars, and the mixed-precision linewidths within 1e-4."""
+    import bench
+
+    prob = Problem.load(configs["rocksalt"], (16, 16, 16), readiso=True)
+    o64 = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=1, precision="fp64")
+    o32 = Options(**{**o64.__dict__, "precision": "mixed"})
+    lists = QLists.monte_carlo(prob, o64)
+    sr = ScatteringRates(prob)
+    lw64 = sr.generate(o64, lists).copy()
+    xi64 = sr.Xi
+    lw32 = sr.generate(o32, lists).copy()
+    sr.close()
+    q1s = np.unique(lists.row_q1)
+    kept = []
+    for q1 in q1s[[1, len(q1s) // 2, -1]]:
+        rows = np.nonzero(lists.row_q1 == q1)[0]
+        r0, r1 = int(rows[0]), int(rows[-1]) + 1
+        g, x, _ = orc.scattering(prob, o64, lists, rows=(r0, r1))
+        kept.append((r0, r1, g, x))
+    idx, lw_ref, xi_ref = bench.oracle_rows_finish(prob, o64, lists, kept)
+    sel = np.unique(lists.row_q1[idx]) - 1
+    np.testing.assert_allclose(lw64[sel], lw_ref[sel], rtol=LW_RTOL, atol=1e-14 * np.abs(lw_ref).max())
+    np.testing.assert_allclose(lw32[sel], lw_ref[sel], rtol=1e-4, atol=1e-12 * np.abs(lw_ref).max())
+    _xi_flips(xi64[idx], xi_ref)
+
+
+@pytest.mark.parametrize("name,grid", [("fluorite", (6, 6, 6)), ("l12", (6, 6, 6)), ("perovskite", (5, 5, 5))])
+def test_tensor_core_fused_kernel(configs, name, grid):
+    """The tcgen05 fused kernel (9, 12 and 15 modes, mixed precision, automatic): the path is
+    taken; its linewidths agree with the oracle within 1e-4 (relative, with an absolute floor
+    of 1e-6 of the largest), Xi with the FP64 GPU path within 1e-4 of its largest entry, and
+    kappa with the FP64 path within 1e-4 (the benchmark spec's bar); it agrees with the FP32 SIMT
+    kernel (tensor_cores = 2) to the same bars."""
+    prob = Problem.load(configs[name], grid, readiso=True)
+    o64 = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=3, precision="fp64")
+    otc = Options(**{**o64.__dict__, "precision": "mixed"})
+    osimt = Options(**{**otc.__dict__, "tensor_cores": 2})
+    lists = QLists.monte_carlo(prob, o64)
+    sr = ScatteringRates(prob)
+    lw64 = sr.generate(o64, lists).copy()
+    assert sr.last_path() == 0
+    xi64 = sr.Xi
+    _, ki64 = sr.kappa(o64)
+    lwtc = sr.generate(otc, lists).copy()
+    assert sr.last_path() == 1
+    xitc = sr.Xi
+    _, kitc = sr.kappa(otc)
+    lwsimt = sr.generate(osimt, lists).copy()
+    assert sr.last_path() == 0
+    sr.close()
+    ref = orc.full_run(prob, o64, lists)
+    scale = np.abs(ref["linewidth"]).max()
+    np.testing.assert_allclose(lw64, ref["linewidth"], rtol=LW_RTOL, atol=1e-14 * scale)
+    np.testing.assert_allclose(lwtc, ref["linewidth"], rtol=1e-4, atol=1e-6 * scale)
+    np.testing.assert_allclose(lwtc, lwsimt, rtol=1e-4, atol=1e-6 * scale)
+    assert np.abs(xitc - xi64).max() <= 1e-4 * np.abs(xi64).max()
+    np.testing.assert_allclose(kitc, ki64, rtol=MIXED_KAPPA_RTOL, atol=MIXED_KAPPA_RTOL * np.abs(ki64).max())
+
+
+def test_grid_hdf5_kappa_identity(configs, tmp_path):
+    """The reference's own consistency check of its two outputs
+    (tests/thermal_conductivity/test_thermal_conductivity.py:24-40): the diagonal of kappa_SMA
+    plus the collective part (= kappa_iter) equals the diagonal of the per-mode
+    thermal_conductivity of outfile.thermal_conductivity_grid.hdf5 summed over points and
+    modes and divided by number_of_qpoints (rtol 1e-7, numpy's default there); also through
+    the C++ driver, which writes both files."""
+    import subprocess
+    import shutil
+    from pathlib import Path
+
+    from h5read import H5File
+    from tdep_gb300 import KAPPA_AU_TO_SI, write_grid_hdf5
+
+    prob = Problem.load(configs["rocksalt"], (6, 6, 6), readiso=True)
+    opts = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=4)
+    sr = ScatteringRates(prob)
+    lw = sr.generate(opts).copy()
+    ks, ki = sr.kappa(opts)
+    fn = sr.Fn.copy()
+    sr.close()
+    f = H5File(write_grid_hdf5(tmp_path / "grid.hdf5", prob, 300.0, lw, fn))
+    k2 = f.datasets["thermal_conductivity"].sum(axis=(0, 1)) / f.attrs["number_of_qpoints"][0]
+    np.testing.assert_allclose(np.diag(k2), np.diag(ki) * KAPPA_AU_TO_SI, rtol=1e-7)
+    d = tmp_path / "drv"
+    shutil.copytree(configs["rocksalt"], d)
+    exe = Path(__file__).resolve().parent.parent / "tdep_gb300" / "bin" / "thermal_conductivity"
+    r = subprocess.run([str(exe), "-qg", "6", "6", "6", "--readiso", "--noisotope", "--seed", "4",
+                        "--temperature", "300", "--dir", str(d)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    data1 = np.loadtxt(d / "outfile.thermal_conductivity")
+    g = H5File(d / "outfile.thermal_conductivity_grid.hdf5")
+    k3 = np.diag(g.datasets["thermal_conductivity"].sum(axis=(0, 1)) / g.attrs["number_of_qpoints"][0])
+    np.testing.assert_allclose(data1[0][:3] + data1[1][:3], k3, rtol=1e-7)
