@@ -279,8 +279,12 @@ int solve_point(const Crystal &c, const FC2 &fc, const V3 &qr, const V3 *qdir, i
         for (int r = 0; r < nb; ++r) E[r + (size_t)nb * b] = V[r + (size_t)nb * ord[b]];
     }
     // Degenerate subspaces: rotate the eigenvectors so that the velocity operator along
-    // a fixed generic direction is diagonal inside each subspace, then use
-    // Hellmann-Feynman velocities v = <e|dD/dk|e> / (2 omega).
+    // a fixed generic direction is diagonal inside each subspace (a deterministic gauge);
+    // the velocities follow the reference's rule for degenerate subspaces
+    // (type_forceconstant_secondorder_dynamicalmatrix.f90:313-360): every mode of a
+    // subspace gets, per direction, the mean of the subspace's Hellmann-Feynman values
+    // <e|dD/dk|e> / (2 omega), which does not depend on the gauge. Subspaces are the modes
+    // within lo_freqtol of one another (return_degenerate_subspaces, :911-980).
     const double dir[3] = {1.0, 1.33, 1.45624623};
     for (int b0 = 0; b0 < nb;) {
         int b1 = b0 + 1;
@@ -325,6 +329,7 @@ int solve_point(const Crystal &c, const FC2 &fc, const V3 &qr, const V3 *qdir, i
         }
         b0 = b1;
     }
+    std::vector<double> hf((size_t)nb * 3);  // <e_b|dD/dk_d|e_b>
     for (int b = 0; b < nb; ++b) {
         omega[b] = om[b];
         for (int r = 0; r < nb; ++r) {
@@ -338,8 +343,26 @@ int solve_point(const Crystal &c, const FC2 &fc, const V3 &qr, const V3 *qdir, i
                 for (int cc = 0; cc < nb; ++cc) gy += G[(size_t)d * nb * nb + r + (size_t)nb * cc] * E[cc + (size_t)nb * b];
                 s += std::conj(E[r + (size_t)nb * b]) * gy;
             }
-            vel[b * 3 + d] = om[b] > kFreqTol ? s.real() / (2.0 * om[b]) : 0.0;
+            hf[b * 3 + d] = s.real();
         }
+    }
+    // subspaces: a mode joins the first subspace holding a mode within lo_freqtol of it
+    std::vector<int> sub_of(nb, -1);
+    int nsub = 0;
+    for (int b = 0; b < nb; ++b) {
+        for (int a = 0; a < b && sub_of[b] < 0; ++a)
+            if (std::fabs(om[a] - om[b]) < kFreqTol) sub_of[b] = sub_of[a];
+        if (sub_of[b] < 0) sub_of[b] = nsub++;
+    }
+    for (int b = 0; b < nb; ++b) {
+        double m[3] = {0, 0, 0};
+        int cnt = 0;
+        for (int a = 0; a < nb; ++a)
+            if (sub_of[a] == sub_of[b]) {
+                ++cnt;
+                for (int d = 0; d < 3; ++d) m[d] += hf[a * 3 + d];
+            }
+        for (int d = 0; d < 3; ++d) vel[b * 3 + d] = om[b] > kFreqTol ? (m[d] / cnt) / (2.0 * om[b]) : 0.0;
     }
     return kOk;
 }
