@@ -306,6 +306,22 @@ int tdg_triplets_static(tdg_ctx *ctx, int32_t q1, const int32_t *sample, int64_t
                         int64_t *written);
 
 /*
+ * Symmetry-irreducible parameters of the third-order force constants, Phi3 = B x (the
+ * construction of the reference's forcemap, type_forcemap_returntensors.f90:250-362: orbits
+ * of the triplets under the space group and the site permutations, the components a
+ * representative's stabiliser leaves free, and the operation that maps the representative
+ * onto each member). B acts on the mass-weighted constants fc3_mwm; each orbit's columns are
+ * orthonormal on its representative. Call with t_col0, t_ncol, coef and x all NULL to get
+ * n_x (parameters) and n_coef (doubles of coef); then: t_col0[t], t_ncol[t] give the columns
+ * of triplet t, coef holds for every triplet (in order) a 27 x t_ncol[t] block, row c =
+ * component i + 3j + 9k, and x the parameters of the problem's own constants (B^T on the
+ * representatives). TDG_ERR_SYMMETRY when the triplet list is not closed under the group.
+ * The problem must carry op_fmap and atom_shift (tdg_problem_load fills them).
+ */
+int tdg_fc3_irreducible(const tdg_problem *prob, int32_t *n_x, int64_t *n_coef, int32_t *t_col0, int32_t *t_ncol,
+                        double *coef, double *x);
+
+/*
  * Differentiation with respect to the third-order force constants. None of the three entry
  * points below has a counterpart in the reference; they serve d(kappa)/d(Phi3) and
  * d(Gamma)/d(Phi3).

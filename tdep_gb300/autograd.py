@@ -6,8 +6,9 @@ adjoint of get_kappa + symmetrize_kappa on the host (tdg_kappa_sma_vjp) and the 
 kernel (tdg_adjoint_fc3), which recomputes Psi per q-triplet instead of storing it.
 Tensors are CPU float64, as the C-ABI takes host buffers; the work runs on the device.
 
-Any parameterisation of Phi3 that is a torch function of parameters x (for example an
-irreducible basis, Phi3 = B x) composes with ThreePhononKappa through autograd.
+Any parameterisation of Phi3 that is a torch function of parameters x composes with
+ThreePhononKappa through autograd; fc3_from_irreducible is the symmetry-irreducible one
+(Problem.fc3_irreducible, after the reference's forcemap).
 """
 from __future__ import annotations
 
@@ -65,3 +66,13 @@ class ThreePhononKappa(torch.autograd.Function):
 def linewidth_and_kappa(fc3_mwm: torch.Tensor, sr: ScatteringRates, opts: Options, lists: QLists):
     """Differentiable (linewidth, kappa_sma) of the given mass-weighted Phi3."""
     return ThreePhononKappa.apply(fc3_mwm, sr, opts, lists)
+
+
+def fc3_from_irreducible(x: torch.Tensor, B) -> torch.Tensor:
+    """Mass-weighted Phi3 [n_fc3, 27] = B x for the symmetry-irreducible parameters x
+    (Problem.fc3_irreducible returns x and the sparse B); differentiable in x, so
+    d kappa / d x = B^T d kappa / d fc3_mwm comes out of autograd."""
+    coo = B.tocoo()
+    idx = torch.from_numpy(np.vstack([coo.row, coo.col]).astype(np.int64))
+    Bt = torch.sparse_coo_tensor(idx, torch.from_numpy(coo.data), size=coo.shape, dtype=torch.float64)
+    return torch.sparse.mm(Bt, x.reshape(-1, 1)).reshape(-1, 27)

@@ -107,6 +107,38 @@ class Problem:
                 kw[k] = np.ctypeslib.as_array(p, shape=(n,)).copy() if (n > 0 and p) else np.zeros(n, dtype=ct)
         return cls(**kw)
 
+    def fc3_irreducible(self):
+        """Symmetry-irreducible parameters of the third-order force constants
+        (tdg_fc3_irreducible): returns (x [n_x], B) with B a scipy.sparse CSR matrix of shape
+        (n_fc3 * 27, n_x) such that fc3_mwm.ravel() = B @ x for symmetric constants."""
+        import scipy.sparse as sp
+
+        ps = self.struct()
+        nx, nc = C.c_int32(0), C.c_int64(0)
+        L = N.lib()
+        N.check(L.tdg_fc3_irreducible(C.byref(ps), C.byref(nx), C.byref(nc), None, None, None, None),
+                "tdg_fc3_irreducible")
+        col0 = np.zeros(self.n_fc3, np.int32)
+        ncol = np.zeros(self.n_fc3, np.int32)
+        coef = np.zeros(max(1, nc.value))
+        x = np.zeros(max(1, nx.value))
+        N.check(L.tdg_fc3_irreducible(C.byref(ps), C.byref(nx), C.byref(nc), N.ptr(col0, C.c_int32),
+                                      N.ptr(ncol, C.c_int32), N.ptr(coef, C.c_double), N.ptr(x, C.c_double)),
+                "tdg_fc3_irreducible")
+        rows, cols, vals = [], [], []
+        off = 0
+        for t in range(self.n_fc3):
+            k = int(ncol[t])
+            blk = coef[off:off + 27 * k].reshape(27, k)
+            r, c = np.nonzero(np.abs(blk) > 0)
+            rows.append(27 * t + r)
+            cols.append(col0[t] + c)
+            vals.append(blk[r, c])
+            off += 27 * k
+        B = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                          shape=(self.n_fc3 * 27, nx.value))
+        return x[: nx.value].copy(), B
+
     def struct(self) -> N.TdgProblem:
         s = N.TdgProblem()
         for k in _SCALARS:

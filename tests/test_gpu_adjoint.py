@@ -154,3 +154,37 @@ def test_adjoint_large_cell_matches_oracle(configs):
     sr.close()
     ref = orc.adjoint_fc3(prob, opts, lists, lw_bar)
     assert np.linalg.norm(g - ref) <= 1e-3 * np.linalg.norm(ref)
+
+
+def test_dkappa_dirreducible_against_central_differences(configs):
+    """d kappa_xx / d x for the symmetry-irreducible third-order parameters x (Phi3 = B x,
+    Problem.fc3_irreducible) through fc3_from_irreducible and ThreePhononKappa, against
+    central differences of the device forward pass in x on 8 seeded parameters; the
+    gradient is B^T of the per-entry gradient."""
+    torch = pytest.importorskip("torch")
+    from tdep_gb300.autograd import fc3_from_irreducible, linewidth_and_kappa
+
+    prob = Problem.load(configs["rocksalt"], (8, 8, 8), readiso=True)
+    opts = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=5)
+    lists = QLists.monte_carlo(prob, opts)
+    x0, B = prob.fc3_irreducible()
+    sr = ScatteringRates(prob)
+    x = torch.tensor(x0, dtype=torch.float64, requires_grad=True)
+    _, ks = linewidth_and_kappa(fc3_from_irreducible(x, B), sr, opts, lists)
+    ks[0, 0].backward()
+    g = x.grad.numpy().copy()
+
+    def kxx(xv):
+        sr.set_fc3((B @ xv).reshape(-1, 27))
+        sr.generate(opts, lists)
+        return sr.kappa(opts, maxiter=0)[0][0, 0]
+
+    rng = np.random.default_rng(7)
+    for j in rng.choice(x0.size, size=min(8, x0.size), replace=False):
+        h = 1e-4 * max(abs(x0[j]), np.abs(x0).max() * 1e-3)
+        xp, xm = x0.copy(), x0.copy()
+        xp[j] += h
+        xm[j] -= h
+        fd = (kxx(xp) - kxx(xm)) / (2 * h)
+        assert abs(fd - g[j]) <= 1e-5 * np.abs(g).max() + 1e-4 * abs(g[j]), (j, fd, g[j])
+    sr.close()
