@@ -355,6 +355,23 @@ int tdg_kappa_sma_vjp(tdg_ctx *ctx, const tdg_opts *opts, const double *kappa_ba
 int tdg_adjoint_fc3(tdg_ctx *ctx, const tdg_opts *opts, const double *lw_bar, double *mwm_bar, double *stats);
 
 /*
+ * Vector-Jacobian product of kappa_iter (iterative_solution + symmetrize_kappa,
+ * kappa.f90:326-495) for the cotangent kappa_bar (3x3 column-major), no reference
+ * counterpart. At the converged solution of the last tdg_kappa call (maxiter > 0) it solves
+ * the transposed fixed point lambda = kbar - T^T Xi^T Q^-1 D lambda on the device (maxiter
+ * and tol as for tdg_kappa, the same mixing schedule; *n_iter receives the iterations),
+ * writes the cotangent of the linewidths to lw_bar [n_irr*n_mode] (through qs = 2 linewidth
+ * and F0 = v / qs) and keeps on the device the cotangent of the three-phonon terms of Xi,
+ * mapped back through the row symmetrisations. The next tdg_adjoint_fc3 adds that term, so
+ * tdg_adjoint_fc3(lw_bar) then returns d(kappa_bar : kappa_iter) / d fc3_mwm. The stored term
+ * lasts until the next tdg_scattering, tdg_kappa or tdg_set_fc3. Shared-memory kernel path
+ * only (up to 18 modes); the active entries of the reference's od_terms > 0 averaging are
+ * taken from a fresh forward pass of the raw three-phonon terms.
+ */
+int tdg_kappa_iter_vjp(tdg_ctx *ctx, const tdg_opts *opts, const double *kappa_bar, int32_t maxiter, double tol,
+                       double *lw_bar, int32_t *n_iter);
+
+/*
  * Thermal conductivity from the current scattering state (main.f90:216-244):
  * kappa_sma (get_kappa, kappa.f90:28-75), the iterative BTE (kappa.f90:326-495) with
  * maxiter steps and tolerance tol, kappa_iter, both symmetrised (kappa.f90:308-324).

@@ -125,6 +125,7 @@ SIGNATURES = {
     "tdg_write_grid_hdf5": (C.c_int, [C.c_char_p, C.POINTER(TdgProblem), C.c_double, _f64p, _f64p]),
     "tdg_fc3_irreducible": (C.c_int, [C.POINTER(TdgProblem), _i32p, C.POINTER(C.c_int64), _i32p, _i32p, _f64p,
                                       _f64p]),
+    "tdg_kappa_iter_vjp": (C.c_int, [C.c_void_p, C.POINTER(TdgOpts), _f64p, C.c_int32, C.c_double, _f64p, _i32p]),
     "tdg_last_path": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "tdg_pool_usage": (C.c_int, [C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "tdg_natural_isotopes": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),

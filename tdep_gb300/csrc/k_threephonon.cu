@@ -109,10 +109,11 @@ __device__ __forceinline__ C phase3(const Fc3Dev &fc, const MeshDev &m, const in
 // Shared-memory layout (bytes) for mode count n and complex size cs.
 struct Layout {
     size_t om1, om2, om3, inv1, be2, be3, s1, s2, s3, v1, v2, v3, wrow, r2, f32, masks, E1, E2, E3, ph, Q, A, B,
-        rowid, red, wsum, total;
+        rowid, red, wsum, xb, total;
 };
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
-__host__ __device__ inline Layout make_layout(int n, int cs) {
+// adj: the adjoint's extra n^2 doubles (column sums of the scattering-matrix cotangent).
+__host__ __device__ inline Layout make_layout(int n, int cs, bool adj = false) {
     Layout L;
     size_t o = 0;
     const size_t dn = align16(sizeof(double) * n);
@@ -151,6 +152,8 @@ __host__ __device__ inline Layout make_layout(int n, int cs) {
     L.rowid = o; o += align16(sizeof(int) * n);
     L.red = o; o += align16(sizeof(int2) * kMaxRed);
     L.wsum = o; o += align16(sizeof(int) * 33);
+    L.xb = o;
+    if (adj) o += align16(sizeof(double) * n2);
     L.total = o;
     return L;
 }
@@ -175,7 +178,7 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
     constexpr int NA = N / 3;
     constexpr uint32_t kAll = (N >= 32) ? 0xffffffffu : ((1u << N) - 1u);
     extern __shared__ __align__(16) unsigned char smem[];
-    const Layout L = make_layout(N, sizeof(C));
+    const Layout L = make_layout(N, sizeof(C), ADJ);
     double *om1 = (double *)(smem + L.om1);
     double *om2 = (double *)(smem + L.om2);
     double *om3 = (double *)(smem + L.om3);
@@ -363,9 +366,35 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
             // d|Psi|^2 / d P[abc] = 2 Re(conj(Psi) E1[a][b1] E2[b][b2] E3[c][b3]), so with
             // W = G conj(Psi):  Q[abc] = sum_b W_b E1[a][b1] E2[b][b2] E3[c][b3] and
             // d L / d mwm_t(i,j,k) = 2 Re(phase_t Q[3a1+i][3a2+j][3a3+k]).
+            // with a scattering-matrix cotangent xi_bar (the BTE adjoint): the Xi row terms
+            // 2 F om2/om1 at (q2', b2) and 2 F om3/om1 at (q3', b3) of every equivalent
+            // triplet add xi_bar(row, .) times those factors to the cotangent of F;
+            // R2[b1][b2] and XB[b1][b3] hold xi_bar summed over the equivalent triplets
+            double *XB = (double *)(smem + L.xb);
+            if (a.xi_bar) {
+                for (int e = tid; e < 2 * N2; e += bd) {
+                    const int x = e % N2, b1 = x / N, bb = x % N, row = rowid[b1];
+                    double sum = 0.0;
+                    if (row >= 0) {
+                        const double *wr = a.xi_bar + (int64_t)row * ld;
+                        for (int k = 0; k < nred; ++k) {
+                            const int2 pr = red[k];
+                            sum += wr[(int64_t)(e < N2 ? pr.x : pr.y) * N + bb];
+                        }
+                    }
+                    if (e < N2) R2[x] = sum;
+                    else XB[x] = sum;
+                }
+                __syncthreads();
+            }
             for (int i = tid; i < N3; i += bd) {
                 const int row = rowid[i / N2];
-                const double g = row >= 0 ? a.lam[row] * (double)nred * F[i] : 0.0;
+                double cot = row >= 0 ? a.lam[row] * (double)nred : 0.0;
+                if (a.xi_bar && row >= 0) {
+                    const int b1 = i / N2, b2 = (i / N) % N, b3 = i % N;
+                    cot += 2.0 * (om2[b2] * R2[b1 * N + b2] + om3[b3] * XB[b1 * N + b3]) * inv1[b1];
+                }
+                const double g = cot * F[i];
                 const C psi = B[i];
                 C w;
                 w.x = (R)(g * (double)psi.x);
@@ -478,7 +507,7 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
 // `extra` bytes of dynamic shared memory follow the kernel's layout (adjoint accumulator).
 template <int N, typename R, bool ADJ>
 int grid_n(int n_sm, int n_trip, size_t extra, int ctas_per_sm = 0) {
-    const Layout L = make_layout(N, sizeof(typename CT<R>::C));
+    const Layout L = make_layout(N, sizeof(typename CT<R>::C), ADJ);
     const size_t bytes = L.total + extra;
     if (cudaFuncSetAttribute(k_threephonon<N, R, ADJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
         cudaSuccess) {
@@ -499,7 +528,7 @@ int grid_n(int n_sm, int n_trip, size_t extra, int ctas_per_sm = 0) {
 
 template <int N, typename R, bool ADJ>
 cudaError_t launch_grid(const ThreePhArgs &a, int grid, size_t extra, cudaStream_t s) {
-    const Layout L = make_layout(N, sizeof(typename CT<R>::C));
+    const Layout L = make_layout(N, sizeof(typename CT<R>::C), ADJ);
     k_threephonon<N, R, ADJ><<<grid, threads_for(N), L.total + extra, s>>>(a);
     return cudaGetLastError();
 }

@@ -240,6 +240,11 @@ struct tdg_ctx {
     int32_t last_ntrip = 0;
     bool last_third = false;
     DevBuf<double> d_lam, d_slices, d_mwm_bar;
+    // BTE adjoint (tdg_kappa_iter_vjp): cotangent of the raw three-phonon terms of Xi, the
+    // recomputed raw terms, and work arrays; fn_iter: c->Fn is an iterative solution
+    DevBuf<double> d_xi_bar, d_od_raw, d_gam_tmp, d_zv, d_yv, d_xpart, d_tf, d_xtf;
+    bool xi_bar_ready = false, fn_iter = false;
+    int last_prec = 0;
     // large-cell path: real-split eigenvector matrices (built once), operand planes, Psi, phases
     DevBuf<__nv_bfloat16> d_bmat, d_lnx;
     DevBuf<float2> d_psi, d_lnph;
@@ -1599,7 +1604,10 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
     c->last_rows = rows;
     c->last_ntrip = ntrip;
     c->last_third = o->thirdorder != 0;
+    c->last_prec = o->precision;
     c->have_scattering = true;
+    c->fn_iter = false;
+    c->xi_bar_ready = false;
     pt.mark("linewidths and F0 (host)");
     return kOk;
 }
@@ -1896,6 +1904,8 @@ extern "C" int tdg_kappa(tdg_ctx *c, const tdg_opts *o, int32_t maxiter, double 
     symmetrize_kappa(c, kappa_iter);
     symmetrize_kappa(c, kappa_sma);
     c->Fn = Fn;
+    c->fn_iter = maxiter > 0;
+    c->xi_bar_ready = false;
     if (fn_out) std::memcpy(fn_out, Fn.data(), sizeof(double) * Fn.size());
     if (n_iter) *n_iter = iters;
     return kOk;
@@ -1932,6 +1942,7 @@ extern "C" int tdg_set_fc3(tdg_ctx *c, const double *fc3_mwm) {
     CUDA_TRY(c->fc3_mwm32.upload(mf.data(), cnt, c->stream));
     CUDA_TRY(cudaStreamSynchronize(c->stream));
     c->have_scattering = false;
+    c->xi_bar_ready = false;
     return kOk;
 }
 
@@ -2059,6 +2070,208 @@ int adjoint_large_cell(tdg_ctx *c, const std::vector<double> &lam, double *mwm_b
 }
 }  // namespace
 
+extern "C" int tdg_kappa_iter_vjp(tdg_ctx *c, const tdg_opts *o, const double *kappa_bar, int32_t maxiter,
+                                  double tol, double *lw_bar, int32_t *n_iter) {
+    XferScope xs(c ? c->xfer : nullptr);
+    PoolScope pscope(c ? c->stream : nullptr, c ? c->pool : nullptr);
+    if (!c || !kappa_bar || !lw_bar) return set_error(kErrParam, "tdg_kappa_iter_vjp: null argument");
+    int st = validate_opts(o);
+    if (st) return st;
+    if (!c->have_scattering || !c->last_third || !c->fn_iter)
+        return set_error(kErrParam, "tdg_kappa_iter_vjp: call tdg_scattering (three-phonon) and tdg_kappa with "
+                                    "iterations first");
+    if (c->last_ln) return set_error(kErrParam, "tdg_kappa_iter_vjp: not supported on the large-cell path");
+    if (maxiter < 1) return set_error(kErrParam, "tdg_kappa_iter_vjp: maxiter must be positive");
+    CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    const int n = c->n, N = c->N, nirr = c->nirr, nr = c->n_row;
+    const int64_t ncol = (int64_t)N * n;
+    const double T = o->temperature;
+    const bool classical = o->classical != 0;
+    // d kappa_iter / d F per irreducible mode: kappa = S(S(sum_r w_r F_r (x) v_r)) (get_kappa,
+    // symmetrize_kappa; lo_chop as the identity), so kbar_r = w_r Mb v_r with Mb = S^T S^T kappa_bar.
+    auto St = [&](const double *x, double *y) {
+        for (int i = 0; i < 9; ++i) y[i] = 0.0;
+        for (int j = 0; j < c->nop; ++j) {
+            const double *m = &c->op_cart[9 * j];
+            for (int k = 0; k < 3; ++k)
+                for (int l = 0; l < 3; ++l) {
+                    double sum = 0.0;
+                    for (int a = 0; a < 3; ++a)
+                        for (int b = 0; b < 3; ++b) sum += m[a + 3 * k] * x[a + 3 * b] * m[b + 3 * l];
+                    y[k + 3 * l] += sum / c->nop;
+                }
+        }
+    };
+    double t1[9], Mb[9];
+    St(kappa_bar, t1);
+    St(t1, Mb);
+    const size_t nf = (size_t)nirr * n * 3;
+    std::vector<double> kbar(nf, 0.0);
+    for (int q1 = 0; q1 < nirr; ++q1) {
+        const int f = c->irr_full[q1] - 1;
+        for (int b1 = 0; b1 < n; ++b1) {
+            const double om1 = c->omega[(size_t)f * n + b1];
+            if (om1 < kFreqTol) continue;
+            const double cv = classical ? kKbHartree : harmonic_oscillator_cv(T, om1);
+            const double w = cv / c->volume * c->irr_weight[q1];
+            const double *v = &c->vel[((size_t)f * n + b1) * 3];
+            for (int x = 0; x < 3; ++x)
+                kbar[((size_t)q1 * n + b1) * 3 + x] = w * (Mb[x] * v[0] + Mb[x + 3] * v[1] + Mb[x + 6] * v[2]);
+        }
+    }
+    // T F on the full mesh (the foldout of kappa.f90:382-404) and X T F
+    std::vector<double> tf((size_t)ncol * 3);
+    for (int q = 0; q < N; ++q) {
+        const int op = c->full_op[q], l = c->full_irr[q] - 1;
+        const double *m = &c->op_cart[9 * (std::abs(op) - 1)];
+        const double sg = op > 0 ? 1.0 : -1.0;
+        for (int b = 0; b < n; ++b) {
+            const double *F = &c->Fn[((size_t)l * n + b) * 3];
+            for (int x = 0; x < 3; ++x)
+                tf[((size_t)q * n + b) * 3 + x] = sg * (m[x] * F[0] + m[x + 3] * F[1] + m[x + 6] * F[2]);
+        }
+    }
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t x) {
+        if (e == cudaSuccess) e = x;
+    };
+    chk(c->d_tf.upload(tf.data(), tf.size(), s));
+    chk(c->d_xtf.alloc((size_t)nr * 3));
+    chk(c->d_zv.alloc((size_t)nr * 3));
+    chk(c->d_yv.alloc((size_t)ncol * 3));
+    chk(c->d_xpart.alloc((size_t)xit_parts(nr) * 3 * ncol));
+    if (e != cudaSuccess) return set_error(kErrDevice, std::string("allocation failed: ") + cudaGetErrorString(e));
+    std::vector<double> xtf((size_t)nr * 3), z((size_t)nr * 3), y((size_t)ncol * 3);
+    CUDA_TRY(launch_xi_rowdot(c->d_xi.p, nr, ncol, c->d_tf.p, c->d_xtf.p, s));
+    CUDA_TRY(copy_async(xtf.data(), c->d_xtf.p, sizeof(double) * xtf.size(), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    // degeneracy averaging (kappa.f90:418-435) of an irreducible array, in place
+    auto degen_avg = [&](std::vector<double> &a) {
+        std::vector<double> out(a.size());
+        for (int q1 = 0; q1 < nirr; ++q1) {
+            const int f = c->irr_full[q1] - 1;
+            for (int b1 = 0; b1 < n; ++b1) {
+                const int dg = c->degen[(size_t)f * n + b1];
+                const int32_t *dm = &c->degen_mode[((size_t)f * n + b1) * n];
+                for (int x = 0; x < 3; ++x) {
+                    double sum = 0.0;
+                    for (int j = 0; j < dg; ++j) sum += a[((size_t)q1 * n + dm[j] - 1) * 3 + x];
+                    out[((size_t)q1 * n + b1) * 3 + x] = sum / dg;
+                }
+            }
+        }
+        a.swap(out);
+    };
+    // z_r = (D lambda)_r / qs_r on the rows
+    auto make_z = [&](const std::vector<double> &dl) {
+        for (int r = 0; r < nr; ++r) {
+            const int q1 = c->row_q1[r] - 1, b1 = c->row_b1[r] - 1;
+            const double qs = c->qs[(size_t)q1 * n + b1];
+            for (int x = 0; x < 3; ++x)
+                z[(size_t)r * 3 + x] = qs < kFreqTol ? 0.0 : dl[((size_t)q1 * n + b1) * 3 + x] / qs;
+        }
+    };
+    // adjoint fixed point lambda = kbar - T^T X^T Q^-1 D lambda, iterated with the forward
+    // pass's mixing schedule and convergence test (kappa.f90:437-490)
+    std::vector<double> lam = kbar, nw(nf), dl;
+    std::vector<double> scf;
+    double mix = 0.95;
+    int it = 0;
+    for (it = 1; it <= maxiter; ++it) {
+        dl = lam;
+        degen_avg(dl);
+        make_z(dl);
+        CUDA_TRY(copy_async(c->d_zv.p, z.data(), sizeof(double) * z.size(), cudaMemcpyHostToDevice, s));
+        CUDA_TRY(launch_xit_gemv(c->d_xi.p, nr, ncol, c->d_zv.p, c->d_xpart.p, c->d_yv.p, s));
+        CUDA_TRY(copy_async(y.data(), c->d_yv.p, sizeof(double) * y.size(), cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(cudaStreamSynchronize(s));
+        nw = kbar;
+        for (int q = 0; q < N; ++q) {  // T^T: sum of R^T y over the star, with the sign of the operation
+            const int op = c->full_op[q], l = c->full_irr[q] - 1;
+            const double *m = &c->op_cart[9 * (std::abs(op) - 1)];
+            const double sg = op > 0 ? 1.0 : -1.0;
+            for (int b = 0; b < n; ++b) {
+                const double *yy = &y[((size_t)q * n + b) * 3];
+                for (int x = 0; x < 3; ++x)
+                    nw[((size_t)l * n + b) * 3 + x] -= sg * (m[3 * x] * yy[0] + m[3 * x + 1] * yy[1] + m[3 * x + 2] * yy[2]);
+            }
+        }
+        double g0 = 0.0;
+        for (size_t i = 0; i < nf; i += 3) {
+            double g1 = 0.0, g2 = 0.0;
+            for (int x = 0; x < 3; ++x) {
+                g1 += (lam[i + x] - nw[i + x]) * (lam[i + x] - nw[i + x]);
+                g2 += lam[i + x] * lam[i + x];
+            }
+            if (g2 > kSqTol) g0 += g1 / g2;
+            for (int x = 0; x < 3; ++x) lam[i + x] = lam[i + x] * (1.0 - mix) + mix * nw[i + x];
+        }
+        scf.push_back(g0 / nirr / n);
+        if (it >= 3 && scf[it - 1] + scf[it - 2] + scf[it - 3] < tol) break;
+        if (it > 15 && mix > 0.50) mix *= 0.98;
+    }
+    if (n_iter) *n_iter = std::min(it, maxiter);
+    dl = lam;
+    degen_avg(dl);
+    make_z(dl);
+    // linewidth cotangent: F0 = v / qs and the 1/qs of the update, qs = 2 linewidth
+    for (size_t i = 0; i < (size_t)nirr * n; ++i) lw_bar[i] = 0.0;
+    for (int r = 0; r < nr; ++r) {
+        const int q1 = c->row_q1[r] - 1, b1 = c->row_b1[r] - 1;
+        const size_t i = (size_t)q1 * n + b1;
+        const double qs = c->qs[i];
+        if (qs < kFreqTol) continue;
+        const int f = c->irr_full[q1] - 1;
+        const double *v = &c->vel[((size_t)f * n + b1) * 3];
+        double g = 0.0;
+        for (int x = 0; x < 3; ++x) g += dl[i * 3 + x] * xtf[(size_t)r * 3 + x];
+        if (c->linewidth[i] > kFreqTol)
+            for (int x = 0; x < 3; ++x) g -= lam[i * 3 + x] * v[x];
+        lw_bar[i] = 2.0 * g / (qs * qs);
+    }
+    // Xi cotangent W = -z (T F)^T through the adjoint row symmetrisations, given the raw
+    // three-phonon terms of a fresh forward pass (the distribution's active entries)
+    chk(c->d_xi_bar.alloc((size_t)nr * ncol));
+    chk(c->d_od_raw.alloc((size_t)nr * ncol));
+    chk(c->d_gam_tmp.alloc((size_t)nr));
+    if (e != cudaSuccess) return set_error(kErrDevice, std::string("allocation failed: ") + cudaGetErrorString(e));
+    CUDA_TRY(copy_async(c->d_zv.p, z.data(), sizeof(double) * z.size(), cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemsetAsync(c->d_od_raw.p, 0, sizeof(double) * (size_t)nr * ncol, s));
+    CUDA_TRY(cudaMemsetAsync(c->d_gam_tmp.p, 0, sizeof(double) * nr, s));
+    CUDA_TRY(cudaMemsetAsync(c->d_status.p, 0, sizeof(int32_t), s));
+    ThreePhArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.mesh = c->mesh();
+    a.ph = c->last_ph;
+    a.rows = c->last_rows;
+    a.fc.n = c->n_fc3;
+    a.fc.n_atom = c->na;
+    a.fc.blk_ptr = c->fc3_blk.p;
+    a.fc.lv = c->fc3_lv.p;
+    a.fc.mwm = c->fc3_mwm.p;
+    a.fc.mwm32 = c->fc3_mwm32.p;
+    a.fc.twiddle = c->tw.p;
+    a.fc.twiddle32 = c->tw32.p;
+    a.fc.abase = c->fc3_abase.p;
+    a.trip = c->d_trip.p;
+    a.n_trip = c->last_ntrip;
+    a.red = c->d_red.p;
+    a.cand_mask = c->d_mask.p;
+    a.gamma = c->d_gam_tmp.p;
+    a.od = c->d_od_raw.p;
+    a.status = c->d_status.p;
+    CUDA_TRY(launch_threephonon(a, c->last_prec, c->n_sm, 0, s));
+    CUDA_TRY(launch_xibar_fill(nr, ncol, c->d_zv.p, c->d_tf.p, c->d_xi_bar.p, s));
+    CUDA_TRY(launch_sym_tile_adjoint(c->mesh(), c->orbits, nr, c->d_row_q1.p, c->d_od_raw.p, c->d_xi_bar.p,
+                                     c->d_sbits.p, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    st = read_status(c);
+    if (st) return st;
+    c->xi_bar_ready = true;
+    return kOk;
+}
+
 extern "C" int tdg_adjoint_fc3(tdg_ctx *c, const tdg_opts *o, const double *lw_bar, double *mwm_bar, double *stats) {
     XferScope xs(c ? c->xfer : nullptr);
     PoolScope pscope(c ? c->stream : nullptr, c ? c->pool : nullptr);
@@ -2083,7 +2296,12 @@ extern "C" int tdg_adjoint_fc3(tdg_ctx *c, const tdg_opts *o, const double *lw_b
         lam[r] = acc / (double)dg;
     }
     const int ntrip = c->last_ntrip;
-    if (c->last_ln) return adjoint_large_cell(c, lam, mwm_bar, stats);
+    if (c->last_ln) {
+        if (c->xi_bar_ready)
+            return set_error(kErrParam, "tdg_adjoint_fc3: the scattering-matrix cotangent of tdg_kappa_iter_vjp is "
+                                        "not supported on the large-cell path");
+        return adjoint_large_cell(c, lam, mwm_bar, stats);
+    }
     // the CTA's gradient slice lives in shared memory when it is small enough
     const bool acc_smem = (size_t)c->n_fc3 * 27 * sizeof(double) <= 48 * 1024;
     const int grid = threephonon_adjoint_grid(n, o->precision, c->n_sm, ntrip, c->n_fc3, acc_smem);
@@ -2102,6 +2320,7 @@ extern "C" int tdg_adjoint_fc3(tdg_ctx *c, const tdg_opts *o, const double *lw_b
     CUDA_TRY(cudaMemsetAsync(c->d_slices.p, 0, sizeof(double) * (size_t)std::max(grid, 1) * nm, s));
     CUDA_TRY(cudaMemsetAsync(c->d_status.p, 0, sizeof(int32_t), s));
     ThreePhArgs a;
+    std::memset(&a, 0, sizeof a);
     a.mesh = c->mesh();
     a.ph = c->last_ph;
     a.rows = c->last_rows;
@@ -2124,6 +2343,7 @@ extern "C" int tdg_adjoint_fc3(tdg_ctx *c, const tdg_opts *o, const double *lw_b
     a.lam = c->d_lam.p;
     a.mwm_bar = c->d_slices.p;
     a.acc_in_smem = acc_smem ? 1 : 0;
+    a.xi_bar = c->xi_bar_ready ? c->d_xi_bar.p : nullptr;
     CUDA_TRY(cudaEventRecord(ev[1], s));
     CUDA_TRY(launch_threephonon_adjoint(a, o->precision, grid, s));
     CUDA_TRY(cudaEventRecord(ev[2], s));

@@ -151,6 +151,8 @@ struct ThreePhArgs {
     const double *lam;
     double *mwm_bar;            // FP64 slices, zeroed before the launch
     int32_t acc_in_smem;        // accumulate the CTA's slice in shared memory, store it once
+    const double *xi_bar;       // adjoint only, may be null: cotangent of the raw three-phonon
+                                // row terms of Xi ([n_row * n_full*n], tdg_kappa_iter_vjp)
     // tensor-core kernel only (k_threephonon_tc): real-split eigenvector images of every mesh
     // point (4 KB each), the per-block transposed FP32 force constants and their offsets
     const unsigned char *tc_eimg;
@@ -178,6 +180,16 @@ size_t tc_fct_floats(int n_fc, int n_blk);
 cudaError_t launch_tc_prep_fc(const int32_t *blk_ptr, int32_t n_blk, const float *mwm32, int32_t *toff, float *out,
                               cudaStream_t s);
 cudaError_t launch_tc_eimg(int32_t n_full, int32_t n, const float2 *egvs32, unsigned char *out, cudaStream_t s);
+// Adjoint of the BTE (k_bte_adjoint.cu): y = X^T z (FP64, 3 right-hand sides, part holds
+// xit_parts(n_row) * 3 * n_col doubles), out = X f row by row, W = -z f^T, and the adjoint
+// of the row symmetrisations on W given the raw three-phonon terms od_raw.
+int xit_parts(int32_t n_row);
+cudaError_t launch_xit_gemv(const double *xi, int32_t n_row, int64_t n_col, const double *z, double *part, double *y,
+                            cudaStream_t s);
+cudaError_t launch_xi_rowdot(const double *xi, int32_t n_row, int64_t n_col, const double *f, double *out,
+                             cudaStream_t s);
+cudaError_t launch_xibar_fill(int32_t n_row, int64_t n_col, const double *z, const double *f, double *w,
+                              cudaStream_t s);
 
 struct FourPhArgs {
     MeshDev mesh;
@@ -290,6 +302,10 @@ cudaError_t launch_sample_bits(int32_t n_full, int32_t n_row, const int64_t *rbe
                                const int32_t *list, uint32_t *bits, cudaStream_t s);
 cudaError_t launch_sym_tile(const MeshDev &m, const OrbitDev &o, int32_t n_row, const int32_t *row_q1, double *xi,
                             const uint32_t *sbits, bool dist, bool scat, cudaStream_t s);
+// Adjoint of symmetrize_scatmat then symmetrize_and_distribute (three-phonon terms) on the
+// cotangent w in place, the distribution's active entries given by the raw terms od_raw.
+cudaError_t launch_sym_tile_adjoint(const MeshDev &m, const OrbitDev &o, int32_t n_row, const int32_t *row_q1,
+                                    const double *od_raw, double *w, const uint32_t *sbits, cudaStream_t s);
 // K8: buf[r*3+a] = sum_j xi[r, j] * fbb[j*3 + a] on the FP32 pipe; xi and fbb as (hi, lo)
 // float pairs accumulated in double-float when df (FP64 runs), else as floats with FMA chains
 // added into double-float accumulators (mixed precision). launch_split_xi converts the FP64

@@ -418,6 +418,22 @@ class ScatteringRates:
                 "tdg_kappa_sma_vjp")
         return out.reshape(p.n_irr, p.n_mode)
 
+    def kappa_iter_vjp(self, opts: Options, kappa_bar: np.ndarray, maxiter: int | None = None,
+                       tol: float | None = None) -> np.ndarray:
+        """Cotangent of the linewidths for d(kappa_bar : kappa_iter) (tdg_kappa_iter_vjp);
+        the next adjoint_fc3 also adds the scattering-matrix term it leaves on the device."""
+        p = self.prob
+        o = opts.struct(p.grid)
+        kb = np.ascontiguousarray(np.asarray(kappa_bar, np.float64).reshape(3, 3).ravel(order="F"))
+        out = np.zeros(p.n_irr * p.n_mode)
+        nit = C.c_int32(0)
+        mi = opts.itermaxsteps if maxiter is None else maxiter
+        tl = opts.itertol if tol is None else tol
+        N.check(self._lib.tdg_kappa_iter_vjp(self._ctx, C.byref(o), N.ptr(kb, C.c_double), int(mi), float(tl),
+                                             N.ptr(out, C.c_double), C.byref(nit)), "tdg_kappa_iter_vjp")
+        self.vjp_iter = nit.value
+        return out.reshape(p.n_irr, p.n_mode)
+
     def adjoint_fc3(self, opts: Options, lw_bar: np.ndarray) -> np.ndarray:
         """(d linewidth / d fc3_mwm)^T lw_bar over the q-triplets of the last generate():
         [n_fc3, 27]. Timing of the pass in self.adjoint_stats."""

@@ -200,19 +200,29 @@ def test_fp64_classical_uneven_per_q1_samples(configs):
 
 
 def test_mixed_precision_kappa(configs):
+    """Mixed precision against FP64 on rocksalt 8^3 with the BTE converged to 1e-12: at the
+    default tolerance (1e-6) the iteration stops 1.7e-4 short of its fixed point on this
+    cell, so two runs that stop one iteration apart differ by that much whatever their
+    precision. The FP64 run at the default tolerance matches the oracle's, iteration count
+    included."""
     prob = Problem.load(configs["rocksalt"], (8, 8, 8), readiso=True)
     o64 = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=3)
     o32 = Options(temperature=300.0, integrationtype=2, isotopescattering=False, seed=3, precision="mixed")
     lists = QLists.monte_carlo(prob, o64)
     sr = ScatteringRates(prob)
     lw64 = sr.generate(o64, lists).copy()
-    _, k64 = sr.kappa(o64)
+    _, k64d = sr.kappa(o64)
+    nit64 = sr.n_iter
+    _, k64 = sr.kappa(o64, maxiter=400, tol=1e-12)
     lw32 = sr.generate(o32, lists).copy()
-    _, k32 = sr.kappa(o32)
+    _, k32 = sr.kappa(o32, maxiter=400, tol=1e-12)
     sr.close()
     big = lw64 > 1e-3 * lw64.max()
     assert np.max(np.abs(lw32[big] / lw64[big] - 1)) < 1e-4
     np.testing.assert_allclose(k32, k64, rtol=MIXED_KAPPA_RTOL, atol=MIXED_KAPPA_RTOL * np.abs(k64).max())
+    ref = orc.full_run(prob, o64, lists)
+    np.testing.assert_allclose(k64d, ref["kappa_iter"], rtol=1e-3, atol=1e-3 * np.abs(ref["kappa_iter"]).max())
+    assert abs(nit64 - ref["n_iter"]) <= 1
 
 
 @pytest.mark.parametrize("name,grid,qg4,it", [("fcc", (8, 8, 8), (4, 4, 4), 2),
