@@ -280,8 +280,37 @@ def parity_record(prob, lists, idx, lw_ref, xi_ref, runs):
     return out
 
 
+def setup_oracle(cfg_name):
+    """The reference arm's workload built without the library: the oracle's own problem from
+    the input files (oracle/problem.py: readers, symmetry, mesh, phonons in numpy) and its own
+    MT19937-64 samples, so that this arm runs the oracle alone."""
+    from oracle import binding as orc
+    from oracle.problem import OracleProblem
+    from tdep_gb300 import Options, QLists, synth
+
+    cfg = CONFIGS[cfg_name]
+    tmp = tempfile.mkdtemp(prefix="tdg_ref_")
+    extra = {"reps": cfg["reps"]} if "reps" in cfg else {}
+    d = synth.write_config(cfg["synth"], Path(tmp) / cfg["synth"], seed=1, **extra)
+    t0 = time.perf_counter()
+    prob = OracleProblem(d, cfg["grid"]).to_problem()
+    log(f"[bench] oracle problem: n_mode={prob.n_mode} n_full={prob.n_full} n_irr={prob.n_irr} "
+        f"({time.perf_counter() - t0:.1f}s)")
+    opts = Options(temperature=cfg["temperature"], integrationtype=cfg["it"], sigma=1.0, isotopescattering=False,
+                   seed=1, precision="fp64", itertol=1e-6, itermaxsteps=200)
+    if "uneven" in cfg:
+        lo, hi = cfg["uneven"]
+        rng = np.random.default_rng(1)
+        samples = {q: np.sort(rng.choice(np.arange(1, prob.n_full + 1), size=int(rng.integers(lo, hi + 1)),
+                                         replace=False)).astype(np.int32) for q in range(1, prob.n_irr + 1)}
+        lists = QLists.per_irreducible(prob, samples3=samples)
+    else:
+        lists = orc.mc_qlists(prob, opts)
+    return cfg, prob, opts, lists
+
+
 def run_reference(args):
-    cfg, prob, opts, lists = setup(args.config, precision="fp64")
+    cfg, prob, opts, lists = setup_oracle(args.config)
     per_step = max(2.0, 20.0 / max(1, args.steps))
     large = prob.n_mode > 18
     if not large:
