@@ -41,6 +41,8 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "3-phonon triplets/s & κ wall time at 1 GB300, mixed vs FP64 at ≤1e-4 κ rel err"
+KAPPA_TIGHT_TOL = 1e-12  # BTE tolerance of the mixed-vs-FP64 kappa comparisons
+KAPPA_TIGHT_MAXITER = 400
 
 CONFIGS = {
     "rocksalt24": dict(synth="rocksalt", grid=(24, 24, 24), it=2, temperature=300.0,
@@ -100,12 +102,25 @@ def setup(cfg_name, precision="mixed"):
     return cfg, prob, opts, lists
 
 
-# DRAM bytes (read + write) of one launch of the fused kernel, from
+# DRAM bytes (read + write) of one launch of the fused kernel, keyed by workload and path (0 the
+# SIMT kernel k_threephonon, 1 the tensor-core kernel k_threephonon_tc), from
 # `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none -k regex:k_threephonon`
-# on `python bench.py --profile --config <name> --steps 1 --warmup 1` (a one-pass capture).
-# dram__bytes_read.sum + dram__bytes_write.sum of one k_threephonon launch (ncu, one pass), from
-# the launch lists summarised in profiles/
-TRAFFIC_PER_LAUNCH = {"rocksalt16": 40_693_760, "rocksalt24": 460_600_000, "perovskite16": 1_098_100_000}
+# on `python bench.py --profile --config <name> --steps 1 --warmup 1` (a one-pass capture),
+# summarised in profiles/
+TRAFFIC_PER_LAUNCH = {("rocksalt16", 0): 40_693_760, ("rocksalt24", 0): 460_600_000,
+                      ("perovskite16", 0): 1_098_100_000}
+KERNEL_NAMES = {
+    0: "k_threephonon (fused pretransform, FP32 SIMT contraction, FP64 delta weights)",
+    1: "k_threephonon_tc (fused pretransform, tcgen05 BF16x3 contraction with FP32 accumulation in tensor "
+       "memory, FP64 delta weights)",
+    2: "large-cell stage: phases, pretransform, 3 tcgen05 BF16x3 GEMM stages, FP64 delta kernel (time of the "
+       "whole stage)"}
+PRECISION_NOTES = {
+    0: "mixed: FP32 pretransform+contraction, FP64 delta weights/occupations/accumulation",
+    1: "mixed: FP32 pretransform, BF16x3 tensor-core contraction with FP32 accumulation, FP64 delta "
+       "weights/occupations/accumulation",
+    2: "mixed: FP32 pretransform, BF16x3 tensor-core contraction with FP32 accumulation, FP64 delta "
+       "weights/occupations/accumulation"}
 
 
 class ClockSampler:
@@ -395,13 +410,14 @@ def fourphonon_leg(cfg_name, steps):
                 ms34.append(sr.stats["device_ms"])
         quart = sr.stats["quartets"]
         t0 = time.perf_counter()
-        _, ki = sr.kappa(o34)
+        sr.kappa(o34)
         kms = 1e3 * (time.perf_counter() - t0)
+        _, ki = sr.kappa(o34, maxiter=KAPPA_TIGHT_MAXITER, tol=KAPPA_TIGHT_TOL)
         d4 = float(np.median(ms34)) - float(np.median(ms3))
         out[prec] = {"q_quartets": int(quart), "pass_ms_3ph_4ph": float(np.median(ms34)),
                      "pass_ms_3ph_only": float(np.median(ms3)), "fourphonon_ms": d4,
                      "q_quartets_per_s": quart / (d4 / 1e3) if d4 > 0 else None, "kappa_wall_ms": kms,
-                     "kappa_xx": float(ki[0, 0])}
+                     "kappa_xx": float(ki[0, 0]), "kappa_tol": KAPPA_TIGHT_TOL}
     sr.close()
     out["mixed_speedup_3ph_4ph"] = out["fp64"]["pass_ms_3ph_4ph"] / out["mixed"]["pass_ms_3ph_4ph"]
     out["kappa_rel_err_mixed_vs_fp64"] = abs(out["mixed"]["kappa_xx"] / out["fp64"]["kappa_xx"] - 1)
@@ -441,12 +457,16 @@ def measure(cfg_name, args, cpu_budget, with_adjoint=True):
     torch.cuda.synchronize()
     clk = clocks.stop()
     graphs = sr.graph_counts()
+    path, shape = sr.last_path(), sr.last_launch()
     lw_mixed = sr.linewidth.copy()
     xi_mixed = sr.Xi if small else None
     t0 = time.perf_counter()
     ks32, ki32 = sr.kappa(opts)
     kappa_ms = 1e3 * (time.perf_counter() - t0)
     kappa_iters = sr.n_iter
+    # the precision figure compares BTE solutions converged far below the default tolerance,
+    # so that a different stopping iteration does not count as arithmetic error
+    _, ki32 = sr.kappa(opts, maxiter=KAPPA_TIGHT_MAXITER, tol=KAPPA_TIGHT_TOL)
     stats = dict(sr.stats)
 
     adjoint = fp64 = None
@@ -475,7 +495,7 @@ def measure(cfg_name, args, cpu_budget, with_adjoint=True):
         fp64_ms = sr.stats["device_ms"]
         lw64 = sr.linewidth.copy()
         xi64 = sr.Xi
-        _, ki64 = sr.kappa(o64)
+        _, ki64 = sr.kappa(o64, maxiter=KAPPA_TIGHT_MAXITER, tol=KAPPA_TIGHT_TOL)
         kappa_err = float(np.max(np.abs(ki32 - ki64)) / np.max(np.abs(ki64)))
         fp64 = {"value": trip / (fp64_ms / 1e3), "ms_per_step": fp64_ms,
                 "mixed_speedup": fp64_ms / float(np.mean(dev_ms)), "kappa_rel_err_mixed_vs_fp64": kappa_err}
@@ -522,7 +542,7 @@ def measure(cfg_name, args, cpu_budget, with_adjoint=True):
     flop_per_trip = 24 * n**4
     gbs = bytes_per_trip * trip / fused_s / 1e9
     tfs = flop_per_trip * trip / fused_s / 1e12
-    traffic = TRAFFIC_PER_LAUNCH.get(cfg_name)
+    traffic = TRAFFIC_PER_LAUNCH.get((cfg_name, path))
     if n <= 6:
         roof = {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
                 "traffic": traffic, "per_unit": f"{bytes_per_trip} bytes per q-triplet (N_t*33*4 + n^3*8)",
@@ -533,10 +553,7 @@ def measure(cfg_name, args, cpu_budget, with_adjoint=True):
                 "traffic": traffic, "per_unit": f"{flop_per_trip} flop per q-triplet (24 n^4)",
                 "units_per_launch": trip, "peak_source": f"{src} dense bf16",
                 "hbm_frac_of_pretransform": gbs / hbm}
-    roof["kernel"] = stats.get("threephonon_kernel") or (
-        "k_threephonon (fused pretransform, FP32 SIMT contraction, FP64 delta weights)" if small else
-        "large-cell stage: phases, pretransform, 3 tcgen05 BF16x3 GEMM stages, FP64 delta kernel "
-        "(time of the whole stage)")
+    roof["kernel"] = KERNEL_NAMES[path]
 
     # ---- CPU baseline sample and parity of its rows against the GPU runs ----
     if small:
@@ -567,7 +584,7 @@ def measure(cfg_name, args, cpu_budget, with_adjoint=True):
         "roofline": roof, "clocks": clk, "launches": launches, "graphs": graphs, "stats": stats,
         "kappa_ms": kappa_ms, "kappa_iters": kappa_iters, "fp64": fp64, "lw_max": float(lw_mixed.max()),
         "cpu": {"value": cpu_trip / cpu_s, "unit": "q-triplets/s", "cores": cores, "kind": "port", "sample": desc},
-        "parity": parity, "tune": autotune_table(),
+        "parity": parity, "tune": autotune_table(), "path": path, "shape": shape,
     }
 
 
@@ -583,10 +600,7 @@ def run_gb300(args):
         "warmup": args.warmup, "ms_per_step": m["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": cfg["workload"], "mesh": list(cfg["grid"]), "n_mode": n, "q_triplets_per_step": m["trip"],
-                   "precision": m["stats"].get("precision_note") or (
-                       "mixed: FP32 pretransform+contraction, FP64 delta weights/occupations/accumulation" if small
-                       else "mixed: FP32 pretransform, BF16x3 tensor-core contraction with FP32 accumulation, FP64 "
-                            "delta weights/occupations/accumulation"),
+                   "precision": PRECISION_NOTES[m["path"]],
                    "l2": "256 MB buffer written between steps (L2 flush); Xi+od working set 2x%.2f GB" % m["xi_gb"]},
         "e2e": m["e2e"],
         "adjoint": m["adjoint"],
@@ -595,7 +609,7 @@ def run_gb300(args):
         "parity": m["parity"],
         "clocks": m["clocks"],
         "gpu_launches": int(m["launches"]),
-        "launch_shapes": {"autotuned": m["tune"],
+        "launch_shapes": {"autotuned": m["tune"], "fused_kernel": m["shape"],
                           "graph_counts_direct_recorded_replayed": m["graphs"],
                           "note": "warm-up calls run the autotuner trials and record the CUDA graph of the "
                                   "three-phonon kernels; timed calls replay it"},

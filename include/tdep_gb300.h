@@ -210,6 +210,13 @@ int tdg_graph_counts(tdg_ctx *ctx, int64_t *counts);
  * yet. The environment variable TDG_TC_SMALL=0 turns path 1 off. */
 int tdg_last_path(tdg_ctx *ctx, int32_t *path);
 
+/* Launch shape of the fused three-phonon kernel in the context's last tdg_scattering (no
+ * reference counterpart): shape[0] the grid (CTAs), shape[1] the CTAs per SM it was sized
+ * for, shape[2] the CUDA runtime's occupancy figure for one SM, shape[3] the count from the
+ * kernel's registers and shared memory; all -1 before the first call and on the large-cell
+ * path. */
+int tdg_last_launch(tdg_ctx *ctx, int32_t *shape);
+
 /*
  * Launch-shape autotuner (no reference counterpart). The first scattering call that needs a
  * launch shape for its mode count, precision and device (the persistent grid of the fused

@@ -127,6 +127,7 @@ SIGNATURES = {
                                       _f64p]),
     "tdg_kappa_iter_vjp": (C.c_int, [C.c_void_p, C.POINTER(TdgOpts), _f64p, C.c_int32, C.c_double, _f64p, _i32p]),
     "tdg_last_path": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "tdg_last_launch": (C.c_int, [C.c_void_p, _i32p]),
     "tdg_pool_usage": (C.c_int, [C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "tdg_natural_isotopes": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "tdg_autotune_load": (C.c_int, [C.c_char_p]),

@@ -15,6 +15,7 @@
 
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
 #include <fstream>
 #include <map>
@@ -87,6 +88,48 @@ bool trials_enabled() {
 }
 
 }  // namespace
+
+int resident_ctas(const void *fn, int threads, size_t dyn_bytes, int *api_out, int *count_out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_bytes) != cudaSuccess ||
+        cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared) !=
+            cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    int api = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&api, fn, threads, dyn_bytes) != cudaSuccess) {
+        cudaGetLastError();
+        api = 0;
+    }
+    // the same count from the kernel's registers and shared memory: registers in units of 256
+    // per warp, shared memory per CTA with the driver's reserve, in units of 128 bytes
+    cudaFuncAttributes fa;
+    int regs_sm = 0, smem_sm = 0, smem_res = 0, thr_sm = 0;
+    int count = 0;
+    if (cudaFuncGetAttributes(&fa, fn) == cudaSuccess &&
+        cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&smem_res, cudaDevAttrReservedSharedMemoryPerBlock, dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev) == cudaSuccess) {
+        const int warps = (threads + 31) / 32;
+        const long regs_cta = (long)warps * (((long)fa.numRegs * 32 + 255) / 256 * 256);
+        const long smem_cta = ((long)dyn_bytes + (long)fa.sharedSizeBytes + smem_res + 127) / 128 * 128;
+        const long by_regs = regs_cta > 0 ? regs_sm / regs_cta : 64;
+        const long by_smem = smem_cta > 0 ? smem_sm / smem_cta : 64;
+        const long by_thr = thr_sm / (warps * 32);
+        count = (int)std::min(std::min(by_regs, by_smem), by_thr);
+    } else {
+        cudaGetLastError();
+    }
+    if (api_out) *api_out = api;
+    if (count_out) *count_out = count;
+    return std::max(api, count);
+}
 
 std::string tune_key(const char *kernel, int n, int precision, int device) {
     cudaDeviceProp prop;

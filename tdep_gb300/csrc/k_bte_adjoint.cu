@@ -1,8 +1,9 @@
 // Adjoint of the iterative BTE solution (kappa.f90:326-495) with respect to the three-phonon
 // scattering matrix: the device parts of tdg_kappa_iter_vjp.
 //
-// At the converged fixed point F = F0 + D(-Q^-1 X T F) (T the foldout of kappa.f90:382-404,
-// X = Xi, Q = diag(qs), D the degeneracy averaging of :418-435), the cotangent lambda of F
+// At the converged fixed point F = G(-Q^-1 X T F, F0) (T the foldout of kappa.f90:382-404,
+// X = Xi, Q = diag(qs), G the in-place degeneracy averaging and F0 addition of :418-435,
+// whose part linear in the update is the degeneracy average D), the cotangent lambda of F
 // solves lambda = kbar - T^T X^T Q^-1 D lambda; the scattering matrix then receives the
 // rank-3 cotangent W(r, c) = -sum_d z(r, d) (T F)(c, d) with z = Q^-1 D lambda, which is
 // mapped back through the row symmetrisations (symmetrize_scatmat, scattering.f90:296-357,

@@ -432,18 +432,8 @@ __global__ void __launch_bounds__(threads4_for(N), min_blocks4(N, sizeof(R) == 8
 template <int N, typename R>
 int grid_n(int n_sm, int n_quart) {
     const Layout4 L = make_layout4(N, sizeof(typename CT<R>::C));
-    if (cudaFuncSetAttribute(k_fourphonon<N, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total) !=
-        cudaSuccess) {
-        cudaGetLastError();
-        return 0;
-    }
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fourphonon<N, R>, threads4_for(N), L.total) !=
-            cudaSuccess ||
-        per_sm < 1) {
-        cudaGetLastError();
-        return 0;
-    }
+    const int per_sm = resident_ctas((const void *)k_fourphonon<N, R>, threads4_for(N), L.total, nullptr, nullptr);
+    if (per_sm < 1) return 0;
     int grid = n_sm * per_sm;
     if (grid > n_quart) grid = n_quart;
     return grid < 1 ? 1 : grid;

@@ -503,24 +503,13 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
 }
 
 // Persistent grid: resident CTAs per SM times the SM count, at most one CTA per item.
-// Persistent grid: resident CTAs per SM times the SM count, at most one CTA per item.
 // `extra` bytes of dynamic shared memory follow the kernel's layout (adjoint accumulator).
 template <int N, typename R, bool ADJ>
-int grid_n(int n_sm, int n_trip, size_t extra, int ctas_per_sm = 0) {
+int grid_n(int n_sm, int n_trip, size_t extra, int ctas_per_sm = 0, int *api = nullptr, int *count = nullptr) {
     const Layout L = make_layout(N, sizeof(typename CT<R>::C), ADJ);
     const size_t bytes = L.total + extra;
-    if (cudaFuncSetAttribute(k_threephonon<N, R, ADJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
-        cudaSuccess) {
-        cudaGetLastError();
-        return 0;
-    }
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_threephonon<N, R, ADJ>, threads_for(N), bytes) !=
-            cudaSuccess ||
-        per_sm < 1) {
-        cudaGetLastError();
-        return 0;
-    }
+    int per_sm = resident_ctas((const void *)k_threephonon<N, R, ADJ>, threads_for(N), bytes, api, count);
+    if (per_sm < 1) return 0;
     if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
     const int grid = n_sm * per_sm;
     return grid > n_trip ? (n_trip > 0 ? n_trip : 1) : grid;
@@ -541,14 +530,14 @@ cudaError_t launch_n(const ThreePhArgs &a, int n_sm, int ctas_per_sm, cudaStream
 }
 
 template <typename R, bool ADJ>
-int grid_prec(int n, int n_sm, int n_trip, size_t extra) {
+int grid_prec(int n, int n_sm, int n_trip, size_t extra, int *api = nullptr, int *count = nullptr) {
     switch (n) {
-        case 3: return grid_n<3, R, ADJ>(n_sm, n_trip, extra);
-        case 6: return grid_n<6, R, ADJ>(n_sm, n_trip, extra);
-        case 9: return grid_n<9, R, ADJ>(n_sm, n_trip, extra);
-        case 12: return grid_n<12, R, ADJ>(n_sm, n_trip, extra);
-        case 15: return grid_n<15, R, ADJ>(n_sm, n_trip, extra);
-        case 18: return grid_n<18, R, ADJ>(n_sm, n_trip, extra);
+        case 3: return grid_n<3, R, ADJ>(n_sm, n_trip, extra, 0, api, count);
+        case 6: return grid_n<6, R, ADJ>(n_sm, n_trip, extra, 0, api, count);
+        case 9: return grid_n<9, R, ADJ>(n_sm, n_trip, extra, 0, api, count);
+        case 12: return grid_n<12, R, ADJ>(n_sm, n_trip, extra, 0, api, count);
+        case 15: return grid_n<15, R, ADJ>(n_sm, n_trip, extra, 0, api, count);
+        case 18: return grid_n<18, R, ADJ>(n_sm, n_trip, extra, 0, api, count);
         default: return 0;
     }
 }
@@ -612,9 +601,10 @@ cudaError_t launch_threephonon(const ThreePhArgs &a, int precision, int n_sm, in
     return launch_prec<float>(a, n_sm, ctas_per_sm, s);
 }
 
-int threephonon_max_per_sm(int n, int precision) {
+int threephonon_max_per_sm(int n, int precision, int *api, int *count) {
     // grid_n with one SM and an unbounded item count gives the CTAs that fit on one SM
-    return precision == 0 ? grid_prec<double, false>(n, 1, 1 << 30, 0) : grid_prec<float, false>(n, 1, 1 << 30, 0);
+    return precision == 0 ? grid_prec<double, false>(n, 1, 1 << 30, 0, api, count)
+                          : grid_prec<float, false>(n, 1, 1 << 30, 0, api, count);
 }
 
 int threephonon_adjoint_grid(int n, int precision, int n_sm, int n_trip, int n_fc, bool acc_in_smem) {

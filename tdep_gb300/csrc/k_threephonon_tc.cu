@@ -394,22 +394,17 @@ __global__ void k_tc_eimg(int32_t n_full, int32_t n, const float2 *egvs32, unsig
 }
 
 template <int N>
-int tc_grid(const ThreePhArgs &a, int n_sm, int ctas_per_sm) {
-    const size_t bytes = tc_layout(N, a.fc.n).total;
-    if (cudaFuncSetAttribute(k_threephonon_tc<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
-        cudaSuccess) {
-        cudaGetLastError();
-        return 0;
-    }
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_threephonon_tc<N>, kTcThreads, bytes) !=
-            cudaSuccess ||
-        per_sm < 1) {
-        cudaGetLastError();
-        return 0;
-    }
+int tc_per_sm(int n_fc, int *api, int *count) {
+    const size_t bytes = tc_layout(N, n_fc).total;
+    const int per_sm = resident_ctas((const void *)k_threephonon_tc<N>, kTcThreads, bytes, api, count);
     // tensor memory: 64 columns per CTA, 512 per SM
-    if (per_sm > 8) per_sm = 8;
+    return per_sm > 8 ? 8 : per_sm;
+}
+
+template <int N>
+int tc_grid(const ThreePhArgs &a, int n_sm, int ctas_per_sm) {
+    int per_sm = tc_per_sm<N>(a.fc.n, nullptr, nullptr);
+    if (per_sm < 1) return 0;
     if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
     const int grid = n_sm * per_sm;
     return grid > a.n_trip ? (a.n_trip > 0 ? a.n_trip : 1) : grid;
@@ -430,15 +425,11 @@ bool threephonon_tc_supported(int n, int precision, int n_fc) {
     return tc_layout(n, n_fc).total <= 110 * 1024;  // at least two CTAs per SM
 }
 
-int threephonon_tc_max_per_sm(int n, int n_fc) {
-    ThreePhArgs a;
-    memset(&a, 0, sizeof a);
-    a.fc.n = n_fc;
-    a.n_trip = 1 << 30;
+int threephonon_tc_max_per_sm(int n, int n_fc, int *api, int *count) {
     switch (n) {
-        case 9: return tc_grid<9>(a, 1, 0);
-        case 12: return tc_grid<12>(a, 1, 0);
-        case 15: return tc_grid<15>(a, 1, 0);
+        case 9: return tc_per_sm<9>(n_fc, api, count);
+        case 12: return tc_per_sm<12>(n_fc, api, count);
+        case 15: return tc_per_sm<15>(n_fc, api, count);
         default: return 0;
     }
 }

@@ -198,6 +198,9 @@ struct tdg_ctx {
     DevBuf<int32_t> d_tc_toff;
     bool tc_eimg_ready = false;
     int last_path = -1;  // 0 SIMT fused kernel, 1 tensor-core fused kernel, 2 large-cell batches
+    // fused three-phonon launch of the last scattering call: grid, CTAs per SM used, the
+    // runtime's occupancy figure and the register/shared-memory count (-1 before any)
+    int last_launch[4] = {-1, -1, -1, -1};
     DevBuf<double2> tw;
     DevBuf<float2> tw32;
     DevBuf<double> d_exp2tab, d_invom;
@@ -428,6 +431,12 @@ void destroy_ctx(tdg_ctx *c) {
 extern "C" int tdg_last_path(tdg_ctx *c, int32_t *path) {
     if (!c || !path) return set_error(kErrParam, "tdg_last_path: null argument");
     *path = c->last_path;
+    return kOk;
+}
+
+extern "C" int tdg_last_launch(tdg_ctx *c, int32_t *shape) {
+    if (!c || !shape) return set_error(kErrParam, "tdg_last_launch: null argument");
+    for (int i = 0; i < 4; ++i) shape[i] = c->last_path == 2 ? -1 : c->last_launch[i];
     return kOk;
 }
 
@@ -1423,7 +1432,9 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
             launches += 6 * ((ntrip + nbmax - 1) / std::max(nbmax, 1));
         } else {
             // persistent grid (CTAs per SM), timed on a prefix of the q-triplets
-            const int maxps = use_tc ? threephonon_tc_max_per_sm(n, c->n_fc3) : threephonon_max_per_sm(n, o->precision);
+            int occ_api = 0, occ_count = 0;
+            const int maxps = use_tc ? threephonon_tc_max_per_sm(n, c->n_fc3, &occ_api, &occ_count)
+                                     : threephonon_max_per_sm(n, o->precision, &occ_api, &occ_count);
             std::vector<int> cand;
             for (int v : {maxps, (3 * maxps + 3) / 4, (maxps + 1) / 2})
                 if (v >= 1 && std::find(cand.begin(), cand.end(), v) == cand.end()) cand.push_back(v);
@@ -1443,6 +1454,11 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
             gk << (use_tc ? "t" : "f") << cps << '/' << std::string(reinterpret_cast<const char *>(&a), sizeof a);
             body3 = [&, fused]() { return fused(a, cps); };
             launches += use_tc ? 2 : 1;
+            const int used = (cps > 0 && cps < maxps) ? cps : maxps;
+            c->last_launch[0] = (int)std::min<int64_t>((int64_t)c->n_sm * used, std::max(ntrip, 1));
+            c->last_launch[1] = used;
+            c->last_launch[2] = occ_api;
+            c->last_launch[3] = occ_count;
         }
         CUDA_TRY(run_graph_region(c, c->graph3, gk.str(), s, body3));
         // (events recorded inside a graph cannot be timed against the others: ev[3] stays out)
@@ -2146,24 +2162,34 @@ extern "C" int tdg_kappa_iter_vjp(tdg_ctx *c, const tdg_opts *o, const double *k
     CUDA_TRY(launch_xi_rowdot(c->d_xi.p, nr, ncol, c->d_tf.p, c->d_xtf.p, s));
     CUDA_TRY(copy_async(xtf.data(), c->d_xtf.p, sizeof(double) * xtf.size(), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
-    // degeneracy averaging (kappa.f90:418-435) of an irreducible array, in place
-    auto degen_avg = [&](std::vector<double> &a) {
-        std::vector<double> out(a.size());
+    // Transpose of distributeF (kappa.f90:418-435). Forward, for b1 = 1..n in turn and in
+    // place: every member of the degenerate set of b1 becomes the set's mean, then F0(b1) is
+    // added to entry b1, so an F0 added early is averaged again by the later members of its
+    // set. Reverse, b1 = n..1: the cotangent of entry b1 goes to F0(b1), then the set's
+    // cotangents are replaced by their mean. lam is the cotangent of the result, xb that of
+    // the update Fnb, f0b (may be null) that of F0.
+    auto distribute_adj = [&](const std::vector<double> &lam, std::vector<double> &xb, std::vector<double> *f0b) {
+        xb = lam;
+        if (f0b) f0b->assign(lam.size(), 0.0);
         for (int q1 = 0; q1 < nirr; ++q1) {
             const int f = c->irr_full[q1] - 1;
-            for (int b1 = 0; b1 < n; ++b1) {
+            double *a = &xb[(size_t)q1 * n * 3];
+            for (int b1 = n - 1; b1 >= 0; --b1) {
+                if (f0b)
+                    for (int x = 0; x < 3; ++x) (*f0b)[((size_t)q1 * n + b1) * 3 + x] += a[b1 * 3 + x];
                 const int dg = c->degen[(size_t)f * n + b1];
+                if (dg == 1) continue;
                 const int32_t *dm = &c->degen_mode[((size_t)f * n + b1) * n];
                 for (int x = 0; x < 3; ++x) {
                     double sum = 0.0;
-                    for (int j = 0; j < dg; ++j) sum += a[((size_t)q1 * n + dm[j] - 1) * 3 + x];
-                    out[((size_t)q1 * n + b1) * 3 + x] = sum / dg;
+                    for (int j = 0; j < dg; ++j) sum += a[(dm[j] - 1) * 3 + x];
+                    sum /= (double)dg;
+                    for (int j = 0; j < dg; ++j) a[(dm[j] - 1) * 3 + x] = sum;
                 }
             }
         }
-        a.swap(out);
     };
-    // z_r = (D lambda)_r / qs_r on the rows
+    // z_r = xb_r / qs_r on the rows (applyXi sets Fnb = -buf / qs, or 0 where qs < lo_freqtol)
     auto make_z = [&](const std::vector<double> &dl) {
         for (int r = 0; r < nr; ++r) {
             const int q1 = c->row_q1[r] - 1, b1 = c->row_b1[r] - 1;
@@ -2172,15 +2198,14 @@ extern "C" int tdg_kappa_iter_vjp(tdg_ctx *c, const tdg_opts *o, const double *k
                 z[(size_t)r * 3 + x] = qs < kFreqTol ? 0.0 : dl[((size_t)q1 * n + b1) * 3 + x] / qs;
         }
     };
-    // adjoint fixed point lambda = kbar - T^T X^T Q^-1 D lambda, iterated with the forward
+    // adjoint fixed point lambda = kbar - T^T X^T Q^-1 xb(lambda), iterated with the forward
     // pass's mixing schedule and convergence test (kappa.f90:437-490)
-    std::vector<double> lam = kbar, nw(nf), dl;
+    std::vector<double> lam = kbar, nw(nf), dl, f0b;
     std::vector<double> scf;
     double mix = 0.95;
     int it = 0;
     for (it = 1; it <= maxiter; ++it) {
-        dl = lam;
-        degen_avg(dl);
+        distribute_adj(lam, dl, nullptr);
         make_z(dl);
         CUDA_TRY(copy_async(c->d_zv.p, z.data(), sizeof(double) * z.size(), cudaMemcpyHostToDevice, s));
         CUDA_TRY(launch_xit_gemv(c->d_xi.p, nr, ncol, c->d_zv.p, c->d_xpart.p, c->d_yv.p, s));
@@ -2212,10 +2237,10 @@ extern "C" int tdg_kappa_iter_vjp(tdg_ctx *c, const tdg_opts *o, const double *k
         if (it > 15 && mix > 0.50) mix *= 0.98;
     }
     if (n_iter) *n_iter = std::min(it, maxiter);
-    dl = lam;
-    degen_avg(dl);
+    distribute_adj(lam, dl, &f0b);
     make_z(dl);
-    // linewidth cotangent: F0 = v / qs and the 1/qs of the update, qs = 2 linewidth
+    // linewidth cotangent: F0 = v / qs (set where linewidth > lo_freqtol) and the 1/qs of the
+    // update, qs = 2 linewidth
     for (size_t i = 0; i < (size_t)nirr * n; ++i) lw_bar[i] = 0.0;
     for (int r = 0; r < nr; ++r) {
         const int q1 = c->row_q1[r] - 1, b1 = c->row_b1[r] - 1;
@@ -2227,7 +2252,7 @@ extern "C" int tdg_kappa_iter_vjp(tdg_ctx *c, const tdg_opts *o, const double *k
         double g = 0.0;
         for (int x = 0; x < 3; ++x) g += dl[i * 3 + x] * xtf[(size_t)r * 3 + x];
         if (c->linewidth[i] > kFreqTol)
-            for (int x = 0; x < 3; ++x) g -= lam[i * 3 + x] * v[x];
+            for (int x = 0; x < 3; ++x) g -= f0b[i * 3 + x] * v[x];
         lw_bar[i] = 2.0 * g / (qs * qs);
     }
     // Xi cotangent W = -z (T F)^T through the adjoint row symmetrisations, given the raw

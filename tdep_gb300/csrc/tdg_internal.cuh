@@ -161,8 +161,9 @@ struct ThreePhArgs {
 };
 // ctas_per_sm: persistent grid of n_sm * ctas_per_sm CTAs (0 or more than fit: as many as fit).
 cudaError_t launch_threephonon(const ThreePhArgs &a, int precision, int n_sm, int ctas_per_sm, cudaStream_t s);
-// CTAs of the fused kernel that fit on one SM (0 if the configuration is not supported).
-int threephonon_max_per_sm(int n, int precision);
+// CTAs of the fused kernel per SM (resident_ctas; 0 if the configuration is not supported);
+// api and count (may be null) receive resident_ctas's two figures.
+int threephonon_max_per_sm(int n, int precision, int *api = nullptr, int *count = nullptr);
 // Adjoint of the three-phonon Gamma with respect to mwm: recomputes Psi per q-triplet and
 // accumulates 2 Re(phase * Q) into a.mwm_bar (one slice per CTA of the returned grid).
 int threephonon_adjoint_grid(int n, int precision, int n_sm, int n_trip, int n_fc, bool acc_in_smem);
@@ -172,7 +173,9 @@ cudaError_t launch_sum_slices(const double *slices, int32_t n_slice, int64_t n, 
 size_t threephonon_smem_bytes(int n, int precision, int n_fc);
 // Tensor-core fused kernel for 9, 12 or 15 modes in mixed precision (k_threephonon_tc.cu).
 bool threephonon_tc_supported(int n, int precision, int n_fc);
-int threephonon_tc_max_per_sm(int n, int n_fc);
+// CTAs per SM of the tensor-core kernel (resident_ctas, at most 8 for the tensor memory);
+// api and count (may be null) receive resident_ctas's two figures.
+int threephonon_tc_max_per_sm(int n, int n_fc, int *api = nullptr, int *count = nullptr);
 cudaError_t launch_threephonon_tc(const ThreePhArgs &a, int n_sm, int ctas_per_sm, cudaStream_t s);
 // Floats of the transposed force-constant copy, its builder (one CTA, n_blk <= 256) and the
 // eigenvector images (n <= 16).
@@ -399,5 +402,11 @@ int tune_lookup(const std::string &key, int dflt);
 // tuned is true when trials ran (their outputs are the caller's to discard).
 cudaError_t tune_pick(const std::string &key, const std::vector<int> &cand, int dflt,
                       const std::function<cudaError_t(int)> &trial, cudaStream_t s, int &choice, bool &tuned);
+// Resident CTAs per SM of kernel fn with `threads` threads and dyn_bytes of dynamic shared
+// memory (the attribute is set, with the largest shared-memory carveout): the larger of the
+// runtime's occupancy figure (api_out) and the count from the kernel's registers and shared
+// memory (count_out); 0 when neither is available. A persistent grid sized from it that is
+// larger than what fits only queues the surplus CTAs.
+int resident_ctas(const void *fn, int threads, size_t dyn_bytes, int *api_out, int *count_out);
 
 }  // namespace tdg

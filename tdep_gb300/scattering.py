@@ -372,6 +372,15 @@ class ScatteringRates:
         N.check(self._lib.tdg_last_path(self._ctx, C.byref(v)), "tdg_last_path")
         return int(v.value)
 
+    def last_launch(self) -> dict:
+        """Launch shape of the fused three-phonon kernel in the last generate()
+        (tdg_last_launch): grid, CTAs per SM used, the runtime's occupancy figure and the
+        register/shared-memory count; -1 each on the large-cell path."""
+        v = np.zeros(4, dtype=np.int32)
+        N.check(self._lib.tdg_last_launch(self._ctx, N.ptr(v, C.c_int32)), "tdg_last_launch")
+        return {"grid": int(v[0]), "ctas_per_sm": int(v[1]), "occupancy_api": int(v[2]),
+                "occupancy_count": int(v[3])}
+
     def graph_counts(self) -> list[int]:
         """Direct runs, CUDA-graph recordings and replays of the three-phonon kernels on this
         context (tdg_graph_counts)."""

@@ -417,8 +417,10 @@ def test_tensor_core_contraction_matches_fp64(configs, name, grid, it):
     assert sr.stats["triplets"] == n64
     _, ktc = sr.kappa(otc)
     sr.close()
-    big = lw64 > 1e-3 * lw64.max()
-    assert np.max(np.abs(lwtc[big] / lw64[big] - 1)) < 1e-4
+    # the BF16x3 operands keep 16 of the 24 mantissa bits, so the error of a small |Psi|^2 is
+    # set by the largest terms of its contraction: rtol 1e-4 plus 1e-6 of the largest linewidth,
+    # the bar of the fused tensor-core kernel's test
+    np.testing.assert_allclose(lwtc, lw64, rtol=1e-4, atol=1e-6 * lw64.max())
     np.testing.assert_allclose(ktc, k64, rtol=MIXED_KAPPA_RTOL, atol=MIXED_KAPPA_RTOL * np.abs(k64).max())
 
 
