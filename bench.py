@@ -106,19 +106,22 @@ def setup(cfg_name, precision="mixed"):
 # SIMT kernel k_threephonon, 1 the tensor-core kernel k_threephonon_tc), from
 # `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none -k regex:k_threephonon`
 # on `python bench.py --profile --config <name> --steps 1 --warmup 1` (a one-pass capture),
-# summarised in profiles/
+# summarised in profiles/. The tensor-core kernel's figure for perovskite16 is its perovskite12
+# capture (224.8 MB for 19404 q-triplets) scaled by the q-triplets of one launch (101233):
+# its traffic is the Xi row scatter, which grows with the q-triplets.
 TRAFFIC_PER_LAUNCH = {("rocksalt16", 0): 40_693_760, ("rocksalt24", 0): 460_600_000,
-                      ("perovskite16", 0): 1_098_100_000}
+                      ("perovskite16", 0): 1_098_100_000, ("perovskite12", 1): 224_781_312,
+                      ("perovskite16", 1): 1_172_700_000}
 KERNEL_NAMES = {
     0: "k_threephonon (fused pretransform, FP32 SIMT contraction, FP64 delta weights)",
     1: "k_threephonon_tc (fused pretransform, tcgen05 BF16x3 contraction with FP32 accumulation in tensor "
-       "memory, FP64 delta weights)",
+       "memory, FP32 delta weights, FP64 sums)",
     2: "large-cell stage: phases, pretransform, 3 tcgen05 BF16x3 GEMM stages, FP64 delta kernel (time of the "
        "whole stage)"}
 PRECISION_NOTES = {
     0: "mixed: FP32 pretransform+contraction, FP64 delta weights/occupations/accumulation",
-    1: "mixed: FP32 pretransform, BF16x3 tensor-core contraction with FP32 accumulation, FP64 delta "
-       "weights/occupations/accumulation",
+    1: "mixed: FP32 pretransform, BF16x3 tensor-core contraction with FP32 accumulation, FP32 delta weights "
+       "of the survivors (FP64 centre differences), FP64 sums/accumulation",
     2: "mixed: FP32 pretransform, BF16x3 tensor-core contraction with FP32 accumulation, FP64 delta "
        "weights/occupations/accumulation"}
 
@@ -352,8 +355,9 @@ def run_reference(args):
 
 def run_profile(args):
     """--profile: warm-up passes then `steps` passes of one stage, nothing else (for ncu):
-    scattering (generate), kappa (one generate, then BTE solves) or offdiag (one generate,
-    then off-diagonal kappa)."""
+    scattering (generate), kappa (one generate, then BTE solves), offdiag (one generate,
+    then off-diagonal kappa) or adjoint (one generate and kappa_SMA, then d kappa_xx / d Phi3
+    passes)."""
     from tdep_gb300 import ScatteringRates
 
     cfg, prob, opts, lists = setup(args.config, precision=args.precision)
@@ -361,6 +365,14 @@ def run_profile(args):
     if args.stage == "scattering":
         for _ in range(args.warmup + args.steps):
             sr.generate(opts, lists)
+    elif args.stage == "adjoint":
+        sr.generate(opts, lists)
+        sr.kappa(opts, maxiter=0)
+        kb = np.zeros((3, 3))
+        kb[0, 0] = 1.0
+        lw_bar = sr.kappa_sma_vjp(opts, kb)
+        for _ in range(args.warmup + args.steps):
+            sr.adjoint_fc3(opts, lw_bar)
     else:
         sr.generate(opts, lists)
         for _ in range(args.warmup + args.steps):
@@ -644,7 +656,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--profile", action="store_true", help="only run passes of one stage, see --stage (for ncu captures)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"], help="with --profile")
-    ap.add_argument("--stage", default="scattering", choices=["scattering", "kappa", "offdiag"], help="with --profile")
+    ap.add_argument("--stage", default="scattering", choices=["scattering", "kappa", "offdiag", "adjoint"],
+                    help="with --profile")
     args = ap.parse_args()
     if args.profile:
         run_profile(args)

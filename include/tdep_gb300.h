@@ -406,10 +406,22 @@ int tdg_kappa_offdiag(tdg_ctx *ctx, const tdg_opts *opts, double *kappa_offdiag)
  * reads infile.ucposcar, infile.forceconstant, infile.forceconstant_thirdorder and, when
  * fourthorder != 0, infile.forceconstant_fourthorder from `dir` (masses from infile.isotopes
  * when readiso != 0), finds the symmetry operations, builds the FFT mesh `grid` and the
- * harmonic phonons. The returned problem owns its arrays; free with tdg_problem_free.
+ * harmonic phonons: the irreducible points are diagonalised and the rest of the mesh takes
+ * their rotated eigenvectors (type_phonon_dispersions_generation.f90:72-170). The returned
+ * problem owns its arrays; free with tdg_problem_free.
  */
 int tdg_problem_load(const char *dir, const int32_t grid[3], int fourthorder, int readiso,
                      int timereversal, tdg_problem **out);
+/*
+ * The same with the harmonic stage on GPU `device` (no reference counterpart; it replaces the
+ * host work of tdg_problem_load inside main.f90:42-181): D(q) and dD/dq at the irreducible
+ * points with the polar Ewald sum, a batched Jacobi eigensolver, the degenerate-subspace
+ * gauge, velocities and degeneracy tables, and the unfold onto the mesh, in FP64; at most 128
+ * modes. The readers, the symmetry search and the mesh stay on the host. Results equal
+ * tdg_problem_load's to rounding. Allocates and frees its own device memory.
+ */
+int tdg_problem_load_device(const char *dir, const int32_t grid[3], int fourthorder, int readiso,
+                            int timereversal, int32_t device, tdg_problem **out);
 void tdg_problem_free(tdg_problem *prob);
 
 /*

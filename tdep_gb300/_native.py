@@ -142,6 +142,8 @@ SIGNATURES = {
     "tdg_adjoint_fc3": (C.c_int, [C.c_void_p, C.POINTER(TdgOpts), _f64p, _f64p, _f64p]),
     "tdg_kappa": (C.c_int, [C.c_void_p, C.POINTER(TdgOpts), C.c_int32, C.c_double, _f64p, _f64p, _f64p, _i32p]),
     "tdg_problem_load": (C.c_int, [C.c_char_p, _i32p, C.c_int, C.c_int, C.c_int, C.POINTER(C.POINTER(TdgProblem))]),
+    "tdg_problem_load_device": (C.c_int, [C.c_char_p, _i32p, C.c_int, C.c_int, C.c_int, C.c_int32,
+                                          C.POINTER(C.POINTER(TdgProblem))]),
     "tdg_problem_free": (None, [C.POINTER(TdgProblem)]),
     "tdg_write_outfile": (C.c_int, [C.c_char_p, C.c_double, _f64p, _f64p, _f64p]),
     "tdg_phonon_frequencies": (C.c_int, [C.c_char_p, C.c_int32, _f64p, _f64p, _f64p]),

@@ -30,7 +30,7 @@ NVCCFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-re
 
 HOST_SRC = ["host/crystal.cpp", "host/qmesh.cpp", "host/phonons.cpp", "host/mcgrid.cpp", "host/problem.cpp",
             "host/h5write.cpp", "host/gridout.cpp", "host/forcemap.cpp"]
-CUDA_SRC = ["k_triplets.cu", "k_threephonon.cu", "k_fourphonon.cu", "k_misc.cu", "tdg_api.cu", "tdg_noalloc.cu", "k_tcgemm.cu", "k_largecell.cu", "k_offdiag.cu", "autotune.cu", "k_threephonon_tc.cu", "k_bte_adjoint.cu"]
+CUDA_SRC = ["k_triplets.cu", "k_threephonon.cu", "k_fourphonon.cu", "k_misc.cu", "tdg_api.cu", "tdg_noalloc.cu", "k_tcgemm.cu", "k_largecell.cu", "k_offdiag.cu", "autotune.cu", "k_threephonon_tc.cu", "k_bte_adjoint.cu", "k_harmonic.cu"]
 HEADERS = ["host/common.hpp", "host/crystal.hpp", "tdg_internal.cuh", "dev_common.cuh", "tc_common.cuh",
            "k3_parts.cuh", "host/h5write.hpp"]
 

@@ -126,8 +126,24 @@ struct Phonons {
     std::vector<int32_t> degen_mode; // n_full*n*n
 };
 // D(q) (type_forceconstant_secondorder_dynamicalmatrix.f90:484-788), Hermitian
-// diagonalisation, group velocities and degeneracy tables at every mesh point.
+// diagonalisation and group velocities at the irreducible points, unfolded onto the mesh
+// with the degeneracy tables (unfold_phonons).
 int build_phonons(const Crystal &c, const FC2 &fc, const QMesh &qp, Phonons &ph);
+// The full mesh from the irreducible points' frequencies, eigenvectors ([q][b][r] complex)
+// and velocities (type_phonon_dispersions_generation.f90:117-170): frequencies and
+// degeneracy tables copied, velocities rotated (negated under time reversal), eigenvectors
+// rotated by lo_eigenvector_transformation_matrix (type_symmetryoperation.f90:243-290) and
+// conjugated under time reversal; fmap and shift as op_atom_maps gives them.
+int unfold_phonons(const Crystal &c, const QMesh &qp, int nb, const double *om_i, const double *egv_i,
+                   const double *vel_i, const std::vector<int32_t> &fmap, const std::vector<double> &shift,
+                   Phonons &ph);
+
+// The same on the GPU `device` (k_harmonic.cu): D(q) and dD/dq at the irreducible points, the
+// Jacobi eigensolver, the subspace gauge, velocities and degeneracy, the unfold; irr_dyngrad
+// receives dD/dq at the irreducible points in the layout of dyn_gradient ([i][x][c][r] complex).
+// Allocates and frees its own device memory.
+int build_phonons_device(const Crystal &c, const FC2 &fc, const QMesh &qp, int device, Phonons &ph,
+                         std::vector<double> &irr_dyngrad);
 
 // Gradient of the mass-weighted dynamical matrix at the Cartesian point q (1/Bohr without
 // 2*pi, as QMesh::q_full) (type_forceconstant_secondorder_dynamicalmatrix.f90:484-788,

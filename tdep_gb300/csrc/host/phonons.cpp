@@ -4,10 +4,11 @@
 // Hermitian diagonalisation (:113-164), group velocities (:167-200) and the degeneracy
 // tables (type_phonon_dispersions.f90:1190-1212).
 //
-// Unlike the reference, which diagonalises the irreducible points and rotates the
-// eigenvectors onto the rest of the mesh, every point is diagonalised directly; the
-// eigenvector gauge inside degenerate subspaces therefore differs, while every
-// degeneracy-summed quantity (linewidths, kappa) is the same.
+// As in the reference (type_phonon_dispersions_generation.f90:72-170), only the irreducible
+// points are diagonalised; every other mesh point takes the frequencies and degeneracy of
+// its irreducible point, the rotated velocities and the eigenvectors rotated by
+// lo_eigenvector_transformation_matrix (type_symmetryoperation.f90:243-290), conjugated
+// under time reversal.
 #include <algorithm>
 #include <numeric>
 #include <thread>
@@ -391,42 +392,78 @@ int build_phonons(const Crystal &c, const FC2 &fc, const QMesh &qp, Phonons &ph)
     V3 kDefaultDir;
     kDefaultDir[0] = 1.0;
     const int nb = 3 * c.na;
-    const int np = qp.n_full;
+    const int np = qp.n_full, ni = qp.n_irr;
+    // irreducible points; the mesh takes the default direction [1,0,0] at Gamma
+    // (type_phonon_dispersions.f90:1099, 1148)
+    std::vector<double> om_i((size_t)ni * nb), egv_i((size_t)ni * nb * nb * 2), vel_i((size_t)ni * nb * 3);
+    std::vector<int> status(ni, kOk);
+    parallel_for(ni, [&](int64_t i) {
+        status[i] = solve_point(c, fc, qp.q_full[qp.irr_full[i] - 1], &kDefaultDir, nb, &om_i[(size_t)i * nb],
+                                &egv_i[(size_t)i * nb * nb * 2], &vel_i[(size_t)i * nb * 3]);
+    });
+    for (int st : status)
+        if (st) return st;
+    std::vector<int32_t> fmap;
+    std::vector<double> shift;
+    int st = op_atom_maps(c, fmap, shift);
+    if (st) return st;
+    return unfold_phonons(c, qp, nb, om_i.data(), egv_i.data(), vel_i.data(), fmap, shift, ph);
+}
+
+int unfold_phonons(const Crystal &c, const QMesh &qp, int nb, const double *om_i, const double *egv_i,
+                   const double *vel_i, const std::vector<int32_t> &fmap, const std::vector<double> &shift,
+                   Phonons &ph) {
+    const int np = qp.n_full, ni = qp.n_irr, na = c.na;
     ph.n_mode = nb;
     ph.omega.assign((size_t)np * nb, 0.0);
     ph.egv.assign((size_t)np * nb * nb * 2, 0.0);
     ph.vel.assign((size_t)np * nb * 3, 0.0);
     ph.degen.assign((size_t)np * nb, 0);
     ph.degen_mode.assign((size_t)np * nb * nb, 0);
-    unsigned nth = std::max(1u, std::thread::hardware_concurrency());
-    nth = std::min<unsigned>(nth, 64);
-    std::vector<int> status(nth, kOk);
-    std::vector<std::thread> th;
-    for (unsigned t = 0; t < nth; ++t)
-        th.emplace_back([&, t]() {
-            for (int q = (int)t; q < np; q += (int)nth) {
-                // The mesh takes the default direction [1,0,0] at Gamma
-                // (type_phonon_dispersions.f90:1099, 1148).
-                int st = solve_point(c, fc, qp.q_full[q], &kDefaultDir, nb, &ph.omega[(size_t)q * nb],
-                                     &ph.egv[(size_t)q * nb * nb * 2], &ph.vel[(size_t)q * nb * 3]);
-                if (st) {
-                    status[t] = st;
-                    return;
-                }
-            }
-        });
-    for (auto &x : th) x.join();
-    for (int st : status)
-        if (st) return st;
-    for (int q = 0; q < np; ++q) {
-        const double *om = &ph.omega[(size_t)q * nb];
+    // degeneracy of the irreducible points (type_phonon_dispersions.f90:1190-1212), copied
+    // onto their stars
+    std::vector<int32_t> dg((size_t)ni * nb), dm((size_t)ni * nb * nb, 0);
+    for (int i = 0; i < ni; ++i) {
+        const double *om = om_i + (size_t)i * nb;
         for (int b1 = 0; b1 < nb; ++b1) {
             int l = 0;
             for (int b2 = 0; b2 < nb; ++b2)
-                if (std::fabs(om[b1] - om[b2]) < kFreqTol) ph.degen_mode[((size_t)q * nb + b1) * nb + l++] = b2 + 1;
-            ph.degen[(size_t)q * nb + b1] = l;
+                if (std::fabs(om[b1] - om[b2]) < kFreqTol) dm[((size_t)i * nb + b1) * nb + l++] = b2 + 1;
+            dg[(size_t)i * nb + b1] = l;
         }
     }
+    parallel_for(np, [&](int64_t q) {
+        const int i = qp.full_irr[q] - 1, iop = qp.full_op[q], o = std::abs(iop) - 1;
+        const M3 &m = c.ops[o].m;
+        const double sg = iop > 0 ? 1.0 : -1.0;
+        const V3 &qi = qp.q_full[qp.irr_full[i] - 1];
+        std::copy(om_i + (size_t)i * nb, om_i + (size_t)(i + 1) * nb, &ph.omega[(size_t)q * nb]);
+        std::copy(&dg[(size_t)i * nb], &dg[(size_t)(i + 1) * nb], &ph.degen[(size_t)q * nb]);
+        std::copy(&dm[(size_t)i * nb * nb], &dm[(size_t)(i + 1) * nb * nb], &ph.degen_mode[(size_t)q * nb * nb]);
+        for (int b = 0; b < nb; ++b) {
+            const double *v = vel_i + ((size_t)i * nb + b) * 3;
+            for (int d = 0; d < 3; ++d)
+                ph.vel[((size_t)q * nb + b) * 3 + d] = sg * (m(d, 0) * v[0] + m(d, 1) * v[1] + m(d, 2) * v[2]);
+        }
+        for (int a2 = 0; a2 < na; ++a2) {
+            const int a1 = fmap[(size_t)o * na + a2];
+            const double *v0 = &shift[((size_t)o * na + a2) * 3];
+            const double arg = -(v0[0] * qi[0] + v0[1] * qi[1] + v0[2] * qi[2]) * kTwoPi;
+            const cplx ph0(std::cos(arg), std::sin(arg));
+            for (int b = 0; b < nb; ++b) {
+                const double *e = egv_i + (((size_t)i * nb + b) * nb + 3 * a2) * 2;
+                for (int x = 0; x < 3; ++x) {
+                    cplx s = 0;
+                    for (int y = 0; y < 3; ++y) s += m(x, y) * cplx(e[2 * y], e[2 * y + 1]);
+                    s *= ph0;
+                    if (iop < 0) s = std::conj(s);
+                    double *out = &ph.egv[(((size_t)q * nb + b) * nb + 3 * a1 + x) * 2];
+                    out[0] = s.real();
+                    out[1] = s.imag();
+                }
+            }
+        }
+    });
     return kOk;
 }
 

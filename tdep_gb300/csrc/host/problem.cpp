@@ -160,9 +160,28 @@ struct ProblemHolder {
 extern "C" const char *tdg_last_error(void) { return tdg::last_error(); }
 extern "C" const char *tdg_version(void) { return "tdep_gb300 0.1 (sm_103a)"; }
 
+namespace tdg {
+namespace {
+int problem_load(const char *dir, const int32_t grid[3], int fourthorder, int readiso, int timereversal, int device,
+                 tdg_problem **out);
+}  // namespace
+}  // namespace tdg
+
 extern "C" int tdg_problem_load(const char *dir, const int32_t grid[3], int fourthorder, int readiso,
                                 int timereversal, tdg_problem **out) {
-    using namespace tdg;
+    return tdg::problem_load(dir, grid, fourthorder, readiso, timereversal, -1, out);
+}
+
+extern "C" int tdg_problem_load_device(const char *dir, const int32_t grid[3], int fourthorder, int readiso,
+                                       int timereversal, int32_t device, tdg_problem **out) {
+    if (device < 0) return tdg::set_error(tdg::kErrParam, "tdg_problem_load_device: negative device");
+    return tdg::problem_load(dir, grid, fourthorder, readiso, timereversal, device, out);
+}
+
+namespace tdg {
+namespace {
+int problem_load(const char *dir, const int32_t grid[3], int fourthorder, int readiso, int timereversal, int device,
+                 tdg_problem **out) {
     if (!dir || !grid || !out) return set_error(kErrParam, "tdg_problem_load: null argument");
     *out = nullptr;
     auto h = std::make_unique<ProblemHolder>();
@@ -191,20 +210,27 @@ extern "C" int tdg_problem_load(const char *dir, const int32_t grid[3], int four
     const int g[3] = {grid[0], grid[1], grid[2]};
     st = build_fft_mesh(h->c, g, timereversal != 0, h->q);
     if (st) return st;
-    st = build_phonons(h->c, fc2, h->q, h->ph);
-    if (st) return st;
+    if (device >= 0) {
+        st = build_phonons_device(h->c, fc2, h->q, device, h->ph, h->irr_dyngrad);
+        if (st) return st;
+    } else {
+        st = build_phonons(h->c, fc2, h->q, h->ph);
+        if (st) return st;
+    }
     // off-diagonal kappa inputs: dD/dq at the irreducible points and the atom maps
     {
         const int nb = 3 * h->c.na, ni = h->q.n_irr;
-        h->irr_dyngrad.assign((size_t)ni * 3 * nb * nb * 2, 0.0);
-        parallel_for(ni, [&](int64_t i) {
-            std::vector<cplx> g((size_t)3 * nb * nb);
-            dyn_gradient(h->c, fc2, h->q.q_full[h->q.irr_full[i] - 1], nb, g.data());
-            for (size_t k = 0; k < g.size(); ++k) {
-                h->irr_dyngrad[((size_t)i * 3 * nb * nb + k) * 2] = g[k].real();
-                h->irr_dyngrad[((size_t)i * 3 * nb * nb + k) * 2 + 1] = g[k].imag();
-            }
-        });
+        if (device < 0) {  // (the device stage returns them with the phonons)
+            h->irr_dyngrad.assign((size_t)ni * 3 * nb * nb * 2, 0.0);
+            parallel_for(ni, [&](int64_t i) {
+                std::vector<cplx> g((size_t)3 * nb * nb);
+                dyn_gradient(h->c, fc2, h->q.q_full[h->q.irr_full[i] - 1], nb, g.data());
+                for (size_t k = 0; k < g.size(); ++k) {
+                    h->irr_dyngrad[((size_t)i * 3 * nb * nb + k) * 2] = g[k].real();
+                    h->irr_dyngrad[((size_t)i * 3 * nb * nb + k) * 2 + 1] = g[k].imag();
+                }
+            });
+        }
         st = op_atom_maps(h->c, h->op_fmap, h->atom_shift);
         if (st) return st;
         for (auto &x : h->op_fmap) x += 1;
@@ -258,6 +284,8 @@ extern "C" int tdg_problem_load(const char *dir, const int32_t grid[3], int four
     *out = &h.release()->p;
     return kOk;
 }
+}  // namespace
+}  // namespace tdg
 
 extern "C" void tdg_problem_free(tdg_problem *prob) {
     if (!prob) return;

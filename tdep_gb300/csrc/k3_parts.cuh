@@ -1,7 +1,8 @@
 // Per-q-triplet stages shared by the two fused three-phonon kernels (the SIMT kernel of
 // k_threephonon.cu and the tensor-core kernel of k_threephonon_tc.cu): loading the mode
-// scalars, the skip rules as bit masks, the FP32 screen of the Gaussians, the FP64 delta
-// weights of the survivors, and the row/column sums with the Gamma and Xi scatter.
+// scalars, the skip rules as bit masks, the FP32 screen of the Gaussians, the delta weights
+// of the survivors (FP64, or FP32 for the tensor-core kernel), and the row/column sums with
+// the Gamma and Xi scatter.
 //
 // Reference (src/thermal_conductivity/scattering_threephonon.f90):
 //   skip rules (:90-101), get_dirac (:219-271), accumulation into Gamma and the Xi row
@@ -195,6 +196,64 @@ __device__ __forceinline__ void k3_survivors(const K3Smem &S, const PhononDev &P
             const double fsum = f0 + f1;
             S.F[idx] = fsum;
             if (nonzero(fsum)) {
+                atomicOr(S.rowbits + b1 * N + b2, 1u << b3);
+                atomicOr(S.colbits + b1 * N + b3, 1u << b2);
+            }
+        }
+    }
+}
+
+// The same in FP32 for the tensor-core kernel (mixed precision): the centre differences
+// om1 - (+-om2 +- om3) in FP64 then rounded to FP32 (relative error 6e-8 of the difference),
+// the width, the exponent and the Gaussian in FP32 (expf), F in FP32 stored as a double
+// for the FP64 sums. Relative error of a weight about 1e-6, against the 1e-5 of the BF16x3
+// contraction; GB300 issues FP64 at 1/64 of the FP32 rate, and this stage was a third of
+// the kernel's FP64 pipe.
+template <int N, typename PsiSq>
+__device__ __forceinline__ void k3_survivors_f32(const K3Smem &S, const PhononDev &P, int nq, float perm,
+                                                 PsiSq psisq) {
+    constexpr int N2 = N * N;
+    constexpr float kSqrt2PiInvF = 0.3989422804014327f;
+    const int it = P.integrationtype;
+    for (int s = threadIdx.x; s < nq; s += blockDim.x) {
+        const uint32_t qv = S.Q[s];
+        const int idx = (int)(qv & 0xffffu);
+        uint32_t live = qv >> 16;
+        const int b1 = idx / N2, b2 = (idx / N) % N, b3 = idx % N;
+        const double o1 = S.om1[b1], o2 = S.om2[b2], o3 = S.om3[b3];
+        float sigma;
+        if (it == 1) {
+            sigma = (float)P.sigma_fixed;
+        } else if (it == 2) {
+            sigma = sqrtf(S.fs1[b1] + S.fs2[b2] + S.fs3[b3]);
+        } else {
+            sigma = (float)(adaptive_pair(S.v1 + 3 * b1, S.v2 + 3 * b2, P.reclat_g) / 3.0 +
+                            adaptive_pair(S.v1 + 3 * b1, S.v3 + 3 * b3, P.reclat_g) / 3.0 +
+                            adaptive_pair(S.v2 + 3 * b2, S.v3 + 3 * b3, P.reclat_g) / 3.0 + P.thresh_sigma);
+        }
+        const float invsig = 1.0f / sigma;
+        const float win8 = 8.0f * sigma, h = 0.5f * invsig * invsig, cg = kSqrt2PiInvF * invsig;
+        float g[4] = {0.f, 0.f, 0.f, 0.f};
+        while (live) {
+            const int j = __ffs(live) - 1;
+            live &= live - 1;
+            // Gaussian j centred at (-om2+om3, om2-om3, om2+om3, -om2-om3), get_dirac's order
+            const double m2 = (j == 1 || j == 2) ? o2 : -o2;
+            const double m3 = (j == 0 || j == 2) ? o3 : -o3;
+            const float dx = (float)(o1 - (m2 + m3));
+            const float gj = fabsf(dx) > win8 ? 0.f : expf(-dx * dx * h) * cg;
+            g[0] = j == 0 ? gj : g[0];
+            g[1] = j == 1 ? gj : g[1];
+            g[2] = j == 2 ? gj : g[2];
+            g[3] = j == 3 ? gj : g[3];
+        }
+        const float d0 = g[0] - g[1], d1 = g[2] - g[3];
+        if (d0 != 0.f || d1 != 0.f) {
+            const float pq = (float)kThreePhononPrefactor * psisq(idx) * (float)S.wrow[b1];
+            const float n2 = (float)S.be2[b2], n3 = (float)S.be3[b3];
+            const float fsum = perm * pq * ((n2 - n3) * d0 + (n2 + n3 + 1.0f) * d1);
+            S.F[idx] = (double)fsum;
+            if (fsum != 0.f) {
                 atomicOr(S.rowbits + b1 * N + b2, 1u << b3);
                 atomicOr(S.colbits + b1 * N + b3, 1u << b2);
             }

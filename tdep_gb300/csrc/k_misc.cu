@@ -199,9 +199,10 @@ __global__ void k_sym_distribute(MeshDev m, OrbitDev o, const int32_t *row_q1, c
 // the row sampled, entries > 0 averaged) and symmetrize_scatmat (scattering.f90:296-357;
 // every orbit, all entries). A CTA takes K = min(256, T / |G_q1|) consecutive orbits of its
 // row's q1 (at most T points), gathers their images' n modes into shared memory with
-// independent loads, averages there in the reference's summation order (each image added
-// mult times, in first-appearance order) and writes the images back. With both passes in
-// one kernel Xi crosses HBM once instead of twice. q1 whose little group is the identity
+// independent loads, averages there (each image weighted by its mult with one FMA, in
+// first-appearance order: the reference adds it mult times, which differs in the last bit)
+// and writes the images back. With both passes in one kernel Xi crosses HBM once instead of
+// twice. q1 whose little group is the identity
 // alone are skipped: every orbit is one point with count 1, and both averages return it.
 __global__ void __launch_bounds__(256) k_sym_tile(MeshDev m, OrbitDev o, const int32_t *row_q1, double *xi,
                                                   const uint32_t *sbits, int do_dist, int do_scat) {
@@ -245,6 +246,9 @@ __global__ void __launch_bounds__(256) k_sym_tile(MeshDev m, OrbitDev o, const i
     for (int it = tid; it < nk * n; it += blockDim.x) {
         const int t = it / n, b2 = it - t * n, k = k0 + t;
         const int p0 = off[t], p1 = off[t + 1];
+        // Each image enters a sum once per operation that gives it (mult, one FMA: the sums
+        // are FP64 on a pipe of 2 operations per clock per SM, the bound of this kernel).
+        bool averaged = false;
         if (do_dist) {
             const int q2 = o.rep[k];
             if ((bits[q2 >> 5] >> (q2 & 31)) & 1u) {
@@ -254,23 +258,23 @@ __global__ void __launch_bounds__(256) k_sym_tile(MeshDev m, OrbitDev o, const i
                     const double v = vals[p * n + b2];
                     if (__double_as_longlong(v) > 0) {  // v > 0, v not NaN
                         nn += pmu[p];
-                        for (int rep = 0; rep < pmu[p]; ++rep) buf += v;
+                        buf = fma(v, (double)pmu[p], buf);
                     }
                 }
                 if (nn) {
                     const double avg = buf * o.rcp[nn];
                     for (int p = p0; p < p1; ++p) vals[p * n + b2] = avg;
+                    averaged = true;
                 }
             }
         }
-        if (do_scat) {
+        // symmetrize_scatmat: the mean over the operations, cnt = sum of mult; on an orbit the
+        // distribution just set to one value that mean is the value itself
+        if (do_scat && !averaged) {
             const int cnt = o.cnt[k];
             if (cnt) {
                 double buf = 0.0;
-                for (int p = p0; p < p1; ++p) {
-                    const double v = vals[p * n + b2];
-                    for (int rep = 0; rep < pmu[p]; ++rep) buf += v;
-                }
+                for (int p = p0; p < p1; ++p) buf = fma(vals[p * n + b2], (double)pmu[p], buf);
                 buf *= o.rcp[cnt];
                 for (int p = p0; p < p1; ++p) vals[p * n + b2] = buf;
             }

@@ -6,25 +6,29 @@
 // Reference (src/thermal_conductivity/scattering_threephonon.f90):
 //   pretransform_phi3 (:275-317)      P(a,b,c) = sum_t mwm_t(i,j,k) exp(-2 pi i (q2.lv2 + q3.lv3))
 //   zgeru x2 + dot_product (:93-113)   Psi(b1,b2,b3) = sum_abc E1(a,b1) E2(b,b2) E3(c,b3) P(a,b,c)
-//   get_dirac (:219-271) and accumulation (:115-135), shared with the SIMT kernel (k3_parts.cuh).
+//   get_dirac (:219-271) and accumulation (:115-135), shared with the SIMT kernel (k3_parts.cuh);
+//   the delta weights of the survivors here in FP32 (k3_survivors_f32), the sums in FP64.
 //
 // Contraction. With the modes padded to 16, each of the three stages contracts one
 // component index of a 16^3 complex tensor with one eigenvector matrix E (16 x 16 complex,
 // e/sqrt(omega), not conjugated), as a real GEMM with M = 256 rows (the two uncontracted
 // indices, two M = 128 tiles), K = 32 and N = 32:
 //   [Yr | Yi] = [Xr | Xi] [[Er, Ei], [-Ei, Er]]
-//   stage 1: rows (b, c), k = a   -> T1 columns b1
-//   stage 2: rows (b1, c), k = b  -> T2 columns b2
+//   stage 1: rows (c, b), k = a   -> T1 columns b1
+//   stage 2: rows (c, b1), k = b  -> T2 columns b2
 //   stage 3: rows (b1, b2), k = c -> Psi columns b3
 // Operands are BF16 hi/lo splits of FP32 values (x = hi + lo, about 16 significant bits);
 // a product is hi*hi + hi*lo + lo*hi accumulated in FP32 in tensor memory (2 accumulators
 // of 32 columns). The B operands (the real-split E of every mesh point, 4 KB each) are
 // built once per context and brought into shared memory by bulk copies on an mbarrier;
 // each stage's accumulator rows are read by the thread of that row (tcgen05.ld), split and
-// stored as the next stage's A operand, with the index rotation of the table above, in
-// 8 x 16-byte core matrices without swizzle (stage 1 and 2 MN-major, stage 3 K-major). The
-// padding (modes and components 15, or 9-15 / 12-15) is zero in P and E and stays exactly
-// zero through the stages.
+// stored as the next stage's A operand, in 8 x 16-byte core matrices without swizzle, all
+// MN-major (a core-matrix row is 8 consecutive M indices at one k). The row orders of the
+// table make every such row one thread's 8 consecutive accumulator columns, so a
+// transition is 16-byte stores. Into the stage-2 operand the 8 lanes of a store phase
+// hold 8 different k (= b) and hit 8 different bank groups; into the stage-3 operand they
+// share k (= c) and conflict. The padding (modes and components 15, or 9-15 / 12-15) is
+// zero in P and E and stays exactly zero through the stages.
 //
 // Pretransform. The force constants are read in a per-block transposed copy (block = atom
 // triple, triplets of a block consecutive and padded to 4), so that the thread of one
@@ -99,6 +103,22 @@ __device__ __forceinline__ void st_split(unsigned char *plane_hi, uint32_t off, 
     tc::split_bf16(x, h, l);
     *(unsigned short *)(plane_hi + off) = h;
     *(unsigned short *)(plane_hi + kAPlane + off) = l;
+}
+
+// One core-matrix row of both planes: the hi and lo parts of x[0..7] as 16 bytes each at
+// off (16-byte aligned) and kAPlane + off.
+__device__ __forceinline__ void st_split8(unsigned char *plane_hi, uint32_t off, const float *x) {
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        unsigned short h0, l0, h1, l1;
+        tc::split_bf16(x[2 * i], h0, l0);
+        tc::split_bf16(x[2 * i + 1], h1, l1);
+        h[i] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+        l[i] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+    }
+    *(uint4 *)(plane_hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
+    *(uint4 *)(plane_hi + kAPlane + off) = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
 // 32 lanes x 32 consecutive columns: thread i of the warp gets lane (base lane + i).
@@ -242,7 +262,7 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a)
         }
         __syncthreads();
         k3_skip_masks<N>(S);
-        // ---- pretransform into the stage-1 operand: rows (b, c), k = a (re) and 16 + a (im) ----
+        // ---- pretransform into the stage-1 operand: rows (c, b), k = a (re) and 16 + a (im) ----
         for (int idx = tid; idx < N3; idx += kTcThreads) {
             const int blk = idx / 27, ijk = idx - 27 * blk;
             const int lo = fc.blk_ptr[blk];
@@ -259,7 +279,7 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a)
             }
             const int a1 = blk / (NA * NA), a2 = (blk / NA) % NA, a3 = blk % NA;
             const int pa = 3 * a1 + ijk % 3, pb = 3 * a2 + (ijk / 3) % 3, pcc = 3 * a3 + ijk / 9;
-            const uint32_t off = a_off_mn(16 * pb + pcc, pa);
+            const uint32_t off = a_off_mn(16 * pcc + pb, pa);
             st_split(Aop, off, ar);
             st_split(Aop, off + 8192u, ai);
         }
@@ -277,7 +297,7 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a)
                     if (go) e_ph ^= 1u;  // else the abort path waits on the same phase again
                 }
                 if (go) {
-                    issue_stage(tbase, a_u, e_u + (uint32_t)stage * kEImgBytes, stage < 2);
+                    issue_stage(tbase, a_u, e_u + (uint32_t)stage * kEImgBytes, true);
                     tc::mma_commit(&mb[1]);
                 }
             }
@@ -288,23 +308,17 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a)
             tc::fence_after_sync();
             float v[32];
             tmem_ld32(taddr, v);
-            if (stage == 0) {
-                // row (b, c) of T1 over b1 -> stage-2 operand rows (b1, c), k = b (MN-major)
-                const int b = mrow >> 4, c = mrow & 15;
-                const uint32_t base = (uint32_t)(((c >> 3) << 7) + ((b >> 3) << 12) + ((b & 7) << 4) + ((c & 7) << 1));
+            if (stage < 2) {
+                // stage 0: row (c, b) of T1 over b1 -> stage-2 operand rows (c, b1), k = b;
+                // stage 1: row (c, b1) of T2 over b2 -> stage-3 operand rows (b1, b2), k = c.
+                // Columns 8g..8g+7 of the row are one core-matrix row: M = 16 hi + 8g, k = lo
+                // (and 16 + lo for the imaginary part, 8192 bytes on).
+                const int hi = stage == 0 ? (mrow >> 4) : (mrow & 15), lo = stage == 0 ? (mrow & 15) : (mrow >> 4);
 #pragma unroll
-                for (int b1 = 0; b1 < 16; ++b1) {
-                    st_split(Aop, base + 256u * b1, v[b1]);
-                    st_split(Aop, base + 256u * b1 + 8192u, v[16 + b1]);
-                }
-            } else if (stage == 1) {
-                // row (b1, c) of T2 over b2 -> stage-3 operand rows (b1, b2), k = c (K-major)
-                const int b1 = mrow >> 4, c = mrow & 15;
-                const uint32_t base = (uint32_t)(256 * b1 + ((c >> 3) << 12) + ((c & 7) << 1));
-#pragma unroll
-                for (int b2 = 0; b2 < 16; ++b2) {
-                    st_split(Aop, base + 16u * b2, v[b2]);
-                    st_split(Aop, base + 16u * b2 + 8192u, v[16 + b2]);
+                for (int g = 0; g < 2; ++g) {
+                    const uint32_t off = a_off_mn(16 * hi + 8 * g, lo);
+                    st_split8(Aop, off, v + 8 * g);
+                    st_split8(Aop, off + 8192u, v + 16 + 8 * g);
                 }
             } else {
                 // row (b1, b2) of Psi over b3 -> |Psi|^2 of the valid modes
@@ -317,7 +331,7 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a)
         }
         if (!ok) break;
         tc::fence_before_sync();
-        // ---- FP32 screen of the Gaussians, survivors queued, FP64 weights ----
+        // ---- FP32 screen of the Gaussians, survivors queued, FP32 weights, FP64 sums ----
         uint32_t live_lo = 0u, live_hi = 0u, live_x = 0u;
         int nsurv = 0;
         const int b1 = mrow >> 4, b2 = mrow & 15;
@@ -328,7 +342,7 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a)
         if (mine && nsurv) k3_enqueue<N>(S, b1 * N + b2, off, live_lo, live_hi, live_x);
         for (int i = tid; i < N3; i += kTcThreads) S.F[i] = 0.0;
         __syncthreads();
-        k3_survivors<N>(S, P, nq, perm, [&](int idx) -> double { return (double)psq[idx]; });
+        k3_survivors_f32<N>(S, P, nq, (float)perm, [&](int idx) -> float { return psq[idx]; });
         k3_sums_scatter<N>(S, a, nred);
     }
     if (!ok) {

@@ -2199,7 +2199,14 @@ extern "C" int tdg_kappa_iter_vjp(tdg_ctx *c, const tdg_opts *o, const double *k
         }
     };
     // adjoint fixed point lambda = kbar - T^T X^T Q^-1 xb(lambda), iterated with the forward
-    // pass's mixing schedule and convergence test (kappa.f90:437-490)
+    // pass's mixing schedule and convergence test (kappa.f90:437-490). The test skips entries
+    // whose squared norm is below lo_sqtol, a threshold set for F; the cotangents are of the
+    // size of c_v / V (1e-8 and below), so the iteration runs on kbar scaled to a largest
+    // entry of 1 (the map is linear) and scales back.
+    double kscale = 0.0;
+    for (double v : kbar) kscale = std::max(kscale, std::fabs(v));
+    if (kscale == 0.0) kscale = 1.0;
+    for (double &v : kbar) v /= kscale;
     std::vector<double> lam = kbar, nw(nf), dl, f0b;
     std::vector<double> scf;
     double mix = 0.95;
@@ -2237,6 +2244,7 @@ extern "C" int tdg_kappa_iter_vjp(tdg_ctx *c, const tdg_opts *o, const double *k
         if (it > 15 && mix > 0.50) mix *= 0.98;
     }
     if (n_iter) *n_iter = std::min(it, maxiter);
+    for (double &v : lam) v *= kscale;
     distribute_adj(lam, dl, &f0b);
     make_z(dl);
     // linewidth cotangent: F0 = v / qs (set where linewidth > lo_freqtol) and the 1/qs of the

@@ -117,7 +117,7 @@ struct Fc4Dev {
 };
 
 // Device status word: kernels record the first failed check here.
-enum DevStatus : int32_t { kDevOk = 0, kDevBadIndex = 1, kDevOverflow = 2, kDevTimeout = 3 };
+enum DevStatus : int32_t { kDevOk = 0, kDevBadIndex = 1, kDevOverflow = 2, kDevTimeout = 3, kDevLinalg = 4 };
 
 // ---- launch wrappers (each returns cudaError_t of the launch) ----
 // K1: count/fill passes of the irreducible-triplet enumeration.

@@ -80,13 +80,19 @@ class Problem:
         return tuple(getattr(self, s) if isinstance(s, str) else s for s in shp)
 
     @classmethod
-    def load(cls, directory, qgrid, fourthorder=False, readiso=False, timereversal=True) -> "Problem":
-        """Read infile.* from `directory` and build mesh and phonons (main.f90:42-181)."""
+    def load(cls, directory, qgrid, fourthorder=False, readiso=False, timereversal=True,
+             device: int | None = None) -> "Problem":
+        """Read infile.* from `directory` and build mesh and phonons (main.f90:42-181); with
+        `device` the harmonic stage runs on that GPU (tdg_problem_load_device)."""
         L = N.lib()
         out = C.POINTER(N.TdgProblem)()
         g = np.ascontiguousarray(qgrid, dtype=np.int32)
-        N.check(L.tdg_problem_load(str(directory).encode(), N.ptr(g, C.c_int32), int(bool(fourthorder)),
-                                   int(bool(readiso)), int(bool(timereversal)), C.byref(out)), "tdg_problem_load")
+        args = (str(directory).encode(), N.ptr(g, C.c_int32), int(bool(fourthorder)), int(bool(readiso)),
+                int(bool(timereversal)))
+        if device is None:
+            N.check(L.tdg_problem_load(*args, C.byref(out)), "tdg_problem_load")
+        else:
+            N.check(L.tdg_problem_load_device(*args, int(device), C.byref(out)), "tdg_problem_load_device")
         try:
             return cls.from_struct(out.contents)
         finally:

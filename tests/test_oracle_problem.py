@@ -76,3 +76,26 @@ def test_oracle_runs_on_its_own_problem(configs, name, grid, it):
     np.testing.assert_allclose(rq["linewidth"], rp["linewidth"], rtol=1e-10, atol=1e-13 * s)
     np.testing.assert_allclose(rq["kappa_sma"], rp["kappa_sma"], rtol=1e-10, atol=1e-12 * np.abs(rp["kappa_sma"]).max())
     np.testing.assert_allclose(rq["kappa_iter"], rp["kappa_iter"], rtol=2e-2, atol=2e-2 * np.abs(rp["kappa_iter"]).max())
+
+
+@pytest.mark.parametrize("name,grid", [("rocksalt", (6, 6, 6)), ("perovskite", (4, 4, 4)), ("fluorite", (4, 4, 4))])
+def test_unfolded_eigenvectors_diagonalise_the_mesh(configs, name, grid):
+    """Only the irreducible points are diagonalised; every other mesh point takes its
+    eigenvectors rotated from its irreducible point (lo_eigenvector_transformation_matrix,
+    conjugated under time reversal), its frequencies copied and its velocities rotated, as
+    type_phonon_dispersions_generation.f90:117-170 does. The rotated eigenvectors must be
+    orthonormal eigenvectors of the oracle's own D(q) at that point (residual below 1e-10 of
+    the largest eigenvalue) and the frequencies exactly those of the irreducible point."""
+    p = Problem.load(configs[name], grid, readiso=True)
+    o = OracleProblem(configs[name], grid)
+    n = p.n_mode
+    lam = (p.omega.max()) ** 2
+    for q in range(p.n_full):
+        D, _ = o._dyn(o.q_cart[q])
+        E = (p.egv[q, ..., 0] + 1j * p.egv[q, ..., 1]).T  # columns are modes
+        w = np.sign(p.omega[q]) * p.omega[q] ** 2
+        assert np.abs(D @ E - E * w[None, :]).max() < 1e-10 * lam
+        assert np.abs(E.conj().T @ E - np.eye(n)).max() < 1e-12
+        i = p.irr_full[p.full_irr[q] - 1] - 1
+        np.testing.assert_array_equal(p.omega[q], p.omega[i])
+        np.testing.assert_array_equal(p.degen[q], p.degen[i])
