@@ -82,11 +82,22 @@ __device__ __forceinline__ const float2 *egvs_ptr<float2>(const PhononDev &ph) {
     return ph.egvs32;
 }
 
-// The adjoint accumulates d L / d mwm per CTA in shared memory in the precision of the
-// contraction (FP64 or FP32) and adds it into the CTA's FP64 slice in global memory every
-// kAdjFlush q-triplets, which bounds the FP32 rounding on the mixed path (GB300's FP64 pipe
-// runs at 1/64 of the FP32 rate and every q-triplet adds into all n_fc3 * 27 entries).
+// The adjoint accumulates d L / d mwm per CTA: FP64 runs in FP64 (in shared memory when the
+// n_fc3 * 27 entries fit, else straight into the CTA's FP64 slice in global memory); mixed
+// runs in FP32, flushed every kAdjFlush q-triplets from shared memory, into a slice of
+// (hi, lo) float pairs with compensated (two-sum) additions. GB300's FP64 pipe runs at 1/64
+// of the FP32 rate and every q-triplet adds into all n_fc3 * 27 entries: FP64 additions and
+// conversions there were half of the mixed adjoint's FP64 pipe.
 constexpr int kAdjFlush = 64;
+
+// hi + lo += v with the rounding error of the high part carried into the low part
+// (Knuth's two-sum).
+__device__ __forceinline__ float2 add_two_sum(float2 a, float v) {
+    const float s = a.x + v;
+    const float bp = s - a.x;
+    const float err = (a.x - (s - bp)) + (v - bp);
+    return make_float2(s, a.y + err);
+}
 
 // exp(-2 pi i (q2.lv2 + q3.lv3)) of force-constant triplet t as an exact root of unity:
 // q = g/N on the mesh and lv integer, so the phase is twiddle[K] with
@@ -152,8 +163,12 @@ __host__ __device__ inline Layout make_layout(int n, int cs, bool adj = false) {
     L.rowid = o; o += align16(sizeof(int) * n);
     L.red = o; o += align16(sizeof(int2) * kMaxRed);
     L.wsum = o; o += align16(sizeof(int) * 33);
-    L.xb = o;
-    if (adj) o += align16(sizeof(double) * n2);
+    // The adjoint's xi_bar sums over b2 (n^2 doubles) live in the survivor-queue region: they
+    // are written after the survivors are done and read before the eigenvectors are loaded
+    // there again (4 n^3 >= 8 n^2 bytes). Keeping them separate cost 1.8 KB at n = 15 and
+    // the third CTA per SM.
+    L.xb = L.Q;
+    (void)adj;
     L.total = o;
     return L;
 }
@@ -349,17 +364,28 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
         double *F = (double *)A;
         for (int i = tid; i < N3; i += bd) F[i] = 0.0;
         __syncthreads();
-        // ---- FP64 delta weights and occupations for the survivors, full warps ----
-        // (the adjoint keeps d F / d|Psi|^2, i.e. F without |Psi|^2)
-        k3_survivors<N>(S, P, nq, perm, [&](int idx) -> double {
-            if constexpr (ADJ) {
-                return 1.0;
-            } else {
-                const C psi = B[idx];
-                const double cr = (double)psi.x, ci = (double)psi.y;
-                return cr * cr + ci * ci;
-            }
-        });
+        // ---- delta weights and occupations for the survivors, full warps: FP64 for FP64
+        // runs, FP32 (from FP64 centre differences) in mixed precision, as the tensor-core
+        // kernel; the adjoint keeps d F / d|Psi|^2, i.e. F without |Psi|^2 ----
+        if constexpr (sizeof(R) == 8) {
+            k3_survivors<N>(S, P, nq, perm, [&](int idx) -> double {
+                if constexpr (ADJ) {
+                    return 1.0;
+                } else {
+                    const C psi = B[idx];
+                    return (double)psi.x * (double)psi.x + (double)psi.y * (double)psi.y;
+                }
+            });
+        } else {
+            k3_survivors_f32<N>(S, P, nq, (float)perm, [&](int idx) -> float {
+                if constexpr (ADJ) {
+                    return 1.0f;
+                } else {
+                    const C psi = B[idx];
+                    return (float)psi.x * (float)psi.x + (float)psi.y * (float)psi.y;
+                }
+            });
+        }
         __syncthreads();
         if constexpr (ADJ) {
             // d L / d|Psi_b|^2 = lam[row(b1)] * nred * dF_b/d|Psi_b|^2 (Gamma += nred * sum F);
@@ -401,6 +427,7 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
                 w.y = (R)(-g * (double)psi.y);
                 B[i] = w;
             }
+            __syncthreads();  // XB shares the eigenvectors' region
             // the survivor queue overwrote the eigenvectors: load them again
             for (int i = tid; i < 3 * N2; i += bd) {
                 const int which = i / N2, e = i % N2;
@@ -472,17 +499,24 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
                         const C q = A[fc.abase[tt] + off];
                         const C p = ph[tl];
                         const R v = (R)2 * (p.x * q.x - p.y * q.y);
-                        if (a.acc_in_smem)
+                        if (a.acc_in_smem) {
                             acc[(size_t)tt * 27 + ijk] += v;
-                        else
+                        } else if constexpr (sizeof(R) == 8) {
                             slice[(size_t)tt * 27 + ijk] += (double)v;
+                        } else {
+                            float2 *s2 = (float2 *)slice + (size_t)tt * 27 + ijk;
+                            *s2 = add_two_sum(*s2, (float)v);
+                        }
                     }
                 }
             }
             __syncthreads();
             if (a.acc_in_smem && ++since_flush == kAdjFlush) {
                 for (int i = tid; i < fc.n * 27; i += bd) {
-                    slice[i] += (double)acc[i];
+                    if constexpr (sizeof(R) == 8)
+                        slice[i] += (double)acc[i];
+                    else
+                        ((float2 *)slice)[i] = add_two_sum(((float2 *)slice)[i], (float)acc[i]);
                     acc[i] = (R)0;
                 }
                 since_flush = 0;
@@ -497,7 +531,12 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
         if (a.acc_in_smem) {
             __syncthreads();
             double *slice = a.mwm_bar + (size_t)blockIdx.x * fc.n * 27;
-            for (int i = tid; i < fc.n * 27; i += bd) slice[i] += (double)acc[i];
+            for (int i = tid; i < fc.n * 27; i += bd) {
+                if constexpr (sizeof(R) == 8)
+                    slice[i] += (double)acc[i];
+                else
+                    ((float2 *)slice)[i] = add_two_sum(((float2 *)slice)[i], (float)acc[i]);
+            }
         }
     }
 }
@@ -563,6 +602,18 @@ __global__ void k_sum_slices(const double *slices, int32_t n_slice, int64_t n, d
     }
 }
 
+// The same over slices of (hi, lo) float pairs (mixed-precision adjoint).
+__global__ void k_sum_slices_f2(const float2 *slices, int32_t n_slice, int64_t n, double *out) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int g = 0; g < n_slice; ++g) {
+            const float2 v = slices[(int64_t)g * n + e];
+            acc += (double)v.x + (double)v.y;
+        }
+        out[e] = acc;
+    }
+}
+
 template <typename R>
 cudaError_t launch_prec(const ThreePhArgs &a, int n_sm, int ctas_per_sm, cudaStream_t s) {
     switch (a.mesh.n_mode) {
@@ -621,10 +672,15 @@ cudaError_t launch_threephonon_adjoint(const ThreePhArgs &a, int precision, int 
     return launch_adj_prec<float>(a, grid, extra, s);
 }
 
-cudaError_t launch_sum_slices(const double *slices, int32_t n_slice, int64_t n, double *out, cudaStream_t s) {
+cudaError_t launch_sum_slices(const double *slices, int32_t n_slice, int64_t n, int precision, double *out,
+                              cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     const int64_t blocks = (n + 255) / 256;
-    k_sum_slices<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, s>>>(slices, n_slice, n, out);
+    const unsigned g = (unsigned)(blocks < 4096 ? blocks : 4096);
+    if (precision == 0)
+        k_sum_slices<<<g, 256, 0, s>>>(slices, n_slice, n, out);
+    else
+        k_sum_slices_f2<<<g, 256, 0, s>>>(reinterpret_cast<const float2 *>(slices), n_slice, n, out);
     return cudaGetLastError();
 }
 

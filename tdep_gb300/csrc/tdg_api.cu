@@ -2380,7 +2380,7 @@ extern "C" int tdg_adjoint_fc3(tdg_ctx *c, const tdg_opts *o, const double *lw_b
     CUDA_TRY(cudaEventRecord(ev[1], s));
     CUDA_TRY(launch_threephonon_adjoint(a, o->precision, grid, s));
     CUDA_TRY(cudaEventRecord(ev[2], s));
-    CUDA_TRY(launch_sum_slices(c->d_slices.p, std::max(grid, 1), nm, c->d_mwm_bar.p, s));
+    CUDA_TRY(launch_sum_slices(c->d_slices.p, std::max(grid, 1), nm, o->precision, c->d_mwm_bar.p, s));
     std::vector<double> dev(nm);
     CUDA_TRY(copy_async(dev.data(), c->d_mwm_bar.p, sizeof(double) * nm, cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaEventRecord(ev[3], s));

@@ -168,8 +168,10 @@ int threephonon_max_per_sm(int n, int precision, int *api = nullptr, int *count 
 // accumulates 2 Re(phase * Q) into a.mwm_bar (one slice per CTA of the returned grid).
 int threephonon_adjoint_grid(int n, int precision, int n_sm, int n_trip, int n_fc, bool acc_in_smem);
 cudaError_t launch_threephonon_adjoint(const ThreePhArgs &a, int precision, int grid, cudaStream_t s);
-// out[e] = sum over g < n_slice of slices[g * n + e], in slice order.
-cudaError_t launch_sum_slices(const double *slices, int32_t n_slice, int64_t n, double *out, cudaStream_t s);
+// out[e] = sum over g < n_slice of slices[g * n + e], in slice order; the slices hold doubles
+// for precision 0 (FP64) and (hi, lo) float pairs otherwise (the mixed adjoint).
+cudaError_t launch_sum_slices(const double *slices, int32_t n_slice, int64_t n, int precision, double *out,
+                              cudaStream_t s);
 size_t threephonon_smem_bytes(int n, int precision, int n_fc);
 // Tensor-core fused kernel for 9, 12 or 15 modes in mixed precision (k_threephonon_tc.cu).
 bool threephonon_tc_supported(int n, int precision, int n_fc);
