@@ -78,6 +78,9 @@ def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
+INPUT_DIRS = {}  # workload -> directory of its infile.* files (written by setup)
+
+
 def setup(cfg_name, precision="mixed"):
     from tdep_gb300 import Options, Problem, QLists, synth
 
@@ -85,6 +88,7 @@ def setup(cfg_name, precision="mixed"):
     tmp = tempfile.mkdtemp(prefix="tdg_bench_")
     extra = {"reps": cfg["reps"]} if "reps" in cfg else {}
     d = synth.write_config(cfg["synth"], Path(tmp) / cfg["synth"], seed=1, **extra)
+    INPUT_DIRS[cfg_name] = d
     t0 = time.perf_counter()
     prob = Problem.load(d, cfg["grid"], readiso=True)
     log(f"[bench] problem: n_mode={prob.n_mode} n_full={prob.n_full} n_irr={prob.n_irr} n_fc3={prob.n_fc3} "
@@ -538,7 +542,36 @@ def measure(cfg_name, args, cpu_budget, with_adjoint=True):
                 "ms": {k: 1e3 * float(np.median([p[i] for p in parts]))
                        for i, k in enumerate(("create", "generate", "kappa", "destroy"))}}
 
+    def e2e_files_run(o, steps):
+        # from the input files: readers, symmetry and mesh on the host, the harmonic stage on
+        # the device (tdg_problem_load_device), then the scattering pass and kappa
+        from tdep_gb300 import Problem
+
+        e2e_s, parts = [], []
+        h2d = d2h = 0
+        for _ in range(steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            p2 = Problem.load(INPUT_DIRS[cfg_name], cfg["grid"], readiso=True, device=0)
+            t1 = time.perf_counter()
+            s2 = ScatteringRates(p2)
+            s2.generate(o, lists)
+            s2.kappa_offdiag(o)
+            s2.kappa(o)
+            h2d, d2h = s2.transfer_bytes()
+            s2.close()
+            torch.cuda.synchronize()
+            t2 = time.perf_counter()
+            e2e_s.append(t2 - t0)
+            parts.append((t1 - t0, t2 - t1))
+        return {"value": trip / float(np.mean(e2e_s)), "unit": "q-triplets/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h),
+                "includes": "infile.* read, symmetry and mesh (host), harmonic stage (device), context creation, "
+                            "generate, off-diagonal kappa, kappa solve",
+                "ms": {k: 1e3 * float(np.median([p[i] for p in parts])) for i, k in enumerate(("load", "rest"))}}
+
     e2e = e2e_run(opts, args.steps)
+    e2e_files = e2e_files_run(opts, max(2, args.steps // 2)) if small else None
     if fp64 is not None:
         fp64["e2e"] = e2e_run(o64, max(2, args.steps // 2))
 
@@ -592,7 +625,8 @@ def measure(cfg_name, args, cpu_budget, with_adjoint=True):
     value = trip * args.steps / (sum(dev_ms) / 1e3)
     return {
         "cfg": cfg, "n": n, "small": small, "value": value, "ms_per_step": float(np.mean(dev_ms)),
-        "trip": trip, "xi_gb": lists.n_row * prob.n_full * n * 8 / 1e9, "e2e": e2e, "adjoint": adjoint,
+        "trip": trip, "xi_gb": lists.n_row * prob.n_full * n * 8 / 1e9, "e2e": e2e, "e2e_files": e2e_files,
+        "adjoint": adjoint,
         "roofline": roof, "clocks": clk, "launches": launches, "graphs": graphs, "stats": stats,
         "kappa_ms": kappa_ms, "kappa_iters": kappa_iters, "fp64": fp64, "lw_max": float(lw_mixed.max()),
         "cpu": {"value": cpu_trip / cpu_s, "unit": "q-triplets/s", "cores": cores, "kind": "port", "sample": desc},
@@ -615,6 +649,7 @@ def run_gb300(args):
                    "precision": PRECISION_NOTES[m["path"]],
                    "l2": "256 MB buffer written between steps (L2 flush); Xi+od working set 2x%.2f GB" % m["xi_gb"]},
         "e2e": m["e2e"],
+        "e2e_from_files": m["e2e_files"],
         "adjoint": m["adjoint"],
         "roofline": m["roofline"],
         "cpu_baseline": m["cpu"],
