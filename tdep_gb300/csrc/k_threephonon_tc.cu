@@ -97,6 +97,17 @@ __host__ __device__ inline TcLayout tc_layout(int n, int nt) {
 __device__ __forceinline__ uint32_t a_off_mn(int m, int k) {
     return (uint32_t)(((m >> 3) << 7) + ((k >> 3) << 12) + ((k & 7) << 4) + ((m & 7) << 1));
 }
+__device__ __forceinline__ uint32_t a_off_k(int m, int k) {
+    return (uint32_t)(((m >> 3) << 7) + ((k >> 3) << 12) + ((m & 7) << 4) + ((k & 7) << 1));
+}
+
+// hi + lo += v, the rounding error of the high part carried into the low part (two-sum).
+__device__ __forceinline__ float2 tc_two_sum(float2 a, float v) {
+    const float s = a.x + v;
+    const float bp = s - a.x;
+    const float err = (a.x - (s - bp)) + (v - bp);
+    return make_float2(s, a.y + err);
+}
 
 __device__ __forceinline__ void st_split(unsigned char *plane_hi, uint32_t off, float x) {
     unsigned short h, l;
@@ -168,7 +179,9 @@ __device__ __forceinline__ void issue_stage(uint32_t tbase, uint32_t a_base, uin
     }
 }
 
-template <int N>
+// ADJ: the adjoint of the linewidths (and, with a.xi_bar, of the Xi row terms) with respect
+// to the force constants; see the comment at the adjoint tail below.
+template <int N, bool ADJ>
 __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a) {
     constexpr int N2 = N * N, N3 = N2 * N;
     constexpr int NA = N / 3;
@@ -342,8 +355,144 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a)
         if (mine && nsurv) k3_enqueue<N>(S, b1 * N + b2, off, live_lo, live_hi, live_x);
         for (int i = tid; i < N3; i += kTcThreads) S.F[i] = 0.0;
         __syncthreads();
-        k3_survivors_f32<N>(S, P, nq, (float)perm, [&](int idx) -> float { return psq[idx]; });
-        k3_sums_scatter<N>(S, a, nred);
+        if constexpr (!ADJ) {
+            k3_survivors_f32<N>(S, P, nq, (float)perm, [&](int idx) -> float { return psq[idx]; });
+            k3_sums_scatter<N>(S, a, nred);
+        } else {
+            // ---- adjoint tail (the SIMT adjoint's algebra, k_threephonon.cu): F without |Psi|^2
+            // gives G_b = cot_b dF_b/d|Psi_b|^2 with cot = lam(row) nred (+ the Xi row terms'
+            // cotangents 2 om2/om1 xi_bar(q2', b2) + 2 om3/om1 xi_bar(q3', b3) over the
+            // equivalent triplets); W = G conj(Psi); Q[abc] = sum_b W_b E1[a,b1] E2[b,b2] E3[c,b3]
+            // by three GEMMs against the real-split E^T images (W E3^T over b3, then E2^T over
+            // b2, then E1^T over b1); d L / d mwm_t(i,j,k) = 2 Re(phase_t Q[3a1+i][3a2+j][3a3+k]).
+            k3_survivors_f32<N>(S, P, nq, (float)perm, [](int) -> float { return 1.0f; });
+            __syncthreads();
+            double *R2 = S.R2, *XB = S.R3;  // in the |Psi|^2 region, which the adjoint does not use
+            if (a.xi_bar) {
+                const int64_t ld = (int64_t)m.n_full * N;
+                for (int e = tid; e < 2 * N2; e += kTcThreads) {
+                    const int x = e % N2, eb1 = x / N, bb = x % N, r = S.rowid[eb1];
+                    double sum = 0.0;
+                    if (r >= 0) {
+                        const double *wr = a.xi_bar + (int64_t)r * ld;
+                        for (int k = 0; k < nred; ++k) {
+                            const int2 pr = S.red[k];
+                            sum += wr[(int64_t)(e < N2 ? pr.x : pr.y) * N + bb];
+                        }
+                    }
+                    if (e < N2)
+                        R2[x] = sum;
+                    else
+                        XB[x] = sum;
+                }
+                __syncthreads();
+            }
+            float gw[16];
+#pragma unroll
+            for (int b3 = 0; b3 < 16; ++b3) gw[b3] = 0.f;
+            {
+                const int r = mine ? S.rowid[b1] : -1;
+                if (r >= 0) {
+                    const double lr = a.lam[r] * (double)nred;
+#pragma unroll
+                    for (int b3 = 0; b3 < N; ++b3) {
+                        double cot = lr;
+                        if (a.xi_bar) cot += 2.0 * (S.om2[b2] * R2[b1 * N + b2] + S.om3[b3] * XB[b1 * N + b3]) * S.inv1[b1];
+                        gw[b3] = (float)(cot * S.F[(b1 * N + b2) * N + b3]);
+                    }
+                }
+            }
+            // F, the queue and the sums are read: the image region takes E3^T, E2^T, E1^T and
+            // the operand region W (K-major: a core-matrix row is 8 consecutive b3 of one row)
+            tc::fence_before_sync();
+            __syncthreads();
+            if (tid == 0) {
+                tc::fence_async_smem();
+                tc::mbar_arrive_expect_tx(&mb[0], 3u * kEImgBytes);
+                tc::bulk_g2s(e_u, a.tc_eimg_t + (size_t)q3 * kEImgBytes, kEImgBytes, &mb[0]);
+                tc::bulk_g2s(e_u + kEImgBytes, a.tc_eimg_t + (size_t)q2 * kEImgBytes, kEImgBytes, &mb[0]);
+                tc::bulk_g2s(e_u + 2 * kEImgBytes, a.tc_eimg_t + (size_t)f1 * kEImgBytes, kEImgBytes, &mb[0]);
+            }
+            tc::fence_after_sync();
+            {
+                float v[32], w[32];
+                tmem_ld32(taddr, v);  // Psi row (b1, b2): stage 3's accumulator is still in tensor memory
+#pragma unroll
+                for (int b3 = 0; b3 < 16; ++b3) {
+                    w[b3] = gw[b3] * v[b3];
+                    w[16 + b3] = -gw[b3] * v[16 + b3];
+                }
+#pragma unroll
+                for (int g = 0; g < 2; ++g) {
+                    const uint32_t off = a_off_k(mrow, 8 * g);
+                    st_split8(Aop, off, w + 8 * g);
+                    st_split8(Aop, off + 8192u, w + 16 + 8 * g);
+                }
+            }
+            // back stages: rows (b1, b2) over c, rows (b1, c) over b, rows (c, b) over a
+#pragma unroll 1
+            for (int stage = 0; stage < 3; ++stage) {
+                tc::fence_async_smem();
+                tc::fence_before_sync();
+                __syncthreads();
+                if (tid == 0) {
+                    tc::fence_after_sync();
+                    bool go = true;
+                    if (stage == 0) {
+                        go = tc::mbar_wait(&mb[0], e_ph, kTcWait);
+                        if (go) e_ph ^= 1u;
+                    }
+                    if (go) {
+                        issue_stage(tbase, a_u, e_u + (uint32_t)stage * kEImgBytes, stage > 0);
+                        tc::mma_commit(&mb[1]);
+                    }
+                }
+                const bool done = tc::mbar_wait(&mb[1], m_ph, kTcWait);
+                ok = __syncthreads_and(done) != 0;
+                if (!ok) break;
+                m_ph ^= 1u;
+                tc::fence_after_sync();
+                float v[32];
+                tmem_ld32(taddr, v);
+                if (stage < 2) {
+                    // stage 0: row (b1, b2) over c -> rows (b1, c), k = b2;
+                    // stage 1: row (b1, c) over b -> rows (c, b), k = b1 (MN-major, as forward)
+                    const int hi = stage == 0 ? (mrow >> 4) : (mrow & 15), lo = stage == 0 ? (mrow & 15) : (mrow >> 4);
+#pragma unroll
+                    for (int g = 0; g < 2; ++g) {
+                        const uint32_t off = a_off_mn(16 * hi + 8 * g, lo);
+                        st_split8(Aop, off, v + 8 * g);
+                        st_split8(Aop, off + 8192u, v + 16 + 8 * g);
+                    }
+                } else {
+                    // row (c, b) of Q over a into the (finished) operand region as [a][b][c]
+                    const int c = mrow >> 4, b = mrow & 15;
+                    float2 *Qs = (float2 *)Aop;
+                    if (b < N && c < N) {
+#pragma unroll
+                        for (int aa = 0; aa < N; ++aa) Qs[(aa * N + b) * N + c] = make_float2(v[aa], v[16 + aa]);
+                    }
+                }
+            }
+            if (!ok) break;
+            __syncthreads();
+            {
+                const float2 *Qs = (const float2 *)Aop;
+                float2 *slice = reinterpret_cast<float2 *>(a.mwm_bar) + (size_t)blockIdx.x * fc.n * 27;
+                constexpr int kGroups = kTcThreads / 27;
+                const int grp = tid / 27, ijk = tid % 27;
+                const int qoff = (ijk % 3) * N2 + ((ijk / 3) % 3) * N + ijk / 9;
+                if (grp < kGroups) {
+                    for (int tt = grp; tt < fc.n; tt += kGroups) {
+                        const float2 q = Qs[fc.abase[tt] + qoff];
+                        const float2 p = ph[tt];
+                        float2 *sl = slice + (size_t)tt * 27 + ijk;
+                        *sl = tc_two_sum(*sl, 2.f * (p.x * q.x - p.y * q.y));
+                    }
+                }
+            }
+            __syncthreads();  // the next q-triplet overwrites the operand region and the phases
+        }
     }
     if (!ok) {
         // a wait ran out: record it, let the copies and MMAs in flight finish (bounded), free
@@ -388,13 +537,14 @@ __global__ void k_tc_prep_fc(const int32_t *blk_ptr, int32_t n_blk, const float 
 // Real-split eigenvector images of every mesh point: B = [[Er, Ei], [-Ei, Er]] (32 x 32,
 // row k = component a (re) / 16 + a, column = mode b (re) / 16 + b), E = egvs32 padded with
 // zeros, split into BF16 hi and lo planes, MN-major core matrices (N groups 128 bytes apart,
-// K groups 512 bytes apart).
-__global__ void k_tc_eimg(int32_t n_full, int32_t n, const float2 *egvs32, unsigned char *out) {
+// K groups 512 bytes apart). transpose: the image of E^T (row k = mode, column = component),
+// the right-multiplier of the adjoint's back-contraction.
+__global__ void k_tc_eimg(int32_t n_full, int32_t n, const float2 *egvs32, unsigned char *out, int transpose) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (int64_t)n_full * 1024) return;
     const int q = (int)(i >> 10), e = (int)(i & 1023);
     const int k = e >> 5, c = e & 31;
-    const int aa = k & 15, b = c & 15;
+    const int aa = transpose ? (c & 15) : (k & 15), b = transpose ? (k & 15) : (c & 15);  // component, mode
     const bool kim = k >= 16, cim = c >= 16;
     float2 z = make_float2(0.f, 0.f);
     if (aa < n && b < n) z = egvs32[((size_t)q * n + b) * n + aa];
@@ -407,28 +557,27 @@ __global__ void k_tc_eimg(int32_t n_full, int32_t n, const float2 *egvs32, unsig
     *(unsigned short *)(img + 2048 + off) = l;
 }
 
-template <int N>
+template <int N, bool ADJ>
 int tc_per_sm(int n_fc, int *api, int *count) {
     const size_t bytes = tc_layout(N, n_fc).total;
-    const int per_sm = resident_ctas((const void *)k_threephonon_tc<N>, kTcThreads, bytes, api, count);
+    const int per_sm = resident_ctas((const void *)k_threephonon_tc<N, ADJ>, kTcThreads, bytes, api, count);
     // tensor memory: 64 columns per CTA, 512 per SM
     return per_sm > 8 ? 8 : per_sm;
 }
 
-template <int N>
-int tc_grid(const ThreePhArgs &a, int n_sm, int ctas_per_sm) {
-    int per_sm = tc_per_sm<N>(a.fc.n, nullptr, nullptr);
+template <int N, bool ADJ>
+int tc_grid(int n_fc, int n_trip, int n_sm, int ctas_per_sm) {
+    int per_sm = tc_per_sm<N, ADJ>(n_fc, nullptr, nullptr);
     if (per_sm < 1) return 0;
     if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
     const int grid = n_sm * per_sm;
-    return grid > a.n_trip ? (a.n_trip > 0 ? a.n_trip : 1) : grid;
+    return grid > n_trip ? (n_trip > 0 ? n_trip : 1) : grid;
 }
 
-template <int N>
-cudaError_t tc_launch(const ThreePhArgs &a, int n_sm, int ctas_per_sm, cudaStream_t s) {
-    const int grid = tc_grid<N>(a, n_sm, ctas_per_sm);
+template <int N, bool ADJ>
+cudaError_t tc_launch_grid(const ThreePhArgs &a, int grid, cudaStream_t s) {
     if (grid < 1) return cudaErrorInvalidConfiguration;
-    k_threephonon_tc<N><<<grid, kTcThreads, tc_layout(N, a.fc.n).total, s>>>(a);
+    k_threephonon_tc<N, ADJ><<<grid, kTcThreads, tc_layout(N, a.fc.n).total, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -441,9 +590,9 @@ bool threephonon_tc_supported(int n, int precision, int n_fc) {
 
 int threephonon_tc_max_per_sm(int n, int n_fc, int *api, int *count) {
     switch (n) {
-        case 9: return tc_per_sm<9>(n_fc, api, count);
-        case 12: return tc_per_sm<12>(n_fc, api, count);
-        case 15: return tc_per_sm<15>(n_fc, api, count);
+        case 9: return tc_per_sm<9, false>(n_fc, api, count);
+        case 12: return tc_per_sm<12, false>(n_fc, api, count);
+        case 15: return tc_per_sm<15, false>(n_fc, api, count);
         default: return 0;
     }
 }
@@ -451,9 +600,29 @@ int threephonon_tc_max_per_sm(int n, int n_fc, int *api, int *count) {
 cudaError_t launch_threephonon_tc(const ThreePhArgs &a, int n_sm, int ctas_per_sm, cudaStream_t s) {
     if (a.n_trip <= 0) return cudaSuccess;
     switch (a.mesh.n_mode) {
-        case 9: return tc_launch<9>(a, n_sm, ctas_per_sm, s);
-        case 12: return tc_launch<12>(a, n_sm, ctas_per_sm, s);
-        case 15: return tc_launch<15>(a, n_sm, ctas_per_sm, s);
+        case 9: return tc_launch_grid<9, false>(a, tc_grid<9, false>(a.fc.n, a.n_trip, n_sm, ctas_per_sm), s);
+        case 12: return tc_launch_grid<12, false>(a, tc_grid<12, false>(a.fc.n, a.n_trip, n_sm, ctas_per_sm), s);
+        case 15: return tc_launch_grid<15, false>(a, tc_grid<15, false>(a.fc.n, a.n_trip, n_sm, ctas_per_sm), s);
+        default: return cudaErrorNotSupported;
+    }
+}
+
+int threephonon_tc_adjoint_grid(int n, int n_sm, int n_trip, int n_fc) {
+    switch (n) {
+        case 9: return tc_grid<9, true>(n_fc, n_trip, n_sm, 0);
+        case 12: return tc_grid<12, true>(n_fc, n_trip, n_sm, 0);
+        case 15: return tc_grid<15, true>(n_fc, n_trip, n_sm, 0);
+        default: return 0;
+    }
+}
+
+cudaError_t launch_threephonon_tc_adjoint(const ThreePhArgs &a, int grid, cudaStream_t s) {
+    if (a.n_trip <= 0) return cudaSuccess;
+    if (!a.tc_eimg || !a.tc_eimg_t || !a.tc_fct || !a.lam || !a.mwm_bar) return cudaErrorInvalidValue;
+    switch (a.mesh.n_mode) {
+        case 9: return tc_launch_grid<9, true>(a, grid, s);
+        case 12: return tc_launch_grid<12, true>(a, grid, s);
+        case 15: return tc_launch_grid<15, true>(a, grid, s);
         default: return cudaErrorNotSupported;
     }
 }
@@ -467,10 +636,11 @@ cudaError_t launch_tc_prep_fc(const int32_t *blk_ptr, int32_t n_blk, const float
     return cudaGetLastError();
 }
 
-cudaError_t launch_tc_eimg(int32_t n_full, int32_t n, const float2 *egvs32, unsigned char *out, cudaStream_t s) {
+cudaError_t launch_tc_eimg(int32_t n_full, int32_t n, const float2 *egvs32, unsigned char *out, cudaStream_t s,
+                           bool transpose) {
     if (n > 16) return cudaErrorInvalidValue;
     const int64_t total = (int64_t)n_full * 1024;
-    k_tc_eimg<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(n_full, n, egvs32, out);
+    k_tc_eimg<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(n_full, n, egvs32, out, transpose ? 1 : 0);
     return cudaGetLastError();
 }
 

@@ -193,10 +193,10 @@ struct tdg_ctx {
     DevBuf<float> fc3_mwm32, fc4_mwm32;
     // tensor-core fused kernel (9-15 modes, mixed): eigenvector images built on first use,
     // transposed force constants rebuilt by every call (tdg_set_fc3 may change them)
-    DevBuf<unsigned char> d_tc_eimg;
+    DevBuf<unsigned char> d_tc_eimg, d_tc_eimg_t;  // E and E^T images (the latter for the adjoint)
     DevBuf<float> d_tc_fct;
     DevBuf<int32_t> d_tc_toff;
-    bool tc_eimg_ready = false;
+    bool tc_eimg_ready = false, tc_eimg_t_ready = false;
     int last_path = -1;  // 0 SIMT fused kernel, 1 tensor-core fused kernel, 2 large-cell batches
     // fused three-phonon launch of the last scattering call: grid, CTAs per SM used, the
     // runtime's occupancy figure and the register/shared-memory count (-1 before any)
@@ -2335,9 +2335,15 @@ extern "C" int tdg_adjoint_fc3(tdg_ctx *c, const tdg_opts *o, const double *lw_b
                                         "not supported on the large-cell path");
         return adjoint_large_cell(c, lam, mwm_bar, stats);
     }
-    // the CTA's gradient slice lives in shared memory when it is small enough
-    const bool acc_smem = (size_t)c->n_fc3 * 27 * sizeof(double) <= 48 * 1024;
-    const int grid = threephonon_adjoint_grid(n, o->precision, c->n_sm, ntrip, c->n_fc3, acc_smem);
+    // after the tensor-core forward pass (mixed precision, 9/12/15 modes) the adjoint runs on
+    // the tensor cores too; otherwise the SIMT kernel's ADJ variant
+    const char *tc_env = std::getenv("TDG_TC_SMALL");
+    const bool use_tc = c->last_path == 1 && o->precision != TDG_PREC_FP64 && o->tensor_cores != 2 &&
+                        !(tc_env && tc_env[0] == '0') && threephonon_tc_supported(n, o->precision, c->n_fc3);
+    // the CTA's gradient slice lives in shared memory when it is small enough (SIMT)
+    const bool acc_smem = !use_tc && (size_t)c->n_fc3 * 27 * sizeof(double) <= 48 * 1024;
+    const int grid = use_tc ? threephonon_tc_adjoint_grid(n, c->n_sm, ntrip, c->n_fc3)
+                            : threephonon_adjoint_grid(n, o->precision, c->n_sm, ntrip, c->n_fc3, acc_smem);
     if (ntrip > 0 && grid < 1) return set_error(kErrDevice, "adjoint kernel configuration failed");
     const int64_t nm = (int64_t)c->n_fc3 * 27;
     cudaError_t e = cudaSuccess;
@@ -2377,8 +2383,24 @@ extern "C" int tdg_adjoint_fc3(tdg_ctx *c, const tdg_opts *o, const double *lw_b
     a.mwm_bar = c->d_slices.p;
     a.acc_in_smem = acc_smem ? 1 : 0;
     a.xi_bar = c->xi_bar_ready ? c->d_xi_bar.p : nullptr;
+    if (use_tc) {
+        if (!c->tc_eimg_t_ready) {
+            CUDA_TRY(c->d_tc_eimg_t.alloc((size_t)c->N * 4096));
+            CUDA_TRY(launch_tc_eimg(c->N, n, c->d_egvs32.p, c->d_tc_eimg_t.p, s, true));
+            c->tc_eimg_t_ready = true;
+        }
+        CUDA_TRY(launch_tc_prep_fc(c->fc3_blk.p, c->na * c->na * c->na, c->fc3_mwm32.p, c->d_tc_toff.p,
+                                   c->d_tc_fct.p, s));
+        a.tc_eimg = c->d_tc_eimg.p;
+        a.tc_eimg_t = c->d_tc_eimg_t.p;
+        a.tc_fct = c->d_tc_fct.p;
+        a.tc_toff = c->d_tc_toff.p;
+    }
     CUDA_TRY(cudaEventRecord(ev[1], s));
-    CUDA_TRY(launch_threephonon_adjoint(a, o->precision, grid, s));
+    if (use_tc)
+        CUDA_TRY(launch_threephonon_tc_adjoint(a, grid, s));
+    else
+        CUDA_TRY(launch_threephonon_adjoint(a, o->precision, grid, s));
     CUDA_TRY(cudaEventRecord(ev[2], s));
     CUDA_TRY(launch_sum_slices(c->d_slices.p, std::max(grid, 1), nm, o->precision, c->d_mwm_bar.p, s));
     std::vector<double> dev(nm);

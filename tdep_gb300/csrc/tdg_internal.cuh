@@ -158,6 +158,8 @@ struct ThreePhArgs {
     const unsigned char *tc_eimg;
     const float *tc_fct;
     const int32_t *tc_toff;
+    // tensor-core adjoint only: the images of the transposed eigenvector matrices (E^T)
+    const unsigned char *tc_eimg_t;
 };
 // ctas_per_sm: persistent grid of n_sm * ctas_per_sm CTAs (0 or more than fit: as many as fit).
 cudaError_t launch_threephonon(const ThreePhArgs &a, int precision, int n_sm, int ctas_per_sm, cudaStream_t s);
@@ -179,12 +181,19 @@ bool threephonon_tc_supported(int n, int precision, int n_fc);
 // api and count (may be null) receive resident_ctas's two figures.
 int threephonon_tc_max_per_sm(int n, int n_fc, int *api = nullptr, int *count = nullptr);
 cudaError_t launch_threephonon_tc(const ThreePhArgs &a, int n_sm, int ctas_per_sm, cudaStream_t s);
+// Its adjoint (the ADJ variant of k_threephonon_tc: Psi again, W = G conj(Psi), the back-
+// contraction through E3^T, E2^T, E1^T on the tensor cores, 2 Re(phase Q) into a.mwm_bar as
+// (hi, lo) float slices, one per CTA of the returned grid; a.acc_in_smem is not used).
+int threephonon_tc_adjoint_grid(int n, int n_sm, int n_trip, int n_fc);
+cudaError_t launch_threephonon_tc_adjoint(const ThreePhArgs &a, int grid, cudaStream_t s);
 // Floats of the transposed force-constant copy, its builder (one CTA, n_blk <= 256) and the
 // eigenvector images (n <= 16).
 size_t tc_fct_floats(int n_fc, int n_blk);
 cudaError_t launch_tc_prep_fc(const int32_t *blk_ptr, int32_t n_blk, const float *mwm32, int32_t *toff, float *out,
                               cudaStream_t s);
-cudaError_t launch_tc_eimg(int32_t n_full, int32_t n, const float2 *egvs32, unsigned char *out, cudaStream_t s);
+// transpose: the image of E^T (rows modes, columns components) for the adjoint.
+cudaError_t launch_tc_eimg(int32_t n_full, int32_t n, const float2 *egvs32, unsigned char *out, cudaStream_t s,
+                           bool transpose = false);
 // Adjoint of the BTE (k_bte_adjoint.cu): y = X^T z (FP64, 3 right-hand sides, part holds
 // xit_parts(n_row) * 3 * n_col doubles), out = X f row by row, W = -z f^T, and the adjoint
 // of the row symmetrisations on W given the raw three-phonon terms od_raw.

@@ -229,3 +229,34 @@ def test_dkappa_iter_dphi3_against_central_differences(configs, precision):
         fd = (kxx(mp) - kxx(mm)) / (2 * h)
         assert abs(fd - g[t, k]) <= bar * abs(g[t, k]) + 1e-6 * np.abs(g).max(), (t, k, fd, g[t, k])
     sr.close()
+
+
+@pytest.mark.parametrize("name,grid", [("perovskite", (4, 4, 4)), ("fluorite", (4, 4, 4)), ("l12", (4, 4, 4))])
+def test_fused_tensor_core_adjoint_matches_fp64(configs, name, grid):
+    """After the tcgen05 fused forward pass (mixed precision, 15, 9 and 12 modes) the adjoint
+    runs on the tensor cores too (Psi again, W = G conj(Psi), back-contraction through the E^T
+    images, FP32 weights, two-sum float slices): the linewidth adjoint against the FP64 SIMT
+    adjoint of the same samples (norm 2e-4), and d kappa_iter,xx / d Phi3 with the
+    scattering-matrix term against the FP64 one (norm 1e-3: mixed kappa_iter moves by 1e-6
+    and the BTE adjoint amplifies it by the iteration's condition)."""
+    prob = Problem.load(configs[name], grid, readiso=True)
+    kw = dict(temperature=300.0, integrationtype=2, isotopescattering=False, seed=19)
+    o64, o32 = Options(**kw), Options(precision="mixed", **kw)
+    lists = QLists.monte_carlo(prob, o64)
+    rng = np.random.default_rng(8)
+    lw_bar = rng.normal(size=(prob.n_irr, prob.n_mode))
+    kb = np.zeros((3, 3))
+    kb[0, 0] = 1.0
+    sr = ScatteringRates(prob)
+    out = {}
+    for tag, o in (("fp64", o64), ("mixed", o32)):
+        sr.generate(o, lists)
+        assert sr.last_path() == (1 if tag == "mixed" else 0)
+        g = sr.adjoint_fc3(o, lw_bar)
+        sr.kappa(o, maxiter=400, tol=1e-14)
+        gi = sr.adjoint_fc3(o, sr.kappa_iter_vjp(o, kb, maxiter=400, tol=1e-14))
+        out[tag] = (g, gi)
+    sr.close()
+    (g64, gi64), (g32, gi32) = out["fp64"], out["mixed"]
+    assert np.linalg.norm(g32 - g64) <= 2e-4 * np.linalg.norm(g64)
+    assert np.linalg.norm(gi32 - gi64) <= 1e-3 * np.linalg.norm(gi64)
