@@ -184,6 +184,7 @@ int problem_load(const char *dir, const int32_t grid[3], int fourthorder, int re
                  tdg_problem **out) {
     if (!dir || !grid || !out) return set_error(kErrParam, "tdg_problem_load: null argument");
     *out = nullptr;
+    PhaseTimer pt("tdg_problem_load");
     auto h = std::make_unique<ProblemHolder>();
     const std::string d = std::string(dir) + "/";
     int st = read_poscar(d + "infile.ucposcar", h->c);
@@ -196,8 +197,10 @@ int problem_load(const char *dir, const int32_t grid[3], int fourthorder, int re
         if (!(h->c.mass[a] > 0))
             return set_error(kErrParam, "unknown element mass for atom " + std::to_string(a + 1) +
                                             "; provide infile.isotopes and --readiso");
+    pt.mark("structure");
     st = find_symmetry(h->c);
     if (st) return st;
+    pt.mark("symmetry");
     FC2 fc2;
     st = read_fc2(d + "infile.forceconstant", h->c, fc2);
     if (st) return st;
@@ -207,9 +210,11 @@ int problem_load(const char *dir, const int32_t grid[3], int fourthorder, int re
         st = read_fc4(d + "infile.forceconstant_fourthorder", h->c, h->f4);
         if (st) return st;
     }
+    pt.mark("force constants");
     const int g[3] = {grid[0], grid[1], grid[2]};
     st = build_fft_mesh(h->c, g, timereversal != 0, h->q);
     if (st) return st;
+    pt.mark("mesh");
     if (device >= 0) {
         st = build_phonons_device(h->c, fc2, h->q, device, h->ph, h->irr_dyngrad);
         if (st) return st;
@@ -217,6 +222,7 @@ int problem_load(const char *dir, const int32_t grid[3], int fourthorder, int re
         st = build_phonons(h->c, fc2, h->q, h->ph);
         if (st) return st;
     }
+    pt.mark(device >= 0 ? "phonons (device)" : "phonons (host)");
     // off-diagonal kappa inputs: dD/dq at the irreducible points and the atom maps
     {
         const int nb = 3 * h->c.na, ni = h->q.n_irr;

@@ -13,10 +13,11 @@
 // (n^5 complex MACs); for each row b1 the n^3 slice of T1 is contracted with E2, E3, E4 in
 // shared memory (3 n^4 complex MACs per b1): 4 n^5 complex MACs per q-quartet in all.
 // Phases are exact roots of unity from integer lattice vectors, as in the three-phonon
-// kernel. Delta weights, occupations and accumulation are FP64 with the reference's
-// window test; an FP32 pre-screen with a safety margin skips Gaussians that are exactly
-// zero in the reference. Precision R: double (FP64 path) or float (mixed path: FP32
-// pretransform and contraction).
+// kernel. An FP32 pre-screen with a safety margin skips Gaussians that are exactly zero in
+// the reference. Precision R: double (FP64 path: delta weights, occupations and
+// accumulation in FP64 with the reference's window test) or float (mixed path: FP32
+// pretransform and contraction, FP32 delta weights and occupations from FP64 centre
+// differences, FP64 accumulation).
 #include <cuda_runtime.h>
 
 #include "dev_common.cuh"
@@ -303,11 +304,53 @@ __global__ void __launch_bounds__(threads4_for(N), min_blocks4(N, sizeof(R) == 8
                 B[o] = acc;
             }
             __syncthreads();
-            // ---- delta weights, occupations (FP64); F in A as doubles ----
+            // ---- delta weights, occupations (FP64, or FP32 on the mixed path); F in A as doubles ----
             double *F = (double *)A;
             const double o1 = om1[b1], w1 = wrow[b1];
             const double pw4 = kFourPhononPrefactor * w1 * w1;
             const float f_o1 = fo1[b1];
+            // FP32 F of one live mode quadruplet (mixed precision), the FP64 branch's algebra
+            auto weights_f32 = [&](uint32_t live, int b1x, int b2, int b3, int b4) -> float {
+                float sigma;
+                if (it == 1) {
+                    sigma = sigfix32;
+                } else if (it == 2) {
+                    sigma = sqrtf(fs1[b1x] + fs2[b2] + fs3[b3] + fs4[b4]);
+                } else {
+                    const double *v1 = vel + 3 * b1x, *v2 = vel + 3 * (N + b2), *v3 = vel + 3 * (2 * N + b3),
+                                 *v4 = vel + 3 * (3 * N + b4);
+                    sigma = (float)(adaptive_pair(v1, v2, P.reclat_g) / 6.0 + adaptive_pair(v1, v3, P.reclat_g) / 6.0 +
+                                    adaptive_pair(v1, v4, P.reclat_g) / 6.0 + adaptive_pair(v2, v3, P.reclat_g) / 6.0 +
+                                    adaptive_pair(v2, v4, P.reclat_g) / 6.0 + adaptive_pair(v3, v4, P.reclat_g) / 6.0 +
+                                    P.thresh_sigma);
+                }
+                const float invsig = 1.0f / sigma;
+                const float win8 = 8.0f * sigma, h = 0.5f * invsig * invsig, cg = 0.3989422804014327f * invsig;
+                const double o2 = om2[b2], o3 = om3[b3], o4 = om4[b4];
+                auto gf = [&](double centre) -> float {
+                    const float dx = (float)(o1 - centre);
+                    return fabsf(dx) > win8 ? 0.f : expf(-dx * dx * h) * cg;
+                };
+                const float d0 = ((live & 1u) ? gf(o2 + o3 + o4) : 0.f) - ((live & 2u) ? gf(-o2 - o3 - o4) : 0.f);
+                const float d1 = ((live & 4u) ? gf(-o2 + o3 + o4) : 0.f) - ((live & 8u) ? gf(o2 - o3 - o4) : 0.f);
+                const float d2 = ((live & 16u) ? gf(o2 - o3 + o4) : 0.f) - ((live & 32u) ? gf(-o2 + o3 - o4) : 0.f);
+                const float d3 = ((live & 64u) ? gf(o2 + o3 - o4) : 0.f) - ((live & 128u) ? gf(-o2 - o3 + o4) : 0.f);
+                if (d0 == 0.f && d1 == 0.f && d2 == 0.f && d3 == 0.f) return 0.f;
+                const C psi = B[b2 * N2 + b3 * N + b4];
+                const float ps = fmaf((float)psi.x, (float)psi.x, (float)psi.y * (float)psi.y);
+                const int k34 = b3 * N + b4;
+                const float n2 = (float)N2v[b2], n2p = (float)N2p[b2], p00 = (float)P00[k34], p11 = (float)P11[k34];
+                float acc = 0.f, a1 = 0.f;
+                if (d0 != 0.f) acc = (float)mult0 * fmaf(n2p, p11, -n2 * p00) * d0;
+                if (d1 != 0.f) a1 = fmaf((float)N2x3[b2], p11, -n2p * p00) * d1;
+                if (d2 != 0.f || d3 != 0.f) {
+                    const float q1 = p00 + (float)be[2 * N + b3], q2 = p00 + (float)be[3 * N + b4];
+                    const float n2px3 = (float)N2px3[b2];
+                    if (d2 != 0.f) a1 = fmaf(n2px3, q1, -n2 * q2) * d2 + a1;
+                    if (d3 != 0.f) a1 = fmaf(n2px3, q2, -n2 * q1) * d3 + a1;
+                }
+                return (float)pw4 * ps * fmaf((float)mult1, a1, acc);
+            };
             for (int o = tid; o < N3; o += bd) {
                 const int b2 = o / N2, b3 = (o / N) % N, b4 = o % N;
                 double fall = 0.0;
@@ -327,6 +370,14 @@ __global__ void __launch_bounds__(threads4_for(N), min_blocks4(N, sizeof(R) == 8
                                (fabsf(f_o1 - (-f2 + f3 - f4)) <= win ? 32u : 0u) |
                                (fabsf(f_o1 - (f2 + f3 - f4)) <= win ? 64u : 0u) |
                                (fabsf(f_o1 - (-f2 - f3 + f4)) <= win ? 128u : 0u);
+                    }
+                    if constexpr (sizeof(R) == 4) {
+                        // mixed precision: the weights in FP32 from FP64 centre differences
+                        // rounded to FP32 (as the three-phonon kernels), F in FP32; GB300 issues
+                        // FP64 at 1/64 of the FP32 rate and the FP64 weights held this kernel's
+                        // FP64 pipe at 76 %
+                        if (live) fall = (double)weights_f32(live, b1, b2, b3, b4);
+                        live = 0u;
                     }
                     if (live) {
                         double sigma, invsig;

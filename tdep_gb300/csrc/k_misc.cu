@@ -246,7 +246,8 @@ __global__ void __launch_bounds__(256) k_sym_tile(MeshDev m, OrbitDev o, const i
     for (int it = tid; it < nk * n; it += blockDim.x) {
         const int t = it / n, b2 = it - t * n, k = k0 + t;
         const int p0 = off[t], p1 = off[t + 1];
-        // Each image enters a sum once per operation that gives it (mult, one FMA: the sums
+        // Each image enters a sum once per operation that gives it: an add for mult 1, else one
+        // FMA with mult (its int-to-double conversion is an FP64-pipe operation too; the sums
         // are FP64 on a pipe of 2 operations per clock per SM, the bound of this kernel).
         bool averaged = false;
         if (do_dist) {
@@ -258,7 +259,7 @@ __global__ void __launch_bounds__(256) k_sym_tile(MeshDev m, OrbitDev o, const i
                     const double v = vals[p * n + b2];
                     if (__double_as_longlong(v) > 0) {  // v > 0, v not NaN
                         nn += pmu[p];
-                        buf = fma(v, (double)pmu[p], buf);
+                        buf = pmu[p] == 1 ? buf + v : fma(v, (double)pmu[p], buf);
                     }
                 }
                 if (nn) {
@@ -274,7 +275,10 @@ __global__ void __launch_bounds__(256) k_sym_tile(MeshDev m, OrbitDev o, const i
             const int cnt = o.cnt[k];
             if (cnt) {
                 double buf = 0.0;
-                for (int p = p0; p < p1; ++p) buf = fma(vals[p * n + b2], (double)pmu[p], buf);
+                for (int p = p0; p < p1; ++p) {
+                    const double v = vals[p * n + b2];
+                    buf = pmu[p] == 1 ? buf + v : fma(v, (double)pmu[p], buf);
+                }
                 buf *= o.rcp[cnt];
                 for (int p = p0; p < p1; ++p) vals[p * n + b2] = buf;
             }

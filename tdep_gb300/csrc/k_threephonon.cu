@@ -84,20 +84,13 @@ __device__ __forceinline__ const float2 *egvs_ptr<float2>(const PhononDev &ph) {
 
 // The adjoint accumulates d L / d mwm per CTA: FP64 runs in FP64 (in shared memory when the
 // n_fc3 * 27 entries fit, else straight into the CTA's FP64 slice in global memory); mixed
-// runs in FP32, flushed every kAdjFlush q-triplets from shared memory, into a slice of
-// (hi, lo) float pairs with compensated (two-sum) additions. GB300's FP64 pipe runs at 1/64
-// of the FP32 rate and every q-triplet adds into all n_fc3 * 27 entries: FP64 additions and
-// conversions there were half of the mixed adjoint's FP64 pipe.
+// runs in FP32 (flushed every kAdjFlush q-triplets from shared memory) into a slice of
+// floats, summed over the slices in FP64 afterwards. GB300's FP64 pipe runs at 1/64 of the
+// FP32 rate and every q-triplet adds into all n_fc3 * 27 entries: FP64 additions and
+// conversions there were half of the mixed adjoint's FP64 pipe, and 4-byte slices keep the
+// per-CTA slices of a large force-constant set (456 x 120 KB at n_fc3 = 1115) in L2 where
+// (hi, lo) pairs spilled to DRAM. A slice takes a few hundred q-triplets' terms.
 constexpr int kAdjFlush = 64;
-
-// hi + lo += v with the rounding error of the high part carried into the low part
-// (Knuth's two-sum).
-__device__ __forceinline__ float2 add_two_sum(float2 a, float v) {
-    const float s = a.x + v;
-    const float bp = s - a.x;
-    const float err = (a.x - (s - bp)) + (v - bp);
-    return make_float2(s, a.y + err);
-}
 
 // exp(-2 pi i (q2.lv2 + q3.lv3)) of force-constant triplet t as an exact root of unity:
 // q = g/N on the mesh and lv integer, so the phase is twiddle[K] with
@@ -504,8 +497,7 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
                         } else if constexpr (sizeof(R) == 8) {
                             slice[(size_t)tt * 27 + ijk] += (double)v;
                         } else {
-                            float2 *s2 = (float2 *)slice + (size_t)tt * 27 + ijk;
-                            *s2 = add_two_sum(*s2, (float)v);
+                            ((float *)slice)[(size_t)tt * 27 + ijk] += (float)v;
                         }
                     }
                 }
@@ -516,7 +508,7 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
                     if constexpr (sizeof(R) == 8)
                         slice[i] += (double)acc[i];
                     else
-                        ((float2 *)slice)[i] = add_two_sum(((float2 *)slice)[i], (float)acc[i]);
+                        ((float *)slice)[i] += (float)acc[i];
                     acc[i] = (R)0;
                 }
                 since_flush = 0;
@@ -535,7 +527,7 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
                 if constexpr (sizeof(R) == 8)
                     slice[i] += (double)acc[i];
                 else
-                    ((float2 *)slice)[i] = add_two_sum(((float2 *)slice)[i], (float)acc[i]);
+                    ((float *)slice)[i] += (float)acc[i];
             }
         }
     }
@@ -602,14 +594,11 @@ __global__ void k_sum_slices(const double *slices, int32_t n_slice, int64_t n, d
     }
 }
 
-// The same over slices of (hi, lo) float pairs (mixed-precision adjoint).
-__global__ void k_sum_slices_f2(const float2 *slices, int32_t n_slice, int64_t n, double *out) {
+// The same over float slices (mixed-precision adjoint).
+__global__ void k_sum_slices_f(const float *slices, int32_t n_slice, int64_t n, double *out) {
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
         double acc = 0.0;
-        for (int g = 0; g < n_slice; ++g) {
-            const float2 v = slices[(int64_t)g * n + e];
-            acc += (double)v.x + (double)v.y;
-        }
+        for (int g = 0; g < n_slice; ++g) acc += (double)slices[(int64_t)g * n + e];
         out[e] = acc;
     }
 }
@@ -680,7 +669,7 @@ cudaError_t launch_sum_slices(const double *slices, int32_t n_slice, int64_t n, 
     if (precision == 0)
         k_sum_slices<<<g, 256, 0, s>>>(slices, n_slice, n, out);
     else
-        k_sum_slices_f2<<<g, 256, 0, s>>>(reinterpret_cast<const float2 *>(slices), n_slice, n, out);
+        k_sum_slices_f<<<g, 256, 0, s>>>(reinterpret_cast<const float *>(slices), n_slice, n, out);
     return cudaGetLastError();
 }
 

@@ -101,13 +101,6 @@ __device__ __forceinline__ uint32_t a_off_k(int m, int k) {
     return (uint32_t)(((m >> 3) << 7) + ((k >> 3) << 12) + ((m & 7) << 4) + ((k & 7) << 1));
 }
 
-// hi + lo += v, the rounding error of the high part carried into the low part (two-sum).
-__device__ __forceinline__ float2 tc_two_sum(float2 a, float v) {
-    const float s = a.x + v;
-    const float bp = s - a.x;
-    const float err = (a.x - (s - bp)) + (v - bp);
-    return make_float2(s, a.y + err);
-}
 
 __device__ __forceinline__ void st_split(unsigned char *plane_hi, uint32_t off, float x) {
     unsigned short h, l;
@@ -478,7 +471,7 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a)
             __syncthreads();
             {
                 const float2 *Qs = (const float2 *)Aop;
-                float2 *slice = reinterpret_cast<float2 *>(a.mwm_bar) + (size_t)blockIdx.x * fc.n * 27;
+                float *slice = reinterpret_cast<float *>(a.mwm_bar) + (size_t)blockIdx.x * fc.n * 27;
                 constexpr int kGroups = kTcThreads / 27;
                 const int grp = tid / 27, ijk = tid % 27;
                 const int qoff = (ijk % 3) * N2 + ((ijk / 3) % 3) * N + ijk / 9;
@@ -486,8 +479,7 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a)
                     for (int tt = grp; tt < fc.n; tt += kGroups) {
                         const float2 q = Qs[fc.abase[tt] + qoff];
                         const float2 p = ph[tt];
-                        float2 *sl = slice + (size_t)tt * 27 + ijk;
-                        *sl = tc_two_sum(*sl, 2.f * (p.x * q.x - p.y * q.y));
+                        slice[(size_t)tt * 27 + ijk] += 2.f * (p.x * q.x - p.y * q.y);
                     }
                 }
             }

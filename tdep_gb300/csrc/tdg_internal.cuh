@@ -170,8 +170,8 @@ int threephonon_max_per_sm(int n, int precision, int *api = nullptr, int *count 
 // accumulates 2 Re(phase * Q) into a.mwm_bar (one slice per CTA of the returned grid).
 int threephonon_adjoint_grid(int n, int precision, int n_sm, int n_trip, int n_fc, bool acc_in_smem);
 cudaError_t launch_threephonon_adjoint(const ThreePhArgs &a, int precision, int grid, cudaStream_t s);
-// out[e] = sum over g < n_slice of slices[g * n + e], in slice order; the slices hold doubles
-// for precision 0 (FP64) and (hi, lo) float pairs otherwise (the mixed adjoint).
+// out[e] = sum over g < n_slice of slices[g * n + e] in FP64, in slice order; the slices hold
+// doubles for precision 0 (FP64) and floats otherwise (the mixed adjoint).
 cudaError_t launch_sum_slices(const double *slices, int32_t n_slice, int64_t n, int precision, double *out,
                               cudaStream_t s);
 size_t threephonon_smem_bytes(int n, int precision, int n_fc);
@@ -183,7 +183,7 @@ int threephonon_tc_max_per_sm(int n, int n_fc, int *api = nullptr, int *count = 
 cudaError_t launch_threephonon_tc(const ThreePhArgs &a, int n_sm, int ctas_per_sm, cudaStream_t s);
 // Its adjoint (the ADJ variant of k_threephonon_tc: Psi again, W = G conj(Psi), the back-
 // contraction through E3^T, E2^T, E1^T on the tensor cores, 2 Re(phase Q) into a.mwm_bar as
-// (hi, lo) float slices, one per CTA of the returned grid; a.acc_in_smem is not used).
+// float slices, one per CTA of the returned grid; a.acc_in_smem is not used).
 int threephonon_tc_adjoint_grid(int n, int n_sm, int n_trip, int n_fc);
 cudaError_t launch_threephonon_tc_adjoint(const ThreePhArgs &a, int grid, cudaStream_t s);
 // Floats of the transposed force-constant copy, its builder (one CTA, n_blk <= 256) and the

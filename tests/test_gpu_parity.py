@@ -281,9 +281,9 @@ def test_mixed_precision_four_phonon_kappa(configs4):
     lists = QLists.monte_carlo(prob, o64)
     sr = ScatteringRates(prob)
     lw64 = sr.generate(o64, lists).copy()
-    _, k64 = sr.kappa(o64)
+    _, k64 = sr.kappa(o64, maxiter=400, tol=1e-12)
     lw32 = sr.generate(o32, lists).copy()
-    _, k32 = sr.kappa(o32)
+    _, k32 = sr.kappa(o32, maxiter=400, tol=1e-12)  # converged: the stopping iteration is not compared
     sr.close()
     big = lw64 > 1e-3 * lw64.max()
     assert np.max(np.abs(lw32[big] / lw64[big] - 1)) < 1e-4
