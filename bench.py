@@ -360,10 +360,31 @@ def run_reference(args):
 def run_profile(args):
     """--profile: warm-up passes then `steps` passes of one stage, nothing else (for ncu):
     scattering (generate), kappa (one generate, then BTE solves), offdiag (one generate,
-    then off-diagonal kappa) or adjoint (one generate and kappa_SMA, then d kappa_xx / d Phi3
-    passes)."""
-    from tdep_gb300 import ScatteringRates
+    then off-diagonal kappa), adjoint (one generate and kappa_SMA, then d kappa_xx / d Phi3
+    passes) or fourphonon (the four-phonon terms alone, 27 x 27 pair samples per irreducible
+    point)."""
+    from tdep_gb300 import Options, Problem, QLists, ScatteringRates, synth
 
+    if args.stage == "fourphonon":
+        # the four-phonon terms alone on the workload's cell: seeded pair samples of 27 x 27
+        # points per irreducible point (the size of the reference's -qg4ph 3 3 3), as in the
+        # three-plus-four-phonon leg of the default run
+        cfg = CONFIGS[args.config]
+        d = synth.write_config(cfg["synth"], Path(tempfile.mkdtemp(prefix="tdg_prof4_")) / cfg["synth"], seed=1,
+                               order4=True)
+        prob = Problem.load(d, cfg["grid"], fourthorder=True, readiso=True)
+        rng4 = np.random.default_rng(2)
+        s4 = {q: tuple(np.sort(rng4.choice(np.arange(1, prob.n_full + 1), size=27, replace=False)).astype(np.int32)
+                       for _ in range(2)) for q in range(1, prob.n_irr + 1)}
+        lists = QLists.per_irreducible(prob, samples4=s4)
+        opts = Options(temperature=cfg["temperature"], integrationtype=cfg["it"], isotopescattering=False, seed=1,
+                       precision=args.precision, thirdorder=False, fourthorder=True)
+        sr = ScatteringRates(prob)
+        for _ in range(args.warmup + args.steps):
+            sr.generate(opts, lists)
+        log(f"[bench] profile (fourphonon): {sr.stats}")
+        sr.close()
+        return
     cfg, prob, opts, lists = setup(args.config, precision=args.precision)
     sr = ScatteringRates(prob)
     if args.stage == "scattering":
@@ -648,8 +669,11 @@ def run_gb300(args):
         "config": {"workload": cfg["workload"], "mesh": list(cfg["grid"]), "n_mode": n, "q_triplets_per_step": m["trip"],
                    "precision": PRECISION_NOTES[m["path"]],
                    "l2": "256 MB buffer written between steps (L2 flush); Xi+od working set 2x%.2f GB" % m["xi_gb"]},
-        "e2e": m["e2e"],
-        "e2e_from_files": m["e2e_files"],
+        # end to end from the input files (readers, symmetry and mesh on the host, the harmonic
+        # stage on the device, then the scattering pass and kappa); the figure with the problem
+        # already built follows it
+        "e2e": m["e2e_files"] or m["e2e"],
+        "e2e_problem_resident": m["e2e"],
         "adjoint": m["adjoint"],
         "roofline": m["roofline"],
         "cpu_baseline": m["cpu"],
@@ -674,7 +698,8 @@ def run_gb300(args):
         r = measure("rocksalt24", args, min(6.0, args.cpu_budget), with_adjoint=True)
         line["rocksalt24"] = {
             "workload": r["cfg"]["workload"], "value": r["value"], "unit": "q-triplets/s",
-            "ms_per_step": r["ms_per_step"], "q_triplets_per_step": r["trip"], "e2e": r["e2e"], "fp64": r["fp64"],
+            "ms_per_step": r["ms_per_step"], "q_triplets_per_step": r["trip"], "e2e": r["e2e_files"] or r["e2e"],
+            "e2e_problem_resident": r["e2e"], "fp64": r["fp64"],
             "adjoint": r["adjoint"], "roofline": r["roofline"], "cpu_baseline": r["cpu"], "parity": r["parity"],
             "clocks": r["clocks"], "gpu_launches": int(r["launches"]), "kappa_wall_ms": r["kappa_ms"]}
     print(json.dumps(line))
@@ -691,7 +716,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--profile", action="store_true", help="only run passes of one stage, see --stage (for ncu captures)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"], help="with --profile")
-    ap.add_argument("--stage", default="scattering", choices=["scattering", "kappa", "offdiag", "adjoint"],
+    ap.add_argument("--stage", default="scattering", choices=["scattering", "kappa", "offdiag", "adjoint", "fourphonon"],
                     help="with --profile")
     args = ap.parse_args()
     if args.profile:

@@ -458,19 +458,30 @@ int read_fc2(const std::string &path, const Crystal &c, FC2 &fc) {
 }
 
 namespace {
+// The first integer / the first three reals of the next non-empty line, parsed in place
+// (strtol / strtod: a string stream and a token vector per line made the force-constant
+// files the slowest part of a problem load). 0 when the line is missing or does not start
+// with the numbers.
 int read_int_line(std::istream &f, int &x) {
     std::string line;
     if (!getline_nonempty(f, line)) return 0;
-    auto t = split_ws(line);
-    x = std::stoi(t.at(0));
+    const char *p = line.c_str();
+    char *end = nullptr;
+    const long v = std::strtol(p, &end, 10);
+    if (end == p) return 0;
+    x = (int)v;
     return 1;
 }
 int read_vec_line(std::istream &f, double *x) {
     std::string line;
     if (!getline_nonempty(f, line)) return 0;
-    auto t = split_ws(line);
-    if (t.size() < 3) return 0;
-    for (int i = 0; i < 3; ++i) x[i] = std::stod(t[i]);
+    const char *p = line.c_str();
+    for (int i = 0; i < 3; ++i) {
+        char *end = nullptr;
+        x[i] = std::strtod(p, &end);
+        if (end == p) return 0;
+        p = end;
+    }
     return 1;
 }
 // A force-constant lattice vector must be integer in fractional coordinates.

@@ -541,21 +541,32 @@ __global__ void k_unfold(UnfoldDev u) {
     }
 }
 
+// Device buffers of one call, from the library's memory pool on the legacy stream (a pool
+// keeps the memory between calls, where cudaMalloc and cudaFree cost tens of microseconds
+// each for the 30-odd buffers of the stage).
 template <typename T>
 struct DBuf {
     T *p = nullptr;
     size_t n = 0;
     ~DBuf() {
-        if (p) cudaFree(p);
+        if (p) cudaFreeAsync(p, 0);
     }
     cudaError_t alloc(size_t count) {
         n = count;
-        return count ? cudaMalloc(&p, sizeof(T) * count) : cudaSuccess;
+        if (!count) return cudaSuccess;
+        cudaMemPool_t pool = shared_device_pool(dev_of_call());
+        return pool ? cudaMallocFromPoolAsync(reinterpret_cast<void **>(&p), sizeof(T) * count, pool, 0)
+                    : cudaMalloc(&p, sizeof(T) * count);
     }
     cudaError_t up(const T *src, size_t count) {
         cudaError_t e = alloc(count);
         if (e != cudaSuccess || !count) return e;
-        return cudaMemcpy(p, src, sizeof(T) * count, cudaMemcpyHostToDevice);
+        return cudaMemcpyAsync(p, src, sizeof(T) * count, cudaMemcpyHostToDevice, 0);
+    }
+    static int dev_of_call() {
+        int d = 0;
+        cudaGetDevice(&d);
+        return d;
     }
 };
 

@@ -218,7 +218,8 @@ __global__ void __launch_bounds__(256) k_sym_tile(MeshDev m, OrbitDev o, const i
     if (k0 >= ke) return;
     const int nk = min(K, ke - k0);
     double *vals = sym_sm;                                 // [T][n]
-    int *pts = (int *)(vals + (size_t)T * n);              // [T] image of each position
+    double *pmud = vals + (size_t)T * n;                   // [T] multiplicity as a double
+    int *pts = (int *)(pmud + T);                          // [T] image of each position
     int *pmu = pts + T;                                    // [T] its multiplicity
     int *off = pmu + T;                                    // [257] first position of each orbit
     const int tid = threadIdx.x;
@@ -232,22 +233,40 @@ __global__ void __launch_bounds__(256) k_sym_tile(MeshDev m, OrbitDev o, const i
         for (int u = 0; u < nu_t; ++u) {
             pts[my + u] = im[u];
             pmu[my + u] = mu[u];
+            pmud[my + u] = (double)mu[u];  // converted once per image, not once per mode
         }
     }
     if (tid == 0) off[nk] = P;
     __syncthreads();
     double *xr = xi + (int64_t)r * m.n_full * n;
-    for (int e = tid; e < P * n; e += blockDim.x) {
-        const int p = e / n, b2 = e - p * n;
-        vals[e] = xr[(int64_t)pts[p] * n + b2];
+    // gather: eight independent loads in flight per thread before their stores (one load
+    // per loop trip left each thread waiting on one gather at a time); p = e / n through
+    // the float reciprocal, exact here (e < 2^13, and (e + 0.5) / n is at least 0.5 / n
+    // from an integer)
+    const int tot = P * n;
+    const float inv_n = 1.0f / (float)n;
+    constexpr int kGather = 8;
+    for (int e0 = tid; e0 < tot; e0 += kGather * blockDim.x) {
+        double v[kGather];
+#pragma unroll
+        for (int u = 0; u < kGather; ++u) {
+            const int e = e0 + u * blockDim.x;
+            const int p = (int)(((float)e + 0.5f) * inv_n), b2 = e - p * n;
+            v[u] = e < tot ? xr[(int64_t)pts[p < P ? p : 0] * n + b2] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < kGather; ++u) {
+            const int e = e0 + u * blockDim.x;
+            if (e < tot) vals[e] = v[u];
+        }
     }
     __syncthreads();
     const uint32_t *bits = sbits ? sbits + (size_t)r * ((m.n_full + 31) / 32) : nullptr;
     for (int it = tid; it < nk * n; it += blockDim.x) {
         const int t = it / n, b2 = it - t * n, k = k0 + t;
         const int p0 = off[t], p1 = off[t + 1];
-        // Each image enters a sum once per operation that gives it: an add for mult 1, else one
-        // FMA with mult (its int-to-double conversion is an FP64-pipe operation too; the sums
+        // Each image enters a sum once per operation that gives it: one FMA with its mult,
+        // converted to double once per image (conversions run on the FP64 pipe too: the sums
         // are FP64 on a pipe of 2 operations per clock per SM, the bound of this kernel).
         bool averaged = false;
         if (do_dist) {
@@ -259,7 +278,7 @@ __global__ void __launch_bounds__(256) k_sym_tile(MeshDev m, OrbitDev o, const i
                     const double v = vals[p * n + b2];
                     if (__double_as_longlong(v) > 0) {  // v > 0, v not NaN
                         nn += pmu[p];
-                        buf = pmu[p] == 1 ? buf + v : fma(v, (double)pmu[p], buf);
+                        buf = fma(v, pmud[p], buf);
                     }
                 }
                 if (nn) {
@@ -275,18 +294,15 @@ __global__ void __launch_bounds__(256) k_sym_tile(MeshDev m, OrbitDev o, const i
             const int cnt = o.cnt[k];
             if (cnt) {
                 double buf = 0.0;
-                for (int p = p0; p < p1; ++p) {
-                    const double v = vals[p * n + b2];
-                    buf = pmu[p] == 1 ? buf + v : fma(v, (double)pmu[p], buf);
-                }
+                for (int p = p0; p < p1; ++p) buf = fma(vals[p * n + b2], pmud[p], buf);
                 buf *= o.rcp[cnt];
                 for (int p = p0; p < p1; ++p) vals[p * n + b2] = buf;
             }
         }
     }
     __syncthreads();
-    for (int e = tid; e < P * n; e += blockDim.x) {
-        const int p = e / n, b2 = e - p * n;
+    for (int e = tid; e < tot; e += blockDim.x) {
+        const int p = (int)(((float)e + 0.5f) * inv_n), b2 = e - p * n;
         xr[(int64_t)pts[p] * n + b2] = vals[e];
     }
 }
@@ -317,9 +333,12 @@ __global__ void k_sample_bits(int32_t n_full, const int64_t *rbeg, const int32_t
 //  - FP64 runs: Xi and F as (hi, lo) float pairs with hi + lo = x to ~2^-48, each term
 //    accumulated in double-float (exact leading product by FMA, cross terms, TwoSum of the
 //    high parts); ~1e-14 relative. Same bytes per element as FP64.
-//  - mixed-precision runs: Xi and F as floats, the 2^-24 rounding of the FP32 contraction
-//    that produced Xi; chains of kChain products by FMA are added into double-float
-//    accumulators, so the sum over 10^5 columns adds no error of its own. Half the bytes.
+//  - floats (Xi and F), chains of kChain products by FMA added into double-float
+//    accumulators: half the bytes. Mixed-precision runs use the pairs too: with floats, the
+//    modes whose F is zero by symmetry (v = 0 at a high-symmetry point) carry 1e-7 of the
+//    typical |F| from the rounding of Xi, above the convergence test's lo_sqtol floor, and
+//    their relative change kept the sum of the last three checks above 1e-6: rocksalt took
+//    200 iterations (the limit) instead of 31-33, with kappa already converged.
 // A CTA takes ROWS rows (4 or 8, autotuned) and one of the column ranges (gridDim.y): each F
 // value read from L2 serves ROWS rows. Partial sums go to part[row][range][3] (FP64) and are
 // added in range order by k_xi_reduce, so the result does not depend on scheduling. The
@@ -647,7 +666,7 @@ int sym_tile_points(int n_mode) {
 
 size_t sym_tile_smem(int n_mode) {
     const int T = sym_tile_points(n_mode);
-    return sizeof(double) * (size_t)T * n_mode + sizeof(int) * (2 * (size_t)T + 257);
+    return sizeof(double) * (size_t)T * (n_mode + 1) + sizeof(int) * (2 * (size_t)T + 257);
 }
 
 int sym_tile_count(int n_rep, int n_ops, int n_mode) {

@@ -474,7 +474,10 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
 #pragma unroll
                 for (int x = 0; x < N; ++x) A[ab * N + x] = acc[x];
             }
+            // the CTA's slice: doubles on the FP64 path, floats on the mixed path (contiguous
+            // slices of n_fc3 * 27 entries of either type)
             double *slice = a.mwm_bar + (size_t)blockIdx.x * fc.n * 27;
+            float *slicef = reinterpret_cast<float *>(a.mwm_bar) + (size_t)blockIdx.x * fc.n * 27;
             // thread -> one (i,j,k) of the 27 and every groups-th force-constant triplet; within a
             // q-triplet exactly one thread touches each entry, and q-triplets are separated by
             // barriers
@@ -497,7 +500,7 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
                         } else if constexpr (sizeof(R) == 8) {
                             slice[(size_t)tt * 27 + ijk] += (double)v;
                         } else {
-                            ((float *)slice)[(size_t)tt * 27 + ijk] += (float)v;
+                            slicef[(size_t)tt * 27 + ijk] += (float)v;
                         }
                     }
                 }
@@ -508,7 +511,7 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
                     if constexpr (sizeof(R) == 8)
                         slice[i] += (double)acc[i];
                     else
-                        ((float *)slice)[i] += (float)acc[i];
+                        slicef[i] += (float)acc[i];
                     acc[i] = (R)0;
                 }
                 since_flush = 0;
@@ -523,11 +526,12 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
         if (a.acc_in_smem) {
             __syncthreads();
             double *slice = a.mwm_bar + (size_t)blockIdx.x * fc.n * 27;
+            float *slicef = reinterpret_cast<float *>(a.mwm_bar) + (size_t)blockIdx.x * fc.n * 27;
             for (int i = tid; i < fc.n * 27; i += bd) {
                 if constexpr (sizeof(R) == 8)
                     slice[i] += (double)acc[i];
                 else
-                    ((float *)slice)[i] += (float)acc[i];
+                    slicef[i] += (float)acc[i];
             }
         }
     }

@@ -1801,8 +1801,9 @@ extern "C" int tdg_kappa(tdg_ctx *c, const tdg_opts *o, int32_t maxiter, double 
         const int64_t ncol = (int64_t)N * n;
         const size_t nfn = (size_t)nirr * n * 3, nbuf = (size_t)nr * 3;
         CUDA_TRY(c->d_fbb.alloc((size_t)ncol * 3));
-        // element format of the Xi.F products: float pairs for FP64 runs, floats for mixed
-        const bool df = o->precision == TDG_PREC_FP64;
+        // element format of the Xi.F products: float pairs for FP64 and mixed runs (see
+        // k_xi_gemv: with floats the mixed iteration does not pass the convergence test)
+        const bool df = true;
         if (c->xi_fmt != (int)df) {
             CUDA_TRY(c->d_xi_df.alloc(df ? (size_t)nr * ncol : ((size_t)nr * ncol + 1) / 2));
             CUDA_TRY(launch_split_xi(c->d_xi.p, (int64_t)nr * ncol, df, c->d_xi_df.p, s));
@@ -2521,3 +2522,7 @@ extern "C" int tdg_kappa_offdiag(tdg_ctx *c, const tdg_opts *o, double *kappa_of
     std::memcpy(kappa_offdiag, kap, sizeof(kap));
     return kOk;
 }
+
+namespace tdg {
+cudaMemPool_t shared_device_pool(int device) { return device_pool(device); }
+}  // namespace tdg

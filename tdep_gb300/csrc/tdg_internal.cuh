@@ -403,6 +403,10 @@ struct CtxView {
 CtxView ctx_view(tdg_ctx *c);
 
 
+// The library's stream-ordered memory pool of a device (keeps what is freed; contexts and the
+// device harmonic stage allocate from it), or nullptr.
+cudaMemPool_t shared_device_pool(int device);
+
 // ---- launch-shape autotuner (autotune.cu) ----
 // Key of a decision: kernel name, mode count, precision, SM count and device name.
 std::string tune_key(const char *kernel, int n, int precision, int device);
