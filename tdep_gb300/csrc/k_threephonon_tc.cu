@@ -30,10 +30,17 @@
 // share k (= c) and conflict. The padding (modes and components 15, or 9-15 / 12-15) is
 // zero in P and E and stays exactly zero through the stages.
 //
-// Pretransform. The force constants are read in a per-block transposed copy (block = atom
-// triple, triplets of a block consecutive and padded to 4), so that the thread of one
-// output element reads its block's values with 16-byte loads; the phase factors are exact
-// roots of unity from the mesh table, computed once per q-triplet into shared memory.
+// Pretransform. Output element (atom triple, ijk) sums its block's force-constant triplets
+// times their phase factors; the blocks hold 0 to several dozen triplets. A static plan,
+// built once per force-constant set, deals the elements out to the 256 threads (largest
+// first, each to the least-loaded thread) and lays their values out slot-major: slot s of
+// thread t is 4 consecutive triplets of one element (16 bytes at [s][t], zero-padded) and
+// a word with the index of their first phase factor and, on an element's last slot, its
+// operand offset. Every load of a thread is independent of the others (8 in flight per
+// thread), the warp's loads are coalesced, and the threads' slot counts differ by at most
+// one element. The sums run in the triplets' order, as before the plan. The phase factors
+// are exact roots of unity from the mesh table, computed once per q-triplet into shared
+// memory.
 //
 // Every wait is bounded: an MMA or copy that does not complete within about 1 s makes all
 // threads leave together (the decision is a barrier reduction), after waiting for their
@@ -42,7 +49,11 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
+#include <queue>
+#include <utility>
+#include <vector>
 
 #include "dev_common.cuh"
 #include "k3_parts.cuh"
@@ -94,7 +105,7 @@ __host__ __device__ inline TcLayout tc_layout(int n, int nt) {
 // Byte offset of element (m, k) in a 256 x 32 A plane: core matrices of 8 rows x 16 bytes,
 // M groups 128 bytes apart, K groups 4096 bytes apart. MN-major: a core's 8 rows are 8 k,
 // each 8 consecutive m; K-major: its rows are 8 m, each 8 consecutive k.
-__device__ __forceinline__ uint32_t a_off_mn(int m, int k) {
+__host__ __device__ __forceinline__ uint32_t a_off_mn(int m, int k) {
     return (uint32_t)(((m >> 3) << 7) + ((k >> 3) << 12) + ((k & 7) << 4) + ((m & 7) << 1));
 }
 __device__ __forceinline__ uint32_t a_off_k(int m, int k) {
@@ -142,17 +153,20 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// exp(-2 pi i (q2.lv2 + q3.lv3)) of force-constant triplet t as an exact root of unity
-// (see the SIMT kernel): u2, u3 hold g_d L/N_d of q2 and q3.
-__device__ __forceinline__ float2 tc_phase(const Fc3Dev &fc, const MeshDev &m, const int *u2, const int *u3, int t) {
+// Index into the mesh's table of exp(-2 pi i k / L) of the phase factor
+// exp(-2 pi i (q2.lv2 + q3.lv3)) of force-constant triplet t, an exact root of unity (see
+// the SIMT kernel): u2, u3 hold g_d L/N_d of q2 and q3.
+__device__ __forceinline__ int tc_phase_index(const Fc3Dev &fc, const MeshDev &m, const int *u2, const int *u3,
+                                              int t) {
     const int32_t *lv = fc.lv + (size_t)t * 6;
     int S = 0;
 #pragma unroll
-    for (int d = 0; d < 3; ++d) S += u2[d] * lv[d] + u3[d] * lv[3 + d];
+    for (int d = 0; d < 3; ++d) S += u2[d] * __ldg(lv + d) + u3[d] * __ldg(lv + 3 + d);
     int K = S % m.L;
     if (K < 0) K += m.L;
-    return fc.twiddle32[K];
+    return K;
 }
+
 
 // One stage: 2 tiles x 2 K chunks x 3 split products of 128 x 32 x 16, issued by one thread.
 __device__ __forceinline__ void issue_stage(uint32_t tbase, uint32_t a_base, uint32_t e_base, bool a_mn) {
@@ -177,7 +191,6 @@ __device__ __forceinline__ void issue_stage(uint32_t tbase, uint32_t a_base, uin
 template <int N, bool ADJ>
 __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a) {
     constexpr int N2 = N * N, N3 = N2 * N;
-    constexpr int NA = N / 3;
     extern __shared__ __align__(1024) unsigned char smem[];
     const Fc3Dev &fc = a.fc;
     const MeshDev &m = a.mesh;
@@ -263,31 +276,56 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a)
                 u2[d] *= m.lmul[d];
                 u3[d] *= m.lmul[d];
             }
-            for (int i = tid; i < fc.n + 4; i += kTcThreads)
-                ph[i] = i < fc.n ? tc_phase(fc, m, u2, u3, i) : make_float2(0.f, 0.f);
+            // four triplets per thread in flight: their lattice vectors, then their table entries
+            for (int i0 = tid; i0 < fc.n + 4; i0 += 4 * kTcThreads) {
+                int kk[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int i = i0 + u * kTcThreads;
+                    kk[u] = i < fc.n ? tc_phase_index(fc, m, u2, u3, i) : -1;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int i = i0 + u * kTcThreads;
+                    if (i < fc.n + 4) ph[i] = kk[u] >= 0 ? __ldg(fc.twiddle32 + kk[u]) : make_float2(0.f, 0.f);
+                }
+            }
         }
         __syncthreads();
         k3_skip_masks<N>(S);
         // ---- pretransform into the stage-1 operand: rows (c, b), k = a (re) and 16 + a (im) ----
-        for (int idx = tid; idx < N3; idx += kTcThreads) {
-            const int blk = idx / 27, ijk = idx - 27 * blk;
-            const int lo = fc.blk_ptr[blk];
-            const int o0 = a.tc_toff[blk], pc = (a.tc_toff[blk + 1] - o0) / 27;
-            const float4 *mr = (const float4 *)(a.tc_fct + o0 + ijk * pc);
+        // (the plan's slots of this thread: 8 loads of values and 8 of words in flight)
+        {
+            const float4 *pm = a.tc_pm + tid;
+            const uint32_t *pw = a.tc_pword + tid;
             float ar = 0.f, ai = 0.f;
-            for (int j = 0; j < pc; j += 4) {
-                const float4 mv = __ldg(mr + (j >> 2));
-                const float2 p0 = ph[lo + j], p1 = ph[lo + j + 1], p2 = ph[lo + j + 2], p3 = ph[lo + j + 3];
-                ar = fmaf(mv.x, p0.x, ar); ai = fmaf(mv.x, p0.y, ai);
-                ar = fmaf(mv.y, p1.x, ar); ai = fmaf(mv.y, p1.y, ai);
-                ar = fmaf(mv.z, p2.x, ar); ai = fmaf(mv.z, p2.y, ai);
-                ar = fmaf(mv.w, p3.x, ar); ai = fmaf(mv.w, p3.y, ai);
+#pragma unroll 1
+            for (int s0 = 0; s0 < a.tc_slots; s0 += 8) {
+                float4 mv[8];
+                uint32_t wd[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    mv[u] = __ldg(pm + (size_t)(s0 + u) * kTcThreads);
+                    wd[u] = __ldg(pw + (size_t)(s0 + u) * kTcThreads);
+                }
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const float2 *pp = ph + (wd[u] & 0xffffu);
+                    const float2 p0 = pp[0], p1 = pp[1], p2 = pp[2], p3 = pp[3];
+                    ar = fmaf(mv[u].x, p0.x, ar); ai = fmaf(mv[u].x, p0.y, ai);
+                    ar = fmaf(mv[u].y, p1.x, ar); ai = fmaf(mv[u].y, p1.y, ai);
+                    ar = fmaf(mv[u].z, p2.x, ar); ai = fmaf(mv[u].z, p2.y, ai);
+                    ar = fmaf(mv[u].w, p3.x, ar); ai = fmaf(mv[u].w, p3.y, ai);
+                    const uint32_t oc = wd[u] >> 16;  // on an element's last slot: operand offset / 2 + 1
+                    if (oc) {
+                        const uint32_t off = 2u * (oc - 1u);
+                        st_split(Aop, off, ar);
+                        st_split(Aop, off + 8192u, ai);
+                        ar = 0.f;
+                        ai = 0.f;
+                    }
+                }
             }
-            const int a1 = blk / (NA * NA), a2 = (blk / NA) % NA, a3 = blk % NA;
-            const int pa = 3 * a1 + ijk % 3, pb = 3 * a2 + (ijk / 3) % 3, pcc = 3 * a3 + ijk / 9;
-            const uint32_t off = a_off_mn(16 * pcc + pb, pa);
-            st_split(Aop, off, ar);
-            st_split(Aop, off + 8192u, ai);
         }
         // ---- three contraction stages ----
 #pragma unroll 1
@@ -501,29 +539,17 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a)
     if (warp == 0) tc::tmem_dealloc(tbase, 64);
 }
 
-// Per-block transposed copy of the FP32 force constants: block b (atom triple) holds its
-// triplets' 27 values as [ijk][triplet], the triplet count padded to 4 with zeros; toff[b]
-// is the block's first float and toff[n_blk] the total. One CTA.
-__global__ void k_tc_prep_fc(const int32_t *blk_ptr, int32_t n_blk, const float *mwm32, int32_t *toff, float *out) {
-    __shared__ int32_t s_off[256 + 1];
-    if (threadIdx.x == 0) {
-        int32_t o = 0;
-        for (int b = 0; b < n_blk; ++b) {
-            s_off[b] = o;
-            const int32_t c = blk_ptr[b + 1] - blk_ptr[b];
-            o += 27 * ((c + 3) & ~3);
-        }
-        s_off[n_blk] = o;
-    }
-    __syncthreads();
-    for (int b = threadIdx.x; b <= n_blk; b += blockDim.x) toff[b] = s_off[b];
-    for (int b = 0; b < n_blk; ++b) {
-        const int32_t lo = blk_ptr[b], c = blk_ptr[b + 1] - lo, pc = (c + 3) & ~3;
-        for (int e = threadIdx.x; e < 27 * pc; e += blockDim.x) {
-            const int ijk = e / pc, j = e - ijk * pc;
-            out[s_off[b] + e] = j < c ? mwm32[(size_t)(lo + j) * 27 + ijk] : 0.f;
-        }
-    }
+// Values of the pretransform plan from the current FP32 force constants: slot word src =
+// first triplet | ijk << 16 | valid triplets << 21 (0 to 4; the rest of the 16 bytes zero).
+__global__ void k_tc_fill_plan(const uint32_t *src, int64_t n_slot, const float *mwm32, float4 *pm) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_slot) return;
+    const uint32_t w = src[i];
+    const int f = (int)(w & 0xffffu), ijk = (int)((w >> 16) & 31u), nv = (int)(w >> 21);
+    float v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) v[u] = u < nv ? mwm32[(size_t)(f + u) * 27 + ijk] : 0.f;
+    pm[i] = make_float4(v[0], v[1], v[2], v[3]);
 }
 
 // Real-split eigenvector images of every mesh point: B = [[Er, Ei], [-Ei, Er]] (32 x 32,
@@ -591,6 +617,7 @@ int threephonon_tc_max_per_sm(int n, int n_fc, int *api, int *count) {
 
 cudaError_t launch_threephonon_tc(const ThreePhArgs &a, int n_sm, int ctas_per_sm, cudaStream_t s) {
     if (a.n_trip <= 0) return cudaSuccess;
+    if (!a.tc_eimg || !a.tc_pm || !a.tc_pword || a.tc_slots < 8 || a.tc_slots % 8 != 0) return cudaErrorInvalidValue;
     switch (a.mesh.n_mode) {
         case 9: return tc_launch_grid<9, false>(a, tc_grid<9, false>(a.fc.n, a.n_trip, n_sm, ctas_per_sm), s);
         case 12: return tc_launch_grid<12, false>(a, tc_grid<12, false>(a.fc.n, a.n_trip, n_sm, ctas_per_sm), s);
@@ -610,7 +637,9 @@ int threephonon_tc_adjoint_grid(int n, int n_sm, int n_trip, int n_fc) {
 
 cudaError_t launch_threephonon_tc_adjoint(const ThreePhArgs &a, int grid, cudaStream_t s) {
     if (a.n_trip <= 0) return cudaSuccess;
-    if (!a.tc_eimg || !a.tc_eimg_t || !a.tc_fct || !a.lam || !a.mwm_bar) return cudaErrorInvalidValue;
+    if (!a.tc_eimg || !a.tc_eimg_t || !a.tc_pm || !a.tc_pword || a.tc_slots < 8 || a.tc_slots % 8 != 0 || !a.lam ||
+        !a.mwm_bar)
+        return cudaErrorInvalidValue;
     switch (a.mesh.n_mode) {
         case 9: return tc_launch_grid<9, true>(a, grid, s);
         case 12: return tc_launch_grid<12, true>(a, grid, s);
@@ -619,12 +648,64 @@ cudaError_t launch_threephonon_tc_adjoint(const ThreePhArgs &a, int grid, cudaSt
     }
 }
 
-size_t tc_fct_floats(int n_fc, int n_blk) { return 27 * ((size_t)n_fc + 3 * (size_t)n_blk); }
+int tc_pretransform_plan(int n, int n_blk, const int32_t *blk_ptr, std::vector<uint32_t> &word,
+                         std::vector<uint32_t> &src) {
+    const int na = n / 3;
+    if (n % 3 != 0 || n > 16 || n_blk != na * na * na || blk_ptr[0] != 0) return 0;
+    const int n_fc = blk_ptr[n_blk];
+    if (n_fc < 0 || n_fc + 4 > 0xffff) return 0;
+    // elements (block, ijk) with their slot counts, largest first (stable), each to the
+    // least-loaded thread (lowest index on ties)
+    std::vector<int> blocks(n_blk);
+    for (int b = 0; b < n_blk; ++b) blocks[b] = b;
+    auto slots_of = [&](int b) { return (blk_ptr[b + 1] - blk_ptr[b] + 3) / 4; };
+    std::stable_sort(blocks.begin(), blocks.end(), [&](int x, int y) { return slots_of(x) > slots_of(y); });
+    using Load = std::pair<int, int>;  // (slots, thread)
+    std::priority_queue<Load, std::vector<Load>, std::greater<Load>> heap;
+    for (int t = 0; t < kTcThreads; ++t) heap.push({0, t});
+    std::vector<std::vector<int>> mine(kTcThreads);  // element = 27 block + ijk
+    for (int b : blocks) {
+        const int c = slots_of(b);
+        if (c == 0) break;
+        for (int ijk = 0; ijk < 27; ++ijk) {
+            Load l = heap.top();
+            heap.pop();
+            mine[l.second].push_back(27 * b + ijk);
+            heap.push({l.first + c, l.second});
+        }
+    }
+    int most = 0;
+    while (!heap.empty()) {
+        most = std::max(most, heap.top().first);
+        heap.pop();
+    }
+    const int slots = std::max(8, (most + 7) / 8 * 8);
+    word.assign((size_t)slots * kTcThreads, 0u);
+    src.assign((size_t)slots * kTcThreads, 0u);
+    for (int t = 0; t < kTcThreads; ++t) {
+        int sl = 0;
+        for (int e : mine[t]) {
+            const int b = e / 27, ijk = e % 27;
+            const int lo = blk_ptr[b], c = blk_ptr[b + 1] - lo;
+            const int a1 = b / (na * na), a2 = (b / na) % na, a3 = b % na;
+            const int pa = 3 * a1 + ijk % 3, pb = 3 * a2 + (ijk / 3) % 3, pcc = 3 * a3 + ijk / 9;
+            const uint32_t off = a_off_mn(16 * pcc + pb, pa);  // < 8192, even
+            for (int j = 0; j < c; j += 4) {
+                const size_t i = (size_t)sl * kTcThreads + t;
+                const uint32_t f = (uint32_t)(lo + j), nv = (uint32_t)std::min(4, c - j);
+                word[i] = f | (j + 4 >= c ? ((off / 2u + 1u) << 16) : 0u);
+                src[i] = f | ((uint32_t)ijk << 16) | (nv << 21);
+                ++sl;
+            }
+        }
+    }
+    return slots;
+}
 
-cudaError_t launch_tc_prep_fc(const int32_t *blk_ptr, int32_t n_blk, const float *mwm32, int32_t *toff, float *out,
-                              cudaStream_t s) {
-    if (n_blk > 256) return cudaErrorInvalidValue;
-    k_tc_prep_fc<<<1, 256, 0, s>>>(blk_ptr, n_blk, mwm32, toff, out);
+cudaError_t launch_tc_fill_plan(const uint32_t *src, int slots, const float *mwm32, float4 *pm, cudaStream_t s) {
+    const int64_t n_slot = (int64_t)slots * kTcThreads;
+    if (n_slot <= 0) return cudaErrorInvalidValue;
+    k_tc_fill_plan<<<(unsigned)((n_slot + 255) / 256), 256, 0, s>>>(src, n_slot, mwm32, pm);
     return cudaGetLastError();
 }
 

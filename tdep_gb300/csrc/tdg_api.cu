@@ -191,11 +191,13 @@ struct tdg_ctx {
     std::vector<int> fc3_perm;  // device (block-sorted) position -> index in the problem
     DevBuf<double> fc3_mwm, fc4_mwm;
     DevBuf<float> fc3_mwm32, fc4_mwm32;
-    // tensor-core fused kernel (9-15 modes, mixed): eigenvector images built on first use,
-    // transposed force constants rebuilt by every call (tdg_set_fc3 may change them)
+    // tensor-core fused kernel (9-15 modes, mixed): eigenvector images built on first use;
+    // the pretransform plan's layout built with the force constants (tc_slots 0: no plan),
+    // its values refilled by every call (tdg_set_fc3 may change them)
     DevBuf<unsigned char> d_tc_eimg, d_tc_eimg_t;  // E and E^T images (the latter for the adjoint)
-    DevBuf<float> d_tc_fct;
-    DevBuf<int32_t> d_tc_toff;
+    DevBuf<uint32_t> d_tc_pword, d_tc_psrc;
+    DevBuf<float4> d_tc_pm;
+    int tc_slots = 0;
     bool tc_eimg_ready = false, tc_eimg_t_ready = false;
     int last_path = -1;  // 0 SIMT fused kernel, 1 tensor-core fused kernel, 2 large-cell batches
     // fused three-phonon launch of the last scattering call: grid, CTAs per SM used, the
@@ -631,6 +633,15 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
         chk(launch_egv_scaled((int64_t)nm, c->n, c->d_egv.p, c->d_omega.p, c->d_egvs.p, c->d_egvs32.p, s));
     chk(c->d_disorder.upload(c->disorder.data(), c->disorder.size(), s));
     chk(c->fc3_blk.upload(blk_ptr3.data(), blk_ptr3.size(), s));
+    if (c->n == 9 || c->n == 12 || c->n == 15) {
+        std::vector<uint32_t> pword, psrc;
+        c->tc_slots = tc_pretransform_plan(c->n, na * na * na, blk_ptr3.data(), pword, psrc);
+        if (c->tc_slots > 0) {
+            chk(c->d_tc_pword.upload(pword.data(), pword.size(), s));
+            chk(c->d_tc_psrc.upload(psrc.data(), psrc.size(), s));
+            chk(c->d_tc_pm.alloc(pword.size()));
+        }
+    }
     chk(c->fc3_abase.upload(abase3.data(), abase3.size(), s));
     chk(c->fc3_lv.upload(lv3.data(), lv3.size(), s));
     chk(c->fc3_mwm.upload(mwm3.data(), mwm3.size(), s));
@@ -1369,7 +1380,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         c->last_ln = n > 18 || o->tensor_cores == 1;
         const char *tc_env = std::getenv("TDG_TC_SMALL");
         const bool use_tc = !c->last_ln && o->tensor_cores != 2 && !(tc_env && tc_env[0] == '0') &&
-                            threephonon_tc_supported(n, o->precision, c->n_fc3);
+                            threephonon_tc_supported(n, o->precision, c->n_fc3) && c->tc_slots > 0;
         c->last_path = c->last_ln ? 2 : (use_tc ? 1 : 0);
         if (use_tc) {
             if (!c->tc_eimg_ready) {
@@ -1379,12 +1390,10 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
                 CUDA_TRY(launch_tc_eimg(N, n, c->d_egvs32.p, c->d_tc_eimg.p, s));
                 c->tc_eimg_ready = true;
             }
-            chk(c->d_tc_fct.alloc(tc_fct_floats(c->n_fc3, c->na * c->na * c->na)));
-            chk(c->d_tc_toff.alloc((size_t)c->na * c->na * c->na + 1));
-            if (e != cudaSuccess) return set_error(kErrDevice, std::string("allocation failed: ") + cudaGetErrorString(e));
             a.tc_eimg = c->d_tc_eimg.p;
-            a.tc_fct = c->d_tc_fct.p;
-            a.tc_toff = c->d_tc_toff.p;
+            a.tc_pm = c->d_tc_pm.p;
+            a.tc_pword = c->d_tc_pword.p;
+            a.tc_slots = c->tc_slots;
         }
         // the launch shape comes first (autotuner trials run outside any graph), then the
         // three-phonon part of the pipeline runs directly or as the context's graph
@@ -1441,8 +1450,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
             const std::string key = tune_key(use_tc ? "threephonon_tc" : "threephonon", n, o->precision, c->device);
             auto fused = [&, use_tc](const ThreePhArgs &x, int v) -> cudaError_t {
                 if (!use_tc) return launch_threephonon(x, o->precision, c->n_sm, v, s);
-                const cudaError_t ep = launch_tc_prep_fc(c->fc3_blk.p, c->na * c->na * c->na, c->fc3_mwm32.p,
-                                                         c->d_tc_toff.p, c->d_tc_fct.p, s);
+                const cudaError_t ep = launch_tc_fill_plan(c->d_tc_psrc.p, c->tc_slots, c->fc3_mwm32.p, c->d_tc_pm.p, s);
                 if (ep != cudaSuccess) return ep;
                 return launch_threephonon_tc(x, c->n_sm, v, s);
             };
@@ -2340,7 +2348,8 @@ extern "C" int tdg_adjoint_fc3(tdg_ctx *c, const tdg_opts *o, const double *lw_b
     // the tensor cores too; otherwise the SIMT kernel's ADJ variant
     const char *tc_env = std::getenv("TDG_TC_SMALL");
     const bool use_tc = c->last_path == 1 && o->precision != TDG_PREC_FP64 && o->tensor_cores != 2 &&
-                        !(tc_env && tc_env[0] == '0') && threephonon_tc_supported(n, o->precision, c->n_fc3);
+                        !(tc_env && tc_env[0] == '0') && threephonon_tc_supported(n, o->precision, c->n_fc3) &&
+                        c->tc_slots > 0;
     // the CTA's gradient slice lives in shared memory when it is small enough (SIMT)
     const bool acc_smem = !use_tc && (size_t)c->n_fc3 * 27 * sizeof(double) <= 48 * 1024;
     const int grid = use_tc ? threephonon_tc_adjoint_grid(n, c->n_sm, ntrip, c->n_fc3)
@@ -2390,12 +2399,12 @@ extern "C" int tdg_adjoint_fc3(tdg_ctx *c, const tdg_opts *o, const double *lw_b
             CUDA_TRY(launch_tc_eimg(c->N, n, c->d_egvs32.p, c->d_tc_eimg_t.p, s, true));
             c->tc_eimg_t_ready = true;
         }
-        CUDA_TRY(launch_tc_prep_fc(c->fc3_blk.p, c->na * c->na * c->na, c->fc3_mwm32.p, c->d_tc_toff.p,
-                                   c->d_tc_fct.p, s));
+        CUDA_TRY(launch_tc_fill_plan(c->d_tc_psrc.p, c->tc_slots, c->fc3_mwm32.p, c->d_tc_pm.p, s));
         a.tc_eimg = c->d_tc_eimg.p;
         a.tc_eimg_t = c->d_tc_eimg_t.p;
-        a.tc_fct = c->d_tc_fct.p;
-        a.tc_toff = c->d_tc_toff.p;
+        a.tc_pm = c->d_tc_pm.p;
+        a.tc_pword = c->d_tc_pword.p;
+        a.tc_slots = c->tc_slots;
     }
     CUDA_TRY(cudaEventRecord(ev[1], s));
     if (use_tc)

@@ -154,10 +154,12 @@ struct ThreePhArgs {
     const double *xi_bar;       // adjoint only, may be null: cotangent of the raw three-phonon
                                 // row terms of Xi ([n_row * n_full*n], tdg_kappa_iter_vjp)
     // tensor-core kernel only (k_threephonon_tc): real-split eigenvector images of every mesh
-    // point (4 KB each), the per-block transposed FP32 force constants and their offsets
+    // point (4 KB each) and the pretransform plan (tc_pretransform_plan): tc_slots x 256
+    // values (4 FP32 force constants per slot) and words
     const unsigned char *tc_eimg;
-    const float *tc_fct;
-    const int32_t *tc_toff;
+    const float4 *tc_pm;
+    const uint32_t *tc_pword;
+    int32_t tc_slots;
     // tensor-core adjoint only: the images of the transposed eigenvector matrices (E^T)
     const unsigned char *tc_eimg_t;
 };
@@ -186,11 +188,16 @@ cudaError_t launch_threephonon_tc(const ThreePhArgs &a, int n_sm, int ctas_per_s
 // float slices, one per CTA of the returned grid; a.acc_in_smem is not used).
 int threephonon_tc_adjoint_grid(int n, int n_sm, int n_trip, int n_fc);
 cudaError_t launch_threephonon_tc_adjoint(const ThreePhArgs &a, int grid, cudaStream_t s);
-// Floats of the transposed force-constant copy, its builder (one CTA, n_blk <= 256) and the
-// eigenvector images (n <= 16).
-size_t tc_fct_floats(int n_fc, int n_blk);
-cudaError_t launch_tc_prep_fc(const int32_t *blk_ptr, int32_t n_blk, const float *mwm32, int32_t *toff, float *out,
-                              cudaStream_t s);
+// Pretransform plan of the tensor-core kernel for n modes and the force-constant blocks
+// blk_ptr (n_blk + 1 offsets, host memory): the elements (atom triple, ijk) dealt out to
+// the 256 threads of a CTA, slot-major ([slot][thread]); word = first phase-factor index |
+// (operand offset / 2 + 1) << 16 on an element's last slot, src = first triplet | ijk << 16
+// | valid triplets << 21. Returns the slot count (a multiple of 8), 0 if the set does not fit.
+int tc_pretransform_plan(int n, int n_blk, const int32_t *blk_ptr, std::vector<uint32_t> &word,
+                         std::vector<uint32_t> &src);
+// The plan's values from the FP32 force constants ([n_fc * 27]), slots x 256 float4.
+cudaError_t launch_tc_fill_plan(const uint32_t *src, int slots, const float *mwm32, float4 *pm, cudaStream_t s);
+// Real-split eigenvector images (n <= 16).
 // transpose: the image of E^T (rows modes, columns components) for the adjoint.
 cudaError_t launch_tc_eimg(int32_t n_full, int32_t n, const float2 *egvs32, unsigned char *out, cudaStream_t s,
                            bool transpose = false);
