@@ -27,6 +27,8 @@ struct K3Smem {
     double *R3;            // [n^2] column sums, then Xi row terms
     double *F;             // [n^3] dense F (zero where no survivor)
     float *fo1, *fo2, *fo3, *fs1, *fs2, *fs3;
+    float *fl1, *fl2, *fl3;  // omega - (double)fo in FP32: omega = fo + fl to about 2^-48
+    float *fb2, *fb3, *fw1;  // be2, be3 and wrow in FP32 (the FP32 weights)
     uint32_t *m12, *m13, *m23;
     uint32_t *zmask;       // [2]: omega2 < tol, omega3 < tol
     uint32_t *rowbits;     // [n^2] b3 with a non-zero F for each (b1, b2)
@@ -56,9 +58,16 @@ __device__ __forceinline__ void k3_load_modes(const K3Smem &S, const ThreePhArgs
         S.s1[b] = P.sigsq[(size_t)rec.q1 * N + b];
         S.s2[b] = P.sigsq[(size_t)i2 * N + b];
         S.s3[b] = P.sigsq[(size_t)i3 * N + b];
-        S.fo1[b] = P.omega32[(size_t)f1 * N + b];
-        S.fo2[b] = P.omega32[(size_t)q2 * N + b];
-        S.fo3[b] = P.omega32[(size_t)q3 * N + b];
+        const float h1 = P.omega32[(size_t)f1 * N + b], h2 = P.omega32[(size_t)q2 * N + b],
+                    h3 = P.omega32[(size_t)q3 * N + b];
+        S.fo1[b] = h1;
+        S.fo2[b] = h2;
+        S.fo3[b] = h3;
+        S.fl1[b] = (float)(S.om1[b] - (double)h1);
+        S.fl2[b] = (float)(S.om2[b] - (double)h2);
+        S.fl3[b] = (float)(S.om3[b] - (double)h3);
+        S.fb2[b] = (float)S.be2[b];
+        S.fb3[b] = (float)S.be3[b];
         S.fs1[b] = P.sigsq32[(size_t)rec.q1 * N + b];
         S.fs2[b] = P.sigsq32[(size_t)i2 * N + b];
         S.fs3[b] = P.sigsq32[(size_t)i3 * N + b];
@@ -71,6 +80,7 @@ __device__ __forceinline__ void k3_load_modes(const K3Smem &S, const ThreePhArgs
         const bool on = (mask[b >> 5] >> (b & 31)) & 1u;
         S.rowid[b] = on ? r : -1;
         S.wrow[b] = a.rows.w3q[(size_t)rec.q1 * N + b];
+        S.fw1[b] = (float)S.wrow[b];
         S.m12[b] = 0u;
         S.m13[b] = 0u;
         S.m23[b] = 0u;
@@ -203,27 +213,43 @@ __device__ __forceinline__ void k3_survivors(const K3Smem &S, const PhononDev &P
     }
 }
 
-// The same in FP32 for the tensor-core kernel (mixed precision): the centre differences
-// om1 - (+-om2 +- om3) in FP64 then rounded to FP32 (relative error 6e-8 of the difference),
-// the width, the exponent and the Gaussian in FP32 (expf), F in FP32 stored as a double
-// for the FP64 sums. Relative error of a weight about 1e-6, against the 1e-5 of the BF16x3
-// contraction; GB300 issues FP64 at 1/64 of the FP32 rate, and this stage was a third of
-// the kernel's FP64 pipe.
+// om1 - (m2 + m3) from the FP32 pairs omega = h + l (h = the FP32 omega, l the FP32 rest):
+// the sums of the h parts with their exact rounding errors (Knuth's TwoSum, FP32 additions
+// only) plus the l parts. Accurate to about 2^-24 of the difference plus 2^-46 of omega, as
+// the FP64 difference rounded to FP32; no FP64 operation (GB300 issues FP64 at 1/64 of the
+// FP32 rate).
+__device__ __forceinline__ float k3_centre_diff(float h1, float l1, float h2, float l2, float h3, float l3) {
+    const float s = h2 + h3;
+    const float bs = s - h2;
+    const float es = (h2 - (s - bs)) + (h3 - bs);  // h2 + h3 = s + es exactly
+    const float d = h1 - s;
+    const float bd = d - h1;
+    const float ed = (h1 - (d - bd)) + (-s - bd);  // h1 - s = d + ed exactly
+    return d + (ed + ((l1 - l2 - l3) - es));
+}
+
+// The same in FP32 for the mixed-precision kernels: the centre differences om1 - (+-om2 +-
+// om3) from FP32 pairs (k3_centre_diff, as accurate as the FP64 difference rounded to
+// FP32), the width, the exponent and the Gaussian in FP32 (expf), the occupation factors
+// and row weight from FP32 copies made once per mode, F in FP32 stored as a double for the
+// FP64 sums. Relative error of a weight about 1e-6, against the 1e-5 of the BF16x3
+// contraction.
 template <int N, typename PsiSq>
 __device__ __forceinline__ void k3_survivors_f32(const K3Smem &S, const PhononDev &P, int nq, float perm,
                                                  PsiSq psisq) {
     constexpr int N2 = N * N;
     constexpr float kSqrt2PiInvF = 0.3989422804014327f;
     const int it = P.integrationtype;
+    const float sfix = (float)P.sigma_fixed;
+    const float pref = (float)kThreePhononPrefactor;
     for (int s = threadIdx.x; s < nq; s += blockDim.x) {
         const uint32_t qv = S.Q[s];
         const int idx = (int)(qv & 0xffffu);
         uint32_t live = qv >> 16;
         const int b1 = idx / N2, b2 = (idx / N) % N, b3 = idx % N;
-        const double o1 = S.om1[b1], o2 = S.om2[b2], o3 = S.om3[b3];
         float sigma;
         if (it == 1) {
-            sigma = (float)P.sigma_fixed;
+            sigma = sfix;
         } else if (it == 2) {
             sigma = sqrtf(S.fs1[b1] + S.fs2[b2] + S.fs3[b3]);
         } else {
@@ -233,14 +259,15 @@ __device__ __forceinline__ void k3_survivors_f32(const K3Smem &S, const PhononDe
         }
         const float invsig = 1.0f / sigma;
         const float win8 = 8.0f * sigma, h = 0.5f * invsig * invsig, cg = kSqrt2PiInvF * invsig;
+        const float h1 = S.fo1[b1], l1 = S.fl1[b1], h2 = S.fo2[b2], l2 = S.fl2[b2], h3 = S.fo3[b3], l3 = S.fl3[b3];
         float g[4] = {0.f, 0.f, 0.f, 0.f};
         while (live) {
             const int j = __ffs(live) - 1;
             live &= live - 1;
             // Gaussian j centred at (-om2+om3, om2-om3, om2+om3, -om2-om3), get_dirac's order
-            const double m2 = (j == 1 || j == 2) ? o2 : -o2;
-            const double m3 = (j == 0 || j == 2) ? o3 : -o3;
-            const float dx = (float)(o1 - (m2 + m3));
+            const float sg2 = (j == 1 || j == 2) ? 1.f : -1.f;
+            const float sg3 = (j == 0 || j == 2) ? 1.f : -1.f;
+            const float dx = k3_centre_diff(h1, l1, sg2 * h2, sg2 * l2, sg3 * h3, sg3 * l3);
             const float gj = fabsf(dx) > win8 ? 0.f : expf(-dx * dx * h) * cg;
             g[0] = j == 0 ? gj : g[0];
             g[1] = j == 1 ? gj : g[1];
@@ -249,8 +276,8 @@ __device__ __forceinline__ void k3_survivors_f32(const K3Smem &S, const PhononDe
         }
         const float d0 = g[0] - g[1], d1 = g[2] - g[3];
         if (d0 != 0.f || d1 != 0.f) {
-            const float pq = (float)kThreePhononPrefactor * psisq(idx) * (float)S.wrow[b1];
-            const float n2 = (float)S.be2[b2], n3 = (float)S.be3[b3];
+            const float pq = pref * psisq(idx) * S.fw1[b1];
+            const float n2 = S.fb2[b2], n3 = S.fb3[b3];
             const float fsum = perm * pq * ((n2 - n3) * d0 + (n2 + n3 + 1.0f) * d1);
             S.F[idx] = (double)fsum;
             if (fsum != 0.f) {

@@ -11,7 +11,8 @@
 //           writes the next stage's operand with the new index last, so that after
 //           contracting a (E1), b (E2) and c (E3) the result is Psi[b1][b2][b3]
 //   delta   get_dirac and the accumulation of Gamma and the Xi row terms
-//           (scattering_threephonon.f90:115-135, 219-271), FP64 weights and sums.
+//           (scattering_threephonon.f90:115-135, 219-271): FP32 screen, FP32 Gaussians
+//           and occupation factors from FP64 centre differences, FP64 sums.
 // GEMM operands are BF16 hi/lo splits of FP32 values (hi*hi + hi*lo + lo*hi into an FP32
 // tensor-memory accumulator, about 16 significant bits per operand) in shared memory as
 // 8 x 16-byte core matrices without swizzle, both operands MN-major; the layout and the
@@ -30,6 +31,7 @@ namespace tdg {
 namespace {
 
 constexpr double kLnPrefactor = 3.141592653589793 / 16.0;
+constexpr float kSqrt2PiInvF = 0.3989422804014327f;
 constexpr long long kLnWaitCycles = 4000000000LL;  // about 2 s at 2 GHz
 
 __device__ __forceinline__ void store_split(__nv_bfloat16 *hi, __nv_bfloat16 *lo, int64_t i, float v) {
@@ -428,8 +430,8 @@ __global__ void __launch_bounds__(kLnGemmThreads, 1) k_ln_gemm(LnGemmArgs g) {
 // Gaussian inside its 8-sigma window. In blocks of BB rows b2 (16 or 32, autotuned): (A) every pair is screened
 // in FP32 (window with a margin far above FP32 rounding, degeneracy skips pre-checked in
 // FP32), the survivors are compacted into a queue with a block scan; (B) full warps evaluate
-// the queue with the reference's FP64 window test, weights and occupations into a dense F;
-// (C) R2[b2] = sum_b3 F and R3[b3] += sum_b2 F.
+// the queue's Gaussians (the reference's 8-sigma window) and occupations in FP32 into a
+// dense FP64 F; (C) R2[b2] = sum_b3 F and R3[b3] += sum_b2 F in FP64.
 
 struct LnDeltaArgs {
     MeshDev mesh;
@@ -448,7 +450,7 @@ struct LnDeltaArgs {
 
 __host__ __device__ inline size_t ln_delta_smem(int n, int bb) {
     return sizeof(double) * ((size_t)14 * n + (size_t)bb * n) + sizeof(uint32_t) * (size_t)bb * n +
-           sizeof(int) * 33 + sizeof(float) * 4 * (size_t)n + 16;
+           sizeof(int) * 33 + sizeof(float) * 6 * (size_t)n + 16;
 }
 
 // ADJ: the adjoint's weights. F holds G_b = lam(row) * nred * dF_b/d|Psi_b|^2 of the
@@ -480,7 +482,7 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
     int *wsum = (int *)(Q + (size_t)BB * n);
     // FP32 copies for the screen (double -> float conversions run on the FP64 pipe, so they
     // are made once per mode here instead of once per pair); NaN marks omega < 1e-9 Ha.
-    float *g2 = (float *)(wsum + 33), *g3 = g2 + n, *t2 = g3 + n, *t3 = t2 + n;
+    float *g2 = (float *)(wsum + 33), *g3 = g2 + n, *t2 = g3 + n, *t3 = t2 + n, *c2 = t3 + n, *c3 = c2 + n;
     for (int b = tid; b < n; b += bd) {
         om2[b] = P.omega[(size_t)q2 * n + b];
         om3[b] = P.omega[(size_t)q3 * n + b];
@@ -492,6 +494,8 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
         g3[b] = om3[b] < kFreqTolD ? __int_as_float(0x7fc00000) : (float)om3[b];
         t2[b] = (float)s2[b];
         t3[b] = (float)s3[b];
+        c2[b] = (float)be2[b];
+        c3[b] = (float)be3[b];
         for (int d = 0; d < 3; ++d) {
             v2[b * 3 + d] = P.vel[((size_t)q2 * n + b) * 3 + d];
             v3[b * 3 + d] = P.vel[((size_t)q3 * n + b) * 3 + d];
@@ -509,6 +513,7 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
     // the adjoint's G = lambda(row) * k * dF/d|Psi|^2
     const double pw = perm * kLnPrefactor * w;
     const double fadj = ADJ ? a.lam[row] * (double)rec.red_cnt * pw : 0.0;
+    const float pwf = (float)pw;
     const int it = P.integrationtype;
     const float fo1 = (float)o1, fs1 = (float)s1, fsig = (float)P.sigma_fixed;
     const float2 *psi = a.psi + ((int64_t)s * n + b1) * n * n;
@@ -548,48 +553,51 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
             if (l) Q[k++] = (uint32_t)e | (l << 16);
         }
         __syncthreads();
-        // (B) FP64 delta weights and occupations of the survivors, full warps
+        // (B) delta weights and occupations of the survivors, full warps: the Gaussians and
+        // occupation factors in FP32 from FP64 centre differences (the path is mixed
+        // precision; GB300 issues FP64 at 1/64 of the FP32 rate), the sums in FP64
         for (int i = tid; i < total; i += bd) {
             const uint32_t qv = Q[i];
             const int e = (int)(qv & 0xffffu);
-            const uint32_t live = qv >> 16;
+            uint32_t live = qv >> 16;
             const int b2 = bb + e / n, b3 = e % n;
             const double o2 = om2[b2], o3 = om3[b3];
-            double sigma, invsig;
+            float sigma;
             if (it == 1) {
-                sigma = P.sigma_fixed;
-                invsig = 1.0 / sigma;
+                sigma = fsig;
             } else if (it == 2) {
-                const double sq = s1 + s2[b2] + s3[b3];
-                invsig = rsqrt(sq);
-                sigma = sq * invsig;
+                sigma = sqrtf(fs1 + t2[b2] + t3[b3]);
             } else {
-                sigma = adaptive_pair(v1, v2 + 3 * b2, P.reclat_g) / 3.0;
-                sigma += adaptive_pair(v1, v3 + 3 * b3, P.reclat_g) / 3.0;
-                sigma += adaptive_pair(v2 + 3 * b2, v3 + 3 * b3, P.reclat_g) / 3.0;
-                sigma += P.thresh_sigma;
-                invsig = 1.0 / sigma;
+                sigma = (float)(adaptive_pair(v1, v2 + 3 * b2, P.reclat_g) / 3.0 +
+                                adaptive_pair(v1, v3 + 3 * b3, P.reclat_g) / 3.0 +
+                                adaptive_pair(v2 + 3 * b2, v3 + 3 * b3, P.reclat_g) / 3.0 + P.thresh_sigma);
             }
-            const double win8 = 8.0 * sigma, h = 0.5 * invsig * invsig, cg = kSqrt2PiInv * invsig;
-            const double *tab = P.exp2tab;
-            double d0, d1;
-            dirac3(live, o1, o2, o3, win8, h, cg, tab, d0, d1);
-            if (!nonzero(d0) && !nonzero(d1)) continue;
-            // (n2 - n3) d0 + (n2 + n3 + 1) d1, forming only the terms whose weight is non-zero
-            // (usually one: a mode triplet rarely sits in a window of both kinds)
-            const double n2 = be2[b2], n3 = be3[b3];
-            double occ = 0.0;
-            if (nonzero(d0)) occ = (n2 - n3) * d0;
-            if (nonzero(d1)) occ = fma(n2 + n3 + 1.0, d1, occ);
+            const float invsig = 1.0f / sigma;
+            const float win8 = 8.0f * sigma, h = 0.5f * invsig * invsig, cg = kSqrt2PiInvF * invsig;
+            float gs[4] = {0.f, 0.f, 0.f, 0.f};
+            while (live) {
+                const int j = __ffs(live) - 1;
+                live &= live - 1;
+                // Gaussian j centred at (-om2+om3, om2-om3, om2+om3, -om2-om3), get_dirac's order
+                const double m2 = (j == 1 || j == 2) ? o2 : -o2;
+                const double m3 = (j == 0 || j == 2) ? o3 : -o3;
+                const float dx = (float)(o1 - (m2 + m3));
+                const float gj = fabsf(dx) > win8 ? 0.f : expf(-dx * dx * h) * cg;
+                gs[0] = j == 0 ? gj : gs[0];
+                gs[1] = j == 1 ? gj : gs[1];
+                gs[2] = j == 2 ? gj : gs[2];
+                gs[3] = j == 3 ? gj : gs[3];
+            }
+            const float d0 = gs[0] - gs[1], d1 = gs[2] - gs[3];
+            if (d0 == 0.f && d1 == 0.f) continue;
+            const float n2 = c2[b2], n3 = c3[b3];
+            const float occ = (n2 - n3) * d0 + (n2 + n3 + 1.0f) * d1;
             if (ADJ) {
-                F[e] = fadj * occ;
+                F[e] = fadj * (double)occ;
                 continue;
             }
             const float2 ps = psi[b2 * n + b3];
-            // |Psi|^2 of the FP32 contraction result in FP32 (one conversion instead of two
-            // plus two FP64 operations); the weights and sums stay FP64
-            const double p2 = (double)fmaf(ps.x, ps.x, ps.y * ps.y);
-            F[e] = (pw * p2) * occ;
+            F[e] = (double)(pwf * fmaf(ps.x, ps.x, ps.y * ps.y) * occ);
         }
         __syncthreads();
         if (ADJ) {

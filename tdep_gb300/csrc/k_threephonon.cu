@@ -136,7 +136,7 @@ __host__ __device__ inline Layout make_layout(int n, int cs, bool adj = false) {
     L.v3 = o; o += 3 * dn;
     L.wrow = o; o += dn;
     L.r2 = o; o += align16(sizeof(double) * n2);
-    L.f32 = o; o += align16(sizeof(float) * n * 6);            // om1..3, s1..3 in FP32
+    L.f32 = o; o += align16(sizeof(float) * n * 12);           // om1..3, s1..3, om lo parts, be2, be3, wrow in FP32
     L.masks = o; o += align16(sizeof(uint32_t) * (3 * n + 2 + 2 * n2));  // m12, m13, m23, z2, z3, row/col bits
     // E1..E3 and the phase chunk are dead once Psi is formed: the survivor queue reuses them.
     const size_t ez = align16(cs * n2);
@@ -223,6 +223,8 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
     S.s1 = s1; S.s2 = s2; S.s3 = s3; S.v1 = v1; S.v2 = v2; S.v3 = v3; S.wrow = wrow;
     S.R2 = R2; S.R3 = (double *)B; S.F = (double *)A;
     S.fo1 = fo1; S.fo2 = fo2; S.fo3 = fo3; S.fs1 = fs1; S.fs2 = fs2; S.fs3 = fs3;
+    S.fl1 = fs3 + N; S.fl2 = fs3 + 2 * N; S.fl3 = fs3 + 3 * N; S.fb2 = fs3 + 4 * N; S.fb3 = fs3 + 5 * N;
+    S.fw1 = fs3 + 6 * N;
     S.m12 = m12; S.m13 = m13; S.m23 = m23; S.zmask = zmask; S.rowbits = rowbits; S.colbits = colbits;
     S.Q = Q; S.rowid = rowid; S.red = red; S.wsum = wsum;
     const int tid = threadIdx.x, bd = blockDim.x;

@@ -91,7 +91,7 @@ __host__ __device__ inline TcLayout tc_layout(int n, int nt) {
     L.psq = o; o += tc_al(sizeof(float) * n3);  // |Psi|^2, then the row and column sums (2 n^2 doubles)
     L.om = o; o += 9 * tc_al(sizeof(double) * n) + tc_al(sizeof(double) * n);  // om1..3 inv1 be2 be3 s1..3, wrow
     L.v = o; o += 3 * tc_al(sizeof(double) * 3 * n);
-    L.f32 = o; o += tc_al(sizeof(float) * 6 * n);
+    L.f32 = o; o += tc_al(sizeof(float) * 12 * n);
     L.masks = o; o += tc_al(sizeof(uint32_t) * (3 * n + 2 + 2 * n2));
     L.rowid = o; o += tc_al(sizeof(int) * n);
     L.red = o; o += tc_al(sizeof(int2) * kMaxRed);
@@ -213,6 +213,8 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a)
         S.v1 = v; S.v2 = v + dv; S.v3 = v + 2 * dv;
         float *f = (float *)(smem + L.f32);
         S.fo1 = f; S.fo2 = f + N; S.fo3 = f + 2 * N; S.fs1 = f + 3 * N; S.fs2 = f + 4 * N; S.fs3 = f + 5 * N;
+        S.fl1 = f + 6 * N; S.fl2 = f + 7 * N; S.fl3 = f + 8 * N; S.fb2 = f + 9 * N; S.fb3 = f + 10 * N;
+        S.fw1 = f + 11 * N;
         uint32_t *mk = (uint32_t *)(smem + L.masks);
         S.m12 = mk; S.m13 = mk + N; S.m23 = mk + 2 * N; S.zmask = mk + 3 * N;
         S.rowbits = S.zmask + 2; S.colbits = S.rowbits + N2;
@@ -247,8 +249,12 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a)
     uint32_t e_ph = 0, m_ph = 0;
     bool ok = true;
 
+    // the next q-triplet's record is loaded one iteration ahead
+    TripletRec rec_next;
+    if ((int)blockIdx.x < a.n_trip) rec_next = a.trip[blockIdx.x];
     for (int t = blockIdx.x; t < a.n_trip && ok; t += gridDim.x) {
-        const TripletRec rec = a.trip[t];
+        const TripletRec rec = rec_next;
+        if (t + (int)gridDim.x < a.n_trip) rec_next = a.trip[t + gridDim.x];
         const int f1 = m.irr_full[rec.q1];
         const int q2 = rec.q2, q3 = rec.q3;
         const int i2 = m.full_irr[q2], i3 = m.full_irr[q3];
@@ -384,7 +390,10 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a)
         int nq = 0;
         const int off = block_exclusive_scan(nsurv, S.wsum, nq);  // contains barriers: the operands are dead
         if (mine && nsurv) k3_enqueue<N>(S, b1 * N + b2, off, live_lo, live_hi, live_x);
-        for (int i = tid; i < N3; i += kTcThreads) S.F[i] = 0.0;
+        // the forward pass reads F only where the row and column bits are set (entries written
+        // by this q-triplet's survivors); the adjoint reads all of it
+        if constexpr (ADJ)
+            for (int i = tid; i < N3; i += kTcThreads) S.F[i] = 0.0;
         __syncthreads();
         if constexpr (!ADJ) {
             k3_survivors_f32<N>(S, P, nq, (float)perm, [&](int idx) -> float { return psq[idx]; });
