@@ -4,6 +4,8 @@
 #include <algorithm>
 #include <fstream>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <map>
@@ -117,6 +119,48 @@ bool getline_nonempty(std::istream &is, std::string &line) {
     }
     return false;
 }
+
+// A text file in memory, handed out line by line (the force-constant files run to tens of
+// thousands of lines; a stream, a string per line and a library conversion per number made
+// them the slowest part of a problem load).
+class TextFile {
+  public:
+    bool open(const std::string &path) {
+        std::FILE *f = std::fopen(path.c_str(), "rb");
+        if (!f) return false;
+        bool ok = std::fseek(f, 0, SEEK_END) == 0;
+        const long n = ok ? std::ftell(f) : -1;
+        ok = n >= 0 && std::fseek(f, 0, SEEK_SET) == 0;
+        if (ok) {
+            buf_.assign((size_t)n + 1, '\0');
+            ok = n == 0 || std::fread(buf_.data(), 1, (size_t)n, f) == (size_t)n;
+        }
+        std::fclose(f);
+        pos_ = 0;
+        return ok;
+    }
+    // The next line with a non-blank character (its start; the line ends at a line break or
+    // at the terminating NUL); false at the end of the file.
+    bool next(const char *&line) {
+        const size_t n = buf_.size() - 1;
+        while (pos_ < n) {
+            const char *s = buf_.data() + pos_;
+            const char *nl = static_cast<const char *>(std::memchr(s, '\n', n - pos_));
+            const char *t = nl ? nl : buf_.data() + n;
+            pos_ = (size_t)(t - buf_.data()) + (nl ? 1 : 0);
+            for (const char *q = s; q < t; ++q)
+                if (*q != ' ' && *q != '\t' && *q != '\r') {
+                    line = s;
+                    return true;
+                }
+        }
+        return false;
+    }
+
+  private:
+    std::vector<char> buf_;
+    size_t pos_ = 0;
+};
 
 }  // namespace
 
@@ -312,17 +356,146 @@ int find_symmetry(Crystal &c) {
     return kOk;
 }
 
+bool parse_real(const char *p, const char **end, double *x) {
+    static const double kPow10[23] = {1e0,  1e1,  1e2,  1e3,  1e4,  1e5,  1e6,  1e7,  1e8,  1e9,  1e10, 1e11,
+                                      1e12, 1e13, 1e14, 1e15, 1e16, 1e17, 1e18, 1e19, 1e20, 1e21, 1e22};
+    static const uint64_t kPow10u[19] = {1ull,
+                                         10ull,
+                                         100ull,
+                                         1000ull,
+                                         10000ull,
+                                         100000ull,
+                                         1000000ull,
+                                         10000000ull,
+                                         100000000ull,
+                                         1000000000ull,
+                                         10000000000ull,
+                                         100000000000ull,
+                                         1000000000000ull,
+                                         10000000000000ull,
+                                         100000000000000ull,
+                                         1000000000000000ull,
+                                         10000000000000000ull,
+                                         100000000000000000ull,
+                                         1000000000000000000ull};
+    const char *s = p;
+    while (*s == ' ' || *s == '\t') ++s;
+    const char *start = s;
+    bool neg = false;
+    if (*s == '+' || *s == '-') {
+        neg = *s == '-';
+        ++s;
+    }
+    // m: up to 19 significant digits, value m 10^e10; tz: trailing zeros of m
+    uint64_t m = 0;
+    int e10 = 0, nd = 0, tz = 0;
+    bool any = false, exact = !(s[0] == '0' && (s[1] == 'x' || s[1] == 'X'));  // hexadecimal: strtod
+    for (; exact && *s >= '0' && *s <= '9'; ++s) {
+        any = true;
+        const int d = *s - '0';
+        if (nd < 19) {
+            m = m * 10 + (uint64_t)d;
+            if (m) ++nd;
+            tz = d ? 0 : tz + 1;
+        } else {
+            ++e10;
+            if (d) exact = false;
+        }
+    }
+    if (*s == '.') {
+        ++s;
+        for (; *s >= '0' && *s <= '9'; ++s) {
+            any = true;
+            const int d = *s - '0';
+            if (nd < 19) {
+                m = m * 10 + (uint64_t)d;
+                if (m) ++nd;
+                tz = d ? 0 : tz + 1;
+                --e10;
+            } else if (d) {
+                exact = false;
+            }
+        }
+    }
+    if (any && (*s == 'e' || *s == 'E')) {
+        const char *q = s + 1;
+        bool en = false;
+        if (*q == '+' || *q == '-') {
+            en = *q == '-';
+            ++q;
+        }
+        if (*q >= '0' && *q <= '9') {
+            int ev = 0;
+            for (; *q >= '0' && *q <= '9'; ++q)
+                if (ev < 100000) ev = ev * 10 + (*q - '0');
+            e10 += en ? -ev : ev;
+            s = q;
+        }
+    }
+    if (any && exact) {
+        if (m == 0) {
+            *x = neg ? -0.0 : 0.0;
+            *end = s;
+            return true;
+        }
+        if (tz > 0) {
+            m /= kPow10u[tz];
+            e10 += tz;
+        }
+        if (m <= (uint64_t(1) << 53) && e10 >= -22 && e10 <= 22) {
+            const double v = (double)m;
+            *x = e10 < 0 ? v / kPow10[-e10] : v * kPow10[e10];
+            if (neg) *x = -*x;
+            *end = s;
+            return true;
+        }
+    }
+    char *q = nullptr;
+    *x = std::strtod(start, &q);
+    *end = q;
+    return q != start;
+}
+
+namespace {
+// The first integer / the first k reals of the next non-empty line, parsed in place. 0 when
+// the line is missing or does not start with the numbers.
+int read_int_line(TextFile &f, int &x) {
+    const char *p = nullptr;
+    if (!f.next(p)) return 0;
+    char *end = nullptr;
+    const long v = std::strtol(p, &end, 10);
+    if (end == p) return 0;
+    x = (int)v;
+    return 1;
+}
+int read_reals_line(TextFile &f, int k, double *x) {
+    const char *p = nullptr;
+    if (!f.next(p)) return 0;
+    for (int i = 0; i < k; ++i) {
+        const char *end = nullptr;
+        if (!parse_real(p, &end, x + i)) return 0;
+        p = end;
+    }
+    return 1;
+}
+int read_vec_line(TextFile &f, double *x) { return read_reals_line(f, 3, x); }
+// A force-constant lattice vector must be integer in fractional coordinates.
+int to_lattice(const double *x, int32_t *out) {
+    for (int i = 0; i < 3; ++i) {
+        const double r = anint(x[i]);
+        if (std::fabs(x[i] - r) > 1e-6) return 0;
+        out[i] = (int32_t)r;
+    }
+    return 1;
+}
+}  // namespace
+
 int read_fc2(const std::string &path, const Crystal &c, FC2 &fc) {
-    std::ifstream f(path);
-    if (!f) return set_error(kErrIo, "cannot open " + path);
-    std::string line;
+    TextFile f;
+    if (!f.open(path)) return set_error(kErrIo, "cannot open " + path);
     auto first_tokens = [&](int k, std::vector<double> &out) -> bool {
-        if (!getline_nonempty(f, line)) return false;
-        auto t = split_ws(line);
-        if ((int)t.size() < k) return false;
         out.resize(k);
-        for (int i = 0; i < k; ++i) out[i] = std::stod(t[i]);
-        return true;
+        return read_reals_line(f, k, out.data()) != 0;
     };
     std::vector<double> v;
     if (!first_tokens(1, v)) return set_error(kErrIo, "truncated " + path);
@@ -457,52 +630,15 @@ int read_fc2(const std::string &path, const Crystal &c, FC2 &fc) {
     return kOk;
 }
 
-namespace {
-// The first integer / the first three reals of the next non-empty line, parsed in place
-// (strtol / strtod: a string stream and a token vector per line made the force-constant
-// files the slowest part of a problem load). 0 when the line is missing or does not start
-// with the numbers.
-int read_int_line(std::istream &f, int &x) {
-    std::string line;
-    if (!getline_nonempty(f, line)) return 0;
-    const char *p = line.c_str();
-    char *end = nullptr;
-    const long v = std::strtol(p, &end, 10);
-    if (end == p) return 0;
-    x = (int)v;
-    return 1;
-}
-int read_vec_line(std::istream &f, double *x) {
-    std::string line;
-    if (!getline_nonempty(f, line)) return 0;
-    const char *p = line.c_str();
-    for (int i = 0; i < 3; ++i) {
-        char *end = nullptr;
-        x[i] = std::strtod(p, &end);
-        if (end == p) return 0;
-        p = end;
-    }
-    return 1;
-}
-// A force-constant lattice vector must be integer in fractional coordinates.
-int to_lattice(const double *x, int32_t *out) {
-    for (int i = 0; i < 3; ++i) {
-        const double r = anint(x[i]);
-        if (std::fabs(x[i] - r) > 1e-6) return 0;
-        out[i] = (int32_t)r;
-    }
-    return 1;
-}
-}  // namespace
 
 int read_fc3(const std::string &path, const Crystal &c, FC3 &fc) {
-    std::ifstream f(path);
-    if (!f) return set_error(kErrIo, "cannot open " + path);
+    TextFile f;
+    if (!f.open(path)) return set_error(kErrIo, "cannot open " + path);
     int na = 0;
     double cut[3];
     if (!read_int_line(f, na)) return set_error(kErrIo, "truncated " + path);
-    std::string line;
-    if (!getline_nonempty(f, line)) return set_error(kErrIo, "truncated " + path);
+    const char *line = nullptr;
+    if (!f.next(line)) return set_error(kErrIo, "truncated " + path);
     (void)cut;
     if (na != c.na) return set_error(kErrIo, "different number of atoms in \"" + path + "\" and the structure");
     fc.atoms.clear();
@@ -548,12 +684,12 @@ int read_fc3(const std::string &path, const Crystal &c, FC3 &fc) {
 }
 
 int read_fc4(const std::string &path, const Crystal &c, FC4 &fc) {
-    std::ifstream f(path);
-    if (!f) return set_error(kErrIo, "cannot open " + path);
+    TextFile f;
+    if (!f.open(path)) return set_error(kErrIo, "cannot open " + path);
     int na = 0;
     if (!read_int_line(f, na)) return set_error(kErrIo, "truncated " + path);
-    std::string line;
-    if (!getline_nonempty(f, line)) return set_error(kErrIo, "truncated " + path);
+    const char *line = nullptr;
+    if (!f.next(line)) return set_error(kErrIo, "truncated " + path);
     if (na != c.na) return set_error(kErrIo, "different number of atoms in \"" + path + "\" and the structure");
     fc.atoms.clear();
     fc.lv.clear();

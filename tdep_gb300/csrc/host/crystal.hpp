@@ -66,6 +66,11 @@ struct FC2 {
 // the only one the reference accepts) it also reads the dielectric tensor, the Ewald
 // parameter and the Born charges, and sets up the long-range term
 // (type_forceconstant_secondorder_loto.f90:10-99).
+// The decimal real at p (leading blanks skipped; *end after it), correctly rounded as
+// strtod: digits and power of ten exact in one FP64 operation (Clinger's fast path: at most
+// 2^53 after dropping trailing zeros, 10^-22..10^22), otherwise strtod. False when p holds
+// no number.
+bool parse_real(const char *p, const char **end, double *x);
 int read_fc2(const std::string &path, const Crystal &c, FC2 &fc);
 
 // Long-range dipole-dipole dynamical matrix, reciprocal-space sum only

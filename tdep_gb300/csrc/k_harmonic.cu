@@ -14,16 +14,20 @@
 //                      lo_eigenvector_transformation_matrix (type_symmetryoperation.f90:243-290)
 //
 // Every step is the host stage's (host/phonons.cpp) operation for operation, in FP64, so the
-// two agree to rounding; the device's sin, cos, exp and sqrt differ from the host library's
-// by an ulp or so. Kernels:
+// two agree to rounding (the device's sin, cos, exp and sqrt differ from the host library's
+// by an ulp or so), except the order of the Jacobi rotations up to 24 modes (parallel
+// ordering; the same rotations, the eigenpairs agree to rounding, degenerate subspaces up to
+// their basis, which the velocity gauge then fixes). Kernels:
 //   k_longrange  one CTA per irreducible point: the Ewald pair sums over the reciprocal
 //                vectors (chunks of per-vector scalars in shared memory), then the Hermitian
 //                completion, the Born charges on both sides and the on-site term;
 //   k_dynmat     one CTA per irreducible point, one thread per matrix element: the pairs of
 //                its atom pair in file order (the host's summation order), the long-range
 //                blocks and the non-analytic term, with masses;
-//   k_eigen      one warp per irreducible point, matrices in global memory (cached): Jacobi
-//                sweeps with every lane deriving the same rotation, sorting, the Gamma acoustic
+//   k_eigen      one warp per irreducible point (one per CTA), up to 24 modes the matrices in
+//                shared memory and parallel-order Jacobi sweeps (one lane per rotation of a
+//                step), beyond that global memory and cyclic sweeps with every lane deriving
+//                the same rotation; sorting, the Gamma acoustic
 //                modes, the velocity-operator gauge of degenerate subspaces, Hellmann-Feynman
 //                velocities with the subspace mean, degeneracy tables;
 //   k_unfold     one thread per (mesh point, mode, atom).
@@ -328,6 +332,120 @@ __device__ bool warp_jacobi(int n, double2 *A, double2 *V, double *w) {
     return conv;
 }
 
+// The same eigenproblem for n <= 32 with A and V in shared memory, by parallel ordering:
+// each step rotates m/2 disjoint pairs (p, q) of the round-robin tournament over m = n
+// rounded up to even indices (an index >= n pairs with nothing), one lane deriving each
+// pair's rotation from the same snapshot of A (a pair's 2 x 2 block is touched by no other
+// pair of the step), then A <- A J, A <- J^H A and V <- V J for all pairs at once; m - 1
+// steps make a sweep. GB300 issues FP64 at 2 lanes per clock per SM, so a rotation derived
+// by every lane of the warp (the cyclic form above) costs 32 times its arithmetic; here 16
+// rotations share one such derivation. The rotations are the cyclic form's, applied in
+// another order: the eigenpairs agree to rounding (within degenerate subspaces the basis
+// may differ; the velocity-operator gauge fixes it afterwards). rot: 16 x 4 doubles of
+// shared memory. Returns false when 100 sweeps do not converge.
+__device__ bool warp_jacobi_par(int n, double2 *A, double2 *V, double *w, double *rot) {
+    const int lane = threadIdx.x & 31;
+    const int m = (n + 1) & ~1, half = m / 2;
+    for (int k = lane; k < n * n; k += 32) V[k] = make_double2((k % n) == (k / n) ? 1.0 : 0.0, 0.0);
+    double scale = 0.0;
+    for (int k = lane; k < n * n; k += 32) scale += cnorm(A[k]);
+    for (int o = 16; o > 0; o >>= 1) scale += __shfl_xor_sync(0xffffffffu, scale, o);
+    __syncwarp();
+    if (scale == 0.0) {
+        for (int k = lane; k < n; k += 32) w[k] = 0.0;
+        __syncwarp();
+        return true;
+    }
+    // pair i of step s (circle method): slot 0 stays, slots 1..m-1 rotate by s
+    auto pair_of = [&](int s, int i, int &p, int &q) {
+        const int a = i == 0 ? 0 : 1 + (i - 1 + s) % (m - 1);
+        const int b = 1 + (m - 1 - i - 1 + s) % (m - 1);
+        p = a < b ? a : b;
+        q = a < b ? b : a;
+    };
+    bool conv = false;
+    for (int sweep = 0; sweep < 100; ++sweep) {
+        double off = 0.0;
+        for (int k = lane; k < n * n; k += 32)
+            if ((k % n) != (k / n)) off += cnorm(A[k]);
+        for (int o = 16; o > 0; o >>= 1) off += __shfl_xor_sync(0xffffffffu, off, o);
+        if (off <= 1e-30 * scale) {
+            conv = true;
+            break;
+        }
+        for (int st = 0; st < m - 1; ++st) {
+            __syncwarp();
+            if (lane < half) {
+                int p, q;
+                pair_of(st, lane, p, q);
+                double cs = 1.0, sn = 0.0, ux = 1.0, uy = 0.0;
+                if (q < n) {
+                    const double2 g = A[p + (size_t)n * q];
+                    const double ag = hypot(g.x, g.y);
+                    if (ag > 1e-300) {
+                        ux = g.x / ag;
+                        uy = g.y / ag;
+                        const double app = A[p + (size_t)n * p].x, aqq = A[q + (size_t)n * q].x;
+                        const double tau = (aqq - app) / (2.0 * ag);
+                        const double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+                        cs = 1.0 / sqrt(1.0 + t * t);
+                        sn = t * cs;
+                    }
+                }
+                rot[4 * lane] = cs;
+                rot[4 * lane + 1] = sn;
+                rot[4 * lane + 2] = ux;
+                rot[4 * lane + 3] = uy;
+            }
+            __syncwarp();
+            for (int task = lane; task < half * n; task += 32) {  // A <- A J, V <- V J
+                const int i = task / n, k = task % n;
+                int p, q;
+                pair_of(st, i, p, q);
+                if (q >= n) continue;
+                const double cs = rot[4 * i], sn = rot[4 * i + 1];
+                const double2 u = make_double2(rot[4 * i + 2], rot[4 * i + 3]);
+                const double2 jqp = cscale(cconj(u), -sn), jqq = cscale(cconj(u), cs);
+                const double2 akp = A[k + (size_t)n * p], akq = A[k + (size_t)n * q];
+                A[k + (size_t)n * p] = cadd(cscale(akp, cs), cmul(akq, jqp));
+                A[k + (size_t)n * q] = cadd(cscale(akp, sn), cmul(akq, jqq));
+                const double2 vkp = V[k + (size_t)n * p], vkq = V[k + (size_t)n * q];
+                V[k + (size_t)n * p] = cadd(cscale(vkp, cs), cmul(vkq, jqp));
+                V[k + (size_t)n * q] = cadd(cscale(vkp, sn), cmul(vkq, jqq));
+            }
+            __syncwarp();
+            for (int task = lane; task < half * n; task += 32) {  // A <- J^H A
+                const int i = task / n, k = task % n;
+                int p, q;
+                pair_of(st, i, p, q);
+                if (q >= n) continue;
+                const double cs = rot[4 * i], sn = rot[4 * i + 1];
+                const double2 u = make_double2(rot[4 * i + 2], rot[4 * i + 3]);
+                const double2 jqp = cscale(cconj(u), -sn), jqq = cscale(cconj(u), cs);
+                const double2 apk = A[p + (size_t)n * k], aqk = A[q + (size_t)n * k];
+                A[p + (size_t)n * k] = cadd(cscale(apk, cs), cmul(cconj(jqp), aqk));
+                A[q + (size_t)n * k] = cadd(cscale(apk, sn), cmul(cconj(jqq), aqk));
+            }
+            __syncwarp();
+            if (lane < half) {
+                int p, q;
+                pair_of(st, lane, p, q);
+                if (q < n) {
+                    A[p + (size_t)n * q] = make_double2(0.0, 0.0);
+                    A[q + (size_t)n * p] = make_double2(0.0, 0.0);
+                    A[p + (size_t)n * p].y = 0.0;
+                    A[q + (size_t)n * q].y = 0.0;
+                }
+            }
+        }
+        __syncwarp();
+    }
+    __syncwarp();
+    for (int k = lane; k < n; k += 32) w[k] = A[k + (size_t)n * k].x;
+    __syncwarp();
+    return conv;
+}
+
 // Stable sort of n < 128 keys into ord (by lane 0; the others wait at the caller's syncwarp).
 __device__ void stable_order(int n, const double *key, int *ord) {
     for (int i = 0; i < n; ++i) ord[i] = i;
@@ -342,13 +460,21 @@ __device__ void stable_order(int n, const double *key, int *ord) {
     }
 }
 
-constexpr int kEigWarps = 4;
+constexpr int kEigWarps = 1;  // one warp per CTA: the points spread over the SMs, each with its own FP64 pipe
 constexpr int kMaxModes = 128;
+
+// Up to this many modes the matrices of a point (A, V, E) live in shared memory: every
+// Jacobi rotation stores what the next one loads, and through global memory each of those
+// round trips went to L2.
+constexpr int kEigSmemModes = 24;
+inline size_t eigen_smem_bytes(int n) { return n <= kEigSmemModes ? (size_t)3 * n * n * sizeof(double2) : 0; }
 
 __global__ void __launch_bounds__(32 * kEigWarps) k_eigen(HarmDev h) {
     __shared__ int s_ord[kEigWarps][kMaxModes];
     __shared__ double s_key[kEigWarps][kMaxModes];
     __shared__ int s_sub[kEigWarps][kMaxModes];
+    __shared__ double s_rot[kEigWarps][64];
+    extern __shared__ double2 s_mat[];  // kEigWarps == 1: A, V, E of the CTA's point
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int iq = blockIdx.x * kEigWarps + wid;
     if (iq >= h.nirr) return;
@@ -356,12 +482,19 @@ __global__ void __launch_bounds__(32 * kEigWarps) k_eigen(HarmDev h) {
     int *ord = s_ord[wid];
     double *key = s_key[wid];
     int *sub = s_sub[wid];
-    double2 *A = h.D + (size_t)iq * n * n;
-    double2 *V = h.V + (size_t)iq * n * n;
+    const bool local = kEigWarps == 1 && n <= kEigSmemModes;
+    double2 *Ag = h.D + (size_t)iq * n * n;
+    double2 *Eg = h.egv + (size_t)iq * n * n;  // E[b * n + r]
+    double2 *A = local ? s_mat : Ag;
+    double2 *V = local ? s_mat + n * n : h.V + (size_t)iq * n * n;
+    double2 *E = local ? s_mat + 2 * n * n : Eg;
     const double2 *G = h.Gd + (size_t)iq * 3 * n * n;
     double *w = h.w + (size_t)iq * n;
     double *om = h.om + (size_t)iq * n;
-    double2 *E = h.egv + (size_t)iq * n * n;  // E[b * n + r]
+    if (local) {
+        for (int k = lane; k < n * n; k += 32) A[k] = Ag[k];
+        __syncwarp();
+    }
     // Hermitise against rounding
     for (int k = lane; k < n * n; k += 32) {
         const int i = k % n, j = k / n;
@@ -373,7 +506,7 @@ __global__ void __launch_bounds__(32 * kEigWarps) k_eigen(HarmDev h) {
         }
     }
     __syncwarp();
-    if (!warp_jacobi(n, A, V, w)) {
+    if (!(local ? warp_jacobi_par(n, A, V, w, s_rot[wid]) : warp_jacobi(n, A, V, w))) {
         if (lane == 0) atomicExch(h.status, (int32_t)kDevLinalg);
         return;
     }
@@ -490,6 +623,9 @@ __global__ void __launch_bounds__(32 * kEigWarps) k_eigen(HarmDev h) {
         for (int b2 = l; b2 < n; ++b2) dm[b2] = 0;
         h.degen[(size_t)iq * n + b] = l;
     }
+    if (local) {
+        for (int k = lane; k < n * n; k += 32) Eg[k] = E[k];
+    }
 }
 
 struct UnfoldDev {
@@ -576,6 +712,7 @@ int build_phonons_device(const Crystal &c, const FC2 &fc, const QMesh &qp, int d
                          std::vector<double> &irr_dyngrad) {
     const int na = c.na, nb = 3 * na, ni = qp.n_irr, nf = qp.n_full, nop = (int)c.ops.size();
     if (nb > kMaxModes) return set_error(kErrParam, "device harmonic stage: at most 128 modes");
+    PhaseTimer pt("harmonic stage (device)");
     if (cudaSetDevice(device) != cudaSuccess) {
         cudaGetLastError();
         return set_error(kErrDevice, "device harmonic stage: cannot select the device");
@@ -607,6 +744,7 @@ int build_phonons_device(const Crystal &c, const FC2 &fc, const QMesh &qp, int d
     for (int q = 0; q < nf; ++q)
         for (int d = 0; d < 3; ++d) qf[(size_t)q * 3 + d] = qp.q_full[q][d];
 
+    pt.mark("host tables");
     const bool polar = fc.polar == 3;
     const int np2 = na * (na + 1) / 2;
     DBuf<int32_t> d_pptr, d_status, d_deg, d_dm, d_degf, d_dmf, d_fmap, d_fi, d_fo, d_if;
@@ -645,6 +783,7 @@ int build_phonons_device(const Crystal &c, const FC2 &fc, const QMesh &qp, int d
     chk(d_status.alloc(1));
     if (e != cudaSuccess) return set_error(kErrDevice, std::string("device harmonic stage: ") + cudaGetErrorString(e));
     chk(cudaMemset(d_status.p, 0, sizeof(int32_t)));
+    pt.mark("allocations and uploads");
     HarmDev h;
     std::memset(&h, 0, sizeof h);
     h.na = na;
@@ -686,12 +825,13 @@ int build_phonons_device(const Crystal &c, const FC2 &fc, const QMesh &qp, int d
     // the gradient at the irreducible points is an output (off-diagonal kappa)
     std::vector<double2> gd((size_t)ni * 3 * nb * nb);
     chk(cudaMemcpy(gd.data(), d_Gd.p, sizeof(double2) * gd.size(), cudaMemcpyDeviceToHost));
-    k_eigen<<<(ni + kEigWarps - 1) / kEigWarps, 32 * kEigWarps>>>(h);
+    k_eigen<<<(ni + kEigWarps - 1) / kEigWarps, 32 * kEigWarps, eigen_smem_bytes(nb)>>>(h);
     chk(cudaGetLastError());
     int32_t dst = 0;
     chk(cudaMemcpy(&dst, d_status.p, sizeof(int32_t), cudaMemcpyDeviceToHost));
     if (e != cudaSuccess) return set_error(kErrDevice, std::string("device harmonic stage: ") + cudaGetErrorString(e));
     if (dst) return set_error(kErrLinalg, "device harmonic stage: Jacobi eigensolver did not converge");
+    pt.mark("D(q), dD/dq, eigenvectors");
     irr_dyngrad.assign((size_t)ni * 3 * nb * nb * 2, 0.0);
     std::memcpy(irr_dyngrad.data(), gd.data(), sizeof(double) * irr_dyngrad.size());
     // unfold onto the mesh
@@ -732,9 +872,12 @@ int build_phonons_device(const Crystal &c, const FC2 &fc, const QMesh &qp, int d
     u.egv = d_egvf.p;
     u.deg = d_degf.p;
     u.dm = d_dmf.p;
+    pt.mark("unfold uploads");
     const int64_t total = (int64_t)nf * nb * na;
     k_unfold<<<(unsigned)((total + 255) / 256), 256>>>(u);
     chk(cudaGetLastError());
+    chk(cudaStreamSynchronize(0));
+    pt.mark("unfold");
     ph.n_mode = nb;
     ph.omega.resize((size_t)nf * nb);
     ph.vel.resize((size_t)nf * nb * 3);
@@ -747,6 +890,7 @@ int build_phonons_device(const Crystal &c, const FC2 &fc, const QMesh &qp, int d
     chk(cudaMemcpy(ph.degen.data(), d_degf.p, sizeof(int32_t) * ph.degen.size(), cudaMemcpyDeviceToHost));
     chk(cudaMemcpy(ph.degen_mode.data(), d_dmf.p, sizeof(int32_t) * ph.degen_mode.size(), cudaMemcpyDeviceToHost));
     if (e != cudaSuccess) return set_error(kErrDevice, std::string("device harmonic stage: ") + cudaGetErrorString(e));
+    pt.mark("downloads");
     return kOk;
 }
 

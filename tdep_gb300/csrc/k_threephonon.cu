@@ -278,7 +278,49 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
             }
         }
         constexpr int PC = phase_chunk(N, sizeof(C));
-        for (int c0 = 0; c0 < fc.n; c0 += PC) {
+        bool planned = false;
+        if constexpr (sizeof(R) == 4) {
+            // FP32 with a pretransform plan (all phase factors at once; k_threephonon_tc.cu
+            // explains the plan): each thread's slots, 8 values and 8 words in flight, the
+            // sums in the triplets' order as below
+            if (a.plan_slots > 0) {
+                planned = true;
+                __syncthreads();
+                for (int i = tid; i < fc.n + 4; i += bd)
+                    ph[i] = i < fc.n ? phase3<C>(fc, m, gi2, gi3, i) : czero<C>();
+                __syncthreads();
+                const float4 *pm = a.plan_pm + tid;
+                const uint32_t *pw = a.plan_word + tid;
+                float ar = 0.f, ai = 0.f;
+#pragma unroll 1
+                for (int s0 = 0; s0 < a.plan_slots; s0 += 8) {
+                    float4 mv[8];
+                    uint32_t wd[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        mv[u] = __ldg(pm + (size_t)(s0 + u) * bd);
+                        wd[u] = __ldg(pw + (size_t)(s0 + u) * bd);
+                    }
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const C *pp = ph + (wd[u] & 0xffffu);
+                        const C p0 = pp[0], p1 = pp[1], p2 = pp[2], p3 = pp[3];
+                        ar = fmaf(mv[u].x, p0.x, ar); ai = fmaf(mv[u].x, p0.y, ai);
+                        ar = fmaf(mv[u].y, p1.x, ar); ai = fmaf(mv[u].y, p1.y, ai);
+                        ar = fmaf(mv[u].z, p2.x, ar); ai = fmaf(mv[u].z, p2.y, ai);
+                        ar = fmaf(mv[u].w, p3.x, ar); ai = fmaf(mv[u].w, p3.y, ai);
+                        const uint32_t oc = wd[u] >> 16;  // on an element's last slot: its index + 1
+                        if (oc) {
+                            A[oc - 1u].x = ar;
+                            A[oc - 1u].y = ai;
+                            ar = 0.f;
+                            ai = 0.f;
+                        }
+                    }
+                }
+            }
+        }
+        for (int c0 = 0; !planned && c0 < fc.n; c0 += PC) {
             const int cn = min(PC, fc.n - c0);
             __syncthreads();
             for (int i = tid; i < cn; i += bd) ph[i] = phase3<C>(fc, m, gi2, gi3, c0 + i);
@@ -635,6 +677,13 @@ cudaError_t launch_exp_neg_check(const double *t, int32_t n, double *out, const 
     if (n <= 0) return cudaSuccess;
     k_exp_neg_check<<<(n + 255) / 256, 256, 0, s>>>(t, n, out, tab);
     return cudaGetLastError();
+}
+
+int threephonon_threads(int n) { return threads_for(n); }
+
+bool threephonon_plan_fits(int n, int n_fc) {
+    // the plan path holds all phase factors (and 4 zero ones after them) in the phase region
+    return n >= 3 && n <= 16 && n_fc + 4 <= phase_chunk(n, (int)sizeof(float2));
 }
 
 size_t threephonon_smem_bytes(int n, int precision, int) {

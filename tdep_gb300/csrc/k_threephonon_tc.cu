@@ -302,11 +302,11 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a)
         // ---- pretransform into the stage-1 operand: rows (c, b), k = a (re) and 16 + a (im) ----
         // (the plan's slots of this thread: 8 loads of values and 8 of words in flight)
         {
-            const float4 *pm = a.tc_pm + tid;
-            const uint32_t *pw = a.tc_pword + tid;
+            const float4 *pm = a.plan_pm + tid;
+            const uint32_t *pw = a.plan_word + tid;
             float ar = 0.f, ai = 0.f;
 #pragma unroll 1
-            for (int s0 = 0; s0 < a.tc_slots; s0 += 8) {
+            for (int s0 = 0; s0 < a.plan_slots; s0 += 8) {
                 float4 mv[8];
                 uint32_t wd[8];
 #pragma unroll
@@ -550,7 +550,7 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a)
 
 // Values of the pretransform plan from the current FP32 force constants: slot word src =
 // first triplet | ijk << 16 | valid triplets << 21 (0 to 4; the rest of the 16 bytes zero).
-__global__ void k_tc_fill_plan(const uint32_t *src, int64_t n_slot, const float *mwm32, float4 *pm) {
+__global__ void k_fill_plan(const uint32_t *src, int64_t n_slot, const float *mwm32, float4 *pm) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_slot) return;
     const uint32_t w = src[i];
@@ -626,7 +626,7 @@ int threephonon_tc_max_per_sm(int n, int n_fc, int *api, int *count) {
 
 cudaError_t launch_threephonon_tc(const ThreePhArgs &a, int n_sm, int ctas_per_sm, cudaStream_t s) {
     if (a.n_trip <= 0) return cudaSuccess;
-    if (!a.tc_eimg || !a.tc_pm || !a.tc_pword || a.tc_slots < 8 || a.tc_slots % 8 != 0) return cudaErrorInvalidValue;
+    if (!a.tc_eimg || !a.plan_pm || !a.plan_word || a.plan_slots < 8 || a.plan_slots % 8 != 0) return cudaErrorInvalidValue;
     switch (a.mesh.n_mode) {
         case 9: return tc_launch_grid<9, false>(a, tc_grid<9, false>(a.fc.n, a.n_trip, n_sm, ctas_per_sm), s);
         case 12: return tc_launch_grid<12, false>(a, tc_grid<12, false>(a.fc.n, a.n_trip, n_sm, ctas_per_sm), s);
@@ -646,7 +646,7 @@ int threephonon_tc_adjoint_grid(int n, int n_sm, int n_trip, int n_fc) {
 
 cudaError_t launch_threephonon_tc_adjoint(const ThreePhArgs &a, int grid, cudaStream_t s) {
     if (a.n_trip <= 0) return cudaSuccess;
-    if (!a.tc_eimg || !a.tc_eimg_t || !a.tc_pm || !a.tc_pword || a.tc_slots < 8 || a.tc_slots % 8 != 0 || !a.lam ||
+    if (!a.tc_eimg || !a.tc_eimg_t || !a.plan_pm || !a.plan_word || a.plan_slots < 8 || a.plan_slots % 8 != 0 || !a.lam ||
         !a.mwm_bar)
         return cudaErrorInvalidValue;
     switch (a.mesh.n_mode) {
@@ -657,10 +657,11 @@ cudaError_t launch_threephonon_tc_adjoint(const ThreePhArgs &a, int grid, cudaSt
     }
 }
 
-int tc_pretransform_plan(int n, int n_blk, const int32_t *blk_ptr, std::vector<uint32_t> &word,
-                         std::vector<uint32_t> &src) {
+int pretransform_plan(int n, int n_blk, const int32_t *blk_ptr, int threads, bool tc_operand,
+                      std::vector<uint32_t> &word, std::vector<uint32_t> &src) {
     const int na = n / 3;
-    if (n % 3 != 0 || n > 16 || n_blk != na * na * na || blk_ptr[0] != 0) return 0;
+    if (n % 3 != 0 || n > 16 || n_blk != na * na * na || blk_ptr[0] != 0 || threads < 32 || threads % 32 != 0)
+        return 0;
     const int n_fc = blk_ptr[n_blk];
     if (n_fc < 0 || n_fc + 4 > 0xffff) return 0;
     // elements (block, ijk) with their slot counts, largest first (stable), each to the
@@ -671,8 +672,8 @@ int tc_pretransform_plan(int n, int n_blk, const int32_t *blk_ptr, std::vector<u
     std::stable_sort(blocks.begin(), blocks.end(), [&](int x, int y) { return slots_of(x) > slots_of(y); });
     using Load = std::pair<int, int>;  // (slots, thread)
     std::priority_queue<Load, std::vector<Load>, std::greater<Load>> heap;
-    for (int t = 0; t < kTcThreads; ++t) heap.push({0, t});
-    std::vector<std::vector<int>> mine(kTcThreads);  // element = 27 block + ijk
+    for (int t = 0; t < threads; ++t) heap.push({0, t});
+    std::vector<std::vector<int>> mine(threads);  // element = 27 block + ijk
     for (int b : blocks) {
         const int c = slots_of(b);
         if (c == 0) break;
@@ -689,20 +690,22 @@ int tc_pretransform_plan(int n, int n_blk, const int32_t *blk_ptr, std::vector<u
         heap.pop();
     }
     const int slots = std::max(8, (most + 7) / 8 * 8);
-    word.assign((size_t)slots * kTcThreads, 0u);
-    src.assign((size_t)slots * kTcThreads, 0u);
-    for (int t = 0; t < kTcThreads; ++t) {
+    word.assign((size_t)slots * threads, 0u);
+    src.assign((size_t)slots * threads, 0u);
+    for (int t = 0; t < threads; ++t) {
         int sl = 0;
         for (int e : mine[t]) {
             const int b = e / 27, ijk = e % 27;
             const int lo = blk_ptr[b], c = blk_ptr[b + 1] - lo;
             const int a1 = b / (na * na), a2 = (b / na) % na, a3 = b % na;
             const int pa = 3 * a1 + ijk % 3, pb = 3 * a2 + (ijk / 3) % 3, pcc = 3 * a3 + ijk / 9;
-            const uint32_t off = a_off_mn(16 * pcc + pb, pa);  // < 8192, even
+            // tensor-core operand: byte offset / 2 (< 4096); fused SIMT kernel: index of
+            // P(a, b, c) in its n^3 array (< 4096)
+            const uint32_t code = tc_operand ? a_off_mn(16 * pcc + pb, pa) / 2u : (uint32_t)((pa * n + pb) * n + pcc);
             for (int j = 0; j < c; j += 4) {
-                const size_t i = (size_t)sl * kTcThreads + t;
+                const size_t i = (size_t)sl * threads + t;
                 const uint32_t f = (uint32_t)(lo + j), nv = (uint32_t)std::min(4, c - j);
-                word[i] = f | (j + 4 >= c ? ((off / 2u + 1u) << 16) : 0u);
+                word[i] = f | (j + 4 >= c ? ((code + 1u) << 16) : 0u);
                 src[i] = f | ((uint32_t)ijk << 16) | (nv << 21);
                 ++sl;
             }
@@ -711,10 +714,11 @@ int tc_pretransform_plan(int n, int n_blk, const int32_t *blk_ptr, std::vector<u
     return slots;
 }
 
-cudaError_t launch_tc_fill_plan(const uint32_t *src, int slots, const float *mwm32, float4 *pm, cudaStream_t s) {
-    const int64_t n_slot = (int64_t)slots * kTcThreads;
+cudaError_t launch_fill_plan(const uint32_t *src, int slots, int threads, const float *mwm32, float4 *pm,
+                             cudaStream_t s) {
+    const int64_t n_slot = (int64_t)slots * threads;
     if (n_slot <= 0) return cudaErrorInvalidValue;
-    k_tc_fill_plan<<<(unsigned)((n_slot + 255) / 256), 256, 0, s>>>(src, n_slot, mwm32, pm);
+    k_fill_plan<<<(unsigned)((n_slot + 255) / 256), 256, 0, s>>>(src, n_slot, mwm32, pm);
     return cudaGetLastError();
 }
 

@@ -192,12 +192,15 @@ struct tdg_ctx {
     DevBuf<double> fc3_mwm, fc4_mwm;
     DevBuf<float> fc3_mwm32, fc4_mwm32;
     // tensor-core fused kernel (9-15 modes, mixed): eigenvector images built on first use;
-    // the pretransform plan's layout built with the force constants (tc_slots 0: no plan),
-    // its values refilled by every call (tdg_set_fc3 may change them)
+    // the pretransform plans' layouts (pretransform_plan) built with the force constants,
+    // one for the tensor-core kernel and one for the FP32 SIMT kernel (slots 0: no plan),
+    // their values refilled by every call (tdg_set_fc3 may change them)
     DevBuf<unsigned char> d_tc_eimg, d_tc_eimg_t;  // E and E^T images (the latter for the adjoint)
-    DevBuf<uint32_t> d_tc_pword, d_tc_psrc;
-    DevBuf<float4> d_tc_pm;
-    int tc_slots = 0;
+    struct Plan {
+        DevBuf<uint32_t> word, src;
+        DevBuf<float4> pm;
+        int slots = 0, threads = 0;
+    } tc_plan, simt_plan;
     bool tc_eimg_ready = false, tc_eimg_t_ready = false;
     int last_path = -1;  // 0 SIMT fused kernel, 1 tensor-core fused kernel, 2 large-cell batches
     // fused three-phonon launch of the last scattering call: grid, CTAs per SM used, the
@@ -279,6 +282,9 @@ struct tdg_ctx {
     std::vector<double> irr_dyngrad, atom_shift, q_full;
     std::vector<int32_t> op_fmap;
     DevBuf<double2> d_grad, d_odwork;
+    DevBuf<int2> d_od_items;
+    DevBuf<int32_t> d_od_itemptr;
+    int od_items = 0;
     DevBuf<double> d_shift, d_qfull, d_lwcv, d_odS, d_irr_weight;
     DevBuf<int32_t> d_fmap;
 
@@ -633,15 +639,18 @@ extern "C" int tdg_create(tdg_ctx **out, const tdg_problem *p, int device) {
         chk(launch_egv_scaled((int64_t)nm, c->n, c->d_egv.p, c->d_omega.p, c->d_egvs.p, c->d_egvs32.p, s));
     chk(c->d_disorder.upload(c->disorder.data(), c->disorder.size(), s));
     chk(c->fc3_blk.upload(blk_ptr3.data(), blk_ptr3.size(), s));
-    if (c->n == 9 || c->n == 12 || c->n == 15) {
+    auto make_plan = [&](tdg_ctx::Plan &pl, int threads, bool tc_operand) {
         std::vector<uint32_t> pword, psrc;
-        c->tc_slots = tc_pretransform_plan(c->n, na * na * na, blk_ptr3.data(), pword, psrc);
-        if (c->tc_slots > 0) {
-            chk(c->d_tc_pword.upload(pword.data(), pword.size(), s));
-            chk(c->d_tc_psrc.upload(psrc.data(), psrc.size(), s));
-            chk(c->d_tc_pm.alloc(pword.size()));
+        pl.threads = threads;
+        pl.slots = pretransform_plan(c->n, na * na * na, blk_ptr3.data(), threads, tc_operand, pword, psrc);
+        if (pl.slots > 0) {
+            chk(pl.word.upload(pword.data(), pword.size(), s));
+            chk(pl.src.upload(psrc.data(), psrc.size(), s));
+            chk(pl.pm.alloc(pword.size()));
         }
-    }
+    };
+    if (c->n == 9 || c->n == 12 || c->n == 15) make_plan(c->tc_plan, 256, true);
+    if (threephonon_plan_fits(c->n, (int)(blk_ptr3.back()))) make_plan(c->simt_plan, threephonon_threads(c->n), false);
     chk(c->fc3_abase.upload(abase3.data(), abase3.size(), s));
     chk(c->fc3_lv.upload(lv3.data(), lv3.size(), s));
     chk(c->fc3_mwm.upload(mwm3.data(), mwm3.size(), s));
@@ -1380,7 +1389,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
         c->last_ln = n > 18 || o->tensor_cores == 1;
         const char *tc_env = std::getenv("TDG_TC_SMALL");
         const bool use_tc = !c->last_ln && o->tensor_cores != 2 && !(tc_env && tc_env[0] == '0') &&
-                            threephonon_tc_supported(n, o->precision, c->n_fc3) && c->tc_slots > 0;
+                            threephonon_tc_supported(n, o->precision, c->n_fc3) && c->tc_plan.slots > 0;
         c->last_path = c->last_ln ? 2 : (use_tc ? 1 : 0);
         if (use_tc) {
             if (!c->tc_eimg_ready) {
@@ -1391,9 +1400,6 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
                 c->tc_eimg_ready = true;
             }
             a.tc_eimg = c->d_tc_eimg.p;
-            a.tc_pm = c->d_tc_pm.p;
-            a.tc_pword = c->d_tc_pword.p;
-            a.tc_slots = c->tc_slots;
         }
         // the launch shape comes first (autotuner trials run outside any graph), then the
         // three-phonon part of the pipeline runs directly or as the context's graph
@@ -1448,10 +1454,22 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
             for (int v : {maxps, (3 * maxps + 3) / 4, (maxps + 1) / 2})
                 if (v >= 1 && std::find(cand.begin(), cand.end(), v) == cand.end()) cand.push_back(v);
             const std::string key = tune_key(use_tc ? "threephonon_tc" : "threephonon", n, o->precision, c->device);
-            auto fused = [&, use_tc](const ThreePhArgs &x, int v) -> cudaError_t {
+            // the plan of the kernel in use (the SIMT kernel's in FP32 only)
+            tdg_ctx::Plan *plan = use_tc ? &c->tc_plan
+                                         : (o->precision != TDG_PREC_FP64 && c->simt_plan.slots > 0 ? &c->simt_plan
+                                                                                                  : nullptr);
+            if (plan) {
+                a.plan_pm = plan->pm.p;
+                a.plan_word = plan->word.p;
+                a.plan_slots = plan->slots;
+            }
+            auto fused = [&, use_tc, plan](const ThreePhArgs &x, int v) -> cudaError_t {
+                if (plan) {
+                    const cudaError_t ep =
+                        launch_fill_plan(plan->src.p, plan->slots, plan->threads, c->fc3_mwm32.p, plan->pm.p, s);
+                    if (ep != cudaSuccess) return ep;
+                }
                 if (!use_tc) return launch_threephonon(x, o->precision, c->n_sm, v, s);
-                const cudaError_t ep = launch_tc_fill_plan(c->d_tc_psrc.p, c->tc_slots, c->fc3_mwm32.p, c->d_tc_pm.p, s);
-                if (ep != cudaSuccess) return ep;
                 return launch_threephonon_tc(x, c->n_sm, v, s);
             };
             bool tuned = false;
@@ -1461,7 +1479,7 @@ extern "C" int tdg_scattering(tdg_ctx *c, const tdg_opts *o, const tdg_qlists *q
             if (tuned) CUDA_TRY(rezero_outputs(c, nr, ld, s));
             gk << (use_tc ? "t" : "f") << cps << '/' << std::string(reinterpret_cast<const char *>(&a), sizeof a);
             body3 = [&, fused]() { return fused(a, cps); };
-            launches += use_tc ? 2 : 1;
+            launches += plan ? 2 : 1;
             const int used = (cps > 0 && cps < maxps) ? cps : maxps;
             c->last_launch[0] = (int)std::min<int64_t>((int64_t)c->n_sm * used, std::max(ntrip, 1));
             c->last_launch[1] = used;
@@ -2349,7 +2367,7 @@ extern "C" int tdg_adjoint_fc3(tdg_ctx *c, const tdg_opts *o, const double *lw_b
     const char *tc_env = std::getenv("TDG_TC_SMALL");
     const bool use_tc = c->last_path == 1 && o->precision != TDG_PREC_FP64 && o->tensor_cores != 2 &&
                         !(tc_env && tc_env[0] == '0') && threephonon_tc_supported(n, o->precision, c->n_fc3) &&
-                        c->tc_slots > 0;
+                        c->tc_plan.slots > 0;
     // the CTA's gradient slice lives in shared memory when it is small enough (SIMT)
     const bool acc_smem = !use_tc && (size_t)c->n_fc3 * 27 * sizeof(double) <= 48 * 1024;
     const int grid = use_tc ? threephonon_tc_adjoint_grid(n, c->n_sm, ntrip, c->n_fc3)
@@ -2399,12 +2417,16 @@ extern "C" int tdg_adjoint_fc3(tdg_ctx *c, const tdg_opts *o, const double *lw_b
             CUDA_TRY(launch_tc_eimg(c->N, n, c->d_egvs32.p, c->d_tc_eimg_t.p, s, true));
             c->tc_eimg_t_ready = true;
         }
-        CUDA_TRY(launch_tc_fill_plan(c->d_tc_psrc.p, c->tc_slots, c->fc3_mwm32.p, c->d_tc_pm.p, s));
         a.tc_eimg = c->d_tc_eimg.p;
         a.tc_eimg_t = c->d_tc_eimg_t.p;
-        a.tc_pm = c->d_tc_pm.p;
-        a.tc_pword = c->d_tc_pword.p;
-        a.tc_slots = c->tc_slots;
+    }
+    tdg_ctx::Plan *plan = use_tc ? &c->tc_plan
+                                 : (o->precision != TDG_PREC_FP64 && c->simt_plan.slots > 0 ? &c->simt_plan : nullptr);
+    if (plan) {
+        CUDA_TRY(launch_fill_plan(plan->src.p, plan->slots, plan->threads, c->fc3_mwm32.p, plan->pm.p, s));
+        a.plan_pm = plan->pm.p;
+        a.plan_word = plan->word.p;
+        a.plan_slots = plan->slots;
     }
     CUDA_TRY(cudaEventRecord(ev[1], s));
     if (use_tc)
@@ -2452,6 +2474,7 @@ extern "C" int tdg_kappa_offdiag(tdg_ctx *c, const tdg_opts *o, double *kappa_of
     if (c->irr_dyngrad.empty())
         return set_error(kErrParam, "tdg_kappa_offdiag: the problem has no irr_dyngrad/op_fmap/atom_shift");
     CUDA_TRY(cudaSetDevice(c->device));
+    PhaseTimer pt("tdg_kappa_offdiag");
     cudaStream_t s = c->stream;
     const int n = c->n, nirr = c->nirr;
     const size_t nn = (size_t)n * n;
@@ -2462,7 +2485,19 @@ extern "C" int tdg_kappa_offdiag(tdg_ctx *c, const tdg_opts *o, double *kappa_of
         CUDA_TRY(c->d_qfull.upload(c->q_full.data(), c->q_full.size(), s));
         CUDA_TRY(c->d_irr_weight.upload(c->irr_weight.data(), c->irr_weight.size(), s));
         if (c->d_op_cart.n == 0) CUDA_TRY(c->d_op_cart.upload(c->op_cart.data(), c->op_cart.size(), s));
-        const size_t w = offdiag_work_elems(n, nirr);
+        // (point, operation) items of the per-operation kernels, point-major
+        std::vector<int2> items;
+        std::vector<int32_t> iptr(nirr + 1, 0);
+        for (int q = 0; q < nirr; ++q) {
+            for (int k = 0; k < c->irr_nop[q]; ++k) items.push_back(make_int2(q, k));
+            iptr[q + 1] = (int32_t)items.size();
+        }
+        c->od_items = (int)items.size();
+        if (n <= kOffdiagSmemModes) {
+            CUDA_TRY(c->d_od_items.upload(items.data(), items.size(), s));
+            CUDA_TRY(c->d_od_itemptr.upload(iptr.data(), iptr.size(), s));
+        }
+        const size_t w = offdiag_work_elems(n, nirr, c->od_items);
         if (w) CUDA_TRY(c->d_odwork.alloc(w));
         CUDA_TRY(c->d_odS.alloc((size_t)nirr * 9));
     }
@@ -2477,6 +2512,7 @@ extern "C" int tdg_kappa_offdiag(tdg_ctx *c, const tdg_opts *o, double *kappa_of
         }
     }
     CUDA_TRY(c->d_lwcv.upload(lwcv.data(), lwcv.size(), s));
+    pt.mark("uploads");
     OffdiagArgs a{};
     a.n = n;
     a.na = c->na;
@@ -2497,12 +2533,16 @@ extern "C" int tdg_kappa_offdiag(tdg_ctx *c, const tdg_opts *o, double *kappa_of
     a.inv_volume = 1.0 / c->volume;
     a.chop_tol = 1E-10 / (kGroupVelAuToMs / 1000.0);
     a.work = c->d_odwork.p;
+    a.part = c->d_odwork.p;
+    a.items = c->d_od_items.p;
+    a.item_ptr = c->d_od_itemptr.p;
     a.vel = nullptr;
     a.S = c->d_odS.p;
-    CUDA_TRY(launch_offdiag(a, nirr, s));
+    CUDA_TRY(launch_offdiag(a, nirr, c->od_items, s));
     std::vector<double> S((size_t)nirr * 9);
     CUDA_TRY(copy_async(S.data(), c->d_odS.p, sizeof(double) * S.size(), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
+    pt.mark("little-group sandwiches (device)");
     // star of each irreducible point: (1/n_star) sum_R R S R^T (kappa.f90:221-231)
     std::vector<double> K((size_t)nirr * 9, 0.0);
     std::vector<int> nstar(nirr, 0);
@@ -2529,6 +2569,7 @@ extern "C" int tdg_kappa_offdiag(tdg_ctx *c, const tdg_opts *o, double *kappa_of
     for (int k = 0; k < 9; ++k) kap[k] = lo_chop(kap[k], tol);
     symmetrize_kappa(c, kap);
     std::memcpy(kappa_offdiag, kap, sizeof(kap));
+    pt.mark("stars (host)");
     return kOk;
 }
 

@@ -153,13 +153,15 @@ struct ThreePhArgs {
     int32_t acc_in_smem;        // accumulate the CTA's slice in shared memory, store it once
     const double *xi_bar;       // adjoint only, may be null: cotangent of the raw three-phonon
                                 // row terms of Xi ([n_row * n_full*n], tdg_kappa_iter_vjp)
+    // pretransform plan of the fused kernel launched (pretransform_plan; FP32 force constants):
+    // plan_slots x (its threads) values, 4 force constants per slot, and words; plan_slots 0:
+    // none (the SIMT kernel then walks the blocks; the tensor-core kernel requires the plan)
+    const float4 *plan_pm;
+    const uint32_t *plan_word;
+    int32_t plan_slots;
     // tensor-core kernel only (k_threephonon_tc): real-split eigenvector images of every mesh
-    // point (4 KB each) and the pretransform plan (tc_pretransform_plan): tc_slots x 256
-    // values (4 FP32 force constants per slot) and words
+    // point (4 KB each)
     const unsigned char *tc_eimg;
-    const float4 *tc_pm;
-    const uint32_t *tc_pword;
-    int32_t tc_slots;
     // tensor-core adjoint only: the images of the transposed eigenvector matrices (E^T)
     const unsigned char *tc_eimg_t;
 };
@@ -188,15 +190,21 @@ cudaError_t launch_threephonon_tc(const ThreePhArgs &a, int n_sm, int ctas_per_s
 // float slices, one per CTA of the returned grid; a.acc_in_smem is not used).
 int threephonon_tc_adjoint_grid(int n, int n_sm, int n_trip, int n_fc);
 cudaError_t launch_threephonon_tc_adjoint(const ThreePhArgs &a, int grid, cudaStream_t s);
-// Pretransform plan of the tensor-core kernel for n modes and the force-constant blocks
-// blk_ptr (n_blk + 1 offsets, host memory): the elements (atom triple, ijk) dealt out to
-// the 256 threads of a CTA, slot-major ([slot][thread]); word = first phase-factor index |
-// (operand offset / 2 + 1) << 16 on an element's last slot, src = first triplet | ijk << 16
+// Pretransform plan of a fused kernel for n modes and the force-constant blocks blk_ptr
+// (n_blk + 1 offsets, host memory): the elements (atom triple, ijk) dealt out to the threads
+// of a CTA, slot-major ([slot][thread]); word = first phase-factor index | (code + 1) << 16
+// on an element's last slot, code = the tensor-core operand's byte offset / 2 (tc_operand)
+// or the index of P(a, b, c) in the SIMT kernel's n^3 array; src = first triplet | ijk << 16
 // | valid triplets << 21. Returns the slot count (a multiple of 8), 0 if the set does not fit.
-int tc_pretransform_plan(int n, int n_blk, const int32_t *blk_ptr, std::vector<uint32_t> &word,
-                         std::vector<uint32_t> &src);
-// The plan's values from the FP32 force constants ([n_fc * 27]), slots x 256 float4.
-cudaError_t launch_tc_fill_plan(const uint32_t *src, int slots, const float *mwm32, float4 *pm, cudaStream_t s);
+int pretransform_plan(int n, int n_blk, const int32_t *blk_ptr, int threads, bool tc_operand,
+                      std::vector<uint32_t> &word, std::vector<uint32_t> &src);
+// The plan's values from the FP32 force constants ([n_fc * 27]), slots x threads float4.
+cudaError_t launch_fill_plan(const uint32_t *src, int slots, int threads, const float *mwm32, float4 *pm,
+                             cudaStream_t s);
+// Threads per CTA of the fused SIMT kernel for n modes, and whether its FP32 passes can take
+// a pretransform plan for n_fc force-constant triplets (all phase factors at once).
+int threephonon_threads(int n);
+bool threephonon_plan_fits(int n, int n_fc);
 // Real-split eigenvector images (n <= 16).
 // transpose: the image of E^T (rows modes, columns components) for the adjoint.
 cudaError_t launch_tc_eimg(int32_t n_full, int32_t n, const float2 *egvs32, unsigned char *out, cudaStream_t s,
@@ -375,7 +383,7 @@ cudaError_t launch_bte_update(const BteDev &d, const double *buf, cudaStream_t s
 int bte_part_elems(int32_t n_irr);
 
 // What an entry point compiled outside the context's own file needs of a context.
-// Off-diagonal kappa (k_offdiag.cu), one CTA per irreducible point. Index tables 0-based.
+// Off-diagonal kappa (k_offdiag.cu). Index tables 0-based.
 constexpr int kOffdiagSmemModes = 18;  // up to this many modes the work arrays live in shared memory
 struct OffdiagArgs {
     int32_t n, na, n_op;
@@ -394,12 +402,18 @@ struct OffdiagArgs {
     const double *irr_weight; // [n_irr]
     double inv_volume;
     double chop_tol;          // velocity components below this become 0 (kappa.f90:209)
-    double2 *work;            // offdiag_work_elems(n, n_irr) beyond kOffdiagSmemModes modes
+    double2 *work;            // beyond kOffdiagSmemModes modes: offdiag_work_elems(n, n_irr, 0)
+    // up to kOffdiagSmemModes modes: the (point, operation index) items, point-major in
+    // operation order, the first item of each point ([n_irr + 1]) and the items' parts
+    // ([n_items][3][n][n], offdiag_work_elems(n, n_irr, n_items))
+    const int2 *items;
+    const int32_t *item_ptr;
+    double2 *part;
     double *vel;              // optional [n_irr][n][n][3] off-diagonal velocities
     double *S;                // [n_irr][9] sum over mode pairs of w v v^T, column-major
 };
-size_t offdiag_work_elems(int n, int n_irr);
-cudaError_t launch_offdiag(const OffdiagArgs &a, int n_irr, cudaStream_t s);
+size_t offdiag_work_elems(int n, int n_irr, int n_items);
+cudaError_t launch_offdiag(const OffdiagArgs &a, int n_irr, int n_items, cudaStream_t s);
 
 struct CtxView {
     int device;

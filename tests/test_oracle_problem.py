@@ -24,6 +24,12 @@ def test_host_stage_against_the_oracle_problem(configs, name, grid):
     mine = sorted((t[0], t[1], t[2], *np.round(t[3]).astype(int), *np.round(t[4]).astype(int)) for t in o.fc3)
     theirs = sorted(tuple(int(x) for x in (*(p.fc3_atoms[t] - 1), *p.fc3_lv[t])) for t in range(p.n_fc3))
     assert mine == theirs
+    # force-constant values, file order (the library parses the numbers itself; the two
+    # mass-weighting orders differ by an ulp or two)
+    ism = 1.0 / np.sqrt(o.mass)
+    ref = np.array([t[5] * ism[t[0]] * ism[t[1]] * ism[t[2]] for t in o.fc3])
+    np.testing.assert_array_equal(p.fc3_atoms - 1, [t[:3] for t in o.fc3])
+    np.testing.assert_allclose(p.fc3_mwm, ref, rtol=0, atol=1e-15 * np.abs(ref).max())
     # the same point group (as a set of Cartesian rotations)
     R = {tuple(np.round(p.op_cart[k].reshape(3, 3, order="F"), 8).ravel()) for k in range(p.n_op)}
     Ro = {tuple(np.round(o.lat @ W @ np.linalg.inv(o.lat), 8).ravel()) for W, _ in o.ops}
