@@ -332,120 +332,6 @@ __device__ bool warp_jacobi(int n, double2 *A, double2 *V, double *w) {
     return conv;
 }
 
-// The same eigenproblem for n <= 32 with A and V in shared memory, by parallel ordering:
-// each step rotates m/2 disjoint pairs (p, q) of the round-robin tournament over m = n
-// rounded up to even indices (an index >= n pairs with nothing), one lane deriving each
-// pair's rotation from the same snapshot of A (a pair's 2 x 2 block is touched by no other
-// pair of the step), then A <- A J, A <- J^H A and V <- V J for all pairs at once; m - 1
-// steps make a sweep. GB300 issues FP64 at 2 lanes per clock per SM, so a rotation derived
-// by every lane of the warp (the cyclic form above) costs 32 times its arithmetic; here 16
-// rotations share one such derivation. The rotations are the cyclic form's, applied in
-// another order: the eigenpairs agree to rounding (within degenerate subspaces the basis
-// may differ; the velocity-operator gauge fixes it afterwards). rot: 16 x 4 doubles of
-// shared memory. Returns false when 100 sweeps do not converge.
-__device__ bool warp_jacobi_par(int n, double2 *A, double2 *V, double *w, double *rot) {
-    const int lane = threadIdx.x & 31;
-    const int m = (n + 1) & ~1, half = m / 2;
-    for (int k = lane; k < n * n; k += 32) V[k] = make_double2((k % n) == (k / n) ? 1.0 : 0.0, 0.0);
-    double scale = 0.0;
-    for (int k = lane; k < n * n; k += 32) scale += cnorm(A[k]);
-    for (int o = 16; o > 0; o >>= 1) scale += __shfl_xor_sync(0xffffffffu, scale, o);
-    __syncwarp();
-    if (scale == 0.0) {
-        for (int k = lane; k < n; k += 32) w[k] = 0.0;
-        __syncwarp();
-        return true;
-    }
-    // pair i of step s (circle method): slot 0 stays, slots 1..m-1 rotate by s
-    auto pair_of = [&](int s, int i, int &p, int &q) {
-        const int a = i == 0 ? 0 : 1 + (i - 1 + s) % (m - 1);
-        const int b = 1 + (m - 1 - i - 1 + s) % (m - 1);
-        p = a < b ? a : b;
-        q = a < b ? b : a;
-    };
-    bool conv = false;
-    for (int sweep = 0; sweep < 100; ++sweep) {
-        double off = 0.0;
-        for (int k = lane; k < n * n; k += 32)
-            if ((k % n) != (k / n)) off += cnorm(A[k]);
-        for (int o = 16; o > 0; o >>= 1) off += __shfl_xor_sync(0xffffffffu, off, o);
-        if (off <= 1e-30 * scale) {
-            conv = true;
-            break;
-        }
-        for (int st = 0; st < m - 1; ++st) {
-            __syncwarp();
-            if (lane < half) {
-                int p, q;
-                pair_of(st, lane, p, q);
-                double cs = 1.0, sn = 0.0, ux = 1.0, uy = 0.0;
-                if (q < n) {
-                    const double2 g = A[p + (size_t)n * q];
-                    const double ag = hypot(g.x, g.y);
-                    if (ag > 1e-300) {
-                        ux = g.x / ag;
-                        uy = g.y / ag;
-                        const double app = A[p + (size_t)n * p].x, aqq = A[q + (size_t)n * q].x;
-                        const double tau = (aqq - app) / (2.0 * ag);
-                        const double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-                        cs = 1.0 / sqrt(1.0 + t * t);
-                        sn = t * cs;
-                    }
-                }
-                rot[4 * lane] = cs;
-                rot[4 * lane + 1] = sn;
-                rot[4 * lane + 2] = ux;
-                rot[4 * lane + 3] = uy;
-            }
-            __syncwarp();
-            for (int task = lane; task < half * n; task += 32) {  // A <- A J, V <- V J
-                const int i = task / n, k = task % n;
-                int p, q;
-                pair_of(st, i, p, q);
-                if (q >= n) continue;
-                const double cs = rot[4 * i], sn = rot[4 * i + 1];
-                const double2 u = make_double2(rot[4 * i + 2], rot[4 * i + 3]);
-                const double2 jqp = cscale(cconj(u), -sn), jqq = cscale(cconj(u), cs);
-                const double2 akp = A[k + (size_t)n * p], akq = A[k + (size_t)n * q];
-                A[k + (size_t)n * p] = cadd(cscale(akp, cs), cmul(akq, jqp));
-                A[k + (size_t)n * q] = cadd(cscale(akp, sn), cmul(akq, jqq));
-                const double2 vkp = V[k + (size_t)n * p], vkq = V[k + (size_t)n * q];
-                V[k + (size_t)n * p] = cadd(cscale(vkp, cs), cmul(vkq, jqp));
-                V[k + (size_t)n * q] = cadd(cscale(vkp, sn), cmul(vkq, jqq));
-            }
-            __syncwarp();
-            for (int task = lane; task < half * n; task += 32) {  // A <- J^H A
-                const int i = task / n, k = task % n;
-                int p, q;
-                pair_of(st, i, p, q);
-                if (q >= n) continue;
-                const double cs = rot[4 * i], sn = rot[4 * i + 1];
-                const double2 u = make_double2(rot[4 * i + 2], rot[4 * i + 3]);
-                const double2 jqp = cscale(cconj(u), -sn), jqq = cscale(cconj(u), cs);
-                const double2 apk = A[p + (size_t)n * k], aqk = A[q + (size_t)n * k];
-                A[p + (size_t)n * k] = cadd(cscale(apk, cs), cmul(cconj(jqp), aqk));
-                A[q + (size_t)n * k] = cadd(cscale(apk, sn), cmul(cconj(jqq), aqk));
-            }
-            __syncwarp();
-            if (lane < half) {
-                int p, q;
-                pair_of(st, lane, p, q);
-                if (q < n) {
-                    A[p + (size_t)n * q] = make_double2(0.0, 0.0);
-                    A[q + (size_t)n * p] = make_double2(0.0, 0.0);
-                    A[p + (size_t)n * p].y = 0.0;
-                    A[q + (size_t)n * q].y = 0.0;
-                }
-            }
-        }
-        __syncwarp();
-    }
-    __syncwarp();
-    for (int k = lane; k < n; k += 32) w[k] = A[k + (size_t)n * k].x;
-    __syncwarp();
-    return conv;
-}
-
 // Stable sort of n < 128 keys into ord (by lane 0; the others wait at the caller's syncwarp).
 __device__ void stable_order(int n, const double *key, int *ord) {
     for (int i = 0; i < n; ++i) ord[i] = i;
@@ -463,18 +349,10 @@ __device__ void stable_order(int n, const double *key, int *ord) {
 constexpr int kEigWarps = 1;  // one warp per CTA: the points spread over the SMs, each with its own FP64 pipe
 constexpr int kMaxModes = 128;
 
-// Up to this many modes the matrices of a point (A, V, E) live in shared memory: every
-// Jacobi rotation stores what the next one loads, and through global memory each of those
-// round trips went to L2.
-constexpr int kEigSmemModes = 24;
-inline size_t eigen_smem_bytes(int n) { return n <= kEigSmemModes ? (size_t)3 * n * n * sizeof(double2) : 0; }
-
 __global__ void __launch_bounds__(32 * kEigWarps) k_eigen(HarmDev h) {
     __shared__ int s_ord[kEigWarps][kMaxModes];
     __shared__ double s_key[kEigWarps][kMaxModes];
     __shared__ int s_sub[kEigWarps][kMaxModes];
-    __shared__ double s_rot[kEigWarps][64];
-    extern __shared__ double2 s_mat[];  // kEigWarps == 1: A, V, E of the CTA's point
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int iq = blockIdx.x * kEigWarps + wid;
     if (iq >= h.nirr) return;
@@ -482,19 +360,12 @@ __global__ void __launch_bounds__(32 * kEigWarps) k_eigen(HarmDev h) {
     int *ord = s_ord[wid];
     double *key = s_key[wid];
     int *sub = s_sub[wid];
-    const bool local = kEigWarps == 1 && n <= kEigSmemModes;
-    double2 *Ag = h.D + (size_t)iq * n * n;
-    double2 *Eg = h.egv + (size_t)iq * n * n;  // E[b * n + r]
-    double2 *A = local ? s_mat : Ag;
-    double2 *V = local ? s_mat + n * n : h.V + (size_t)iq * n * n;
-    double2 *E = local ? s_mat + 2 * n * n : Eg;
+    double2 *A = h.D + (size_t)iq * n * n;
+    double2 *V = h.V + (size_t)iq * n * n;
     const double2 *G = h.Gd + (size_t)iq * 3 * n * n;
     double *w = h.w + (size_t)iq * n;
     double *om = h.om + (size_t)iq * n;
-    if (local) {
-        for (int k = lane; k < n * n; k += 32) A[k] = Ag[k];
-        __syncwarp();
-    }
+    double2 *E = h.egv + (size_t)iq * n * n;  // E[b * n + r]
     // Hermitise against rounding
     for (int k = lane; k < n * n; k += 32) {
         const int i = k % n, j = k / n;
@@ -506,7 +377,7 @@ __global__ void __launch_bounds__(32 * kEigWarps) k_eigen(HarmDev h) {
         }
     }
     __syncwarp();
-    if (!(local ? warp_jacobi_par(n, A, V, w, s_rot[wid]) : warp_jacobi(n, A, V, w))) {
+    if (!warp_jacobi(n, A, V, w)) {
         if (lane == 0) atomicExch(h.status, (int32_t)kDevLinalg);
         return;
     }
@@ -623,9 +494,285 @@ __global__ void __launch_bounds__(32 * kEigWarps) k_eigen(HarmDev h) {
         for (int b2 = l; b2 < n; ++b2) dm[b2] = 0;
         h.degen[(size_t)iq * n + b] = l;
     }
-    if (local) {
-        for (int k = lane; k < n * n; k += 32) Eg[k] = E[k];
+}
+
+// ---- up to kEigCtaModes modes: one CTA of kEigCtaThreads per irreducible point ----
+// GB300 issues FP64 at 2 lanes per clock per SM and the work of one point is a chain of
+// dependent FP64 steps, so a point's time is its latency: the CTA spreads each step over
+// 4 warps, keeps every matrix in shared memory, and runs the Jacobi sweeps in parallel
+// order (cta_jacobi). The products of the subspace gauge and of the Hellmann-Feynman
+// velocities are split into G E first (one task per (direction, component, mode)) and the
+// sandwich after, with the summation order of the warp kernel's single loops.
+constexpr int kEigCtaModes = 24;
+constexpr int kEigCtaThreads = 128;
+
+// Sum of v over the CTA, the same value in every thread (red: 32 doubles of shared memory).
+__device__ double cta_sum(double v, double *red) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __syncthreads();  // red is free
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    double s = 0.0;
+    for (int i = 0; i < nw; ++i) s += red[i];
+    return s;
+}
+
+// The Hermitian eigenproblem of the n x n matrix A (column-major, shared memory, n <= 32)
+// by the CTA: the rotations of the cyclic Jacobi (warp_jacobi) in parallel order. Each step
+// rotates the m/2 disjoint pairs (p, q) of a round-robin tournament over m = n rounded up to
+// even indices (an index >= n pairs with nothing), thread i deriving pair i's rotation from
+// the same snapshot of A (a pair's 2 x 2 block is touched by no other pair of the step),
+// then A <- A J, A <- J^H A and V <- V J for all pairs at once; m - 1 steps make a sweep.
+// The sweeps to convergence are the cyclic order's (a numpy emulation of both orders on
+// random Hermitian matrices, n = 3 to 24) and the eigenpairs agree to rounding (degenerate
+// subspaces up to their basis). rot: 64 doubles, pq: (m - 1) m / 2 short2, red: 32 doubles.
+// Returns false when 100 sweeps do not converge.
+__device__ bool cta_jacobi(int n, double2 *A, double2 *V, double *w, double *rot, short2 *pq, double *red) {
+    const int tid = threadIdx.x, T = blockDim.x;
+    const int m = (n + 1) & ~1, half = m / 2;
+    for (int k = tid; k < n * n; k += T) V[k] = make_double2((k % n) == (k / n) ? 1.0 : 0.0, 0.0);
+    for (int i = tid; i < (m - 1) * half; i += T) {  // circle method: slot 0 stays, the others rotate
+        const int st = i / half, j = i % half;
+        const int a = j == 0 ? 0 : 1 + (j - 1 + st) % (m - 1);
+        const int b = 1 + (m - 2 - j + st) % (m - 1);
+        pq[i] = make_short2((short)min(a, b), (short)max(a, b));
     }
+    double part = 0.0;
+    for (int k = tid; k < n * n; k += T) part += cnorm(A[k]);
+    const double scale = cta_sum(part, red);
+    if (scale == 0.0) {
+        for (int k = tid; k < n; k += T) w[k] = 0.0;
+        __syncthreads();
+        return true;
+    }
+    bool conv = false;
+    for (int sweep = 0; sweep < 100; ++sweep) {
+        part = 0.0;
+        for (int k = tid; k < n * n; k += T)
+            if ((k % n) != (k / n)) part += cnorm(A[k]);
+        if (cta_sum(part, red) <= 1e-30 * scale) {
+            conv = true;
+            break;
+        }
+        for (int st = 0; st < m - 1; ++st) {
+            const short2 *ps = pq + st * half;
+            if (tid < half) {
+                const int p = ps[tid].x, q = ps[tid].y;
+                double cs = 1.0, sn = 0.0, ux = 1.0, uy = 0.0;
+                if (q < n) {
+                    const double2 g = A[p + (size_t)n * q];
+                    const double ag = hypot(g.x, g.y);
+                    if (ag > 1e-300) {
+                        ux = g.x / ag;
+                        uy = g.y / ag;
+                        const double app = A[p + (size_t)n * p].x, aqq = A[q + (size_t)n * q].x;
+                        const double tau = (aqq - app) / (2.0 * ag);
+                        const double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+                        cs = 1.0 / sqrt(1.0 + t * t);
+                        sn = t * cs;
+                    }
+                }
+                rot[4 * tid] = cs;
+                rot[4 * tid + 1] = sn;
+                rot[4 * tid + 2] = ux;
+                rot[4 * tid + 3] = uy;
+            }
+            __syncthreads();
+            for (int task = tid; task < half * n; task += T) {  // A <- A J, V <- V J
+                const int i = task / n, k = task % n;
+                const int p = ps[i].x, q = ps[i].y;
+                if (q >= n) continue;
+                const double cs = rot[4 * i], sn = rot[4 * i + 1];
+                const double2 u = make_double2(rot[4 * i + 2], rot[4 * i + 3]);
+                const double2 jqp = cscale(cconj(u), -sn), jqq = cscale(cconj(u), cs);
+                const double2 akp = A[k + (size_t)n * p], akq = A[k + (size_t)n * q];
+                A[k + (size_t)n * p] = cadd(cscale(akp, cs), cmul(akq, jqp));
+                A[k + (size_t)n * q] = cadd(cscale(akp, sn), cmul(akq, jqq));
+                const double2 vkp = V[k + (size_t)n * p], vkq = V[k + (size_t)n * q];
+                V[k + (size_t)n * p] = cadd(cscale(vkp, cs), cmul(vkq, jqp));
+                V[k + (size_t)n * q] = cadd(cscale(vkp, sn), cmul(vkq, jqq));
+            }
+            __syncthreads();
+            for (int task = tid; task < half * n; task += T) {  // A <- J^H A
+                const int i = task / n, k = task % n;
+                const int p = ps[i].x, q = ps[i].y;
+                if (q >= n) continue;
+                const double cs = rot[4 * i], sn = rot[4 * i + 1];
+                const double2 u = make_double2(rot[4 * i + 2], rot[4 * i + 3]);
+                const double2 jqp = cscale(cconj(u), -sn), jqq = cscale(cconj(u), cs);
+                const double2 apk = A[p + (size_t)n * k], aqk = A[q + (size_t)n * k];
+                A[p + (size_t)n * k] = cadd(cscale(apk, cs), cmul(cconj(jqp), aqk));
+                A[q + (size_t)n * k] = cadd(cscale(apk, sn), cmul(cconj(jqq), aqk));
+            }
+            __syncthreads();
+            if (tid < half) {
+                const int p = ps[tid].x, q = ps[tid].y;
+                if (q < n) {
+                    A[p + (size_t)n * q] = make_double2(0.0, 0.0);
+                    A[q + (size_t)n * p] = make_double2(0.0, 0.0);
+                    A[p + (size_t)n * p].y = 0.0;
+                    A[q + (size_t)n * q].y = 0.0;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int k = tid; k < n; k += T) w[k] = A[k + (size_t)n * k].x;
+    __syncthreads();
+    return conv;
+}
+
+// Shared memory of k_eigen_cta for n modes (bytes).
+inline size_t eigen_cta_smem(int n) {
+    const size_t nn = (size_t)n * n, m = (size_t)((n + 1) & ~1);
+    return sizeof(double2) * 8 * nn                      // A, V, E, GE (3 nn), Pm, U
+           + sizeof(double) * (64 + 32 + 2 * (size_t)n + 3 * (size_t)n)  // rot, red, key, pw, hf
+           + sizeof(int) * 2 * (size_t)n                 // ord, sub
+           + sizeof(short2) * (m - 1) * (m / 2) + 16;
+}
+
+__global__ void __launch_bounds__(kEigCtaThreads) k_eigen_cta(HarmDev h) {
+    extern __shared__ double2 s_cta[];
+    const int iq = blockIdx.x, n = h.nb, tid = threadIdx.x, T = blockDim.x;
+    const size_t nn = (size_t)n * n;
+    double2 *A = s_cta, *V = A + nn, *E = V + nn, *GE = E + nn, *Pm = GE + 3 * nn, *U = Pm + nn;
+    double *rot = reinterpret_cast<double *>(U + nn), *red = rot + 64, *key = red + 32, *pw = key + n, *hf = pw + n;
+    int *ord = reinterpret_cast<int *>(hf + 3 * n), *sub = ord + n;
+    short2 *pq = reinterpret_cast<short2 *>(sub + n);
+    const double2 *Ag = h.D + (size_t)iq * nn;
+    const double2 *G = h.Gd + (size_t)iq * 3 * nn;
+    double *w = h.w + (size_t)iq * n;
+    double *om = h.om + (size_t)iq * n;
+    // Hermitise against rounding
+    for (int k = tid; k < (int)nn; k += T) {
+        const int i = k % n, j = k / n, i0 = min(i, j), j0 = max(i, j);  // the pair (i0, j0), i0 <= j0
+        const double2 a = Ag[i0 + (size_t)n * j0], b = cconj(Ag[j0 + (size_t)n * i0]);
+        const double2 sm = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y + b.y));
+        A[k] = i <= j ? sm : cconj(sm);
+    }
+    __syncthreads();
+    if (!cta_jacobi(n, A, V, w, rot, pq, red)) {
+        if (tid == 0) atomicExch(h.status, (int32_t)kDevLinalg);
+        return;
+    }
+    const double *qr = h.qirr + 3 * iq;
+    if (tid == 0) {
+        if (qr[0] * qr[0] + qr[1] * qr[1] + qr[2] * qr[2] < kSqTolD) {  // acoustic modes at Gamma
+            for (int b = 0; b < n; ++b) key[b] = fabs(w[b]);
+            stable_order(n, key, ord);
+            for (int i = 0; i < min(3, n); ++i) w[ord[i]] = 0.0;
+        }
+        for (int b = 0; b < n; ++b) key[b] = negsqrt(w[b]);
+        stable_order(n, key, ord);
+        for (int b = 0; b < n; ++b) om[b] = negsqrt(w[ord[b]]);
+    }
+    __syncthreads();
+    for (int k = tid; k < (int)nn; k += T) {
+        const int b = k / n, r = k % n;
+        E[k] = V[r + (size_t)n * ord[b]];
+    }
+    __syncthreads();
+    // degenerate subspaces (contiguous, within lo_freqtol of the first): the velocity
+    // operator along a fixed generic direction diagonalised inside each
+    const double dir[3] = {1.0, 1.33, 1.45624623};
+    for (int b0 = 0; b0 < n;) {
+        int b1 = b0 + 1;
+        while (b1 < n && fabs(om[b1] - om[b0]) < kFreqTolH) ++b1;
+        const int k = b1 - b0;
+        if (k > 1) {
+            // GE[(d n + r) k + y] = sum_cc G_d[r, cc] E[b0 + y][cc]
+            for (int t = tid; t < 3 * n * k; t += T) {
+                const int y = t % k, dr = t / k, d = dr / n, r = dr % n;
+                double2 gy = make_double2(0.0, 0.0);
+                for (int cc = 0; cc < n; ++cc)
+                    gy = cadd(gy, cmul(G[(size_t)d * nn + r + (size_t)n * cc], E[(size_t)(b0 + y) * n + cc]));
+                GE[t] = gy;
+            }
+            __syncthreads();
+            for (int xy = tid; xy < k * k; xy += T) {
+                const int x = xy % k, y = xy / k;
+                double2 sm = make_double2(0.0, 0.0);
+                for (int d = 0; d < 3; ++d)
+                    for (int r = 0; r < n; ++r)
+                        sm = cadd(sm, cscale(cmul(cconj(E[(size_t)(b0 + x) * n + r]), GE[(size_t)(d * n + r) * k + y]),
+                                             dir[d]));
+                Pm[x + k * y] = sm;
+            }
+            __syncthreads();
+            for (int xy = tid; xy < k * k; xy += T) {
+                const int x = xy % k, y = xy / k;
+                if (x <= y) {
+                    const double2 a = Pm[x + k * y], b = cconj(Pm[y + k * x]);
+                    const double2 sm = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y + b.y));
+                    Pm[x + k * y] = sm;
+                    Pm[y + k * x] = cconj(sm);
+                }
+            }
+            __syncthreads();
+            if (!cta_jacobi(k, Pm, U, pw, rot, pq, red)) {
+                if (tid == 0) atomicExch(h.status, (int32_t)kDevLinalg);
+                return;
+            }
+            if (tid == 0) stable_order(k, pw, ord);
+            // the subspace's rows of E, before the rotation, into GE as scratch
+            for (int t = tid; t < k * n; t += T) GE[t] = E[(size_t)b0 * n + t];
+            __syncthreads();
+            // sub = E_sub U[:, po]
+            for (int t = tid; t < k * n; t += T) {
+                const int y = t / n, r = t % n;
+                double2 sm = make_double2(0.0, 0.0);
+                for (int x = 0; x < k; ++x) sm = cadd(sm, cmul(GE[(size_t)x * n + r], U[x + k * ord[y]]));
+                E[(size_t)(b0 + y) * n + r] = sm;
+            }
+            __syncthreads();
+        }
+        b0 = b1;
+    }
+    // Hellmann-Feynman values <e_b|dD/dk_d|e_b>: GE[(d n + r) n + b] = sum_cc G_d[r, cc] E[b][cc]
+    for (int t = tid; t < 3 * (int)nn; t += T) {
+        const int b = t % n, dr = t / n, d = dr / n, r = dr % n;
+        double2 gy = make_double2(0.0, 0.0);
+        for (int cc = 0; cc < n; ++cc) gy = cadd(gy, cmul(G[(size_t)d * nn + r + (size_t)n * cc], E[(size_t)b * n + cc]));
+        GE[t] = gy;
+    }
+    __syncthreads();
+    for (int bd = tid; bd < 3 * n; bd += T) {
+        const int b = bd / 3, d = bd % 3;
+        double2 sm = make_double2(0.0, 0.0);
+        for (int r = 0; r < n; ++r) sm = cadd(sm, cmul(cconj(E[(size_t)b * n + r]), GE[(size_t)(d * n + r) * n + b]));
+        hf[bd] = sm.x;
+    }
+    if (tid == 0) {  // a mode joins the first subspace holding a mode within lo_freqtol of it
+        int nsub = 0;
+        for (int b = 0; b < n; ++b) {
+            sub[b] = -1;
+            for (int a = 0; a < b && sub[b] < 0; ++a)
+                if (fabs(om[a] - om[b]) < kFreqTolH) sub[b] = sub[a];
+            if (sub[b] < 0) sub[b] = nsub++;
+        }
+    }
+    __syncthreads();
+    double *vel = h.vel + (size_t)iq * n * 3;
+    for (int b = tid; b < n; b += T) {
+        double mv[3] = {0.0, 0.0, 0.0};
+        int cnt = 0;
+        for (int a = 0; a < n; ++a)
+            if (sub[a] == sub[b]) {
+                ++cnt;
+                for (int d = 0; d < 3; ++d) mv[d] += hf[a * 3 + d];
+            }
+        for (int d = 0; d < 3; ++d) vel[b * 3 + d] = om[b] > kFreqTolH ? (mv[d] / cnt) / (2.0 * om[b]) : 0.0;
+        int l = 0;
+        int32_t *dm = h.degen_mode + ((size_t)iq * n + b) * n;
+        for (int b2 = 0; b2 < n; ++b2) {
+            if (fabs(om[b] - om[b2]) < kFreqTolH) dm[l++] = b2 + 1;
+        }
+        for (int b2 = l; b2 < n; ++b2) dm[b2] = 0;
+        h.degen[(size_t)iq * n + b] = l;
+    }
+    double2 *Eg = h.egv + (size_t)iq * nn;  // E[b * n + r]
+    for (int k = tid; k < (int)nn; k += T) Eg[k] = E[k];
 }
 
 struct UnfoldDev {
@@ -825,7 +972,13 @@ int build_phonons_device(const Crystal &c, const FC2 &fc, const QMesh &qp, int d
     // the gradient at the irreducible points is an output (off-diagonal kappa)
     std::vector<double2> gd((size_t)ni * 3 * nb * nb);
     chk(cudaMemcpy(gd.data(), d_Gd.p, sizeof(double2) * gd.size(), cudaMemcpyDeviceToHost));
-    k_eigen<<<(ni + kEigWarps - 1) / kEigWarps, 32 * kEigWarps, eigen_smem_bytes(nb)>>>(h);
+    if (nb <= kEigCtaModes) {
+        const size_t sm = eigen_cta_smem(nb);
+        chk(cudaFuncSetAttribute(k_eigen_cta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        if (e == cudaSuccess) k_eigen_cta<<<ni, kEigCtaThreads, sm>>>(h);
+    } else {
+        k_eigen<<<(ni + kEigWarps - 1) / kEigWarps, 32 * kEigWarps>>>(h);
+    }
     chk(cudaGetLastError());
     int32_t dst = 0;
     chk(cudaMemcpy(&dst, d_status.p, sizeof(int32_t), cudaMemcpyDeviceToHost));

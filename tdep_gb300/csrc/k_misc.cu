@@ -327,26 +327,28 @@ __global__ void k_sample_bits(int32_t n_full, const int64_t *rbeg, const int32_t
 // K8: three dot products per row of Xi (kappa.f90:411-413, the lo_gemv calls).
 // Xi streams from HBM once per BTE iteration; F (3 x n_col) stays in L2. GB300's FP64 pipe
 // (2 FMA per SM and clock) would make an FP64 product with three right-hand sides
-// compute-bound at ~1.2 TB/s of Xi, so the product runs on the FP32 pipe in one of two
-// element formats, converted once per kappa call (k_split_xi) and per iteration for F
-// (k_foldout):
-//  - FP64 runs: Xi and F as (hi, lo) float pairs with hi + lo = x to ~2^-48, each term
-//    accumulated in double-float (exact leading product by FMA, cross terms, TwoSum of the
-//    high parts); ~1e-14 relative. Same bytes per element as FP64.
-//  - floats (Xi and F), chains of kChain products by FMA added into double-float
-//    accumulators: half the bytes. Mixed-precision runs use the pairs too: with floats, the
-//    modes whose F is zero by symmetry (v = 0 at a high-symmetry point) carry 1e-7 of the
-//    typical |F| from the rounding of Xi, above the convergence test's lo_sqtol floor, and
-//    their relative change kept the sum of the last three checks above 1e-6: rocksalt took
-//    200 iterations (the limit) instead of 31-33, with kappa already converged.
-// A CTA takes ROWS rows (4 or 8, autotuned) and one of the column ranges (gridDim.y): each F
-// value read from L2 serves ROWS rows. Partial sums go to part[row][range][3] (FP64) and are
-// added in range order by k_xi_reduce, so the result does not depend on scheduling. The
-// in-CTA reduction stays in double-float too: FP64 shuffles and adds in every CTA's epilogue
-// cost more than the product itself once there are more than a few ranges.
+// compute-bound at ~1.2 TB/s of Xi, so the product runs on the FP32 pipe: Xi and F as
+// (hi, lo) float pairs with hi + lo = x to ~2^-48 (converted once per kappa call, k_split_xi,
+// and per iteration for F, k_foldout), each term accumulated in double-float (exact leading
+// product by FMA, cross terms, TwoSum of the high parts); ~1e-14 relative, the bytes of FP64.
+// The rows go in pairs: pair p and column j are one float4 (hi of rows 2p and 2p + 1, lo of
+// both), so that the double-float arithmetic of the two rows runs in the packed FP32x2
+// instructions (__ffma2_rn, __fadd2_rn, __fmul2_rn: per component the scalar IEEE operation),
+// half the instructions of the scalar form, which left the product issue-bound at 0.58 of
+// the copy peak.
+// Floats for Xi (half the bytes) were the mixed-precision format until they failed the
+// convergence test: the modes whose F is zero by symmetry (v = 0 at a high-symmetry point)
+// carry 1e-7 of the typical |F| from the rounding of Xi, above the test's lo_sqtol floor,
+// and their relative change kept the sum of the last three checks above 1e-6 (rocksalt took
+// 200 iterations, the limit, instead of 31-33, with kappa already converged).
+// A CTA takes PAIRS row pairs (2 or 4, autotuned) and one of the column ranges (gridDim.y):
+// each F value read from L2 serves 2 PAIRS rows. Partial sums go to part[row][range][3]
+// (FP64) and are added in range order by k_xi_reduce, so the result does not depend on
+// scheduling. The in-CTA reduction stays in double-float too: FP64 shuffles and adds in
+// every CTA's epilogue cost more than the product itself once there are more than a few
+// ranges.
 constexpr int kGemvRows = 4;
 constexpr int kGemvMaxSplit = 32;
-constexpr int kChain = 4;
 
 // Ranges of at most 32768 columns, and enough CTAs for about two waves of 4 per SM.
 int gemv_split(int32_t n_row, int64_t n_col, int n_sm) {
@@ -377,18 +379,6 @@ __device__ __forceinline__ float2 split_df(double x) {
     return make_float2(hi, sign ? -lo : lo);
 }
 
-// x rounded to float (ties away from zero) by integer operations; magnitudes outside
-// [2^-126, 2^127) take the FP64 conversion.
-__device__ __forceinline__ float round_f32(double x) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const int e = (int)((b >> 52) & 0x7FF);
-    if (e == 0) return 0.f;
-    if (e < 897 || e > 1149) return (float)x;
-    const unsigned int v = ((unsigned int)(b >> 32) & 0x80000000u) | ((unsigned int)(e - 896) << 23) |
-                           (unsigned int)((b >> 29) & 0x7FFFFFu);
-    return __uint_as_float(v + (unsigned int)((b >> 28) & 1u));  // a carry moves into the exponent
-}
-
 // (a.x + a.y) + (b.x + b.y) in double-float (TwoSum of the high parts)
 __device__ __forceinline__ float2 df_add(float2 a, float2 b) {
     const float t = a.x + b.x;
@@ -397,195 +387,99 @@ __device__ __forceinline__ float2 df_add(float2 a, float2 b) {
     return make_float2(t, a.y + b.y + e);
 }
 
-// s += p in double-float
-__device__ __forceinline__ void df_add1(float2 &s, float p) {
-    const float t = s.x + p;
-    const float bb = t - s.x;
-    s.y += (s.x - (t - bb)) + (p - bb);
-    s.x = t;
+// Two double-float accumulators (s, sl: high and low parts of rows 2p and 2p + 1) += x * f
+// for the two rows' elements (x, xl) and one F value (f, fl, the same in both components);
+// nx = -x. The scalar form per component: p = x f, pe = fma(x, f, -p), cross = fma(x, fl,
+// xl f), TwoSum of s and p, sl += (e + pe) + cross. A subtraction a - b is fma(b, -1, a),
+// rounded once as a - b is.
+__device__ __forceinline__ void df2_fma(float2 &s, float2 &sl, float2 x, float2 nx, float2 xl, float2 f, float2 fl) {
+    const float2 m1 = make_float2(-1.f, -1.f);
+    const float2 p = __fmul2_rn(x, f);
+    const float2 npe = __ffma2_rn(nx, f, p);  // p - x f = -pe exactly
+    const float2 cross = __ffma2_rn(x, fl, __fmul2_rn(xl, f));
+    const float2 t = __fadd2_rn(s, p);
+    const float2 bb = __ffma2_rn(s, m1, t);                        // t - s
+    const float2 e1 = __ffma2_rn(__ffma2_rn(bb, m1, t), m1, s);    // s - (t - bb)
+    const float2 e = __fadd2_rn(e1, __ffma2_rn(bb, m1, p));       // + (p - bb)
+    s = t;
+    sl = __fadd2_rn(sl, __fadd2_rn(__ffma2_rn(npe, m1, e), cross));  // sl + ((e + pe) + cross)
 }
 
-// s += a * b in double-float
-__device__ __forceinline__ void df_fma(float2 &s, float2 a, float2 b) {
-    const float p = a.x * b.x;
-    const float pe = fmaf(a.x, b.x, -p);
-    const float cross = fmaf(a.x, b.y, a.y * b.x);
-    const float t = s.x + p;
-    const float bb = t - s.x;
-    const float e = (s.x - (t - bb)) + (p - bb);
-    s.x = t;
-    s.y += e + pe + cross;
-}
-
-template <bool DF>
-__global__ void k_split_xi(const double *xi, int64_t n, void *out) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        if constexpr (DF)
-            static_cast<float2 *>(out)[i] = split_df(__ldcs(xi + i));
-        else
-            static_cast<float *>(out)[i] = round_f32(__ldcs(xi + i));
+// Xi as double-float row pairs: pair p, column j at p * n_col + j as (hi of row 2p, hi of
+// row 2p + 1, lo of row 2p, lo of row 2p + 1); an odd last row pairs with a zero row.
+__global__ void k_split_xi(const double *xi, int32_t n_row, int64_t n_col, float4 *out) {
+    const int n_pair = (n_row + 1) / 2;
+    for (int p = blockIdx.y; p < n_pair; p += gridDim.y) {
+        const double *r0 = xi + (int64_t)(2 * p) * n_col;
+        const bool two = 2 * p + 1 < n_row;
+        for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n_col; j += (int64_t)gridDim.x * blockDim.x) {
+            const float2 a = split_df(__ldcs(r0 + j));
+            const float2 b = two ? split_df(__ldcs(r0 + n_col + j)) : make_float2(0.f, 0.f);
+            out[(int64_t)p * n_col + j] = make_float4(a.x, b.x, a.y, b.y);
+        }
     }
 }
 
-// DF: xi, fbb as float2 (FP64 runs); otherwise as float (mixed precision). Loads of four
-// consecutive columns per thread (16 bytes) measured slower than these 4-byte coalesced loads.
-template <bool DF, int ROWS>
-__global__ void __launch_bounds__(256) k_xi_gemv(const void *__restrict__ xi_, int32_t n_row, int64_t n_col,
-                                                 const void *__restrict__ fbb_, double *part, const int32_t *skip) {
-    __shared__ float2 sh[ROWS * 3][8];
+template <int PAIRS>
+__global__ void __launch_bounds__(256) k_xi_gemv(const float4 *__restrict__ xi, int32_t n_row, int64_t n_col,
+                                                 const float2 *__restrict__ fbb, double *part, const int32_t *skip) {
+    __shared__ float2 sh[2 * PAIRS * 3][8];
     if (skip && *skip) return;
-    const int r0 = blockIdx.x * ROWS;
-    const int nr = min(ROWS, n_row - r0);
-    // column ranges start on multiples of 8 (16-byte float4 loads of Xi and F)
+    const int p0 = blockIdx.x * PAIRS;
+    const int np = min(PAIRS, (n_row + 1) / 2 - p0);
+    const int r0 = 2 * p0, nr = min(2 * PAIRS, n_row - r0);
     const int64_t per = ((n_col + gridDim.y - 1) / gridDim.y + 7) / 8 * 8;
     const int64_t c0 = min(n_col, per * blockIdx.y), c1 = min(n_col, c0 + per);
-    float2 acc[ROWS][3];
+    float2 ah[PAIRS][3], al[PAIRS][3];
 #pragma unroll
-    for (int k = 0; k < ROWS; ++k) acc[k][0] = acc[k][1] = acc[k][2] = make_float2(0.f, 0.f);
+    for (int k = 0; k < PAIRS; ++k)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) ah[k][d] = al[k][d] = make_float2(0.f, 0.f);
+    const float4 *xr[PAIRS];
+#pragma unroll
+    for (int k = 0; k < PAIRS; ++k) xr[k] = xi + (int64_t)(p0 + min(k, np - 1)) * n_col;
     const int64_t step = blockDim.x;
     int64_t j = c0 + threadIdx.x;
-    if constexpr (DF) {
-        const float2 *xi = static_cast<const float2 *>(xi_);
-        const float2 *fbb = static_cast<const float2 *>(fbb_);
-        for (; j + step < c1; j += 2 * step) {
-            float2 x[2][ROWS];
+    auto column = [&](const float4 (&x)[PAIRS], int64_t jj) {
+        float2 fh[3], fl[3];
 #pragma unroll
-            for (int u = 0; u < 2; ++u)
-#pragma unroll
-                for (int k = 0; k < ROWS; ++k)
-                    x[u][k] = k < nr ? __ldcs(xi + (int64_t)(r0 + k) * n_col + j + u * step) : make_float2(0.f, 0.f);
-#pragma unroll
-            for (int u = 0; u < 2; ++u) {
-                const float2 *f = fbb + (j + u * step) * 3;
-                const float2 f0 = __ldg(f), f1 = __ldg(f + 1), f2 = __ldg(f + 2);
-#pragma unroll
-                for (int k = 0; k < ROWS; ++k) {
-                    df_fma(acc[k][0], x[u][k], f0);
-                    df_fma(acc[k][1], x[u][k], f1);
-                    df_fma(acc[k][2], x[u][k], f2);
-                }
-            }
+        for (int d = 0; d < 3; ++d) {
+            const float2 t = __ldg(fbb + jj * 3 + d);
+            fh[d] = make_float2(t.x, t.x);
+            fl[d] = make_float2(t.y, t.y);
         }
-        for (; j < c1; j += step) {
-            const float2 *f = fbb + j * 3;
-            const float2 f0 = __ldg(f), f1 = __ldg(f + 1), f2 = __ldg(f + 2);
 #pragma unroll
-            for (int k = 0; k < ROWS; ++k) {
-                const float2 x = k < nr ? __ldcs(xi + (int64_t)(r0 + k) * n_col + j) : make_float2(0.f, 0.f);
-                df_fma(acc[k][0], x, f0);
-                df_fma(acc[k][1], x, f1);
-                df_fma(acc[k][2], x, f2);
-            }
+        for (int k = 0; k < PAIRS; ++k) {
+            const float2 xh = make_float2(x[k].x, x[k].y), xl = make_float2(x[k].z, x[k].w);
+            const float2 nx = make_float2(-x[k].x, -x[k].y);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) df2_fma(ah[k][d], al[k][d], xh, nx, xl, fh[d], fl[d]);
         }
-    } else if (n_col % 4 == 0) {
-        // float4 loads: a thread takes groups of 4 consecutive columns (rows 16-byte aligned
-        // since n_col % 4 == 0; F of 4 columns is 12 floats, three float4), two groups per
-        // trip, and adds each 8-product FP32 chain into the double-float accumulators
-        const float *xi = static_cast<const float *>(xi_);
-        const float4 *fbb4 = static_cast<const float4 *>(fbb_);
-        const float4 *xr[ROWS];
+    };
+    // four columns per thread and trip: 4 PAIRS 16-byte loads in flight
+    for (; j + 3 * step < c1; j += 4 * step) {
+        float4 x[4][PAIRS];
 #pragma unroll
-        for (int k = 0; k < ROWS; ++k) xr[k] = reinterpret_cast<const float4 *>(xi + (int64_t)(r0 + min(k, nr - 1)) * n_col);
-        const int64_t g1 = c1 / 4;
-        int64_t g = c0 / 4 + threadIdx.x;
-        for (; g + step < g1; g += 2 * step) {
-            float4 x[2][ROWS];
+        for (int u = 0; u < 4; ++u)
 #pragma unroll
-            for (int u = 0; u < 2; ++u)
+            for (int k = 0; k < PAIRS; ++k)
+                x[u][k] = k < np ? __ldcs(xr[k] + j + u * step) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-                for (int k = 0; k < ROWS; ++k) x[u][k] = __ldcs(xr[k] + g + u * step);
-            float f[2][12];
+        for (int u = 0; u < 4; ++u) column(x[u], j + u * step);
+    }
+    for (; j < c1; j += step) {
+        float4 x[PAIRS];
 #pragma unroll
-            for (int u = 0; u < 2; ++u)
-#pragma unroll
-                for (int v = 0; v < 3; ++v) {
-                    const float4 t = __ldg(fbb4 + 3 * (g + u * step) + v);
-                    f[u][4 * v] = t.x;
-                    f[u][4 * v + 1] = t.y;
-                    f[u][4 * v + 2] = t.z;
-                    f[u][4 * v + 3] = t.w;
-                }
-#pragma unroll
-            for (int k = 0; k < ROWS; ++k)
-#pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    float c = x[0][k].x * f[0][d];
-                    c = fmaf(x[0][k].y, f[0][3 + d], c);
-                    c = fmaf(x[0][k].z, f[0][6 + d], c);
-                    c = fmaf(x[0][k].w, f[0][9 + d], c);
-                    c = fmaf(x[1][k].x, f[1][d], c);
-                    c = fmaf(x[1][k].y, f[1][3 + d], c);
-                    c = fmaf(x[1][k].z, f[1][6 + d], c);
-                    c = fmaf(x[1][k].w, f[1][9 + d], c);
-                    if (k < nr) df_add1(acc[k][d], c);
-                }
-        }
-        for (; g < g1; g += step) {
-            float4 x[ROWS];
-#pragma unroll
-            for (int k = 0; k < ROWS; ++k) x[k] = __ldcs(xr[k] + g);
-            float f[12];
-#pragma unroll
-            for (int v = 0; v < 3; ++v) {
-                const float4 t = __ldg(fbb4 + 3 * g + v);
-                f[4 * v] = t.x;
-                f[4 * v + 1] = t.y;
-                f[4 * v + 2] = t.z;
-                f[4 * v + 3] = t.w;
-            }
-#pragma unroll
-            for (int k = 0; k < ROWS; ++k)
-#pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    float c = x[k].x * f[d];
-                    c = fmaf(x[k].y, f[3 + d], c);
-                    c = fmaf(x[k].z, f[6 + d], c);
-                    c = fmaf(x[k].w, f[9 + d], c);
-                    if (k < nr) df_add1(acc[k][d], c);
-                }
-        }
-    } else {
-        const float *xi = static_cast<const float *>(xi_);
-        const float *fbb = static_cast<const float *>(fbb_);
-        for (; j + (kChain - 1) * step < c1; j += kChain * step) {
-            float x[kChain][ROWS], f[kChain][3];
-#pragma unroll
-            for (int u = 0; u < kChain; ++u)
-#pragma unroll
-                for (int k = 0; k < ROWS; ++k)
-                    x[u][k] = k < nr ? __ldcs(xi + (int64_t)(r0 + k) * n_col + j + u * step) : 0.f;
-#pragma unroll
-            for (int u = 0; u < kChain; ++u)
-#pragma unroll
-                for (int d = 0; d < 3; ++d) f[u][d] = __ldg(fbb + (j + u * step) * 3 + d);
-#pragma unroll
-            for (int k = 0; k < ROWS; ++k)
-#pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    float c = x[0][k] * f[0][d];
-#pragma unroll
-                    for (int u = 1; u < kChain; ++u) c = fmaf(x[u][k], f[u][d], c);
-                    df_add1(acc[k][d], c);
-                }
-        }
-        for (; j < c1; j += step) {
-            const float *f = fbb + j * 3;
-            const float f0 = __ldg(f), f1 = __ldg(f + 1), f2 = __ldg(f + 2);
-#pragma unroll
-            for (int k = 0; k < ROWS; ++k) {
-                const float x = k < nr ? __ldcs(xi + (int64_t)(r0 + k) * n_col + j) : 0.f;
-                df_add1(acc[k][0], x * f0);
-                df_add1(acc[k][1], x * f1);
-                df_add1(acc[k][2], x * f2);
-            }
-        }
+        for (int k = 0; k < PAIRS; ++k) x[k] = k < np ? __ldcs(xr[k] + j) : make_float4(0.f, 0.f, 0.f, 0.f);
+        column(x, j);
     }
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
-    for (int k = 0; k < ROWS; ++k)
+    for (int k = 0; k < 2 * PAIRS; ++k)
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            float2 v = acc[k][d];
+            const float2 hp = ah[k / 2][d], lp = al[k / 2][d];
+            float2 v = (k & 1) ? make_float2(hp.y, lp.y) : make_float2(hp.x, lp.x);
             for (int o = 16; o > 0; o >>= 1) {
                 float2 u;
                 u.x = __shfl_down_sync(0xffffffffu, v.x, o);
@@ -702,10 +596,9 @@ cudaError_t launch_sym_tile(const MeshDev &m, const OrbitDev &o, int32_t n_row, 
 }
 
 // foldout (kappa.f90:382-404): F of every full-mesh point from its irreducible point,
-// Fbb(q, b) = sign(op) * R_|op| Fn(irr(q), b), one thread per (q, b).
-template <bool DF>
+// Fbb(q, b) = sign(op) * R_|op| Fn(irr(q), b) as double-float pairs, one thread per (q, b).
 __global__ void k_foldout(int32_t n_full, int32_t n_mode, const int32_t *full_op, const int32_t *full_irr,
-                          const double *op_cart, const double *fn, void *fbb, const int32_t *skip) {
+                          const double *op_cart, const double *fn, float2 *fbb, const int32_t *skip) {
     if (skip && *skip) return;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (int64_t)n_full * n_mode) return;
@@ -714,39 +607,27 @@ __global__ void k_foldout(int32_t n_full, int32_t n_mode, const int32_t *full_op
     const double *m = op_cart + 9 * (abs(iop) - 1);
     const double *v = fn + ((int64_t)full_irr[iq] * n_mode + b) * 3;
     const double sg = iop > 0 ? 1.0 : -1.0;
-    for (int d = 0; d < 3; ++d) {
-        const double y = sg * (m[d] * v[0] + m[d + 3] * v[1] + m[d + 6] * v[2]);
-        if constexpr (DF)
-            static_cast<float2 *>(fbb)[i * 3 + d] = split_df(y);
-        else
-            static_cast<float *>(fbb)[i * 3 + d] = round_f32(y);
-    }
+    for (int d = 0; d < 3; ++d) fbb[i * 3 + d] = split_df(sg * (m[d] * v[0] + m[d + 3] * v[1] + m[d + 6] * v[2]));
 }
 
 cudaError_t launch_foldout(int32_t n_full, int32_t n_mode, const int32_t *full_op, const int32_t *full_irr,
-                           const double *op_cart, const double *fn, bool df, void *fbb, cudaStream_t s,
-                           const int32_t *skip) {
+                           const double *op_cart, const double *fn, float2 *fbb, cudaStream_t s, const int32_t *skip) {
     const int64_t n = (int64_t)n_full * n_mode;
     if (n <= 0) return cudaSuccess;
-    if (df)
-        k_foldout<true><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n_full, n_mode, full_op, full_irr, op_cart, fn, fbb,
-                                                                     skip);
-    else
-        k_foldout<false><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n_full, n_mode, full_op, full_irr, op_cart, fn,
-                                                                      fbb, skip);
+    k_foldout<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n_full, n_mode, full_op, full_irr, op_cart, fn, fbb, skip);
     return cudaGetLastError();
 }
 
 size_t xi_gemv_part_elems(int32_t n_row) { return (size_t)n_row * kGemvMaxSplit * 3; }
 
-cudaError_t launch_split_xi(const double *xi, int64_t n, bool df, void *out, cudaStream_t s) {
-    if (n <= 0) return cudaSuccess;
-    const int64_t blocks = (n + 255) / 256;
-    const unsigned g = (unsigned)(blocks < 65536 ? blocks : 65536);
-    if (df)
-        k_split_xi<true><<<g, 256, 0, s>>>(xi, n, out);
-    else
-        k_split_xi<false><<<g, 256, 0, s>>>(xi, n, out);
+size_t xi_pairs_elems(int32_t n_row, int64_t n_col) { return (size_t)((n_row + 1) / 2) * (size_t)n_col; }
+
+cudaError_t launch_split_xi(const double *xi, int32_t n_row, int64_t n_col, float4 *out, cudaStream_t s) {
+    if (n_row <= 0 || n_col <= 0) return cudaSuccess;
+    const int n_pair = (n_row + 1) / 2;
+    const int64_t bx = (n_col + 255) / 256;
+    dim3 grid((unsigned)(bx < 64 ? bx : 64), (unsigned)(n_pair < 65535 ? n_pair : 65535));
+    k_split_xi<<<grid, 256, 0, s>>>(xi, n_row, n_col, out);
     return cudaGetLastError();
 }
 
@@ -757,7 +638,7 @@ int xi_gemv_max_split(int64_t n_col) {
     return (int)(k < 1 ? 1 : (k > kGemvMaxSplit ? kGemvMaxSplit : k));
 }
 
-cudaError_t launch_xi_gemv(const void *xi, int32_t n_row, int64_t n_col, bool df, const void *fbb, double *part,
+cudaError_t launch_xi_gemv(const float4 *xi, int32_t n_row, int64_t n_col, const float2 *fbb, double *part,
                            double *buf, int n_sm, cudaStream_t s, const int32_t *skip, int shape) {
     if (n_row <= 0) return cudaSuccess;
     // shape = rows per CTA * 100 + column ranges; 0: 4 rows and the default split
@@ -766,14 +647,10 @@ cudaError_t launch_xi_gemv(const void *xi, int32_t n_row, int64_t n_col, bool df
     if (split <= 0) split = gemv_split(n_row, n_col, n_sm);
     split = std::min(split, xi_gemv_max_split(n_col));
     dim3 grid((unsigned)((n_row + rows - 1) / rows), (unsigned)split);
-    if (df && rows == 8)
-        k_xi_gemv<true, 8><<<grid, 256, 0, s>>>(xi, n_row, n_col, fbb, part, skip);
-    else if (df)
-        k_xi_gemv<true, 4><<<grid, 256, 0, s>>>(xi, n_row, n_col, fbb, part, skip);
-    else if (rows == 8)
-        k_xi_gemv<false, 8><<<grid, 256, 0, s>>>(xi, n_row, n_col, fbb, part, skip);
+    if (rows == 8)
+        k_xi_gemv<4><<<grid, 256, 0, s>>>(xi, n_row, n_col, fbb, part, skip);
     else
-        k_xi_gemv<false, 4><<<grid, 256, 0, s>>>(xi, n_row, n_col, fbb, part, skip);
+        k_xi_gemv<2><<<grid, 256, 0, s>>>(xi, n_row, n_col, fbb, part, skip);
     k_xi_reduce<<<(n_row * 3 + 255) / 256, 256, 0, s>>>(part, n_row, split, buf, skip);
     return cudaGetLastError();
 }

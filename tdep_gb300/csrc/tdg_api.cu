@@ -241,7 +241,8 @@ struct tdg_ctx {
     DevBuf<unsigned char> d_scr4;
     // BTE buffers
     DevBuf<double> d_buf, d_part;
-    DevBuf<float2> d_fbb, d_xi_df;  // F and Xi as double-float pairs for the BTE product
+    DevBuf<float2> d_fbb;   // F as double-float pairs for the BTE product
+    DevBuf<float4> d_xi_df;  // Xi as double-float row pairs (launch_split_xi)
     // state of the last tdg_scattering that the adjoint pass reuses
     PhononDev last_ph{};
     RowsDev last_rows{};
@@ -277,7 +278,7 @@ struct tdg_ctx {
     int last_ln_tune = 324;  // its launch shape (delta row block * 10 + GEMM stages)
     DevBuf<__nv_bfloat16> d_bmat_t;  // transposed real-split matrices (adjoint)
     DevBuf<float> d_ghi, d_glo;      // double-float gradient accumulator (large-cell adjoint)
-    int xi_fmt = -1;  // d_xi_df holds the current Xi as float pairs (1), floats (0), or nothing (-1)
+    int xi_fmt = -1;  // d_xi_df holds the current Xi (1) or nothing (-1)
     // off-diagonal kappa inputs (host copies; uploaded by the first tdg_kappa_offdiag)
     std::vector<double> irr_dyngrad, atom_shift, q_full;
     std::vector<int32_t> op_fmap;
@@ -1827,13 +1828,12 @@ extern "C" int tdg_kappa(tdg_ctx *c, const tdg_opts *o, int32_t maxiter, double 
         const int64_t ncol = (int64_t)N * n;
         const size_t nfn = (size_t)nirr * n * 3, nbuf = (size_t)nr * 3;
         CUDA_TRY(c->d_fbb.alloc((size_t)ncol * 3));
-        // element format of the Xi.F products: float pairs for FP64 and mixed runs (see
-        // k_xi_gemv: with floats the mixed iteration does not pass the convergence test)
-        const bool df = true;
-        if (c->xi_fmt != (int)df) {
-            CUDA_TRY(c->d_xi_df.alloc(df ? (size_t)nr * ncol : ((size_t)nr * ncol + 1) / 2));
-            CUDA_TRY(launch_split_xi(c->d_xi.p, (int64_t)nr * ncol, df, c->d_xi_df.p, s));
-            c->xi_fmt = (int)df;
+        // the Xi.F products take Xi as double-float row pairs (k_xi_gemv; floats fail the
+        // mixed iteration's convergence test)
+        if (c->xi_fmt != 1) {
+            CUDA_TRY(c->d_xi_df.alloc(xi_pairs_elems(nr, ncol)));
+            CUDA_TRY(launch_split_xi(c->d_xi.p, nr, ncol, c->d_xi_df.p, s));
+            c->xi_fmt = 1;
         }
         CUDA_TRY(c->d_buf.alloc(nbuf));
         CUDA_TRY(c->d_part.alloc(xi_gemv_part_elems(nr)));
@@ -1890,8 +1890,7 @@ extern "C" int tdg_kappa(tdg_ctx *c, const tdg_opts *o, int32_t maxiter, double 
         // column split of the Xi products, autotuned per problem size on F0's foldout
         int split = 0;
         {
-            CUDA_TRY(launch_foldout(N, n, c->d_full_op.p, c->d_full_irr.p, c->d_op_cart.p, c->d_fn.p, df, c->d_fbb.p,
-                                    s));
+            CUDA_TRY(launch_foldout(N, n, c->d_full_op.p, c->d_full_irr.p, c->d_op_cart.p, c->d_fn.p, c->d_fbb.p, s));
             // shapes: rows per CTA (4, 8) * 100 + column ranges (the default, twice it)
             const int s0 = xi_gemv_default_split(nr, ncol, c->n_sm), smax = xi_gemv_max_split(ncol);
             std::vector<int> cand;
@@ -1900,21 +1899,21 @@ extern "C" int tdg_kappa(tdg_ctx *c, const tdg_opts *o, int32_t maxiter, double 
                     if (v <= smax && std::find(cand.begin(), cand.end(), rows * 100 + v) == cand.end())
                         cand.push_back(rows * 100 + v);
             std::ostringstream key;
-            key << "xigemv/r" << nr << "/c" << ncol;
+            key << "xigemv2/r" << nr << "/c" << ncol;
             bool tuned = false;
-            CUDA_TRY(tune_pick(tune_key(key.str().c_str(), n, df ? 0 : 1, c->device), cand, 400 + s0,
+            CUDA_TRY(tune_pick(tune_key(key.str().c_str(), n, 0, c->device), cand, 400 + s0,
                                [&](int v) {
-                                   return launch_xi_gemv(c->d_xi_df.p, nr, ncol, df, c->d_fbb.p, c->d_part.p,
+                                   return launch_xi_gemv(c->d_xi_df.p, nr, ncol, c->d_fbb.p, c->d_part.p,
                                                          c->d_buf.p, c->n_sm, s, nullptr, v);
                                },
                                s, split, tuned));
         }
         auto iterations = [&](int k) -> cudaError_t {
             for (int j = 0; j < k; ++j) {
-                cudaError_t e = launch_foldout(N, n, c->d_full_op.p, c->d_full_irr.p, c->d_op_cart.p, c->d_fn.p, df,
+                cudaError_t e = launch_foldout(N, n, c->d_full_op.p, c->d_full_irr.p, c->d_op_cart.p, c->d_fn.p,
                                                c->d_fbb.p, s, done);
                 if (e == cudaSuccess)
-                    e = launch_xi_gemv(c->d_xi_df.p, nr, ncol, df, c->d_fbb.p, c->d_part.p, c->d_buf.p, c->n_sm, s,
+                    e = launch_xi_gemv(c->d_xi_df.p, nr, ncol, c->d_fbb.p, c->d_part.p, c->d_buf.p, c->n_sm, s,
                                        done, split);
                 if (e == cudaSuccess) e = launch_bte_update(bd, c->d_buf.p, s);
                 if (e != cudaSuccess) return e;
@@ -1926,7 +1925,7 @@ extern "C" int tdg_kappa(tdg_ctx *c, const tdg_opts *o, int32_t maxiter, double 
         for (int it0 = 0; it0 < maxiter; it0 += kBteChunk) {
             const int k = std::min(kBteChunk, maxiter - it0);
             std::ostringstream key;
-            key << k << '/' << df << '/' << split << '/' << std::string(reinterpret_cast<const char *>(&bd), sizeof bd)
+            key << k << '/' << split << '/' << std::string(reinterpret_cast<const char *>(&bd), sizeof bd)
                 << '/'
                 << (const void *)c->d_xi_df.p << (const void *)c->d_fbb.p << (const void *)c->d_part.p
                 << (const void *)c->d_buf.p << (const void *)c->d_fn.p << ncol;

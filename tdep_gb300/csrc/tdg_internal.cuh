@@ -335,15 +335,16 @@ cudaError_t launch_sym_tile(const MeshDev &m, const OrbitDev &o, int32_t n_row, 
 // cotangent w in place, the distribution's active entries given by the raw terms od_raw.
 cudaError_t launch_sym_tile_adjoint(const MeshDev &m, const OrbitDev &o, int32_t n_row, const int32_t *row_q1,
                                     const double *od_raw, double *w, const uint32_t *sbits, cudaStream_t s);
-// K8: buf[r*3+a] = sum_j xi[r, j] * fbb[j*3 + a] on the FP32 pipe; xi and fbb as (hi, lo)
-// float pairs accumulated in double-float when df (FP64 runs), else as floats with FMA chains
-// added into double-float accumulators (mixed precision). launch_split_xi converts the FP64
-// Xi; part: xi_gemv_part_elems(n_row) doubles.
-cudaError_t launch_split_xi(const double *xi, int64_t n, bool df, void *out, cudaStream_t s);
+// K8: buf[r*3+a] = sum_j xi[r, j] * fbb[j*3 + a] on the FP32 pipe, xi and fbb as (hi, lo)
+// float pairs accumulated in double-float. launch_split_xi converts the FP64 Xi into row
+// pairs (xi_pairs_elems(n_row, n_col) float4: hi of rows 2p and 2p + 1, lo of both); part:
+// xi_gemv_part_elems(n_row) doubles.
+size_t xi_pairs_elems(int32_t n_row, int64_t n_col);
+cudaError_t launch_split_xi(const double *xi, int32_t n_row, int64_t n_col, float4 *out, cudaStream_t s);
 size_t xi_gemv_part_elems(int32_t n_row);
 // shape: rows per CTA (4 or 8) * 100 + column ranges per row group (0: 4 rows and a default
 // split sized for about two waves).
-cudaError_t launch_xi_gemv(const void *xi, int32_t n_row, int64_t n_col, bool df, const void *fbb, double *part,
+cudaError_t launch_xi_gemv(const float4 *xi, int32_t n_row, int64_t n_col, const float2 *fbb, double *part,
                            double *buf, int n_sm, cudaStream_t s, const int32_t *skip = nullptr, int shape = 0);
 int xi_gemv_default_split(int32_t n_row, int64_t n_col, int n_sm);
 int xi_gemv_max_split(int64_t n_col);
@@ -355,9 +356,9 @@ cudaError_t launch_mma_check(int variant, int n, const float *a, const float *b,
 
 // foldout of the BTE: fbb[(q*n + b)*3 + d] = sign * (R fn[(irr(q)*n + b)*3 ..])_d, with
 // full_op signed 1-based operations (negative: time reversal) and full_irr 0-based; stored
-// as (hi, lo) float pairs when df, else as floats (the Xi.F element format).
+// as (hi, lo) float pairs (the Xi.F element format).
 cudaError_t launch_foldout(int32_t n_full, int32_t n_mode, const int32_t *full_op, const int32_t *full_irr,
-                           const double *op_cart, const double *fn, bool df, void *fbb, cudaStream_t s,
+                           const double *op_cart, const double *fn, float2 *fbb, cudaStream_t s,
                            const int32_t *skip = nullptr);
 
 // Device state of the BTE iteration (kappa.f90:326-495): the iteration counter, the mixing

@@ -60,8 +60,24 @@ _FIELDS_I32 = {
 _SCALARS = ("n_atom", "n_mode", "n_op", "n_full", "n_irr", "n_fc3", "n_fc4")
 
 
+class _LoadedProblem:
+    """Owner of a tdg_problem the library allocated: freed (tdg_problem_free) when the last
+    array viewing its memory is gone."""
+
+    def __init__(self, ptr):
+        self.ptr = ptr
+
+    def __del__(self):
+        try:
+            N.lib().tdg_problem_free(self.ptr)
+        except Exception:
+            pass
+
+
 class Problem:
-    """Numpy-owned tdg_problem. Arrays use the C-ABI layouts (see include/tdep_gb300.h)."""
+    """tdg_problem with numpy arrays in the C-ABI layouts (see include/tdep_gb300.h). A loaded
+    problem's arrays view the library's memory (no copy); the library's problem lives as long
+    as any of them."""
 
     def __init__(self, **kw):
         for k in _SCALARS:
@@ -93,13 +109,12 @@ class Problem:
             N.check(L.tdg_problem_load(*args, C.byref(out)), "tdg_problem_load")
         else:
             N.check(L.tdg_problem_load_device(*args, int(device), C.byref(out)), "tdg_problem_load_device")
-        try:
-            return cls.from_struct(out.contents)
-        finally:
-            L.tdg_problem_free(out)
+        owner = _LoadedProblem(out)
+        return cls.from_struct(out.contents, owner)
 
     @classmethod
-    def from_struct(cls, s: N.TdgProblem) -> "Problem":
+    def from_struct(cls, s: N.TdgProblem, owner=None) -> "Problem":
+        """The arrays of s, copied, or (owner: the object that frees s) viewed in place."""
         kw = {k: getattr(s, k) for k in _SCALARS}
         for k in ("latvec", "reclat", "inv_reclat"):
             kw[k] = np.array(getattr(s, k)[:], dtype=np.float64)
@@ -107,10 +122,18 @@ class Problem:
         kw["grid"] = np.array(s.grid[:], dtype=np.int32)
         dims = dict(kw)
         for table, ct in ((_FIELDS_F64, np.float64), (_FIELDS_I32, np.int32)):
+            cty = C.c_double if ct is np.float64 else C.c_int32
             for k, shp in table.items():
                 n = int(np.prod([dims[x] if isinstance(x, str) else x for x in shp]))
                 p = getattr(s, k)
-                kw[k] = np.ctypeslib.as_array(p, shape=(n,)).copy() if (n > 0 and p) else np.zeros(n, dtype=ct)
+                if n == 0 or not p:
+                    kw[k] = np.zeros(n, dtype=ct)
+                elif owner is None:
+                    kw[k] = np.ctypeslib.as_array(p, shape=(n,)).copy()
+                else:
+                    buf = (cty * n).from_address(C.cast(p, C.c_void_p).value)
+                    buf._owner = owner  # the arrays keep the library's problem alive
+                    kw[k] = np.ctypeslib.as_array(buf)
         return cls(**kw)
 
     def fc3_irreducible(self):
