@@ -187,10 +187,15 @@ class OracleProblem:
         self.rrot = rrot
 
         def index_of(v):
-            w = np.round(v * g).astype(int) % g
-            return (w[:, 0] * g[1] + w[:, 1]) * g[2] + w[:, 2]
+            # mesh index of each fractional point, -1 where it is not on the mesh (an
+            # operation that does not map a mesh with unequal dimensions onto itself)
+            x = v * g
+            w = np.round(x).astype(int)
+            on = np.all(np.abs(x - w) < 1e-6, axis=1)
+            w = w % g
+            return np.where(on, (w[:, 0] * g[1] + w[:, 1]) * g[2] + w[:, 2], -1)
 
-        imgs = np.stack([index_of(ijk @ R.T / g * 1.0) for R in rrot], 1)  # [N, nop]
+        imgs = np.stack([index_of((ijk / g) @ R.T) for R in rrot], 1)  # [N, nop]
         self.imgs = imgs
         rev = index_of(-(ijk / g)) if timereversal else None
         irr_of = np.full(N, -1)
@@ -200,9 +205,9 @@ class OracleProblem:
                 continue
             k = len(irr_list)
             irr_list.append(i)
-            orbit = set(imgs[i].tolist())
+            orbit = set(x for x in imgs[i].tolist() if x >= 0)
             if timereversal:
-                orbit |= set(rev[imgs[i]].tolist())
+                orbit |= set(rev[list(orbit)].tolist())
             for j in orbit:
                 if irr_of[j] < 0:
                     irr_of[j] = k
@@ -293,17 +298,22 @@ class OracleProblem:
         gi = np.round(self.gfrac * g).astype(int)
 
         def index_of(v):
-            w = np.round(v).astype(int) % g
+            # mesh index of the fractional point v, -1 off the mesh
+            x = v * g
+            w = np.round(x).astype(int)
+            if np.any(np.abs(x - w) > 1e-6):
+                return -1
+            w = w % g
             return (w[0] * g[1] + w[1]) * g[2] + w[2]
 
         for k, i in enumerate(self.irr_full):
             for j, R in enumerate(self.rrot):
-                t = index_of(R @ gi[i])
-                if full_op[t] == 0 and self.full_irr[t] == k:
+                t = index_of(R @ (gi[i] / g))
+                if t >= 0 and full_op[t] == 0 and self.full_irr[t] == k:
                     full_op[t] = j + 1
             for j, R in enumerate(self.rrot):
-                t = index_of(-(R @ gi[i]))
-                if full_op[t] == 0 and self.full_irr[t] == k:
+                t = index_of(-(R @ (gi[i] / g)))
+                if t >= 0 and full_op[t] == 0 and self.full_irr[t] == k:
                     full_op[t] = -(j + 1)
         irr_ops = np.zeros((nirr, nop), int)
         for k, i in enumerate(self.irr_full):

@@ -1,66 +1,14 @@
 // Gamma-centred FFT q-mesh with its irreducible wedge, the map from every point to the
 // wedge and the little groups of the irreducible points.
 // Follows type_qpointmesh_gridgeneration.f90:8-545 (build_grid for lo_fft_mesh),
-// :612-680 (on-grid test, index from coordinate) and type_qpointmesh.f90:660-700
-// (lo_get_small_group_of_qpoint).
+// :612-680 (on-grid test, index from coordinate; here exact, on integer coordinates) and
+// type_qpointmesh.f90:660-700 (lo_get_small_group_of_qpoint).
 #include <algorithm>
+#include <numeric>
 
 #include "crystal.hpp"
 
 namespace tdg {
-
-namespace {
-
-// lo_clean_fractional_coordinates (gottochblandat.f90:1261-1283) with tol = lo_sqtol.
-double clean_frac(double x) {
-    double y = x;
-    for (int guard = 0; guard < 64; ++guard) {
-        if (std::fabs(y) < kSqTol) y = 0.0;
-        if (std::fabs(y - 1.0) < kSqTol) y = 0.0;
-        if (y > 1.0) y -= 1.0;
-        if (y < 0.0) y += 1.0;
-        if (y > -kSqTol && y < 1.0) break;
-    }
-    return y;
-}
-
-bool on_grid(const int g[3], const V3 &r) {
-    double s = 0;
-    for (int j = 0; j < 3; ++j) {
-        const double v = r[j] * g[j] + 1.0;
-        s += std::fabs(v - anint(v));
-    }
-    return s < kTol;
-}
-
-// 1-based linear index of a fractional coordinate on the grid.
-int index_from_coordinate(const int g[3], const V3 &r) {
-    int gi[3];
-    for (int j = 0; j < 3; ++j) {
-        const double v = clean_frac(r[j]) * g[j] + 1.0;
-        gi[j] = (int)anint(v);
-    }
-    for (int j = 0; j < 3; ++j) {
-        if (gi[j] > g[j]) gi[j] -= g[j];
-        if (gi[j] < 1) gi[j] += g[j];
-    }
-    return (gi[0] - 1) * g[1] * g[2] + (gi[1] - 1) * g[2] + gi[2];
-}
-
-V3 apply_int(const int32_t *m, const V3 &v, double sign) {
-    V3 r;
-    for (int i = 0; i < 3; ++i) r[i] = sign * (m[i] * v[0] + m[i + 3] * v[1] + m[i + 6] * v[2]);
-    return r;
-}
-
-void inverse_int(const int32_t *m, int32_t *inv) {
-    M3 a;
-    for (int k = 0; k < 9; ++k) a.a[k] = m[k];
-    M3 b = inverse(a);
-    for (int k = 0; k < 9; ++k) inv[k] = (int32_t)anint(b.a[k]);
-}
-
-}  // namespace
 
 int build_fft_mesh(const Crystal &c, const int grid[3], bool timereversal, QMesh &qp) {
     for (int i = 0; i < 3; ++i)
@@ -69,61 +17,99 @@ int build_fft_mesh(const Crystal &c, const int grid[3], bool timereversal, QMesh
     const int np = grid[0] * grid[1] * grid[2];
     const int nsym = (int)c.ops.size();
     qp.n_full = np;
+    PhaseTimer pt("mesh");
 
     // Points in fractional coordinates, moved to the first zone. The zone test uses the
     // shortest Cartesian vector among the 27 nearest reciprocal lattice translations,
     // with lo_degenvector breaking ties predictably.
     qp.qfrac.assign(np, V3());
-    for (int i = 1, l = 0; i <= grid[0]; ++i)
-        for (int j = 1; j <= grid[1]; ++j)
-            for (int k = 1; k <= grid[2]; ++k, ++l) {
-                V3 v0;
-                v0[0] = (i - 1.0) / grid[0];
-                v0[1] = (j - 1.0) / grid[1];
-                v0[2] = (k - 1.0) / grid[2];
-                double best = 1e300;
-                V3 bv = v0;
-                for (int a = -1; a <= 1; ++a)
-                    for (int b = -1; b <= 1; ++b)
-                        for (int cc = -1; cc <= 1; ++cc) {
-                            V3 w;
-                            w[0] = v0[0] - a;
-                            w[1] = v0[1] - b;
-                            w[2] = v0[2] - cc;
-                            V3 kc = mul(c.reclat, w);
-                            for (int d = 0; d < 3; ++d) kc[d] += kDegenVector[d];
-                            const double s = sqnorm(kc);
-                            if (s < best - 1e-12) {
-                                best = s;
-                                bv = w;
-                            }
-                        }
-                qp.qfrac[l] = bv;
-            }
+    // the same points as integers: qfrac = nq / g exactly
+    std::vector<int32_t> nq((size_t)np * 3);
+    parallel_for(np, [&](int64_t l) {  // point l = ((i - 1) g1 + j - 1) g2 + k - 1
+        const int k = (int)(l % grid[2]) + 1, j = (int)((l / grid[2]) % grid[1]) + 1,
+                  i = (int)(l / ((int64_t)grid[1] * grid[2])) + 1;
+        V3 v0;
+        v0[0] = (i - 1.0) / grid[0];
+        v0[1] = (j - 1.0) / grid[1];
+        v0[2] = (k - 1.0) / grid[2];
+        double best = 1e300;
+        V3 bv = v0;
+        int sh[3] = {0, 0, 0};
+        for (int a = -1; a <= 1; ++a)
+            for (int b = -1; b <= 1; ++b)
+                for (int cc = -1; cc <= 1; ++cc) {
+                    V3 w;
+                    w[0] = v0[0] - a;
+                    w[1] = v0[1] - b;
+                    w[2] = v0[2] - cc;
+                    V3 kc = mul(c.reclat, w);
+                    for (int d = 0; d < 3; ++d) kc[d] += kDegenVector[d];
+                    const double s = sqnorm(kc);
+                    if (s < best - 1e-12) {
+                        best = s;
+                        bv = w;
+                        sh[0] = a;
+                        sh[1] = b;
+                        sh[2] = cc;
+                    }
+                }
+        qp.qfrac[l] = bv;
+        nq[(size_t)l * 3] = i - 1 - sh[0] * grid[0];
+        nq[(size_t)l * 3 + 1] = j - 1 - sh[1] * grid[1];
+        nq[(size_t)l * 3 + 2] = k - 1 - sh[2] * grid[2];
+    });
 
+    pt.mark("first zone");
     // Connections: op j maps point i to point connections[i][j] (time reversal: -index).
+    // The reference tests in fractional coordinates whether R q is on the mesh and whether
+    // R^-1 maps its image back onto q. On integer coordinates the first test is exact:
+    // (R q)_i = sum_k R_ik n_k / g_k is on the mesh when num_i = sum_k R_ik n_k (L / g_k), L
+    // the least common multiple of the g_k, is a multiple of L / g_i; the second test then
+    // always holds (R^-1 is an integer matrix and maps the image's mesh point, which differs
+    // from R q by a reciprocal lattice vector, back onto q's).
     const int nc = timereversal ? 2 * nsym : nsym;
     std::vector<int> conn((size_t)np * nc, 0);
-    std::vector<int32_t> irfm(9 * nsym);
-    for (int j = 0; j < nsym; ++j) inverse_int(c.ops[j].rfm, &irfm[9 * j]);
-    // rows are independent: all host threads (54 ms for 24^3 and 48 operations on one core)
+    int64_t L = grid[0];
+    for (int d = 1; d < 3; ++d) L = L / std::gcd(L, (int64_t)grid[d]) * grid[d];
+    const int64_t sg3[3] = {L / grid[0], L / grid[1], L / grid[2]};
+    // rows are independent: all host threads. With equal dimensions (L / g = 1) every image
+    // is on the mesh and the wrap needs no division.
+    const bool equal = sg3[0] == 1 && sg3[1] == 1 && sg3[2] == 1;
     parallel_for(np, [&](int64_t i) {
-        const V3 &v0 = qp.qfrac[i];
-        for (int tr = 0; tr < (timereversal ? 2 : 1); ++tr) {
-            const double sg = tr ? -1.0 : 1.0;
-            for (int j = 0; j < nsym; ++j) {
-                V3 v1 = apply_int(c.ops[j].rfm, v0, sg);
-                if (!on_grid(grid, v1)) continue;
-                const int ii = index_from_coordinate(grid, v1);
-                V3 v2 = apply_int(&irfm[9 * j], qp.qfrac[ii - 1], sg);
-                if (!on_grid(grid, v2)) continue;
-                const int jj = index_from_coordinate(grid, v2);
-                if (jj != i + 1) continue;
+        const int32_t *n = &nq[(size_t)i * 3];
+        for (int j = 0; j < nsym; ++j) {
+            const int32_t *m = c.ops[j].rfm;
+            int64_t gi[3];
+            bool on = true;
+            if (equal) {
+                const int g = grid[0];
+                for (int r = 0; r < 3; ++r) {
+                    int v = m[r] * n[0] + m[r + 3] * n[1] + m[r + 6] * n[2];
+                    while (v < 0) v += g;
+                    while (v >= g) v -= g;
+                    gi[r] = v;
+                }
+            } else {
+                for (int r = 0; r < 3 && on; ++r) {
+                    const int64_t num = m[r] * n[0] * sg3[0] + m[r + 3] * n[1] * sg3[1] + m[r + 6] * n[2] * sg3[2];
+                    on = num % sg3[r] == 0;
+                    gi[r] = num / sg3[r];
+                }
+            }
+            if (!on) continue;
+            for (int tr = 0; tr < (timereversal ? 2 : 1); ++tr) {
+                int64_t idx = 0;
+                for (int r = 0; r < 3; ++r) {
+                    const int64_t v = ((tr ? -gi[r] : gi[r]) % grid[r] + grid[r]) % grid[r];
+                    idx = idx * grid[r] + v;
+                }
+                const int ii = (int)idx + 1;
                 conn[(size_t)i * nc + j + tr * nsym] = tr ? -ii : ii;
             }
         }
     });
 
+    pt.mark("connections");
     // Irreducible points: smallest index of every orbit.
     std::vector<int> ind(np, 1);
     for (int i = 0; i < np; ++i)
@@ -172,10 +158,11 @@ int build_fft_mesh(const Crystal &c, const int grid[3], bool timereversal, QMesh
         qp.q_full[i] = r;
     }
 
+    pt.mark("wedge and q");
     // Little groups of the irreducible points (proper operations, no time reversal).
     qp.irr_nop.assign(qp.n_irr, 0);
     qp.irr_ops.assign((size_t)qp.n_irr * nsym, 0);
-    for (int k = 0; k < qp.n_irr; ++k) {
+    parallel_for(qp.n_irr, [&](int64_t k) {
         const V3 &v0 = qp.q_full[qp.irr_full[k] - 1];
         int ctr = 0;
         for (int i = 0; i < nsym; ++i) {
@@ -187,7 +174,8 @@ int build_fft_mesh(const Crystal &c, const int grid[3], bool timereversal, QMesh
             if (sqnorm(f) < kSqTol) qp.irr_ops[(size_t)k * nsym + ctr++] = i + 1;
         }
         qp.irr_nop[k] = ctr;
-    }
+    });
+    pt.mark("little groups");
     return kOk;
 }
 

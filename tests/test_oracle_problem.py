@@ -12,7 +12,10 @@ from tdep_gb300 import Problem
 
 
 @pytest.mark.parametrize("name,grid", [("fcc", (8, 8, 8)), ("rocksalt", (6, 6, 6)), ("perovskite", (4, 4, 4)),
-                                       ("fluorite", (4, 4, 4)), ("l12", (4, 4, 4))])
+                                       ("fluorite", (4, 4, 4)), ("l12", (4, 4, 4)),
+                                       # unequal dimensions: only the operations that map the
+                                       # mesh onto itself connect its points
+                                       ("rocksalt", (6, 5, 4)), ("perovskite", (4, 3, 2))])
 def test_host_stage_against_the_oracle_problem(configs, name, grid):
     p = Problem.load(configs[name], grid, readiso=True)
     o = OracleProblem(configs[name], grid)
