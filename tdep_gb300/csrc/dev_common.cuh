@@ -45,6 +45,28 @@ __device__ __forceinline__ void cfma(C &acc, const C &a, const C &b) {
 
 __device__ __forceinline__ bool nonzero(double x) { return (__double_as_longlong(x) << 1) != 0; }
 
+// om1 - (m2 + m3) from the FP32 pairs omega = h + l (h = the FP32 omega, l the FP32 rest):
+// the sums of the h parts with their exact rounding errors (Knuth's TwoSum, FP32 additions
+// only) plus the l parts. Accurate to about 2^-24 of the difference plus 2^-46 of omega, as
+// the FP64 difference rounded to FP32; no FP64 operation (GB300 issues FP64 at 1/64 of the
+// FP32 rate).
+__device__ __forceinline__ float centre_diff_f32(float h1, float l1, float h2, float l2, float h3, float l3) {
+    const float s = h2 + h3;
+    const float bs = s - h2;
+    const float es = (h2 - (s - bs)) + (h3 - bs);  // h2 + h3 = s + es exactly
+    const float d = h1 - s;
+    const float bd = d - h1;
+    const float ed = (h1 - (d - bd)) + (-s - bd);  // h1 - s = d + ed exactly
+    return d + (ed + ((l1 - l2 - l3) - es));
+}
+
+// |x - y| < lo_freqtol (1e-9) for x = h1 + l1 and y = h2 + l2 given as FP32 (hi, rest)
+// pairs: where the test can hold, h1 - h2 is exact (Sterbenz) and the result is the FP64
+// difference to ~1e-17.
+__device__ __forceinline__ bool close_f32(float h1, float l1, float h2, float l2) {
+    return fabsf((h1 - h2) + (l1 - l2)) < 1e-9f;
+}
+
 // Exclusive scan of one int per thread over the block (blockDim a multiple of 32).
 __device__ __forceinline__ int block_exclusive_scan(int v, int *wsum, int &total) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;

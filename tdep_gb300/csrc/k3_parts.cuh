@@ -26,6 +26,8 @@ struct K3Smem {
     double *R2;            // [n^2] row sums, then Xi row terms
     double *R3;            // [n^2] column sums, then Xi row terms
     double *F;             // [n^3] dense F (zero where no survivor)
+    float *Ff;             // or F in FP32 (the tensor-core forward pass: k3_survivors_f32 and
+                           // k3_sums_scatter with FLOAT_F)
     float *fo1, *fo2, *fo3, *fs1, *fs2, *fs3;
     float *fl1, *fl2, *fl3;  // omega - (double)fo in FP32: omega = fo + fl to about 2^-48
     float *fb2, *fb3, *fw1;  // be2, be3 and wrow in FP32 (the FP32 weights)
@@ -102,13 +104,11 @@ __device__ __forceinline__ void k3_skip_masks(const K3Smem &S) {
     for (int i = tid; i < 3 * N2 + 2 * N; i += bd) {
         if (i < 3 * N2) {
             const int which = i / N2, x = (i % N2) / N, y = i % N;
-            const double *pa = which == 2 ? S.om2 : S.om1;
-            const double *pb = which == 0 ? S.om2 : S.om3;
-            const float *fa = which == 2 ? S.fo2 : S.fo1;
-            const float *fb = which == 0 ? S.fo2 : S.fo3;
+            const float *fa = which == 2 ? S.fo2 : S.fo1, *la = which == 2 ? S.fl2 : S.fl1;
+            const float *fb = which == 0 ? S.fo2 : S.fo3, *lb = which == 0 ? S.fl2 : S.fl3;
             uint32_t *mk = which == 0 ? S.m12 : (which == 1 ? S.m13 : S.m23);
-            // |x - y| < 1e-9 in FP64 needs |fx - fy| below 1e-8 in FP32 at these magnitudes
-            if (fabsf(fa[x] - fb[y]) < 1e-8f && fabs(pa[x] - pb[y]) < kFreqTolD) atomicOr(mk + x, 1u << y);
+            // |x - y| < 1e-9 from the FP32 (hi, rest) frequency pairs (close_f32)
+            if (close_f32(fa[x], la[x], fb[y], lb[y])) atomicOr(mk + x, 1u << y);
         } else {
             const int j = i - 3 * N2, which = j / N, b = j % N;
             const double w = which == 0 ? S.om2[b] : S.om3[b];
@@ -213,28 +213,13 @@ __device__ __forceinline__ void k3_survivors(const K3Smem &S, const PhononDev &P
     }
 }
 
-// om1 - (m2 + m3) from the FP32 pairs omega = h + l (h = the FP32 omega, l the FP32 rest):
-// the sums of the h parts with their exact rounding errors (Knuth's TwoSum, FP32 additions
-// only) plus the l parts. Accurate to about 2^-24 of the difference plus 2^-46 of omega, as
-// the FP64 difference rounded to FP32; no FP64 operation (GB300 issues FP64 at 1/64 of the
-// FP32 rate).
-__device__ __forceinline__ float k3_centre_diff(float h1, float l1, float h2, float l2, float h3, float l3) {
-    const float s = h2 + h3;
-    const float bs = s - h2;
-    const float es = (h2 - (s - bs)) + (h3 - bs);  // h2 + h3 = s + es exactly
-    const float d = h1 - s;
-    const float bd = d - h1;
-    const float ed = (h1 - (d - bd)) + (-s - bd);  // h1 - s = d + ed exactly
-    return d + (ed + ((l1 - l2 - l3) - es));
-}
-
 // The same in FP32 for the mixed-precision kernels: the centre differences om1 - (+-om2 +-
-// om3) from FP32 pairs (k3_centre_diff, as accurate as the FP64 difference rounded to
+// om3) from FP32 pairs (centre_diff_f32, as accurate as the FP64 difference rounded to
 // FP32), the width, the exponent and the Gaussian in FP32 (expf), the occupation factors
 // and row weight from FP32 copies made once per mode, F in FP32 stored as a double for the
 // FP64 sums. Relative error of a weight about 1e-6, against the 1e-5 of the BF16x3
 // contraction.
-template <int N, typename PsiSq>
+template <int N, bool FLOAT_F = false, typename PsiSq>
 __device__ __forceinline__ void k3_survivors_f32(const K3Smem &S, const PhononDev &P, int nq, float perm,
                                                  PsiSq psisq) {
     constexpr int N2 = N * N;
@@ -267,7 +252,7 @@ __device__ __forceinline__ void k3_survivors_f32(const K3Smem &S, const PhononDe
             // Gaussian j centred at (-om2+om3, om2-om3, om2+om3, -om2-om3), get_dirac's order
             const float sg2 = (j == 1 || j == 2) ? 1.f : -1.f;
             const float sg3 = (j == 0 || j == 2) ? 1.f : -1.f;
-            const float dx = k3_centre_diff(h1, l1, sg2 * h2, sg2 * l2, sg3 * h3, sg3 * l3);
+            const float dx = centre_diff_f32(h1, l1, sg2 * h2, sg2 * l2, sg3 * h3, sg3 * l3);
             const float gj = fabsf(dx) > win8 ? 0.f : expf(-dx * dx * h) * cg;
             g[0] = j == 0 ? gj : g[0];
             g[1] = j == 1 ? gj : g[1];
@@ -279,7 +264,10 @@ __device__ __forceinline__ void k3_survivors_f32(const K3Smem &S, const PhononDe
             const float pq = pref * psisq(idx) * S.fw1[b1];
             const float n2 = S.fb2[b2], n3 = S.fb3[b3];
             const float fsum = perm * pq * ((n2 - n3) * d0 + (n2 + n3 + 1.0f) * d1);
-            S.F[idx] = (double)fsum;
+            if constexpr (FLOAT_F)
+                S.Ff[idx] = fsum;
+            else
+                S.F[idx] = (double)fsum;
             if (fsum != 0.f) {
                 atomicOr(S.rowbits + b1 * N + b2, 1u << b3);
                 atomicOr(S.colbits + b1 * N + b3, 1u << b2);
@@ -292,7 +280,7 @@ __device__ __forceinline__ void k3_survivors_f32(const K3Smem &S, const PhononDe
 // sampling row times the nred equivalent triplets, then the Xi row terms 2 F om/om1 added
 // for each equivalent triplet (scattering_threephonon.f90:115-135). Starts and ends with
 // barriers of its own.
-template <int N>
+template <int N, bool FLOAT_F = false>
 __device__ __forceinline__ void k3_sums_scatter(const K3Smem &S, const ThreePhArgs &a, int nred) {
     constexpr int N2 = N * N;
     const int tid = threadIdx.x, bd = blockDim.x;
@@ -301,12 +289,17 @@ __device__ __forceinline__ void k3_sums_scatter(const K3Smem &S, const ThreePhAr
     for (int e = tid; e < 2 * N2; e += bd) {
         double sum = 0.0;
         if (e < N2) {
-            for (uint32_t bits = S.rowbits[e]; bits; bits &= bits - 1) sum += S.F[e * N + __ffs(bits) - 1];
+            for (uint32_t bits = S.rowbits[e]; bits; bits &= bits - 1) {
+                const int i = e * N + __ffs(bits) - 1;
+                sum += FLOAT_F ? (double)S.Ff[i] : S.F[i];
+            }
             S.R2[e] = sum;
         } else {
             const int e3 = e - N2, b1 = e3 / N, b3 = e3 % N;
-            for (uint32_t bits = S.colbits[e3]; bits; bits &= bits - 1)
-                sum += S.F[(b1 * N + __ffs(bits) - 1) * N + b3];
+            for (uint32_t bits = S.colbits[e3]; bits; bits &= bits - 1) {
+                const int i = (b1 * N + __ffs(bits) - 1) * N + b3;
+                sum += FLOAT_F ? (double)S.Ff[i] : S.F[i];
+            }
             S.R3[e3] = sum;
         }
     }

@@ -12,7 +12,7 @@
 //           contracting a (E1), b (E2) and c (E3) the result is Psi[b1][b2][b3]
 //   delta   get_dirac and the accumulation of Gamma and the Xi row terms
 //           (scattering_threephonon.f90:115-135, 219-271): FP32 screen, FP32 Gaussians
-//           and occupation factors from FP64 centre differences, FP64 sums.
+//           and occupation factors from FP32 frequency pairs, FP64 sums.
 // GEMM operands are BF16 hi/lo splits of FP32 values (hi*hi + hi*lo + lo*hi into an FP32
 // tensor-memory accumulator, about 16 significant bits per operand) in shared memory as
 // 8 x 16-byte core matrices without swizzle, both operands MN-major; the layout and the
@@ -450,7 +450,7 @@ struct LnDeltaArgs {
 
 __host__ __device__ inline size_t ln_delta_smem(int n, int bb) {
     return sizeof(double) * ((size_t)14 * n + (size_t)bb * n) + sizeof(uint32_t) * (size_t)bb * n +
-           sizeof(int) * 33 + sizeof(float) * 6 * (size_t)n + 16;
+           sizeof(int) * 33 + sizeof(float) * 8 * (size_t)n + 16;
 }
 
 // ADJ: the adjoint's weights. F holds G_b = lam(row) * nred * dF_b/d|Psi_b|^2 of the
@@ -483,6 +483,7 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
     // FP32 copies for the screen (double -> float conversions run on the FP64 pipe, so they
     // are made once per mode here instead of once per pair); NaN marks omega < 1e-9 Ha.
     float *g2 = (float *)(wsum + 33), *g3 = g2 + n, *t2 = g3 + n, *t3 = t2 + n, *c2 = t3 + n, *c3 = c2 + n;
+    float *l2 = c3 + n, *l3 = l2 + n;  // om - (double)g, the FP32 rest of each frequency
     for (int b = tid; b < n; b += bd) {
         om2[b] = P.omega[(size_t)q2 * n + b];
         om3[b] = P.omega[(size_t)q3 * n + b];
@@ -496,6 +497,8 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
         t3[b] = (float)s3[b];
         c2[b] = (float)be2[b];
         c3[b] = (float)be3[b];
+        l2[b] = om2[b] < kFreqTolD ? 0.f : (float)(om2[b] - (double)g2[b]);
+        l3[b] = om3[b] < kFreqTolD ? 0.f : (float)(om3[b] - (double)g3[b]);
         for (int d = 0; d < 3; ++d) {
             v2[b * 3 + d] = P.vel[((size_t)q2 * n + b) * 3 + d];
             v3[b * 3 + d] = P.vel[((size_t)q3 * n + b) * 3 + d];
@@ -516,6 +519,7 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
     const float pwf = (float)pw;
     const int it = P.integrationtype;
     const float fo1 = (float)o1, fs1 = (float)s1, fsig = (float)P.sigma_fixed;
+    const float fl1 = (float)(o1 - (double)fo1);
     const float2 *psi = a.psi + ((int64_t)s * n + b1) * n * n;
     // 4-bit live mask of the Gaussians of pair (b2, b3), 0 when a skip rule applies
     // (scattering_threephonon.f90:90-101) or no Gaussian can reach its window. FP64 work
@@ -523,10 +527,12 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
     auto screen = [&](int b2, int b3) -> uint32_t {
         const float f2 = g2[b2], f3 = g3[b3];
         if (f2 != f2 || f3 != f3) return 0u;  // omega2 or omega3 below 1e-9 Ha
-        // |x - y| < 1e-9 in FP64 needs |fx - fy| below 1e-8 in FP32 at these magnitudes
-        if (fabsf(fo1 - f2) < 1e-8f && fabs(o1 - om2[b2]) < kFreqTolD) return 0u;
-        if (fabsf(fo1 - f3) < 1e-8f && fabs(o1 - om3[b3]) < kFreqTolD) return 0u;
-        if (fabsf(f2 - f3) < 1e-8f && fabs(om2[b2] - om3[b3]) < kFreqTolD) return 0u;
+        // |x - y| < 1e-9 from the FP32 (hi, rest) pairs: the hi difference is exact where it
+        // matters (Sterbenz), so the test is the FP64 one to ~1e-17; no FP64 instruction (a
+        // short-circuit FP64 test is evaluated for every pair once the compiler if-converts it)
+        if (close_f32(fo1, fl1, f2, l2[b2])) return 0u;
+        if (close_f32(fo1, fl1, f3, l3[b3])) return 0u;
+        if (close_f32(f2, l2[b2], f3, l3[b3])) return 0u;
         if (it == 6) return 15u;  // the velocity-difference width can cancel in FP32: not screened
         const float sg = it == 1 ? fsig : sqrtf(fs1 + t2[b2] + t3[b3]);
         const float win = 8.0f * sg * 1.001f + 1e-6f * (fo1 + f2 + f3);
@@ -554,14 +560,15 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
         }
         __syncthreads();
         // (B) delta weights and occupations of the survivors, full warps: the Gaussians and
-        // occupation factors in FP32 from FP64 centre differences (the path is mixed
-        // precision; GB300 issues FP64 at 1/64 of the FP32 rate), the sums in FP64
+        // occupation factors in FP32, the centre differences from FP32 (hi, rest) frequency
+        // pairs (the path is mixed precision; GB300 issues FP64 at 1/64 of the FP32 rate, and
+        // an FP64 warp instruction holds its pipe for 16 cycles whatever its active lanes),
+        // the sums in FP64
         for (int i = tid; i < total; i += bd) {
             const uint32_t qv = Q[i];
             const int e = (int)(qv & 0xffffu);
             uint32_t live = qv >> 16;
             const int b2 = bb + e / n, b3 = e % n;
-            const double o2 = om2[b2], o3 = om3[b3];
             float sigma;
             if (it == 1) {
                 sigma = fsig;
@@ -575,13 +582,15 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
             const float invsig = 1.0f / sigma;
             const float win8 = 8.0f * sigma, h = 0.5f * invsig * invsig, cg = kSqrt2PiInvF * invsig;
             float gs[4] = {0.f, 0.f, 0.f, 0.f};
+            const float h2 = g2[b2], r2 = l2[b2], h3 = g3[b3], r3 = l3[b3];
             while (live) {
                 const int j = __ffs(live) - 1;
                 live &= live - 1;
-                // Gaussian j centred at (-om2+om3, om2-om3, om2+om3, -om2-om3), get_dirac's order
-                const double m2 = (j == 1 || j == 2) ? o2 : -o2;
-                const double m3 = (j == 0 || j == 2) ? o3 : -o3;
-                const float dx = (float)(o1 - (m2 + m3));
+                // Gaussian j centred at (-om2+om3, om2-om3, om2+om3, -om2-om3), get_dirac's
+                // order; the centre difference from the FP32 (hi, rest) pairs, no FP64
+                const float sg2 = (j == 1 || j == 2) ? 1.f : -1.f;
+                const float sg3 = (j == 0 || j == 2) ? 1.f : -1.f;
+                const float dx = centre_diff_f32(fo1, fl1, sg2 * h2, sg2 * r2, sg3 * h3, sg3 * r3);
                 const float gj = fabsf(dx) > win8 ? 0.f : expf(-dx * dx * h) * cg;
                 gs[0] = j == 0 ? gj : gs[0];
                 gs[1] = j == 1 ? gj : gs[1];

@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
     K3Smem S;
     S.om1 = om1; S.om2 = om2; S.om3 = om3; S.inv1 = inv1; S.be2 = be2; S.be3 = be3;
     S.s1 = s1; S.s2 = s2; S.s3 = s3; S.v1 = v1; S.v2 = v2; S.v3 = v3; S.wrow = wrow;
-    S.R2 = R2; S.R3 = (double *)B; S.F = (double *)A;
+    S.R2 = R2; S.R3 = (double *)B; S.F = (double *)A; S.Ff = nullptr;
     S.fo1 = fo1; S.fo2 = fo2; S.fo3 = fo3; S.fs1 = fs1; S.fs2 = fs2; S.fs3 = fs3;
     S.fl1 = fs3 + N; S.fl2 = fs3 + 2 * N; S.fl3 = fs3 + 3 * N; S.fb2 = fs3 + 4 * N; S.fb3 = fs3 + 5 * N;
     S.fw1 = fs3 + 6 * N;
@@ -397,9 +397,11 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
         const int off = block_exclusive_scan(nsurv, wsum, nq);  // contains __syncthreads
         // E1..E3 and the phases are dead: the queue overwrites them.
         if (tid < N2 && nsurv) k3_enqueue<N>(S, tid, off, live_lo, live_hi, live_x);
-        // dense F (doubles) in A, zero where no survivor
+        // dense F (doubles) in A; the forward pass reads it only where the row/column bits
+        // are set (entries its survivors wrote), the adjoint all of it (zero where no survivor)
         double *F = (double *)A;
-        for (int i = tid; i < N3; i += bd) F[i] = 0.0;
+        if constexpr (ADJ)
+            for (int i = tid; i < N3; i += bd) F[i] = 0.0;
         __syncthreads();
         // ---- delta weights and occupations for the survivors, full warps: FP64 for FP64
         // runs, FP32 (from FP64 centre differences) in mixed precision, as the tensor-core

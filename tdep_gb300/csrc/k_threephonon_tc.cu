@@ -70,25 +70,44 @@ constexpr int kAPlane = 16384;             // one A plane: 256 rows x 32 k x 2 b
 constexpr long long kTcWait = 2000000000LL;  // about 1 s at 2 GHz
 
 // Shared-memory layout (bytes) of the tensor-core kernel for mode count n and nt
-// force-constant triplets. Region X holds the A operand (hi, lo), the three E images and
-// the phase factors while Psi is formed; afterwards the survivor queue and the dense F
-// reuse it.
+// force-constant triplets. Region X holds the A operand (hi, lo), the E images and the
+// phase factors while Psi is formed; afterwards it is reused.
+//  forward: E1 and E2 at the start of each q-triplet, E3 into the phase factors' place once
+//           the pretransform is done; after stage 3 the survivor queue, F in FP32 and
+//           |Psi|^2 (then the row and column sums) all in X: 55.5 KB at 15 modes and 1115
+//           force-constant triplets, 4 CTAs per SM;
+//  adjoint: the three E images at once (the back-contraction reloads them as E^T), the
+//           phase factors kept to the end for 2 Re(phase Q); queue and FP64 F in X, |Psi|^2
+//           after it (74.4 KB, 3 CTAs per SM).
 struct TcLayout {
-    size_t A, E, ph, Q, F, psq, om, f32, v, masks, rowid, red, wsum, mbar, tslot, total;
+    size_t A, E, E3, ph, Q, F, psq, om, f32, v, masks, rowid, red, wsum, mbar, tslot, total;
 };
 __host__ __device__ inline size_t tc_al(size_t x, size_t a = 16) { return (x + a - 1) / a * a; }
-__host__ __device__ inline TcLayout tc_layout(int n, int nt) {
+__host__ __device__ inline TcLayout tc_layout(int n, int nt, bool adj) {
     TcLayout L;
     const size_t n2 = (size_t)n * n, n3 = n2 * n;
+    const size_t phb = tc_al(sizeof(float2) * ((size_t)nt + 4));
     L.A = 0;
     L.E = 2 * kAPlane;
-    L.ph = L.E + 3 * kEImgBytes;
-    const size_t x_end = L.ph + tc_al(sizeof(float2) * ((size_t)nt + 4));
     L.Q = 0;
     L.F = tc_al(sizeof(uint32_t) * n3);
-    const size_t y_end = L.F + sizeof(double) * n3;
-    size_t o = tc_al(x_end > y_end ? x_end : y_end, 128);
-    L.psq = o; o += tc_al(sizeof(float) * n3);  // |Psi|^2, then the row and column sums (2 n^2 doubles)
+    size_t o;
+    if (!adj) {
+        L.ph = L.E + 2 * kEImgBytes;
+        L.E3 = L.ph;
+        const size_t x_end = L.ph + (phb > (size_t)kEImgBytes ? phb : (size_t)kEImgBytes);
+        L.psq = L.F + tc_al(sizeof(float) * n3);
+        const size_t y_end = L.psq + tc_al(sizeof(float) * n3 > 2 * n2 * sizeof(double) ? sizeof(float) * n3
+                                                                                         : 2 * n2 * sizeof(double));
+        o = tc_al(x_end > y_end ? x_end : y_end, 128);
+    } else {
+        L.ph = L.E + 3 * kEImgBytes;
+        L.E3 = L.E + 2 * kEImgBytes;
+        const size_t x_end = L.ph + phb;
+        const size_t y_end = L.F + sizeof(double) * n3;
+        o = tc_al(x_end > y_end ? x_end : y_end, 128);
+        L.psq = o; o += tc_al(sizeof(float) * n3);  // |Psi|^2, then the row and column sums (2 n^2 doubles)
+    }
     L.om = o; o += 9 * tc_al(sizeof(double) * n) + tc_al(sizeof(double) * n);  // om1..3 inv1 be2 be3 s1..3, wrow
     L.v = o; o += 3 * tc_al(sizeof(double) * 3 * n);
     L.f32 = o; o += tc_al(sizeof(float) * 12 * n);
@@ -96,7 +115,7 @@ __host__ __device__ inline TcLayout tc_layout(int n, int nt) {
     L.rowid = o; o += tc_al(sizeof(int) * n);
     L.red = o; o += tc_al(sizeof(int2) * kMaxRed);
     L.wsum = o; o += tc_al(sizeof(int) * 33);
-    L.mbar = o; o += 16;
+    L.mbar = o; o += 32;  // [0] E1, E2 (and E3 in the adjoint) copies, [1] MMA completion, [2] E3 copy
     L.tslot = o; o += 16;
     L.total = o;
     return L;
@@ -189,18 +208,18 @@ __device__ __forceinline__ void issue_stage(uint32_t tbase, uint32_t a_base, uin
 // ADJ: the adjoint of the linewidths (and, with a.xi_bar, of the Xi row terms) with respect
 // to the force constants; see the comment at the adjoint tail below.
 template <int N, bool ADJ>
-__global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a) {
+__global__ void __launch_bounds__(kTcThreads, ADJ ? 3 : 4) k_threephonon_tc(ThreePhArgs a) {
     constexpr int N2 = N * N, N3 = N2 * N;
     extern __shared__ __align__(1024) unsigned char smem[];
     const Fc3Dev &fc = a.fc;
     const MeshDev &m = a.mesh;
     const PhononDev &P = a.ph;
-    const TcLayout L = tc_layout(N, fc.n);
+    const TcLayout L = tc_layout(N, fc.n, ADJ);
     unsigned char *Aop = smem + L.A;
     unsigned char *Eimg = smem + L.E;
     float2 *ph = (float2 *)(smem + L.ph);
     float *psq = (float *)(smem + L.psq);
-    uint64_t *mb = (uint64_t *)(smem + L.mbar);  // [0] E-image copies, [1] MMA completion
+    uint64_t *mb = (uint64_t *)(smem + L.mbar);  // [0] E-image copies, [1] MMA completion, [2] E3 (forward)
     uint32_t *tslot = (uint32_t *)(smem + L.tslot);
     K3Smem S;
     {
@@ -220,7 +239,8 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a)
         S.rowbits = S.zmask + 2; S.colbits = S.rowbits + N2;
         S.R2 = (double *)(smem + L.psq);  // |Psi|^2 is dead when the sums start
         S.R3 = S.R2 + N2;
-        S.F = (double *)(smem + L.F);
+        S.F = ADJ ? (double *)(smem + L.F) : nullptr;
+        S.Ff = ADJ ? nullptr : (float *)(smem + L.F);
         S.Q = (uint32_t *)(smem + L.Q);
         S.rowid = (int *)(smem + L.rowid);
         S.red = (int2 *)(smem + L.red);
@@ -234,6 +254,7 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a)
     if (tid == 0) {
         tc::mbar_init(&mb[0], 1);
         tc::mbar_init(&mb[1], 1);
+        tc::mbar_init(&mb[2], 1);
         tc::fence_mbar_init();
     }
     tc::fence_before_sync();
@@ -245,8 +266,9 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a)
     const int row = tid & 127;
     const int mrow = 128 * tile + row;  // row of the 256-row operand (two uncontracted indices, 16 x 16)
     const uint32_t taddr = tbase + ((uint32_t)(32 * (warp & 3)) << 16) + 32u * (uint32_t)tile;
-    const uint32_t a_u = tc::smem_u32(Aop), e_u = tc::smem_u32(Eimg);
-    uint32_t e_ph = 0, m_ph = 0;
+    const uint32_t a_u = tc::smem_u32(Aop), e_u = tc::smem_u32(Eimg), e3_u = tc::smem_u32(smem + L.E3);
+    uint32_t e_ph = 0, m_ph = 0, e3_ph = 0;
+    bool e3_pending = false;  // thread 0: an E3 copy was issued and not yet waited for
     bool ok = true;
 
     // the next q-triplet's record is loaded one iteration ahead
@@ -260,14 +282,17 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a)
         const int i2 = m.full_irr[q2], i3 = m.full_irr[q3];
         const int nred = rec.red_cnt;
         const double perm = (q2 == q3) ? 1.0 : 2.0;
-        // E images of q1, q2, q3 into shared memory (the region was last read by the previous
-        // q-triplet's MMAs and reused by its F, both finished before the last barrier)
+        // E images of q1 and q2 (the adjoint: and q3) into shared memory (the region was last
+        // read by the previous q-triplet's MMAs and reused by its queue, F and |Psi|^2, all
+        // finished before the last barrier); the forward pass brings E3 once the
+        // pretransform has released the phase factors' place
         if (tid == 0) {
             tc::fence_async_smem();  // the generic accesses of the region (ordered by the last barrier) come first
-            tc::mbar_arrive_expect_tx(&mb[0], 3u * kEImgBytes);
+            tc::mbar_arrive_expect_tx(&mb[0], (ADJ ? 3u : 2u) * kEImgBytes);
             tc::bulk_g2s(e_u, a.tc_eimg + (size_t)f1 * kEImgBytes, kEImgBytes, &mb[0]);
             tc::bulk_g2s(e_u + kEImgBytes, a.tc_eimg + (size_t)q2 * kEImgBytes, kEImgBytes, &mb[0]);
-            tc::bulk_g2s(e_u + 2 * kEImgBytes, a.tc_eimg + (size_t)q3 * kEImgBytes, kEImgBytes, &mb[0]);
+            if constexpr (ADJ)
+                tc::bulk_g2s(e3_u, a.tc_eimg + (size_t)q3 * kEImgBytes, kEImgBytes, &mb[0]);
         }
         k3_load_modes<N>(S, a, rec, f1, q2, q3, i2, i3);
         // A operand zeroed (padding must be exact zeros), phase factors of all triplets
@@ -345,9 +370,23 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a)
                 if (stage == 0) {
                     go = tc::mbar_wait(&mb[0], e_ph, kTcWait);
                     if (go) e_ph ^= 1u;  // else the abort path waits on the same phase again
+                    if (!ADJ && go) {
+                        // the pretransform is done (the barrier above): E3 into the phase
+                        // factors' place, for stage 3
+                        tc::mbar_arrive_expect_tx(&mb[2], kEImgBytes);
+                        tc::bulk_g2s(e3_u, a.tc_eimg + (size_t)q3 * kEImgBytes, kEImgBytes, &mb[2]);
+                        e3_pending = true;
+                    }
+                }
+                if (!ADJ && stage == 2 && go) {
+                    go = tc::mbar_wait(&mb[2], e3_ph, kTcWait);
+                    if (go) {
+                        e3_ph ^= 1u;
+                        e3_pending = false;
+                    }
                 }
                 if (go) {
-                    issue_stage(tbase, a_u, e_u + (uint32_t)stage * kEImgBytes, true);
+                    issue_stage(tbase, a_u, stage == 2 ? e3_u : e_u + (uint32_t)stage * kEImgBytes, true);
                     tc::mma_commit(&mb[1]);
                 }
             }
@@ -396,8 +435,8 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a)
             for (int i = tid; i < N3; i += kTcThreads) S.F[i] = 0.0;
         __syncthreads();
         if constexpr (!ADJ) {
-            k3_survivors_f32<N>(S, P, nq, (float)perm, [&](int idx) -> float { return psq[idx]; });
-            k3_sums_scatter<N>(S, a, nred);
+            k3_survivors_f32<N, true>(S, P, nq, (float)perm, [&](int idx) -> float { return psq[idx]; });
+            k3_sums_scatter<N, true>(S, a, nred);
         } else {
             // ---- adjoint tail (the SIMT adjoint's algebra, k_threephonon.cu): F without |Psi|^2
             // gives G_b = cot_b dF_b/d|Psi_b|^2 with cot = lam(row) nred (+ the Xi row terms'
@@ -540,6 +579,7 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_threephonon_tc(ThreePhArgs a)
             atomicExch(a.status, (int32_t)kDevTimeout);
             tc::mbar_wait(&mb[0], e_ph, kTcWait);
             tc::mbar_wait(&mb[1], m_ph, kTcWait);
+            if (e3_pending) tc::mbar_wait(&mb[2], e3_ph, kTcWait);
         }
     }
     tc::fence_before_sync();
@@ -586,7 +626,7 @@ __global__ void k_tc_eimg(int32_t n_full, int32_t n, const float2 *egvs32, unsig
 
 template <int N, bool ADJ>
 int tc_per_sm(int n_fc, int *api, int *count) {
-    const size_t bytes = tc_layout(N, n_fc).total;
+    const size_t bytes = tc_layout(N, n_fc, ADJ).total;
     const int per_sm = resident_ctas((const void *)k_threephonon_tc<N, ADJ>, kTcThreads, bytes, api, count);
     // tensor memory: 64 columns per CTA, 512 per SM
     return per_sm > 8 ? 8 : per_sm;
@@ -604,7 +644,7 @@ int tc_grid(int n_fc, int n_trip, int n_sm, int ctas_per_sm) {
 template <int N, bool ADJ>
 cudaError_t tc_launch_grid(const ThreePhArgs &a, int grid, cudaStream_t s) {
     if (grid < 1) return cudaErrorInvalidConfiguration;
-    k_threephonon_tc<N, ADJ><<<grid, kTcThreads, tc_layout(N, a.fc.n).total, s>>>(a);
+    k_threephonon_tc<N, ADJ><<<grid, kTcThreads, tc_layout(N, a.fc.n, ADJ).total, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -612,7 +652,8 @@ cudaError_t tc_launch_grid(const ThreePhArgs &a, int grid, cudaStream_t s) {
 
 bool threephonon_tc_supported(int n, int precision, int n_fc) {
     if (precision == 0 || (n != 9 && n != 12 && n != 15)) return false;
-    return tc_layout(n, n_fc).total <= 110 * 1024;  // at least two CTAs per SM
+    // at least two CTAs per SM in both passes
+    return tc_layout(n, n_fc, false).total <= 110 * 1024 && tc_layout(n, n_fc, true).total <= 110 * 1024;
 }
 
 int threephonon_tc_max_per_sm(int n, int n_fc, int *api, int *count) {
