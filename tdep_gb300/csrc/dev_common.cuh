@@ -67,6 +67,21 @@ __device__ __forceinline__ bool close_f32(float h1, float l1, float h2, float l2
     return fabsf((h1 - h2) + (l1 - l2)) < 1e-9f;
 }
 
+// Double-float accumulation on the FP32 pipe: s += p (TwoSum of the high parts), and the
+// sum of two double-float values.
+__device__ __forceinline__ void df_acc(float2 &s, float p) {
+    const float t = s.x + p;
+    const float bb = t - s.x;
+    s.y += (s.x - (t - bb)) + (p - bb);
+    s.x = t;
+}
+__device__ __forceinline__ float2 df_merge(float2 a, float2 b) {
+    const float t = a.x + b.x;
+    const float bb = t - a.x;
+    const float e = (a.x - (t - bb)) + (b.x - bb);
+    return make_float2(t, a.y + b.y + e);
+}
+
 // Exclusive scan of one int per thread over the block (blockDim a multiple of 32).
 __device__ __forceinline__ int block_exclusive_scan(int v, int *wsum, int &total) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;

@@ -449,7 +449,7 @@ struct LnDeltaArgs {
 };
 
 __host__ __device__ inline size_t ln_delta_smem(int n, int bb) {
-    return sizeof(double) * ((size_t)14 * n + (size_t)bb * n) + sizeof(uint32_t) * (size_t)bb * n +
+    return sizeof(double) * (size_t)14 * n + sizeof(float) * (size_t)bb * n + sizeof(uint32_t) * (size_t)bb * n +
            sizeof(int) * 33 + sizeof(float) * 8 * (size_t)n + 16;
 }
 
@@ -477,7 +477,8 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
     const int f1 = m.irr_full[rec.q1], q2 = rec.q2, q3 = rec.q3;
     const int i2 = m.full_irr[q2], i3 = m.full_irr[q3];
     double *om2 = (double *)sm, *om3 = om2 + n, *be2 = om3 + n, *be3 = be2 + n, *s2 = be3 + n, *s3 = s2 + n;
-    double *v2 = s3 + n, *v3 = v2 + 3 * n, *R2 = v3 + 3 * n, *R3 = R2 + n, *F = R3 + n;
+    double *v2 = s3 + n, *v3 = v2 + 3 * n, *R2 = v3 + 3 * n, *R3 = R2 + n;
+    float *F = (float *)(R3 + n);  // the block's F in FP32 (its values are FP32 products)
     uint32_t *Q = (uint32_t *)(F + (size_t)BB * n);
     int *wsum = (int *)(Q + (size_t)BB * n);
     // FP32 copies for the screen (double -> float conversions run on the FP64 pipe, so they
@@ -516,7 +517,7 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
     // the adjoint's G = lambda(row) * k * dF/d|Psi|^2
     const double pw = perm * kLnPrefactor * w;
     const double fadj = ADJ ? a.lam[row] * (double)rec.red_cnt * pw : 0.0;
-    const float pwf = (float)pw;
+    const float pwf = (float)pw, fadjf = (float)fadj;
     const int it = P.integrationtype;
     const float fo1 = (float)o1, fs1 = (float)s1, fsig = (float)P.sigma_fixed;
     const float fl1 = (float)(o1 - (double)fo1);
@@ -551,7 +552,7 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
             lives |= (uint64_t)l << (4 * (e - e0));
             ns += l != 0u;
         }
-        for (int e = tid; e < cnt; e += bd) F[e] = 0.0;
+        for (int e = tid; e < cnt; e += bd) F[e] = 0.f;
         int total = 0;
         int k = block_exclusive_scan(ns, wsum, total);  // contains __syncthreads
         for (int e = e0; e < e1; ++e) {
@@ -602,17 +603,17 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
             const float n2 = c2[b2], n3 = c3[b3];
             const float occ = (n2 - n3) * d0 + (n2 + n3 + 1.0f) * d1;
             if (ADJ) {
-                F[e] = fadj * (double)occ;
+                F[e] = fadjf * occ;
                 continue;
             }
             const float2 ps = psi[b2 * n + b3];
-            F[e] = (double)(pwf * fmaf(ps.x, ps.x, ps.y * ps.y) * occ);
+            F[e] = pwf * fmaf(ps.x, ps.x, ps.y * ps.y) * occ;
         }
         __syncthreads();
         if (ADJ) {
             float2 *wr = a.w + ((int64_t)s * n + b1) * n * n + (int64_t)bb * n;
             for (int e = tid; e < cnt; e += bd) {
-                const float g = (float)F[e];
+                const float g = F[e];
                 const float2 ps = wr[e];
                 wr[e] = make_float2(g * ps.x, -g * ps.y);
             }
@@ -620,30 +621,31 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
             continue;
         }
         // (C) row sums of the block and running column sums, spread over the whole block: a
-        // warp per row with the columns split over its lanes, two threads per column
+        // warp per row with the columns split over its lanes, two threads per column; the
+        // block sums in double-float on the FP32 pipe (TwoSum; exact to ~2^-44 for these
+        // few hundred FP32 terms), turned into FP64 once per row and column: an FP64 warp
+        // instruction holds GB300's FP64 pipe 16 cycles whatever its active lanes, and the
+        // FP64 adds over the dense block had been about 40 % of the kernel
         {
             const int lane = tid & 31, wid = tid >> 5, nw = bd >> 5;
             for (int r = wid; r < nbb; r += nw) {
-                double sum = 0.0;
-                for (int b3 = lane; b3 < n; b3 += 32) {
-                    const double f = F[r * n + b3];
-                    if (nonzero(f)) sum += f;
-                }
+                float2 sum = make_float2(0.f, 0.f);
+                for (int b3 = lane; b3 < n; b3 += 32) df_acc(sum, F[r * n + b3]);
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-                if (lane == 0) R2[bb + r] = sum;
+                for (int o = 16; o > 0; o >>= 1)
+                    sum = df_merge(sum, make_float2(__shfl_xor_sync(0xffffffffu, sum.x, o),
+                                                    __shfl_xor_sync(0xffffffffu, sum.y, o)));
+                if (lane == 0) R2[bb + r] = (double)sum.x + (double)sum.y;
             }
             const int n2c = ((2 * n + 31) / 32) * 32;
             for (int t = tid; t < n2c; t += bd) {  // warp-uniform trip count
                 const int b3 = t >> 1, h = t & 1;
-                double sum = 0.0;
+                float2 sum = make_float2(0.f, 0.f);
                 if (b3 < n)
-                    for (int r = h; r < nbb; r += 2) {
-                        const double f = F[r * n + b3];
-                        if (nonzero(f)) sum += f;
-                    }
-                sum += __shfl_xor_sync(0xffffffffu, sum, 1);
-                if (h == 0 && b3 < n) R3[b3] += sum;
+                    for (int r = h; r < nbb; r += 2) df_acc(sum, F[r * n + b3]);
+                sum = df_merge(sum, make_float2(__shfl_xor_sync(0xffffffffu, sum.x, 1),
+                                                __shfl_xor_sync(0xffffffffu, sum.y, 1)));
+                if (h == 0 && b3 < n) R3[b3] += (double)sum.x + (double)sum.y;
             }
         }
         __syncthreads();
