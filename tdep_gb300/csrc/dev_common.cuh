@@ -82,6 +82,14 @@ __device__ __forceinline__ float2 df_merge(float2 a, float2 b) {
     return make_float2(t, a.y + b.y + e);
 }
 
+// Square root by the hardware approximation (sqrt.approx.f32, a few ulp): for the FP32
+// screens, whose windows carry a relative margin of 1e-3.
+__device__ __forceinline__ float sqrt_screen(float x) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // Exclusive scan of one int per thread over the block (blockDim a multiple of 32).
 __device__ __forceinline__ int block_exclusive_scan(int v, int *wsum, int &total) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;

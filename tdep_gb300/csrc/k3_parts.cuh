@@ -24,7 +24,8 @@ struct K3Smem {
     double *v1, *v2, *v3;  // [3n]
     double *wrow;
     double *R2;            // [n^2] row sums, then Xi row terms
-    double *R3;            // [n^2] column sums, then Xi row terms
+    double *R3;            // [n^2] column sums
+    double *R2s, *R3s;     // [n^2] each: the Xi row terms of the sums
     double *F;             // [n^3] dense F (zero where no survivor)
     float *Ff;             // or F in FP32 (the tensor-core forward pass: k3_survivors_f32 and
                            // k3_sums_scatter with FLOAT_F)
@@ -137,7 +138,7 @@ __device__ __forceinline__ int k3_screen(const K3Smem &S, int it, float sigfix32
         const float f_o3 = S.fo3[b3];
         float sg = 0.f;
         if (it == 1) sg = sigfix32;
-        else if (it == 2) sg = sqrtf(S.fs1[b1] + S.fs2[b2] + S.fs3[b3]);
+        else if (it == 2) sg = sqrt_screen(S.fs1[b1] + S.fs2[b2] + S.fs3[b3]);
         const float win = 8.0f * sg * 1.001f + 1e-6f * (f_o1 + f_o2 + f_o3);
         uint32_t live = 15u;  // the -it 6 width can cancel in FP32: not screened
         if (it != 6) {
@@ -304,6 +305,8 @@ __device__ __forceinline__ void k3_sums_scatter(const K3Smem &S, const ThreePhAr
         }
     }
     __syncthreads();
+    // Gamma from the row sums (threads < N) and the Xi row terms 2 F om/om1 of each entry,
+    // computed once for all equivalent triplets into R2s / R3s
     if (tid < N) {
         const int row = S.rowid[tid];
         if (row >= 0) {
@@ -312,17 +315,14 @@ __device__ __forceinline__ void k3_sums_scatter(const K3Smem &S, const ThreePhAr
             if (nonzero(g)) atomicAdd(a.gamma + row, (double)nred * g);
         }
     }
-    // the Xi row terms 2 F om/om1 of each entry, computed once for all equivalent triplets
-    // (after Gamma has read R2)
-    __syncthreads();
     for (int e = tid; e < 2 * N2; e += bd) {
         if (e < N2) {
             const double v = S.R2[e];
-            S.R2[e] = nonzero(v) ? 2.0 * v * S.om2[e % N] * S.inv1[e / N] : 0.0;
+            S.R2s[e] = nonzero(v) ? 2.0 * v * S.om2[e % N] * S.inv1[e / N] : 0.0;
         } else {
             const int e3 = e - N2;
             const double v = S.R3[e3];
-            S.R3[e3] = nonzero(v) ? 2.0 * v * S.om3[e3 % N] * S.inv1[e3 / N] : 0.0;
+            S.R3s[e3] = nonzero(v) ? 2.0 * v * S.om3[e3 % N] * S.inv1[e3 / N] : 0.0;
         }
     }
     __syncthreads();
@@ -332,12 +332,12 @@ __device__ __forceinline__ void k3_sums_scatter(const K3Smem &S, const ThreePhAr
         if (e < N2) {
             const int b1 = e / N, b2 = e % N;
             const int row = S.rowid[b1];
-            const double v = S.R2[e];
+            const double v = S.R2s[e];
             if (row >= 0 && nonzero(v)) atomicAdd(a.od + row * ld + (int64_t)pr.x * N + b2, v);
         } else {
             const int e3 = e - N2, b1 = e3 / N, b3 = e3 % N;
             const int row = S.rowid[b1];
-            const double v = S.R3[e3];
+            const double v = S.R3s[e3];
             if (row >= 0 && nonzero(v)) atomicAdd(a.od + row * ld + (int64_t)pr.y * N + b3, v);
         }
     }

@@ -535,7 +535,7 @@ __global__ void __launch_bounds__(256) k_ln_delta(LnDeltaArgs a) {
         if (close_f32(fo1, fl1, f3, l3[b3])) return 0u;
         if (close_f32(f2, l2[b2], f3, l3[b3])) return 0u;
         if (it == 6) return 15u;  // the velocity-difference width can cancel in FP32: not screened
-        const float sg = it == 1 ? fsig : sqrtf(fs1 + t2[b2] + t3[b3]);
+        const float sg = it == 1 ? fsig : sqrt_screen(fs1 + t2[b2] + t3[b3]);
         const float win = 8.0f * sg * 1.001f + 1e-6f * (fo1 + f2 + f3);
         return (fabsf(fo1 + f2 - f3) <= win ? 1u : 0u) | (fabsf(fo1 - f2 + f3) <= win ? 2u : 0u) |
                (fabsf(fo1 - f2 - f3) <= win ? 4u : 0u) | (fo1 + f2 + f3 <= win ? 8u : 0u);

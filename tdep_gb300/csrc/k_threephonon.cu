@@ -222,6 +222,7 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
     S.om1 = om1; S.om2 = om2; S.om3 = om3; S.inv1 = inv1; S.be2 = be2; S.be3 = be3;
     S.s1 = s1; S.s2 = s2; S.s3 = s3; S.v1 = v1; S.v2 = v2; S.v3 = v3; S.wrow = wrow;
     S.R2 = R2; S.R3 = (double *)B; S.F = (double *)A; S.Ff = nullptr;
+    S.R2s = S.R3 + N2; S.R3s = S.R2s + N2;  // B (8 n^3 or more bytes) is free when the sums start
     S.fo1 = fo1; S.fo2 = fo2; S.fo3 = fo3; S.fs1 = fs1; S.fs2 = fs2; S.fs3 = fs3;
     S.fl1 = fs3 + N; S.fl2 = fs3 + 2 * N; S.fl3 = fs3 + 3 * N; S.fb2 = fs3 + 4 * N; S.fb3 = fs3 + 5 * N;
     S.fw1 = fs3 + 6 * N;

@@ -97,8 +97,9 @@ __host__ __device__ inline TcLayout tc_layout(int n, int nt, bool adj) {
         L.E3 = L.ph;
         const size_t x_end = L.ph + (phb > (size_t)kEImgBytes ? phb : (size_t)kEImgBytes);
         L.psq = L.F + tc_al(sizeof(float) * n3);
-        const size_t y_end = L.psq + tc_al(sizeof(float) * n3 > 2 * n2 * sizeof(double) ? sizeof(float) * n3
-                                                                                         : 2 * n2 * sizeof(double));
+        // |Psi|^2, then the row and column sums and their Xi row terms (4 n^2 doubles)
+        const size_t y_end = L.psq + tc_al(sizeof(float) * n3 > 4 * n2 * sizeof(double) ? sizeof(float) * n3
+                                                                                         : 4 * n2 * sizeof(double));
         o = tc_al(x_end > y_end ? x_end : y_end, 128);
     } else {
         L.ph = L.E + 3 * kEImgBytes;
@@ -239,6 +240,8 @@ __global__ void __launch_bounds__(kTcThreads, ADJ ? 3 : 4) k_threephonon_tc(Thre
         S.rowbits = S.zmask + 2; S.colbits = S.rowbits + N2;
         S.R2 = (double *)(smem + L.psq);  // |Psi|^2 is dead when the sums start
         S.R3 = S.R2 + N2;
+        S.R2s = S.R3 + N2;
+        S.R3s = S.R2s + N2;
         S.F = ADJ ? (double *)(smem + L.F) : nullptr;
         S.Ff = ADJ ? nullptr : (float *)(smem + L.F);
         S.Q = (uint32_t *)(smem + L.Q);
