@@ -1,5 +1,6 @@
 // Host stage of thermal_conductivity: reading the input files and building the flattened
 // problem (main.f90:42-181), error reporting and the output file (main.f90:246-294).
+#include <atomic>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -8,6 +9,7 @@
 #include <fstream>
 #include <memory>
 #include <mutex>
+#include <thread>
 
 #include <unistd.h>
 
@@ -76,16 +78,24 @@ double harmonic_oscillator_cv(double temp, double omega) {
 namespace {
 
 // Worker threads of parallel_for, created once (hardware threads - 1; the caller is the last
-// one). One job at a time; a job finishes only after every worker has taken part in it.
+// one). One job at a time. A job is a shared object that the workers take when they wake;
+// indices are claimed in chunks, and the caller returns as soon as every index is done,
+// without waiting for the workers that woke late (they find nothing left to claim, so the
+// caller's function is never called after it returns). Waiting for every worker to check
+// in, as before, cost a wake-up of all threads per parallel_for (about 0.5 ms per call on
+// the 16-core Grace host, several calls per problem load).
 struct Pool {
+    struct Job {
+        const std::function<void(int64_t)> *fn = nullptr;
+        int64_t n = 0, chunk = 1;
+        std::atomic<int64_t> next{0}, done{0};
+    };
     std::mutex mu;
-    std::condition_variable cv_start, cv_done;
+    std::condition_variable cv_start;
     std::atomic<bool> busy{false};
-    const std::function<void(int64_t)> *fn = nullptr;
-    int64_t n = 0;
-    std::atomic<int64_t> next{0};
+    std::shared_ptr<Job> cur;
     uint64_t gen = 0;
-    unsigned active = 0, nw = 0;
+    unsigned nw = 0;
     pid_t pid = 0;
     Pool() {
         pid = getpid();
@@ -93,38 +103,47 @@ struct Pool {
         nw = hc - 1;
         for (unsigned t = 0; t < nw; ++t) std::thread([this] { loop(); }).detach();
     }
-    void work() {
-        for (int64_t i = next++; i < n; i = next++) (*fn)(i);
+    static void work(Job &j) {
+        for (;;) {
+            const int64_t i0 = j.next.fetch_add(j.chunk);
+            if (i0 >= j.n) return;
+            const int64_t i1 = std::min(j.n, i0 + j.chunk);
+            for (int64_t i = i0; i < i1; ++i) (*j.fn)(i);
+            j.done.fetch_add(i1 - i0);
+        }
     }
     void loop() {
         uint64_t seen = 0;
         for (;;) {
-            std::unique_lock<std::mutex> lk(mu);
-            cv_start.wait(lk, [&] { return gen != seen; });
-            seen = gen;
-            lk.unlock();
-            work();
-            lk.lock();
-            if (--active == 0) cv_done.notify_one();
+            std::shared_ptr<Job> j;
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                cv_start.wait(lk, [&] { return gen != seen; });
+                seen = gen;
+                j = cur;
+            }
+            if (j) work(*j);
         }
     }
     bool run(int64_t count, const std::function<void(int64_t)> &f) {
         if (nw == 0 || getpid() != pid) return false;
         bool idle = false;
         if (!busy.compare_exchange_strong(idle, true)) return false;
+        auto j = std::make_shared<Job>();
+        j->fn = &f;
+        j->n = count;
+        j->chunk = std::max<int64_t>(1, count / (8 * (int64_t)(nw + 1)));
         {
             std::lock_guard<std::mutex> lk(mu);
-            fn = &f;
-            n = count;
-            next = 0;
-            active = nw;
+            cur = j;
             ++gen;
         }
         cv_start.notify_all();
-        work();
+        work(*j);
+        while (j->done.load() < count) std::this_thread::yield();
         {
-            std::unique_lock<std::mutex> lk(mu);
-            cv_done.wait(lk, [&] { return active == 0; });
+            std::lock_guard<std::mutex> lk(mu);
+            cur.reset();
         }
         busy = false;
         return true;

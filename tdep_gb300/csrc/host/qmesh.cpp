@@ -25,6 +25,54 @@ int build_fft_mesh(const Crystal &c, const int grid[3], bool timereversal, QMesh
     qp.qfrac.assign(np, V3());
     // the same points as integers: qfrac = nq / g exactly
     std::vector<int32_t> nq((size_t)np * 3);
+    // Connections: op j maps point i to point connections[i][j] (time reversal: -index).
+    // The reference tests in fractional coordinates whether R q is on the mesh and whether
+    // R^-1 maps its image back onto q. On integer coordinates the first test is exact:
+    // (R q)_i = sum_k R_ik n_k / g_k is on the mesh when num_i = sum_k R_ik n_k (L / g_k), L
+    // the least common multiple of the g_k, is a multiple of L / g_i; the second test then
+    // always holds (R^-1 is an integer matrix and maps the image's mesh point, which differs
+    // from R q by a reciprocal lattice vector, back onto q's).
+    const int nc = timereversal ? 2 * nsym : nsym;
+    std::vector<int> conn((size_t)np * nc, 0);
+    int64_t L = grid[0];
+    for (int d = 1; d < 3; ++d) L = L / std::gcd(L, (int64_t)grid[d]) * grid[d];
+    const int64_t sg3[3] = {L / grid[0], L / grid[1], L / grid[2]};
+    // With equal dimensions (L / g = 1) every image is on the mesh and the wrap needs no
+    // division. Each point's row is made right after its first-zone coordinates.
+    const bool equal = sg3[0] == 1 && sg3[1] == 1 && sg3[2] == 1;
+    auto connect = [&](int64_t i) {
+        const int32_t *n = &nq[(size_t)i * 3];
+        for (int j = 0; j < nsym; ++j) {
+            const int32_t *m = c.ops[j].rfm;
+            int64_t gi[3];
+            bool on = true;
+            if (equal) {
+                const int g = grid[0];
+                for (int r = 0; r < 3; ++r) {
+                    int v = m[r] * n[0] + m[r + 3] * n[1] + m[r + 6] * n[2];
+                    while (v < 0) v += g;
+                    while (v >= g) v -= g;
+                    gi[r] = v;
+                }
+            } else {
+                for (int r = 0; r < 3 && on; ++r) {
+                    const int64_t num = m[r] * n[0] * sg3[0] + m[r + 3] * n[1] * sg3[1] + m[r + 6] * n[2] * sg3[2];
+                    on = num % sg3[r] == 0;
+                    gi[r] = num / sg3[r];
+                }
+            }
+            if (!on) continue;
+            for (int tr = 0; tr < (timereversal ? 2 : 1); ++tr) {
+                int64_t idx = 0;
+                for (int r = 0; r < 3; ++r) {
+                    const int64_t v = ((tr ? -gi[r] : gi[r]) % grid[r] + grid[r]) % grid[r];
+                    idx = idx * grid[r] + v;
+                }
+                const int ii = (int)idx + 1;
+                conn[(size_t)i * nc + j + tr * nsym] = tr ? -ii : ii;
+            }
+        }
+    };
     parallel_for(np, [&](int64_t l) {  // point l = ((i - 1) g1 + j - 1) g2 + k - 1
         const int k = (int)(l % grid[2]) + 1, j = (int)((l / grid[2]) % grid[1]) + 1,
                   i = (int)(l / ((int64_t)grid[1] * grid[2])) + 1;
@@ -57,59 +105,10 @@ int build_fft_mesh(const Crystal &c, const int grid[3], bool timereversal, QMesh
         nq[(size_t)l * 3] = i - 1 - sh[0] * grid[0];
         nq[(size_t)l * 3 + 1] = j - 1 - sh[1] * grid[1];
         nq[(size_t)l * 3 + 2] = k - 1 - sh[2] * grid[2];
+        connect(l);  // its images under every operation (needs only its own coordinates)
     });
 
-    pt.mark("first zone");
-    // Connections: op j maps point i to point connections[i][j] (time reversal: -index).
-    // The reference tests in fractional coordinates whether R q is on the mesh and whether
-    // R^-1 maps its image back onto q. On integer coordinates the first test is exact:
-    // (R q)_i = sum_k R_ik n_k / g_k is on the mesh when num_i = sum_k R_ik n_k (L / g_k), L
-    // the least common multiple of the g_k, is a multiple of L / g_i; the second test then
-    // always holds (R^-1 is an integer matrix and maps the image's mesh point, which differs
-    // from R q by a reciprocal lattice vector, back onto q's).
-    const int nc = timereversal ? 2 * nsym : nsym;
-    std::vector<int> conn((size_t)np * nc, 0);
-    int64_t L = grid[0];
-    for (int d = 1; d < 3; ++d) L = L / std::gcd(L, (int64_t)grid[d]) * grid[d];
-    const int64_t sg3[3] = {L / grid[0], L / grid[1], L / grid[2]};
-    // rows are independent: all host threads. With equal dimensions (L / g = 1) every image
-    // is on the mesh and the wrap needs no division.
-    const bool equal = sg3[0] == 1 && sg3[1] == 1 && sg3[2] == 1;
-    parallel_for(np, [&](int64_t i) {
-        const int32_t *n = &nq[(size_t)i * 3];
-        for (int j = 0; j < nsym; ++j) {
-            const int32_t *m = c.ops[j].rfm;
-            int64_t gi[3];
-            bool on = true;
-            if (equal) {
-                const int g = grid[0];
-                for (int r = 0; r < 3; ++r) {
-                    int v = m[r] * n[0] + m[r + 3] * n[1] + m[r + 6] * n[2];
-                    while (v < 0) v += g;
-                    while (v >= g) v -= g;
-                    gi[r] = v;
-                }
-            } else {
-                for (int r = 0; r < 3 && on; ++r) {
-                    const int64_t num = m[r] * n[0] * sg3[0] + m[r + 3] * n[1] * sg3[1] + m[r + 6] * n[2] * sg3[2];
-                    on = num % sg3[r] == 0;
-                    gi[r] = num / sg3[r];
-                }
-            }
-            if (!on) continue;
-            for (int tr = 0; tr < (timereversal ? 2 : 1); ++tr) {
-                int64_t idx = 0;
-                for (int r = 0; r < 3; ++r) {
-                    const int64_t v = ((tr ? -gi[r] : gi[r]) % grid[r] + grid[r]) % grid[r];
-                    idx = idx * grid[r] + v;
-                }
-                const int ii = (int)idx + 1;
-                conn[(size_t)i * nc + j + tr * nsym] = tr ? -ii : ii;
-            }
-        }
-    });
-
-    pt.mark("connections");
+    pt.mark("first zone and connections");
     // Irreducible points: smallest index of every orbit.
     std::vector<int> ind(np, 1);
     for (int i = 0; i < np; ++i)
