@@ -287,8 +287,28 @@ __global__ void __launch_bounds__(threads_for(N), min_blocks_for(N, sizeof(R) ==
             if (a.plan_slots > 0) {
                 planned = true;
                 __syncthreads();
-                for (int i = tid; i < fc.n + 4; i += bd)
-                    ph[i] = i < fc.n ? phase3<C>(fc, m, gi2, gi3, i) : czero<C>();
+                // four triplets per thread in flight: their lattice vectors, then their table entries
+                for (int i0 = tid; i0 < fc.n + 4; i0 += 4 * bd) {
+                    int kk[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int i = i0 + u * bd;
+                        kk[u] = -1;
+                        if (i < fc.n) {
+                            const int32_t *lv = fc.lv + (size_t)i * 6;
+                            int S2 = 0;
+#pragma unroll
+                            for (int d = 0; d < 3; ++d) S2 += gi2[d] * __ldg(lv + d) + gi3[d] * __ldg(lv + 3 + d);
+                            int K = S2 % m.L;
+                            kk[u] = K < 0 ? K + m.L : K;
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int i = i0 + u * bd;
+                        if (i < fc.n + 4) ph[i] = kk[u] >= 0 ? twiddle_at<C>(fc, kk[u]) : czero<C>();
+                    }
+                }
                 __syncthreads();
                 const float4 *pm = a.plan_pm + tid;
                 const uint32_t *pw = a.plan_word + tid;
