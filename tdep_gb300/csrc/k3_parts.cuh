@@ -287,21 +287,31 @@ __device__ __forceinline__ void k3_sums_scatter(const K3Smem &S, const ThreePhAr
     const int tid = threadIdx.x, bd = blockDim.x;
     const int64_t ld = (int64_t)a.mesh.n_full * N;
     __syncthreads();
+    // FP32 F: the sums in double-float on the FP32 pipe (TwoSum; exact to ~2^-44 for these
+    // at most n terms), one conversion to FP64 per sum, instead of a conversion and an FP64
+    // add per term on GB300's 2-lane-per-clock FP64 pipe
     for (int e = tid; e < 2 * N2; e += bd) {
         double sum = 0.0;
+        float2 dsum = make_float2(0.f, 0.f);
         if (e < N2) {
             for (uint32_t bits = S.rowbits[e]; bits; bits &= bits - 1) {
                 const int i = e * N + __ffs(bits) - 1;
-                sum += FLOAT_F ? (double)S.Ff[i] : S.F[i];
+                if constexpr (FLOAT_F)
+                    df_acc(dsum, S.Ff[i]);
+                else
+                    sum += S.F[i];
             }
-            S.R2[e] = sum;
+            S.R2[e] = FLOAT_F ? (double)dsum.x + (double)dsum.y : sum;
         } else {
             const int e3 = e - N2, b1 = e3 / N, b3 = e3 % N;
             for (uint32_t bits = S.colbits[e3]; bits; bits &= bits - 1) {
                 const int i = (b1 * N + __ffs(bits) - 1) * N + b3;
-                sum += FLOAT_F ? (double)S.Ff[i] : S.F[i];
+                if constexpr (FLOAT_F)
+                    df_acc(dsum, S.Ff[i]);
+                else
+                    sum += S.F[i];
             }
-            S.R3[e3] = sum;
+            S.R3[e3] = FLOAT_F ? (double)dsum.x + (double)dsum.y : sum;
         }
     }
     __syncthreads();
