@@ -20,7 +20,8 @@
 // Operands are BF16 hi/lo splits of FP32 values (x = hi + lo, about 16 significant bits);
 // a product is hi*hi + hi*lo + lo*hi accumulated in FP32 in tensor memory (2 accumulators
 // of 32 columns). The B operands (the real-split E of every mesh point, 4 KB each) are
-// built once per context and brought into shared memory by bulk copies on an mbarrier;
+// built once per context and brought into shared memory by bulk copies on mbarriers (the
+// forward pass: E1 and E2 at the start of a q-triplet, E3 once the pretransform is done);
 // each stage's accumulator rows are read by the thread of that row (tcgen05.ld), split and
 // stored as the next stage's A operand, in 8 x 16-byte core matrices without swizzle, all
 // MN-major (a core-matrix row is 8 consecutive M indices at one k). The row orders of the
